@@ -1,0 +1,322 @@
+"""GB300-native H2* / (H2+H)* HODLRdD operator and GMRES (sm_103a).
+
+Host-side Python mirror of the reference's operator interface. Everything
+runs through the C ABI of libh2w.so (include/h2w.h): the tree and plan are
+built by native host code, the compression, every matvec pass and GMRES run
+as CUDA kernels on the GPU. There is no CPU fallback: without the built
+library or a GPU the calls raise.
+
+Reference interface mirrored here (paths within the reference project):
+  initialisation(...)          {1D,2D,3D}/codes/matvec.hpp  (tree_initialisation, mat_vec_prod)
+  iterative_solver(...)        {1D,2D,3D}/codes/gmres.hpp   (GMRES, resid, max_iter)
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import synth  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libh2w.so")
+
+OK = 0
+ERR_NOT_CONVERGED = -5
+FORM_NESTED, FORM_SEMINESTED = 0, 1
+KERNEL_IE, KERNEL_RBF = 0, 1
+ASSEMBLE_NCA, ASSEMBLE_IMPORT, ASSEMBLE_LEARNED = 0, 1, 2
+PREC_FP64, PREC_FP32 = 0, 1
+HOST, DEVICE = 0, 1
+LISTS = {"charge": 0, "nbr": 1, "il": 2, "isvertex": 3, "far_check": 4, "far_charge": 5,
+         "ver_check": 6, "ver_charge": 7, "sn_row": 8, "sn_col": 9}
+
+EXPORTS = ["h2w_create", "h2w_destroy", "h2w_last_error", "h2w_set_points", "h2w_gen_grid", "h2w_gen_uniform",
+           "h2w_get_points", "h2w_num_points", "h2w_build_tree", "h2w_get_list", "h2w_import_list",
+           "h2w_assemble", "h2w_storage_entries", "h2w_operator_bytes", "h2w_matvec", "h2w_gmres",
+           "h2w_gmres_ir", "h2w_dense_matvec"]
+
+
+class H2WError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("h2w error %d: %s" % (code, msg))
+        self.code = code
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("form", ctypes.c_int), ("choice", ctypes.c_int),
+                ("tol_pow", ctypes.c_int), ("nlevels", ctypes.c_int), ("rank_cap", ctypes.c_int),
+                ("kernel_n", ctypes.c_int64), ("diag_n", ctypes.c_int64), ("device", ctypes.c_int)]
+
+
+_lib = None
+
+
+def build(force=False):
+    from . import build as _b
+    return _b.build(force=force)
+
+
+def lib():
+    """Load libh2w.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, I64, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+    sig = {
+        "h2w_create": [ctypes.POINTER(_Config), ctypes.POINTER(P)],
+        "h2w_destroy": [P],
+        "h2w_set_points": [P, P, I64],
+        "h2w_gen_grid": [P, I64],
+        "h2w_gen_uniform": [P, ctypes.c_uint64, I64],
+        "h2w_get_points": [P, P],
+        "h2w_num_points": [P, ctypes.POINTER(I64)],
+        "h2w_build_tree": [P],
+        "h2w_get_list": [P, I, P, P, ctypes.POINTER(I64), ctypes.POINTER(I64)],
+        "h2w_import_list": [P, I, P, P, I64],
+        "h2w_assemble": [P, I],
+        "h2w_storage_entries": [P, ctypes.POINTER(D)],
+        "h2w_operator_bytes": [P, I, ctypes.POINTER(I64)],
+        "h2w_matvec": [P, P, P, I, I, I, P],
+        "h2w_gmres": [P, P, P, I, I, I, ctypes.POINTER(I), ctypes.POINTER(D)],
+        "h2w_gmres_ir": [P, P, P, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)],
+        "h2w_dense_matvec": [P, P, P, I64, I64, I],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = I
+    L.h2w_last_error.argtypes = [P]
+    L.h2w_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def levels_for(dim, n_param, leaf_param):
+    """Tree depth exactly as the reference drivers compute it
+    (1D/codes/main.cpp:13, 2D/codes/main.cpp:13, 3D/codes/main.cpp:11)."""
+    if dim == 1:
+        return int(math.ceil(math.log(float(n_param) / leaf_param) / math.log(2)))
+    if dim == 2:
+        return int(math.ceil(2.0 * math.log(float(n_param) / leaf_param) / math.log(4)))
+    return int(math.ceil(3 * math.log(float(n_param) / leaf_param) / math.log(8)))
+
+
+class H2Operator:
+    """One compressed kernel matrix on one GPU (a handle of the C ABI)."""
+
+    def __init__(self, dim, form, choice, tol_pow, nlevels, rank_cap=0, kernel_n=0, diag_n=0, device=0):
+        L = lib()
+        cfg = _Config(dim, form, choice, tol_pow, nlevels, rank_cap, kernel_n, diag_n, device)
+        h = ctypes.c_void_p()
+        rc = L.h2w_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != OK:
+            raise H2WError(rc, "h2w_create failed (no CUDA device or bad configuration)")
+        self.h = h
+        self.dim, self.form, self.choice, self.tol_pow, self.nlevels = dim, form, choice, tol_pow, nlevels
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().h2w_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, allow=()):
+        if rc != OK and rc not in allow:
+            raise H2WError(rc, lib().h2w_last_error(self.h).decode())
+        return rc
+
+    # points and tree
+    def set_points(self, pts):
+        p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, self.dim)
+        self._ck(lib().h2w_set_points(self.h, _ptr(p), p.shape[0]))
+
+    def gen_grid(self, n_per_axis):
+        self._ck(lib().h2w_gen_grid(self.h, n_per_axis))
+
+    def gen_uniform(self, seed, n):
+        self._ck(lib().h2w_gen_uniform(self.h, seed, n))
+
+    @property
+    def N(self):
+        n = ctypes.c_int64()
+        self._ck(lib().h2w_num_points(self.h, ctypes.byref(n)))
+        return n.value
+
+    def points(self):
+        out = np.empty((self.N, self.dim))
+        self._ck(lib().h2w_get_points(self.h, _ptr(out)))
+        return out
+
+    def build_tree(self):
+        self._ck(lib().h2w_build_tree(self.h))
+
+    def get_list(self, name):
+        w = LISTS[name]
+        npt, nv = ctypes.c_int64(), ctypes.c_int64()
+        self._ck(lib().h2w_get_list(self.h, w, None, None, ctypes.byref(npt), ctypes.byref(nv)))
+        ptr = np.empty(npt.value, dtype=np.int64)
+        val = np.empty(max(nv.value, 1), dtype=np.int32)
+        self._ck(lib().h2w_get_list(self.h, w, _ptr(ptr), _ptr(val), None, None))
+        return ptr, val[:nv.value]
+
+    def import_list(self, name, ptr, val):
+        p = np.ascontiguousarray(ptr, dtype=np.int64)
+        v = np.ascontiguousarray(val, dtype=np.int32)
+        if v.size == 0:
+            v = np.zeros(1, dtype=np.int32)
+        self._ck(lib().h2w_import_list(self.h, LISTS[name], _ptr(p), _ptr(v), p.size))
+
+    def assemble(self, mode=ASSEMBLE_NCA):
+        self._ck(lib().h2w_assemble(self.h, mode))
+
+    def storage_entries(self):
+        e = ctypes.c_double()
+        self._ck(lib().h2w_storage_entries(self.h, ctypes.byref(e)))
+        return e.value
+
+    def operator_bytes(self, precision=PREC_FP64):
+        b = ctypes.c_int64()
+        self._ck(lib().h2w_operator_bytes(self.h, precision, ctypes.byref(b)))
+        return b.value
+
+    # products
+    def matvec(self, x, precision=PREC_FP64):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        nrhs = 1 if x.ndim == 1 else x.shape[1]
+        xc = np.asfortranarray(x.reshape(self.N, nrhs)) if x.ndim > 1 else x
+        y = np.empty_like(xc)
+        self._ck(lib().h2w_matvec(self.h, ctypes.c_void_p(xc.ctypes.data), ctypes.c_void_p(y.ctypes.data), nrhs,
+                                  precision, HOST, None))
+        return y
+
+    def matvec_device(self, x_ptr, y_ptr, nrhs=1, precision=PREC_FP64, stream=0):
+        self._ck(lib().h2w_matvec(self.h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), nrhs, precision, DEVICE,
+                                  ctypes.c_void_p(stream) if stream else None))
+
+    def dense_matvec(self, x, row0=0, nrows=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = self.N - row0 if nrows is None else nrows
+        y = np.empty(n)
+        self._ck(lib().h2w_dense_matvec(self.h, _ptr(x), _ptr(y), row0, n, HOST))
+        return y
+
+    def gmres(self, b, x0=None, max_iter=500, tol_pow=10):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.ones(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        it, res = ctypes.c_int(), ctypes.c_double()
+        rc = lib().h2w_gmres(self.h, _ptr(b), _ptr(x), max_iter, tol_pow, HOST, ctypes.byref(it), ctypes.byref(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return x, it.value, res.value
+
+    def gmres_ir(self, b, x0=None, max_outer=20, inner_iter=100, tol_pow=10):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.ones(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        oi, ii, res = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        rc = lib().h2w_gmres_ir(self.h, _ptr(b), _ptr(x), max_outer, inner_iter, tol_pow, HOST, ctypes.byref(oi),
+                                ctypes.byref(ii), ctypes.byref(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return x, oi.value, ii.value, res.value
+
+
+class _TreeView:
+    """The few members of the reference's tree object that callers read
+    (K->N, K->memory, findMemory_*, getTruePoten)."""
+
+    def __init__(self, op):
+        self._op = op
+        self.N = op.N
+        self.memory = 0.0
+
+    def findMemory(self):
+        self.memory = self._op.storage_entries()
+        return self.memory
+
+    findMemory_n = findMemory
+    findMemory_sn = findMemory
+
+    def getTruePoten(self, charge):
+        return self._op.dense_matvec(charge)
+
+
+class initialisation:
+    """Mirror of the reference's operator facade (class initialisation,
+    1D/codes/matvec.hpp:73-181, 2D/codes/matvec.hpp:106-173,
+    3D/codes/matvec.hpp:6-180): constructor arguments as the reference's,
+    tree_initialisation() assembles, mat_vec_prod(charge, output) fills
+    output in original point order. dim and form replace the compile-time
+    -DUSE_* choice; points (optional) replaces the uniform grid."""
+
+    def __init__(self, n_param, nLevels, nParticlesInLeaf, L, TOL_POW, Kernel_Choice, dim=1, form=FORM_NESTED,
+                 points=None, device=0, rank_cap=0):
+        if L != 1:
+            raise ValueError("the reference's grids and trees are defined for L = 1")
+        self.dim, self.form = dim, form
+        self.N_param, self.nLevels, self.nParticlesInLeaf = n_param, nLevels, nParticlesInLeaf
+        self.TOL_POW, self.Kernel_Choice, self.points = TOL_POW, Kernel_Choice, points
+        self.device, self.rank_cap = device, rank_cap
+        self.op = None
+        self.K = None
+
+    def tree_initialisation(self, mode=ASSEMBLE_NCA, skeleton=None):
+        if self.points is None:
+            N = self.N_param ** self.dim
+        else:
+            N = int(np.asarray(self.points).reshape(-1, self.dim).shape[0])
+        # 1D drivers push the grid twice before evaluating entries, so the
+        # RBF diagonal there is sqrt(2N) (1D/codes/matvec.hpp:102-106, kernel.hpp:180)
+        diag_n = 2 * N if self.dim == 1 else N
+        op = H2Operator(self.dim, self.form, self.Kernel_Choice, self.TOL_POW, self.nLevels, self.rank_cap,
+                        kernel_n=N, diag_n=diag_n, device=self.device)
+        if self.points is None:
+            op.gen_grid(self.N_param)
+        else:
+            op.set_points(self.points)
+        op.build_tree()
+        if skeleton is not None:
+            for name, (p, v) in skeleton.items():
+                op.import_list(name, p, v)
+            mode = ASSEMBLE_IMPORT
+        op.assemble(mode)
+        self.op = op
+        self.K = _TreeView(op)
+
+    def mat_vec_prod(self, charge, output=None):
+        y = self.op.matvec(charge)
+        if output is not None:
+            output.resize(y.shape, refcheck=False)
+            output[...] = y
+        return y
+
+
+class iterative_solver:
+    """Mirror of the reference's GMRES driver (class iterative_solver,
+    {1D,2D,3D}/codes/gmres.hpp:14-201): unrestarted FP64 GMRES on the GPU;
+    after GMRES() the members resid and max_iter hold the final residual
+    and the iteration count, as in the reference."""
+
+    def __init__(self, max_iter, gmres_tol_pow):
+        self.restart = max_iter
+        self.max_iter = max_iter
+        self.gmres_tol_pow = gmres_tol_pow
+        self.gmres_tol = 10.0 ** (-gmres_tol_pow)
+        self.resid = 0.0
+
+    def GMRES(self, A, x, b):
+        xs, it, res = A.op.gmres(b, x0=x, max_iter=self.max_iter, tol_pow=self.gmres_tol_pow)
+        x[...] = xs
+        self.resid = res
+        self.max_iter = it
+        return x

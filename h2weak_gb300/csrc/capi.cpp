@@ -1,0 +1,1775 @@
+// C ABI of the GB300 H2* / (H2+H)* library: handle, tree, GPU assembly,
+// packed-operator plan, matvec launches and device-resident GMRES.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "h2w_internal.h"
+#include "kernels.cuh"
+
+using namespace h2w;
+
+namespace {
+
+struct CudaError : std::runtime_error {
+    explicit CudaError(const std::string &s) : std::runtime_error(s) {}
+};
+struct ApiError : std::runtime_error {
+    int code;
+    ApiError(int c, const std::string &s) : std::runtime_error(s), code(c) {}
+};
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+template <class T> struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() {}
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { reset(); }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t cnt) {
+        reset();
+        if (cnt == 0) cnt = 1;
+        cudaError_t e = cudaMalloc(&p, cnt * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw ApiError(H2W_ERR_NOMEM, "cudaMalloc of " + std::to_string(cnt * sizeof(T)) + " bytes failed");
+        }
+        n = cnt;
+    }
+    void upload(const std::vector<T> &v, cudaStream_t st = 0) {
+        alloc(v.size());
+        if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    }
+};
+
+inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
+
+constexpr int XW_CAP = 4096;          // gathered source width per target (elements)
+constexpr int64_t ROW_CHUNK = 32768;  // rows * width per target (elements)
+
+}  // namespace
+
+struct h2w_handle {
+    h2w_config cfg{};
+    std::string err;
+    std::vector<double> pts;
+    Tree tree;
+    bool has_tree = false, has_op = false;
+    // skeletons: far[j] (2D/3D, j>=2), ver[j] (nested 2D/3D and 1D nested, j>=1), pairs[j]
+    std::vector<Skel> far, ver;
+    std::vector<Pairs> pairs;
+    bool imp[10] = {false};
+    std::vector<std::vector<int64_t>> imp_ptr;
+    std::vector<std::vector<int32_t>> imp_val;
+    // kernel parameters
+    double diag = 0, c2d = 0, four_pi = 0, loga = 0, den_small = 0, kii = 0;
+    // device state
+    DBuf<double> d_pts;
+    DBuf<int32_t> d_perm;
+    DBuf<double> d_op;
+    DBuf<float> d_op32;
+    DBuf<Target> d_T;
+    DBuf<Panel> d_P;
+    DBuf<Seg> d_S;
+    DBuf<double> d_ws, d_x, d_y;
+    DBuf<float> d_ws32, d_x32, d_y32;
+    std::vector<Phase> phases;
+    bool fused_scatter = true;
+    int64_t ws_n = 0, yperm_off = 0, op_n = 0;
+    double storage = 0;
+    int64_t op_bytes_read = 0;  // elements of operator data one matvec reads
+    // GMRES state
+    DBuf<double> g_V, g_w, g_vcur, g_H, g_cs, g_sn, g_s, g_part, g_scal, g_tmp, g_b, g_r, g_npart;
+    DBuf<int32_t> g_iter;
+    int g_m = -1;
+    cudaStream_t stream = nullptr;
+
+    KParams kparams() const {
+        KParams k;
+        k.pts = d_pts.p;
+        k.dim = cfg.dim;
+        k.choice = cfg.choice;
+        k.diag = diag;
+        k.c2d = c2d;
+        k.four_pi = four_pi;
+        k.loga = loga;
+        k.den_small = den_small;
+        return k;
+    }
+};
+
+namespace {
+
+// ------------------------------------------------------ kernel set-up ---
+// Gauss-Legendre 16-point self term, as the reference integrates it
+// (1D/codes/integral1d.hpp:17-39, 2D/codes/integral2d.hpp:60-90,
+// 3D/codes/integral3d.hpp:13-50); nodes by Newton iteration on the Legendre
+// recurrence, ordered by |x| with the negative node first.
+void gl16(std::vector<double> &x, std::vector<double> &w) {
+    const int n = 16;
+    std::vector<std::pair<long double, long double>> pr;
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (int i = 1; i <= n; ++i) {
+        long double z = cosl(pi * (i - 0.25L) / (n + 0.5L)), pp = 0;
+        for (int it = 0; it < 100; ++it) {
+            long double p1 = 1, p2 = 0;
+            for (int k = 1; k <= n; ++k) {
+                long double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0L * k - 1.0L) * z * p2 - (k - 1.0L) * p3) / k;
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0L);
+            long double dz = p1 / pp;
+            z -= dz;
+            if (fabsl(dz) < 1e-30L) break;
+        }
+        pr.push_back({z, 2.0L / ((1.0L - z * z) * pp * pp)});
+    }
+    std::sort(pr.begin(), pr.end(), [](auto &a, auto &b) {
+        long double fa = fabsl(a.first), fb = fabsl(b.first);
+        return fa != fb ? fa < fb : a.first < b.first;
+    });
+    x.clear();
+    w.clear();
+    for (auto &p : pr) {
+        x.push_back((double)p.first);
+        w.push_back((double)p.second);
+    }
+}
+
+void setup_kernel(h2w_handle *h) {
+    const double PI = 4.0 * std::atan(1.0);
+    const int dim = h->cfg.dim;
+    const int64_t N = h->tree.N;
+    const int64_t kn = h->cfg.kernel_n > 0 ? h->cfg.kernel_n : N;
+    const int64_t dn = h->cfg.diag_n > 0 ? h->cfg.diag_n : N;
+    h->c2d = (-1.0 / (2 * PI)) * 0.5;
+    h->four_pi = 4.0 * PI;
+    const double a = 0.0001;
+    h->loga = std::log(a);
+    h->den_small = a * std::log(a) - 1.0;
+    if (h->cfg.choice == 0) {
+        double hh = dim == 1 ? 1.0 / double(kn) : (dim == 2 ? 1.0 / std::sqrt(double(kn)) : 1.0 / std::cbrt(double(kn)));
+        std::vector<double> x, w;
+        gl16(x, w);
+        double lo = 0.0, hi = hh * 0.5, cx = 0.5 * (hi - lo), Lx = 0.5 * (hi + lo), res = 0.0, hd;
+        if (dim == 1) {
+            for (int i = 0; i < 16; ++i) res += w[i] * std::log(std::fabs(1.0 * (cx * x[i] + Lx)));
+            res *= cx;
+            res *= 2;
+            hd = hh;
+        } else if (dim == 2) {
+            const double c = -1.0 / (2 * PI);
+            for (int i = 0; i < 16; ++i) {
+                double tx = cx * x[i] + Lx;
+                for (int j = 0; j < 16; ++j) {
+                    double ty = cx * x[j] + Lx;
+                    res += w[i] * w[j] * (c * 0.5 * std::log(tx * tx + ty * ty));
+                }
+            }
+            res *= (cx * cx);
+            res *= 4;
+            hd = std::pow(hh, 2.0);
+        } else {
+            for (int i = 0; i < 16; ++i) {
+                double tx = cx * x[i] + Lx;
+                for (int j = 0; j < 16; ++j) {
+                    double ty = cx * x[j] + Lx;
+                    for (int k = 0; k < 16; ++k) {
+                        double tz = cx * x[k] + Lx;
+                        res += (w[i] * w[j] * w[k] * (1.0 / ((4 * PI) * std::sqrt(tx * tx + ty * ty + tz * tz))));
+                    }
+                }
+            }
+            res *= (cx * cx * cx);
+            res *= 8;
+            hd = std::pow(hh, 3.0);
+        }
+        h->kii = res;
+        h->diag = (1.0 + res) / hd;
+    } else {
+        h->diag = dim == 2 ? 1.0 : std::sqrt((double)dn);
+    }
+}
+
+// ------------------------------------------------------------- helpers ---
+std::vector<int32_t> box_pts(const Tree &t, int j, int64_t k) {
+    return std::vector<int32_t>(t.perm.begin() + t.off[j][k], t.perm.begin() + t.off[j][k + 1]);
+}
+void append(std::vector<int32_t> &a, const int32_t *b, int64_t n) { a.insert(a.end(), b, b + n); }
+
+// ------------------------------------------------------------ NCA runs ---
+// Run the batched NCA on problems (R[p], C[p]); returns local pivots.
+void run_nca(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+             std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
+    const size_t np = R.size();
+    prow.assign(np, {});
+    pcol.assign(np, {});
+    const double tol = std::pow(10, -1.0 * h->cfg.tol_pow);
+    const int cap = h->cfg.rank_cap > 0 ? h->cfg.rank_cap : 512;
+    const size_t budget = (size_t)3 << 30;  // scratch bytes per batch
+    KParams kp = h->kparams();
+    size_t p0 = 0;
+    while (p0 < np) {
+        std::vector<NcaProb> probs;
+        std::vector<int32_t> idx;
+        size_t scr = 0;
+        int64_t piv = 0;
+        int mx1 = 1, mx2 = 1, mxr = 1;
+        size_t p = p0;
+        for (; p < np; ++p) {
+            int n1 = (int)R[p].size(), n2 = (int)C[p].size();
+            int rc = std::min(std::min(n1, n2), cap);
+            size_t need = (size_t)rc * (size_t)(n1 + n2);
+            if (!probs.empty() && (scr + need) * 8 > budget) break;
+            NcaProb pb{};
+            pb.ri = (int64_t)idx.size();
+            append(idx, R[p].data(), n1);
+            pb.ci = (int64_t)idx.size();
+            append(idx, C[p].data(), n2);
+            pb.u = (int64_t)scr;
+            pb.v = (int64_t)(scr + (size_t)rc * n1);
+            scr += need;
+            pb.piv = piv;
+            piv += rc;
+            pb.n1 = n1;
+            pb.n2 = n2;
+            pb.rcap = rc;
+            probs.push_back(pb);
+            mx1 = std::max(mx1, n1);
+            mx2 = std::max(mx2, n2);
+            mxr = std::max(mxr, rc);
+        }
+        DBuf<NcaProb> dp;
+        DBuf<int32_t> di, drank, dpr, dpc, dst;
+        DBuf<double> dscr;
+        dp.upload(probs, h->stream);
+        di.upload(idx, h->stream);
+        dscr.alloc(scr);
+        drank.alloc(probs.size());
+        dpr.alloc((size_t)piv);
+        dpc.alloc((size_t)piv);
+        dst.alloc(1);
+        CK(cudaMemsetAsync(dst.p, 0, 4, h->stream));
+        CK(launch_nca(dp.p, (int)probs.size(), di.p, kp, tol, dscr.p, drank.p, dpr.p, dpc.p, dst.p, mx1, mx2, mxr,
+                      h->stream));
+        std::vector<int32_t> rk(probs.size()), hpr((size_t)piv), hpc((size_t)piv);
+        int32_t status = 0;
+        CK(cudaMemcpyAsync(rk.data(), drank.p, rk.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+        if (piv) {
+            CK(cudaMemcpyAsync(hpr.data(), dpr.p, hpr.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(hpc.data(), dpc.p, hpc.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+        }
+        CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (status & 1) throw ApiError(H2W_ERR_RANK, "an NCA block needed more than rank_cap pivots");
+        if (status & 2) throw ApiError(H2W_ERR_ARG, "non-finite kernel entries (coincident points?) in an NCA block");
+        for (size_t q = 0; q < probs.size(); ++q) {
+            const NcaProb &pb = probs[q];
+            prow[p0 + q].assign(hpr.begin() + pb.piv, hpr.begin() + pb.piv + rk[q]);
+            pcol[p0 + q].assign(hpc.begin() + pb.piv, hpc.begin() + pb.piv + rk[q]);
+        }
+        p0 = p;
+    }
+}
+
+void skel_from_pivots(Skel &s, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+                      const std::vector<std::vector<int32_t>> &pr, const std::vector<std::vector<int32_t>> &pc) {
+    s.ptr.assign(R.size() + 1, 0);
+    s.chk.clear();
+    s.chg.clear();
+    for (size_t k = 0; k < R.size(); ++k) {
+        for (size_t i = 0; i < pr[k].size(); ++i) {
+            s.chk.push_back(R[k][(size_t)pr[k][i]]);
+            s.chg.push_back(C[k][(size_t)pc[k][i]]);
+        }
+        s.ptr[k + 1] = (int64_t)s.chk.size();
+    }
+}
+
+// rows of the far NCA / far transfer of box (j,k): leaf points or the
+// children's far check points (pivot_selection_bottom_up, 2D :537-550)
+std::vector<int32_t> far_rows(const h2w_handle *h, int j, int64_t k) {
+    const Tree &t = h->tree;
+    if (j == t.nL) return box_pts(t, j, k);
+    std::vector<int32_t> r;
+    const Skel &s = h->far[(size_t)j + 1];
+    for (int c = 0; c < t.nch; ++c) {
+        int64_t q = k * t.nch + c;
+        append(r, s.chk.data() + s.ptr[q], s.rank(q));
+    }
+    return r;
+}
+// rows of a vertex / 1D nested transfer: leaf points or children's check points
+std::vector<int32_t> ver_rows(const h2w_handle *h, int j, int64_t k) {
+    const Tree &t = h->tree;
+    if (j == t.nL) return box_pts(t, j, k);
+    std::vector<int32_t> r;
+    const Skel &s = h->ver[(size_t)j + 1];
+    for (int c = 0; c < t.nch; ++c) {
+        int64_t q = k * t.nch + c;
+        append(r, s.chk.data() + s.ptr[q], s.rank(q));
+    }
+    return r;
+}
+
+void nca_far(h2w_handle *h) {
+    const Tree &t = h->tree;
+    h->far.assign((size_t)t.nL + 1, Skel{});
+    for (int j = 0; j <= t.nL; ++j) h->far[(size_t)j].ptr.assign((size_t)t.nbox[(size_t)j] + 1, 0);
+    for (int j = t.nL; j >= 2; --j) {
+        const int64_t nb = t.nbox[(size_t)j];
+        std::vector<std::vector<int32_t>> R((size_t)nb), C((size_t)nb), pr, pc;
+        for (int64_t k = 0; k < nb; ++k) {
+            R[(size_t)k] = far_rows(h, j, k);
+            for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e) {
+                if (t.ilv[(size_t)j][(size_t)e]) continue;
+                std::vector<int32_t> c = far_rows(h, j, t.il[(size_t)j][(size_t)e]);
+                append(C[(size_t)k], c.data(), (int64_t)c.size());
+            }
+        }
+        run_nca(h, R, C, pr, pc);
+        skel_from_pivots(h->far[(size_t)j], R, C, pr, pc);
+    }
+}
+
+void nca_ver(h2w_handle *h) {
+    const Tree &t = h->tree;
+    h->ver.assign((size_t)t.nL + 1, Skel{});
+    h->ver[0].ptr.assign(2, 0);
+    for (int j = 1; j <= t.nL; ++j) {
+        const int64_t nb = t.nbox[(size_t)j];
+        std::vector<std::vector<int32_t>> R((size_t)nb), C((size_t)nb), pr, pc;
+        for (int64_t k = 0; k < nb; ++k) {
+            R[(size_t)k] = box_pts(t, j, k);
+            auto &c = C[(size_t)k];
+            if (t.dim == 1) {
+                for (int s = 0; s < 2; ++s) {
+                    int32_t q = t.nb[(size_t)j][(size_t)(k * 2 + s)];
+                    if (q != -1) append(c, t.perm.data() + t.off[(size_t)j][(size_t)q], t.cnt(j, q));
+                }
+            } else {
+                for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e) {
+                    if (!t.ilv[(size_t)j][(size_t)e]) continue;
+                    int32_t q = t.il[(size_t)j][(size_t)e];
+                    append(c, t.perm.data() + t.off[(size_t)j][(size_t)q], t.cnt(j, q));
+                }
+            }
+            if (j > 1) {
+                const Skel &ps = h->ver[(size_t)j - 1];
+                int64_t par = k / t.nch;
+                append(c, ps.chg.data() + ps.ptr[(size_t)par], ps.rank(par));
+            }
+        }
+        run_nca(h, R, C, pr, pc);
+        skel_from_pivots(h->ver[(size_t)j], R, C, pr, pc);
+    }
+}
+
+// Pair lists: 2D/3D semi-nested vertex pairs, 1D sibling pairs.
+void pair_layout(h2w_handle *h) {
+    const Tree &t = h->tree;
+    h->pairs.assign((size_t)t.nL + 1, Pairs{});
+    for (int j = 1; j <= t.nL; ++j) {
+        Pairs &P = h->pairs[(size_t)j];
+        for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+            if (t.dim == 1) {
+                for (int s = 0; s < 2; ++s) {
+                    int32_t q = t.nb[(size_t)j][(size_t)(k * 2 + s)];
+                    if (q == -1) continue;
+                    P.box.push_back((int32_t)k);
+                    P.slot.push_back(s);
+                    P.other.push_back(q);
+                }
+            } else {
+                for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e) {
+                    if (!t.ilv[(size_t)j][(size_t)e]) continue;
+                    P.box.push_back((int32_t)k);
+                    P.slot.push_back((int32_t)(e - t.ilp[(size_t)j][(size_t)k]));
+                    P.other.push_back(t.il[(size_t)j][(size_t)e]);
+                }
+            }
+        }
+        P.ptr.assign(P.box.size() + 1, 0);
+    }
+}
+
+void nca_pairs(h2w_handle *h) {
+    const Tree &t = h->tree;
+    std::vector<std::vector<int32_t>> R, C, pr, pc;
+    for (int j = 1; j <= t.nL; ++j) {
+        Pairs &P = h->pairs[(size_t)j];
+        for (size_t p = 0; p < P.box.size(); ++p) {
+            R.push_back(box_pts(t, j, P.box[p]));
+            C.push_back(box_pts(t, j, P.other[p]));
+        }
+    }
+    run_nca(h, R, C, pr, pc);
+    size_t q = 0;
+    for (int j = 1; j <= t.nL; ++j) {
+        Pairs &P = h->pairs[(size_t)j];
+        P.row.clear();
+        P.col.clear();
+        for (size_t p = 0; p < P.box.size(); ++p, ++q) {
+            for (size_t i = 0; i < pr[q].size(); ++i) {
+                P.row.push_back(R[q][(size_t)pr[q][i]]);
+                P.col.push_back(C[q][(size_t)pc[q][i]]);
+            }
+            P.ptr[p + 1] = (int64_t)P.row.size();
+        }
+    }
+}
+
+// --------------------------------------------------------- list import ---
+// Per-(level, box) CSR lists -> skeletons / pairs.
+void import_skel(h2w_handle *h, int which_chk, int which_chg, std::vector<Skel> &S, int jmin) {
+    const Tree &t = h->tree;
+    const auto &p1 = h->imp_ptr[(size_t)which_chk];
+    const auto &v1 = h->imp_val[(size_t)which_chk];
+    const auto &v2 = h->imp_val[(size_t)which_chg];
+    const auto &p2 = h->imp_ptr[(size_t)which_chg];
+    S.assign((size_t)t.nL + 1, Skel{});
+    int64_t base = 0;
+    for (int j = 0; j <= t.nL; ++j) {
+        Skel &s = S[(size_t)j];
+        s.ptr.assign((size_t)t.nbox[(size_t)j] + 1, 0);
+        for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+            int64_t b = base + k;
+            int64_t a0 = p1[(size_t)b], a1 = p1[(size_t)b + 1];
+            if (p2[(size_t)b + 1] - p2[(size_t)b] != a1 - a0) throw ApiError(H2W_ERR_ARG, "pivot lists differ in length");
+            if (j >= jmin)
+                for (int64_t i = a0; i < a1; ++i) {
+                    s.chk.push_back(v1[(size_t)i]);
+                    s.chg.push_back(v2[(size_t)(p2[(size_t)b] + i - a0)]);
+                }
+            s.ptr[(size_t)k + 1] = (int64_t)s.chk.size();
+        }
+        base += t.nbox[(size_t)j];
+    }
+}
+
+void import_pairs(h2w_handle *h) {
+    const Tree &t = h->tree;
+    const auto &pr = h->imp_ptr[H2W_LIST_SN_ROW];
+    const auto &vr = h->imp_val[H2W_LIST_SN_ROW];
+    const auto &pcp = h->imp_ptr[H2W_LIST_SN_COL];
+    const auto &vc = h->imp_val[H2W_LIST_SN_COL];
+    // entry index of (j, k, slot) in the CSR
+    int64_t e = 0;
+    std::vector<std::vector<int64_t>> first((size_t)t.nL + 1);
+    for (int j = 0; j <= t.nL; ++j) {
+        first[(size_t)j].assign((size_t)t.nbox[(size_t)j] + 1, 0);
+        for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+            first[(size_t)j][(size_t)k] = e;
+            if (t.dim == 1) e += j >= 1 ? 2 : 0;
+            else e += t.ilp[(size_t)j][(size_t)k + 1] - t.ilp[(size_t)j][(size_t)k];
+        }
+    }
+    if ((int64_t)pr.size() != e + 1) throw ApiError(H2W_ERR_ARG, "pair list has the wrong number of entries");
+    for (int j = 1; j <= t.nL; ++j) {
+        Pairs &P = h->pairs[(size_t)j];
+        P.row.clear();
+        P.col.clear();
+        for (size_t p = 0; p < P.box.size(); ++p) {
+            int64_t q = first[(size_t)j][(size_t)P.box[p]] + P.slot[p];
+            int64_t a0 = pr[(size_t)q], a1 = pr[(size_t)q + 1];
+            int64_t b0 = pcp[(size_t)q], b1 = pcp[(size_t)q + 1];
+            if (a1 - a0 != b1 - b0) throw ApiError(H2W_ERR_ARG, "pair pivot lists differ in length");
+            P.row.insert(P.row.end(), vr.begin() + a0, vr.begin() + a1);
+            P.col.insert(P.col.end(), vc.begin() + b0, vc.begin() + b1);
+            P.ptr[p + 1] = (int64_t)P.row.size();
+        }
+    }
+}
+
+// ---------------------------------------------------------------- plan ---
+struct PlanBuilder {
+    h2w_handle *h;
+    std::vector<Target> T;
+    std::vector<Panel> P;
+    std::vector<Seg> S;
+    std::vector<int32_t> idx;
+    std::vector<FillJob> fills;
+    std::vector<FactorJob> factors;
+    std::vector<XferJob> xfers;
+    int64_t opn = 0, fn = 0;
+    int max_xfer_n = 0;
+    int64_t read_elems = 0;
+
+    int64_t alloc(int64_t rows, int64_t cols, int32_t &lda) {
+        lda = (int32_t)pad4(cols);
+        int64_t a = opn;
+        opn += pad4((int64_t)lda * rows);
+        return a;
+    }
+    int64_t put_idx(const int32_t *v, int64_t n) {
+        int64_t o = (int64_t)idx.size();
+        append(idx, v, n);
+        return o;
+    }
+    int64_t put_idx(const std::vector<int32_t> &v) { return put_idx(v.data(), (int64_t)v.size()); }
+
+    struct PanelSpec {
+        int64_t a;
+        int32_t lda, w;
+        std::vector<Seg> segs;  // xoff relative to panel
+    };
+    // Emit a target (row- and column-split as needed).
+    void emit(int64_t dst, int32_t nrows, int32_t flags, const std::vector<PanelSpec> &panels) {
+        if (nrows <= 0) return;
+        int64_t xw = 0;
+        for (auto &p : panels) xw += pad4(p.w);
+        for (auto &p : panels) read_elems += (int64_t)nrows * p.w;
+        if (xw == 0) return;
+        if (xw <= XW_CAP) {
+            int64_t rows_per = std::max<int64_t>(1, std::min<int64_t>(nrows, ROW_CHUNK / std::max<int64_t>(xw, 1)));
+            for (int64_t r0 = 0; r0 < nrows; r0 += rows_per) {
+                int32_t nr = (int32_t)std::min<int64_t>(rows_per, nrows - r0);
+                Target tg{};
+                tg.dst = dst + r0;
+                tg.nrows = nr;
+                tg.flags = flags;
+                tg.p0 = (int32_t)P.size();
+                int32_t xo = 0;
+                for (auto &p : panels) {
+                    Panel pn{};
+                    pn.a = p.a + r0 * p.lda;
+                    pn.lda = p.lda;
+                    pn.w = p.w;
+                    pn.xoff = xo;
+                    pn.s0 = (int32_t)S.size();
+                    for (auto s : p.segs) S.push_back(s);
+                    pn.s1 = (int32_t)S.size();
+                    P.push_back(pn);
+                    xo += (int32_t)pad4(p.w);
+                }
+                tg.p1 = (int32_t)P.size();
+                tg.xw = xo;
+                tg.gsz = xo >= 256 ? 32 : (xo >= 128 ? 16 : (xo >= 48 ? 8 : 4));
+                T.push_back(tg);
+            }
+            return;
+        }
+        // column split: one sub-target per chunk of <= XW_CAP columns, atomically accumulated
+        if (flags & T_SCATTER) h->fused_scatter = false;
+        for (auto &p : panels) {
+            for (int64_t c0 = 0; c0 < p.w; c0 += XW_CAP) {
+                int64_t c1 = std::min<int64_t>(p.w, c0 + XW_CAP);
+                PanelSpec q;
+                q.a = p.a + c0;
+                q.lda = p.lda;
+                q.w = (int32_t)(c1 - c0);
+                for (auto s : p.segs) {
+                    int64_t s0 = s.xoff, s1 = s.xoff + s.len;
+                    int64_t lo = std::max(s0, c0), hi = std::min(s1, c1);
+                    if (lo >= hi) continue;
+                    Seg ns = s;
+                    ns.src = s.src + (lo - s0);
+                    ns.len = (int32_t)(hi - lo);
+                    ns.xoff = (int32_t)(lo - c0);
+                    q.segs.push_back(ns);
+                }
+                // the sub-panel's row starts are no longer 4-aligned unless c0 is
+                int64_t rd = read_elems;
+                emit(dst, nrows, T_ATOMIC, {q});
+                read_elems = rd;
+            }
+        }
+    }
+};
+
+// Host-side bounds and alignment check of every work item before any of it
+// reaches the GPU: an inconsistent plan becomes an error status, never an
+// out-of-bounds access.
+void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
+    auto bad = [](const char *what) { throw ApiError(H2W_ERR_STATE, std::string("internal plan check failed: ") + what); };
+    const int64_t N = h->tree.N, wsn = h->ws_n, opn = pb.opn, nidx = (int64_t)pb.idx.size();
+    for (const Phase &ph : h->phases)
+        if (ph.t0 < 0 || ph.t1 < ph.t0 || ph.t1 > (int64_t)pb.T.size() || ph.max_xw > XW_CAP) bad("phase");
+    for (const Target &t : pb.T) {
+        if (t.nrows < 1 || t.dst < 0 || t.dst + t.nrows > wsn) bad("target rows");
+        if (t.p0 < 0 || t.p1 < t.p0 || t.p1 > (int32_t)pb.P.size()) bad("target panels");
+        if (!(t.gsz == 4 || t.gsz == 8 || t.gsz == 16 || t.gsz == 32)) bad("gsz");
+        if ((t.flags & T_SCATTER) && (t.dst < h->yperm_off || t.dst + t.nrows > h->yperm_off + N)) bad("scatter rows");
+        int64_t xw = 0;
+        for (int32_t q = t.p0; q < t.p1; ++q) {
+            const Panel &p = pb.P[(size_t)q];
+            if (p.a < 0 || p.a % 4 || p.lda % 4 || p.lda < p.w || p.w < 0) bad("panel layout");
+            if (p.a + (int64_t)(t.nrows - 1) * p.lda + p.w > opn) bad("panel extent");
+            if (p.xoff % 4 || p.xoff != xw) bad("panel xoff");
+            if (p.s0 < 0 || p.s1 < p.s0 || p.s1 > (int32_t)pb.S.size()) bad("panel segs");
+            for (int32_t e = p.s0; e < p.s1; ++e) {
+                const Seg &sg = pb.S[(size_t)e];
+                if (sg.len < 0 || sg.xoff < 0 || sg.xoff + sg.len > p.w) bad("segment span");
+                if (sg.flags & S_GATHER) {
+                    if (sg.src < 0 || sg.src + sg.len > N) bad("gather segment");
+                } else if (sg.src < 0 || sg.src + sg.len > wsn) bad("workspace segment");
+            }
+            xw += pad4(p.w);
+        }
+        if (xw != t.xw || xw > XW_CAP) bad("target width");
+    }
+    for (const FactorJob &f : pb.factors)
+        if (f.r < 1 || f.f < 0 || f.f + (int64_t)f.r * f.r > pb.fn || f.ii < 0 || f.ii + f.r > nidx || f.jj < 0 ||
+            f.jj + f.r > nidx)
+            bad("factor job");
+    for (const XferJob &x : pb.xfers) {
+        if (x.r < 1 || x.n < 1 || x.n > pb.max_xfer_n || x.f < 0 || x.f + (int64_t)x.r * x.r > pb.fn) bad("xfer job");
+        if (x.jj < 0 || x.jj + x.r > nidx || x.pi < 0 || x.pi + x.n > nidx) bad("xfer indices");
+        bool row = x.mode == X_ROW_RL || x.mode == X_ROW_R;
+        if (row) {
+            if (x.ld1 < x.r || x.a1 < 0 || x.a1 + (int64_t)(x.n - 1) * x.ld1 + x.r > opn) bad("xfer rows");
+            if (x.a2 >= 0 && (x.ld2 < x.n || x.a2 + (int64_t)(x.r - 1) * x.ld2 + x.n > opn)) bad("xfer transposed");
+        } else if (x.ld1 < x.n || x.a1 < 0 || x.a1 + (int64_t)(x.r - 1) * x.ld1 + x.n > opn) {
+            bad("xfer columns");
+        }
+    }
+    for (const FillJob &f : pb.fills)
+        if (f.nr < 1 || f.nc < 1 || f.lda < f.nc || f.a < 0 || f.a + (int64_t)(f.nr - 1) * f.lda + f.nc > opn ||
+            f.ri < 0 || f.ri + f.nr > nidx || f.ci < 0 || f.ci + f.nc > nidx)
+            bad("fill job");
+    for (int32_t v : pb.idx)
+        if (v < 0 || v >= N) bad("point index");
+}
+
+void build_plan(h2w_handle *h) {
+    Tree &t = h->tree;
+    const int L = t.nL, dim = t.dim;
+    const bool sn = h->cfg.form == H2W_FORM_SEMINESTED;
+    const bool has_far = dim > 1;
+    const bool has_ver = (dim == 1 && !sn) || (dim > 1 && !sn);
+    const bool has_pairs = sn;
+    PlanBuilder pb;
+    pb.h = h;
+    h->fused_scatter = true;
+
+    // ---- workspace layout
+    int64_t wsn = 0;
+    h->yperm_off = wsn;
+    wsn += t.N;
+    std::vector<int64_t> fo((size_t)L + 2, 0), fi((size_t)L + 2, 0), vo((size_t)L + 2, 0), vi((size_t)L + 2, 0),
+        to((size_t)L + 2, 0);
+    std::vector<std::vector<int64_t>> poff((size_t)L + 1);
+    for (int j = 1; j <= L; ++j) {
+        if (has_far && j >= 2) {
+            int64_t R = (int64_t)h->far[(size_t)j].chk.size();
+            fo[(size_t)j] = wsn; wsn += R;
+            fi[(size_t)j] = wsn; wsn += R;
+        }
+        if (has_ver) {
+            int64_t R = (int64_t)h->ver[(size_t)j].chk.size();
+            vo[(size_t)j] = wsn; wsn += R;
+            vi[(size_t)j] = wsn; wsn += R;
+        }
+        if (has_pairs) {
+            to[(size_t)j] = wsn;
+            wsn += (int64_t)h->pairs[(size_t)j].row.size();
+        }
+    }
+    h->ws_n = wsn;
+    auto leaf_gather = [&](int j, int64_t q, int32_t xoff) {
+        Seg s{};
+        s.src = t.off[(size_t)j][(size_t)q];
+        s.len = (int32_t)t.cnt(j, q);
+        s.xoff = xoff;
+        s.flags = S_GATHER;
+        return s;
+    };
+    auto ws_seg = [&](int64_t src, int64_t len, int32_t xoff) {
+        Seg s{};
+        s.src = src;
+        s.len = (int32_t)len;
+        s.xoff = xoff;
+        s.flags = S_WS;
+        return s;
+    };
+
+    // ---- transfer matrices (far and vertex / 1D nested)
+    struct Xfer { int64_t up = -1, dn = -1; int32_t ldu = 0, ldd = 0, rows = 0, r = 0; };
+    std::vector<std::vector<Xfer>> fx((size_t)L + 1), vx((size_t)L + 1);
+    auto make_xfer = [&](const Skel &s, int64_t k, const std::vector<int32_t> &rows, Xfer &x) {
+        int32_t r = (int32_t)s.rank(k);
+        x.r = r;
+        x.rows = (int32_t)rows.size();
+        if (r == 0 || rows.empty()) return;
+        FactorJob fj{};
+        fj.f = pb.fn;
+        pb.fn += (int64_t)r * r;
+        fj.ii = pb.put_idx(s.chk.data() + s.ptr[(size_t)k], r);
+        fj.jj = pb.put_idx(s.chg.data() + s.ptr[(size_t)k], r);
+        fj.r = r;
+        pb.factors.push_back(fj);
+        x.up = pb.alloc(r, x.rows, x.ldu);
+        x.dn = pb.alloc(x.rows, r, x.ldd);
+        XferJob xj{};
+        xj.f = fj.f;
+        xj.jj = fj.jj;
+        xj.pi = pb.put_idx(rows);
+        xj.a1 = x.dn;
+        xj.ld1 = x.ldd;
+        xj.a2 = x.up;
+        xj.ld2 = x.ldu;
+        xj.r = r;
+        xj.n = x.rows;
+        xj.mode = X_ROW_RL;
+        pb.xfers.push_back(xj);
+        pb.max_xfer_n = std::max(pb.max_xfer_n, x.rows);
+    };
+    for (int j = 1; j <= L; ++j) {
+        const int64_t nb = t.nbox[(size_t)j];
+        if (has_far && j >= 2) {
+            fx[(size_t)j].resize((size_t)nb);
+            for (int64_t k = 0; k < nb; ++k) make_xfer(h->far[(size_t)j], k, far_rows(h, j, k), fx[(size_t)j][(size_t)k]);
+        }
+        if (has_ver) {
+            vx[(size_t)j].resize((size_t)nb);
+            for (int64_t k = 0; k < nb; ++k) make_xfer(h->ver[(size_t)j], k, ver_rows(h, j, k), vx[(size_t)j][(size_t)k]);
+        }
+    }
+    auto child_off = [&](const Skel &s, int64_t k) { return s.ptr[(size_t)(k * t.nch)]; };
+    auto child_len = [&](const Skel &s, int64_t k) { return s.ptr[(size_t)((k + 1) * t.nch)] - s.ptr[(size_t)(k * t.nch)]; };
+
+    // ---- UP phases, levels L..1
+    for (int j = L; j >= 1; --j) {
+        int64_t t0 = (int64_t)pb.T.size();
+        for (int kind = 0; kind < 2; ++kind) {
+            if (kind == 0 && !(has_far && j >= 2)) continue;
+            if (kind == 1 && !has_ver) continue;
+            const Skel &s = kind == 0 ? h->far[(size_t)j] : h->ver[(size_t)j];
+            const auto &X = kind == 0 ? fx[(size_t)j] : vx[(size_t)j];
+            const int64_t outb = kind == 0 ? fo[(size_t)j] : vo[(size_t)j];
+            for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+                const Xfer &x = X[(size_t)k];
+                if (x.up < 0) continue;
+                PlanBuilder::PanelSpec ps;
+                ps.a = x.up;
+                ps.lda = x.ldu;
+                ps.w = x.rows;
+                if (j == L) ps.segs.push_back(leaf_gather(j, k, 0));
+                else {
+                    const Skel &cs = kind == 0 ? h->far[(size_t)j + 1] : h->ver[(size_t)j + 1];
+                    const int64_t cb = kind == 0 ? fo[(size_t)j + 1] : vo[(size_t)j + 1];
+                    ps.segs.push_back(ws_seg(cb + child_off(cs, k), child_len(cs, k), 0));
+                }
+                pb.emit(outb + s.ptr[(size_t)k], x.r, T_ACCUM, {ps});
+            }
+        }
+        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
+    }
+
+    // ---- coupling phase: M2L (far, vertex), near field, pair phase A
+    std::vector<std::vector<int64_t>> pfac((size_t)L + 1);
+    {
+        int64_t t0 = (int64_t)pb.T.size();
+        for (int j = 1; j <= L; ++j) {
+            for (int kind = 0; kind < 2; ++kind) {
+                if (kind == 0 && !(has_far && j >= 2)) continue;
+                if (kind == 1 && !has_ver) continue;
+                const Skel &s = kind == 0 ? h->far[(size_t)j] : h->ver[(size_t)j];
+                const int64_t outb = kind == 0 ? fo[(size_t)j] : vo[(size_t)j];
+                const int64_t inb = kind == 0 ? fi[(size_t)j] : vi[(size_t)j];
+                for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+                    int32_t r = (int32_t)s.rank(k);
+                    if (r == 0) continue;
+                    std::vector<int32_t> srcs;
+                    if (dim == 1) {
+                        for (int sl = 0; sl < 2; ++sl) {
+                            int32_t q = t.nb[(size_t)j][(size_t)(k * 2 + sl)];
+                            if (q != -1) srcs.push_back(q);
+                        }
+                    } else {
+                        for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e)
+                            if ((bool)t.ilv[(size_t)j][(size_t)e] == (kind == 1)) srcs.push_back(t.il[(size_t)j][(size_t)e]);
+                    }
+                    int64_t W = 0;
+                    for (int32_t q : srcs) W += s.rank(q);
+                    if (W == 0) continue;
+                    PlanBuilder::PanelSpec ps;
+                    ps.a = pb.alloc(r, W, ps.lda);
+                    ps.w = (int32_t)W;
+                    int64_t ri = pb.put_idx(s.chk.data() + s.ptr[(size_t)k], r);
+                    int32_t co = 0;
+                    for (int32_t q : srcs) {
+                        int32_t rq = (int32_t)s.rank(q);
+                        if (rq == 0) continue;
+                        ps.segs.push_back(ws_seg(outb + s.ptr[(size_t)q], rq, co));
+                        FillJob fj{};
+                        fj.a = ps.a + co;
+                        fj.ri = ri;
+                        fj.ci = pb.put_idx(s.chk.data() + s.ptr[(size_t)q], rq);
+                        fj.nr = r;
+                        fj.nc = rq;
+                        fj.lda = ps.lda;
+                        pb.fills.push_back(fj);
+                        co += rq;
+                    }
+                    pb.emit(inb + s.ptr[(size_t)k], r, T_ACCUM, {ps});
+                }
+            }
+        }
+        // near field: neighbour slots in order, then self (assemble_NearField)
+        for (int64_t k = 0; k < t.nbox[(size_t)L]; ++k) {
+            int32_t n = (int32_t)t.cnt(L, k);
+            if (n == 0) continue;
+            std::vector<int32_t> srcs;
+            if (dim > 1)
+                for (int sl = 0; sl < t.nnb; ++sl) {
+                    int32_t q = t.nb[(size_t)L][(size_t)(k * t.nnb + sl)];
+                    if (q != -1) srcs.push_back(q);
+                }
+            srcs.push_back((int32_t)k);
+            int64_t W = 0;
+            for (int32_t q : srcs) W += t.cnt(L, q);
+            PlanBuilder::PanelSpec ps;
+            ps.a = pb.alloc(n, W, ps.lda);
+            ps.w = (int32_t)W;
+            int64_t ri = pb.put_idx(t.perm.data() + t.off[(size_t)L][(size_t)k], n);
+            int32_t co = 0;
+            for (int32_t q : srcs) {
+                int32_t nq = (int32_t)t.cnt(L, q);
+                if (nq == 0) continue;
+                ps.segs.push_back(leaf_gather(L, q, co));
+                FillJob fj{};
+                fj.a = ps.a + co;
+                fj.ri = ri;
+                fj.ci = pb.put_idx(t.perm.data() + t.off[(size_t)L][(size_t)q], nq);
+                fj.nr = n;
+                fj.nc = nq;
+                fj.lda = ps.lda;
+                pb.fills.push_back(fj);
+                co += nq;
+            }
+            pb.emit(h->yperm_off + t.off[(size_t)L][(size_t)k], n, T_ACCUM, {ps});
+        }
+        // pair phase A: t_p = G_p x_q with G = R^-1 L^-1 K(I, q) (2D/3D) or V^T = L^-1 K(I, q) (1D)
+        if (has_pairs)
+            for (int j = 1; j <= L; ++j) {
+                Pairs &Pp = h->pairs[(size_t)j];
+                pfac[(size_t)j].assign(Pp.box.size(), -1);
+                for (size_t p = 0; p < Pp.box.size(); ++p) {
+                    int32_t r = (int32_t)(Pp.ptr[p + 1] - Pp.ptr[p]);
+                    int32_t q = Pp.other[p];
+                    int32_t nq = (int32_t)t.cnt(j, q);
+                    if (r == 0 || nq == 0) continue;
+                    FactorJob fj{};
+                    fj.f = pb.fn;
+                    pb.fn += (int64_t)r * r;
+                    fj.ii = pb.put_idx(Pp.row.data() + Pp.ptr[p], r);
+                    fj.jj = pb.put_idx(Pp.col.data() + Pp.ptr[p], r);
+                    fj.r = r;
+                    pb.factors.push_back(fj);
+                    pfac[(size_t)j][p] = fj.f;
+                    PlanBuilder::PanelSpec ps;
+                    ps.a = pb.alloc(r, nq, ps.lda);
+                    ps.w = nq;
+                    ps.segs.push_back(leaf_gather(j, q, 0));
+                    XferJob xj{};
+                    xj.f = fj.f;
+                    xj.jj = fj.ii;  // column modes read K(I, p)
+                    xj.pi = pb.put_idx(t.perm.data() + t.off[(size_t)j][(size_t)q], nq);
+                    xj.a1 = ps.a;
+                    xj.ld1 = ps.lda;
+                    xj.a2 = -1;
+                    xj.r = r;
+                    xj.n = nq;
+                    xj.mode = dim == 1 ? X_COL_L : X_COL_LR;
+                    pb.xfers.push_back(xj);
+                    pb.max_xfer_n = std::max(pb.max_xfer_n, nq);
+                    pb.emit(to[(size_t)j] + Pp.ptr[p], r, T_ACCUM, {ps});
+                }
+            }
+        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
+    }
+
+    // ---- pair phase B matrices per box: [Ac_p1 | Ac_p2 | ...] (n_box x sum r_p)
+    struct BMat { int64_t a = -1; int32_t lda = 0, w = 0; std::vector<Seg> segs; };
+    std::vector<std::vector<BMat>> bm((size_t)L + 1);
+    if (has_pairs)
+        for (int j = 1; j <= L; ++j) {
+            bm[(size_t)j].resize((size_t)t.nbox[(size_t)j]);
+            Pairs &Pp = h->pairs[(size_t)j];
+            // pairs are grouped by box in ascending box order
+            size_t p = 0;
+            while (p < Pp.box.size()) {
+                int32_t k = Pp.box[p];
+                size_t p1 = p;
+                int64_t W = 0;
+                while (p1 < Pp.box.size() && Pp.box[p1] == k) { W += Pp.ptr[p1 + 1] - Pp.ptr[p1]; ++p1; }
+                int32_t n = (int32_t)t.cnt(j, k);
+                BMat &B = bm[(size_t)j][(size_t)k];
+                if (W > 0 && n > 0) {
+                    B.a = pb.alloc(n, W, B.lda);
+                    B.w = (int32_t)W;
+                    int64_t ri = pb.put_idx(t.perm.data() + t.off[(size_t)j][(size_t)k], n);
+                    int32_t co = 0;
+                    for (size_t q = p; q < p1; ++q) {
+                        int32_t r = (int32_t)(Pp.ptr[q + 1] - Pp.ptr[q]);
+                        if (r == 0) continue;
+                        B.segs.push_back(ws_seg(to[(size_t)j] + Pp.ptr[q], r, co));
+                        if (dim == 1) {
+                            // U = K(box, J) R^-1 with the pair's factors (1D ACA_only_nodesUV)
+                            XferJob xj{};
+                            xj.f = pfac[(size_t)j][q];
+                            xj.jj = pb.put_idx(Pp.col.data() + Pp.ptr[q], r);
+                            xj.pi = ri;
+                            xj.a1 = B.a + co;
+                            xj.ld1 = B.lda;
+                            xj.a2 = -1;
+                            xj.r = r;
+                            xj.n = n;
+                            xj.mode = X_ROW_R;
+                            if (xj.f >= 0) pb.xfers.push_back(xj);
+                            pb.max_xfer_n = std::max(pb.max_xfer_n, n);
+                        } else {
+                            FillJob fj{};
+                            fj.a = B.a + co;
+                            fj.ri = ri;
+                            fj.ci = pb.put_idx(Pp.col.data() + Pp.ptr[q], r);
+                            fj.nr = n;
+                            fj.nc = r;
+                            fj.lda = B.lda;
+                            pb.fills.push_back(fj);
+                        }
+                        co += r;
+                    }
+                }
+                p = p1;
+            }
+        }
+    // ---- DOWN phases, levels 1..L-1, then the leaf phase
+    for (int j = 1; j < L; ++j) {
+        int64_t t0 = (int64_t)pb.T.size();
+        for (int kind = 0; kind < 2; ++kind) {
+            if (kind == 0 && !(has_far && j >= 2)) continue;
+            if (kind == 1 && !has_ver) continue;
+            const Skel &s = kind == 0 ? h->far[(size_t)j] : h->ver[(size_t)j];
+            const Skel &cs = kind == 0 ? h->far[(size_t)j + 1] : h->ver[(size_t)j + 1];
+            const auto &X = kind == 0 ? fx[(size_t)j] : vx[(size_t)j];
+            const int64_t inb = kind == 0 ? fi[(size_t)j] : vi[(size_t)j];
+            const int64_t cinb = kind == 0 ? fi[(size_t)j + 1] : vi[(size_t)j + 1];
+            for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+                const Xfer &x = X[(size_t)k];
+                if (x.dn < 0) continue;
+                PlanBuilder::PanelSpec ps;
+                ps.a = x.dn;
+                ps.lda = x.ldd;
+                ps.w = x.r;
+                ps.segs.push_back(ws_seg(inb + s.ptr[(size_t)k], x.r, 0));
+                pb.emit(cinb + child_off(cs, k), x.rows, T_ACCUM, {ps});
+            }
+        }
+        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
+    }
+    {
+        int64_t t0 = (int64_t)pb.T.size();
+        for (int64_t k = 0; k < t.nbox[(size_t)L]; ++k) {
+            int32_t n = (int32_t)t.cnt(L, k);
+            if (n == 0) continue;
+            std::vector<PlanBuilder::PanelSpec> pans;
+            if (has_far && L >= 2 && fx[(size_t)L][(size_t)k].dn >= 0) {
+                const Xfer &x = fx[(size_t)L][(size_t)k];
+                PlanBuilder::PanelSpec ps;
+                ps.a = x.dn;
+                ps.lda = x.ldd;
+                ps.w = x.r;
+                ps.segs.push_back(ws_seg(fi[(size_t)L] + h->far[(size_t)L].ptr[(size_t)k], x.r, 0));
+                pans.push_back(ps);
+            }
+            if (has_ver && vx[(size_t)L][(size_t)k].dn >= 0) {
+                const Xfer &x = vx[(size_t)L][(size_t)k];
+                PlanBuilder::PanelSpec ps;
+                ps.a = x.dn;
+                ps.lda = x.ldd;
+                ps.w = x.r;
+                ps.segs.push_back(ws_seg(vi[(size_t)L] + h->ver[(size_t)L].ptr[(size_t)k], x.r, 0));
+                pans.push_back(ps);
+            }
+            if (has_pairs)
+                for (int j = 1; j <= L; ++j) {
+                    int64_t a = k >> (dim * (L - j));
+                    const BMat &B = bm[(size_t)j][(size_t)a];
+                    if (B.a < 0) continue;
+                    PlanBuilder::PanelSpec ps;
+                    ps.a = B.a + (t.off[(size_t)L][(size_t)k] - t.off[(size_t)j][(size_t)a]) * B.lda;
+                    ps.lda = B.lda;
+                    ps.w = B.w;
+                    ps.segs = B.segs;
+                    pans.push_back(ps);
+                }
+            pb.emit(h->yperm_off + t.off[(size_t)L][(size_t)k], n, T_ACCUM | T_SCATTER, pans);
+        }
+        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
+    }
+    // leaves without any far contribution would never be scattered by the
+    // fused path; fall back to an explicit scatter then.
+    {
+        int64_t covered = 0;
+        const Phase &lp = h->phases.back();
+        for (int64_t q = lp.t0; q < lp.t1; ++q)
+            if (pb.T[(size_t)q].flags & T_SCATTER) covered += pb.T[(size_t)q].nrows;
+        if (covered != t.N) h->fused_scatter = false;
+        if (!h->fused_scatter)
+            for (int64_t q = lp.t0; q < lp.t1; ++q)
+                if (pb.T[(size_t)q].flags & T_SCATTER) pb.T[(size_t)q].flags = T_ACCUM;
+    }
+    for (auto &ph : h->phases) {
+        int mx = 0;
+        for (int64_t q = ph.t0; q < ph.t1; ++q) mx = std::max(mx, pb.T[(size_t)q].xw);
+        ph.max_xw = mx;
+    }
+    for (auto &x : pb.xfers)
+        if (x.f < 0) throw ApiError(H2W_ERR_STATE, "internal: unresolved factor");
+    validate_plan(pb, h);
+
+    // ---- device buffers and assembly kernels
+    cudaStream_t st = h->stream;
+    h->op_n = pb.opn;
+    h->op_bytes_read = pb.read_elems;
+    h->d_op.alloc((size_t)pb.opn);
+    CK(cudaMemsetAsync(h->d_op.p, 0, (size_t)pb.opn * 8, st));
+    DBuf<int32_t> didx;
+    DBuf<FillJob> dfill;
+    DBuf<FactorJob> dfac;
+    DBuf<XferJob> dxf;
+    DBuf<double> dF;
+    didx.upload(pb.idx, st);
+    dfill.upload(pb.fills, st);
+    dfac.upload(pb.factors, st);
+    dxf.upload(pb.xfers, st);
+    dF.alloc((size_t)std::max<int64_t>(pb.fn, 1));
+    KParams kp = h->kparams();
+    CK(launch_factor(dfac.p, (int)pb.factors.size(), didx.p, kp, dF.p, st));
+    CK(launch_xfer(dxf.p, (int)pb.xfers.size(), pb.max_xfer_n, didx.p, kp, dF.p, h->d_op.p, st));
+    CK(launch_fill(dfill.p, (int)pb.fills.size(), didx.p, kp, h->d_op.p, st));
+    h->d_T.upload(pb.T, st);
+    h->d_P.upload(pb.P, st);
+    h->d_S.upload(pb.S, st);
+    h->d_ws.alloc((size_t)h->ws_n);
+    CK(cudaStreamSynchronize(st));
+    h->d_op32.reset();
+    h->d_ws32.reset();
+}
+
+// Stored-entry count of the reference (findMemory_n / findMemory_sn).
+double storage_entries(h2w_handle *h) {
+    const Tree &t = h->tree;
+    const int L = t.nL, dim = t.dim;
+    const bool sn = h->cfg.form == H2W_FORM_SEMINESTED;
+    double mem = 0;
+    auto nrank = [](const Skel &s, int64_t k) { return (double)s.rank(k); };
+    if (dim == 1) {
+        for (int j = 1; j <= L; ++j)
+            for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+                if (!sn) {
+                    const Skel &s = h->ver[(size_t)j];
+                    double r = nrank(s, k);
+                    if (j == L) mem += 2.0 * r * (double)t.cnt(j, k);
+                    else for (int c = 0; c < 2; ++c) mem += 2.0 * r * nrank(h->ver[(size_t)j + 1], 2 * k + c);
+                    for (int sl = 0; sl < 2; ++sl) {
+                        int32_t q = t.nb[(size_t)j][(size_t)(k * 2 + sl)];
+                        if (q != -1) mem += r * nrank(s, q);
+                    }
+                }
+            }
+        if (!sn)
+            for (int64_t k = 0; k < t.nbox[(size_t)L]; ++k) mem += (double)t.cnt(L, k) * (double)t.cnt(L, k);
+        else
+            for (int j = 1; j <= L; ++j) {
+                const Pairs &P = h->pairs[(size_t)j];
+                for (size_t p = 0; p < P.box.size(); ++p) {
+                    double r = (double)(P.ptr[p + 1] - P.ptr[p]);
+                    mem += r * ((double)t.cnt(j, P.box[p]) + (double)t.cnt(j, P.other[p]));
+                }
+            }
+        return mem;
+    }
+    for (int j = 2; j <= L; ++j)
+        for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+            const Skel &s = h->far[(size_t)j];
+            double r = nrank(s, k);
+            if (r > 0) mem += 2.0 * r * (double)far_rows(h, j, k).size();
+            for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e)
+                if (!t.ilv[(size_t)j][(size_t)e]) mem += r * nrank(s, t.il[(size_t)j][(size_t)e]);
+        }
+    if (!sn) {
+        for (int j = 1; j <= L; ++j)
+            for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+                const Skel &s = h->ver[(size_t)j];
+                double r = nrank(s, k);
+                if (j == L) mem += 2.0 * r * (double)t.cnt(j, k);
+                else for (int c = 0; c < t.nch; ++c) mem += 2.0 * r * nrank(h->ver[(size_t)j + 1], k * t.nch + c);
+                for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e)
+                    if (t.ilv[(size_t)j][(size_t)e]) mem += r * nrank(s, t.il[(size_t)j][(size_t)e]);
+            }
+    } else {
+        for (int j = 1; j <= L; ++j) {
+            const Pairs &P = h->pairs[(size_t)j];
+            for (size_t p = 0; p < P.box.size(); ++p) {
+                double r = (double)(P.ptr[p + 1] - P.ptr[p]);
+                if (r == 0) continue;
+                mem += 2.0 * r * r + r * (double)t.cnt(j, P.box[p]) + r * (double)t.cnt(j, P.other[p]);
+            }
+        }
+    }
+    for (int64_t k = 0; k < t.nbox[(size_t)L]; ++k) {
+        double n = (double)t.cnt(L, k);
+        mem += n * n;
+        for (int sl = 0; sl < t.nnb; ++sl) {
+            int32_t q = t.nb[(size_t)L][(size_t)(k * t.nnb + sl)];
+            if (q != -1) mem += n * (double)t.cnt(L, q);
+        }
+    }
+    return mem;
+}
+
+// ---------------------------------------------------------- matvec run ---
+void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st) {
+    CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
+    for (const Phase &ph : h->phases)
+        CK(launch_brg_f64(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op.p, h->d_ws.p, dx, dy,
+                          h->d_perm.p, st));
+    if (!h->fused_scatter) CK(launch_scatter_f64(h->d_ws.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
+}
+
+void ensure_f32(h2w_handle *h) {
+    if (h->d_op32.p) return;
+    h->d_op32.alloc((size_t)h->op_n);
+    CK(launch_convert_f32(h->d_op.p, h->d_op32.p, h->op_n, h->stream));
+    h->d_ws32.alloc((size_t)h->ws_n);
+    h->d_x32.alloc((size_t)h->tree.N);
+    h->d_y32.alloc((size_t)h->tree.N);
+    CK(cudaStreamSynchronize(h->stream));
+}
+
+void run_matvec_f32(h2w_handle *h, const float *dx, float *dy, cudaStream_t st) {
+    CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
+    for (const Phase &ph : h->phases)
+        CK(launch_brg_f32(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op32.p, h->d_ws32.p, dx, dy,
+                          h->d_perm.p, st));
+    if (!h->fused_scatter) CK(launch_scatter_f32(h->d_ws32.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
+}
+
+// --------------------------------------------------------------- GMRES ---
+GmresDev gmres_state(h2w_handle *h, int m) {
+    const int64_t N = h->tree.N;
+    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(2 * 152, (N + 1023) / 1024));
+    if (h->g_m != m) {
+        h->g_V.alloc((size_t)N * (size_t)(m + 1));
+        h->g_w.alloc((size_t)N);
+        h->g_vcur.alloc((size_t)N);
+        h->g_H.alloc((size_t)(m + 1) * (size_t)m);
+        h->g_cs.alloc((size_t)m + 1);
+        h->g_sn.alloc((size_t)m + 1);
+        h->g_s.alloc((size_t)m + 1);
+        h->g_part.alloc((size_t)3 * nblk * (size_t)(m + 1));
+        h->g_scal.alloc(8);
+        h->g_iter.alloc(1);
+        h->g_tmp.alloc((size_t)N);
+        h->g_r.alloc((size_t)N);
+        h->g_m = m;
+    }
+    GmresDev g;
+    g.V = h->g_V.p;
+    g.w = h->g_w.p;
+    g.vcur = h->g_vcur.p;
+    g.H = h->g_H.p;
+    g.cs = h->g_cs.p;
+    g.sn = h->g_sn.p;
+    g.s = h->g_s.p;
+    g.part = h->g_part.p;
+    g.scal = h->g_scal.p;
+    g.iter = h->g_iter.p;
+    g.N = N;
+    g.m = m;
+    g.nblk = nblk;
+    return g;
+}
+
+double dnorm(h2w_handle *h, const double *x) {
+    if (!h->g_npart.p) h->g_npart.alloc(256);
+    if (!h->g_scal.p) h->g_scal.alloc(8);
+    CK(vec_norm(x, h->tree.N, h->g_npart.p, 256, h->g_scal.p + 4, h->stream));
+    double v;
+    CK(cudaMemcpyAsync(&v, h->g_scal.p + 4, 8, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return v;
+}
+
+// Solve the upper-triangular least-squares system H(0:k,0:k) y = s(0:k) on
+// the host, as Update does (*/codes/gmres.hpp:77-90), then x += V y.
+void gmres_xupdate(h2w_handle *h, const GmresDev &g, double *dx, int k) {
+    const int m = g.m;
+    std::vector<double> H((size_t)(m + 1) * (size_t)(k + 1)), s((size_t)k + 1);
+    CK(cudaMemcpyAsync(H.data(), g.H, H.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(s.data(), g.s, s.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    auto Hc = [&](int r, int c) { return H[(size_t)r + (size_t)c * (size_t)(m + 1)]; };
+    std::vector<double> y = s;
+    for (int i = k; i >= 0; --i) {
+        y[(size_t)i] /= Hc(i, i);
+        for (int j = i - 1; j >= 0; --j) y[(size_t)j] -= Hc(j, i) * y[(size_t)i];
+    }
+    CK(cudaMemcpyAsync(h->g_tmp.p, y.data(), y.size() * 8, cudaMemcpyHostToDevice, h->stream));
+    CK(gmres_update(g, dx, h->g_tmp.p, k, h->stream));
+}
+
+// FP64 GMRES on device vectors; matvec precision chosen by prec.
+int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double tol, int prec, int *iters,
+              double *resid) {
+    GmresDev g = gmres_state(h, max_iter);
+    cudaStream_t st = h->stream;
+    const int64_t N = h->tree.N;
+    auto A = [&](const double *in, double *out) {
+        if (prec == H2W_PREC_FP32) {
+            ensure_f32(h);
+            CK(vec_f64_to_f32(in, h->d_x32.p, N, st));
+            run_matvec_f32(h, h->d_x32.p, h->d_y32.p, st);
+            CK(vec_f32_to_f64(h->d_y32.p, out, N, st));
+        } else {
+            run_matvec_f64(h, in, out, st);
+        }
+    };
+    double normb = dnorm(h, db);
+    if (normb == 0.0) normb = 1;
+    A(dx, h->g_r.p);
+    CK(gmres_start(g, db, h->g_r.p, normb, st));
+    double sc[4];
+    CK(cudaMemcpyAsync(sc, g.scal, 32, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *resid = sc[1];
+    if (sc[1] <= tol) {
+        *iters = 0;
+        return H2W_OK;
+    }
+    for (int i = 0; i < max_iter; ++i) {
+        A(g.vcur, g.w);
+        CK(gmres_cgs2(g, st));
+        CK(gmres_finish_iter(g, tol, st));
+        CK(cudaMemcpyAsync(sc, g.scal, 32, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        *resid = sc[1];
+        if (sc[2] != 0.0) {
+            gmres_xupdate(h, g, dx, i);
+            CK(cudaStreamSynchronize(st));
+            *iters = i + 1;
+            return H2W_OK;
+        }
+    }
+    gmres_xupdate(h, g, dx, max_iter - 1);
+    A(dx, h->g_r.p);
+    CK(vec_axpby(1.0, db, -1.0, h->g_r.p, h->g_r.p, N, st));
+    *resid = dnorm(h, h->g_r.p) / normb;
+    *iters = max_iter;
+    return *resid < tol ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+}
+
+int fail(h2w_handle *h, int code, const std::string &m) {
+    if (h) h->err = m;
+    return code;
+}
+
+template <class F>
+int guarded(h2w_handle *h, F &&f) {
+    if (!h) return H2W_ERR_ARG;
+    try {
+        if (h->cfg.device >= 0 && cudaSetDevice(h->cfg.device) != cudaSuccess)
+            return fail(h, H2W_ERR_CUDA, "cudaSetDevice failed");
+        return f();
+    } catch (const ApiError &e) {
+        return fail(h, e.code, e.what());
+    } catch (const CudaError &e) {
+        return fail(h, H2W_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(h, H2W_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(h, H2W_ERR_ARG, e.what());
+    }
+}
+
+void require_points(h2w_handle *h) {
+    if (h->pts.empty()) throw ApiError(H2W_ERR_STATE, "no points set");
+}
+void require_tree(h2w_handle *h) {
+    if (!h->has_tree) throw ApiError(H2W_ERR_STATE, "tree not built (call h2w_build_tree)");
+}
+void require_op(h2w_handle *h) {
+    if (!h->has_op) throw ApiError(H2W_ERR_STATE, "operator not assembled (call h2w_assemble)");
+}
+
+}  // namespace
+
+// ================================================================ C ABI ===
+extern "C" {
+
+int h2w_create(const h2w_config *cfg, h2w_handle **out) {
+    if (!cfg || !out) return H2W_ERR_ARG;
+    *out = nullptr;
+    if (cfg->dim < 1 || cfg->dim > 3 || (cfg->form != 0 && cfg->form != 1) || (cfg->choice != 0 && cfg->choice != 1) ||
+        cfg->nlevels < 1 || cfg->tol_pow < 0 || cfg->rank_cap < 0)
+        return H2W_ERR_ARG;
+    h2w_handle *h = nullptr;
+    if (cfg->device >= 0) {
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return H2W_ERR_CUDA;
+        if (cfg->device >= ndev) return H2W_ERR_ARG;
+        h = new h2w_handle;
+        h->cfg = *cfg;
+        if (cudaSetDevice(cfg->device) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete h;
+            return H2W_ERR_CUDA;
+        }
+    } else {
+        // host-only handle: points, tree and lists, no device work
+        h = new h2w_handle;
+        h->cfg = *cfg;
+    }
+    *out = h;
+    return H2W_OK;
+}
+
+int h2w_destroy(h2w_handle *h) {
+    if (!h) return H2W_OK;
+    if (h->cfg.device >= 0) cudaSetDevice(h->cfg.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaStream_t st = h->stream;
+    delete h;
+    if (st) cudaStreamDestroy(st);
+    return H2W_OK;
+}
+
+const char *h2w_last_error(const h2w_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+int h2w_set_points(h2w_handle *h, const double *pts, int64_t n) {
+    return guarded(h, [&] {
+        if (!pts || n < 1 || n > INT32_MAX - 1) throw ApiError(H2W_ERR_ARG, "bad point array");
+        h->pts.assign(pts, pts + (size_t)n * h->cfg.dim);
+        for (double v : h->pts)
+            if (!std::isfinite(v)) throw ApiError(H2W_ERR_ARG, "non-finite point coordinate");
+        h->has_tree = h->has_op = false;
+        return H2W_OK;
+    });
+}
+
+int h2w_gen_grid(h2w_handle *h, int64_t n) {
+    return guarded(h, [&] {
+        const int d = h->cfg.dim;
+        if (n < 1) throw ApiError(H2W_ERR_ARG, "bad grid size");
+        int64_t N = d == 1 ? n : (d == 2 ? n * n : n * n * n);
+        if (N > INT32_MAX - 1) throw ApiError(H2W_ERR_ARG, "grid too large");
+        std::vector<double> node((size_t)n);
+        const double L = 1.0;
+        for (int64_t k = 0; k < n; ++k) node[(size_t)k] = -L + 2.0 * L * (k + 1.0) / (n + 1.0);
+        h->pts.resize((size_t)N * d);
+        if (d == 1) {
+            for (int64_t k = 0; k < n; ++k) h->pts[(size_t)k] = -1.0 + 2.0 * (k + 1.0) / (n + 1.0);
+        } else if (d == 2) {
+            for (int64_t j = 0; j < n; ++j)
+                for (int64_t k = 0; k < n; ++k) {
+                    size_t i = (size_t)(j * n + k);
+                    h->pts[2 * i] = node[(size_t)k];
+                    h->pts[2 * i + 1] = node[(size_t)j];
+                }
+        } else {
+            for (int64_t j = 0; j < n; ++j)
+                for (int64_t k = 0; k < n; ++k)
+                    for (int64_t i = 0; i < n; ++i) {
+                        size_t q = (size_t)((j * n + k) * n + i);
+                        h->pts[3 * q] = node[(size_t)k];
+                        h->pts[3 * q + 1] = node[(size_t)j];
+                        h->pts[3 * q + 2] = node[(size_t)i];
+                    }
+        }
+        h->has_tree = h->has_op = false;
+        return H2W_OK;
+    });
+}
+
+int h2w_gen_uniform(h2w_handle *h, uint64_t seed, int64_t n) {
+    return guarded(h, [&] {
+        const int d = h->cfg.dim;
+        if (n < 1 || n > INT32_MAX - 1) throw ApiError(H2W_ERR_ARG, "bad point count");
+        h->pts.resize((size_t)n * d);
+        for (int64_t i = 0; i < n * d; ++i) {
+            uint64_t z = seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            z = z ^ (z >> 31);
+            double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+            h->pts[(size_t)i] = 2.0 * u - 1.0;
+        }
+        h->has_tree = h->has_op = false;
+        return H2W_OK;
+    });
+}
+
+int h2w_get_points(h2w_handle *h, double *pts) {
+    return guarded(h, [&] {
+        require_points(h);
+        if (!pts) throw ApiError(H2W_ERR_ARG, "null output");
+        std::memcpy(pts, h->pts.data(), h->pts.size() * 8);
+        return H2W_OK;
+    });
+}
+
+int h2w_num_points(h2w_handle *h, int64_t *n) {
+    return guarded(h, [&] {
+        if (!n) throw ApiError(H2W_ERR_ARG, "null output");
+        *n = (int64_t)(h->pts.size() / (size_t)h->cfg.dim);
+        return H2W_OK;
+    });
+}
+
+int h2w_build_tree(h2w_handle *h) {
+    return guarded(h, [&] {
+        require_points(h);
+        h->tree = Tree{};
+        h->tree.dim = h->cfg.dim;
+        h->tree.nL = h->cfg.nlevels;
+        h->tree.N = (int64_t)(h->pts.size() / (size_t)h->cfg.dim);
+        h->tree.pts = h->pts;
+        build_tree(h->tree);
+        h->has_tree = true;
+        h->has_op = false;
+        if (h->cfg.device >= 0) {
+            h->d_pts.upload(h->pts, h->stream);
+            h->d_perm.upload(h->tree.perm, h->stream);
+            CK(cudaStreamSynchronize(h->stream));
+        }
+        setup_kernel(h);
+        for (int w = 0; w < 10; ++w) h->imp[w] = false;
+        h->imp_ptr.assign(10, {});
+        h->imp_val.assign(10, {});
+        return H2W_OK;
+    });
+}
+
+int h2w_get_list(h2w_handle *h, int which, int64_t *ptr, int32_t *val, int64_t *nptr, int64_t *nval) {
+    return guarded(h, [&] {
+        require_tree(h);
+        const Tree &t = h->tree;
+        std::vector<int64_t> P{0};
+        std::vector<int32_t> V;
+        auto add = [&](const int32_t *v, int64_t n) {
+            V.insert(V.end(), v, v + n);
+            P.push_back((int64_t)V.size());
+        };
+        const bool op = h->has_op;
+        for (int j = 0; j <= t.nL; ++j)
+            for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+                switch (which) {
+                case H2W_LIST_CHARGE:
+                    if (j == 0) {
+                        std::vector<int32_t> a((size_t)t.N);
+                        for (int64_t i = 0; i < t.N; ++i) a[(size_t)i] = (int32_t)i;
+                        add(a.data(), t.N);
+                    } else add(t.perm.data() + t.off[(size_t)j][(size_t)k], t.cnt(j, k));
+                    break;
+                case H2W_LIST_NBR: add(t.nb[(size_t)j].data() + k * t.nnb, t.nnb); break;
+                case H2W_LIST_IL:
+                case H2W_LIST_ISVERTEX: {
+                    int64_t a = t.ilp[(size_t)j][(size_t)k], b = t.ilp[(size_t)j][(size_t)k + 1];
+                    if (j == 0) { add(nullptr, 0); break; }
+                    if (which == H2W_LIST_IL) add(t.il[(size_t)j].data() + a, b - a);
+                    else {
+                        std::vector<int32_t> f;
+                        for (int64_t e = a; e < b; ++e) f.push_back(t.ilv[(size_t)j][(size_t)e]);
+                        add(f.data(), (int64_t)f.size());
+                    }
+                    break;
+                }
+                case H2W_LIST_FAR_CHECK:
+                case H2W_LIST_FAR_CHARGE:
+                case H2W_LIST_VER_CHECK:
+                case H2W_LIST_VER_CHARGE: {
+                    const bool farl = which == H2W_LIST_FAR_CHECK || which == H2W_LIST_FAR_CHARGE;
+                    const bool chk = which == H2W_LIST_FAR_CHECK || which == H2W_LIST_VER_CHECK;
+                    const std::vector<Skel> *S = nullptr;
+                    if (op) {
+                        if (t.dim == 1) S = farl && h->cfg.form == 0 ? &h->ver : nullptr;
+                        else S = farl ? &h->far : (h->cfg.form == 0 ? &h->ver : nullptr);
+                    }
+                    if (!S || S->empty() || (*S)[(size_t)j].ptr.empty()) { add(nullptr, 0); break; }
+                    const Skel &s = (*S)[(size_t)j];
+                    add((chk ? s.chk.data() : s.chg.data()) + s.ptr[(size_t)k], s.rank(k));
+                    break;
+                }
+                case H2W_LIST_SN_ROW:
+                case H2W_LIST_SN_COL: {
+                    int nslot = t.dim == 1 ? (j >= 1 ? 2 : 0)
+                                           : (int)(t.ilp[(size_t)j][(size_t)k + 1] - t.ilp[(size_t)j][(size_t)k]);
+                    if (t.dim == 1 && j == 0) break;
+                    for (int sl = 0; sl < nslot; ++sl) {
+                        bool done = false;
+                        if (op && h->cfg.form == 1 && j >= 1) {
+                            const Pairs &Pp = h->pairs[(size_t)j];
+                            for (size_t p = 0; p < Pp.box.size(); ++p)
+                                if (Pp.box[p] == k && Pp.slot[p] == sl) {
+                                    const auto &src = which == H2W_LIST_SN_ROW ? Pp.row : Pp.col;
+                                    add(src.data() + Pp.ptr[p], Pp.ptr[p + 1] - Pp.ptr[p]);
+                                    done = true;
+                                    break;
+                                }
+                        }
+                        if (!done) add(nullptr, 0);
+                    }
+                    break;
+                }
+                default: throw ApiError(H2W_ERR_ARG, "unknown list");
+                }
+            }
+        if (nptr) *nptr = (int64_t)P.size();
+        if (nval) *nval = (int64_t)V.size();
+        if (ptr) std::memcpy(ptr, P.data(), P.size() * 8);
+        if (val && !V.empty()) std::memcpy(val, V.data(), V.size() * 4);
+        return H2W_OK;
+    });
+}
+
+int h2w_import_list(h2w_handle *h, int which, const int64_t *ptr, const int32_t *val, int64_t nptr) {
+    return guarded(h, [&] {
+        require_tree(h);
+        if (which < H2W_LIST_FAR_CHECK || which > H2W_LIST_SN_COL || !ptr || nptr < 1)
+            throw ApiError(H2W_ERR_ARG, "bad import");
+        h->imp_ptr[(size_t)which].assign(ptr, ptr + nptr);
+        int64_t nv = ptr[nptr - 1];
+        h->imp_val[(size_t)which].assign(val, val + nv);
+        for (int32_t v : h->imp_val[(size_t)which])
+            if (v < 0 || v >= h->tree.N) throw ApiError(H2W_ERR_ARG, "imported pivot out of range");
+        h->imp[which] = true;
+        return H2W_OK;
+    });
+}
+
+int h2w_assemble(h2w_handle *h, int mode) {
+    return guarded(h, [&] {
+        require_tree(h);
+        if (h->cfg.device < 0) throw ApiError(H2W_ERR_STATE, "host-only handle (device < 0) cannot assemble");
+        const Tree &t = h->tree;
+        const bool sn = h->cfg.form == H2W_FORM_SEMINESTED;
+        h->phases.clear();
+        h->has_op = false;
+        if (mode == H2W_ASSEMBLE_NCA || mode == H2W_ASSEMBLE_LEARNED) {
+            if (t.dim > 1) nca_far(h);
+            if (!sn) nca_ver(h);
+            if (sn) {
+                pair_layout(h);
+                nca_pairs(h);
+            }
+        } else if (mode == H2W_ASSEMBLE_IMPORT) {
+            if (t.dim > 1) {
+                if (!h->imp[H2W_LIST_FAR_CHECK] || !h->imp[H2W_LIST_FAR_CHARGE])
+                    throw ApiError(H2W_ERR_STATE, "far pivots not imported");
+                import_skel(h, H2W_LIST_FAR_CHECK, H2W_LIST_FAR_CHARGE, h->far, 2);
+                if (!sn) {
+                    if (!h->imp[H2W_LIST_VER_CHECK] || !h->imp[H2W_LIST_VER_CHARGE])
+                        throw ApiError(H2W_ERR_STATE, "vertex pivots not imported");
+                    import_skel(h, H2W_LIST_VER_CHECK, H2W_LIST_VER_CHARGE, h->ver, 1);
+                }
+            } else if (!sn) {
+                if (!h->imp[H2W_LIST_FAR_CHECK] || !h->imp[H2W_LIST_FAR_CHARGE])
+                    throw ApiError(H2W_ERR_STATE, "nested-basis pivots not imported");
+                import_skel(h, H2W_LIST_FAR_CHECK, H2W_LIST_FAR_CHARGE, h->ver, 1);
+            }
+            if (sn) {
+                if (!h->imp[H2W_LIST_SN_ROW] || !h->imp[H2W_LIST_SN_COL])
+                    throw ApiError(H2W_ERR_STATE, "pair pivots not imported");
+                pair_layout(h);
+                import_pairs(h);
+            }
+        } else {
+            throw ApiError(H2W_ERR_ARG, "unknown assembly mode");
+        }
+        if (t.dim == 1 || sn) {
+            if (h->far.empty()) {
+                h->far.assign((size_t)t.nL + 1, Skel{});
+                for (int j = 0; j <= t.nL; ++j) h->far[(size_t)j].ptr.assign((size_t)t.nbox[(size_t)j] + 1, 0);
+            }
+        }
+        if (sn && h->ver.empty()) {
+            h->ver.assign((size_t)t.nL + 1, Skel{});
+            for (int j = 0; j <= t.nL; ++j) h->ver[(size_t)j].ptr.assign((size_t)t.nbox[(size_t)j] + 1, 0);
+        }
+        if (!sn && h->pairs.empty()) h->pairs.assign((size_t)t.nL + 1, Pairs{});
+        build_plan(h);
+        h->storage = storage_entries(h);
+        h->has_op = true;
+        h->g_m = -1;
+        return H2W_OK;
+    });
+}
+
+int h2w_storage_entries(h2w_handle *h, double *e) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!e) throw ApiError(H2W_ERR_ARG, "null output");
+        *e = h->storage;
+        return H2W_OK;
+    });
+}
+
+int h2w_operator_bytes(h2w_handle *h, int precision, int64_t *bytes) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!bytes) throw ApiError(H2W_ERR_ARG, "null output");
+        *bytes = h->op_bytes_read * (precision == H2W_PREC_FP32 ? 4 : 8);
+        return H2W_OK;
+    });
+}
+
+int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precision, int where, void *stream) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!x || !y || nrhs < 1 || (where != H2W_HOST && where != H2W_DEVICE)) throw ApiError(H2W_ERR_ARG, "bad matvec arguments");
+        cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+        const int64_t N = h->tree.N;
+        if (where == H2W_HOST) {
+            h->d_x.n < (size_t)N ? h->d_x.alloc((size_t)N) : (void)0;
+            h->d_y.n < (size_t)N ? h->d_y.alloc((size_t)N) : (void)0;
+        }
+        for (int c = 0; c < nrhs; ++c) {
+            const double *xc = x + (size_t)c * N;
+            double *yc = y + (size_t)c * N;
+            const double *dx = xc;
+            double *dy = yc;
+            if (where == H2W_HOST) {
+                CK(cudaMemcpyAsync(h->d_x.p, xc, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+                dx = h->d_x.p;
+                dy = h->d_y.p;
+            }
+            if (precision == H2W_PREC_FP32) {
+                ensure_f32(h);
+                CK(vec_f64_to_f32(dx, h->d_x32.p, N, st));
+                run_matvec_f32(h, h->d_x32.p, h->d_y32.p, st);
+                CK(vec_f32_to_f64(h->d_y32.p, dy, N, st));
+            } else {
+                run_matvec_f64(h, dx, dy, st);
+            }
+            if (where == H2W_HOST) CK(cudaMemcpyAsync(yc, h->d_y.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
+        }
+        if (where == H2W_HOST) CK(cudaStreamSynchronize(st));
+        return H2W_OK;
+    });
+}
+
+int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_pow, int where, int *iters,
+              double *resid) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!b || !x || max_iter < 1 || !iters || !resid) throw ApiError(H2W_ERR_ARG, "bad gmres arguments");
+        const int64_t N = h->tree.N;
+        double tol = std::pow(10, -1.0 * tol_pow);
+        const double *db = b;
+        double *dx = x;
+        if (where == H2W_HOST) {
+            h->g_b.n < (size_t)N ? h->g_b.alloc((size_t)N) : (void)0;
+            h->d_x.n < (size_t)N ? h->d_x.alloc((size_t)N) : (void)0;
+            CK(cudaMemcpyAsync(h->g_b.p, b, (size_t)N * 8, cudaMemcpyHostToDevice, h->stream));
+            CK(cudaMemcpyAsync(h->d_x.p, x, (size_t)N * 8, cudaMemcpyHostToDevice, h->stream));
+            db = h->g_b.p;
+            dx = h->d_x.p;
+        }
+        int rc = gmres_run(h, db, dx, max_iter, tol, H2W_PREC_FP64, iters, resid);
+        if (where == H2W_HOST) {
+            CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        }
+        return rc;
+    });
+}
+
+int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int inner_iter, int tol_pow, int where,
+                 int *outer_iters, int *inner_total, double *resid) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!b || !x || max_outer < 1 || inner_iter < 1 || !outer_iters || !inner_total || !resid)
+            throw ApiError(H2W_ERR_ARG, "bad gmres_ir arguments");
+        const int64_t N = h->tree.N;
+        cudaStream_t st = h->stream;
+        double tol = std::pow(10, -1.0 * tol_pow);
+        const double *db = b;
+        double *dx = x;
+        if (where == H2W_HOST) {
+            h->g_b.n < (size_t)N ? h->g_b.alloc((size_t)N) : (void)0;
+            h->d_x.n < (size_t)N ? h->d_x.alloc((size_t)N) : (void)0;
+            CK(cudaMemcpyAsync(h->g_b.p, b, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(h->d_x.p, x, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+            db = h->g_b.p;
+            dx = h->d_x.p;
+        }
+        GmresDev g = gmres_state(h, inner_iter);
+        (void)g;
+        DBuf<double> r, d;
+        r.alloc((size_t)N);
+        d.alloc((size_t)N);
+        double normb = dnorm(h, db);
+        if (normb == 0.0) normb = 1;
+        *inner_total = 0;
+        *outer_iters = 0;
+        int rc = H2W_ERR_NOT_CONVERGED;
+        for (int o = 0; o <= max_outer; ++o) {
+            run_matvec_f64(h, dx, r.p, st);
+            CK(vec_axpby(1.0, db, -1.0, r.p, r.p, N, st));
+            *resid = dnorm(h, r.p) / normb;
+            if (*resid < tol) { rc = H2W_OK; break; }
+            if (o == max_outer) break;
+            CK(cudaMemsetAsync(d.p, 0, (size_t)N * 8, st));
+            int it = 0;
+            double ires = 0;
+            // inner: relative reduction 1e-6 of the current residual, FP32 operator
+            gmres_run(h, r.p, d.p, inner_iter, 1e-6, H2W_PREC_FP32, &it, &ires);
+            *inner_total += it;
+            CK(vec_axpby(1.0, dx, 1.0, d.p, dx, N, st));
+            *outer_iters = o + 1;
+        }
+        if (where == H2W_HOST) {
+            CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
+        }
+        CK(cudaStreamSynchronize(st));
+        return rc;
+    });
+}
+
+int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, int64_t nrows, int where) {
+    return guarded(h, [&] {
+        require_tree(h);
+        const int64_t N = h->tree.N;
+        if (!x || !y || row0 < 0 || nrows < 0 || row0 + nrows > N) throw ApiError(H2W_ERR_ARG, "bad dense arguments");
+        cudaStream_t st = h->stream;
+        const double *dx = x;
+        double *dy = y;
+        DBuf<double> bx, by;
+        if (where == H2W_HOST) {
+            bx.alloc((size_t)N);
+            by.alloc((size_t)std::max<int64_t>(nrows, 1));
+            CK(cudaMemcpyAsync(bx.p, x, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+            dx = bx.p;
+            dy = by.p;
+        }
+        CK(launch_dense_matvec(h->kparams(), N, dx, dy, row0, nrows, st));
+        if (where == H2W_HOST) CK(cudaMemcpyAsync(y, by.p, (size_t)nrows * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return H2W_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,853 @@
+// sm_103a kernels of the GB300 H2* / (H2+H)* library.
+//
+//  * kentry            kernel-matrix entries, operation order and rounding of
+//                      the reference's getMatrixEntry (no FMA contraction)
+//  * nca_kernel        batched NCA/ACA pivot search, one CTA per block
+//                      (1D/codes/aca.hpp:296-446 pivoting and stopping rule)
+//  * factor_kernel     LU of K(I,J) in pivot order = the ACA's L and R
+//  * xfer_kernel       rows K(p,J) R^-1 L^-1 (transfer matrices), columns
+//                      R^-1 L^-1 K(I,p), and the 1D U / V^T factors
+//  * fill_kernel       dense blocks K(I,J) straight into the packed operator
+//  * brg_kernel        the matvec: block-row GEMV over a work list of targets,
+//                      each the sum of row-major panels times gathered sources
+//  * GMRES kernels     CGS2 Arnoldi step, normalisation, Givens rotations
+#include <cfloat>
+#include <climits>
+
+#include "kernels.cuh"
+
+namespace h2w {
+
+// ------------------------------------------------------------ entries ---
+__device__ __forceinline__ double kentry(const KParams &k, int i, int j) {
+    if (i == j) return k.diag;
+    const double *a = k.pts + (size_t)i * k.dim;
+    const double *b = k.pts + (size_t)j * k.dim;
+    if (k.dim == 1) {
+        double R = fabs(__dsub_rn(a[0], b[0]));
+        if (k.choice == 0) return log(R);
+        const double aa = 0.0001;
+        return R < aa ? __ddiv_rn(R, aa) : __ddiv_rn(aa, R);
+    }
+    double dx = __dsub_rn(a[0], b[0]), dy = __dsub_rn(a[1], b[1]);
+    if (k.dim == 2) {
+        double R2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        if (k.choice == 0) return __dmul_rn(k.c2d, log(R2));
+        double R = __dsqrt_rn(R2);
+        const double aa = 0.0001;
+        return R < aa ? __ddiv_rn(R, aa) : __ddiv_rn(aa, R);
+    }
+    double dz = __dsub_rn(a[2], b[2]);
+    double R2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    double R = __dsqrt_rn(R2);
+    if (k.choice == 0) return __ddiv_rn(1.0, __dmul_rn(k.four_pi, R));
+    const double aa = 0.0001;
+    if (R < aa) return __ddiv_rn(__dsub_rn(__dmul_rn(R, log(R)), 1.0), k.den_small);
+    return __ddiv_rn(log(R), k.loga);
+}
+
+// ---------------------------------------------------------- reductions ---
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ bool amax_better(double va, int ia, double vb, int ib) {
+    return va > vb || (va == vb && ia < ib);
+}
+__device__ __forceinline__ void warp_amax(double &v, int &i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_xor_sync(0xffffffffu, v, o);
+        int oi = __shfl_xor_sync(0xffffffffu, i, o);
+        if (amax_better(ov, oi, v, i)) { v = ov; i = oi; }
+    }
+}
+// Block-wide sum; every thread gets the total. sh: >= 32 doubles.
+__device__ double block_sum(double v, double *sh) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int q = 0; q < nw; ++q) t += sh[q];
+    return t;
+}
+// Block-wide argmax of (value, lowest index); every thread gets the result.
+__device__ void block_amax(double &v, int &i, double *shv, int *shi) {
+    warp_amax(v, i);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) { shv[w] = v; shi[w] = i; }
+    __syncthreads();
+    v = shv[0];
+    i = shi[0];
+    for (int q = 1; q < nw; ++q)
+        if (amax_better(shv[q], shi[q], v, i)) { v = shv[q]; i = shi[q]; }
+}
+
+__device__ __forceinline__ bool bit_get(const uint32_t *m, int i) { return (m[i >> 5] >> (i & 31)) & 1u; }
+
+// ----------------------------------------------------------------- NCA ---
+// One CTA per block (I, J). Pivoting and stopping follow ACA_only_nodes:
+// first row with a non-negligible entry, column pivot = first largest |.|
+// among unused columns of the residual row, row pivot = first largest |.|
+// among unused rows of the residual column, stop when ||u|| ||v|| <= tol
+// normS or the rank reaches min(n1, n2). Residual rows and columns are
+// formed entry by entry in pivot order with separate multiply and subtract,
+// so for identical entries they are bitwise those of the reference; norms
+// and dot products are tree reductions (they only enter the stopping test).
+constexpr int NCA_THREADS = 256;
+constexpr int GM_THREADS = 256;
+
+__global__ void __launch_bounds__(NCA_THREADS) nca_kernel(const NcaProb *__restrict__ probs,
+                                                          const int32_t *__restrict__ idx, KParams kp, double tol,
+                                                          double *__restrict__ scr, int32_t *__restrict__ rank_out,
+                                                          int32_t *__restrict__ prow, int32_t *__restrict__ pcol,
+                                                          int32_t *status, int mask1_words, int mask2_words,
+                                                          int coef_len) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t *rmask = reinterpret_cast<uint32_t *>(smem);
+    uint32_t *cmask = rmask + mask1_words;
+    double *coef = reinterpret_cast<double *>(cmask + mask2_words + ((mask1_words + mask2_words) & 1));
+    double *red = coef + coef_len;                       // coef_len * 8 (per-warp partial dots)
+    __shared__ double shv[32];
+    __shared__ int shi[32];
+    __shared__ double shs[32];
+
+    const NcaProb pb = probs[blockIdx.x];
+    const int n1 = pb.n1, n2 = pb.n2, rcap = pb.rcap;
+    const int32_t *I = idx + pb.ri;
+    const int32_t *J = idx + pb.ci;
+    double *U = scr + pb.u;
+    double *V = scr + pb.v;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+
+    for (int q = tid; q < mask1_words; q += nt) rmask[q] = 0u;
+    for (int q = tid; q < mask2_words; q += nt) cmask[q] = 0u;
+    __syncthreads();
+    if (tid == 0) rank_out[blockIdx.x] = 0;
+    const int mn = n1 < n2 ? n1 : n2;
+    if (mn == 0 || rcap == 0) return;
+
+    // first pivot row: first row whose largest |entry| exceeds 1e-36
+    const double tiny = 1e-36;
+    int ri = -1, ci = -1;
+    for (int l = 0; l < n1; ++l) {
+        double bv = -1.0;
+        int bi = INT_MAX;
+        const int gi = I[l];
+        for (int s = tid; s < n2; s += nt) {
+            double v = kentry(kp, gi, J[s]);
+            V[s] = v;
+            double a = fabs(v);
+            if (amax_better(a, s, bv, bi)) { bv = a; bi = s; }
+        }
+        block_amax(bv, bi, shv, shi);
+        if (bv > tiny) { ri = l; ci = bi; break; }
+    }
+    if (ri < 0) return;
+    __syncthreads();
+    double piv = V[ci];
+    double usq = 0.0, vsq = 0.0;
+    int nri = INT_MAX;
+    {
+        double bv = -1.0;
+        int bi = INT_MAX;
+        const int gj = J[ci];
+        for (int t = tid; t < n1; t += nt) {
+            double c = kentry(kp, I[t], gj);
+            double u = __ddiv_rn(c, piv);
+            U[t] = u;
+            usq += u * u;
+            if (t != ri) {
+                double a = fabs(c);
+                if (amax_better(a, t, bv, bi)) { bv = a; bi = t; }
+            }
+        }
+        for (int s = tid; s < n2; s += nt) vsq += V[s] * V[s];
+        block_amax(bv, bi, shv, shi);
+        nri = bi;
+    }
+    double nu = sqrt(block_sum(usq, shs));
+    double nv = sqrt(block_sum(vsq, shs));
+    if (tid == 0) {
+        prow[pb.piv] = ri;
+        pcol[pb.piv] = ci;
+        rmask[ri >> 5] |= 1u << (ri & 31);
+        cmask[ci >> 5] |= 1u << (ci & 31);
+    }
+    int rank = 1;
+    double normS = 0.0;
+    ri = nri;
+    __syncthreads();
+
+    while (nu * nv > tol * normS && rank < mn) {
+        if (rank >= rcap) {
+            if (tid == 0) atomicOr(status, 1);
+            break;
+        }
+        if (ri < 0 || ri >= n1) {  // no finite candidate row
+            if (tid == 0) atomicOr(status, 2);
+            break;
+        }
+        // residual row ri
+        for (int l = tid; l < rank; l += nt) coef[l] = U[(size_t)l * n1 + ri];
+        __syncthreads();
+        double *Vr = V + (size_t)rank * n2;
+        double bv = -1.0;
+        int bi = INT_MAX;
+        vsq = 0.0;
+        {
+            const int gi = I[ri];
+            for (int s = tid; s < n2; s += nt) {
+                double v = kentry(kp, gi, J[s]);
+                for (int l = 0; l < rank; ++l) v = __dsub_rn(v, __dmul_rn(coef[l], V[(size_t)l * n2 + s]));
+                Vr[s] = v;
+                vsq += v * v;
+                if (!bit_get(cmask, s)) {
+                    double a = fabs(v);
+                    if (amax_better(a, s, bv, bi)) { bv = a; bi = s; }
+                }
+            }
+        }
+        block_amax(bv, bi, shv, shi);
+        if (bi < 0 || bi >= n2) {  // no finite candidate column (non-finite entries)
+            if (tid == 0) atomicOr(status, 2);
+            break;
+        }
+        ci = bi;
+        nv = sqrt(block_sum(vsq, shs));
+        // residual column ci
+        piv = Vr[ci];
+        for (int l = tid; l < rank; l += nt) coef[l] = V[(size_t)l * n2 + ci];
+        __syncthreads();
+        double *Ur = U + (size_t)rank * n1;
+        usq = 0.0;
+        bv = -1.0;
+        bi = INT_MAX;
+        {
+            const int gj = J[ci];
+            for (int t = tid; t < n1; t += nt) {
+                double c = kentry(kp, I[t], gj);
+                for (int l = 0; l < rank; ++l) c = __dsub_rn(c, __dmul_rn(coef[l], U[(size_t)l * n1 + t]));
+                double u = __ddiv_rn(c, piv);
+                Ur[t] = u;
+                usq += u * u;
+                if (t != ri && !bit_get(rmask, t)) {
+                    double a = fabs(c);
+                    if (amax_better(a, t, bv, bi)) { bv = a; bi = t; }
+                }
+            }
+        }
+        block_amax(bv, bi, shv, shi);
+        nri = bi;
+        nu = sqrt(block_sum(usq, shs));
+        if (nu < 1e-36 || nv < 1e-36) break;
+        if (tid == 0) {
+            prow[pb.piv + rank] = ri;
+            pcol[pb.piv + rank] = ci;
+            rmask[ri >> 5] |= 1u << (ri & 31);
+            cmask[ci >> 5] |= 1u << (ci & 31);
+        }
+        ++rank;
+        // normS update: dots of every stored u and v with the new ones
+        for (int l = 0; l < rank; ++l) {
+            const double *Ul = U + (size_t)l * n1, *Vl = V + (size_t)l * n2;
+            double du = 0.0, dv = 0.0;
+            for (int t = tid; t < n1; t += nt) du += Ul[t] * Ur[t];
+            for (int s = tid; s < n2; s += nt) dv += Vl[s] * Vr[s];
+            du = warp_sum(du);
+            dv = warp_sum(dv);
+            if (lane == 0) {
+                red[(size_t)(2 * l) * nw + warp] = du;
+                red[(size_t)(2 * l + 1) * nw + warp] = dv;
+            }
+        }
+        __syncthreads();
+        for (int l = tid; l < rank; l += nt) {
+            double du = 0.0, dv = 0.0;
+            for (int q = 0; q < nw; ++q) {
+                du += red[(size_t)(2 * l) * nw + q];
+                dv += red[(size_t)(2 * l + 1) * nw + q];
+            }
+            coef[l] = 2.0 * fabs(du * dv);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double uv = nu * nv;
+            double ns = normS * normS + uv * uv;
+            for (int l = 0; l < rank; ++l) ns += coef[l];
+            shs[0] = sqrt(ns);
+        }
+        __syncthreads();
+        normS = shs[0];
+        ri = nri;
+        __syncthreads();
+    }
+    if (tid == 0) rank_out[blockIdx.x] = rank;
+}
+
+cudaError_t launch_nca(const NcaProb *probs, int nprob, const int32_t *idx, const KParams &kp, double tol,
+                       double *scratch, int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status, int max_n1,
+                       int max_n2, int max_rcap, cudaStream_t st) {
+    if (nprob == 0) return cudaSuccess;
+    int m1 = (max_n1 + 31) / 32, m2 = (max_n2 + 31) / 32;
+    int coef_len = max_rcap + 1;
+    size_t smem = (size_t)(m1 + m2 + 1) * 4 + (size_t)coef_len * 8 + (size_t)coef_len * 2 * (NCA_THREADS / 32) * 8;
+    cudaError_t e = cudaFuncSetAttribute(nca_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    nca_kernel<<<nprob, NCA_THREADS, smem, st>>>(probs, idx, kp, tol, scratch, rank, prow, pcol, status, m1, m2,
+                                                 coef_len);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- factors ---
+// F (r x r, row-major) <- K(I,J) factorised in pivot order: R on and above
+// the diagonal, unit-lower L below it, with the ACA's operation order
+// (R(l,j) = A(l,j) - sum_m L(l,m) R(m,j); L(t,l) = (A(t,l) - sum_m R(m,l) L(t,m)) / R(l,l)).
+__global__ void factor_kernel(const FactorJob *__restrict__ jobs, const int32_t *__restrict__ idx, KParams kp,
+                              double *__restrict__ F) {
+    const FactorJob jb = jobs[blockIdx.x];
+    const int r = jb.r;
+    double *A = F + jb.f;
+    const int32_t *I = idx + jb.ii, *J = idx + jb.jj;
+    for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+        int i = e / r, j = e % r;
+        A[e] = kentry(kp, I[i], J[j]);
+    }
+    __syncthreads();
+    for (int l = 0; l < r; ++l) {
+        for (int j = l + threadIdx.x; j < r; j += blockDim.x) {
+            double v = A[l * r + j];
+            for (int m = 0; m < l; ++m) v = __dsub_rn(v, __dmul_rn(A[l * r + m], A[m * r + j]));
+            A[l * r + j] = v;
+        }
+        __syncthreads();
+        const double piv = A[l * r + l];
+        for (int t = l + 1 + threadIdx.x; t < r; t += blockDim.x) {
+            double v = A[t * r + l];
+            for (int m = 0; m < l; ++m) v = __dsub_rn(v, __dmul_rn(A[m * r + l], A[t * r + m]));
+            A[t * r + l] = __ddiv_rn(v, piv);
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_factor(const FactorJob *jobs, int njobs, const int32_t *idx, const KParams &kp, double *F,
+                          cudaStream_t st) {
+    if (njobs == 0) return cudaSuccess;
+    factor_kernel<<<njobs, 128, 0, st>>>(jobs, idx, kp, F);
+    return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- transfers ---
+// One thread per point p of a job.
+//  X_ROW_RL: y = K(p,J) R^-1 L^-1  (far L2P rows; vertex / 1D M2M^T rows)
+//  X_ROW_R : y = K(p,J) R^-1       (1D U rows)
+//  X_COL_LR: y = R^-1 L^-1 K(I,p)  (semi-nested R^-1 L^-1 Ar columns)
+//  X_COL_L : y = L^-1 K(I,p)       (1D V^T columns)
+// The substitutions follow Eigen's triangularView::solve order as restated
+// in the oracle, so transfer rows are bitwise the reference's for equal entries.
+__global__ void xfer_kernel(const XferJob *__restrict__ jobs, const int32_t *__restrict__ idx, KParams kp,
+                            const double *__restrict__ F, double *__restrict__ op) {
+    const XferJob jb = jobs[blockIdx.y];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= jb.n) return;
+    const int r = jb.r;
+    const double *A = F + jb.f;  // row-major r x r: R upper, L strictly lower
+    const int32_t *J = idx + jb.jj;
+    const int gp = idx[jb.pi + p];
+    const bool row = jb.mode == X_ROW_RL || jb.mode == X_ROW_R;
+    // the output location is the working vector
+    double *y = row ? op + jb.a1 + (int64_t)p * jb.ld1 : op + jb.a1 + p;
+    const int64_t ys = row ? 1 : jb.ld1;
+    for (int j = 0; j < r; ++j) y[j * ys] = kentry(kp, gp, J[j]);  // K(p,J) == K(J,p) bitwise
+    if (row) {
+        // z R = b (forward), then y L = z (backward, unit diagonal)
+        for (int j = 0; j < r; ++j) {
+            double s = y[j];
+            for (int q = 0; q < j; ++q) s = __dsub_rn(s, __dmul_rn(y[q], A[q * r + j]));
+            y[j] = __ddiv_rn(s, A[j * r + j]);
+        }
+        if (jb.mode == X_ROW_RL)
+            for (int j = r - 1; j >= 0; --j) {
+                double s = y[j];
+                for (int q = j + 1; q < r; ++q) s = __dsub_rn(s, __dmul_rn(y[q], A[q * r + j]));
+                y[j] = s;
+            }
+        if (jb.a2 >= 0)
+            for (int j = 0; j < r; ++j) op[jb.a2 + (int64_t)j * jb.ld2 + p] = y[j];
+    } else {
+        // L x = b (forward, unit diagonal), then R x = x (backward)
+        for (int i = 0; i < r; ++i) {
+            double s = y[i * ys];
+            for (int q = 0; q < i; ++q) s = __dsub_rn(s, __dmul_rn(A[i * r + q], y[q * ys]));
+            y[i * ys] = s;
+        }
+        if (jb.mode == X_COL_LR)
+            for (int i = r - 1; i >= 0; --i) {
+                double s = y[i * ys];
+                for (int q = i + 1; q < r; ++q) s = __dsub_rn(s, __dmul_rn(A[i * r + q], y[q * ys]));
+                y[i * ys] = __ddiv_rn(s, A[i * r + i]);
+            }
+    }
+}
+
+cudaError_t launch_xfer(const XferJob *jobs, int njobs, int max_n, const int32_t *idx, const KParams &kp,
+                        const double *F, double *op, cudaStream_t st) {
+    if (njobs == 0 || max_n == 0) return cudaSuccess;
+    const int bs = 64;
+    for (int j0 = 0; j0 < njobs; j0 += 65535) {
+        int nj = njobs - j0 < 65535 ? njobs - j0 : 65535;
+        dim3 grid((unsigned)((max_n + bs - 1) / bs), (unsigned)nj);
+        xfer_kernel<<<grid, bs, 0, st>>>(jobs + j0, idx, kp, F, op);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// --------------------------------------------------------------- fills ---
+__global__ void fill_kernel(const FillJob *__restrict__ jobs, const int32_t *__restrict__ idx, KParams kp,
+                            double *__restrict__ op) {
+    const FillJob jb = jobs[blockIdx.y];
+    const int64_t total = (int64_t)jb.nr * jb.nc;
+    const int32_t *R = idx + jb.ri, *C = idx + jb.ci;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        int i = (int)(e / jb.nc), c = (int)(e % jb.nc);
+        op[jb.a + (int64_t)i * jb.lda + c] = kentry(kp, R[i], C[c]);
+    }
+}
+
+cudaError_t launch_fill(const FillJob *jobs, int njobs, const int32_t *idx, const KParams &kp, double *op,
+                        cudaStream_t st) {
+    if (njobs == 0) return cudaSuccess;
+    for (int j0 = 0; j0 < njobs; j0 += 65535) {
+        int nj = njobs - j0 < 65535 ? njobs - j0 : 65535;
+        dim3 grid(8, (unsigned)nj);
+        fill_kernel<<<grid, 256, 0, st>>>(jobs + j0, idx, kp, op);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+__global__ void convert_f32_kernel(const double *__restrict__ s, float *__restrict__ d, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = (float)s[i];
+}
+cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    convert_f32_kernel<<<1216, 256, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- block-row GEMV ---
+// One CTA per target. The gathered sources of all panels are staged in
+// shared memory; rows are distributed over lane groups of gsz lanes, each
+// lane streaming 16-byte (FP64: 2, FP32: 4 elements) chunks of the row-major
+// panel rows, reduced with xor shuffles inside the group.
+constexpr int BRG_THREADS = 256;
+
+template <class T> struct Vec16;
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+
+template <class T>
+__device__ __forceinline__ T dot16(const typename Vec16<T>::type a, const T *x);
+template <>
+__device__ __forceinline__ double dot16<double>(const double2 a, const double *x) {
+    return a.x * x[0] + a.y * x[1];
+}
+template <>
+__device__ __forceinline__ float dot16<float>(const float4 a, const float *x) {
+    return a.x * x[0] + a.y * x[1] + a.z * x[2] + a.w * x[3];
+}
+
+template <class T>
+__global__ void __launch_bounds__(BRG_THREADS) brg_kernel(const Target *__restrict__ Tg, const Panel *__restrict__ Pn,
+                                                         const Seg *__restrict__ Sg, int64_t t0,
+                                                         const T *__restrict__ A, T *ws, const T *__restrict__ xin,
+                                                         T *yout, const int32_t *__restrict__ perm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);
+    using V16 = typename Vec16<T>::type;
+    constexpr int VN = Vec16<T>::n;
+    const Target tg = Tg[t0 + blockIdx.x];
+    for (int p = tg.p0; p < tg.p1; ++p) {
+        const Panel pn = Pn[p];
+        for (int s = pn.s0; s < pn.s1; ++s) {
+            const Seg sg = Sg[s];
+            T *dst = xs + pn.xoff + sg.xoff;
+            if (sg.flags & S_GATHER)
+                for (int c = threadIdx.x; c < sg.len; c += blockDim.x) dst[c] = xin[perm[sg.src + c]];
+            else
+                for (int c = threadIdx.x; c < sg.len; c += blockDim.x) dst[c] = ws[sg.src + c];
+        }
+    }
+    __syncthreads();
+    const int g = tg.gsz;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sub = lane / g, gl = lane % g;
+    const int rpw = 32 / g, step = (BRG_THREADS / 32) * rpw;
+    for (int ib = warp * rpw; ib < tg.nrows; ib += step) {
+        const int i = ib + sub;
+        T acc = T(0);
+        if (i < tg.nrows) {
+            for (int p = tg.p0; p < tg.p1; ++p) {
+                const Panel pn = Pn[p];
+                const T *row = A + pn.a + (int64_t)i * pn.lda;
+                const T *xp = xs + pn.xoff;
+                const int wfull = (pn.w / VN) * VN;
+                for (int c = gl * VN; c < wfull; c += g * VN) {
+                    V16 a = *reinterpret_cast<const V16 *>(row + c);
+                    acc += dot16<T>(a, xp + c);
+                }
+                for (int c = wfull + gl; c < pn.w; c += g) acc += row[c] * xp[c];
+            }
+        }
+        for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (i < tg.nrows && gl == 0) {
+            const int64_t d = tg.dst + i;
+            if (tg.flags & T_SCATTER) {
+                T v = (tg.flags & T_ACCUM) ? ws[d] + acc : acc;
+                yout[perm[d]] = v;
+            } else if (tg.flags & T_ATOMIC) {
+                atomicAdd(ws + d, acc);
+            } else if (tg.flags & T_ACCUM) {
+                ws[d] += acc;
+            } else {
+                ws[d] = acc;
+            }
+        }
+    }
+}
+
+template <class T>
+static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
+                                const T *A, T *ws, const T *xin, T *yout, const int32_t *perm, cudaStream_t st) {
+    if (t1 <= t0) return cudaSuccess;
+    size_t smem = (size_t)(max_xw > 0 ? max_xw : 1) * sizeof(T);
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(brg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    for (int64_t b = t0; b < t1; b += 2147483647LL) {
+        int64_t nb = t1 - b < 2147483647LL ? t1 - b : 2147483647LL;
+        brg_kernel<T><<<(unsigned)nb, BRG_THREADS, smem, st>>>(Tg, P, S, b, A, ws, xin, yout, perm);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
+                           const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
+                           cudaStream_t st) {
+    return launch_brg_t<double>(T, P, S, t0, t1, max_xw, A, ws, xin, yout, perm, st);
+}
+cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
+                           const float *A, float *ws, const float *xin, float *yout, const int32_t *perm,
+                           cudaStream_t st) {
+    return launch_brg_t<float>(T, P, S, t0, t1, max_xw, A, ws, xin, yout, perm, st);
+}
+
+template <class T>
+__global__ void scatter_kernel(const T *__restrict__ yp, T *__restrict__ y, const int32_t *__restrict__ perm, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[perm[i]] = yp[i];
+}
+cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st) {
+    scatter_kernel<double><<<608, 256, 0, st>>>(yp, y, perm, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_scatter_f32(const float *yp, float *y, const int32_t *perm, int64_t n, cudaStream_t st) {
+    scatter_kernel<float><<<608, 256, 0, st>>>(yp, y, perm, n);
+    return cudaGetLastError();
+}
+
+// -------------------------------------------------------- dense oracle ---
+__global__ void dense_kernel(KParams kp, int64_t N, const double *__restrict__ x, double *__restrict__ y,
+                             int64_t row0) {
+    __shared__ double sh[32];
+    const int64_t r = row0 + blockIdx.x;
+    double acc = 0.0;
+    for (int64_t j = threadIdx.x; j < N; j += blockDim.x) acc += kentry(kp, (int)r, (int)j) * x[j];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) y[blockIdx.x] = acc;
+}
+cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0, int64_t nrows,
+                                cudaStream_t st) {
+    for (int64_t b = 0; b < nrows; b += 2147483647LL) {
+        int64_t nb = nrows - b < 2147483647LL ? nrows - b : 2147483647LL;
+        dense_kernel<<<(unsigned)nb, 256, 0, st>>>(kp, N, x, y + b, row0 + b);
+    }
+    return cudaGetLastError();
+}
+
+// --------------------------------------------------------------- GMRES ---
+// Classical Gram-Schmidt with one reorthogonalisation (CGS2), FP64, on a
+// device-resident Krylov basis. Block b owns rows [b*chunk, (b+1)*chunk);
+// per-block partial sums go through three buffers so that no block
+// overwrites a partial another block still reads.
+__device__ __forceinline__ void gm_rows(int64_t N, int nblk, int64_t &r0, int64_t &r1) {
+    int64_t chunk = (N + nblk - 1) / nblk;
+    r0 = (int64_t)blockIdx.x * chunk;
+    r1 = r0 + chunk < N ? r0 + chunk : N;
+}
+
+// out[b*(m+1)+k] = sum_{t in block b} V[t,k] w[t], k <= i
+__device__ void gm_block_dots(const GmresDev &g, int i, int64_t r0, int64_t r1, double *red, double *out) {
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = 0; k <= i; ++k) {
+        const double *Vk = g.V + (size_t)k * g.N;
+        double acc = 0.0;
+        for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) acc += Vk[t] * g.w[t];
+        acc = warp_sum(acc);
+        if (lane == 0) red[k * nw + warp] = acc;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k <= i; k += blockDim.x) {
+        double s = 0.0;
+        for (int q = 0; q < nw; ++q) s += red[k * nw + q];
+        out[(size_t)blockIdx.x * (g.m + 1) + k] = s;
+    }
+}
+
+__global__ void gm_dots(GmresDev g) {
+    extern __shared__ double red[];
+    const int i = *g.iter;
+    int64_t r0, r1;
+    gm_rows(g.N, g.nblk, r0, r1);
+    gm_block_dots(g, i, r0, r1, red, g.part);
+}
+
+// h = sum_b in; w -= V h; H(:,i) (=|+=) h; out <- new dots (pass 0) or ||w||^2 partials (pass 1)
+__global__ void gm_update(GmresDev g, int pass) {
+    extern __shared__ double shm[];
+    double *h = shm;
+    double *red = shm + (g.m + 1);
+    const double *in = g.part + (size_t)pass * g.nblk * (g.m + 1);
+    double *out = g.part + (size_t)(pass + 1) * g.nblk * (g.m + 1);
+    const int i = *g.iter;
+    for (int k = threadIdx.x; k <= i; k += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < g.nblk; ++b) s += in[(size_t)b * (g.m + 1) + k];
+        h[k] = s;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int k = threadIdx.x; k <= i; k += blockDim.x) {
+            double *Hk = g.H + (size_t)i * (g.m + 1) + k;
+            *Hk = pass == 0 ? h[k] : *Hk + h[k];
+        }
+    int64_t r0, r1;
+    gm_rows(g.N, g.nblk, r0, r1);
+    for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+        double v = g.w[t];
+        for (int k = 0; k <= i; ++k) v -= g.V[(size_t)k * g.N + t] * h[k];
+        g.w[t] = v;
+    }
+    __syncthreads();
+    if (pass == 0) {
+        gm_block_dots(g, i, r0, r1, red, out);
+    } else {
+        const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        double acc = 0.0;
+        for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) acc += g.w[t] * g.w[t];
+        acc = warp_sum(acc);
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int q = 0; q < nw; ++q) s += red[q];
+            out[(size_t)blockIdx.x * (g.m + 1)] = s;
+        }
+    }
+}
+
+// H(i+1,i) = ||w||; V[:,i+1] = vcur = (1/H(i+1,i)) w
+__global__ void gm_normalise(GmresDev g) {
+    __shared__ double hn;
+    const double *in = g.part + (size_t)2 * g.nblk * (g.m + 1);
+    const int i = *g.iter;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int b = 0; b < g.nblk; ++b) s += in[(size_t)b * (g.m + 1)];
+        hn = sqrt(s);
+        if (blockIdx.x == 0) g.H[(size_t)i * (g.m + 1) + i + 1] = hn;
+    }
+    __syncthreads();
+    const double ih = 1.0 / hn;
+    int64_t r0, r1;
+    gm_rows(g.N, g.nblk, r0, r1);
+    double *Vn = g.V + (size_t)(i + 1) * g.N;
+    for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+        double v = ih * g.w[t];
+        Vn[t] = v;
+        g.vcur[t] = v;
+    }
+}
+
+__device__ void gm_apply(double &dx, double &dy, double cs, double sn) {
+    double temp = __dadd_rn(__dmul_rn(cs, dx), __dmul_rn(sn, dy));
+    dy = __dadd_rn(__dmul_rn(-sn, dx), __dmul_rn(cs, dy));
+    dx = temp;
+}
+
+// Givens rotations on column i (*/codes/gmres.hpp:30-75,156-162); resid = |s(i+1)| / ||b||.
+__global__ void gm_givens(GmresDev g, double tol) {
+    const int i = *g.iter;
+    double *Hc = g.H + (size_t)i * (g.m + 1);
+    if (g.scal[2] != 0.0) return;  // already converged: leave state untouched
+    for (int k = 0; k < i; ++k) gm_apply(Hc[k], Hc[k + 1], g.cs[k], g.sn[k]);
+    double dx = Hc[i], dy = Hc[i + 1], cs, sn;
+    if (dy == 0.0) { cs = 1.0; sn = 0.0; }
+    else if (fabs(dy) > fabs(dx)) {
+        double temp = dx / dy;
+        sn = 1.0 / sqrt(1.0 + temp * temp);
+        cs = temp * sn;
+    } else {
+        double temp = dy / dx;
+        cs = 1.0 / sqrt(1.0 + temp * temp);
+        sn = temp * cs;
+    }
+    g.cs[i] = cs;
+    g.sn[i] = sn;
+    gm_apply(Hc[i], Hc[i + 1], cs, sn);
+    gm_apply(g.s[i], g.s[i + 1], cs, sn);
+    double resid = fabs(g.s[i + 1]) / g.scal[0];
+    g.scal[1] = resid;
+    if (resid < tol) g.scal[2] = 1.0;
+    else if (i + 1 < g.m) *g.iter = i + 1;
+}
+
+cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st) {
+    const int nw = GM_THREADS / 32;
+    size_t sm_dots = (size_t)(g.m + 1) * nw * sizeof(double);
+    size_t sm_upd = (size_t)(g.m + 1) * (nw + 1) * sizeof(double);
+    static bool cfg = false;
+    if (!cfg) {
+        cudaFuncSetAttribute(gm_dots, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(gm_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cfg = true;
+    }
+    gm_dots<<<g.nblk, GM_THREADS, sm_dots, st>>>(g);
+    gm_update<<<g.nblk, GM_THREADS, sm_upd, st>>>(g, 0);
+    gm_update<<<g.nblk, GM_THREADS, sm_upd, st>>>(g, 1);
+    return cudaGetLastError();
+}
+
+cudaError_t gmres_finish_iter(const GmresDev &g, double tol, cudaStream_t st) {
+    gm_normalise<<<g.nblk, GM_THREADS, 0, st>>>(g);
+    gm_givens<<<1, 1, 0, st>>>(g, tol);
+    return cudaGetLastError();
+}
+
+// r = b - Ax; beta = ||r||; V[:,0] = vcur = r / beta; s = beta e1; iter = 0
+__global__ void gm_resid_part(GmresDev g, const double *__restrict__ b, const double *__restrict__ Ax) {
+    __shared__ double sh[32];
+    int64_t r0, r1;
+    gm_rows(g.N, g.nblk, r0, r1);
+    double acc = 0.0;
+    for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+        double r = b[t] - Ax[t];
+        g.w[t] = r;
+        acc += r * r;
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) g.part[blockIdx.x] = acc;
+}
+__global__ void gm_start_fin(GmresDev g, double normb) {
+    __shared__ double beta;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int b = 0; b < g.nblk; ++b) s += g.part[b];
+        beta = sqrt(s);
+        if (blockIdx.x == 0) {
+            for (int k = 0; k <= g.m; ++k) { g.s[k] = 0.0; g.cs[k] = 0.0; g.sn[k] = 0.0; }
+            g.s[0] = beta;
+            g.scal[0] = normb;
+            g.scal[1] = beta / normb;
+            g.scal[2] = 0.0;
+            g.scal[3] = beta;
+            *g.iter = 0;
+        }
+    }
+    __syncthreads();
+    const double ib = 1.0 / beta;
+    int64_t r0, r1;
+    gm_rows(g.N, g.nblk, r0, r1);
+    for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+        double v = g.w[t] * ib;
+        g.V[t] = v;
+        g.vcur[t] = v;
+    }
+}
+cudaError_t gmres_start(const GmresDev &g, const double *b, const double *Ax, double normb, cudaStream_t st) {
+    gm_resid_part<<<g.nblk, GM_THREADS, 0, st>>>(g, b, Ax);
+    gm_start_fin<<<g.nblk, GM_THREADS, 0, st>>>(g, normb);
+    return cudaGetLastError();
+}
+
+// x += sum_{j<=k} V[:,j] y[j]  (y precomputed by the back-substitution, in g.s)
+__global__ void gm_xupdate(GmresDev g, double *__restrict__ x, const double *__restrict__ y, int k) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < g.N; t += (int64_t)gridDim.x * blockDim.x) {
+        double v = x[t];
+        for (int j = 0; j <= k; ++j) v += g.V[(size_t)j * g.N + t] * y[j];
+        x[t] = v;
+    }
+}
+cudaError_t gmres_update(const GmresDev &g, double *x, const double *y, int k, cudaStream_t st) {
+    gm_xupdate<<<g.nblk, GM_THREADS, 0, st>>>(g, x, y, k);
+    return cudaGetLastError();
+}
+
+__global__ void norm_part(const double *__restrict__ x, int64_t n, double *part) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        acc += x[t] * x[t];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+__global__ void norm_fin(const double *part, int nblk, double *out) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += part[b];
+    *out = sqrt(s);
+}
+cudaError_t vec_norm(const double *x, int64_t n, double *part, int nblk, double *out, cudaStream_t st) {
+    norm_part<<<nblk, GM_THREADS, 0, st>>>(x, n, part);
+    norm_fin<<<1, 1, 0, st>>>(part, nblk, out);
+    return cudaGetLastError();
+}
+
+__global__ void axpby_kernel(double a, const double *x, double b, const double *y, double *z, int64_t n) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        z[t] = a * x[t] + b * y[t];
+}
+cudaError_t vec_axpby(double a, const double *x, double b, const double *y, double *z, int64_t n, cudaStream_t st) {
+    axpby_kernel<<<608, 256, 0, st>>>(a, x, b, y, z, n);
+    return cudaGetLastError();
+}
+__global__ void d2f_kernel(const double *x, float *y, int64_t n) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        y[t] = (float)x[t];
+}
+__global__ void f2d_kernel(const float *x, double *y, int64_t n) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        y[t] = (double)x[t];
+}
+cudaError_t vec_f64_to_f32(const double *x, float *y, int64_t n, cudaStream_t st) {
+    d2f_kernel<<<608, 256, 0, st>>>(x, y, n);
+    return cudaGetLastError();
+}
+cudaError_t vec_f32_to_f64(const float *x, double *y, int64_t n, cudaStream_t st) {
+    f2d_kernel<<<608, 256, 0, st>>>(x, y, n);
+    return cudaGetLastError();
+}
+
+}  // namespace h2w

@@ -1,0 +1,73 @@
+// Device-side entry points of the GB300 H2* / (H2+H)* library (sm_103a).
+// Host code calls these launch wrappers; every pointer is a device pointer.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "h2w_internal.h"
+
+namespace h2w {
+
+// Kernel-matrix entry parameters (reference kernel.hpp getMatrixEntry).
+struct KParams {
+    const double *pts;   // N*dim, original order
+    int dim, choice;
+    double diag;         // value on the diagonal
+    double c2d;          // 2D IE: (-1/(2 pi)) * 0.5
+    double four_pi;      // 3D IE: 4 pi
+    double loga;         // 3D RBF: log(a)
+    double den_small;    // 3D RBF: a log(a) - 1
+};
+
+struct NcaProb {
+    int64_t ri, ci;      // row / column index lists in the index buffer
+    int64_t u, v;        // scratch offsets: U (n1 x rcap, column l at u + l*n1), V (rcap x n2)
+    int64_t piv;         // output pivot offset (rcap entries)
+    int32_t n1, n2, rcap, pad;
+};
+
+// Assembly
+cudaError_t launch_nca(const NcaProb *probs, int nprob, const int32_t *idx, const KParams &kp, double tol,
+                       double *scratch, int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status,
+                       int max_n1, int max_n2, int max_rcap, cudaStream_t st);
+cudaError_t launch_factor(const FactorJob *jobs, int njobs, const int32_t *idx, const KParams &kp, double *F,
+                          cudaStream_t st);
+cudaError_t launch_xfer(const XferJob *jobs, int njobs, int max_n, const int32_t *idx, const KParams &kp,
+                        const double *F, double *op, cudaStream_t st);
+cudaError_t launch_fill(const FillJob *jobs, int njobs, const int32_t *idx, const KParams &kp, double *op,
+                        cudaStream_t st);
+cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStream_t st);
+
+// Matvec: one block-row GEMV launch over targets [t0, t1).
+cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
+                           const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
+                           cudaStream_t st);
+cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
+                           const float *A, float *ws, const float *xin, float *yout, const int32_t *perm,
+                           cudaStream_t st);
+cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
+cudaError_t launch_scatter_f32(const float *yp, float *y, const int32_t *perm, int64_t n, cudaStream_t st);
+
+// Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
+cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,
+                                int64_t nrows, cudaStream_t st);
+
+// GMRES building blocks (FP64). V is column-major N x (m+1).
+struct GmresDev {
+    double *V, *w, *vcur, *H, *cs, *sn, *s;  // V: N x (m+1); H: (m+1) x m column-major
+    double *part;                             // 3 * nblk * (m+1) partial sums
+    double *scal;                             // [0] ||b||, [1] resid, [2] converged flag, [3] beta
+    int32_t *iter;                                          // current Arnoldi column i
+    int64_t N;
+    int m, nblk;
+};
+cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st);      // orthogonalise w against V[:, 0..i], H column
+cudaError_t gmres_finish_iter(const GmresDev &g, double tol, cudaStream_t st);  // normalise, Givens, residual
+cudaError_t gmres_start(const GmresDev &g, const double *b, const double *Ax, double normb, cudaStream_t st);
+cudaError_t gmres_update(const GmresDev &g, double *x, const double *y, int k, cudaStream_t st);
+cudaError_t vec_norm(const double *x, int64_t n, double *part, int nblk, double *out, cudaStream_t st);
+cudaError_t vec_axpby(double a, const double *x, double b, const double *y, double *z, int64_t n, cudaStream_t st);
+cudaError_t vec_f64_to_f32(const double *x, float *y, int64_t n, cudaStream_t st);
+cudaError_t vec_f32_to_f64(const float *x, double *y, int64_t n, cudaStream_t st);
+
+}  // namespace h2w

@@ -1,0 +1,127 @@
+/* h2w.h — C ABI of the GB300-native H2* / (H2+H)* HODLRdD operator and solver.
+ *
+ * Drop-in boundary for the hot path of H2weak: the operator object that the
+ * reference's GMRES drives (class initialisation, {1D,2D,3D}/codes/matvec.hpp) and the
+ * GMRES itself (class iterative_solver, {1D,2D,3D}/codes/gmres.hpp). Plain pointers and
+ * sizes only; no C++ or torch types cross this boundary. Every function
+ * returns H2W_OK (0) or a negative status; h2w_last_error() gives the text.
+ *
+ * Ownership and threading: the handle owns all device memory (tree tables,
+ * packed operator, work vectors, CUDA graphs). Callers own x, y, b. One handle
+ * is used by one host thread at a time; distinct handles are independent and
+ * may share a device.
+ */
+#ifndef H2W_H
+#define H2W_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct h2w_handle h2w_handle;
+
+enum {
+    H2W_OK = 0,
+    H2W_ERR_ARG = -1,        /* bad argument or call order */
+    H2W_ERR_CUDA = -2,       /* CUDA runtime error (message has the call) */
+    H2W_ERR_NOMEM = -3,      /* device allocation failed */
+    H2W_ERR_RANK = -4,       /* an NCA rank exceeded the configured cap */
+    H2W_ERR_NOT_CONVERGED = -5,
+    H2W_ERR_STATE = -6       /* call needs an earlier step (tree, assembly) */
+};
+
+enum { H2W_FORM_NESTED = 0, H2W_FORM_SEMINESTED = 1 };           /* -DUSE_nHODLRdD / -DUSE_snHODLRdD */
+enum { H2W_KERNEL_IE = 0, H2W_KERNEL_RBF = 1 };                 /* reference "choice" */
+enum { H2W_ASSEMBLE_NCA = 0, H2W_ASSEMBLE_IMPORT = 1, H2W_ASSEMBLE_LEARNED = 2 };
+enum { H2W_PREC_FP64 = 0, H2W_PREC_FP32 = 1 };
+/* pointer-location flags for vectors */
+enum { H2W_HOST = 0, H2W_DEVICE = 1 };
+
+/* Lists exported by h2w_get_list / accepted by h2w_import_list: CSR over
+ * (level 0..L, box in numbering order); per (level, box, interaction-list
+ * slot) for SN_ROW/SN_COL in 2D/3D and per (level >= 1, box, sibling slot)
+ * in 1D. Values are original point indices except NBR/IL (box numbers) and
+ * ISVERTEX (0/1). */
+enum {
+    H2W_LIST_CHARGE = 0, H2W_LIST_NBR = 1, H2W_LIST_IL = 2, H2W_LIST_ISVERTEX = 3,
+    H2W_LIST_FAR_CHECK = 4, H2W_LIST_FAR_CHARGE = 5, H2W_LIST_VER_CHECK = 6, H2W_LIST_VER_CHARGE = 7,
+    H2W_LIST_SN_ROW = 8, H2W_LIST_SN_COL = 9
+};
+
+typedef struct h2w_config {
+    int dim;          /* 1, 2 or 3 */
+    int form;         /* H2W_FORM_* */
+    int choice;       /* H2W_KERNEL_*: kernel.hpp getMatrixEntry choice 0 / 1 */
+    int tol_pow;      /* NCA/ACA tolerance 10^-tol_pow (aca.hpp LowRank) */
+    int nlevels;      /* tree depth (main.cpp computes it from N and nmax) */
+    int rank_cap;     /* max NCA rank per block; 0 = min(rows, cols) */
+    int64_t kernel_n; /* particles.size() when the kernel object is built (0 = N) */
+    int64_t diag_n;   /* particles.size() when entries are evaluated (0 = N; 1D drivers: 2N) */
+    int device;       /* CUDA device ordinal; -1 = host-only handle (points, tree, lists) */
+} h2w_config;
+
+/* Replaces: new initialisation(N|sqrtN|cbrtN, nLevels, nParticlesInLeaf, L, TOL_POW, choice)
+ * (1D/codes/matvec.hpp:85-93, 2D/codes/matvec.hpp:120-129, 3D/codes/matvec.hpp:19-29). */
+int h2w_create(const h2w_config *cfg, h2w_handle **out);
+/* Replaces the destructor (the reference leaks; this frees everything). */
+int h2w_destroy(h2w_handle *h);
+const char *h2w_last_error(const h2w_handle *h);
+
+/* Points, row-major n x dim, host memory. Replaces the point generation of
+ * set_Uniform_Nodes (1D/codes/HODLR1Dtree.hpp:59-66, 2D :75-91, 3D :82-102). */
+int h2w_set_points(h2w_handle *h, const double *pts, int64_t n);
+/* The reference's uniform grid: n_per_axis^dim interior points of [-1,1]^dim,
+ * -1 + 2(k+1)/(n+1), with the reference's point numbering. */
+int h2w_gen_grid(h2w_handle *h, int64_t n_per_axis);
+/* n points uniform in [-1,1)^dim from the counter-based splitmix64 stream `seed`. */
+int h2w_gen_uniform(h2w_handle *h, uint64_t seed, int64_t n);
+/* Copy the current points out (row-major n x dim). */
+int h2w_get_points(h2w_handle *h, double *pts);
+int h2w_num_points(h2w_handle *h, int64_t *n);
+
+/* Tree, neighbour slots, ordered interaction lists, vertex flags and charge
+ * locations. Replaces createTree + assign_*Interaction* + assign_center_location
+ * + separate_vertex_interaction + assignChargeLocations + assignNonLeafChargeLocations
+ * (1D/codes/HODLR1Dtree.hpp:79-212, 2D/codes/HODLR2Dtree.hpp:104-534, 3D/codes/HODLR3Dtree.hpp:116-1852). */
+int h2w_build_tree(h2w_handle *h);
+/* CSR export of a list; call with NULL arrays to get the sizes. */
+int h2w_get_list(h2w_handle *h, int which, int64_t *ptr, int32_t *val, int64_t *nptr, int64_t *nval);
+
+/* Skeleton import (pivots of another NCA run, e.g. the oracle's), same CSR
+ * layout as h2w_get_list; used by H2W_ASSEMBLE_IMPORT. */
+int h2w_import_list(h2w_handle *h, int which, const int64_t *ptr, const int32_t *val, int64_t nptr);
+
+/* Compress the operator on the GPU. Replaces tree_initialisation's assembly
+ * calls: getNodes / getNodes_ver / assemble_M2L_* / assemble_M2M_ver /
+ * assemble_NearField / getUVtTree_sn / assembleAcAr_sn (and the 1D forms). */
+int h2w_assemble(h2w_handle *h, int mode);
+/* Stored-entry count, exactly findMemory_n / findMemory_sn
+ * (1D/codes/HODLR1Dtree.hpp:535-588, 2D :1207-1305, 3D :2505-2628). */
+int h2w_storage_entries(h2w_handle *h, double *entries);
+/* Bytes of packed operator data one FP64 / FP32 matvec reads. */
+int h2w_operator_bytes(h2w_handle *h, int precision, int64_t *bytes);
+
+/* y = A x for nrhs right-hand sides (column-major N x nrhs, leading dim N),
+ * x and y in original point order. Replaces initialisation::mat_vec_prod
+ * (1D/codes/matvec.hpp:121-138,163-178; 2D :163-182,212-233; 3D :63-83,115-136).
+ * where = H2W_HOST or H2W_DEVICE; stream = cudaStream_t or NULL (default). */
+int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precision, int where, void *stream);
+
+/* GMRES, unrestarted, FP64, device-resident. Replaces iterative_solver::GMRES
+ * ({1D,2D,3D}/codes/gmres.hpp:92-200): x0 = x on entry, stops when |s(i+1)|/||b|| < 10^-tol_pow. */
+int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_pow, int where, int *iters,
+              double *resid);
+/* Mixed precision: FP32 inner GMRES (FP32 operator) wrapped in FP64 iterative
+ * refinement whose residual uses the FP64 operator; stops when the FP64
+ * relative residual ||b - A x|| / ||b|| < 10^-tol_pow. */
+int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int inner_iter, int tol_pow, int where,
+                 int *outer_iters, int *inner_total, double *resid);
+
+/* Dense FP64 product with the exact kernel matrix (getTruePoten,
+ * 1D/codes/HODLR1Dtree.hpp:590-604), on the GPU, rows [row0, row0 + nrows). */
+int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, int64_t nrows, int where);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,69 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Runs the reference's own headers (built by `make -C oracle ref` against the
+Eigen-subset shim, from the reference sources) on small seeded cases and
+stores points, tree lists, NCA pivots, storage counts, matvec outputs, the
+dense product and GMRES results. Needs the reference tree; the committed
+.npz files are what the tests read (no test reads the reference).
+
+    python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+from h2wdump import read_dump, write_input  # noqa: E402
+from h2weak_gb300 import synth  # noqa: E402
+
+# name: dim, form, n_param, nLevels, leaf_param, tol_pow, choice, points (None = grid), gmres tol_pow
+CASES = {
+    "g1d_n_rbf": (1, "n", 2048, 5, 64, 10, 1, None, 10),
+    "g1d_sn_ie": (1, "sn", 2048, 5, 64, 10, 0, None, 10),
+    "g2d_n_ie": (2, "n", 48, 3, 6, 10, 0, None, 10),
+    "g2d_sn_rbf": (2, "sn", 48, 3, 6, 10, 1, None, 10),
+    "g3d_n_rbf": (3, "n", 16, 2, 4, 8, 1, None, 10),
+    "g3d_sn_ie": (3, "sn", 16, 2, 4, 8, 0, None, 10),
+    "g2d_n_rand": (2, "n", 0, 3, 0, 8, 1, ("uniform", 2, 3000), 10),
+    "g3d_n_rand": (3, "n", 0, 2, 0, 8, 1, ("uniform", 3, 4000), 10),
+}
+LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge", "sn_row", "sn_col"]
+
+
+def run_case(name, spec):
+    dim, form, npar, nlev, leaf, tol, ch, pts, gtol = spec
+    if pts is not None:
+        pts = synth.uniform_points(synth.config_seed(40 + dim, 0), pts[2], dim)
+        N = len(pts)
+    else:
+        N = npar ** dim
+    vecs = [synth.normal(synth.config_seed(90, v), N) for v in range(2)]
+    xtrue = synth.normal(synth.config_seed(91, 0), N)
+    inp, out = "/tmp/golden_in_%s.bin" % name, "/tmp/golden_out_%s.bin" % name
+    write_input(inp, pts, vecs, xtrue, dense=True)
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref%dd_%s" % (dim, form))
+    r = subprocess.run([exe, str(npar), str(nlev), str(leaf), "1", str(tol), str(ch), inp, out, "500", str(gtol)],
+                       capture_output=True, text=True, check=True)
+    d = read_dump(out)
+    rec = {"spec": np.array([dim, 0 if form == "n" else 1, npar, nlev, leaf, tol, ch, gtol, N], dtype=np.int64),
+           "points": d["points"].reshape(N, dim), "vecs": np.stack(vecs), "xtrue": xtrue,
+           "memory": d["memory"], "matvec": d["matvec"].reshape(2, N), "dense_matvec": d["dense_matvec"],
+           "gmres_rhs": d["gmres_rhs"], "gmres_x": d["gmres_x"], "gmres_stats": d["gmres_stats"]}
+    for nm in LISTS:
+        rec[nm + "_ptr"] = d[nm + ".ptr"]
+        rec[nm + "_val"] = d[nm + ".val"]
+    if "uv_rank" in d:
+        rec["uv_rank"] = d["uv_rank"]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)
+    return r.stdout.strip().splitlines()[-1]
+
+
+if __name__ == "__main__":
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    for name, spec in CASES.items():
+        print(name, run_case(name, spec))

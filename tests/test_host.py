@@ -1,0 +1,94 @@
+"""Host-side logic of the GPU library, no GPU needed: the C ABI loads and
+exports every declared symbol, and a host-only handle (device = -1) builds
+the tree, neighbour slots, ordered interaction lists, vertex flags and leaf
+permutation bit-exactly as the reference (golden fixtures)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import h2weak_gb300 as hw
+from conftest import ROOT, golden_names, load_golden
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "h2w.h")).read()
+    return sorted(set(re.findall(r"\b(h2w_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = hw.lib()
+    names = declared_symbols()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), n
+    assert sorted(hw.EXPORTS) == sorted(n for n in names if n != "h2w_last_error") or set(hw.EXPORTS) <= set(names)
+
+
+def test_bad_config_is_rejected():
+    with pytest.raises(hw.H2WError):
+        hw.H2Operator(4, 0, 1, 8, 3, device=-1)
+    with pytest.raises(hw.H2WError):
+        hw.H2Operator(2, 0, 7, 8, 3, device=-1)
+
+
+def test_host_only_handle_cannot_assemble():
+    op = hw.H2Operator(2, 0, 1, 8, 2, device=-1)
+    op.gen_grid(16)
+    op.build_tree()
+    with pytest.raises(hw.H2WError):
+        op.assemble()
+
+
+def test_state_errors():
+    op = hw.H2Operator(2, 0, 1, 8, 2, device=-1)
+    with pytest.raises(hw.H2WError):
+        op.build_tree()  # no points yet
+    with pytest.raises(hw.H2WError):
+        op.set_points(np.array([[0.0, np.nan]]))
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_tree_lists_match_reference(name):
+    g = load_golden(name)
+    op = hw.H2Operator(g["dim"], g["form"], g["choice"], g["tol_pow"], g["nlevels"], device=-1)
+    op.set_points(g["points"])
+    op.build_tree()
+    for nm in ["charge", "nbr", "il", "isvertex"]:
+        p, v = op.get_list(nm)
+        assert np.array_equal(p, g[nm + "_ptr"]), nm
+        assert np.array_equal(v, g[nm + "_val"]), nm
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if "rand" not in n])
+def test_grid_points_match_reference(name):
+    g = load_golden(name)
+    op = hw.H2Operator(g["dim"], g["form"], g["choice"], g["tol_pow"], g["nlevels"], device=-1)
+    op.gen_grid(g["n_param"])
+    assert np.array_equal(op.points(), g["points"])
+
+
+def test_uniform_points_match_python_generator():
+    from h2weak_gb300 import synth
+    for dim in (1, 2, 3):
+        op = hw.H2Operator(dim, 0, 1, 8, 2, device=-1)
+        op.gen_uniform(12345, 1000)
+        assert np.array_equal(op.points(), synth.uniform_points(12345, 1000, dim))
+
+
+@pytest.mark.parametrize("dim,n,lv", [(1, 32768, 9), (2, 256, 5), (3, 64, 4)])
+def test_levels_and_lists_at_full_config_sizes(dim, n, lv):
+    """The full-size grids of the benchmark configurations: depth as the
+    reference drivers compute it, and lists equal to the oracle's."""
+    from oracle import Oracle
+    leaf = {1: 64, 2: 8, 3: 5}[dim]
+    assert hw.levels_for(dim, n, leaf) == lv
+    op = hw.H2Operator(dim, 0, 1, 8, lv, device=-1)
+    op.gen_grid(n)
+    op.build_tree()
+    o = Oracle(dim, 0, op.points(), lv, 8, 1, assemble=False)
+    for nm in ["charge", "nbr", "il", "isvertex"]:
+        p1, v1 = op.get_list(nm)
+        p2, v2 = o.csr(nm)
+        assert np.array_equal(p1, p2) and np.array_equal(v1, v2), nm

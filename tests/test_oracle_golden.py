@@ -1,0 +1,44 @@
+"""The CPU oracle against the golden fixtures made by running the
+reference's own code (tests/golden/make_golden.py): tree lists, NCA pivots,
+storage count and matvec must agree bit for bit."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge"]
+
+
+def oracle_for(g):
+    from oracle import Oracle
+    N, dim = g["N"], g["dim"]
+    kn, dn = (N, 2 * N) if dim == 1 else (N, N)
+    return Oracle(dim, g["form"], g["points"], g["nlevels"], g["tol_pow"], g["choice"], kn, dn)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_matches_reference(name):
+    g = load_golden(name)
+    o = oracle_for(g)
+    names = LISTS + (["sn_row", "sn_col"] if g["dim"] > 1 else [])
+    for nm in names:
+        p, v = o.csr(nm)
+        assert np.array_equal(p, g[nm + "_ptr"]), nm
+        assert np.array_equal(v, g[nm + "_val"]), nm
+    if "uv_rank" in g:
+        assert np.array_equal(o.csr("uv_rank")[1], g["uv_rank"])
+    assert o.memory() == g["memory"][0]
+    for k in range(2):
+        assert np.array_equal(o.matvec(g["vecs"][k]), g["matvec"][k])
+
+
+@pytest.mark.parametrize("name", ["g1d_n_rbf", "g2d_n_ie", "g3d_sn_ie"])
+def test_oracle_dense_and_gmres(name):
+    g = load_golden(name)
+    o = oracle_for(g)
+    yd = o.dense_matvec(g["vecs"][0])
+    np.testing.assert_allclose(yd, g["dense_matvec"], rtol=0, atol=1e-12 * np.abs(g["dense_matvec"]).max())
+    x, it, res = o.gmres(g["gmres_rhs"], max_iter=500, tol_pow=g["gtol"])
+    assert it == int(g["gmres_stats"][0])
+    assert res == pytest.approx(g["gmres_stats"][1], rel=1e-6)
+    np.testing.assert_allclose(x, g["gmres_x"], rtol=0, atol=1e-12 * np.abs(g["gmres_x"]).max())
