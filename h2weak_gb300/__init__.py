@@ -53,8 +53,8 @@ _lib = None
 
 
 def build(force=False):
-    from . import build as _b
-    return _b.build(force=force)
+    from . import buildlib
+    return buildlib.build(force=force)
 
 
 def lib():
