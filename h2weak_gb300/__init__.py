@@ -34,7 +34,7 @@ LISTS = {"charge": 0, "nbr": 1, "il": 2, "isvertex": 3, "far_check": 4, "far_cha
 EXPORTS = ["h2w_create", "h2w_destroy", "h2w_last_error", "h2w_set_points", "h2w_gen_grid", "h2w_gen_uniform",
            "h2w_get_points", "h2w_num_points", "h2w_build_tree", "h2w_get_list", "h2w_import_list",
            "h2w_assemble", "h2w_storage_entries", "h2w_operator_bytes", "h2w_matvec", "h2w_gmres",
-           "h2w_gmres_ir", "h2w_dense_matvec"]
+           "h2w_gmres_ir", "h2w_dense_matvec", "h2w_profile", "h2w_profile_phases", "h2w_launch_count"]
 
 
 class H2WError(RuntimeError):
@@ -84,15 +84,24 @@ def lib():
         "h2w_gmres": [P, P, P, I, I, I, ctypes.POINTER(I), ctypes.POINTER(D)],
         "h2w_gmres_ir": [P, P, P, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)],
         "h2w_dense_matvec": [P, P, P, I64, I64, I],
+        "h2w_profile": [P, I],
+        "h2w_profile_phases": [P, I, I, P, P, P, ctypes.POINTER(I)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
         f.argtypes = args
         f.restype = I
+    L.h2w_launch_count.argtypes = []
+    L.h2w_launch_count.restype = I64
     L.h2w_last_error.argtypes = [P]
     L.h2w_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
+
+
+def launch_count():
+    """Kernel launches this library has issued since it was loaded."""
+    return int(lib().h2w_launch_count())
 
 
 def _ptr(a):
@@ -192,6 +201,19 @@ class H2Operator:
         self._ck(lib().h2w_operator_bytes(self.h, precision, ctypes.byref(b)))
         return b.value
 
+    # instrumentation
+    def profile(self, enable):
+        self._ck(lib().h2w_profile(self.h, 1 if enable else 0))
+
+    def profile_phases(self, precision=PREC_FP64):
+        n = ctypes.c_int()
+        self._ck(lib().h2w_profile_phases(self.h, precision, 0, None, None, None, ctypes.byref(n)))
+        la = np.zeros(n.value, dtype=np.int64)
+        ms = np.zeros(n.value)
+        by = np.zeros(n.value)
+        self._ck(lib().h2w_profile_phases(self.h, precision, n.value, _ptr(la), _ptr(ms), _ptr(by), None))
+        return la, ms, by
+
     # products
     def matvec(self, x, precision=PREC_FP64):
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -212,6 +234,27 @@ class H2Operator:
         y = np.empty(n)
         self._ck(lib().h2w_dense_matvec(self.h, _ptr(x), _ptr(y), row0, n, HOST))
         return y
+
+    def gmres_device(self, b_ptr, x_ptr, max_iter=500, tol_pow=10):
+        it, res = ctypes.c_int(), ctypes.c_double()
+        rc = lib().h2w_gmres(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), max_iter, tol_pow, DEVICE,
+                             ctypes.byref(it), ctypes.byref(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return it.value, res.value
+
+    def gmres_ir_device(self, b_ptr, x_ptr, max_outer=20, inner_iter=100, tol_pow=10, where=DEVICE):
+        oi, ii, res = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        rc = lib().h2w_gmres_ir(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), max_outer, inner_iter,
+                                tol_pow, where, ctypes.byref(oi), ctypes.byref(ii), ctypes.byref(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return oi.value, ii.value, res.value
+
+    def gmres_host_ptr(self, b_ptr, x_ptr, max_iter=500, tol_pow=10):
+        it, res = ctypes.c_int(), ctypes.c_double()
+        rc = lib().h2w_gmres(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), max_iter, tol_pow, HOST,
+                             ctypes.byref(it), ctypes.byref(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return it.value, res.value
 
     def gmres(self, b, x0=None, max_iter=500, tol_pow=10):
         b = np.ascontiguousarray(b, dtype=np.float64)

@@ -93,6 +93,12 @@ struct h2w_handle {
     DBuf<double> d_ws, d_x, d_y;
     DBuf<float> d_ws32, d_x32, d_y32;
     std::vector<Phase> phases;
+    std::vector<int64_t> ph_op, ph_vec;   // per phase: operator and vector elements moved
+    // launch profiling of the block-row GEMV (events bracket every phase launch)
+    bool prof = false;
+    struct ProfRec { cudaEvent_t a, b; int prec, phase; };
+    std::vector<ProfRec> prof_recs;
+    std::vector<cudaEvent_t> ev_pool;
     bool fused_scatter = true;
     int64_t ws_n = 0, yperm_off = 0, op_n = 0;
     double storage = 0;
@@ -1031,9 +1037,21 @@ void build_plan(h2w_handle *h) {
             for (int64_t q = lp.t0; q < lp.t1; ++q)
                 if (pb.T[(size_t)q].flags & T_SCATTER) pb.T[(size_t)q].flags = T_ACCUM;
     }
-    for (auto &ph : h->phases) {
+    h->ph_op.assign(h->phases.size(), 0);
+    h->ph_vec.assign(h->phases.size(), 0);
+    for (size_t pi = 0; pi < h->phases.size(); ++pi) {
+        Phase &ph = h->phases[pi];
         int mx = 0;
-        for (int64_t q = ph.t0; q < ph.t1; ++q) mx = std::max(mx, pb.T[(size_t)q].xw);
+        for (int64_t q = ph.t0; q < ph.t1; ++q) {
+            const Target &tg = pb.T[(size_t)q];
+            mx = std::max(mx, tg.xw);
+            h->ph_vec[pi] += (int64_t)tg.nrows * ((tg.flags & (T_ACCUM | T_ATOMIC)) ? 2 : 1);
+            for (int32_t p = tg.p0; p < tg.p1; ++p) {
+                const Panel &pn = pb.P[(size_t)p];
+                h->ph_op[pi] += (int64_t)tg.nrows * pn.w;
+                for (int32_t e = pn.s0; e < pn.s1; ++e) h->ph_vec[pi] += pb.S[(size_t)e].len;
+            }
+        }
         ph.max_xw = mx;
     }
     for (auto &x : pb.xfers)
@@ -1142,11 +1160,39 @@ double storage_entries(h2w_handle *h) {
 }
 
 // ---------------------------------------------------------- matvec run ---
+cudaEvent_t prof_event(h2w_handle *h) {
+    cudaEvent_t e;
+    if (!h->ev_pool.empty()) {
+        e = h->ev_pool.back();
+        h->ev_pool.pop_back();
+    } else {
+        CK(cudaEventCreate(&e));
+    }
+    return e;
+}
+
+template <class F>
+void prof_launch(h2w_handle *h, int prec, int phase, cudaStream_t st, F &&launch) {
+    if (!h->prof || h->phases[(size_t)phase].t1 <= h->phases[(size_t)phase].t0) {
+        CK(launch());
+        return;
+    }
+    h2w_handle::ProfRec r{prof_event(h), prof_event(h), prec, phase};
+    CK(cudaEventRecord(r.a, st));
+    CK(launch());
+    CK(cudaEventRecord(r.b, st));
+    h->prof_recs.push_back(r);
+}
+
 void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st) {
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
-    for (const Phase &ph : h->phases)
-        CK(launch_brg_f64(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op.p, h->d_ws.p, dx, dy,
-                          h->d_perm.p, st));
+    for (size_t q = 0; q < h->phases.size(); ++q) {
+        const Phase &ph = h->phases[q];
+        prof_launch(h, H2W_PREC_FP64, (int)q, st, [&] {
+            return launch_brg_f64(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op.p, h->d_ws.p, dx,
+                                  dy, h->d_perm.p, st);
+        });
+    }
     if (!h->fused_scatter) CK(launch_scatter_f64(h->d_ws.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
 }
 
@@ -1162,9 +1208,13 @@ void ensure_f32(h2w_handle *h) {
 
 void run_matvec_f32(h2w_handle *h, const float *dx, float *dy, cudaStream_t st) {
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
-    for (const Phase &ph : h->phases)
-        CK(launch_brg_f32(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op32.p, h->d_ws32.p, dx, dy,
-                          h->d_perm.p, st));
+    for (size_t q = 0; q < h->phases.size(); ++q) {
+        const Phase &ph = h->phases[q];
+        prof_launch(h, H2W_PREC_FP32, (int)q, st, [&] {
+            return launch_brg_f32(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op32.p, h->d_ws32.p,
+                                  dx, dy, h->d_perm.p, st);
+        });
+    }
     if (!h->fused_scatter) CK(launch_scatter_f32(h->d_ws32.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
 }
 
@@ -1351,6 +1401,11 @@ int h2w_destroy(h2w_handle *h) {
     if (!h) return H2W_OK;
     if (h->cfg.device >= 0) cudaSetDevice(h->cfg.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto &r : h->prof_recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
     cudaStream_t st = h->stream;
     delete h;
     if (st) cudaStreamDestroy(st);
@@ -1748,6 +1803,47 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         return rc;
     });
 }
+
+int h2w_profile(h2w_handle *h, int enable) {
+    return guarded(h, [&] {
+        if (h->cfg.device < 0) throw ApiError(H2W_ERR_STATE, "host-only handle");
+        CK(cudaStreamSynchronize(h->stream));
+        for (auto &r : h->prof_recs) {
+            h->ev_pool.push_back(r.a);
+            h->ev_pool.push_back(r.b);
+        }
+        h->prof_recs.clear();
+        h->prof = enable != 0;
+        return H2W_OK;
+    });
+}
+
+int h2w_profile_phases(h2w_handle *h, int precision, int max_phases, int64_t *launches, double *ms, double *bytes,
+                       int *nphases) {
+    return guarded(h, [&] {
+        require_op(h);
+        const int np = (int)h->phases.size();
+        if (nphases) *nphases = np;
+        if (!launches || !ms || !bytes) return H2W_OK;
+        CK(cudaDeviceSynchronize());
+        const double w = precision == H2W_PREC_FP32 ? 4.0 : 8.0;
+        for (int q = 0; q < std::min(np, max_phases); ++q) {
+            launches[q] = 0;
+            ms[q] = 0.0;
+            bytes[q] = (double)(h->ph_op[(size_t)q] + h->ph_vec[(size_t)q]) * w;
+        }
+        for (auto &r : h->prof_recs) {
+            if (r.prec != precision || r.phase >= max_phases) continue;
+            float t = 0.f;
+            CK(cudaEventElapsedTime(&t, r.a, r.b));
+            launches[r.phase] += 1;
+            ms[r.phase] += (double)t;
+        }
+        return H2W_OK;
+    });
+}
+
+int64_t h2w_launch_count(void) { return launch_count(); }
 
 int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, int64_t nrows, int where) {
     return guarded(h, [&] {

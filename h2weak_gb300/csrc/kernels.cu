@@ -11,12 +11,17 @@
 //  * brg_kernel        the matvec: block-row GEMV over a work list of targets,
 //                      each the sum of row-major panels times gathered sources
 //  * GMRES kernels     CGS2 Arnoldi step, normalisation, Givens rotations
+#include <atomic>
 #include <cfloat>
 #include <climits>
 
 #include "kernels.cuh"
 
 namespace h2w {
+
+static std::atomic<int64_t> g_launches{0};
+int64_t launch_count() { return g_launches.load(); }
+void count_launch(int64_t n) { g_launches.fetch_add(n); }
 
 // ------------------------------------------------------------ entries ---
 __device__ __forceinline__ double kentry(const KParams &k, int i, int j) {
@@ -301,7 +306,7 @@ cudaError_t launch_nca(const NcaProb *probs, int nprob, const int32_t *idx, cons
     if (e != cudaSuccess) return e;
     nca_kernel<<<nprob, NCA_THREADS, smem, st>>>(probs, idx, kp, tol, scratch, rank, prow, pcol, status, m1, m2,
                                                  coef_len);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 
 // ------------------------------------------------------------- factors ---
@@ -340,7 +345,7 @@ cudaError_t launch_factor(const FactorJob *jobs, int njobs, const int32_t *idx, 
                           cudaStream_t st) {
     if (njobs == 0) return cudaSuccess;
     factor_kernel<<<njobs, 128, 0, st>>>(jobs, idx, kp, F);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 
 // ----------------------------------------------------------- transfers ---
@@ -404,6 +409,7 @@ cudaError_t launch_xfer(const XferJob *jobs, int njobs, int max_n, const int32_t
         int nj = njobs - j0 < 65535 ? njobs - j0 : 65535;
         dim3 grid((unsigned)((max_n + bs - 1) / bs), (unsigned)nj);
         xfer_kernel<<<grid, bs, 0, st>>>(jobs + j0, idx, kp, F, op);
+        count_launch();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -429,6 +435,7 @@ cudaError_t launch_fill(const FillJob *jobs, int njobs, const int32_t *idx, cons
         int nj = njobs - j0 < 65535 ? njobs - j0 : 65535;
         dim3 grid(8, (unsigned)nj);
         fill_kernel<<<grid, 256, 0, st>>>(jobs + j0, idx, kp, op);
+        count_launch();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -442,7 +449,7 @@ __global__ void convert_f32_kernel(const double *__restrict__ s, float *__restri
 cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     convert_f32_kernel<<<1216, 256, 0, st>>>(src, dst, n);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 
 // ------------------------------------------------------- block-row GEMV ---
@@ -540,6 +547,7 @@ static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, 
     for (int64_t b = t0; b < t1; b += 2147483647LL) {
         int64_t nb = t1 - b < 2147483647LL ? t1 - b : 2147483647LL;
         brg_kernel<T><<<(unsigned)nb, BRG_THREADS, smem, st>>>(Tg, P, S, b, A, ws, xin, yout, perm);
+        if (nb > 0) count_launch();
     }
     return cudaGetLastError();
 }
@@ -562,11 +570,11 @@ __global__ void scatter_kernel(const T *__restrict__ yp, T *__restrict__ y, cons
 }
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st) {
     scatter_kernel<double><<<608, 256, 0, st>>>(yp, y, perm, n);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 cudaError_t launch_scatter_f32(const float *yp, float *y, const int32_t *perm, int64_t n, cudaStream_t st) {
     scatter_kernel<float><<<608, 256, 0, st>>>(yp, y, perm, n);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 
 // -------------------------------------------------------- dense oracle ---
@@ -584,6 +592,7 @@ cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, d
     for (int64_t b = 0; b < nrows; b += 2147483647LL) {
         int64_t nb = nrows - b < 2147483647LL ? nrows - b : 2147483647LL;
         dense_kernel<<<(unsigned)nb, 256, 0, st>>>(kp, N, x, y + b, row0 + b);
+        count_launch();
     }
     return cudaGetLastError();
 }
@@ -738,13 +747,13 @@ cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st) {
     gm_dots<<<g.nblk, GM_THREADS, sm_dots, st>>>(g);
     gm_update<<<g.nblk, GM_THREADS, sm_upd, st>>>(g, 0);
     gm_update<<<g.nblk, GM_THREADS, sm_upd, st>>>(g, 1);
-    return cudaGetLastError();
+    count_launch(3); return cudaGetLastError();
 }
 
 cudaError_t gmres_finish_iter(const GmresDev &g, double tol, cudaStream_t st) {
     gm_normalise<<<g.nblk, GM_THREADS, 0, st>>>(g);
     gm_givens<<<1, 1, 0, st>>>(g, tol);
-    return cudaGetLastError();
+    count_launch(2); return cudaGetLastError();
 }
 
 // r = b - Ax; beta = ||r||; V[:,0] = vcur = r / beta; s = beta e1; iter = 0
@@ -790,7 +799,7 @@ __global__ void gm_start_fin(GmresDev g, double normb) {
 cudaError_t gmres_start(const GmresDev &g, const double *b, const double *Ax, double normb, cudaStream_t st) {
     gm_resid_part<<<g.nblk, GM_THREADS, 0, st>>>(g, b, Ax);
     gm_start_fin<<<g.nblk, GM_THREADS, 0, st>>>(g, normb);
-    return cudaGetLastError();
+    count_launch(2); return cudaGetLastError();
 }
 
 // x += sum_{j<=k} V[:,j] y[j]  (y precomputed by the back-substitution, in g.s)
@@ -803,7 +812,7 @@ __global__ void gm_xupdate(GmresDev g, double *__restrict__ x, const double *__r
 }
 cudaError_t gmres_update(const GmresDev &g, double *x, const double *y, int k, cudaStream_t st) {
     gm_xupdate<<<g.nblk, GM_THREADS, 0, st>>>(g, x, y, k);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 
 __global__ void norm_part(const double *__restrict__ x, int64_t n, double *part) {
@@ -822,7 +831,7 @@ __global__ void norm_fin(const double *part, int nblk, double *out) {
 cudaError_t vec_norm(const double *x, int64_t n, double *part, int nblk, double *out, cudaStream_t st) {
     norm_part<<<nblk, GM_THREADS, 0, st>>>(x, n, part);
     norm_fin<<<1, 1, 0, st>>>(part, nblk, out);
-    return cudaGetLastError();
+    count_launch(2); return cudaGetLastError();
 }
 
 __global__ void axpby_kernel(double a, const double *x, double b, const double *y, double *z, int64_t n) {
@@ -831,7 +840,7 @@ __global__ void axpby_kernel(double a, const double *x, double b, const double *
 }
 cudaError_t vec_axpby(double a, const double *x, double b, const double *y, double *z, int64_t n, cudaStream_t st) {
     axpby_kernel<<<608, 256, 0, st>>>(a, x, b, y, z, n);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 __global__ void d2f_kernel(const double *x, float *y, int64_t n) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
@@ -843,11 +852,11 @@ __global__ void f2d_kernel(const float *x, double *y, int64_t n) {
 }
 cudaError_t vec_f64_to_f32(const double *x, float *y, int64_t n, cudaStream_t st) {
     d2f_kernel<<<608, 256, 0, st>>>(x, y, n);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 cudaError_t vec_f32_to_f64(const float *x, double *y, int64_t n, cudaStream_t st) {
     f2d_kernel<<<608, 256, 0, st>>>(x, y, n);
-    return cudaGetLastError();
+    count_launch(); return cudaGetLastError();
 }
 
 }  // namespace h2w

@@ -8,6 +8,10 @@
 
 namespace h2w {
 
+// Number of kernel launches issued by this library (all kernels).
+int64_t launch_count();
+void count_launch(int64_t n = 1);
+
 // Kernel-matrix entry parameters (reference kernel.hpp getMatrixEntry).
 struct KParams {
     const double *pts;   // N*dim, original order

@@ -117,6 +117,19 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
 int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int inner_iter, int tol_pow, int where,
                  int *outer_iters, int *inner_total, double *resid);
 
+/* Launch statistics of the block-row GEMV kernel that performs every matvec
+ * pass. While enabled, each phase launch is bracketed by CUDA events on its
+ * own stream; enabling (or disabling) resets the record. (No counterpart in
+ * the reference, whose only instrumentation is clock() accumulators.) */
+int h2w_profile(h2w_handle *h, int enable);
+/* Per phase of one matvec: launches recorded, total device ms, and the
+ * algorithmic bytes one launch moves (operator panels + gathered sources +
+ * destination rows) at the given precision. nphases receives the count. */
+int h2w_profile_phases(h2w_handle *h, int precision, int max_phases, int64_t *launches, double *ms, double *bytes,
+                       int *nphases);
+/* Kernel launches issued by this library since it was loaded. */
+int64_t h2w_launch_count(void);
+
 /* Dense FP64 product with the exact kernel matrix (getTruePoten,
  * 1D/codes/HODLR1Dtree.hpp:590-604), on the GPU, rows [row0, row0 + nrows). */
 int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, int64_t nrows, int where);
