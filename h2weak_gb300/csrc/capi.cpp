@@ -64,7 +64,7 @@ template <class T> struct DBuf {
 inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
 
 constexpr int XW_CAP = 4096;          // gathered source width per target (elements)
-constexpr int64_t ROW_CHUNK = 32768;  // rows * width per target (elements)
+constexpr int64_t ROW_SPLIT = 262144;  // rows * width above which a target is split (load balance)
 
 }  // namespace
 
@@ -91,7 +91,8 @@ struct h2w_handle {
     DBuf<Panel> d_P;
     DBuf<Seg> d_S;
     DBuf<double> d_ws, d_x, d_y;
-    DBuf<float> d_ws32, d_x32, d_y32;
+    DBuf<int32_t> d_ctr, d_err;
+    DBuf<float> d_ws32;
     std::vector<Phase> phases;
     std::vector<int64_t> ph_op, ph_vec;   // per phase: operator and vector elements moved
     // launch profiling of the block-row GEMV (events bracket every phase launch)
@@ -547,7 +548,7 @@ struct PlanBuilder {
         for (auto &p : panels) read_elems += (int64_t)nrows * p.w;
         if (xw == 0) return;
         if (xw <= XW_CAP) {
-            int64_t rows_per = std::max<int64_t>(1, std::min<int64_t>(nrows, ROW_CHUNK / std::max<int64_t>(xw, 1)));
+            int64_t rows_per = std::max<int64_t>(1, std::min<int64_t>(nrows, ROW_SPLIT / std::max<int64_t>(xw, 1)));
             for (int64_t r0 = 0; r0 < nrows; r0 += rows_per) {
                 int32_t nr = (int32_t)std::min<int64_t>(rows_per, nrows - r0);
                 Target tg{};
@@ -570,6 +571,8 @@ struct PlanBuilder {
                 }
                 tg.p1 = (int32_t)P.size();
                 tg.xw = xo;
+                tg.ldsum = 0;
+                for (auto &p : panels) tg.ldsum += p.lda;
                 tg.gsz = xo >= 256 ? 32 : (xo >= 128 ? 16 : (xo >= 48 ? 8 : 4));
                 T.push_back(tg);
             }
@@ -633,6 +636,9 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
             xw += pad4(p.w);
         }
         if (xw != t.xw || xw > XW_CAP) bad("target width");
+        int64_t ls = 0;
+        for (int32_t q = t.p0; q < t.p1; ++q) ls += pb.P[(size_t)q].lda;
+        if (ls != t.ldsum || ls < 1 || ls > BRG_BUF_ELEMS_F64) bad("target leading dimensions");
     }
     for (const FactorJob &f : pb.factors)
         if (f.r < 1 || f.f < 0 || f.f + (int64_t)f.r * f.r > pb.fn || f.ii < 0 || f.ii + f.r > nidx || f.jj < 0 ||
@@ -1037,6 +1043,10 @@ void build_plan(h2w_handle *h) {
             for (int64_t q = lp.t0; q < lp.t1; ++q)
                 if (pb.T[(size_t)q].flags & T_SCATTER) pb.T[(size_t)q].flags = T_ACCUM;
     }
+    for (auto &ph : h->phases)
+        std::stable_sort(pb.T.begin() + ph.t0, pb.T.begin() + ph.t1, [](const Target &a, const Target &b) {
+            return (int64_t)a.nrows * a.ldsum > (int64_t)b.nrows * b.ldsum;
+        });
     h->ph_op.assign(h->phases.size(), 0);
     h->ph_vec.assign(h->phases.size(), 0);
     for (size_t pi = 0; pi < h->phases.size(); ++pi) {
@@ -1082,6 +1092,9 @@ void build_plan(h2w_handle *h) {
     h->d_P.upload(pb.P, st);
     h->d_S.upload(pb.S, st);
     h->d_ws.alloc((size_t)h->ws_n);
+    h->d_ctr.alloc(h->phases.size() + 1);
+    h->d_err.alloc(1);
+    CK(cudaMemsetAsync(h->d_err.p, 0, 4, st));
     CK(cudaStreamSynchronize(st));
     h->d_op32.reset();
     h->d_ws32.reset();
@@ -1186,11 +1199,12 @@ void prof_launch(h2w_handle *h, int prec, int phase, cudaStream_t st, F &&launch
 
 void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st) {
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
+    CK(cudaMemsetAsync(h->d_ctr.p, 0, h->d_ctr.n * 4, st));
     for (size_t q = 0; q < h->phases.size(); ++q) {
         const Phase &ph = h->phases[q];
         prof_launch(h, H2W_PREC_FP64, (int)q, st, [&] {
-            return launch_brg_f64(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op.p, h->d_ws.p, dx,
-                                  dy, h->d_perm.p, st);
+            return launch_brg_f64(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, h->d_ctr.p + q, h->d_op.p, h->d_ws.p,
+                                  dx, dy, h->d_perm.p, h->d_err.p, st);
         });
     }
     if (!h->fused_scatter) CK(launch_scatter_f64(h->d_ws.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
@@ -1201,18 +1215,20 @@ void ensure_f32(h2w_handle *h) {
     h->d_op32.alloc((size_t)h->op_n);
     CK(launch_convert_f32(h->d_op.p, h->d_op32.p, h->op_n, h->stream));
     h->d_ws32.alloc((size_t)h->ws_n);
-    h->d_x32.alloc((size_t)h->tree.N);
-    h->d_y32.alloc((size_t)h->tree.N);
     CK(cudaStreamSynchronize(h->stream));
 }
 
-void run_matvec_f32(h2w_handle *h, const float *dx, float *dy, cudaStream_t st) {
+// FP32 operator and workspace; x and y stay FP64 in original order (the
+// conversions happen in the kernel's gather and scatter).
+void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st) {
+    ensure_f32(h);
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
+    CK(cudaMemsetAsync(h->d_ctr.p, 0, h->d_ctr.n * 4, st));
     for (size_t q = 0; q < h->phases.size(); ++q) {
         const Phase &ph = h->phases[q];
         prof_launch(h, H2W_PREC_FP32, (int)q, st, [&] {
-            return launch_brg_f32(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, ph.max_xw, h->d_op32.p, h->d_ws32.p,
-                                  dx, dy, h->d_perm.p, st);
+            return launch_brg_f32(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, h->d_ctr.p + q, h->d_op32.p,
+                                  h->d_ws32.p, dx, dy, h->d_perm.p, h->d_err.p, st);
         });
     }
     if (!h->fused_scatter) CK(launch_scatter_f32(h->d_ws32.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
@@ -1289,14 +1305,8 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     cudaStream_t st = h->stream;
     const int64_t N = h->tree.N;
     auto A = [&](const double *in, double *out) {
-        if (prec == H2W_PREC_FP32) {
-            ensure_f32(h);
-            CK(vec_f64_to_f32(in, h->d_x32.p, N, st));
-            run_matvec_f32(h, h->d_x32.p, h->d_y32.p, st);
-            CK(vec_f32_to_f64(h->d_y32.p, out, N, st));
-        } else {
-            run_matvec_f64(h, in, out, st);
-        }
+        if (prec == H2W_PREC_FP32) run_matvec_f32(h, in, out, st);
+        else run_matvec_f64(h, in, out, st);
     };
     double normb = dnorm(h, db);
     if (normb == 0.0) normb = 1;
@@ -1330,6 +1340,17 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     *resid = dnorm(h, h->g_r.p) / normb;
     *iters = max_iter;
     return *resid < tol ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+}
+
+// Device-side failure flag of the matvec kernel (a bounded wait that ran out).
+void check_device_error(h2w_handle *h) {
+    int32_t e = 0;
+    CK(cudaMemcpyAsync(&e, h->d_err.p, 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (e) {
+        CK(cudaMemsetAsync(h->d_err.p, 0, 4, h->stream));
+        throw ApiError(H2W_ERR_CUDA, "matvec kernel: a shared-memory staging wait ran out (device error flag)");
+    }
 }
 
 int fail(h2w_handle *h, int code, const std::string &m) {
@@ -1712,16 +1733,16 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
                 dy = h->d_y.p;
             }
             if (precision == H2W_PREC_FP32) {
-                ensure_f32(h);
-                CK(vec_f64_to_f32(dx, h->d_x32.p, N, st));
-                run_matvec_f32(h, h->d_x32.p, h->d_y32.p, st);
-                CK(vec_f32_to_f64(h->d_y32.p, dy, N, st));
+                run_matvec_f32(h, dx, dy, st);
             } else {
                 run_matvec_f64(h, dx, dy, st);
             }
             if (where == H2W_HOST) CK(cudaMemcpyAsync(yc, h->d_y.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
         }
-        if (where == H2W_HOST) CK(cudaStreamSynchronize(st));
+        if (where == H2W_HOST) {
+            CK(cudaStreamSynchronize(st));
+            check_device_error(h);
+        }
         return H2W_OK;
     });
 }
@@ -1744,6 +1765,7 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
             dx = h->d_x.p;
         }
         int rc = gmres_run(h, db, dx, max_iter, tol, H2W_PREC_FP64, iters, resid);
+        check_device_error(h);
         if (where == H2W_HOST) {
             CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream));
             CK(cudaStreamSynchronize(h->stream));
@@ -1800,6 +1822,7 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
             CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
         }
         CK(cudaStreamSynchronize(st));
+        check_device_error(h);
         return rc;
     });
 }

@@ -55,6 +55,7 @@ enum : int32_t { S_WS = 0, S_GATHER = 1 };
 struct Target {
     int64_t dst;
     int32_t nrows, flags, p0, p1, gsz, xw;  // panels [p0,p1), lanes per row, gathered width
+    int32_t ldsum, pad;                      // sum of the panels' leading dimensions
 };
 struct Panel {
     int64_t a;

@@ -453,127 +453,246 @@ cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStr
 }
 
 // ------------------------------------------------------- block-row GEMV ---
-// One CTA per target. The gathered sources of all panels are staged in
-// shared memory; rows are distributed over lane groups of gsz lanes, each
-// lane streaming 16-byte (FP64: 2, FP32: 4 elements) chunks of the row-major
-// panel rows, reduced with xor shuffles inside the group.
+// Persistent, dynamically scheduled block-row GEMV. Each CTA repeatedly
+// claims a target (atomic counter per launch), streams the target's panel
+// rows through two shared-memory buffers with cp.async.bulk (completion
+// tracked by an mbarrier per buffer, so the next chunk is in flight while
+// the current one is multiplied), and gathers the target's sources once
+// into a double-buffered source area. Rows are reduced by groups of gsz
+// lanes with 16-byte shared-memory reads.
 constexpr int BRG_THREADS = 256;
+constexpr int BRG_BUF_BYTES = 65536;   // per panel buffer
+constexpr int BRG_XS_ELEMS = 4096;     // per source buffer (elements)
+constexpr long long BRG_WAIT_LIMIT = 1LL << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// bounded wait; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (long long it = 0; it < BRG_WAIT_LIMIT; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
 
 template <class T> struct Vec16;
 template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
 template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
 
-template <class T>
-__device__ __forceinline__ T dot16(const typename Vec16<T>::type a, const T *x);
-template <>
-__device__ __forceinline__ double dot16<double>(const double2 a, const double *x) {
-    return a.x * x[0] + a.y * x[1];
-}
-template <>
-__device__ __forceinline__ float dot16<float>(const float4 a, const float *x) {
-    return a.x * x[0] + a.y * x[1] + a.z * x[2] + a.w * x[3];
+__device__ __forceinline__ double dot16(const double2 a, const double2 x) { return a.x * x.x + a.y * x.y; }
+__device__ __forceinline__ float dot16(const float4 a, const float4 x) {
+    return a.x * x.x + a.y * x.y + a.z * x.z + a.w * x.w;
 }
 
 template <class T>
-__global__ void __launch_bounds__(BRG_THREADS) brg_kernel(const Target *__restrict__ Tg, const Panel *__restrict__ Pn,
-                                                         const Seg *__restrict__ Sg, int64_t t0,
-                                                         const T *__restrict__ A, T *ws, const T *__restrict__ xin,
-                                                         T *yout, const int32_t *__restrict__ perm) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *xs = reinterpret_cast<T *>(smem_raw);
+__global__ void __launch_bounds__(BRG_THREADS, 1)
+    brg_kernel(const Target *__restrict__ Tg, const Panel *__restrict__ Pn, const Seg *__restrict__ Sg, int64_t t0,
+               int64_t t1, int32_t *ctr, const T *__restrict__ A, T *ws, const double *__restrict__ xin,
+               double *yout, const int32_t *__restrict__ perm, int32_t *err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int BUF = BRG_BUF_BYTES / (int)sizeof(T);
     using V16 = typename Vec16<T>::type;
     constexpr int VN = Vec16<T>::n;
-    const Target tg = Tg[t0 + blockIdx.x];
-    for (int p = tg.p0; p < tg.p1; ++p) {
-        const Panel pn = Pn[p];
-        for (int s = pn.s0; s < pn.s1; ++s) {
-            const Seg sg = Sg[s];
-            T *dst = xs + pn.xoff + sg.xoff;
-            if (sg.flags & S_GATHER)
-                for (int c = threadIdx.x; c < sg.len; c += blockDim.x) dst[c] = xin[perm[sg.src + c]];
-            else
-                for (int c = threadIdx.x; c < sg.len; c += blockDim.x) dst[c] = ws[sg.src + c];
-        }
+    T *bufs = reinterpret_cast<T *>(smem_raw);
+    T *xsb = bufs + 2 * BUF;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int64_t s_t[2];
+    __shared__ int s_r0[2], s_nr[2], s_xs[2];
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
     }
+    fence_proxy_async();
     __syncthreads();
-    const int g = tg.gsz;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int sub = lane / g, gl = lane % g;
-    const int rpw = 32 / g, step = (BRG_THREADS / 32) * rpw;
-    for (int ib = warp * rpw; ib < tg.nrows; ib += step) {
-        const int i = ib + sub;
-        T acc = T(0);
-        if (i < tg.nrows) {
-            for (int p = tg.p0; p < tg.p1; ++p) {
-                const Panel pn = Pn[p];
-                const T *row = A + pn.a + (int64_t)i * pn.lda;
-                const T *xp = xs + pn.xoff;
-                const int wfull = (pn.w / VN) * VN;
-                for (int c = gl * VN; c < wfull; c += g * VN) {
-                    V16 a = *reinterpret_cast<const V16 *>(row + c);
-                    acc += dot16<T>(a, xp + c);
+
+    // chunk generator (thread 0 only)
+    int64_t gt = -1;
+    int gr = 0, gR = 0, gn = 0, gx = 1;
+    auto next_chunk = [&](int b) {
+        if (gt >= 0 && gr + gR < gn) {
+            gr += gR;
+        } else {
+            int64_t q = t0 + (int64_t)atomicAdd(ctr, 1);
+            if (q >= t1) {
+                s_t[b] = -1;
+                return;
+            }
+            gt = q;
+            gr = 0;
+            gn = Tg[q].nrows;
+            int ls = Tg[q].ldsum;
+            gR = BUF / (ls > 0 ? ls : 1);
+            if (gR < 1) gR = 1;
+            gx ^= 1;
+        }
+        const Target tg = Tg[gt];
+        const int nr = gn - gr < gR ? gn - gr : gR;
+        s_t[b] = gt;
+        s_r0[b] = gr;
+        s_nr[b] = nr;
+        s_xs[b] = gx;
+        mbar_expect_tx(&mbar[b], (uint32_t)((int64_t)nr * tg.ldsum * (int64_t)sizeof(T)));
+        int64_t off = 0;
+        for (int p = tg.p0; p < tg.p1; ++p) {
+            const Panel pn = Pn[p];
+            const uint32_t bytes = (uint32_t)((int64_t)nr * pn.lda * (int64_t)sizeof(T));
+            bulk_g2s(bufs + b * BUF + off, A + pn.a + (int64_t)gr * pn.lda, bytes, &mbar[b]);
+            off += (int64_t)nr * pn.lda;
+        }
+    };
+    auto gather = [&](int64_t t, int xsel) {
+        const Target tg = Tg[t];
+        T *xs = xsb + xsel * BRG_XS_ELEMS;
+        for (int p = tg.p0; p < tg.p1; ++p) {
+            const Panel pn = Pn[p];
+            for (int sidx = pn.s0; sidx < pn.s1; ++sidx) {
+                const Seg sg = Sg[sidx];
+                T *dst = xs + pn.xoff + sg.xoff;
+                if (sg.flags & S_GATHER)
+                    for (int c = tid; c < sg.len; c += BRG_THREADS) dst[c] = (T)xin[perm[sg.src + c]];
+                else
+                    for (int c = tid; c < sg.len; c += BRG_THREADS) dst[c] = ws[sg.src + c];
+            }
+        }
+    };
+
+    if (tid == 0) next_chunk(0);
+    __syncthreads();
+    if (s_t[0] < 0) return;
+    gather(s_t[0], s_xs[0]);
+    uint32_t ph0 = 0, ph1 = 0;
+    int b = 0;
+    const int lane = tid & 31, warp = tid >> 5;
+    while (true) {
+        if (tid == 0) next_chunk(b ^ 1);
+        __syncthreads();
+        const bool nv = s_t[b ^ 1] >= 0;
+        if (nv && s_r0[b ^ 1] == 0) gather(s_t[b ^ 1], s_xs[b ^ 1]);
+        const bool ok = mbar_wait(&mbar[b], b ? ph1 : ph0);
+        if (b) ph1 ^= 1; else ph0 ^= 1;
+        if (__syncthreads_or(!ok)) {  // uniform: every thread leaves together
+            if (tid == 0) atomicExch(err, 1);
+            if (nv) mbar_wait(&mbar[b ^ 1], b ? ph0 : ph1);
+            return;
+        }
+        {
+            const Target tg = Tg[s_t[b]];
+            const int r0 = s_r0[b], nr = s_nr[b];
+            const T *xs = xsb + s_xs[b] * BRG_XS_ELEMS;
+            const T *buf = bufs + b * BUF;
+            const int g = tg.gsz;
+            const int sub = lane / g, gl = lane % g;
+            const int rpw = 32 / g, step = (BRG_THREADS / 32) * rpw;
+            for (int ib = warp * rpw; ib < nr; ib += step) {
+                const int i = ib + sub;
+                T acc = T(0);
+                if (i < nr) {
+                    int64_t poff = 0;
+                    for (int p = tg.p0; p < tg.p1; ++p) {
+                        const Panel pn = Pn[p];
+                        const T *row = buf + poff + (int64_t)i * pn.lda;
+                        const T *xp = xs + pn.xoff;
+                        const int wfull = (pn.w / VN) * VN;
+                        for (int c = gl * VN; c < wfull; c += g * VN)
+                            acc += dot16(*reinterpret_cast<const V16 *>(row + c), *reinterpret_cast<const V16 *>(xp + c));
+                        for (int c = wfull + gl; c < pn.w; c += g) acc += row[c] * xp[c];
+                        poff += (int64_t)nr * pn.lda;
+                    }
                 }
-                for (int c = wfull + gl; c < pn.w; c += g) acc += row[c] * xp[c];
+                for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (i < nr && gl == 0) {
+                    const int64_t d = tg.dst + r0 + i;
+                    if (tg.flags & T_SCATTER) {
+                        T v = (tg.flags & T_ACCUM) ? ws[d] + acc : acc;
+                        yout[perm[d]] = (double)v;
+                    } else if (tg.flags & T_ATOMIC) {
+                        atomicAdd(ws + d, acc);
+                    } else if (tg.flags & T_ACCUM) {
+                        ws[d] += acc;
+                    } else {
+                        ws[d] = acc;
+                    }
+                }
             }
         }
-        for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (i < tg.nrows && gl == 0) {
-            const int64_t d = tg.dst + i;
-            if (tg.flags & T_SCATTER) {
-                T v = (tg.flags & T_ACCUM) ? ws[d] + acc : acc;
-                yout[perm[d]] = v;
-            } else if (tg.flags & T_ATOMIC) {
-                atomicAdd(ws + d, acc);
-            } else if (tg.flags & T_ACCUM) {
-                ws[d] += acc;
-            } else {
-                ws[d] = acc;
-            }
-        }
+        __syncthreads();
+        fence_proxy_async();
+        if (!nv) break;
+        b ^= 1;
     }
 }
 
+static int g_num_sms = 0;
+
 template <class T>
-static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
-                                const T *A, T *ws, const T *xin, T *yout, const int32_t *perm, cudaStream_t st) {
+static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
+                                const T *A, T *ws, const double *xin, double *yout, const int32_t *perm, int32_t *err,
+                                cudaStream_t st) {
     if (t1 <= t0) return cudaSuccess;
-    size_t smem = (size_t)(max_xw > 0 ? max_xw : 1) * sizeof(T);
+    const size_t smem = 2 * (size_t)BRG_BUF_BYTES + 2 * (size_t)BRG_XS_ELEMS * sizeof(T);
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(brg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaError_t e = cudaFuncSetAttribute(brg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    for (int64_t b = t0; b < t1; b += 2147483647LL) {
-        int64_t nb = t1 - b < 2147483647LL ? t1 - b : 2147483647LL;
-        brg_kernel<T><<<(unsigned)nb, BRG_THREADS, smem, st>>>(Tg, P, S, b, A, ws, xin, yout, perm);
-        if (nb > 0) count_launch();
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
     }
+    int64_t nt = t1 - t0;
+    int grid = (int)(nt < g_num_sms ? nt : g_num_sms);
+    brg_kernel<T><<<grid, BRG_THREADS, smem, st>>>(Tg, P, S, t0, t1, ctr, A, ws, xin, yout, perm, err);
+    count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
+cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
                            const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
-                           cudaStream_t st) {
-    return launch_brg_t<double>(T, P, S, t0, t1, max_xw, A, ws, xin, yout, perm, st);
+                           int32_t *err, cudaStream_t st) {
+    return launch_brg_t<double>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, err, st);
 }
-cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
-                           const float *A, float *ws, const float *xin, float *yout, const int32_t *perm,
-                           cudaStream_t st) {
-    return launch_brg_t<float>(T, P, S, t0, t1, max_xw, A, ws, xin, yout, perm, st);
+cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
+                           const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
+                           int32_t *err, cudaStream_t st) {
+    return launch_brg_t<float>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, err, st);
 }
 
 template <class T>
-__global__ void scatter_kernel(const T *__restrict__ yp, T *__restrict__ y, const int32_t *__restrict__ perm, int64_t n) {
+__global__ void scatter_kernel2(const T *__restrict__ yp, double *__restrict__ y, const int32_t *__restrict__ perm,
+                                int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        y[perm[i]] = yp[i];
+        y[perm[i]] = (double)yp[i];
 }
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st) {
-    scatter_kernel<double><<<608, 256, 0, st>>>(yp, y, perm, n);
+    scatter_kernel2<double><<<608, 256, 0, st>>>(yp, y, perm, n);
     count_launch(); return cudaGetLastError();
 }
-cudaError_t launch_scatter_f32(const float *yp, float *y, const int32_t *perm, int64_t n, cudaStream_t st) {
-    scatter_kernel<float><<<608, 256, 0, st>>>(yp, y, perm, n);
+cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st) {
+    scatter_kernel2<float><<<608, 256, 0, st>>>(yp, y, perm, n);
     count_launch(); return cudaGetLastError();
 }
 

@@ -42,15 +42,17 @@ cudaError_t launch_fill(const FillJob *jobs, int njobs, const int32_t *idx, cons
                         cudaStream_t st);
 cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStream_t st);
 
-// Matvec: one block-row GEMV launch over targets [t0, t1).
-cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
+// Matvec: one block-row GEMV launch over targets [t0, t1); ctr must be 0.
+// Sources and outputs in original point order are FP64 in both precisions.
+cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
                            const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
-                           cudaStream_t st);
-cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int max_xw,
-                           const float *A, float *ws, const float *xin, float *yout, const int32_t *perm,
-                           cudaStream_t st);
+                           int32_t *err, cudaStream_t st);
+cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
+                           const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
+                           int32_t *err, cudaStream_t st);
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
-cudaError_t launch_scatter_f32(const float *yp, float *y, const int32_t *perm, int64_t n, cudaStream_t st);
+cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
+constexpr int BRG_BUF_ELEMS_F64 = 65536 / 8;  // rows of a target are streamed in chunks of this many elements
 
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,
