@@ -623,7 +623,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
         for (int32_t q = t.p0; q < t.p1; ++q) {
             const Panel &p = pb.P[(size_t)q];
             if (p.a < 0 || p.a % 4 || p.lda % 4 || p.lda < p.w || p.w < 0) bad("panel layout");
-            if (p.a + (int64_t)(t.nrows - 1) * p.lda + p.w > opn) bad("panel extent");
+            if (p.a + (int64_t)(t.nrows - 1) * p.lda + pad4(p.w) > opn) bad("panel extent");
             if (p.xoff % 4 || p.xoff != xw) bad("panel xoff");
             if (p.s0 < 0 || p.s1 < p.s0 || p.s1 > (int32_t)pb.S.size()) bad("panel segs");
             for (int32_t e = p.s0; e < p.s1; ++e) {
@@ -638,7 +638,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
         if (xw != t.xw || xw > XW_CAP) bad("target width");
         int64_t ls = 0;
         for (int32_t q = t.p0; q < t.p1; ++q) ls += pb.P[(size_t)q].lda;
-        if (ls != t.ldsum || ls < 1 || ls > BRG_BUF_ELEMS_F64) bad("target leading dimensions");
+        if (ls != t.ldsum || ls < 1 || t.xw > BRG_SLOT_ELEMS_F64) bad("target leading dimensions");
     }
     for (const FactorJob &f : pb.factors)
         if (f.r < 1 || f.f < 0 || f.f + (int64_t)f.r * f.r > pb.fn || f.ii < 0 || f.ii + f.r > nidx || f.jj < 0 ||

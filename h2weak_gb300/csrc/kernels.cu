@@ -461,7 +461,6 @@ cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStr
 // into a double-buffered source area. Rows are reduced by groups of gsz
 // lanes with 16-byte shared-memory reads.
 constexpr int BRG_THREADS = 256;
-constexpr int BRG_BUF_BYTES = 65536;   // per panel buffer
 constexpr int BRG_XS_ELEMS = 4096;     // per source buffer (elements)
 constexpr long long BRG_WAIT_LIMIT = 1LL << 24;
 
@@ -504,142 +503,183 @@ __device__ __forceinline__ float dot16(const float4 a, const float4 x) {
     return a.x * x.x + a.y * x.y + a.z * x.z + a.w * x.w;
 }
 
+// Warp-specialised: warp 7 is the producer (claims targets with an atomic
+// counter, writes each chunk's metadata and issues its bulk copies into a
+// ring of BRG_SLOTS shared-memory slots, full/empty mbarriers per slot);
+// warps 0..6 consume chunks in order. Consumers gather a target's sources
+// into shared memory when its first chunk arrives, then reduce rows with
+// gsz-lane groups. Every wait is bounded; a wait that runs out sets *err and
+// the warp leaves its loop (the others then run out too).
+constexpr int BRG_SLOTS = 4;
+constexpr int BRG_SLOT_BYTES = 32768;
+constexpr int BRG_CONSUMERS = 7;
+
+struct ChunkMeta {
+    int64_t t;     // target index, -1 = end of stream
+    int32_t r0, nr;
+};
+
 template <class T>
 __global__ void __launch_bounds__(BRG_THREADS, 1)
     brg_kernel(const Target *__restrict__ Tg, const Panel *__restrict__ Pn, const Seg *__restrict__ Sg, int64_t t0,
                int64_t t1, int32_t *ctr, const T *__restrict__ A, T *ws, const double *__restrict__ xin,
                double *yout, const int32_t *__restrict__ perm, int32_t *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    constexpr int BUF = BRG_BUF_BYTES / (int)sizeof(T);
+    constexpr int SLOT = BRG_SLOT_BYTES / (int)sizeof(T);
     using V16 = typename Vec16<T>::type;
     constexpr int VN = Vec16<T>::n;
-    T *bufs = reinterpret_cast<T *>(smem_raw);
-    T *xsb = bufs + 2 * BUF;
-    __shared__ __align__(8) uint64_t mbar[2];
-    __shared__ int64_t s_t[2];
-    __shared__ int s_r0[2], s_nr[2], s_xs[2];
-    const int tid = threadIdx.x;
+    T *slots = reinterpret_cast<T *>(smem_raw);
+    T *xs = slots + BRG_SLOTS * SLOT;
+    __shared__ __align__(8) uint64_t full[BRG_SLOTS], empty[BRG_SLOTS];
+    __shared__ ChunkMeta meta[BRG_SLOTS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int q = 0; q < BRG_SLOTS; ++q) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], BRG_CONSUMERS);
+        }
     }
     fence_proxy_async();
     __syncthreads();
 
-    // chunk generator (thread 0 only)
-    int64_t gt = -1;
-    int gr = 0, gR = 0, gn = 0, gx = 1;
-    auto next_chunk = [&](int b) {
-        if (gt >= 0 && gr + gR < gn) {
-            gr += gR;
-        } else {
+    if (warp == BRG_CONSUMERS) {
+        // ---------------- producer ----------------
+        if (lane != 0) return;
+        int64_t k = 0;
+        bool alive = true;
+        while (alive) {
             int64_t q = t0 + (int64_t)atomicAdd(ctr, 1);
-            if (q >= t1) {
-                s_t[b] = -1;
-                return;
+            const bool last = q >= t1;
+            int nrows = 0, R = 1;
+            Target tg{};
+            if (!last) {
+                tg = Tg[q];
+                nrows = tg.nrows;
+                R = SLOT / tg.xw;
+                if (R < 1) R = 1;
             }
-            gt = q;
-            gr = 0;
-            gn = Tg[q].nrows;
-            int ls = Tg[q].ldsum;
-            gR = BUF / (ls > 0 ? ls : 1);
-            if (gR < 1) gR = 1;
-            gx ^= 1;
-        }
-        const Target tg = Tg[gt];
-        const int nr = gn - gr < gR ? gn - gr : gR;
-        s_t[b] = gt;
-        s_r0[b] = gr;
-        s_nr[b] = nr;
-        s_xs[b] = gx;
-        mbar_expect_tx(&mbar[b], (uint32_t)((int64_t)nr * tg.ldsum * (int64_t)sizeof(T)));
-        int64_t off = 0;
-        for (int p = tg.p0; p < tg.p1; ++p) {
-            const Panel pn = Pn[p];
-            const uint32_t bytes = (uint32_t)((int64_t)nr * pn.lda * (int64_t)sizeof(T));
-            bulk_g2s(bufs + b * BUF + off, A + pn.a + (int64_t)gr * pn.lda, bytes, &mbar[b]);
-            off += (int64_t)nr * pn.lda;
-        }
-    };
-    auto gather = [&](int64_t t, int xsel) {
-        const Target tg = Tg[t];
-        T *xs = xsb + xsel * BRG_XS_ELEMS;
-        for (int p = tg.p0; p < tg.p1; ++p) {
-            const Panel pn = Pn[p];
-            for (int sidx = pn.s0; sidx < pn.s1; ++sidx) {
-                const Seg sg = Sg[sidx];
-                T *dst = xs + pn.xoff + sg.xoff;
-                if (sg.flags & S_GATHER)
-                    for (int c = tid; c < sg.len; c += BRG_THREADS) dst[c] = (T)xin[perm[sg.src + c]];
-                else
-                    for (int c = tid; c < sg.len; c += BRG_THREADS) dst[c] = ws[sg.src + c];
-            }
-        }
-    };
-
-    if (tid == 0) next_chunk(0);
-    __syncthreads();
-    if (s_t[0] < 0) return;
-    gather(s_t[0], s_xs[0]);
-    uint32_t ph0 = 0, ph1 = 0;
-    int b = 0;
-    const int lane = tid & 31, warp = tid >> 5;
-    while (true) {
-        if (tid == 0) next_chunk(b ^ 1);
-        __syncthreads();
-        const bool nv = s_t[b ^ 1] >= 0;
-        if (nv && s_r0[b ^ 1] == 0) gather(s_t[b ^ 1], s_xs[b ^ 1]);
-        const bool ok = mbar_wait(&mbar[b], b ? ph1 : ph0);
-        if (b) ph1 ^= 1; else ph0 ^= 1;
-        if (__syncthreads_or(!ok)) {  // uniform: every thread leaves together
-            if (tid == 0) atomicExch(err, 1);
-            if (nv) mbar_wait(&mbar[b ^ 1], b ? ph0 : ph1);
-            return;
-        }
-        {
-            const Target tg = Tg[s_t[b]];
-            const int r0 = s_r0[b], nr = s_nr[b];
-            const T *xs = xsb + s_xs[b] * BRG_XS_ELEMS;
-            const T *buf = bufs + b * BUF;
-            const int g = tg.gsz;
-            const int sub = lane / g, gl = lane % g;
-            const int rpw = 32 / g, step = (BRG_THREADS / 32) * rpw;
-            for (int ib = warp * rpw; ib < nr; ib += step) {
-                const int i = ib + sub;
-                T acc = T(0);
-                if (i < nr) {
-                    int64_t poff = 0;
-                    for (int p = tg.p0; p < tg.p1; ++p) {
-                        const Panel pn = Pn[p];
-                        const T *row = buf + poff + (int64_t)i * pn.lda;
-                        const T *xp = xs + pn.xoff;
-                        const int wfull = (pn.w / VN) * VN;
-                        for (int c = gl * VN; c < wfull; c += g * VN)
-                            acc += dot16(*reinterpret_cast<const V16 *>(row + c), *reinterpret_cast<const V16 *>(xp + c));
-                        for (int c = wfull + gl; c < pn.w; c += g) acc += row[c] * xp[c];
-                        poff += (int64_t)nr * pn.lda;
-                    }
+            for (int r0 = 0; last ? r0 == 0 : r0 < nrows; r0 += R) {
+                const int sl = (int)(k % BRG_SLOTS);
+                if (k >= BRG_SLOTS && !mbar_wait(&empty[sl], (uint32_t)(((k / BRG_SLOTS) - 1) & 1))) {
+                    atomicExch(err, 1);
+                    alive = false;
+                    break;
                 }
-                for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (i < nr && gl == 0) {
-                    const int64_t d = tg.dst + r0 + i;
-                    if (tg.flags & T_SCATTER) {
-                        T v = (tg.flags & T_ACCUM) ? ws[d] + acc : acc;
-                        yout[perm[d]] = (double)v;
-                    } else if (tg.flags & T_ATOMIC) {
-                        atomicAdd(ws + d, acc);
-                    } else if (tg.flags & T_ACCUM) {
-                        ws[d] += acc;
+                if (last) {
+                    meta[sl].t = -1;
+                    mbar_expect_tx(&full[sl], 0);
+                    alive = false;
+                    break;
+                }
+                const int nr = nrows - r0 < R ? nrows - r0 : R;
+                meta[sl].t = q;
+                meta[sl].r0 = r0;
+                meta[sl].nr = nr;
+                mbar_expect_tx(&full[sl], (uint32_t)((int64_t)nr * tg.xw * (int64_t)sizeof(T)));
+                T *dst = slots + (int64_t)sl * SLOT;
+                for (int p = tg.p0; p < tg.p1; ++p) {
+                    const Panel pn = Pn[p];
+                    const int sp = (pn.w + 3) & ~3;
+                    const T *src = A + pn.a + (int64_t)r0 * pn.lda;
+                    if (pn.lda == sp) {
+                        bulk_g2s(dst, src, (uint32_t)((int64_t)nr * sp * (int64_t)sizeof(T)), &full[sl]);
                     } else {
-                        ws[d] = acc;
+                        for (int i = 0; i < nr; ++i)
+                            bulk_g2s(dst + (int64_t)i * sp, src + (int64_t)i * pn.lda, (uint32_t)(sp * sizeof(T)),
+                                     &full[sl]);
+                    }
+                    dst += (int64_t)nr * sp;
+                }
+                ++k;
+            }
+        }
+        return;
+    }
+
+    // ---------------- consumers ----------------
+    const int ctid = tid;  // 0 .. BRG_CONSUMERS*32-1
+    constexpr int NC = BRG_CONSUMERS * 32;
+    int64_t cur = -1;
+    for (int64_t k = 0;; ++k) {
+        const int sl = (int)(k % BRG_SLOTS);
+        const bool ok = mbar_wait(&full[sl], (uint32_t)((k / BRG_SLOTS) & 1));
+        uint32_t anyfail;
+        asm volatile(
+            "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 2, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+            : "=r"(anyfail)
+            : "r"((uint32_t)!ok), "n"(NC));
+        if (anyfail) {  // all consumers leave together
+            if (ctid == 0) atomicExch(err, 1);
+            break;
+        }
+        const ChunkMeta m = meta[sl];
+        if (m.t < 0) break;
+        const Target tg = Tg[m.t];
+        if (m.t != cur) {
+            asm volatile("bar.sync 1, %0;" ::"n"(NC));  // all consumers done with the previous sources
+            for (int p = tg.p0; p < tg.p1; ++p) {
+                const Panel pn = Pn[p];
+                for (int sidx = pn.s0; sidx < pn.s1; ++sidx) {
+                    const Seg sg = Sg[sidx];
+                    T *dst = xs + pn.xoff + sg.xoff;
+                    if (sg.flags & S_GATHER) {
+                        const int32_t *pp = perm + sg.src;
+                        int c = ctid;
+                        for (; c + 3 * NC < sg.len; c += 4 * NC) {
+                            int i0 = pp[c], i1 = pp[c + NC], i2 = pp[c + 2 * NC], i3 = pp[c + 3 * NC];
+                            double v0 = xin[i0], v1 = xin[i1], v2 = xin[i2], v3 = xin[i3];
+                            dst[c] = (T)v0;
+                            dst[c + NC] = (T)v1;
+                            dst[c + 2 * NC] = (T)v2;
+                            dst[c + 3 * NC] = (T)v3;
+                        }
+                        for (; c < sg.len; c += NC) dst[c] = (T)xin[pp[c]];
+                    } else {
+                        for (int c = ctid; c < sg.len; c += NC) dst[c] = ws[sg.src + c];
                     }
                 }
             }
+            asm volatile("bar.sync 1, %0;" ::"n"(NC));
+            cur = m.t;
         }
-        __syncthreads();
-        fence_proxy_async();
-        if (!nv) break;
-        b ^= 1;
+        const T *buf = slots + (int64_t)sl * SLOT;
+        const int g = tg.gsz;
+        const int sub = lane / g, gl = lane % g;
+        const int rpw = 32 / g, step = BRG_CONSUMERS * rpw;
+        for (int ib = warp * rpw; ib < m.nr; ib += step) {
+            const int i = ib + sub;
+            T acc = T(0);
+            if (i < m.nr) {
+                const T *pbuf = buf;
+                for (int p = tg.p0; p < tg.p1; ++p) {
+                    const Panel pn = Pn[p];
+                    const int sp = (pn.w + 3) & ~3;
+                    const T *row = pbuf + (int64_t)i * sp;
+                    const T *xp = xs + pn.xoff;
+                    const int wfull = (pn.w / VN) * VN;
+                    for (int c = gl * VN; c < wfull; c += g * VN)
+                        acc += dot16(*reinterpret_cast<const V16 *>(row + c), *reinterpret_cast<const V16 *>(xp + c));
+                    for (int c = wfull + gl; c < pn.w; c += g) acc += row[c] * xp[c];
+                    pbuf += (int64_t)m.nr * sp;
+                }
+            }
+            for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (i < m.nr && gl == 0) {
+                const int64_t d = tg.dst + m.r0 + i;
+                if (tg.flags & T_SCATTER) {
+                    T v = (tg.flags & T_ACCUM) ? ws[d] + acc : acc;
+                    yout[perm[d]] = (double)v;
+                } else if (tg.flags & T_ATOMIC) {
+                    atomicAdd(ws + d, acc);
+                } else if (tg.flags & T_ACCUM) {
+                    ws[d] += acc;
+                } else {
+                    ws[d] = acc;
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&empty[sl])) : "memory");
     }
 }
 
@@ -650,7 +690,7 @@ static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, 
                                 const T *A, T *ws, const double *xin, double *yout, const int32_t *perm, int32_t *err,
                                 cudaStream_t st) {
     if (t1 <= t0) return cudaSuccess;
-    const size_t smem = 2 * (size_t)BRG_BUF_BYTES + 2 * (size_t)BRG_XS_ELEMS * sizeof(T);
+    const size_t smem = (size_t)BRG_SLOTS * BRG_SLOT_BYTES + (size_t)BRG_XS_ELEMS * sizeof(T);
     static bool configured = false;
     if (!configured) {
         cudaError_t e = cudaFuncSetAttribute(brg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
