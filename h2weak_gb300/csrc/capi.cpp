@@ -522,10 +522,11 @@ struct PlanBuilder {
     int max_xfer_n = 0;
     int64_t read_elems = 0;
 
+    // column-major block: element (i, c) at a + c*lda + i, lda = pad4(rows)
     int64_t alloc(int64_t rows, int64_t cols, int32_t &lda) {
-        lda = (int32_t)pad4(cols);
+        lda = (int32_t)pad4(rows);
         int64_t a = opn;
-        opn += pad4((int64_t)lda * rows);
+        opn += pad4((int64_t)lda * cols);
         return a;
     }
     int64_t put_idx(const int32_t *v, int64_t n) {
@@ -559,7 +560,7 @@ struct PlanBuilder {
                 int32_t xo = 0;
                 for (auto &p : panels) {
                     Panel pn{};
-                    pn.a = p.a + r0 * p.lda;
+                    pn.a = p.a + r0;
                     pn.lda = p.lda;
                     pn.w = p.w;
                     pn.xoff = xo;
@@ -584,7 +585,7 @@ struct PlanBuilder {
             for (int64_t c0 = 0; c0 < p.w; c0 += XW_CAP) {
                 int64_t c1 = std::min<int64_t>(p.w, c0 + XW_CAP);
                 PanelSpec q;
-                q.a = p.a + c0;
+                q.a = p.a + c0 * p.lda;
                 q.lda = p.lda;
                 q.w = (int32_t)(c1 - c0);
                 for (auto s : p.segs) {
@@ -616,14 +617,13 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
         if (ph.t0 < 0 || ph.t1 < ph.t0 || ph.t1 > (int64_t)pb.T.size() || ph.max_xw > XW_CAP) bad("phase");
     for (const Target &t : pb.T) {
         if (t.nrows < 1 || t.dst < 0 || t.dst + t.nrows > wsn) bad("target rows");
-        if (t.p0 < 0 || t.p1 < t.p0 || t.p1 > (int32_t)pb.P.size()) bad("target panels");
-        if (!(t.gsz == 4 || t.gsz == 8 || t.gsz == 16 || t.gsz == 32)) bad("gsz");
+        if (t.p0 < 0 || t.p1 < t.p0 || t.p1 > (int32_t)pb.P.size() || t.p1 - t.p0 > BRG_MAX_PANELS) bad("target panels");
         if ((t.flags & T_SCATTER) && (t.dst < h->yperm_off || t.dst + t.nrows > h->yperm_off + N)) bad("scatter rows");
         int64_t xw = 0;
         for (int32_t q = t.p0; q < t.p1; ++q) {
             const Panel &p = pb.P[(size_t)q];
-            if (p.a < 0 || p.a % 4 || p.lda % 4 || p.lda < p.w || p.w < 0) bad("panel layout");
-            if (p.a + (int64_t)(t.nrows - 1) * p.lda + pad4(p.w) > opn) bad("panel extent");
+            if (p.a < 0 || p.w < 1 || p.lda < 1) bad("panel layout");
+            if (p.a + (int64_t)(p.w - 1) * p.lda + t.nrows > opn) bad("panel extent");
             if (p.xoff % 4 || p.xoff != xw) bad("panel xoff");
             if (p.s0 < 0 || p.s1 < p.s0 || p.s1 > (int32_t)pb.S.size()) bad("panel segs");
             for (int32_t e = p.s0; e < p.s1; ++e) {
@@ -635,10 +635,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
             }
             xw += pad4(p.w);
         }
-        if (xw != t.xw || xw > XW_CAP) bad("target width");
-        int64_t ls = 0;
-        for (int32_t q = t.p0; q < t.p1; ++q) ls += pb.P[(size_t)q].lda;
-        if (ls != t.ldsum || ls < 1 || t.xw > BRG_SLOT_ELEMS_F64) bad("target leading dimensions");
+        if (xw != t.xw || xw > XW_CAP || xw > BRG_XS_ELEMS) bad("target width");
     }
     for (const FactorJob &f : pb.factors)
         if (f.r < 1 || f.f < 0 || f.f + (int64_t)f.r * f.r > pb.fn || f.ii < 0 || f.ii + f.r > nidx || f.jj < 0 ||
@@ -649,14 +646,14 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
         if (x.jj < 0 || x.jj + x.r > nidx || x.pi < 0 || x.pi + x.n > nidx) bad("xfer indices");
         bool row = x.mode == X_ROW_RL || x.mode == X_ROW_R;
         if (row) {
-            if (x.ld1 < x.r || x.a1 < 0 || x.a1 + (int64_t)(x.n - 1) * x.ld1 + x.r > opn) bad("xfer rows");
-            if (x.a2 >= 0 && (x.ld2 < x.n || x.a2 + (int64_t)(x.r - 1) * x.ld2 + x.n > opn)) bad("xfer transposed");
-        } else if (x.ld1 < x.n || x.a1 < 0 || x.a1 + (int64_t)(x.r - 1) * x.ld1 + x.n > opn) {
+            if (x.ld1 < x.n || x.a1 < 0 || x.a1 + (int64_t)(x.r - 1) * x.ld1 + x.n > opn) bad("xfer rows");
+            if (x.a2 >= 0 && (x.ld2 < x.r || x.a2 + (int64_t)(x.n - 1) * x.ld2 + x.r > opn)) bad("xfer transposed");
+        } else if (x.ld1 < x.r || x.a1 < 0 || x.a1 + (int64_t)(x.n - 1) * x.ld1 + x.r > opn) {
             bad("xfer columns");
         }
     }
     for (const FillJob &f : pb.fills)
-        if (f.nr < 1 || f.nc < 1 || f.lda < f.nc || f.a < 0 || f.a + (int64_t)(f.nr - 1) * f.lda + f.nc > opn ||
+        if (f.nr < 1 || f.nc < 1 || f.lda < f.nr || f.a < 0 || f.a + (int64_t)(f.nc - 1) * f.lda + f.nr > opn ||
             f.ri < 0 || f.ri + f.nr > nidx || f.ci < 0 || f.ci + f.nc > nidx)
             bad("fill job");
     for (int32_t v : pb.idx)
@@ -825,7 +822,7 @@ void build_plan(h2w_handle *h) {
                         if (rq == 0) continue;
                         ps.segs.push_back(ws_seg(outb + s.ptr[(size_t)q], rq, co));
                         FillJob fj{};
-                        fj.a = ps.a + co;
+                        fj.a = ps.a + (int64_t)co * ps.lda;
                         fj.ri = ri;
                         fj.ci = pb.put_idx(s.chk.data() + s.ptr[(size_t)q], rq);
                         fj.nr = r;
@@ -861,7 +858,7 @@ void build_plan(h2w_handle *h) {
                 if (nq == 0) continue;
                 ps.segs.push_back(leaf_gather(L, q, co));
                 FillJob fj{};
-                fj.a = ps.a + co;
+                fj.a = ps.a + (int64_t)co * ps.lda;
                 fj.ri = ri;
                 fj.ci = pb.put_idx(t.perm.data() + t.off[(size_t)L][(size_t)q], nq);
                 fj.nr = n;
@@ -943,7 +940,7 @@ void build_plan(h2w_handle *h) {
                             xj.f = pfac[(size_t)j][q];
                             xj.jj = pb.put_idx(Pp.col.data() + Pp.ptr[q], r);
                             xj.pi = ri;
-                            xj.a1 = B.a + co;
+                            xj.a1 = B.a + (int64_t)co * B.lda;
                             xj.ld1 = B.lda;
                             xj.a2 = -1;
                             xj.r = r;
@@ -953,7 +950,7 @@ void build_plan(h2w_handle *h) {
                             pb.max_xfer_n = std::max(pb.max_xfer_n, n);
                         } else {
                             FillJob fj{};
-                            fj.a = B.a + co;
+                            fj.a = B.a + (int64_t)co * B.lda;
                             fj.ri = ri;
                             fj.ci = pb.put_idx(Pp.col.data() + Pp.ptr[q], r);
                             fj.nr = n;
@@ -1021,7 +1018,7 @@ void build_plan(h2w_handle *h) {
                     const BMat &B = bm[(size_t)j][(size_t)a];
                     if (B.a < 0) continue;
                     PlanBuilder::PanelSpec ps;
-                    ps.a = B.a + (t.off[(size_t)L][(size_t)k] - t.off[(size_t)j][(size_t)a]) * B.lda;
+                    ps.a = B.a + (t.off[(size_t)L][(size_t)k] - t.off[(size_t)j][(size_t)a]);
                     ps.lda = B.lda;
                     ps.w = B.w;
                     ps.segs = B.segs;
@@ -1045,7 +1042,7 @@ void build_plan(h2w_handle *h) {
     }
     for (auto &ph : h->phases)
         std::stable_sort(pb.T.begin() + ph.t0, pb.T.begin() + ph.t1, [](const Target &a, const Target &b) {
-            return (int64_t)a.nrows * a.ldsum > (int64_t)b.nrows * b.ldsum;
+            return (int64_t)a.nrows * a.xw > (int64_t)b.nrows * b.xw;
         });
     h->ph_op.assign(h->phases.size(), 0);
     h->ph_vec.assign(h->phases.size(), 0);

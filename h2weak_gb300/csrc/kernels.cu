@@ -366,37 +366,40 @@ __global__ void xfer_kernel(const XferJob *__restrict__ jobs, const int32_t *__r
     const int32_t *J = idx + jb.jj;
     const int gp = idx[jb.pi + p];
     const bool row = jb.mode == X_ROW_RL || jb.mode == X_ROW_R;
-    // the output location is the working vector
-    double *y = row ? op + jb.a1 + (int64_t)p * jb.ld1 : op + jb.a1 + p;
-    const int64_t ys = row ? 1 : jb.ld1;
+    // Column-major outputs. ROW modes: element (p, j) of the n x r result at
+    // a1 + j*ld1 + p; COL modes: element (i, p) of the r x n result at
+    // a1 + p*ld1 + i. The output location is the working vector.
+    double *y = row ? op + jb.a1 + p : op + jb.a1 + (int64_t)p * jb.ld1;
+    const int64_t ys = row ? jb.ld1 : 1;
     for (int j = 0; j < r; ++j) y[j * ys] = kentry(kp, gp, J[j]);  // K(p,J) == K(J,p) bitwise
     if (row) {
         // z R = b (forward), then y L = z (backward, unit diagonal)
         for (int j = 0; j < r; ++j) {
-            double s = y[j];
-            for (int q = 0; q < j; ++q) s = __dsub_rn(s, __dmul_rn(y[q], A[q * r + j]));
-            y[j] = __ddiv_rn(s, A[j * r + j]);
+            double s = y[j * ys];
+            for (int q = 0; q < j; ++q) s = __dsub_rn(s, __dmul_rn(y[q * ys], A[q * r + j]));
+            y[j * ys] = __ddiv_rn(s, A[j * r + j]);
         }
         if (jb.mode == X_ROW_RL)
             for (int j = r - 1; j >= 0; --j) {
-                double s = y[j];
-                for (int q = j + 1; q < r; ++q) s = __dsub_rn(s, __dmul_rn(y[q], A[q * r + j]));
-                y[j] = s;
+                double s = y[j * ys];
+                for (int q = j + 1; q < r; ++q) s = __dsub_rn(s, __dmul_rn(y[q * ys], A[q * r + j]));
+                y[j * ys] = s;
             }
+        // transposed copy: element (j, p) of the r x n result at a2 + p*ld2 + j
         if (jb.a2 >= 0)
-            for (int j = 0; j < r; ++j) op[jb.a2 + (int64_t)j * jb.ld2 + p] = y[j];
+            for (int j = 0; j < r; ++j) op[jb.a2 + (int64_t)p * jb.ld2 + j] = y[j * ys];
     } else {
         // L x = b (forward, unit diagonal), then R x = x (backward)
         for (int i = 0; i < r; ++i) {
-            double s = y[i * ys];
-            for (int q = 0; q < i; ++q) s = __dsub_rn(s, __dmul_rn(A[i * r + q], y[q * ys]));
-            y[i * ys] = s;
+            double s = y[i];
+            for (int q = 0; q < i; ++q) s = __dsub_rn(s, __dmul_rn(A[i * r + q], y[q]));
+            y[i] = s;
         }
         if (jb.mode == X_COL_LR)
             for (int i = r - 1; i >= 0; --i) {
-                double s = y[i * ys];
-                for (int q = i + 1; q < r; ++q) s = __dsub_rn(s, __dmul_rn(A[i * r + q], y[q * ys]));
-                y[i * ys] = __ddiv_rn(s, A[i * r + i]);
+                double s = y[i];
+                for (int q = i + 1; q < r; ++q) s = __dsub_rn(s, __dmul_rn(A[i * r + q], y[q]));
+                y[i] = __ddiv_rn(s, A[i * r + i]);
             }
     }
 }
@@ -423,8 +426,8 @@ __global__ void fill_kernel(const FillJob *__restrict__ jobs, const int32_t *__r
     const int64_t total = (int64_t)jb.nr * jb.nc;
     const int32_t *R = idx + jb.ri, *C = idx + jb.ci;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        int i = (int)(e / jb.nc), c = (int)(e % jb.nc);
-        op[jb.a + (int64_t)i * jb.lda + c] = kentry(kp, R[i], C[c]);
+        int c = (int)(e / jb.nr), i = (int)(e % jb.nr);
+        op[jb.a + (int64_t)c * jb.lda + i] = kentry(kp, R[i], C[c]);
     }
 }
 
@@ -453,233 +456,122 @@ cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStr
 }
 
 // ------------------------------------------------------- block-row GEMV ---
-// Persistent, dynamically scheduled block-row GEMV. Each CTA repeatedly
-// claims a target (atomic counter per launch), streams the target's panel
-// rows through two shared-memory buffers with cp.async.bulk (completion
-// tracked by an mbarrier per buffer, so the next chunk is in flight while
-// the current one is multiplied), and gathers the target's sources once
-// into a double-buffered source area. Rows are reduced by groups of gsz
-// lanes with 16-byte shared-memory reads.
+// Persistent, dynamically scheduled block-row GEMV over column-major panels.
+// A CTA claims a target (atomic counter, next index prefetched), caches its
+// panel descriptors and gathers its sources into shared memory, then lets
+// lane l of a warp own row l of a 32-row group while the warps of the CTA
+// split the columns: every load is a coalesced 32-row column segment and
+// each lane keeps several independent loads in flight. Partial sums of the
+// column slices meet in shared memory.
 constexpr int BRG_THREADS = 256;
-constexpr int BRG_XS_ELEMS = 4096;     // per source buffer (elements)
-constexpr long long BRG_WAIT_LIMIT = 1LL << 24;
+constexpr int BRG_WARPS = BRG_THREADS / 32;
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-// bounded wait; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (long long it = 0; it < BRG_WAIT_LIMIT; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-template <class T> struct Vec16;
-template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
-template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
-
-__device__ __forceinline__ double dot16(const double2 a, const double2 x) { return a.x * x.x + a.y * x.y; }
-__device__ __forceinline__ float dot16(const float4 a, const float4 x) {
-    return a.x * x.x + a.y * x.y + a.z * x.z + a.w * x.w;
-}
-
-// Warp-specialised: warp 7 is the producer (claims targets with an atomic
-// counter, writes each chunk's metadata and issues its bulk copies into a
-// ring of BRG_SLOTS shared-memory slots, full/empty mbarriers per slot);
-// warps 0..6 consume chunks in order. Consumers gather a target's sources
-// into shared memory when its first chunk arrives, then reduce rows with
-// gsz-lane groups. Every wait is bounded; a wait that runs out sets *err and
-// the warp leaves its loop (the others then run out too).
-constexpr int BRG_SLOTS = 4;
-constexpr int BRG_SLOT_BYTES = 32768;
-constexpr int BRG_CONSUMERS = 7;
-
-struct ChunkMeta {
-    int64_t t;     // target index, -1 = end of stream
-    int32_t r0, nr;
+template <class T> struct BrgSmem {
+    T xs[BRG_XS_ELEMS];
+    T red[BRG_THREADS];
+    Panel pc[BRG_MAX_PANELS];
+    int64_t t, next;
 };
 
 template <class T>
-__global__ void __launch_bounds__(BRG_THREADS, 1)
+__global__ void __launch_bounds__(BRG_THREADS)
     brg_kernel(const Target *__restrict__ Tg, const Panel *__restrict__ Pn, const Seg *__restrict__ Sg, int64_t t0,
                int64_t t1, int32_t *ctr, const T *__restrict__ A, T *ws, const double *__restrict__ xin,
-               double *yout, const int32_t *__restrict__ perm, int32_t *err) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    constexpr int SLOT = BRG_SLOT_BYTES / (int)sizeof(T);
-    using V16 = typename Vec16<T>::type;
-    constexpr int VN = Vec16<T>::n;
-    T *slots = reinterpret_cast<T *>(smem_raw);
-    T *xs = slots + BRG_SLOTS * SLOT;
-    __shared__ __align__(8) uint64_t full[BRG_SLOTS], empty[BRG_SLOTS];
-    __shared__ ChunkMeta meta[BRG_SLOTS];
+               double *yout, const int32_t *__restrict__ perm) {
+    __shared__ BrgSmem<T> sm;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) {
-        for (int q = 0; q < BRG_SLOTS; ++q) {
-            mbar_init(&full[q], 1);
-            mbar_init(&empty[q], BRG_CONSUMERS);
-        }
-    }
-    fence_proxy_async();
+    if (tid == 0) sm.next = t0 + (int64_t)atomicAdd(ctr, 1);
     __syncthreads();
-
-    if (warp == BRG_CONSUMERS) {
-        // ---------------- producer ----------------
-        if (lane != 0) return;
-        int64_t k = 0;
-        bool alive = true;
-        while (alive) {
-            int64_t q = t0 + (int64_t)atomicAdd(ctr, 1);
-            const bool last = q >= t1;
-            int nrows = 0, R = 1;
-            Target tg{};
-            if (!last) {
-                tg = Tg[q];
-                nrows = tg.nrows;
-                R = SLOT / tg.xw;
-                if (R < 1) R = 1;
-            }
-            for (int r0 = 0; last ? r0 == 0 : r0 < nrows; r0 += R) {
-                const int sl = (int)(k % BRG_SLOTS);
-                if (k >= BRG_SLOTS && !mbar_wait(&empty[sl], (uint32_t)(((k / BRG_SLOTS) - 1) & 1))) {
-                    atomicExch(err, 1);
-                    alive = false;
-                    break;
-                }
-                if (last) {
-                    meta[sl].t = -1;
-                    mbar_expect_tx(&full[sl], 0);
-                    alive = false;
-                    break;
-                }
-                const int nr = nrows - r0 < R ? nrows - r0 : R;
-                meta[sl].t = q;
-                meta[sl].r0 = r0;
-                meta[sl].nr = nr;
-                mbar_expect_tx(&full[sl], (uint32_t)((int64_t)nr * tg.xw * (int64_t)sizeof(T)));
-                T *dst = slots + (int64_t)sl * SLOT;
-                for (int p = tg.p0; p < tg.p1; ++p) {
-                    const Panel pn = Pn[p];
-                    const int sp = (pn.w + 3) & ~3;
-                    const T *src = A + pn.a + (int64_t)r0 * pn.lda;
-                    if (pn.lda == sp) {
-                        bulk_g2s(dst, src, (uint32_t)((int64_t)nr * sp * (int64_t)sizeof(T)), &full[sl]);
-                    } else {
-                        for (int i = 0; i < nr; ++i)
-                            bulk_g2s(dst + (int64_t)i * sp, src + (int64_t)i * pn.lda, (uint32_t)(sp * sizeof(T)),
-                                     &full[sl]);
+    while (true) {
+        if (tid == 0) {
+            sm.t = sm.next;
+            if (sm.t < t1) sm.next = t0 + (int64_t)atomicAdd(ctr, 1);
+        }
+        __syncthreads();
+        const int64_t t = sm.t;
+        if (t >= t1) break;
+        const Target tg = Tg[t];
+        const int np = tg.p1 - tg.p0;
+        for (int q = tid; q < np; q += BRG_THREADS) sm.pc[q] = Pn[tg.p0 + q];
+        __syncthreads();
+        // gather sources
+        for (int q = 0; q < np; ++q) {
+            const Panel pn = sm.pc[q];
+            for (int sidx = pn.s0; sidx < pn.s1; ++sidx) {
+                const Seg sg = Sg[sidx];
+                T *dst = sm.xs + pn.xoff + sg.xoff;
+                if (sg.flags & S_GATHER) {
+                    const int32_t *pp = perm + sg.src;
+                    int c = tid;
+                    for (; c + 3 * BRG_THREADS < sg.len; c += 4 * BRG_THREADS) {
+                        const int i0 = pp[c], i1 = pp[c + BRG_THREADS], i2 = pp[c + 2 * BRG_THREADS],
+                                  i3 = pp[c + 3 * BRG_THREADS];
+                        const double v0 = xin[i0], v1 = xin[i1], v2 = xin[i2], v3 = xin[i3];
+                        dst[c] = (T)v0;
+                        dst[c + BRG_THREADS] = (T)v1;
+                        dst[c + 2 * BRG_THREADS] = (T)v2;
+                        dst[c + 3 * BRG_THREADS] = (T)v3;
                     }
-                    dst += (int64_t)nr * sp;
-                }
-                ++k;
-            }
-        }
-        return;
-    }
-
-    // ---------------- consumers ----------------
-    const int ctid = tid;  // 0 .. BRG_CONSUMERS*32-1
-    constexpr int NC = BRG_CONSUMERS * 32;
-    int64_t cur = -1;
-    for (int64_t k = 0;; ++k) {
-        const int sl = (int)(k % BRG_SLOTS);
-        const bool ok = mbar_wait(&full[sl], (uint32_t)((k / BRG_SLOTS) & 1));
-        uint32_t anyfail;
-        asm volatile(
-            "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 2, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
-            : "=r"(anyfail)
-            : "r"((uint32_t)!ok), "n"(NC));
-        if (anyfail) {  // all consumers leave together
-            if (ctid == 0) atomicExch(err, 1);
-            break;
-        }
-        const ChunkMeta m = meta[sl];
-        if (m.t < 0) break;
-        const Target tg = Tg[m.t];
-        if (m.t != cur) {
-            asm volatile("bar.sync 1, %0;" ::"n"(NC));  // all consumers done with the previous sources
-            for (int p = tg.p0; p < tg.p1; ++p) {
-                const Panel pn = Pn[p];
-                for (int sidx = pn.s0; sidx < pn.s1; ++sidx) {
-                    const Seg sg = Sg[sidx];
-                    T *dst = xs + pn.xoff + sg.xoff;
-                    if (sg.flags & S_GATHER) {
-                        const int32_t *pp = perm + sg.src;
-                        int c = ctid;
-                        for (; c + 3 * NC < sg.len; c += 4 * NC) {
-                            int i0 = pp[c], i1 = pp[c + NC], i2 = pp[c + 2 * NC], i3 = pp[c + 3 * NC];
-                            double v0 = xin[i0], v1 = xin[i1], v2 = xin[i2], v3 = xin[i3];
-                            dst[c] = (T)v0;
-                            dst[c + NC] = (T)v1;
-                            dst[c + 2 * NC] = (T)v2;
-                            dst[c + 3 * NC] = (T)v3;
-                        }
-                        for (; c < sg.len; c += NC) dst[c] = (T)xin[pp[c]];
-                    } else {
-                        for (int c = ctid; c < sg.len; c += NC) dst[c] = ws[sg.src + c];
-                    }
-                }
-            }
-            asm volatile("bar.sync 1, %0;" ::"n"(NC));
-            cur = m.t;
-        }
-        const T *buf = slots + (int64_t)sl * SLOT;
-        const int g = tg.gsz;
-        const int sub = lane / g, gl = lane % g;
-        const int rpw = 32 / g, step = BRG_CONSUMERS * rpw;
-        for (int ib = warp * rpw; ib < m.nr; ib += step) {
-            const int i = ib + sub;
-            T acc = T(0);
-            if (i < m.nr) {
-                const T *pbuf = buf;
-                for (int p = tg.p0; p < tg.p1; ++p) {
-                    const Panel pn = Pn[p];
-                    const int sp = (pn.w + 3) & ~3;
-                    const T *row = pbuf + (int64_t)i * sp;
-                    const T *xp = xs + pn.xoff;
-                    const int wfull = (pn.w / VN) * VN;
-                    for (int c = gl * VN; c < wfull; c += g * VN)
-                        acc += dot16(*reinterpret_cast<const V16 *>(row + c), *reinterpret_cast<const V16 *>(xp + c));
-                    for (int c = wfull + gl; c < pn.w; c += g) acc += row[c] * xp[c];
-                    pbuf += (int64_t)m.nr * sp;
-                }
-            }
-            for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (i < m.nr && gl == 0) {
-                const int64_t d = tg.dst + m.r0 + i;
-                if (tg.flags & T_SCATTER) {
-                    T v = (tg.flags & T_ACCUM) ? ws[d] + acc : acc;
-                    yout[perm[d]] = (double)v;
-                } else if (tg.flags & T_ATOMIC) {
-                    atomicAdd(ws + d, acc);
-                } else if (tg.flags & T_ACCUM) {
-                    ws[d] += acc;
+                    for (; c < sg.len; c += BRG_THREADS) dst[c] = (T)xin[pp[c]];
                 } else {
-                    ws[d] = acc;
+                    const T *src = ws + sg.src;
+                    for (int c = tid; c < sg.len; c += BRG_THREADS) dst[c] = src[c];
                 }
             }
         }
-        __syncwarp();
-        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&empty[sl])) : "memory");
+        __syncthreads();
+        // rows, in blocks of up to 256 (8 groups of 32)
+        for (int rb = 0; rb < tg.nrows; rb += BRG_THREADS) {
+            const int rows = tg.nrows - rb < BRG_THREADS ? tg.nrows - rb : BRG_THREADS;
+            const int RG = (rows + 31) >> 5;       // row groups
+            const int S = BRG_WARPS / RG;          // column slices per group
+            const int rg = warp % RG, sl = warp / RG;
+            const int i = rb + rg * 32 + lane;
+            T acc = T(0);
+            if (sl < S && i < tg.nrows) {
+                for (int q = 0; q < np; ++q) {
+                    const Panel pn = sm.pc[q];
+                    const int c0 = (int)(((int64_t)pn.w * sl) / S), c1 = (int)(((int64_t)pn.w * (sl + 1)) / S);
+                    const T *col = A + pn.a + i + (int64_t)c0 * pn.lda;
+                    const T *xp = sm.xs + pn.xoff;
+                    const int64_t ld = pn.lda;
+                    int c = c0;
+                    T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+                    for (; c + 7 < c1; c += 8, col += 8 * ld) {
+                        const T v0 = col[0], v1 = col[ld], v2 = col[2 * ld], v3 = col[3 * ld];
+                        const T v4 = col[4 * ld], v5 = col[5 * ld], v6 = col[6 * ld], v7 = col[7 * ld];
+                        a0 += v0 * xp[c];
+                        a1 += v1 * xp[c + 1];
+                        a2 += v2 * xp[c + 2];
+                        a3 += v3 * xp[c + 3];
+                        a0 += v4 * xp[c + 4];
+                        a1 += v5 * xp[c + 5];
+                        a2 += v6 * xp[c + 6];
+                        a3 += v7 * xp[c + 7];
+                    }
+                    for (; c < c1; ++c, col += ld) a0 += col[0] * xp[c];
+                    acc += (a0 + a1) + (a2 + a3);
+                }
+            }
+            sm.red[tid] = acc;
+            __syncthreads();
+            if (sl == 0 && i < tg.nrows) {
+                T v = acc;
+                for (int q = 1; q < S; ++q) v += sm.red[(rg + q * RG) * 32 + lane];
+                const int64_t d = tg.dst + i;
+                if (tg.flags & T_SCATTER) {
+                    T o = (tg.flags & T_ACCUM) ? ws[d] + v : v;
+                    yout[perm[d]] = (double)o;
+                } else if (tg.flags & T_ATOMIC) {
+                    atomicAdd(ws + d, v);
+                } else if (tg.flags & T_ACCUM) {
+                    ws[d] += v;
+                } else {
+                    ws[d] = v;
+                }
+            }
+            __syncthreads();
+        }
     }
 }
 
@@ -687,25 +579,24 @@ static int g_num_sms = 0;
 
 template <class T>
 static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
-                                const T *A, T *ws, const double *xin, double *yout, const int32_t *perm, int32_t *err,
+                                const T *A, T *ws, const double *xin, double *yout, const int32_t *perm,
                                 cudaStream_t st) {
     if (t1 <= t0) return cudaSuccess;
-    const size_t smem = (size_t)BRG_SLOTS * BRG_SLOT_BYTES + (size_t)BRG_XS_ELEMS * sizeof(T);
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(brg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    static int per_sm = 0;
     if (g_num_sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
         if (g_num_sms <= 0) g_num_sms = 1;
     }
-    int64_t nt = t1 - t0;
-    int grid = (int)(nt < g_num_sms ? nt : g_num_sms);
-    brg_kernel<T><<<grid, BRG_THREADS, smem, st>>>(Tg, P, S, t0, t1, ctr, A, ws, xin, yout, perm, err);
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brg_kernel<T>, BRG_THREADS, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    const int64_t nt = t1 - t0;
+    const int64_t cap = (int64_t)g_num_sms * per_sm;
+    const int grid = (int)(nt < cap ? nt : cap);
+    brg_kernel<T><<<grid, BRG_THREADS, 0, st>>>(Tg, P, S, t0, t1, ctr, A, ws, xin, yout, perm);
     count_launch();
     return cudaGetLastError();
 }
@@ -713,12 +604,14 @@ static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, 
 cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
                            const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
                            int32_t *err, cudaStream_t st) {
-    return launch_brg_t<double>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, err, st);
+    (void)err;
+    return launch_brg_t<double>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, st);
 }
 cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
                            const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
                            int32_t *err, cudaStream_t st) {
-    return launch_brg_t<float>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, err, st);
+    (void)err;
+    return launch_brg_t<float>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, st);
 }
 
 template <class T>

@@ -52,7 +52,8 @@ cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_
                            int32_t *err, cudaStream_t st);
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
-constexpr int BRG_SLOT_ELEMS_F64 = 32768 / 8;  // one row of every panel of a target must fit a staging slot
+constexpr int BRG_XS_ELEMS = 4096;    // gathered source width per target (elements)
+constexpr int BRG_MAX_PANELS = 32;    // panels per target
 
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,
