@@ -474,7 +474,7 @@ template <class T> struct BrgSmem {
 };
 
 template <class T>
-__global__ void __launch_bounds__(BRG_THREADS)
+__global__ void __launch_bounds__(BRG_THREADS, 4)
     brg_kernel(const Target *__restrict__ Tg, const Panel *__restrict__ Pn, const Seg *__restrict__ Sg, int64_t t0,
                int64_t t1, int32_t *ctr, const T *__restrict__ A, T *ws, const double *__restrict__ xin,
                double *yout, const int32_t *__restrict__ perm) {
