@@ -87,9 +87,7 @@ struct h2w_handle {
     DBuf<int32_t> d_perm;
     DBuf<double> d_op;
     DBuf<float> d_op32;
-    DBuf<Target> d_T;
-    DBuf<Panel> d_P;
-    DBuf<Seg> d_S;
+    DBuf<int64_t> d_roff, d_blob;  // packed target records of the matvec
     DBuf<double> d_ws, d_x, d_y;
     DBuf<int32_t> d_ctr, d_err;
     DBuf<float> d_ws32;
@@ -1085,9 +1083,38 @@ void build_plan(h2w_handle *h) {
     CK(launch_factor(dfac.p, (int)pb.factors.size(), didx.p, kp, dF.p, st));
     CK(launch_xfer(dxf.p, (int)pb.xfers.size(), pb.max_xfer_n, didx.p, kp, dF.p, h->d_op.p, st));
     CK(launch_fill(dfill.p, (int)pb.fills.size(), didx.p, kp, h->d_op.p, st));
-    h->d_T.upload(pb.T, st);
-    h->d_P.upload(pb.P, st);
-    h->d_S.upload(pb.S, st);
+    // packed records: header, panels, segments (layout documented at brg_kernel)
+    {
+        std::vector<int64_t> roff{0}, blob;
+        for (const Target &tg : pb.T) {
+            const size_t base = blob.size();
+            int ns = 0;
+            for (int32_t q = tg.p0; q < tg.p1; ++q) ns += pb.P[(size_t)q].s1 - pb.P[(size_t)q].s0;
+            blob.push_back(tg.dst);
+            blob.push_back((int64_t)(uint32_t)tg.nrows | ((int64_t)tg.flags << 32));
+            blob.push_back((int64_t)(uint32_t)(tg.p1 - tg.p0) | ((int64_t)ns << 32));
+            for (int32_t q = tg.p0; q < tg.p1; ++q) {
+                const Panel &pn = pb.P[(size_t)q];
+                blob.push_back(pn.a);
+                blob.push_back((int64_t)(uint32_t)pn.lda | ((int64_t)pn.w << 32));
+                blob.push_back(pn.xoff);
+            }
+            for (int32_t q = tg.p0; q < tg.p1; ++q) {
+                const Panel &pn = pb.P[(size_t)q];
+                for (int32_t e = pn.s0; e < pn.s1; ++e) {
+                    const Seg &sg = pb.S[(size_t)e];
+                    const int64_t code = ((int64_t)(pn.xoff + sg.xoff) << 1) | (sg.flags & S_GATHER ? 1 : 0);
+                    blob.push_back(sg.src);
+                    blob.push_back((int64_t)(uint32_t)sg.len | (code << 32));
+                }
+            }
+            if (blob.size() - base > (size_t)BRG_REC_WORDS)
+                throw ApiError(H2W_ERR_STATE, "internal: target record exceeds the shared-memory record size");
+            roff.push_back((int64_t)blob.size());
+        }
+        h->d_roff.upload(roff, st);
+        h->d_blob.upload(blob, st);
+    }
     h->d_ws.alloc((size_t)h->ws_n);
     h->d_ctr.alloc(h->phases.size() + 1);
     h->d_err.alloc(1);
@@ -1194,17 +1221,23 @@ void prof_launch(h2w_handle *h, int prec, int phase, cudaStream_t st, F &&launch
     h->prof_recs.push_back(r);
 }
 
-void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st) {
+// y = A x. permuted: x and y in leaf order (GMRES works there: no gather or
+// scatter per product); otherwise original point order.
+void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st, bool permuted = false) {
+    const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
-    CK(cudaMemsetAsync(h->d_ctr.p, 0, h->d_ctr.n * 4, st));
     for (size_t q = 0; q < h->phases.size(); ++q) {
         const Phase &ph = h->phases[q];
         prof_launch(h, H2W_PREC_FP64, (int)q, st, [&] {
-            return launch_brg_f64(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, h->d_ctr.p + q, h->d_op.p, h->d_ws.p,
-                                  dx, dy, h->d_perm.p, h->d_err.p, st);
+            return launch_brg_f64(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op.p, h->d_ws.p, dx, dy, perm, st);
         });
     }
-    if (!h->fused_scatter) CK(launch_scatter_f64(h->d_ws.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
+    if (!h->fused_scatter) {
+        if (permuted)
+            CK(cudaMemcpyAsync(dy, h->d_ws.p + h->yperm_off, (size_t)h->tree.N * 8, cudaMemcpyDeviceToDevice, st));
+        else
+            CK(launch_scatter_f64(h->d_ws.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
+    }
 }
 
 void ensure_f32(h2w_handle *h) {
@@ -1217,18 +1250,20 @@ void ensure_f32(h2w_handle *h) {
 
 // FP32 operator and workspace; x and y stay FP64 in original order (the
 // conversions happen in the kernel's gather and scatter).
-void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st) {
+void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st, bool permuted = false) {
     ensure_f32(h);
+    const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
-    CK(cudaMemsetAsync(h->d_ctr.p, 0, h->d_ctr.n * 4, st));
     for (size_t q = 0; q < h->phases.size(); ++q) {
         const Phase &ph = h->phases[q];
         prof_launch(h, H2W_PREC_FP32, (int)q, st, [&] {
-            return launch_brg_f32(h->d_T.p, h->d_P.p, h->d_S.p, ph.t0, ph.t1, h->d_ctr.p + q, h->d_op32.p,
-                                  h->d_ws32.p, dx, dy, h->d_perm.p, h->d_err.p, st);
+            return launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, h->d_ws32.p, dx, dy, perm, st);
         });
     }
-    if (!h->fused_scatter) CK(launch_scatter_f32(h->d_ws32.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
+    if (!h->fused_scatter) {
+        if (permuted) CK(vec_f32_to_f64(h->d_ws32.p + h->yperm_off, dy, h->tree.N, st));
+        else CK(launch_scatter_f32(h->d_ws32.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
+    }
 }
 
 // --------------------------------------------------------------- GMRES ---
@@ -1295,15 +1330,17 @@ void gmres_xupdate(h2w_handle *h, const GmresDev &g, double *dx, int k) {
     CK(gmres_update(g, dx, h->g_tmp.p, k, h->stream));
 }
 
-// FP64 GMRES on device vectors; matvec precision chosen by prec.
+// FP64 GMRES on device vectors in leaf order (the operator is applied as
+// P A P^T, which leaves GMRES unchanged up to rounding); matvec precision
+// chosen by prec.
 int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double tol, int prec, int *iters,
               double *resid) {
     GmresDev g = gmres_state(h, max_iter);
     cudaStream_t st = h->stream;
     const int64_t N = h->tree.N;
     auto A = [&](const double *in, double *out) {
-        if (prec == H2W_PREC_FP32) run_matvec_f32(h, in, out, st);
-        else run_matvec_f64(h, in, out, st);
+        if (prec == H2W_PREC_FP32) run_matvec_f32(h, in, out, st, true);
+        else run_matvec_f64(h, in, out, st, true);
     };
     double normb = dnorm(h, db);
     if (normb == 0.0) normb = 1;
@@ -1337,17 +1374,6 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     *resid = dnorm(h, h->g_r.p) / normb;
     *iters = max_iter;
     return *resid < tol ? H2W_OK : H2W_ERR_NOT_CONVERGED;
-}
-
-// Device-side failure flag of the matvec kernel (a bounded wait that ran out).
-void check_device_error(h2w_handle *h) {
-    int32_t e = 0;
-    CK(cudaMemcpyAsync(&e, h->d_err.p, 4, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    if (e) {
-        CK(cudaMemsetAsync(h->d_err.p, 0, 4, h->stream));
-        throw ApiError(H2W_ERR_CUDA, "matvec kernel: a shared-memory staging wait ran out (device error flag)");
-    }
 }
 
 int fail(h2w_handle *h, int code, const std::string &m) {
@@ -1736,10 +1762,7 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
             }
             if (where == H2W_HOST) CK(cudaMemcpyAsync(yc, h->d_y.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
         }
-        if (where == H2W_HOST) {
-            CK(cudaStreamSynchronize(st));
-            check_device_error(h);
-        }
+        if (where == H2W_HOST) CK(cudaStreamSynchronize(st));
         return H2W_OK;
     });
 }
@@ -1761,8 +1784,14 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
             db = h->g_b.p;
             dx = h->d_x.p;
         }
-        int rc = gmres_run(h, db, dx, max_iter, tol, H2W_PREC_FP64, iters, resid);
-        check_device_error(h);
+        DBuf<double> bp, xp;
+        bp.alloc((size_t)N);
+        xp.alloc((size_t)N);
+        CK(launch_gather_f64(db, bp.p, h->d_perm.p, N, h->stream));
+        CK(launch_gather_f64(dx, xp.p, h->d_perm.p, N, h->stream));
+        int rc = gmres_run(h, bp.p, xp.p, max_iter, tol, H2W_PREC_FP64, iters, resid);
+        CK(launch_scatter_f64(xp.p, dx, h->d_perm.p, N, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
         if (where == H2W_HOST) {
             CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream));
             CK(cudaStreamSynchronize(h->stream));
@@ -1792,16 +1821,24 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         }
         GmresDev g = gmres_state(h, inner_iter);
         (void)g;
-        DBuf<double> r, d;
+        DBuf<double> r, d, bp, xp;
         r.alloc((size_t)N);
         d.alloc((size_t)N);
+        bp.alloc((size_t)N);
+        xp.alloc((size_t)N);
+        CK(launch_gather_f64(db, bp.p, h->d_perm.p, N, st));
+        CK(launch_gather_f64(dx, xp.p, h->d_perm.p, N, st));
+        const double *db_user = db;
+        double *dx_user = dx;
+        db = bp.p;
+        dx = xp.p;
         double normb = dnorm(h, db);
         if (normb == 0.0) normb = 1;
         *inner_total = 0;
         *outer_iters = 0;
         int rc = H2W_ERR_NOT_CONVERGED;
         for (int o = 0; o <= max_outer; ++o) {
-            run_matvec_f64(h, dx, r.p, st);
+            run_matvec_f64(h, dx, r.p, st, true);
             CK(vec_axpby(1.0, db, -1.0, r.p, r.p, N, st));
             *resid = dnorm(h, r.p) / normb;
             if (*resid < tol) { rc = H2W_OK; break; }
@@ -1815,11 +1852,12 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
             CK(vec_axpby(1.0, dx, 1.0, d.p, dx, N, st));
             *outer_iters = o + 1;
         }
+        (void)db_user;
+        CK(launch_scatter_f64(xp.p, dx_user, h->d_perm.p, N, st));
         if (where == H2W_HOST) {
             CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
         }
         CK(cudaStreamSynchronize(st));
-        check_device_error(h);
         return rc;
     });
 }

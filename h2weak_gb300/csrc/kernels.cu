@@ -456,9 +456,10 @@ cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStr
 }
 
 // ------------------------------------------------------- block-row GEMV ---
-// Persistent, dynamically scheduled block-row GEMV over column-major panels.
-// A CTA claims a target (atomic counter, next index prefetched), caches its
-// panel descriptors and gathers its sources into shared memory, then lets
+// Persistent block-row GEMV over column-major panels. A CTA takes targets
+// t0 + blockIdx.x, + gridDim.x, ... (heaviest first, the host sorts them),
+// copies the target's packed record into shared memory, gathers its sources
+// (x through perm, or the workspace) into shared memory, then lets
 // lane l of a warp own row l of a 32-row group while the warps of the CTA
 // split the columns: every load is a coalesced 32-row column segment and
 // each lane keeps several independent loads in flight. Partial sums of the
@@ -466,75 +467,96 @@ cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStr
 constexpr int BRG_THREADS = 256;
 constexpr int BRG_WARPS = BRG_THREADS / 32;
 
-template <class T> struct BrgSmem {
-    T xs[BRG_XS_ELEMS];
-    T red[BRG_THREADS];
-    Panel pc[BRG_MAX_PANELS];
-    int64_t t, next;
-};
-
+// Target record (int64 words), built by the host plan:
+//   [0] dst   [1] nrows | flags << 32   [2] np | ns << 32
+//   np panels x 3 words: a, lda | w << 32, xoff
+//   ns segments x 2 words: src, len | (xoff << 1 | gather) << 32  (xoff: offset in the target's gathered x)
 template <class T>
 __global__ void __launch_bounds__(BRG_THREADS, 4)
-    brg_kernel(const Target *__restrict__ Tg, const Panel *__restrict__ Pn, const Seg *__restrict__ Sg, int64_t t0,
-               int64_t t1, int32_t *ctr, const T *__restrict__ A, T *ws, const double *__restrict__ xin,
-               double *yout, const int32_t *__restrict__ perm) {
-    __shared__ BrgSmem<T> sm;
+    brg_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
+               const T *__restrict__ A, T *ws, const double *__restrict__ xin, double *yout,
+               const int32_t *__restrict__ perm) {
+    __shared__ T xs[BRG_XS_ELEMS];
+    __shared__ T red[BRG_THREADS];
+    __shared__ int64_t rec[BRG_REC_WORDS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) sm.next = t0 + (int64_t)atomicAdd(ctr, 1);
-    __syncthreads();
-    while (true) {
-        if (tid == 0) {
-            sm.t = sm.next;
-            if (sm.t < t1) sm.next = t0 + (int64_t)atomicAdd(ctr, 1);
-        }
+    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
+        const int64_t o = roff[t];
+        const int nw = (int)(roff[t + 1] - o);
+        for (int q = tid; q < nw; q += BRG_THREADS) rec[q] = blob[o + q];
         __syncthreads();
-        const int64_t t = sm.t;
-        if (t >= t1) break;
-        const Target tg = Tg[t];
-        const int np = tg.p1 - tg.p0;
-        for (int q = tid; q < np; q += BRG_THREADS) sm.pc[q] = Pn[tg.p0 + q];
-        __syncthreads();
-        // gather sources
-        for (int q = 0; q < np; ++q) {
-            const Panel pn = sm.pc[q];
-            for (int sidx = pn.s0; sidx < pn.s1; ++sidx) {
-                const Seg sg = Sg[sidx];
-                T *dst = sm.xs + pn.xoff + sg.xoff;
-                if (sg.flags & S_GATHER) {
-                    const int32_t *pp = perm + sg.src;
-                    int c = tid;
-                    for (; c + 3 * BRG_THREADS < sg.len; c += 4 * BRG_THREADS) {
-                        const int i0 = pp[c], i1 = pp[c + BRG_THREADS], i2 = pp[c + 2 * BRG_THREADS],
-                                  i3 = pp[c + 3 * BRG_THREADS];
-                        const double v0 = xin[i0], v1 = xin[i1], v2 = xin[i2], v3 = xin[i3];
-                        dst[c] = (T)v0;
-                        dst[c + BRG_THREADS] = (T)v1;
-                        dst[c + 2 * BRG_THREADS] = (T)v2;
-                        dst[c + 3 * BRG_THREADS] = (T)v3;
-                    }
-                    for (; c < sg.len; c += BRG_THREADS) dst[c] = (T)xin[pp[c]];
-                } else {
-                    const T *src = ws + sg.src;
-                    for (int c = tid; c < sg.len; c += BRG_THREADS) dst[c] = src[c];
+        const int64_t dst = rec[0];
+        const int nrows = (int)(rec[1] & 0xffffffff), flags = (int)(rec[1] >> 32);
+        const int np = (int)(rec[2] & 0xffffffff), ns = (int)(rec[2] >> 32);
+        const int64_t *pan = rec + 3;
+        const int64_t *seg = pan + 3 * np;
+        // gather: every thread walks the segments for its elements
+        {
+            int sidx = 0;
+            int64_t s_src = 0;
+            int s_lo = 0, s_hi = -1, s_g = 0;
+            auto seek = [&](int e) {
+                while (e >= s_hi && sidx < ns) {
+                    const int64_t w1 = seg[2 * sidx + 1];
+                    s_src = seg[2 * sidx];
+                    const int len = (int)(w1 & 0xffffffff);
+                    const int code = (int)(w1 >> 32);
+                    s_lo = code >> 1;
+                    s_hi = s_lo + len;
+                    s_g = code & 1;
+                    ++sidx;
                 }
+            };
+            // elements of the concatenated sources, in segment order
+            int total = 0;
+            if (ns > 0) {
+                const int64_t wl = seg[2 * (ns - 1) + 1];
+                total = (int)(wl >> 33) + (int)(wl & 0xffffffff);
+            }
+            for (int e0 = tid; e0 < total; e0 += 4 * BRG_THREADS) {
+                int64_t idx4[4];
+                int xo4[4], g4[4];
+                int cnt = 0;
+                for (int u = 0; u < 4; ++u) {
+                    const int e = e0 + u * BRG_THREADS;
+                    if (e >= total) break;
+                    seek(e);
+                    if (e < s_lo) {  // padding gap between panels
+                        idx4[u] = -1;
+                    } else {
+                        idx4[u] = s_src + (e - s_lo);
+                    }
+                    xo4[u] = e;
+                    g4[u] = s_g;
+                    ++cnt;
+                }
+                T v4[4];
+                for (int u = 0; u < cnt; ++u) {
+                    const int64_t ix = idx4[u];
+                    if (ix < 0) v4[u] = T(0);
+                    else if (g4[u]) v4[u] = (T)xin[perm ? (int64_t)perm[ix] : ix];
+                    else v4[u] = ws[ix];
+                }
+                for (int u = 0; u < cnt; ++u) xs[xo4[u]] = v4[u];
             }
         }
         __syncthreads();
-        // rows, in blocks of up to 256 (8 groups of 32)
-        for (int rb = 0; rb < tg.nrows; rb += BRG_THREADS) {
-            const int rows = tg.nrows - rb < BRG_THREADS ? tg.nrows - rb : BRG_THREADS;
-            const int RG = (rows + 31) >> 5;       // row groups
-            const int S = BRG_WARPS / RG;          // column slices per group
+        for (int rb = 0; rb < nrows; rb += BRG_THREADS) {
+            const int rows = nrows - rb < BRG_THREADS ? nrows - rb : BRG_THREADS;
+            const int RG = (rows + 31) >> 5;
+            const int S = BRG_WARPS / RG;
             const int rg = warp % RG, sl = warp / RG;
             const int i = rb + rg * 32 + lane;
             T acc = T(0);
-            if (sl < S && i < tg.nrows) {
+            if (sl < S && i < nrows) {
                 for (int q = 0; q < np; ++q) {
-                    const Panel pn = sm.pc[q];
-                    const int c0 = (int)(((int64_t)pn.w * sl) / S), c1 = (int)(((int64_t)pn.w * (sl + 1)) / S);
-                    const T *col = A + pn.a + i + (int64_t)c0 * pn.lda;
-                    const T *xp = sm.xs + pn.xoff;
-                    const int64_t ld = pn.lda;
+                    const int64_t pa = pan[3 * q];
+                    const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
+                    const int xoff = (int)pan[3 * q + 2];
+                    const int c0 = (int)(((int64_t)w * sl) / S), c1 = (int)(((int64_t)w * (sl + 1)) / S);
+                    const T *col = A + pa + i + (int64_t)c0 * lda;
+                    const T *xp = xs + xoff;
+                    const int64_t ld = lda;
                     int c = c0;
                     T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
                     for (; c + 7 < c1; c += 8, col += 8 * ld) {
@@ -553,18 +575,18 @@ __global__ void __launch_bounds__(BRG_THREADS, 4)
                     acc += (a0 + a1) + (a2 + a3);
                 }
             }
-            sm.red[tid] = acc;
+            red[tid] = acc;
             __syncthreads();
-            if (sl == 0 && i < tg.nrows) {
+            if (sl == 0 && i < nrows) {
                 T v = acc;
-                for (int q = 1; q < S; ++q) v += sm.red[(rg + q * RG) * 32 + lane];
-                const int64_t d = tg.dst + i;
-                if (tg.flags & T_SCATTER) {
-                    T o = (tg.flags & T_ACCUM) ? ws[d] + v : v;
-                    yout[perm[d]] = (double)o;
-                } else if (tg.flags & T_ATOMIC) {
+                for (int q = 1; q < S; ++q) v += red[(rg + q * RG) * 32 + lane];
+                const int64_t d = dst + i;
+                if (flags & T_SCATTER) {
+                    const T ov = (flags & T_ACCUM) ? ws[d] + v : v;
+                    yout[perm ? (int64_t)perm[d] : d] = (double)ov;
+                } else if (flags & T_ATOMIC) {
                     atomicAdd(ws + d, v);
-                } else if (tg.flags & T_ACCUM) {
+                } else if (flags & T_ACCUM) {
                     ws[d] += v;
                 } else {
                     ws[d] = v;
@@ -578,9 +600,8 @@ __global__ void __launch_bounds__(BRG_THREADS, 4)
 static int g_num_sms = 0;
 
 template <class T>
-static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
-                                const T *A, T *ws, const double *xin, double *yout, const int32_t *perm,
-                                cudaStream_t st) {
+static cudaError_t launch_brg_t(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const T *A, T *ws,
+                                const double *xin, double *yout, const int32_t *perm, cudaStream_t st) {
     if (t1 <= t0) return cudaSuccess;
     static int per_sm = 0;
     if (g_num_sms == 0) {
@@ -596,22 +617,18 @@ static cudaError_t launch_brg_t(const Target *Tg, const Panel *P, const Seg *S, 
     const int64_t nt = t1 - t0;
     const int64_t cap = (int64_t)g_num_sms * per_sm;
     const int grid = (int)(nt < cap ? nt : cap);
-    brg_kernel<T><<<grid, BRG_THREADS, 0, st>>>(Tg, P, S, t0, t1, ctr, A, ws, xin, yout, perm);
+    brg_kernel<T><<<grid, BRG_THREADS, 0, st>>>(roff, blob, t0, t1, A, ws, xin, yout, perm);
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
-                           const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
-                           int32_t *err, cudaStream_t st) {
-    (void)err;
-    return launch_brg_t<double>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, st);
+cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const double *A,
+                           double *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st) {
+    return launch_brg_t<double>(roff, blob, t0, t1, A, ws, xin, yout, perm, st);
 }
-cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
-                           const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
-                           int32_t *err, cudaStream_t st) {
-    (void)err;
-    return launch_brg_t<float>(T, P, S, t0, t1, ctr, A, ws, xin, yout, perm, st);
+cudaError_t launch_brg_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const float *A,
+                           float *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st) {
+    return launch_brg_t<float>(roff, blob, t0, t1, A, ws, xin, yout, perm, st);
 }
 
 template <class T>
@@ -622,6 +639,15 @@ __global__ void scatter_kernel2(const T *__restrict__ yp, double *__restrict__ y
 }
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st) {
     scatter_kernel2<double><<<608, 256, 0, st>>>(yp, y, perm, n);
+    count_launch(); return cudaGetLastError();
+}
+__global__ void gather_kernel(const double *__restrict__ x, double *__restrict__ xp, const int32_t *__restrict__ perm,
+                              int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        xp[i] = x[perm[i]];
+}
+cudaError_t launch_gather_f64(const double *x, double *xp, const int32_t *perm, int64_t n, cudaStream_t st) {
+    gather_kernel<<<608, 256, 0, st>>>(x, xp, perm, n);
     count_launch(); return cudaGetLastError();
 }
 cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st) {

@@ -42,18 +42,19 @@ cudaError_t launch_fill(const FillJob *jobs, int njobs, const int32_t *idx, cons
                         cudaStream_t st);
 cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStream_t st);
 
-// Matvec: one block-row GEMV launch over targets [t0, t1); ctr must be 0.
-// Sources and outputs in original point order are FP64 in both precisions.
-cudaError_t launch_brg_f64(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
-                           const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
-                           int32_t *err, cudaStream_t st);
-cudaError_t launch_brg_f32(const Target *T, const Panel *P, const Seg *S, int64_t t0, int64_t t1, int32_t *ctr,
-                           const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
-                           int32_t *err, cudaStream_t st);
+// Matvec: one block-row GEMV launch over targets [t0, t1) of the packed
+// target records (roff: record offsets, blob: records). xin / yout are FP64
+// in original point order when perm != NULL, in leaf order when perm == NULL.
+cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const double *A,
+                           double *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
+cudaError_t launch_brg_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const float *A,
+                           float *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
+cudaError_t launch_gather_f64(const double *x, double *xp, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
 constexpr int BRG_XS_ELEMS = 4096;    // gathered source width per target (elements)
 constexpr int BRG_MAX_PANELS = 32;    // panels per target
+constexpr int BRG_REC_WORDS = 1024;   // packed record of one target (int64 words)
 
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,
