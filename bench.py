@@ -292,9 +292,25 @@ def main():
         la, ms, by = op.profile_phases(prec)
         prof[nm] = (la, ms, by)
     op.profile(False)
+    # isolated matvecs per precision: per-phase device time
+    phase_us = {}
+    y_d = torch.empty_like(x_d)
+    for prec, nm in ((hw.PREC_FP32, "fp32"), (hw.PREC_FP64, "fp64")):
+        for _ in range(3):
+            op.matvec_device(xt_d.data_ptr(), y_d.data_ptr(), precision=prec)
+        op.profile(True)
+        for _ in range(20):
+            op.matvec_device(xt_d.data_ptr(), y_d.data_ptr(), precision=prec)
+        torch.cuda.synchronize()
+        la, ms, by = op.profile_phases(prec)
+        op.profile(False)
+        phase_us[nm] = {"us": [round(float(m) / max(int(l), 1) * 1e3, 2) for m, l in zip(ms, la)],
+                        "MB": [round(float(b) / 1e6, 2) for b in by],
+                        "total_us": round(float(ms.sum()) / 20 * 1e3, 1)}
     peak, peak_kind = load_peaks()
+    # entries 0..P-1: per-phase launches (phased mode); entry P: whole-matvec
+    # cooperative launches (default mode)
     best = None
-    tot_ms = sum(float(p[1].sum()) for p in prof.values())
     for nm, (la, ms, by) in prof.items():
         for q in range(len(la)):
             if la[q] == 0:
@@ -302,21 +318,29 @@ def main():
             if best is None or ms[q] > best[2]:
                 best = (nm, q, float(ms[q]), int(la[q]), float(by[q]))
     nm, q, msq, laq, byq = best
+    whole = q == len(prof[nm][0]) - 1
+    tot_ms = sum(float(p[1].sum()) for p in prof.values())
     achieved = byq / (msq / laq / 1e3) / 1e9
-    la32, ms32, by32 = prof["fp32"]
-    n_mv32 = int(la32.max()) if la32.size else 0
-    mv32_ms = float(ms32.sum()) / max(n_mv32, 1)
-    mv32_gbs = float((by32 * (la32 > 0)).sum()) / (mv32_ms / 1e3) / 1e9 if n_mv32 else 0.0
-    la64, ms64, by64 = prof["fp64"]
-    n_mv64 = int(la64.max()) if la64.size else 0
-    mv64_ms = float(ms64.sum()) / max(n_mv64, 1)
+    ctype = "float" if nm == "fp32" else "double"
+
+    def per_mv(p):
+        la, ms, by = p
+        n = int(la.max()) if la.size else 0
+        if n == 0:
+            return 0.0, 0.0
+        t = float(ms.sum()) / n
+        b = float(by[-1]) if la[-1] else float((by * (la > 0)).sum())
+        return t, b / (t / 1e3) / 1e9
+    mv32_ms, mv32_gbs = per_mv(prof["fp32"])
+    mv64_ms, mv64_gbs = per_mv(prof["fp64"])
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None,
-            "kernel": "brg_kernel<%s> phase %d (%s)" % ("float" if nm == "fp32" else "double", q,
-                                                        "of %d phases" % len(prof[nm][0])),
+            "kernel": ("brg_coop_kernel<%s> (one cooperative launch = one whole matvec, %d phases)"
+                       % (ctype, len(prof[nm][0]) - 1)) if whole else
+                      ("brg_kernel<%s> phase %d of %d" % (ctype, q, len(prof[nm][0]) - 1)),
             "bytes_per_launch": byq, "launch_us": msq / laq * 1e3, "launches": laq,
-            "share_of_gemv_time": msq / tot_ms if tot_ms else None, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
-            if peak_kind == "measured" else peak_kind}
+            "share_of_gemv_time": msq / tot_ms if tot_ms else None,
+            "peak_kind": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured" else peak_kind}
 
     # CPU baseline: the oracle on this host's cores
     cpu = None
@@ -345,8 +369,8 @@ def main():
         "mixed": {"ms_per_solve": ms_mixed / K, "outer": outer, "inner_total": inner, "resid": res_mixed,
                   "rel_err_vs_xtrue": err_mixed, "fp32_matvec_ms": mv32_ms, "fp32_matvec_gbs": mv32_gbs},
         "fp64": {"ms_per_solve": ms_fp64 / K, "iters": it64, "resid": res64, "rel_err_vs_xtrue": err_fp64,
-                 "matvec_ms": mv64_ms, "speedup_mixed_over_fp64": ms_fp64 / ms_mixed},
-        "assembly_s": t_asm, "storage_entries": storage,
+                 "matvec_ms": mv64_ms, "matvec_gbs": mv64_gbs, "speedup_mixed_over_fp64": ms_fp64 / ms_mixed},
+        "assembly_s": t_asm, "storage_entries": storage, "phases": phase_us,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -90,6 +90,9 @@ struct h2w_handle {
     DBuf<int64_t> d_roff, d_blob;  // packed target records of the matvec
     DBuf<double> d_ws, d_x, d_y;
     DBuf<int32_t> d_ctr, d_err;
+    DBuf<int64_t> d_pstart;
+    DBuf<unsigned> d_bar;
+    bool coop = true;  // one cooperative launch per matvec (else one launch per phase)
     DBuf<float> d_ws32;
     std::vector<Phase> phases;
     std::vector<int64_t> ph_op, ph_vec;   // per phase: operator and vector elements moved
@@ -519,6 +522,9 @@ struct PlanBuilder {
     int64_t opn = 0, fn = 0;
     int max_xfer_n = 0;
     int64_t read_elems = 0;
+    // phase window of the targets being emitted, and per target
+    int lo = 0, hi = 0;
+    std::vector<std::pair<int, int>> win;
 
     // column-major block: element (i, c) at a + c*lda + i, lda = pad4(rows)
     int64_t alloc(int64_t rows, int64_t cols, int32_t &lda) {
@@ -574,6 +580,7 @@ struct PlanBuilder {
                 for (auto &p : panels) tg.ldsum += p.lda;
                 tg.gsz = xo >= 256 ? 32 : (xo >= 128 ? 16 : (xo >= 48 ? 8 : 4));
                 T.push_back(tg);
+                win.push_back({lo, hi});
             }
             return;
         }
@@ -755,9 +762,13 @@ void build_plan(h2w_handle *h) {
     auto child_off = [&](const Skel &s, int64_t k) { return s.ptr[(size_t)(k * t.nch)]; };
     auto child_len = [&](const Skel &s, int64_t k) { return s.ptr[(size_t)((k + 1) * t.nch)] - s.ptr[(size_t)(k * t.nch)]; };
 
+    // Phase windows (2L+1 phases): up_j at L-j; M2L_j within [L-j+1, L+j-2]
+    // (level 1: L); down_j at L+j; leaf at 2L; near field and pair phase A
+    // anywhere before the leaf phase. Flexible targets are spread later.
+    const int NPH = 2 * L + 1;
     // ---- UP phases, levels L..1
     for (int j = L; j >= 1; --j) {
-        int64_t t0 = (int64_t)pb.T.size();
+        pb.lo = pb.hi = L - j;
         for (int kind = 0; kind < 2; ++kind) {
             if (kind == 0 && !(has_far && j >= 2)) continue;
             if (kind == 1 && !has_ver) continue;
@@ -780,14 +791,14 @@ void build_plan(h2w_handle *h) {
                 pb.emit(outb + s.ptr[(size_t)k], x.r, T_ACCUM, {ps});
             }
         }
-        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
     }
 
     // ---- coupling phase: M2L (far, vertex), near field, pair phase A
     std::vector<std::vector<int64_t>> pfac((size_t)L + 1);
     {
-        int64_t t0 = (int64_t)pb.T.size();
         for (int j = 1; j <= L; ++j) {
+            pb.lo = L - j + 1;
+            pb.hi = j == 1 ? L : L + j - 2;
             for (int kind = 0; kind < 2; ++kind) {
                 if (kind == 0 && !(has_far && j >= 2)) continue;
                 if (kind == 1 && !has_ver) continue;
@@ -834,6 +845,8 @@ void build_plan(h2w_handle *h) {
             }
         }
         // near field: neighbour slots in order, then self (assemble_NearField)
+        pb.lo = 0;
+        pb.hi = NPH - 2;
         for (int64_t k = 0; k < t.nbox[(size_t)L]; ++k) {
             int32_t n = (int32_t)t.cnt(L, k);
             if (n == 0) continue;
@@ -904,7 +917,6 @@ void build_plan(h2w_handle *h) {
                     pb.emit(to[(size_t)j] + Pp.ptr[p], r, T_ACCUM, {ps});
                 }
             }
-        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
     }
 
     // ---- pair phase B matrices per box: [Ac_p1 | Ac_p2 | ...] (n_box x sum r_p)
@@ -964,7 +976,7 @@ void build_plan(h2w_handle *h) {
         }
     // ---- DOWN phases, levels 1..L-1, then the leaf phase
     for (int j = 1; j < L; ++j) {
-        int64_t t0 = (int64_t)pb.T.size();
+        pb.lo = pb.hi = L + j;
         for (int kind = 0; kind < 2; ++kind) {
             if (kind == 0 && !(has_far && j >= 2)) continue;
             if (kind == 1 && !has_ver) continue;
@@ -984,10 +996,9 @@ void build_plan(h2w_handle *h) {
                 pb.emit(cinb + child_off(cs, k), x.rows, T_ACCUM, {ps});
             }
         }
-        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
     }
     {
-        int64_t t0 = (int64_t)pb.T.size();
+        pb.lo = pb.hi = NPH - 1;
         for (int64_t k = 0; k < t.nbox[(size_t)L]; ++k) {
             int32_t n = (int32_t)t.cnt(L, k);
             if (n == 0) continue;
@@ -1024,7 +1035,47 @@ void build_plan(h2w_handle *h) {
                 }
             pb.emit(h->yperm_off + t.off[(size_t)L][(size_t)k], n, T_ACCUM | T_SCATTER, pans);
         }
-        h->phases.push_back({t0, (int64_t)pb.T.size(), 0});
+    }
+    // ---- phase assignment: fixed targets at their phase, flexible targets
+    // (largest first) into the least-loaded phase of their window
+    {
+        const size_t nt = pb.T.size();
+        std::vector<int> ph(nt, 0);
+        std::vector<double> load((size_t)NPH, 0.0);
+        std::vector<size_t> flex;
+        auto elems = [&](size_t q) { return (double)pb.T[q].nrows * (double)pb.T[q].xw; };
+        for (size_t q = 0; q < nt; ++q) {
+            if (pb.win[q].first == pb.win[q].second) {
+                ph[q] = pb.win[q].first;
+                load[(size_t)ph[q]] += elems(q);
+            } else {
+                flex.push_back(q);
+            }
+        }
+        std::stable_sort(flex.begin(), flex.end(), [&](size_t a, size_t b) { return elems(a) > elems(b); });
+        for (size_t q : flex) {
+            int best = pb.win[q].first;
+            for (int p2 = pb.win[q].first; p2 <= pb.win[q].second; ++p2)
+                if (load[(size_t)p2] < load[(size_t)best]) best = p2;
+            ph[q] = best;
+            load[(size_t)best] += elems(q);
+        }
+        std::vector<size_t> order(nt);
+        for (size_t q = 0; q < nt; ++q) order[q] = q;
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            if (ph[a] != ph[b]) return ph[a] < ph[b];
+            return elems(a) > elems(b);
+        });
+        std::vector<Target> T2(nt);
+        for (size_t q = 0; q < nt; ++q) T2[q] = pb.T[order[q]];
+        pb.T.swap(T2);
+        h->phases.clear();
+        size_t q = 0;
+        for (int p2 = 0; p2 < NPH; ++p2) {
+            size_t q0 = q;
+            while (q < nt && ph[order[q]] == p2) ++q;
+            if (q > q0) h->phases.push_back({(int64_t)q0, (int64_t)q, 0});
+        }
     }
     // leaves without any far contribution would never be scattered by the
     // fused path; fall back to an explicit scatter then.
@@ -1038,10 +1089,6 @@ void build_plan(h2w_handle *h) {
             for (int64_t q = lp.t0; q < lp.t1; ++q)
                 if (pb.T[(size_t)q].flags & T_SCATTER) pb.T[(size_t)q].flags = T_ACCUM;
     }
-    for (auto &ph : h->phases)
-        std::stable_sort(pb.T.begin() + ph.t0, pb.T.begin() + ph.t1, [](const Target &a, const Target &b) {
-            return (int64_t)a.nrows * a.xw > (int64_t)b.nrows * b.xw;
-        });
     h->ph_op.assign(h->phases.size(), 0);
     h->ph_vec.assign(h->phases.size(), 0);
     for (size_t pi = 0; pi < h->phases.size(); ++pi) {
@@ -1119,6 +1166,18 @@ void build_plan(h2w_handle *h) {
     h->d_ctr.alloc(h->phases.size() + 1);
     h->d_err.alloc(1);
     CK(cudaMemsetAsync(h->d_err.p, 0, 4, st));
+    {
+        std::vector<int64_t> ps;
+        for (auto &ph : h->phases) ps.push_back(ph.t0);
+        ps.push_back(h->phases.empty() ? 0 : h->phases.back().t1);
+        h->d_pstart.upload(ps, st);
+    }
+    h->d_bar.alloc(2);
+    CK(cudaMemsetAsync(h->d_bar.p, 0, 8, st));
+    {
+        const char *m = getenv("H2W_MATVEC");
+        h->coop = !(m && std::string(m) == "phased");
+    }
     CK(cudaStreamSynchronize(st));
     h->d_op32.reset();
     h->d_ws32.reset();
@@ -1208,9 +1267,11 @@ cudaEvent_t prof_event(h2w_handle *h) {
     return e;
 }
 
+// phase == number of phases: the whole matvec (cooperative launch)
 template <class F>
 void prof_launch(h2w_handle *h, int prec, int phase, cudaStream_t st, F &&launch) {
-    if (!h->prof || h->phases[(size_t)phase].t1 <= h->phases[(size_t)phase].t0) {
+    const bool whole = phase >= (int)h->phases.size();
+    if (!h->prof || (!whole && h->phases[(size_t)phase].t1 <= h->phases[(size_t)phase].t0)) {
         CK(launch());
         return;
     }
@@ -1225,12 +1286,20 @@ void prof_launch(h2w_handle *h, int prec, int phase, cudaStream_t st, F &&launch
 // scatter per product); otherwise original point order.
 void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st, bool permuted = false) {
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
+    const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
-    for (size_t q = 0; q < h->phases.size(); ++q) {
-        const Phase &ph = h->phases[q];
-        prof_launch(h, H2W_PREC_FP64, (int)q, st, [&] {
-            return launch_brg_f64(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op.p, h->d_ws.p, dx, dy, perm, st);
+    if (h->coop) {
+        prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
+            return launch_coop_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op.p, h->d_ws.p, dx, dy, perm,
+                                   h->d_bar.p, h->d_err.p, st);
         });
+    } else {
+        for (size_t q = 0; q < h->phases.size(); ++q) {
+            const Phase &ph = h->phases[q];
+            prof_launch(h, H2W_PREC_FP64, (int)q, st, [&] {
+                return launch_brg_f64(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op.p, h->d_ws.p, dx, dy, perm, st);
+            });
+        }
     }
     if (!h->fused_scatter) {
         if (permuted)
@@ -1253,12 +1322,21 @@ void ensure_f32(h2w_handle *h) {
 void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st, bool permuted = false) {
     ensure_f32(h);
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
+    const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
-    for (size_t q = 0; q < h->phases.size(); ++q) {
-        const Phase &ph = h->phases[q];
-        prof_launch(h, H2W_PREC_FP32, (int)q, st, [&] {
-            return launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, h->d_ws32.p, dx, dy, perm, st);
+    if (h->coop) {
+        prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
+            return launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op32.p, h->d_ws32.p, dx, dy,
+                                   perm, h->d_bar.p, h->d_err.p, st);
         });
+    } else {
+        for (size_t q = 0; q < h->phases.size(); ++q) {
+            const Phase &ph = h->phases[q];
+            prof_launch(h, H2W_PREC_FP32, (int)q, st, [&] {
+                return launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, h->d_ws32.p, dx, dy, perm,
+                                      st);
+            });
+        }
     }
     if (!h->fused_scatter) {
         if (permuted) CK(vec_f32_to_f64(h->d_ws32.p + h->yperm_off, dy, h->tree.N, st));
@@ -1374,6 +1452,20 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     *resid = dnorm(h, h->g_r.p) / normb;
     *iters = max_iter;
     return *resid < tol ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+}
+
+// Device-side failure flag of the cooperative matvec (a grid barrier whose
+// bounded wait ran out).
+void check_device_error(h2w_handle *h) {
+    if (!h->d_err.p) return;
+    int32_t e = 0;
+    CK(cudaMemcpyAsync(&e, h->d_err.p, 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (e) {
+        CK(cudaMemsetAsync(h->d_err.p, 0, 4, h->stream));
+        CK(cudaMemsetAsync(h->d_bar.p, 0, 8, h->stream));
+        throw ApiError(H2W_ERR_CUDA, "matvec: a grid-barrier wait ran out (device error flag)");
+    }
 }
 
 int fail(h2w_handle *h, int code, const std::string &m) {
@@ -1762,7 +1854,10 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
             }
             if (where == H2W_HOST) CK(cudaMemcpyAsync(yc, h->d_y.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
         }
-        if (where == H2W_HOST) CK(cudaStreamSynchronize(st));
+        if (where == H2W_HOST) {
+            CK(cudaStreamSynchronize(st));
+            check_device_error(h);
+        }
         return H2W_OK;
     });
 }
@@ -1792,6 +1887,7 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
         int rc = gmres_run(h, bp.p, xp.p, max_iter, tol, H2W_PREC_FP64, iters, resid);
         CK(launch_scatter_f64(xp.p, dx, h->d_perm.p, N, h->stream));
         CK(cudaStreamSynchronize(h->stream));
+        check_device_error(h);
         if (where == H2W_HOST) {
             CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream));
             CK(cudaStreamSynchronize(h->stream));
@@ -1858,6 +1954,7 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
             CK(cudaMemcpyAsync(x, h->d_x.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
         }
         CK(cudaStreamSynchronize(st));
+        check_device_error(h);
         return rc;
     });
 }
@@ -1880,16 +1977,21 @@ int h2w_profile_phases(h2w_handle *h, int precision, int max_phases, int64_t *la
                        int *nphases) {
     return guarded(h, [&] {
         require_op(h);
-        const int np = (int)h->phases.size();
+        const int np = (int)h->phases.size() + 1;  // last entry: whole-matvec (cooperative) launches
         if (nphases) *nphases = np;
         if (!launches || !ms || !bytes) return H2W_OK;
         CK(cudaDeviceSynchronize());
         const double w = precision == H2W_PREC_FP32 ? 4.0 : 8.0;
+        double tot = 0.0;
         for (int q = 0; q < std::min(np, max_phases); ++q) {
             launches[q] = 0;
             ms[q] = 0.0;
-            bytes[q] = (double)(h->ph_op[(size_t)q] + h->ph_vec[(size_t)q]) * w;
+            if (q < np - 1) {
+                bytes[q] = (double)(h->ph_op[(size_t)q] + h->ph_vec[(size_t)q]) * w;
+                tot += bytes[q];
+            }
         }
+        if (np - 1 < max_phases) bytes[np - 1] = tot;
         for (auto &r : h->prof_recs) {
             if (r.prec != precision || r.phase >= max_phases) continue;
             float t = 0.f;

@@ -471,129 +471,190 @@ constexpr int BRG_WARPS = BRG_THREADS / 32;
 //   [0] dst   [1] nrows | flags << 32   [2] np | ns << 32
 //   np panels x 3 words: a, lda | w << 32, xoff
 //   ns segments x 2 words: src, len | (xoff << 1 | gather) << 32  (xoff: offset in the target's gathered x)
+template <class T> struct BrgShared {
+    T xs[BRG_XS_ELEMS];
+    T red[BRG_THREADS];
+    int64_t rec[BRG_REC_WORDS];
+};
+
+// One target: rows [dst, dst+nrows) from its packed record (see above).
+template <class T>
+__device__ __forceinline__ void brg_target(BrgShared<T> &sh, int64_t t, const int64_t *__restrict__ roff,
+                                           const int64_t *__restrict__ blob, const T *__restrict__ A, T *ws,
+                                           const double *__restrict__ xin, double *yout,
+                                           const int32_t *__restrict__ perm) {
+    T *xs = sh.xs;
+    T *red = sh.red;
+    int64_t *rec = sh.rec;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t o = roff[t];
+    const int nw = (int)(roff[t + 1] - o);
+    for (int q = tid; q < nw; q += BRG_THREADS) rec[q] = blob[o + q];
+    __syncthreads();
+    const int64_t dst = rec[0];
+    const int nrows = (int)(rec[1] & 0xffffffff), flags = (int)(rec[1] >> 32);
+    const int np = (int)(rec[2] & 0xffffffff), ns = (int)(rec[2] >> 32);
+    const int64_t *pan = rec + 3;
+    const int64_t *seg = pan + 3 * np;
+    // gather: every thread walks the segments for its elements
+    {
+        int sidx = 0;
+        int64_t s_src = 0;
+        int s_lo = 0, s_hi = -1, s_g = 0;
+        auto seek = [&](int e) {
+            while (e >= s_hi && sidx < ns) {
+                const int64_t w1 = seg[2 * sidx + 1];
+                s_src = seg[2 * sidx];
+                const int len = (int)(w1 & 0xffffffff);
+                const int code = (int)(w1 >> 32);
+                s_lo = code >> 1;
+                s_hi = s_lo + len;
+                s_g = code & 1;
+                ++sidx;
+            }
+        };
+        // elements of the concatenated sources, in segment order
+        int total = 0;
+        if (ns > 0) {
+            const int64_t wl = seg[2 * (ns - 1) + 1];
+            total = (int)(wl >> 33) + (int)(wl & 0xffffffff);
+        }
+        for (int e0 = tid; e0 < total; e0 += 4 * BRG_THREADS) {
+            int64_t idx4[4];
+            int xo4[4], g4[4];
+            int cnt = 0;
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * BRG_THREADS;
+                if (e >= total) break;
+                seek(e);
+                if (e < s_lo) {  // padding gap between panels
+                    idx4[u] = -1;
+                } else {
+                    idx4[u] = s_src + (e - s_lo);
+                }
+                xo4[u] = e;
+                g4[u] = s_g;
+                ++cnt;
+            }
+            T v4[4];
+            for (int u = 0; u < cnt; ++u) {
+                const int64_t ix = idx4[u];
+                if (ix < 0) v4[u] = T(0);
+                else if (g4[u]) v4[u] = (T)xin[perm ? (int64_t)perm[ix] : ix];
+                else v4[u] = ws[ix];
+            }
+            for (int u = 0; u < cnt; ++u) xs[xo4[u]] = v4[u];
+        }
+    }
+    __syncthreads();
+    for (int rb = 0; rb < nrows; rb += BRG_THREADS) {
+        const int rows = nrows - rb < BRG_THREADS ? nrows - rb : BRG_THREADS;
+        const int RG = (rows + 31) >> 5;
+        const int S = BRG_WARPS / RG;
+        const int rg = warp % RG, sl = warp / RG;
+        const int i = rb + rg * 32 + lane;
+        T acc = T(0);
+        if (sl < S && i < nrows) {
+            for (int q = 0; q < np; ++q) {
+                const int64_t pa = pan[3 * q];
+                const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
+                const int xoff = (int)pan[3 * q + 2];
+                const int c0 = (int)(((int64_t)w * sl) / S), c1 = (int)(((int64_t)w * (sl + 1)) / S);
+                const T *col = A + pa + i + (int64_t)c0 * lda;
+                const T *xp = xs + xoff;
+                const int64_t ld = lda;
+                int c = c0;
+                T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+                for (; c + 7 < c1; c += 8, col += 8 * ld) {
+                    const T v0 = col[0], v1 = col[ld], v2 = col[2 * ld], v3 = col[3 * ld];
+                    const T v4 = col[4 * ld], v5 = col[5 * ld], v6 = col[6 * ld], v7 = col[7 * ld];
+                    a0 += v0 * xp[c];
+                    a1 += v1 * xp[c + 1];
+                    a2 += v2 * xp[c + 2];
+                    a3 += v3 * xp[c + 3];
+                    a0 += v4 * xp[c + 4];
+                    a1 += v5 * xp[c + 5];
+                    a2 += v6 * xp[c + 6];
+                    a3 += v7 * xp[c + 7];
+                }
+                for (; c < c1; ++c, col += ld) a0 += col[0] * xp[c];
+                acc += (a0 + a1) + (a2 + a3);
+            }
+        }
+        red[tid] = acc;
+        __syncthreads();
+        if (sl == 0 && i < nrows) {
+            T v = acc;
+            for (int q = 1; q < S; ++q) v += red[(rg + q * RG) * 32 + lane];
+            const int64_t d = dst + i;
+            if (flags & T_SCATTER) {
+                const T ov = (flags & T_ACCUM) ? ws[d] + v : v;
+                yout[perm ? (int64_t)perm[d] : d] = (double)ov;
+            } else if (flags & T_ATOMIC) {
+                atomicAdd(ws + d, v);
+            } else if (flags & T_ACCUM) {
+                ws[d] += v;
+            } else {
+                ws[d] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <class T>
 __global__ void __launch_bounds__(BRG_THREADS, 4)
     brg_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
                const T *__restrict__ A, T *ws, const double *__restrict__ xin, double *yout,
                const int32_t *__restrict__ perm) {
-    __shared__ T xs[BRG_XS_ELEMS];
-    __shared__ T red[BRG_THREADS];
-    __shared__ int64_t rec[BRG_REC_WORDS];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) {
-        const int64_t o = roff[t];
-        const int nw = (int)(roff[t + 1] - o);
-        for (int q = tid; q < nw; q += BRG_THREADS) rec[q] = blob[o + q];
-        __syncthreads();
-        const int64_t dst = rec[0];
-        const int nrows = (int)(rec[1] & 0xffffffff), flags = (int)(rec[1] >> 32);
-        const int np = (int)(rec[2] & 0xffffffff), ns = (int)(rec[2] >> 32);
-        const int64_t *pan = rec + 3;
-        const int64_t *seg = pan + 3 * np;
-        // gather: every thread walks the segments for its elements
-        {
-            int sidx = 0;
-            int64_t s_src = 0;
-            int s_lo = 0, s_hi = -1, s_g = 0;
-            auto seek = [&](int e) {
-                while (e >= s_hi && sidx < ns) {
-                    const int64_t w1 = seg[2 * sidx + 1];
-                    s_src = seg[2 * sidx];
-                    const int len = (int)(w1 & 0xffffffff);
-                    const int code = (int)(w1 >> 32);
-                    s_lo = code >> 1;
-                    s_hi = s_lo + len;
-                    s_g = code & 1;
-                    ++sidx;
+    __shared__ BrgShared<T> sh;
+    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) brg_target<T>(sh, t, roff, blob, A, ws, xin, yout, perm);
+}
+
+// Grid-wide barrier for the cooperative matvec (all CTAs are co-resident by
+// construction of the cooperative launch). bar[0] counts arrivals, bar[1] is
+// the generation. The spin is bounded: a barrier that never completes sets
+// *err and lets the CTA continue, so the kernel always ends.
+__device__ void grid_barrier(unsigned *bar, unsigned nblocks, int32_t *err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == gen) {
+                if (++it > (1LL << 26)) {
+                    atomicExch(err, 1);
+                    break;
                 }
-            };
-            // elements of the concatenated sources, in segment order
-            int total = 0;
-            if (ns > 0) {
-                const int64_t wl = seg[2 * (ns - 1) + 1];
-                total = (int)(wl >> 33) + (int)(wl & 0xffffffff);
-            }
-            for (int e0 = tid; e0 < total; e0 += 4 * BRG_THREADS) {
-                int64_t idx4[4];
-                int xo4[4], g4[4];
-                int cnt = 0;
-                for (int u = 0; u < 4; ++u) {
-                    const int e = e0 + u * BRG_THREADS;
-                    if (e >= total) break;
-                    seek(e);
-                    if (e < s_lo) {  // padding gap between panels
-                        idx4[u] = -1;
-                    } else {
-                        idx4[u] = s_src + (e - s_lo);
-                    }
-                    xo4[u] = e;
-                    g4[u] = s_g;
-                    ++cnt;
-                }
-                T v4[4];
-                for (int u = 0; u < cnt; ++u) {
-                    const int64_t ix = idx4[u];
-                    if (ix < 0) v4[u] = T(0);
-                    else if (g4[u]) v4[u] = (T)xin[perm ? (int64_t)perm[ix] : ix];
-                    else v4[u] = ws[ix];
-                }
-                for (int u = 0; u < cnt; ++u) xs[xo4[u]] = v4[u];
+                __nanosleep(32);
             }
         }
-        __syncthreads();
-        for (int rb = 0; rb < nrows; rb += BRG_THREADS) {
-            const int rows = nrows - rb < BRG_THREADS ? nrows - rb : BRG_THREADS;
-            const int RG = (rows + 31) >> 5;
-            const int S = BRG_WARPS / RG;
-            const int rg = warp % RG, sl = warp / RG;
-            const int i = rb + rg * 32 + lane;
-            T acc = T(0);
-            if (sl < S && i < nrows) {
-                for (int q = 0; q < np; ++q) {
-                    const int64_t pa = pan[3 * q];
-                    const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
-                    const int xoff = (int)pan[3 * q + 2];
-                    const int c0 = (int)(((int64_t)w * sl) / S), c1 = (int)(((int64_t)w * (sl + 1)) / S);
-                    const T *col = A + pa + i + (int64_t)c0 * lda;
-                    const T *xp = xs + xoff;
-                    const int64_t ld = lda;
-                    int c = c0;
-                    T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-                    for (; c + 7 < c1; c += 8, col += 8 * ld) {
-                        const T v0 = col[0], v1 = col[ld], v2 = col[2 * ld], v3 = col[3 * ld];
-                        const T v4 = col[4 * ld], v5 = col[5 * ld], v6 = col[6 * ld], v7 = col[7 * ld];
-                        a0 += v0 * xp[c];
-                        a1 += v1 * xp[c + 1];
-                        a2 += v2 * xp[c + 2];
-                        a3 += v3 * xp[c + 3];
-                        a0 += v4 * xp[c + 4];
-                        a1 += v5 * xp[c + 5];
-                        a2 += v6 * xp[c + 6];
-                        a3 += v7 * xp[c + 7];
-                    }
-                    for (; c < c1; ++c, col += ld) a0 += col[0] * xp[c];
-                    acc += (a0 + a1) + (a2 + a3);
-                }
-            }
-            red[tid] = acc;
-            __syncthreads();
-            if (sl == 0 && i < nrows) {
-                T v = acc;
-                for (int q = 1; q < S; ++q) v += red[(rg + q * RG) * 32 + lane];
-                const int64_t d = dst + i;
-                if (flags & T_SCATTER) {
-                    const T ov = (flags & T_ACCUM) ? ws[d] + v : v;
-                    yout[perm ? (int64_t)perm[d] : d] = (double)ov;
-                } else if (flags & T_ATOMIC) {
-                    atomicAdd(ws + d, v);
-                } else if (flags & T_ACCUM) {
-                    ws[d] += v;
-                } else {
-                    ws[d] = v;
-                }
-            }
-            __syncthreads();
-        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// The whole matvec in one cooperative launch: phases separated by grid
+// barriers; targets of a phase striped over the CTAs.
+template <class T>
+__global__ void __launch_bounds__(BRG_THREADS, 4)
+    brg_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
+                    const int64_t *__restrict__ pstart, int nphase, const T *__restrict__ A, T *ws,
+                    const double *__restrict__ xin, double *yout, const int32_t *__restrict__ perm, unsigned *bar,
+                    int32_t *err) {
+    __shared__ BrgShared<T> sh;
+    for (int p = 0; p < nphase; ++p) {
+        const int64_t t1 = pstart[p + 1];
+        for (int64_t t = pstart[p] + blockIdx.x; t < t1; t += gridDim.x)
+            brg_target<T>(sh, t, roff, blob, A, ws, xin, yout, perm);
+        if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
     }
 }
 
@@ -620,6 +681,42 @@ static cudaError_t launch_brg_t(const int64_t *roff, const int64_t *blob, int64_
     brg_kernel<T><<<grid, BRG_THREADS, 0, st>>>(roff, blob, t0, t1, A, ws, xin, yout, perm);
     count_launch();
     return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t launch_coop_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                                 const T *A, T *ws, const double *xin, double *yout, const int32_t *perm,
+                                 unsigned *bar, int32_t *err, cudaStream_t st) {
+    if (nphase <= 0) return cudaSuccess;
+    static int per_sm = 0;
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brg_coop_kernel<T>, BRG_THREADS, 0);
+        if (per_sm <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    }
+    const int grid = g_num_sms * per_sm;
+    void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&A, (void *)&ws,
+                    (void *)&xin, (void *)&yout, (void *)&perm, (void *)&bar, (void *)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)brg_coop_kernel<T>, dim3(grid), dim3(BRG_THREADS), args,
+                                                0, st);
+    count_launch();
+    return e;
+}
+
+cudaError_t launch_coop_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
+                            unsigned *bar, int32_t *err, cudaStream_t st) {
+    return launch_coop_t<double>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, st);
+}
+cudaError_t launch_coop_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
+                            unsigned *bar, int32_t *err, cudaStream_t st) {
+    return launch_coop_t<float>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, st);
 }
 
 cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const double *A,

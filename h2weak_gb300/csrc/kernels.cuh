@@ -49,6 +49,14 @@ cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0,
                            double *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
 cudaError_t launch_brg_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const float *A,
                            float *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
+// The whole matvec as one cooperative launch: phase p covers targets
+// [pstart[p], pstart[p+1]); bar (2 unsigned, zero) is the grid barrier state.
+cudaError_t launch_coop_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
+                            unsigned *bar, int32_t *err, cudaStream_t st);
+cudaError_t launch_coop_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
+                            unsigned *bar, int32_t *err, cudaStream_t st);
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_gather_f64(const double *x, double *xp, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
