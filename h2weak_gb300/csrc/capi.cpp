@@ -64,7 +64,7 @@ template <class T> struct DBuf {
 inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
 
 constexpr int XW_CAP = 4096;          // gathered source width per target (elements)
-constexpr int64_t ROW_SPLIT = 262144;  // rows * width above which a target is split (load balance)
+constexpr int64_t ROW_SPLIT = 16384;  // rows * width above which a target is split (load balance)
 
 }  // namespace
 
@@ -553,7 +553,9 @@ struct PlanBuilder {
         for (auto &p : panels) read_elems += (int64_t)nrows * p.w;
         if (xw == 0) return;
         if (xw <= XW_CAP) {
-            int64_t rows_per = std::max<int64_t>(1, std::min<int64_t>(nrows, ROW_SPLIT / std::max<int64_t>(xw, 1)));
+            // row chunks are multiples of 4 rows so the kernel's 16-byte column loads stay aligned
+            int64_t rows_per = std::max<int64_t>(4, (ROW_SPLIT / std::max<int64_t>(xw, 1)) & ~int64_t(3));
+            rows_per = std::min<int64_t>(rows_per, nrows);
             for (int64_t r0 = 0; r0 < nrows; r0 += rows_per) {
                 int32_t nr = (int32_t)std::min<int64_t>(rows_per, nrows - r0);
                 Target tg{};
@@ -628,7 +630,8 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
         for (int32_t q = t.p0; q < t.p1; ++q) {
             const Panel &p = pb.P[(size_t)q];
             if (p.a < 0 || p.w < 1 || p.lda < 1) bad("panel layout");
-            if (p.a + (int64_t)(p.w - 1) * p.lda + t.nrows > opn) bad("panel extent");
+            const bool vec = (p.a % 4 == 0) && (p.lda % 4 == 0);
+            if (p.a + (int64_t)(p.w - 1) * p.lda + (vec ? pad4(t.nrows) : t.nrows) > opn) bad("panel extent");
             if (p.xoff % 4 || p.xoff != xw) bad("panel xoff");
             if (p.s0 < 0 || p.s1 < p.s0 || p.s1 > (int32_t)pb.S.size()) bad("panel segs");
             for (int32_t e = p.s0; e < p.s1; ++e) {

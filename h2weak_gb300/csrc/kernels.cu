@@ -471,9 +471,23 @@ constexpr int BRG_WARPS = BRG_THREADS / 32;
 //   [0] dst   [1] nrows | flags << 32   [2] np | ns << 32
 //   np panels x 3 words: a, lda | w << 32, xoff
 //   ns segments x 2 words: src, len | (xoff << 1 | gather) << 32  (xoff: offset in the target's gathered x)
+template <class T> struct Vec16;
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+__device__ __forceinline__ void vfma(double *acc, const double2 v, const double x) {
+    acc[0] += v.x * x;
+    acc[1] += v.y * x;
+}
+__device__ __forceinline__ void vfma(float *acc, const float4 v, const float x) {
+    acc[0] += v.x * x;
+    acc[1] += v.y * x;
+    acc[2] += v.z * x;
+    acc[3] += v.w * x;
+}
+
 template <class T> struct BrgShared {
     T xs[BRG_XS_ELEMS];
-    T red[BRG_THREADS];
+    T red[BRG_WARPS * 32 * Vec16<T>::n];
     int64_t rec[BRG_REC_WORDS];
 };
 
@@ -547,45 +561,78 @@ __device__ __forceinline__ void brg_target(BrgShared<T> &sh, int64_t t, const in
         }
     }
     __syncthreads();
-    for (int rb = 0; rb < nrows; rb += BRG_THREADS) {
-        const int rows = nrows - rb < BRG_THREADS ? nrows - rb : BRG_THREADS;
-        const int RG = (rows + 31) >> 5;
-        const int S = BRG_WARPS / RG;
-        const int rg = warp % RG, sl = warp / RG;
-        const int i = rb + rg * 32 + lane;
-        T acc = T(0);
-        if (sl < S && i < nrows) {
+    // Rows in blocks of RB = 32*VN. Within a block, a warp's lane l owns the
+    // VN-row slice rq = l % RQ (16-byte vector loads down a column) and
+    // column phase cs = l / RQ, so one load instruction covers 32/RQ columns.
+    // The warps of the CTA split the columns of each block.
+    using V16 = typename Vec16<T>::type;
+    constexpr int VN = Vec16<T>::n;
+    constexpr int RB = 32 * VN;
+    const int nblk = (nrows + RB - 1) / RB;
+    for (int bb = 0; bb < nblk; bb += BRG_WARPS) {
+        const int nb_here = nblk - bb < BRG_WARPS ? nblk - bb : BRG_WARPS;
+        const int S = BRG_WARPS / nb_here;        // warps (column slices) per row block
+        const int myb = warp % nb_here, sl = warp / nb_here;
+        const int rb = (bb + myb) * RB;
+        const int rows = nrows - rb < RB ? nrows - rb : RB;
+        int RQ = 1;
+        while (RQ * VN < rows) RQ <<= 1;          // row slices of this block (power of two <= 32)
+        const int CS = 32 / RQ;                   // column phases per load
+        const int rq = lane % RQ, cs = lane / RQ;
+        const int r_lo = rb + rq * VN;            // first row of the lane's slice
+        T acc[VN];
+#pragma unroll
+        for (int v = 0; v < VN; ++v) acc[v] = T(0);
+        if (sl < S && r_lo < nrows) {
             for (int q = 0; q < np; ++q) {
                 const int64_t pa = pan[3 * q];
                 const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
                 const int xoff = (int)pan[3 * q + 2];
                 const int c0 = (int)(((int64_t)w * sl) / S), c1 = (int)(((int64_t)w * (sl + 1)) / S);
-                const T *col = A + pa + i + (int64_t)c0 * lda;
                 const T *xp = xs + xoff;
                 const int64_t ld = lda;
-                int c = c0;
-                T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-                for (; c + 7 < c1; c += 8, col += 8 * ld) {
-                    const T v0 = col[0], v1 = col[ld], v2 = col[2 * ld], v3 = col[3 * ld];
-                    const T v4 = col[4 * ld], v5 = col[5 * ld], v6 = col[6 * ld], v7 = col[7 * ld];
-                    a0 += v0 * xp[c];
-                    a1 += v1 * xp[c + 1];
-                    a2 += v2 * xp[c + 2];
-                    a3 += v3 * xp[c + 3];
-                    a0 += v4 * xp[c + 4];
-                    a1 += v5 * xp[c + 5];
-                    a2 += v6 * xp[c + 6];
-                    a3 += v7 * xp[c + 7];
+                const T *base = A + pa + r_lo;
+                if (((pa & 3) == 0) && ((lda & 3) == 0)) {
+                    int c = c0 + cs;
+                    for (; c + 3 * CS < c1; c += 4 * CS) {
+                        const V16 v0 = *reinterpret_cast<const V16 *>(base + (int64_t)c * ld);
+                        const V16 v1 = *reinterpret_cast<const V16 *>(base + (int64_t)(c + CS) * ld);
+                        const V16 v2 = *reinterpret_cast<const V16 *>(base + (int64_t)(c + 2 * CS) * ld);
+                        const V16 v3 = *reinterpret_cast<const V16 *>(base + (int64_t)(c + 3 * CS) * ld);
+                        const T x0 = xp[c], x1 = xp[c + CS], x2 = xp[c + 2 * CS], x3 = xp[c + 3 * CS];
+                        vfma(acc, v0, x0);
+                        vfma(acc, v1, x1);
+                        vfma(acc, v2, x2);
+                        vfma(acc, v3, x3);
+                    }
+                    for (; c < c1; c += CS) vfma(acc, *reinterpret_cast<const V16 *>(base + (int64_t)c * ld), xp[c]);
+                } else {
+                    const int nv = nrows - r_lo < VN ? nrows - r_lo : VN;
+                    for (int c = c0 + cs; c < c1; c += CS) {
+                        const T xc = xp[c];
+                        const T *col = base + (int64_t)c * ld;
+#pragma unroll
+                        for (int v = 0; v < VN; ++v)
+                            if (v < nv) acc[v] += col[v] * xc;
+                    }
                 }
-                for (; c < c1; ++c, col += ld) a0 += col[0] * xp[c];
-                acc += (a0 + a1) + (a2 + a3);
             }
         }
-        red[tid] = acc;
+        // reduce over the column phases of the warp
+#pragma unroll
+        for (int v = 0; v < VN; ++v)
+            for (int o = RQ; o < 32; o <<= 1) acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], o);
+        if (cs == 0 && sl < S)
+#pragma unroll
+            for (int v = 0; v < VN; ++v) red[warp * RB + rq * VN + v] = acc[v];
         __syncthreads();
-        if (sl == 0 && i < nrows) {
-            T v = acc;
-            for (int q = 1; q < S; ++q) v += red[(rg + q * RG) * 32 + lane];
+        // combine the column slices of each block and write
+        for (int e = tid; e < nb_here * RB; e += BRG_THREADS) {
+            const int mb = e / RB, r = e % RB;
+            const int i = (bb + mb) * RB + r;
+            if (i >= nrows) continue;
+            T v = T(0);
+            for (int q = 0; q < S; ++q) v += red[(mb + q * nb_here) * RB + r];
             const int64_t d = dst + i;
             if (flags & T_SCATTER) {
                 const T ov = (flags & T_ACCUM) ? ws[d] + v : v;
