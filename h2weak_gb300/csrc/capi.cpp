@@ -63,8 +63,8 @@ template <class T> struct DBuf {
 
 inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
 
-constexpr int XW_CAP = 2048;          // gathered source width per target (elements)
-constexpr int64_t ROW_SPLIT = BRG_BUF_ELEMS;  // staged rows * width of one target
+constexpr int XW_CAP = 4096;          // gathered source width per target (elements)
+constexpr int64_t ROW_SPLIT = 16384;  // rows * width above which a target is split (load balance)
 
 }  // namespace
 
@@ -644,9 +644,6 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
             xw += pad4(p.w);
         }
         if (xw != t.xw || xw > XW_CAP || xw > BRG_XS_ELEMS) bad("target width");
-        int64_t wsum = 0;
-        for (int32_t q = t.p0; q < t.p1; ++q) wsum += pb.P[(size_t)q].w;
-        if (pad4(t.nrows) * wsum > BRG_BUF_ELEMS) bad("target exceeds the staging buffer");
     }
     for (const FactorJob &f : pb.factors)
         if (f.r < 1 || f.f < 0 || f.f + (int64_t)f.r * f.r > pb.fn || f.ii < 0 || f.ii + f.r > nidx || f.jj < 0 ||
@@ -1303,8 +1300,7 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
         for (size_t q = 0; q < h->phases.size(); ++q) {
             const Phase &ph = h->phases[q];
             prof_launch(h, H2W_PREC_FP64, (int)q, st, [&] {
-                return launch_phase_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p, (int)q, ph.t1 - ph.t0, h->d_op.p,
-                                        h->d_ws.p, dx, dy, perm, h->d_bar.p, h->d_err.p, st);
+                return launch_brg_f64(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op.p, h->d_ws.p, dx, dy, perm, st);
             });
         }
     }
@@ -1340,8 +1336,8 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
         for (size_t q = 0; q < h->phases.size(); ++q) {
             const Phase &ph = h->phases[q];
             prof_launch(h, H2W_PREC_FP32, (int)q, st, [&] {
-                return launch_phase_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p, (int)q, ph.t1 - ph.t0, h->d_op32.p,
-                                        h->d_ws32.p, dx, dy, perm, h->d_bar.p, h->d_err.p, st);
+                return launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, h->d_ws32.p, dx, dy, perm,
+                                      st);
             });
         }
     }

@@ -466,6 +466,7 @@ cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStr
 // column slices meet in shared memory.
 constexpr int BRG_THREADS = 256;
 constexpr int BRG_WARPS = BRG_THREADS / 32;
+constexpr int BRG_U = 4;  // vector loads per lane per round
 
 // Target record (int64 words), built by the host plan:
 //   [0] dst   [1] nrows | flags << 32   [2] np | ns << 32
@@ -485,129 +486,51 @@ __device__ __forceinline__ void vfma(float *acc, const float4 v, const float x) 
     acc[3] += v.w * x;
 }
 
-// Shared memory of one matvec CTA: two matrix staging buffers, three record
-// buffers (records run two targets ahead, matrix blocks one target ahead),
-// the gathered sources and the cross-warp partial sums.
+// VN rows of an unaligned column, zero past nv.
+template <class T> __device__ __forceinline__ typename Vec16<T>::type load_rows(const T *p, int nv);
+template <> __device__ __forceinline__ double2 load_rows<double>(const double *p, int nv) {
+    return make_double2(p[0], nv > 1 ? p[1] : 0.0);
+}
+template <> __device__ __forceinline__ float4 load_rows<float>(const float *p, int nv) {
+    return make_float4(p[0], nv > 1 ? p[1] : 0.f, nv > 2 ? p[2] : 0.f, nv > 3 ? p[3] : 0.f);
+}
+
 template <class T> struct BrgShared {
-    T buf[2][BRG_BUF_ELEMS];
     T xs[BRG_XS_ELEMS];
     T red[BRG_WARPS * 32 * Vec16<T>::n];
-    int64_t rec[3][BRG_REC_WORDS];
+    int64_t rec[BRG_REC_WORDS];
 };
 
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// Issue the asynchronous copy of a target's record into rec.
-__device__ __forceinline__ void brg_fetch_record(int64_t *rec, int64_t t, const int64_t *__restrict__ roff,
-                                                 const int64_t *__restrict__ blob) {
-    const int64_t o = roff[t];
-    const int nw = (int)(roff[t + 1] - o);
-    for (int q = threadIdx.x; q < nw; q += BRG_THREADS) cp_async8(rec + q, blob + o + q);
-}
-
-// Issue the asynchronous copy of a target's panels (column-major, rows
-// rounded up to 16 bytes) into a staging buffer; column stride sld = rows
-// rounded up to 4.
+// One target: rows [dst, dst+nrows) from its packed record (see above).
 template <class T>
-__device__ __forceinline__ void brg_fetch_matrix(T *buf, const int64_t *rec, const T *__restrict__ A) {
-    const int nrows = (int)(rec[1] & 0xffffffff);
-    const int np = (int)(rec[2] & 0xffffffff);
-    const int sld = (nrows + 3) & ~3;
-    constexpr int E16 = 16 / (int)sizeof(T);  // elements per 16 bytes
-    const int nch = (nrows + E16 - 1) / E16;  // 16-byte chunks per column
-    const int64_t *pan = rec + 3;
-    int so = 0;
-    for (int q = 0; q < np; ++q) {
-        const int64_t pa = pan[3 * q];
-        const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
-        T *dst = buf + so;
-        if (((pa & 3) == 0) && ((lda & 3) == 0)) {
-            const int tot = w * nch;
-            for (int e = threadIdx.x; e < tot; e += BRG_THREADS) {
-                const int c = e / nch, k = e % nch;
-                cp_async16(dst + c * sld + k * E16, A + pa + (int64_t)c * lda + k * E16);
-            }
-        } else {
-            const int tot = w * nrows;
-            for (int e = threadIdx.x; e < tot; e += BRG_THREADS) {
-                const int c = e / nrows, r = e % nrows;
-                if (sizeof(T) == 8) cp_async8(dst + c * sld + r, A + pa + (int64_t)c * lda + r);
-                else cp_async4(dst + c * sld + r, A + pa + (int64_t)c * lda + r);
-            }
-        }
-        so += w * sld;
-    }
-}
-
-// Gather a target's sources into xs, then multiply the staged panels.
-template <class T>
-__device__ __forceinline__ void brg_compute(BrgShared<T> &sh, const int64_t *rec, const T *buf, T *ws,
-                                            const double *__restrict__ xin, double *yout,
-                                            const int32_t *__restrict__ perm) {
+__device__ __forceinline__ void brg_target(BrgShared<T> &sh, int64_t t, const int64_t *__restrict__ roff,
+                                           const int64_t *__restrict__ blob, const T *__restrict__ A, T *ws,
+                                           const double *__restrict__ xin, double *yout,
+                                           const int32_t *__restrict__ perm) {
     T *xs = sh.xs;
     T *red = sh.red;
+    int64_t *rec = sh.rec;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t o = roff[t];
+    const int nw = (int)(roff[t + 1] - o);
+    for (int q = tid; q < nw; q += BRG_THREADS) rec[q] = blob[o + q];
+    __syncthreads();
     const int64_t dst = rec[0];
     const int nrows = (int)(rec[1] & 0xffffffff), flags = (int)(rec[1] >> 32);
     const int np = (int)(rec[2] & 0xffffffff), ns = (int)(rec[2] >> 32);
     const int64_t *pan = rec + 3;
     const int64_t *seg = pan + 3 * np;
-    {
-        int sidx = 0;
-        int64_t s_src = 0;
-        int s_lo = 0, s_hi = -1, s_g = 0;
-        int total = 0;
-        if (ns > 0) {
-            const int64_t wl = seg[2 * (ns - 1) + 1];
-            total = (int)(wl >> 33) + (int)(wl & 0xffffffff);
-        }
-        for (int e0 = tid; e0 < total; e0 += 4 * BRG_THREADS) {
-            int64_t idx4[4];
-            int g4[4], cnt = 0;
-            for (int u = 0; u < 4; ++u) {
-                const int e = e0 + u * BRG_THREADS;
-                if (e >= total) break;
-                while (e >= s_hi && sidx < ns) {
-                    const int64_t w1 = seg[2 * sidx + 1];
-                    s_src = seg[2 * sidx];
-                    const int code = (int)(w1 >> 32);
-                    s_lo = code >> 1;
-                    s_hi = s_lo + (int)(w1 & 0xffffffff);
-                    s_g = code & 1;
-                    ++sidx;
-                }
-                idx4[u] = e < s_lo ? -1 : s_src + (e - s_lo);
-                g4[u] = s_g;
-                ++cnt;
-            }
-            T v4[4];
-            for (int u = 0; u < cnt; ++u) {
-                const int64_t ix = idx4[u];
-                if (ix < 0) v4[u] = T(0);
-                else if (g4[u]) v4[u] = (T)xin[perm ? (int64_t)perm[ix] : ix];
-                else v4[u] = ws[ix];
-            }
-            for (int u = 0; u < cnt; ++u) xs[e0 + u * BRG_THREADS] = v4[u];
-        }
-    }
-    __syncthreads();
+    // Rows in blocks of RB = 32*VN. Within a block, a warp's lane l owns the
+    // VN-row slice rq = l % RQ (16-byte vector loads down a column) and
+    // column phase cs = l / RQ, so one load instruction covers 32/RQ columns;
+    // the warps of the CTA split the columns. Each lane walks its (panel,
+    // column) pairs in rounds of BRG_U loads kept in registers; the first
+    // round is issued before the sources are gathered, and every later round
+    // is issued before the previous one is consumed.
     using V16 = typename Vec16<T>::type;
     constexpr int VN = Vec16<T>::n;
     constexpr int RB = 32 * VN;
-    const int sld = (nrows + 3) & ~3;
+    constexpr int U = BRG_U;
     const int nblk = (nrows + RB - 1) / RB;
     for (int bb = 0; bb < nblk; bb += BRG_WARPS) {
         const int nb_here = nblk - bb < BRG_WARPS ? nblk - bb : BRG_WARPS;
@@ -620,32 +543,106 @@ __device__ __forceinline__ void brg_compute(BrgShared<T> &sh, const int64_t *rec
         const int CS = 32 / RQ;
         const int rq = lane % RQ, cs = lane / RQ;
         const int r_lo = rb + rq * VN;
+        const int nv = nrows - r_lo < VN ? nrows - r_lo : VN;  // valid rows of the slice
+        const bool active = sl < S && r_lo < nrows;
+        // cursor over (panel, column)
+        int q = -1, c = 0, c1 = 0, xo = 0;
+        int64_t ld = 0;
+        const T *base = nullptr;
+        bool vec = true;
+        auto next_panel = [&]() {
+            while (true) {
+                ++q;
+                if (q >= np) return false;
+                const int64_t pa = pan[3 * q];
+                const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
+                const int c0 = (int)(((int64_t)w * sl) / S);
+                c1 = (int)(((int64_t)w * (sl + 1)) / S);
+                c = c0 + cs;
+                xo = (int)pan[3 * q + 2];
+                ld = lda;
+                base = A + pa + r_lo;
+                vec = ((pa & 3) == 0) && ((lda & 3) == 0);
+                if (c < c1) return true;
+            }
+        };
+        auto fill = [&](V16 *va, int *xa) {
+            int n = 0;
+            if (!active) return 0;
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (q >= np) break;
+                if (c >= c1 && !next_panel()) break;
+                const T *pcol = base + (int64_t)c * ld;
+                va[u] = vec ? *reinterpret_cast<const V16 *>(pcol) : load_rows<T>(pcol, nv);
+                xa[u] = xo + c;
+                c += CS;
+                ++n;
+            }
+            return n;
+        };
+        V16 va[U];
+        int xa[U];
+        if (active) next_panel();
+        int na = fill(va, xa);
+        if (bb == 0) {
+            // gather the sources while the first round of loads is in flight
+            int sidx = 0;
+            int64_t s_src = 0;
+            int s_lo = 0, s_hi = -1, s_g = 0;
+            int total = 0;
+            if (ns > 0) {
+                const int64_t wl = seg[2 * (ns - 1) + 1];
+                total = (int)(wl >> 33) + (int)(wl & 0xffffffff);
+            }
+            for (int e0 = tid; e0 < total; e0 += 4 * BRG_THREADS) {
+                int64_t idx4[4];
+                int g4[4], cnt = 0;
+                for (int u = 0; u < 4; ++u) {
+                    const int e = e0 + u * BRG_THREADS;
+                    if (e >= total) break;
+                    while (e >= s_hi && sidx < ns) {
+                        const int64_t w1 = seg[2 * sidx + 1];
+                        s_src = seg[2 * sidx];
+                        const int code = (int)(w1 >> 32);
+                        s_lo = code >> 1;
+                        s_hi = s_lo + (int)(w1 & 0xffffffff);
+                        s_g = code & 1;
+                        ++sidx;
+                    }
+                    idx4[u] = e < s_lo ? -1 : s_src + (e - s_lo);
+                    g4[u] = s_g;
+                    ++cnt;
+                }
+                T v4[4];
+                for (int u = 0; u < cnt; ++u) {
+                    const int64_t ix = idx4[u];
+                    if (ix < 0) v4[u] = T(0);
+                    else if (g4[u]) v4[u] = (T)xin[perm ? (int64_t)perm[ix] : ix];
+                    else v4[u] = ws[ix];
+                }
+                for (int u = 0; u < cnt; ++u) xs[e0 + u * BRG_THREADS] = v4[u];
+            }
+            __syncthreads();
+        }
         T acc[VN];
 #pragma unroll
         for (int v = 0; v < VN; ++v) acc[v] = T(0);
-        if (sl < S && r_lo < nrows) {
-            int so = 0;
-            for (int q = 0; q < np; ++q) {
-                const int w = (int)(pan[3 * q + 1] >> 32);
-                const int xoff = (int)pan[3 * q + 2];
-                const int c0 = (int)(((int64_t)w * sl) / S), c1 = (int)(((int64_t)w * (sl + 1)) / S);
-                const T *xp = xs + xoff;
-                const T *base = buf + so + r_lo;
-                int c = c0 + cs;
-                for (; c + 3 * CS < c1; c += 4 * CS) {
-                    const V16 v0 = *reinterpret_cast<const V16 *>(base + c * sld);
-                    const V16 v1 = *reinterpret_cast<const V16 *>(base + (c + CS) * sld);
-                    const V16 v2 = *reinterpret_cast<const V16 *>(base + (c + 2 * CS) * sld);
-                    const V16 v3 = *reinterpret_cast<const V16 *>(base + (c + 3 * CS) * sld);
-                    vfma(acc, v0, xp[c]);
-                    vfma(acc, v1, xp[c + CS]);
-                    vfma(acc, v2, xp[c + 2 * CS]);
-                    vfma(acc, v3, xp[c + 3 * CS]);
-                }
-                for (; c < c1; c += CS) vfma(acc, *reinterpret_cast<const V16 *>(base + c * sld), xp[c]);
-                so += w * sld;
+        while (na > 0) {
+            V16 vb[U];
+            int xb[U];
+            const int nb = fill(vb, xb);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (u < na) vfma(acc, va[u], xs[xa[u]]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                va[u] = vb[u];
+                xa[u] = xb[u];
             }
+            na = nb;
         }
+        // reduce over the column phases of the warp
 #pragma unroll
         for (int v = 0; v < VN; ++v)
             for (int o = RQ; o < 32; o <<= 1) acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], o);
@@ -658,7 +655,7 @@ __device__ __forceinline__ void brg_compute(BrgShared<T> &sh, const int64_t *rec
             const int i = (bb + mb) * RB + r;
             if (i >= nrows) continue;
             T v = T(0);
-            for (int q = 0; q < S; ++q) v += red[(mb + q * nb_here) * RB + r];
+            for (int q2 = 0; q2 < S; ++q2) v += red[(mb + q2 * nb_here) * RB + r];
             const int64_t d = dst + i;
             if (flags & T_SCATTER) {
                 const T ov = (flags & T_ACCUM) ? ws[d] + v : v;
@@ -673,6 +670,15 @@ __device__ __forceinline__ void brg_compute(BrgShared<T> &sh, const int64_t *rec
         }
         __syncthreads();
     }
+}
+
+template <class T>
+__global__ void __launch_bounds__(BRG_THREADS, 2)
+    brg_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
+               const T *__restrict__ A, T *ws, const double *__restrict__ xin, double *yout,
+               const int32_t *__restrict__ perm) {
+    __shared__ BrgShared<T> sh;
+    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) brg_target<T>(sh, t, roff, blob, A, ws, xin, yout, perm);
 }
 
 // Grid-wide barrier for the cooperative matvec (all CTAs are co-resident by
@@ -705,80 +711,30 @@ __device__ void grid_barrier(unsigned *bar, unsigned nblocks, int32_t *err) {
     __syncthreads();
 }
 
-// Persistent matvec CTA: runs phases [p0, p1) of the target list; between
-// phases a grid barrier (cooperative launch, p1 - p0 > 1) or nothing (one
-// launch per phase). The CTA's targets of a phase are pstart[p] + blockIdx.x
-// + k*gridDim.x. Records are fetched two targets ahead and matrix blocks one
-// target ahead, across phase barriers, so after a barrier only the source
-// gather and the shared-memory product remain on the critical path.
+// The whole matvec in one cooperative launch: phases separated by grid
+// barriers; targets of a phase striped over the CTAs.
 template <class T>
-__global__ void __launch_bounds__(BRG_THREADS, 1)
-    brg_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
-               const int64_t *__restrict__ pstart, int p0, int p1, const T *__restrict__ A, T *ws,
-               const double *__restrict__ xin, double *yout, const int32_t *__restrict__ perm, unsigned *bar,
-               int32_t *err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    BrgShared<T> &sh = *reinterpret_cast<BrgShared<T> *>(smem_raw);
-    const int64_t G = gridDim.x, b = blockIdx.x;
-    // k-th target of this CTA over phases [p0, p1), or -1
-    auto target_of = [&](int64_t k, int &ph) -> int64_t {
-        for (int p = p0; p < p1; ++p) {
-            const int64_t n = pstart[p + 1] - pstart[p];
-            const int64_t mine = n > b ? (n - b + G - 1) / G : 0;
-            if (k < mine) {
-                ph = p;
-                return pstart[p] + b + k * G;
-            }
-            k -= mine;
-        }
-        ph = p1;
-        return -1;
-    };
-    int ph_cur = p1, ph_nx = p1, ph_nx2 = p1;
-    int64_t t_cur = target_of(0, ph_cur);
-    const int64_t t_first2 = target_of(1, ph_nx);
-    if (t_cur >= 0) brg_fetch_record(sh.rec[0], t_cur, roff, blob);
-    cp_async_commit();
-    cp_async_wait_all();
-    __syncthreads();
-    if (t_cur >= 0) brg_fetch_matrix<T>(sh.buf[0], sh.rec[0], A);
-    if (t_first2 >= 0) brg_fetch_record(sh.rec[1], t_first2, roff, blob);
-    cp_async_commit();
-    int cur_phase = p0;
-    for (int64_t k = 0;; ++k) {
-        // one barrier per phase boundary crossed before this target
-        const int phase_of_t = t_cur >= 0 ? ph_cur : p1;
-        while (cur_phase < phase_of_t) {
-            if (cur_phase + 1 < p1) grid_barrier(bar, (unsigned)G, err);
-            ++cur_phase;
-        }
-        if (t_cur < 0) break;
-        cp_async_wait_all();  // matrix of this target, record of the next
-        __syncthreads();
-        const int64_t t_nx = target_of(k + 1, ph_nx);
-        const int64_t t_nx2 = target_of(k + 2, ph_nx2);
-        if (t_nx >= 0) brg_fetch_matrix<T>(sh.buf[(k + 1) & 1], sh.rec[(k + 1) % 3], A);
-        if (t_nx2 >= 0) brg_fetch_record(sh.rec[(k + 2) % 3], t_nx2, roff, blob);
-        cp_async_commit();
-        brg_compute<T>(sh, sh.rec[k % 3], sh.buf[k & 1], ws, xin, yout, perm);
-        t_cur = t_nx;
-        ph_cur = ph_nx;
+__global__ void __launch_bounds__(BRG_THREADS, 2)
+    brg_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
+                    const int64_t *__restrict__ pstart, int nphase, const T *__restrict__ A, T *ws,
+                    const double *__restrict__ xin, double *yout, const int32_t *__restrict__ perm, unsigned *bar,
+                    int32_t *err) {
+    __shared__ BrgShared<T> sh;
+    for (int p = 0; p < nphase; ++p) {
+        const int64_t t1 = pstart[p + 1];
+        for (int64_t t = pstart[p] + blockIdx.x; t < t1; t += gridDim.x)
+            brg_target<T>(sh, t, roff, blob, A, ws, xin, yout, perm);
+        if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
     }
-    cp_async_wait_all();
 }
 
 static int g_num_sms = 0;
 
 template <class T>
-static cudaError_t brg_prepare(int &grid_cap) {
+static cudaError_t launch_brg_t(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const T *A, T *ws,
+                                const double *xin, double *yout, const int32_t *perm, cudaStream_t st) {
+    if (t1 <= t0) return cudaSuccess;
     static int per_sm = 0;
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(brg_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sizeof(BrgShared<T>));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
     if (g_num_sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -786,43 +742,38 @@ static cudaError_t brg_prepare(int &grid_cap) {
         if (g_num_sms <= 0) g_num_sms = 1;
     }
     if (per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brg_kernel<T>, BRG_THREADS, sizeof(BrgShared<T>));
-        if (per_sm <= 0) return cudaErrorInvalidConfiguration;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brg_kernel<T>, BRG_THREADS, 0);
+        if (per_sm <= 0) per_sm = 1;
     }
-    grid_cap = g_num_sms * per_sm;
-    return cudaSuccess;
-}
-
-// One launch per phase [p, p+1), grid sized to the phase's targets.
-template <class T>
-static cudaError_t launch_phase_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int p,
-                                  int64_t ntargets, const T *A, T *ws, const double *xin, double *yout,
-                                  const int32_t *perm, unsigned *bar, int32_t *err, cudaStream_t st) {
-    if (ntargets <= 0) return cudaSuccess;
-    int cap = 0;
-    cudaError_t e = brg_prepare<T>(cap);
-    if (e != cudaSuccess) return e;
-    const int grid = (int)(ntargets < cap ? ntargets : cap);
-    brg_kernel<T><<<grid, BRG_THREADS, sizeof(BrgShared<T>), st>>>(roff, blob, pstart, p, p + 1, A, ws, xin, yout,
-                                                                    perm, bar, err);
+    const int64_t nt = t1 - t0;
+    const int64_t cap = (int64_t)g_num_sms * per_sm;
+    const int grid = (int)(nt < cap ? nt : cap);
+    brg_kernel<T><<<grid, BRG_THREADS, 0, st>>>(roff, blob, t0, t1, A, ws, xin, yout, perm);
     count_launch();
     return cudaGetLastError();
 }
 
-// All phases in one cooperative launch.
 template <class T>
 static cudaError_t launch_coop_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                                  const T *A, T *ws, const double *xin, double *yout, const int32_t *perm,
                                  unsigned *bar, int32_t *err, cudaStream_t st) {
     if (nphase <= 0) return cudaSuccess;
-    int cap = 0;
-    cudaError_t e = brg_prepare<T>(cap);
-    if (e != cudaSuccess) return e;
-    int p0 = 0, p1 = nphase;
-    void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&p0, (void *)&p1, (void *)&A,
-                    (void *)&ws, (void *)&xin, (void *)&yout, (void *)&perm, (void *)&bar, (void *)&err};
-    e = cudaLaunchCooperativeKernel((const void *)brg_kernel<T>, dim3(cap), dim3(BRG_THREADS), args,
-                                    sizeof(BrgShared<T>), st);
+    static int per_sm = 0;
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brg_coop_kernel<T>, BRG_THREADS, 0);
+        if (per_sm <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    }
+    const int grid = g_num_sms * per_sm;
+    void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&A, (void *)&ws,
+                    (void *)&xin, (void *)&yout, (void *)&perm, (void *)&bar, (void *)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)brg_coop_kernel<T>, dim3(grid), dim3(BRG_THREADS), args,
+                                                0, st);
     count_launch();
     return e;
 }
@@ -837,15 +788,14 @@ cudaError_t launch_coop_f32(const int64_t *roff, const int64_t *blob, const int6
                             unsigned *bar, int32_t *err, cudaStream_t st) {
     return launch_coop_t<float>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, st);
 }
-cudaError_t launch_phase_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int p,
-                             int64_t ntargets, const double *A, double *ws, const double *xin, double *yout,
-                             const int32_t *perm, unsigned *bar, int32_t *err, cudaStream_t st) {
-    return launch_phase_t<double>(roff, blob, pstart, p, ntargets, A, ws, xin, yout, perm, bar, err, st);
+
+cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const double *A,
+                           double *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st) {
+    return launch_brg_t<double>(roff, blob, t0, t1, A, ws, xin, yout, perm, st);
 }
-cudaError_t launch_phase_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int p,
-                             int64_t ntargets, const float *A, float *ws, const double *xin, double *yout,
-                             const int32_t *perm, unsigned *bar, int32_t *err, cudaStream_t st) {
-    return launch_phase_t<float>(roff, blob, pstart, p, ntargets, A, ws, xin, yout, perm, bar, err, st);
+cudaError_t launch_brg_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const float *A,
+                           float *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st) {
+    return launch_brg_t<float>(roff, blob, t0, t1, A, ws, xin, yout, perm, st);
 }
 
 template <class T>

@@ -42,15 +42,13 @@ cudaError_t launch_fill(const FillJob *jobs, int njobs, const int32_t *idx, cons
                         cudaStream_t st);
 cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStream_t st);
 
-// Matvec over the packed target records (roff: record offsets, blob:
-// records). xin / yout are FP64, in original point order when perm != NULL,
-// in leaf order when perm == NULL. One launch per phase p (ntargets targets):
-cudaError_t launch_phase_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int p,
-                             int64_t ntargets, const double *A, double *ws, const double *xin, double *yout,
-                             const int32_t *perm, unsigned *bar, int32_t *err, cudaStream_t st);
-cudaError_t launch_phase_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int p,
-                             int64_t ntargets, const float *A, float *ws, const double *xin, double *yout,
-                             const int32_t *perm, unsigned *bar, int32_t *err, cudaStream_t st);
+// Matvec: one block-row GEMV launch over targets [t0, t1) of the packed
+// target records (roff: record offsets, blob: records). xin / yout are FP64
+// in original point order when perm != NULL, in leaf order when perm == NULL.
+cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const double *A,
+                           double *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
+cudaError_t launch_brg_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const float *A,
+                           float *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
 // The whole matvec as one cooperative launch: phase p covers targets
 // [pstart[p], pstart[p+1]); bar (2 unsigned, zero) is the grid barrier state.
 cudaError_t launch_coop_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
@@ -62,8 +60,7 @@ cudaError_t launch_coop_f32(const int64_t *roff, const int64_t *blob, const int6
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_gather_f64(const double *x, double *xp, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
-constexpr int BRG_XS_ELEMS = 2048;    // gathered source width per target (elements)
-constexpr int BRG_BUF_ELEMS = 8192;   // staged matrix block of one target (elements)
+constexpr int BRG_XS_ELEMS = 4096;    // gathered source width per target (elements)
 constexpr int BRG_MAX_PANELS = 32;    // panels per target
 constexpr int BRG_REC_WORDS = 1024;   // packed record of one target (int64 words)
 
