@@ -466,7 +466,6 @@ cudaError_t launch_convert_f32(const double *src, float *dst, int64_t n, cudaStr
 // column slices meet in shared memory.
 constexpr int BRG_THREADS = 256;
 constexpr int BRG_WARPS = BRG_THREADS / 32;
-constexpr int BRG_U = 4;  // vector loads per lane per round
 
 // Target record (int64 words), built by the host plan:
 //   [0] dst   [1] nrows | flags << 32   [2] np | ns << 32
@@ -484,15 +483,6 @@ __device__ __forceinline__ void vfma(float *acc, const float4 v, const float x) 
     acc[1] += v.y * x;
     acc[2] += v.z * x;
     acc[3] += v.w * x;
-}
-
-// VN rows of an unaligned column, zero past nv.
-template <class T> __device__ __forceinline__ typename Vec16<T>::type load_rows(const T *p, int nv);
-template <> __device__ __forceinline__ double2 load_rows<double>(const double *p, int nv) {
-    return make_double2(p[0], nv > 1 ? p[1] : 0.0);
-}
-template <> __device__ __forceinline__ float4 load_rows<float>(const float *p, int nv) {
-    return make_float4(p[0], nv > 1 ? p[1] : 0.f, nv > 2 ? p[2] : 0.f, nv > 3 ? p[3] : 0.f);
 }
 
 template <class T> struct BrgShared {
@@ -520,127 +510,113 @@ __device__ __forceinline__ void brg_target(BrgShared<T> &sh, int64_t t, const in
     const int np = (int)(rec[2] & 0xffffffff), ns = (int)(rec[2] >> 32);
     const int64_t *pan = rec + 3;
     const int64_t *seg = pan + 3 * np;
+    // gather: every thread walks the segments for its elements
+    {
+        int sidx = 0;
+        int64_t s_src = 0;
+        int s_lo = 0, s_hi = -1, s_g = 0;
+        auto seek = [&](int e) {
+            while (e >= s_hi && sidx < ns) {
+                const int64_t w1 = seg[2 * sidx + 1];
+                s_src = seg[2 * sidx];
+                const int len = (int)(w1 & 0xffffffff);
+                const int code = (int)(w1 >> 32);
+                s_lo = code >> 1;
+                s_hi = s_lo + len;
+                s_g = code & 1;
+                ++sidx;
+            }
+        };
+        // elements of the concatenated sources, in segment order
+        int total = 0;
+        if (ns > 0) {
+            const int64_t wl = seg[2 * (ns - 1) + 1];
+            total = (int)(wl >> 33) + (int)(wl & 0xffffffff);
+        }
+        for (int e0 = tid; e0 < total; e0 += 4 * BRG_THREADS) {
+            int64_t idx4[4];
+            int xo4[4], g4[4];
+            int cnt = 0;
+            for (int u = 0; u < 4; ++u) {
+                const int e = e0 + u * BRG_THREADS;
+                if (e >= total) break;
+                seek(e);
+                if (e < s_lo) {  // padding gap between panels
+                    idx4[u] = -1;
+                } else {
+                    idx4[u] = s_src + (e - s_lo);
+                }
+                xo4[u] = e;
+                g4[u] = s_g;
+                ++cnt;
+            }
+            T v4[4];
+            for (int u = 0; u < cnt; ++u) {
+                const int64_t ix = idx4[u];
+                if (ix < 0) v4[u] = T(0);
+                else if (g4[u]) v4[u] = (T)xin[perm ? (int64_t)perm[ix] : ix];
+                else v4[u] = ws[ix];
+            }
+            for (int u = 0; u < cnt; ++u) xs[xo4[u]] = v4[u];
+        }
+    }
+    __syncthreads();
     // Rows in blocks of RB = 32*VN. Within a block, a warp's lane l owns the
     // VN-row slice rq = l % RQ (16-byte vector loads down a column) and
-    // column phase cs = l / RQ, so one load instruction covers 32/RQ columns;
-    // the warps of the CTA split the columns. Each lane walks its (panel,
-    // column) pairs in rounds of BRG_U loads kept in registers; the first
-    // round is issued before the sources are gathered, and every later round
-    // is issued before the previous one is consumed.
+    // column phase cs = l / RQ, so one load instruction covers 32/RQ columns.
+    // The warps of the CTA split the columns of each block.
     using V16 = typename Vec16<T>::type;
     constexpr int VN = Vec16<T>::n;
     constexpr int RB = 32 * VN;
-    constexpr int U = BRG_U;
     const int nblk = (nrows + RB - 1) / RB;
     for (int bb = 0; bb < nblk; bb += BRG_WARPS) {
         const int nb_here = nblk - bb < BRG_WARPS ? nblk - bb : BRG_WARPS;
-        const int S = BRG_WARPS / nb_here;
+        const int S = BRG_WARPS / nb_here;        // warps (column slices) per row block
         const int myb = warp % nb_here, sl = warp / nb_here;
         const int rb = (bb + myb) * RB;
         const int rows = nrows - rb < RB ? nrows - rb : RB;
         int RQ = 1;
-        while (RQ * VN < rows) RQ <<= 1;
-        const int CS = 32 / RQ;
+        while (RQ * VN < rows) RQ <<= 1;          // row slices of this block (power of two <= 32)
+        const int CS = 32 / RQ;                   // column phases per load
         const int rq = lane % RQ, cs = lane / RQ;
-        const int r_lo = rb + rq * VN;
-        const int nv = nrows - r_lo < VN ? nrows - r_lo : VN;  // valid rows of the slice
-        const bool active = sl < S && r_lo < nrows;
-        // cursor over (panel, column)
-        int q = -1, c = 0, c1 = 0, xo = 0;
-        int64_t ld = 0;
-        const T *base = nullptr;
-        bool vec = true;
-        auto next_panel = [&]() {
-            while (true) {
-                ++q;
-                if (q >= np) return false;
-                const int64_t pa = pan[3 * q];
-                const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
-                const int c0 = (int)(((int64_t)w * sl) / S);
-                c1 = (int)(((int64_t)w * (sl + 1)) / S);
-                c = c0 + cs;
-                xo = (int)pan[3 * q + 2];
-                ld = lda;
-                base = A + pa + r_lo;
-                vec = ((pa & 3) == 0) && ((lda & 3) == 0);
-                if (c < c1) return true;
-            }
-        };
-        auto fill = [&](V16 *va, int *xa) {
-            int n = 0;
-            if (!active) return 0;
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                if (q >= np) break;
-                if (c >= c1 && !next_panel()) break;
-                const T *pcol = base + (int64_t)c * ld;
-                va[u] = vec ? *reinterpret_cast<const V16 *>(pcol) : load_rows<T>(pcol, nv);
-                xa[u] = xo + c;
-                c += CS;
-                ++n;
-            }
-            return n;
-        };
-        V16 va[U];
-        int xa[U];
-        if (active) next_panel();
-        int na = fill(va, xa);
-        if (bb == 0) {
-            // gather the sources while the first round of loads is in flight
-            int sidx = 0;
-            int64_t s_src = 0;
-            int s_lo = 0, s_hi = -1, s_g = 0;
-            int total = 0;
-            if (ns > 0) {
-                const int64_t wl = seg[2 * (ns - 1) + 1];
-                total = (int)(wl >> 33) + (int)(wl & 0xffffffff);
-            }
-            for (int e0 = tid; e0 < total; e0 += 4 * BRG_THREADS) {
-                int64_t idx4[4];
-                int g4[4], cnt = 0;
-                for (int u = 0; u < 4; ++u) {
-                    const int e = e0 + u * BRG_THREADS;
-                    if (e >= total) break;
-                    while (e >= s_hi && sidx < ns) {
-                        const int64_t w1 = seg[2 * sidx + 1];
-                        s_src = seg[2 * sidx];
-                        const int code = (int)(w1 >> 32);
-                        s_lo = code >> 1;
-                        s_hi = s_lo + (int)(w1 & 0xffffffff);
-                        s_g = code & 1;
-                        ++sidx;
-                    }
-                    idx4[u] = e < s_lo ? -1 : s_src + (e - s_lo);
-                    g4[u] = s_g;
-                    ++cnt;
-                }
-                T v4[4];
-                for (int u = 0; u < cnt; ++u) {
-                    const int64_t ix = idx4[u];
-                    if (ix < 0) v4[u] = T(0);
-                    else if (g4[u]) v4[u] = (T)xin[perm ? (int64_t)perm[ix] : ix];
-                    else v4[u] = ws[ix];
-                }
-                for (int u = 0; u < cnt; ++u) xs[e0 + u * BRG_THREADS] = v4[u];
-            }
-            __syncthreads();
-        }
+        const int r_lo = rb + rq * VN;            // first row of the lane's slice
         T acc[VN];
 #pragma unroll
         for (int v = 0; v < VN; ++v) acc[v] = T(0);
-        while (na > 0) {
-            V16 vb[U];
-            int xb[U];
-            const int nb = fill(vb, xb);
+        if (sl < S && r_lo < nrows) {
+            for (int q = 0; q < np; ++q) {
+                const int64_t pa = pan[3 * q];
+                const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
+                const int xoff = (int)pan[3 * q + 2];
+                const int c0 = (int)(((int64_t)w * sl) / S), c1 = (int)(((int64_t)w * (sl + 1)) / S);
+                const T *xp = xs + xoff;
+                const int64_t ld = lda;
+                const T *base = A + pa + r_lo;
+                if (((pa & 3) == 0) && ((lda & 3) == 0)) {
+                    int c = c0 + cs;
+                    for (; c + 3 * CS < c1; c += 4 * CS) {
+                        const V16 v0 = *reinterpret_cast<const V16 *>(base + (int64_t)c * ld);
+                        const V16 v1 = *reinterpret_cast<const V16 *>(base + (int64_t)(c + CS) * ld);
+                        const V16 v2 = *reinterpret_cast<const V16 *>(base + (int64_t)(c + 2 * CS) * ld);
+                        const V16 v3 = *reinterpret_cast<const V16 *>(base + (int64_t)(c + 3 * CS) * ld);
+                        const T x0 = xp[c], x1 = xp[c + CS], x2 = xp[c + 2 * CS], x3 = xp[c + 3 * CS];
+                        vfma(acc, v0, x0);
+                        vfma(acc, v1, x1);
+                        vfma(acc, v2, x2);
+                        vfma(acc, v3, x3);
+                    }
+                    for (; c < c1; c += CS) vfma(acc, *reinterpret_cast<const V16 *>(base + (int64_t)c * ld), xp[c]);
+                } else {
+                    const int nv = nrows - r_lo < VN ? nrows - r_lo : VN;
+                    for (int c = c0 + cs; c < c1; c += CS) {
+                        const T xc = xp[c];
+                        const T *col = base + (int64_t)c * ld;
 #pragma unroll
-            for (int u = 0; u < U; ++u)
-                if (u < na) vfma(acc, va[u], xs[xa[u]]);
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                va[u] = vb[u];
-                xa[u] = xb[u];
+                        for (int v = 0; v < VN; ++v)
+                            if (v < nv) acc[v] += col[v] * xc;
+                    }
+                }
             }
-            na = nb;
         }
         // reduce over the column phases of the warp
 #pragma unroll
@@ -650,12 +626,13 @@ __device__ __forceinline__ void brg_target(BrgShared<T> &sh, int64_t t, const in
 #pragma unroll
             for (int v = 0; v < VN; ++v) red[warp * RB + rq * VN + v] = acc[v];
         __syncthreads();
+        // combine the column slices of each block and write
         for (int e = tid; e < nb_here * RB; e += BRG_THREADS) {
             const int mb = e / RB, r = e % RB;
             const int i = (bb + mb) * RB + r;
             if (i >= nrows) continue;
             T v = T(0);
-            for (int q2 = 0; q2 < S; ++q2) v += red[(mb + q2 * nb_here) * RB + r];
+            for (int q = 0; q < S; ++q) v += red[(mb + q * nb_here) * RB + r];
             const int64_t d = dst + i;
             if (flags & T_SCATTER) {
                 const T ov = (flags & T_ACCUM) ? ws[d] + v : v;
@@ -673,7 +650,7 @@ __device__ __forceinline__ void brg_target(BrgShared<T> &sh, int64_t t, const in
 }
 
 template <class T>
-__global__ void __launch_bounds__(BRG_THREADS, 2)
+__global__ void __launch_bounds__(BRG_THREADS, 4)
     brg_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
                const T *__restrict__ A, T *ws, const double *__restrict__ xin, double *yout,
                const int32_t *__restrict__ perm) {
@@ -714,7 +691,7 @@ __device__ void grid_barrier(unsigned *bar, unsigned nblocks, int32_t *err) {
 // The whole matvec in one cooperative launch: phases separated by grid
 // barriers; targets of a phase striped over the CTAs.
 template <class T>
-__global__ void __launch_bounds__(BRG_THREADS, 2)
+__global__ void __launch_bounds__(BRG_THREADS, 4)
     brg_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
                     const int64_t *__restrict__ pstart, int nphase, const T *__restrict__ A, T *ws,
                     const double *__restrict__ xin, double *yout, const int32_t *__restrict__ perm, unsigned *bar,
