@@ -83,6 +83,8 @@ def lib():
         "h2w_matvec": [P, P, P, I, I, I, P],
         "h2w_gmres": [P, P, P, I, I, I, ctypes.POINTER(I), ctypes.POINTER(D)],
         "h2w_gmres_ir": [P, P, P, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)],
+        "h2w_gmres_batch": [P, P, P, I, I, I, I, P, P],
+        "h2w_gmres_ir_batch": [P, P, P, I, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), P],
         "h2w_dense_matvec": [P, P, P, I64, I64, I],
         "h2w_profile": [P, I],
         "h2w_profile_phases": [P, I, I, P, P, P, ctypes.POINTER(I)],
@@ -272,6 +274,53 @@ class H2Operator:
                                 ctypes.byref(ii), ctypes.byref(res))
         self._ck(rc, allow=(ERR_NOT_CONVERGED,))
         return x, oi.value, ii.value, res.value
+
+
+    # many right-hand sides (columns of an N x nrhs array)
+    def _cols(self, a):
+        a = np.asarray(a, dtype=np.float64)
+        return np.asfortranarray(a.reshape(self.N, -1))
+
+    def gmres_batch(self, B, X0=None, max_iter=200, tol_pow=10):
+        """Per-column GMRES on all columns of B at once (one multi-vector
+        product per Arnoldi step). Returns X, iterations and residuals per column."""
+        B = self._cols(B)
+        X = np.asfortranarray(np.ones_like(B)) if X0 is None else self._cols(np.array(X0, dtype=np.float64))
+        k = B.shape[1]
+        it = np.zeros(k, dtype=np.int32)
+        res = np.zeros(k)
+        rc = lib().h2w_gmres_batch(self.h, _ptr(B), _ptr(X), k, max_iter, tol_pow, HOST, _ptr(it), _ptr(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return X, it, res
+
+    def gmres_batch_device(self, b_ptr, x_ptr, nrhs, max_iter=200, tol_pow=10):
+        it = np.zeros(nrhs, dtype=np.int32)
+        res = np.zeros(nrhs)
+        rc = lib().h2w_gmres_batch(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), nrhs, max_iter, tol_pow,
+                                   DEVICE, _ptr(it), _ptr(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return it, res
+
+    def gmres_ir_batch(self, B, X0=None, max_outer=20, inner_iter=100, tol_pow=10):
+        """FP32-operator batched inner GMRES inside FP64 iterative refinement,
+        all columns of B at once. Returns X, outer steps, inner steps, residuals."""
+        B = self._cols(B)
+        X = np.asfortranarray(np.ones_like(B)) if X0 is None else self._cols(np.array(X0, dtype=np.float64))
+        k = B.shape[1]
+        oi, ii = ctypes.c_int(), ctypes.c_int()
+        res = np.zeros(k)
+        rc = lib().h2w_gmres_ir_batch(self.h, _ptr(B), _ptr(X), k, max_outer, inner_iter, tol_pow, HOST,
+                                      ctypes.byref(oi), ctypes.byref(ii), _ptr(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return X, oi.value, ii.value, res
+
+    def gmres_ir_batch_device(self, b_ptr, x_ptr, nrhs, max_outer=20, inner_iter=100, tol_pow=10, where=DEVICE):
+        oi, ii = ctypes.c_int(), ctypes.c_int()
+        res = np.zeros(nrhs)
+        rc = lib().h2w_gmres_ir_batch(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), nrhs, max_outer,
+                                      inner_iter, tol_pow, where, ctypes.byref(oi), ctypes.byref(ii), _ptr(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return oi.value, ii.value, res
 
 
 class _TreeView:

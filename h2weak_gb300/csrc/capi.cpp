@@ -1,6 +1,7 @@
 // C ABI of the GB300 H2* / (H2+H)* library: handle, tree, GPU assembly,
 // packed-operator plan, matvec launches and device-resident GMRES.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -65,6 +66,7 @@ inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
 
 constexpr int XW_CAP = 4096;          // gathered source width per target (elements)
 constexpr int64_t ROW_SPLIT = 16384;  // rows * width above which a target is split (load balance)
+constexpr int64_t MR_ROWS = 64;      // rows per target of the multi-vector stream (its result tile)
 
 }  // namespace
 
@@ -88,6 +90,8 @@ struct h2w_handle {
     DBuf<double> d_op;
     DBuf<float> d_op32;
     DBuf<int64_t> d_roff, d_blob;  // packed target records of the matvec
+    DBuf<int64_t> d_roff_m, d_blob_m, d_pstart_m;  // the multi-vector stream (64-row targets)
+    std::vector<Phase> mphases;
     DBuf<double> d_ws, d_x, d_y;
     DBuf<int32_t> d_ctr, d_err;
     DBuf<int64_t> d_pstart;
@@ -109,6 +113,13 @@ struct h2w_handle {
     DBuf<double> g_V, g_w, g_vcur, g_H, g_cs, g_sn, g_s, g_part, g_scal, g_tmp, g_b, g_r, g_npart;
     DBuf<int32_t> g_iter;
     int g_m = -1;
+    // multiple right-hand sides: interleaved workspaces (ws_n x rp), staging, batched GMRES
+    DBuf<double> m_wsd, m_xi, m_yi, m_ri, m_di, m_bi, m_stage_x, m_stage_y, m_onorm, m_ores;
+    DBuf<float> m_wsf, m_xf;
+    std::vector<int64_t> ph_t0, ph_t1;   // phase target ranges (per-phase launches)
+    DBuf<double> gb_V, gb_w, gb_vcur, gb_H, gb_cs, gb_sn, gb_s, gb_part, gb_hsum, gb_normb, gb_resid, gb_y;
+    DBuf<int32_t> gb_conv, gb_iter;
+    int gb_m = -1, gb_rp = 0;
     cudaStream_t stream = nullptr;
 
     KParams kparams() const {
@@ -525,6 +536,10 @@ struct PlanBuilder {
     // phase window of the targets being emitted, and per target
     int lo = 0, hi = 0;
     std::vector<std::pair<int, int>> win;
+    // split parameters of the stream being realised: targets are cut into
+    // row chunks of max(min_rows, row_split / width) rows (multiples of 4)
+    int64_t row_split = ROW_SPLIT;
+    int64_t min_rows = 4;
 
     // column-major block: element (i, c) at a + c*lda + i, lda = pad4(rows)
     int64_t alloc(int64_t rows, int64_t cols, int32_t &lda) {
@@ -545,16 +560,45 @@ struct PlanBuilder {
         int32_t lda, w;
         std::vector<Seg> segs;  // xoff relative to panel
     };
-    // Emit a target (row- and column-split as needed).
+    // A block-row product before any splitting; the same logical targets are
+    // realised once per target stream (single-vector and multi-vector).
+    struct LTarget {
+        int64_t dst;
+        int32_t nrows, flags;
+        std::vector<PanelSpec> panels;
+        int lo, hi;
+    };
+    std::vector<LTarget> logical;
     void emit(int64_t dst, int32_t nrows, int32_t flags, const std::vector<PanelSpec> &panels) {
+        if (nrows <= 0) return;
+        for (auto &p : panels) read_elems += (int64_t)nrows * p.w;
+        logical.push_back({dst, nrows, flags, panels, lo, hi});
+    }
+    // Realise the logical targets with the given split parameters into T/P/S/win.
+    void realize(int64_t rs, int64_t mr) {
+        T.clear();
+        P.clear();
+        S.clear();
+        win.clear();
+        row_split = rs;
+        min_rows = mr;
+        for (const LTarget &l : logical) {
+            lo = l.lo;
+            hi = l.hi;
+            split(l.dst, l.nrows, l.flags, l.panels);
+        }
+    }
+    // Cut a target into row chunks and, past XW_CAP gathered columns, into
+    // atomically accumulated column chunks.
+    void split(int64_t dst, int32_t nrows, int32_t flags, const std::vector<PanelSpec> &panels) {
         if (nrows <= 0) return;
         int64_t xw = 0;
         for (auto &p : panels) xw += pad4(p.w);
-        for (auto &p : panels) read_elems += (int64_t)nrows * p.w;
         if (xw == 0) return;
         if (xw <= XW_CAP) {
             // row chunks are multiples of 4 rows so the kernel's 16-byte column loads stay aligned
-            int64_t rows_per = std::max<int64_t>(4, (ROW_SPLIT / std::max<int64_t>(xw, 1)) & ~int64_t(3));
+            int64_t rows_per =
+                std::max<int64_t>(min_rows, (row_split / std::max<int64_t>(xw, 1)) & ~int64_t(3));
             rows_per = std::min<int64_t>(rows_per, nrows);
             for (int64_t r0 = 0; r0 < nrows; r0 += rows_per) {
                 int32_t nr = (int32_t)std::min<int64_t>(rows_per, nrows - r0);
@@ -605,10 +649,7 @@ struct PlanBuilder {
                     ns.xoff = (int32_t)(lo - c0);
                     q.segs.push_back(ns);
                 }
-                // the sub-panel's row starts are no longer 4-aligned unless c0 is
-                int64_t rd = read_elems;
-                emit(dst, nrows, T_ATOMIC, {q});
-                read_elems = rd;
+                split(dst, nrows, T_ATOMIC, {q});
             }
         }
     }
@@ -617,10 +658,10 @@ struct PlanBuilder {
 // Host-side bounds and alignment check of every work item before any of it
 // reaches the GPU: an inconsistent plan becomes an error status, never an
 // out-of-bounds access.
-void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
+void validate_plan(const PlanBuilder &pb, const h2w_handle *h, const std::vector<Phase> &phases) {
     auto bad = [](const char *what) { throw ApiError(H2W_ERR_STATE, std::string("internal plan check failed: ") + what); };
     const int64_t N = h->tree.N, wsn = h->ws_n, opn = pb.opn, nidx = (int64_t)pb.idx.size();
-    for (const Phase &ph : h->phases)
+    for (const Phase &ph : phases)
         if (ph.t0 < 0 || ph.t1 < ph.t0 || ph.t1 > (int64_t)pb.T.size() || ph.max_xw > XW_CAP) bad("phase");
     for (const Target &t : pb.T) {
         if (t.nrows < 1 || t.dst < 0 || t.dst + t.nrows > wsn) bad("target rows");
@@ -666,6 +707,101 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h) {
             bad("fill job");
     for (int32_t v : pb.idx)
         if (v < 0 || v >= N) bad("point index");
+}
+
+// Phase assignment of the realised targets: fixed targets at their phase,
+// flexible ones (largest first) into the least-loaded phase of their window;
+// targets sorted by phase, heaviest first within a phase.
+void assign_phases(h2w_handle *h, PlanBuilder &pb, int NPH, std::vector<Phase> &phases) {
+    const size_t nt = pb.T.size();
+    std::vector<int> ph(nt, 0);
+    std::vector<double> load((size_t)NPH, 0.0);
+    std::vector<size_t> flex;
+    auto elems = [&](size_t q) { return (double)pb.T[q].nrows * (double)pb.T[q].xw; };
+    for (size_t q = 0; q < nt; ++q) {
+        if (pb.win[q].first == pb.win[q].second) {
+            ph[q] = pb.win[q].first;
+            load[(size_t)ph[q]] += elems(q);
+        } else {
+            flex.push_back(q);
+        }
+    }
+    std::stable_sort(flex.begin(), flex.end(), [&](size_t a, size_t b) { return elems(a) > elems(b); });
+    for (size_t q : flex) {
+        int best = pb.win[q].first;
+        for (int p2 = pb.win[q].first; p2 <= pb.win[q].second; ++p2)
+            if (load[(size_t)p2] < load[(size_t)best]) best = p2;
+        ph[q] = best;
+        load[(size_t)best] += elems(q);
+    }
+    std::vector<size_t> order(nt);
+    for (size_t q = 0; q < nt; ++q) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        if (ph[a] != ph[b]) return ph[a] < ph[b];
+        return elems(a) > elems(b);
+    });
+    std::vector<Target> T2(nt);
+    for (size_t q = 0; q < nt; ++q) T2[q] = pb.T[order[q]];
+    pb.T.swap(T2);
+    phases.clear();
+    size_t q = 0;
+    for (int p2 = 0; p2 < NPH; ++p2) {
+        size_t q0 = q;
+        while (q < nt && ph[order[q]] == p2) ++q;
+        if (q > q0) phases.push_back({(int64_t)q0, (int64_t)q, 0});
+    }
+    // leaves without any far contribution would never be scattered by the
+    // fused path; fall back to an explicit scatter then.
+    int64_t covered = 0;
+    const Phase &lp = phases.back();
+    for (int64_t r = lp.t0; r < lp.t1; ++r)
+        if (pb.T[(size_t)r].flags & T_SCATTER) covered += pb.T[(size_t)r].nrows;
+    if (covered != h->tree.N) h->fused_scatter = false;
+    if (!h->fused_scatter)
+        for (int64_t r = lp.t0; r < lp.t1; ++r)
+            if (pb.T[(size_t)r].flags & T_SCATTER) pb.T[(size_t)r].flags = T_ACCUM;
+    for (Phase &p2 : phases) {
+        int mx = 0;
+        for (int64_t r = p2.t0; r < p2.t1; ++r) mx = std::max(mx, pb.T[(size_t)r].xw);
+        p2.max_xw = mx;
+    }
+}
+
+// Packed records: header, panels, segments (layout documented at brg_kernel),
+// plus the phase starts.
+void pack_records(const PlanBuilder &pb, const std::vector<Phase> &phases, std::vector<int64_t> &roff,
+                  std::vector<int64_t> &blob, std::vector<int64_t> &pstart) {
+    roff.assign(1, 0);
+    blob.clear();
+    for (const Target &tg : pb.T) {
+        const size_t base = blob.size();
+        int ns = 0;
+        for (int32_t q = tg.p0; q < tg.p1; ++q) ns += pb.P[(size_t)q].s1 - pb.P[(size_t)q].s0;
+        blob.push_back(tg.dst);
+        blob.push_back((int64_t)(uint32_t)tg.nrows | ((int64_t)tg.flags << 32));
+        blob.push_back((int64_t)(uint32_t)(tg.p1 - tg.p0) | ((int64_t)ns << 32));
+        for (int32_t q = tg.p0; q < tg.p1; ++q) {
+            const Panel &pn = pb.P[(size_t)q];
+            blob.push_back(pn.a);
+            blob.push_back((int64_t)(uint32_t)pn.lda | ((int64_t)pn.w << 32));
+            blob.push_back(pn.xoff);
+        }
+        for (int32_t q = tg.p0; q < tg.p1; ++q) {
+            const Panel &pn = pb.P[(size_t)q];
+            for (int32_t e = pn.s0; e < pn.s1; ++e) {
+                const Seg &sg = pb.S[(size_t)e];
+                const int64_t code = ((int64_t)(pn.xoff + sg.xoff) << 1) | (sg.flags & S_GATHER ? 1 : 0);
+                blob.push_back(sg.src);
+                blob.push_back((int64_t)(uint32_t)sg.len | (code << 32));
+            }
+        }
+        if (blob.size() - base > (size_t)BRG_REC_WORDS)
+            throw ApiError(H2W_ERR_STATE, "internal: target record exceeds the shared-memory record size");
+        roff.push_back((int64_t)blob.size());
+    }
+    pstart.clear();
+    for (auto &ph : phases) pstart.push_back(ph.t0);
+    pstart.push_back(phases.empty() ? 0 : phases.back().t1);
 }
 
 void build_plan(h2w_handle *h) {
@@ -1039,67 +1175,17 @@ void build_plan(h2w_handle *h) {
             pb.emit(h->yperm_off + t.off[(size_t)L][(size_t)k], n, T_ACCUM | T_SCATTER, pans);
         }
     }
-    // ---- phase assignment: fixed targets at their phase, flexible targets
-    // (largest first) into the least-loaded phase of their window
-    {
-        const size_t nt = pb.T.size();
-        std::vector<int> ph(nt, 0);
-        std::vector<double> load((size_t)NPH, 0.0);
-        std::vector<size_t> flex;
-        auto elems = [&](size_t q) { return (double)pb.T[q].nrows * (double)pb.T[q].xw; };
-        for (size_t q = 0; q < nt; ++q) {
-            if (pb.win[q].first == pb.win[q].second) {
-                ph[q] = pb.win[q].first;
-                load[(size_t)ph[q]] += elems(q);
-            } else {
-                flex.push_back(q);
-            }
-        }
-        std::stable_sort(flex.begin(), flex.end(), [&](size_t a, size_t b) { return elems(a) > elems(b); });
-        for (size_t q : flex) {
-            int best = pb.win[q].first;
-            for (int p2 = pb.win[q].first; p2 <= pb.win[q].second; ++p2)
-                if (load[(size_t)p2] < load[(size_t)best]) best = p2;
-            ph[q] = best;
-            load[(size_t)best] += elems(q);
-        }
-        std::vector<size_t> order(nt);
-        for (size_t q = 0; q < nt; ++q) order[q] = q;
-        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
-            if (ph[a] != ph[b]) return ph[a] < ph[b];
-            return elems(a) > elems(b);
-        });
-        std::vector<Target> T2(nt);
-        for (size_t q = 0; q < nt; ++q) T2[q] = pb.T[order[q]];
-        pb.T.swap(T2);
-        h->phases.clear();
-        size_t q = 0;
-        for (int p2 = 0; p2 < NPH; ++p2) {
-            size_t q0 = q;
-            while (q < nt && ph[order[q]] == p2) ++q;
-            if (q > q0) h->phases.push_back({(int64_t)q0, (int64_t)q, 0});
-        }
-    }
-    // leaves without any far contribution would never be scattered by the
-    // fused path; fall back to an explicit scatter then.
-    {
-        int64_t covered = 0;
-        const Phase &lp = h->phases.back();
-        for (int64_t q = lp.t0; q < lp.t1; ++q)
-            if (pb.T[(size_t)q].flags & T_SCATTER) covered += pb.T[(size_t)q].nrows;
-        if (covered != t.N) h->fused_scatter = false;
-        if (!h->fused_scatter)
-            for (int64_t q = lp.t0; q < lp.t1; ++q)
-                if (pb.T[(size_t)q].flags & T_SCATTER) pb.T[(size_t)q].flags = T_ACCUM;
-    }
+    // ---- target streams. Single-vector: fine row chunks (load balance of a
+    // GEMV); multi-vector: 64-row chunks, one result tile per target.
+    std::vector<int64_t> roff, blob, pstart, roff_m, blob_m, pstart_m;
+    pb.realize(ROW_SPLIT, 4);
+    assign_phases(h, pb, NPH, h->phases);
     h->ph_op.assign(h->phases.size(), 0);
     h->ph_vec.assign(h->phases.size(), 0);
     for (size_t pi = 0; pi < h->phases.size(); ++pi) {
-        Phase &ph = h->phases[pi];
-        int mx = 0;
+        const Phase &ph = h->phases[pi];
         for (int64_t q = ph.t0; q < ph.t1; ++q) {
             const Target &tg = pb.T[(size_t)q];
-            mx = std::max(mx, tg.xw);
             h->ph_vec[pi] += (int64_t)tg.nrows * ((tg.flags & (T_ACCUM | T_ATOMIC)) ? 2 : 1);
             for (int32_t p = tg.p0; p < tg.p1; ++p) {
                 const Panel &pn = pb.P[(size_t)p];
@@ -1107,11 +1193,15 @@ void build_plan(h2w_handle *h) {
                 for (int32_t e = pn.s0; e < pn.s1; ++e) h->ph_vec[pi] += pb.S[(size_t)e].len;
             }
         }
-        ph.max_xw = mx;
     }
     for (auto &x : pb.xfers)
         if (x.f < 0) throw ApiError(H2W_ERR_STATE, "internal: unresolved factor");
-    validate_plan(pb, h);
+    validate_plan(pb, h, h->phases);
+    pack_records(pb, h->phases, roff, blob, pstart);
+    pb.realize(0, MR_ROWS);
+    assign_phases(h, pb, NPH, h->mphases);
+    validate_plan(pb, h, h->mphases);
+    pack_records(pb, h->mphases, roff_m, blob_m, pstart_m);
 
     // ---- device buffers and assembly kernels
     cudaStream_t st = h->stream;
@@ -1133,48 +1223,16 @@ void build_plan(h2w_handle *h) {
     CK(launch_factor(dfac.p, (int)pb.factors.size(), didx.p, kp, dF.p, st));
     CK(launch_xfer(dxf.p, (int)pb.xfers.size(), pb.max_xfer_n, didx.p, kp, dF.p, h->d_op.p, st));
     CK(launch_fill(dfill.p, (int)pb.fills.size(), didx.p, kp, h->d_op.p, st));
-    // packed records: header, panels, segments (layout documented at brg_kernel)
-    {
-        std::vector<int64_t> roff{0}, blob;
-        for (const Target &tg : pb.T) {
-            const size_t base = blob.size();
-            int ns = 0;
-            for (int32_t q = tg.p0; q < tg.p1; ++q) ns += pb.P[(size_t)q].s1 - pb.P[(size_t)q].s0;
-            blob.push_back(tg.dst);
-            blob.push_back((int64_t)(uint32_t)tg.nrows | ((int64_t)tg.flags << 32));
-            blob.push_back((int64_t)(uint32_t)(tg.p1 - tg.p0) | ((int64_t)ns << 32));
-            for (int32_t q = tg.p0; q < tg.p1; ++q) {
-                const Panel &pn = pb.P[(size_t)q];
-                blob.push_back(pn.a);
-                blob.push_back((int64_t)(uint32_t)pn.lda | ((int64_t)pn.w << 32));
-                blob.push_back(pn.xoff);
-            }
-            for (int32_t q = tg.p0; q < tg.p1; ++q) {
-                const Panel &pn = pb.P[(size_t)q];
-                for (int32_t e = pn.s0; e < pn.s1; ++e) {
-                    const Seg &sg = pb.S[(size_t)e];
-                    const int64_t code = ((int64_t)(pn.xoff + sg.xoff) << 1) | (sg.flags & S_GATHER ? 1 : 0);
-                    blob.push_back(sg.src);
-                    blob.push_back((int64_t)(uint32_t)sg.len | (code << 32));
-                }
-            }
-            if (blob.size() - base > (size_t)BRG_REC_WORDS)
-                throw ApiError(H2W_ERR_STATE, "internal: target record exceeds the shared-memory record size");
-            roff.push_back((int64_t)blob.size());
-        }
-        h->d_roff.upload(roff, st);
-        h->d_blob.upload(blob, st);
-    }
+    h->d_roff.upload(roff, st);
+    h->d_blob.upload(blob, st);
+    h->d_pstart.upload(pstart, st);
+    h->d_roff_m.upload(roff_m, st);
+    h->d_blob_m.upload(blob_m, st);
+    h->d_pstart_m.upload(pstart_m, st);
     h->d_ws.alloc((size_t)h->ws_n);
     h->d_ctr.alloc(h->phases.size() + 1);
     h->d_err.alloc(1);
     CK(cudaMemsetAsync(h->d_err.p, 0, 4, st));
-    {
-        std::vector<int64_t> ps;
-        for (auto &ph : h->phases) ps.push_back(ph.t0);
-        ps.push_back(h->phases.empty() ? 0 : h->phases.back().t1);
-        h->d_pstart.upload(ps, st);
-    }
     h->d_bar.alloc(2);
     CK(cudaMemsetAsync(h->d_bar.p, 0, 8, st));
     {
@@ -1347,6 +1405,140 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     }
 }
 
+// ----------------------------------------------- multiple right-hand sides ---
+// Interleaved block width for nrhs columns (the multi-vector kernel is
+// compiled for 16, 32 and 64).
+int rp_for(int nrhs) { return nrhs <= 16 ? 16 : (nrhs <= 32 ? 32 : 64); }
+constexpr int MR_MAX = 64;
+
+// Y = A X for an interleaved leaf-order block of rp vectors (xi, yi: N x rp).
+void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double *yi, cudaStream_t st) {
+    const int nph = (int)h->mphases.size();
+    const size_t wsz = (size_t)h->ws_n * (size_t)rp;
+    if (h->ws_n >= (int64_t)INT32_MAX - 2 || h->tree.N >= (int64_t)INT32_MAX - 2)
+        throw ApiError(H2W_ERR_ARG, "workspace too large for the multi-vector kernel's source map");
+    MrPhases ph{h->ph_t0.data(), h->ph_t1.data(), nph};
+    const MrPhases *phased = h->coop ? nullptr : &ph;
+    if (prec == H2W_PREC_FP32) {
+        ensure_f32(h);
+        if (h->m_wsf.n < wsz) h->m_wsf.alloc(wsz);
+        CK(cudaMemsetAsync(h->m_wsf.p, 0, wsz * 4, st));
+        const size_t nx = (size_t)h->tree.N * (size_t)rp;
+        if (h->m_xf.n < nx) h->m_xf.alloc(nx);
+        CK(vec_f64_to_f32(xi, h->m_xf.p, (int64_t)nx, st));
+        CK(launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op32.p, h->m_wsf.p, h->m_xf.p, yi,
+                         h->d_bar.p, h->d_err.p, st));
+        if (!h->fused_scatter) CK(launch_mr_widen_f32(h->m_wsf.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
+    } else {
+        if (h->m_wsd.n < wsz) h->m_wsd.alloc(wsz);
+        CK(cudaMemsetAsync(h->m_wsd.p, 0, wsz * 8, st));
+        CK(launch_mr_f64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op.p, h->m_wsd.p, xi, yi,
+                         h->d_bar.p, h->d_err.p, st));
+        if (!h->fused_scatter) CK(launch_mr_widen_f64(h->m_wsd.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
+    }
+}
+
+void ensure_multi_vectors(h2w_handle *h) {
+    const size_t n = (size_t)h->tree.N * MR_MAX;
+    if (h->m_xi.n < n) h->m_xi.alloc(n);
+    if (h->m_yi.n < n) h->m_yi.alloc(n);
+}
+
+GmresBatch gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
+    const int64_t N = h->tree.N;
+    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(2 * 152, (N + 255) / 256));
+    if (h->gb_m != m || h->gb_rp != rp) {
+        h->gb_V.alloc((size_t)N * rp * (size_t)(m + 1));
+        h->gb_w.alloc((size_t)N * rp);
+        h->gb_vcur.alloc((size_t)N * rp);
+        h->gb_H.alloc((size_t)rp * (size_t)(m + 1) * (size_t)m);
+        h->gb_cs.alloc((size_t)rp * (m + 1));
+        h->gb_sn.alloc((size_t)rp * (m + 1));
+        h->gb_s.alloc((size_t)rp * (m + 1));
+        h->gb_part.alloc((size_t)nblk * (m + 1) * rp);
+        h->gb_hsum.alloc((size_t)(m + 1) * rp);
+        h->gb_normb.alloc((size_t)rp);
+        h->gb_resid.alloc((size_t)rp);
+        h->gb_y.alloc((size_t)(m + 1) * rp);
+        h->gb_conv.alloc((size_t)rp);
+        h->gb_iter.alloc(1);
+        h->gb_m = m;
+        h->gb_rp = rp;
+    }
+    GmresBatch g;
+    g.V = h->gb_V.p;
+    g.w = h->gb_w.p;
+    g.vcur = h->gb_vcur.p;
+    g.H = h->gb_H.p;
+    g.cs = h->gb_cs.p;
+    g.sn = h->gb_sn.p;
+    g.s = h->gb_s.p;
+    g.part = h->gb_part.p;
+    g.hsum = h->gb_hsum.p;
+    g.normb = h->gb_normb.p;
+    g.resid = h->gb_resid.p;
+    g.y = h->gb_y.p;
+    g.conv = h->gb_conv.p;
+    g.iter = h->gb_iter.p;
+    g.N = N;
+    g.m = m;
+    g.rp = rp;
+    g.nrhs = nrhs;
+    g.nblk = nblk;
+    return g;
+}
+
+// Lockstep GMRES over the nrhs <= rp systems of an interleaved leaf-order
+// block: bi right-hand sides, xi initial guesses (updated in place; x0_zero:
+// skip the initial product). iters / resid per column (nrhs entries).
+int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrhs, int max_iter, double tol, int prec,
+                    bool x0_zero, int *iters, double *resid) {
+    if (max_iter < 1 || max_iter > 400) throw ApiError(H2W_ERR_ARG, "batched GMRES: max_iter must be in 1..400");
+    GmresBatch g = gmb_state(h, max_iter, rp, nrhs);
+    cudaStream_t st = h->stream;
+    CK(gmb_norms(g, bi, g.normb, 1, st));
+    if (x0_zero) {
+        CK(gmb_start(g, bi, nullptr, tol, st));
+    } else {
+        if (h->m_ri.n < (size_t)h->tree.N * rp) h->m_ri.alloc((size_t)h->tree.N * MR_MAX);
+        run_matvec_multi(h, prec, rp, xi, h->m_ri.p, st);
+        CK(gmb_start(g, bi, h->m_ri.p, tol, st));
+    }
+    std::vector<int32_t> conv((size_t)rp);
+    auto read_conv = [&] {
+        CK(cudaMemcpyAsync(conv.data(), g.conv, (size_t)rp * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int c = 0; c < nrhs; ++c)
+            if (conv[(size_t)c] == -1) return false;
+        return true;
+    };
+    bool done = read_conv();
+    int last = -1;
+    for (int i = 0; i < max_iter && !done; ++i) {
+        run_matvec_multi(h, prec, rp, g.vcur, g.w, st);
+        CK(gmb_arnoldi(g, tol, st));
+        last = i;
+        done = read_conv();
+    }
+    int kmax = -1;
+    for (int c = 0; c < nrhs; ++c) {
+        const int cv = conv[(size_t)c];
+        kmax = std::max(kmax, cv >= 0 ? cv : (cv == -1 ? last : -1));
+    }
+    CK(gmb_finish(g, xi, last, kmax, st));
+    std::vector<double> rs((size_t)rp);
+    CK(cudaMemcpyAsync(rs.data(), g.resid, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    bool all = true;
+    for (int c = 0; c < nrhs; ++c) {
+        const int cv = conv[(size_t)c];
+        iters[c] = cv >= 0 ? cv + 1 : (cv == -2 ? 0 : last + 1);
+        resid[c] = rs[(size_t)c];
+        if (cv == -1) all = false;
+    }
+    return all ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+}
+
 // --------------------------------------------------------------- GMRES ---
 GmresDev gmres_state(h2w_handle *h, int m) {
     const int64_t N = h->tree.N;
@@ -1469,6 +1661,40 @@ void check_device_error(h2w_handle *h) {
         CK(cudaMemsetAsync(h->d_bar.p, 0, 8, h->stream));
         throw ApiError(H2W_ERR_CUDA, "matvec: a grid-barrier wait ran out (device error flag)");
     }
+}
+
+// Column blocks of up to 64 right-hand sides: stage (host) and pack into
+// interleaved leaf order, run f on the block, unpack x back.
+template <class F>
+void for_rhs_blocks(h2w_handle *h, const double *b, double *x, int nrhs, int where, F &&f) {
+    const int64_t N = h->tree.N;
+    cudaStream_t st = h->stream;
+    ensure_multi_vectors(h);
+    if (h->m_bi.n < (size_t)N * MR_MAX) h->m_bi.alloc((size_t)N * MR_MAX);
+    if (where == H2W_HOST) {
+        if (h->m_stage_x.n < (size_t)N * MR_MAX) h->m_stage_x.alloc((size_t)N * MR_MAX);
+        if (h->m_stage_y.n < (size_t)N * MR_MAX) h->m_stage_y.alloc((size_t)N * MR_MAX);
+    }
+    for (int c0 = 0; c0 < nrhs; c0 += MR_MAX) {
+        const int nc = std::min(MR_MAX, nrhs - c0), rp = rp_for(nc);
+        const double *bc = b + (size_t)c0 * N;
+        double *xc = x + (size_t)c0 * N;
+        const double *xsrc = xc;
+        if (where == H2W_HOST) {
+            CK(cudaMemcpyAsync(h->m_stage_x.p, bc, (size_t)N * nc * 8, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(h->m_stage_y.p, xc, (size_t)N * nc * 8, cudaMemcpyHostToDevice, st));
+            bc = h->m_stage_x.p;
+            xsrc = h->m_stage_y.p;
+        }
+        CK(launch_mr_pack(bc, N, h->m_bi.p, h->d_perm.p, N, nc, rp, st));
+        CK(launch_mr_pack(xsrc, N, h->m_xi.p, h->d_perm.p, N, nc, rp, st));
+        f(c0, nc, rp, h->m_bi.p, h->m_xi.p);
+        CK(launch_mr_unpack(h->m_xi.p, where == H2W_HOST ? h->m_stage_y.p : xc, N, h->d_perm.p, N, nc, rp, st));
+        if (where == H2W_HOST)
+            CK(cudaMemcpyAsync(xc, h->m_stage_y.p, (size_t)N * nc * 8, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    check_device_error(h);
 }
 
 int fail(h2w_handle *h, int code, const std::string &m) {
@@ -1808,6 +2034,15 @@ int h2w_assemble(h2w_handle *h, int mode) {
         h->storage = storage_entries(h);
         h->has_op = true;
         h->g_m = -1;
+        h->gb_m = -1;
+        h->ph_t0.clear();
+        h->ph_t1.clear();
+        for (const Phase &ph : h->mphases) {
+            h->ph_t0.push_back(ph.t0);
+            h->ph_t1.push_back(ph.t1);
+        }
+        h->m_wsd.reset();
+        h->m_wsf.reset();
         return H2W_OK;
     });
 }
@@ -1836,6 +2071,33 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
         if (!x || !y || nrhs < 1 || (where != H2W_HOST && where != H2W_DEVICE)) throw ApiError(H2W_ERR_ARG, "bad matvec arguments");
         cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
         const int64_t N = h->tree.N;
+        if (nrhs > 1) {
+            // blocks of up to 64 columns through the multi-vector kernel
+            ensure_multi_vectors(h);
+            if (where == H2W_HOST) {
+                if (h->m_stage_x.n < (size_t)N * MR_MAX) h->m_stage_x.alloc((size_t)N * MR_MAX);
+                if (h->m_stage_y.n < (size_t)N * MR_MAX) h->m_stage_y.alloc((size_t)N * MR_MAX);
+            }
+            for (int c0 = 0; c0 < nrhs; c0 += MR_MAX) {
+                const int nc = std::min(MR_MAX, nrhs - c0), rp = rp_for(nc);
+                const double *xc = x + (size_t)c0 * N;
+                double *yc = y + (size_t)c0 * N;
+                if (where == H2W_HOST) {
+                    CK(cudaMemcpyAsync(h->m_stage_x.p, xc, (size_t)N * nc * 8, cudaMemcpyHostToDevice, st));
+                    xc = h->m_stage_x.p;
+                }
+                CK(launch_mr_pack(xc, N, h->m_xi.p, h->d_perm.p, N, nc, rp, st));
+                run_matvec_multi(h, precision == H2W_PREC_FP32 ? H2W_PREC_FP32 : H2W_PREC_FP64, rp, h->m_xi.p,
+                                 h->m_yi.p, st);
+                CK(launch_mr_unpack(h->m_yi.p, where == H2W_HOST ? h->m_stage_y.p : yc, N, h->d_perm.p, N, nc, rp,
+                                    st));
+                if (where == H2W_HOST)
+                    CK(cudaMemcpyAsync(yc, h->m_stage_y.p, (size_t)N * nc * 8, cudaMemcpyDeviceToHost, st));
+            }
+            if (where == H2W_HOST) CK(cudaStreamSynchronize(st));
+            check_device_error(h);
+            return H2W_OK;
+        }
         if (where == H2W_HOST) {
             h->d_x.n < (size_t)N ? h->d_x.alloc((size_t)N) : (void)0;
             h->d_y.n < (size_t)N ? h->d_y.alloc((size_t)N) : (void)0;
@@ -1958,6 +2220,78 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         }
         CK(cudaStreamSynchronize(st));
         check_device_error(h);
+        return rc;
+    });
+}
+
+int h2w_gmres_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max_iter, int tol_pow, int where,
+                    int *iters, double *resid) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!b || !x || nrhs < 1 || max_iter < 1 || max_iter > 400 || !iters || !resid ||
+            (where != H2W_HOST && where != H2W_DEVICE))
+            throw ApiError(H2W_ERR_ARG, "bad gmres_batch arguments");
+        const double tol = std::pow(10, -1.0 * tol_pow);
+        int rc = H2W_OK;
+        for_rhs_blocks(h, b, x, nrhs, where, [&](int c0, int nc, int rp, double *bi, double *xi) {
+            int r = gmres_batch_run(h, bi, xi, rp, nc, max_iter, tol, H2W_PREC_FP64, false, iters + c0, resid + c0);
+            if (r != H2W_OK) rc = r;
+        });
+        return rc;
+    });
+}
+
+int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max_outer, int inner_iter,
+                       int tol_pow, int where, int *outer_iters, int *inner_total, double *resid) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!b || !x || nrhs < 1 || max_outer < 1 || inner_iter < 1 || inner_iter > 400 || !outer_iters ||
+            !inner_total || !resid || (where != H2W_HOST && where != H2W_DEVICE))
+            throw ApiError(H2W_ERR_ARG, "bad gmres_ir_batch arguments");
+        const int64_t N = h->tree.N;
+        cudaStream_t st = h->stream;
+        const double tol = std::pow(10, -1.0 * tol_pow);
+        *outer_iters = 0;
+        *inner_total = 0;
+        int rc = H2W_OK;
+        if (h->m_ri.n < (size_t)N * MR_MAX) h->m_ri.alloc((size_t)N * MR_MAX);
+        if (h->m_di.n < (size_t)N * MR_MAX) h->m_di.alloc((size_t)N * MR_MAX);
+        if (!h->m_onorm.p) h->m_onorm.alloc(MR_MAX);
+        if (!h->m_ores.p) h->m_ores.alloc(MR_MAX);
+        for_rhs_blocks(h, b, x, nrhs, where, [&](int c0, int nc, int rp, double *bi, double *xi) {
+            GmresBatch g = gmb_state(h, inner_iter, rp, nc);
+            const size_t len = (size_t)N * rp;
+            CK(gmb_norms(g, bi, h->m_onorm.p, 1, st));
+            std::vector<double> nb((size_t)rp), nr((size_t)rp);
+            CK(cudaMemcpyAsync(nb.data(), h->m_onorm.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
+            std::vector<int> it((size_t)rp);
+            std::vector<double> ir((size_t)rp);
+            bool ok = false;
+            for (int o = 0; o <= max_outer; ++o) {
+                // FP64 residual r = b - A x
+                run_matvec_multi(h, H2W_PREC_FP64, rp, xi, h->m_ri.p, st);
+                CK(vec_axpby(1.0, bi, -1.0, h->m_ri.p, h->m_ri.p, (int64_t)len, st));
+                CK(gmb_norms(g, h->m_ri.p, h->m_ores.p, 0, st));
+                CK(cudaMemcpyAsync(nr.data(), h->m_ores.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                ok = true;
+                for (int c = 0; c < nc; ++c) {
+                    resid[c0 + c] = nr[(size_t)c] / nb[(size_t)c];
+                    if (!(resid[c0 + c] < tol)) ok = false;
+                }
+                if (ok || o == max_outer) break;
+                // FP32-operator inner GMRES on A d = r from d = 0, relative tolerance 1e-6
+                CK(cudaMemsetAsync(h->m_di.p, 0, len * 8, st));
+                gmres_batch_run(h, h->m_ri.p, h->m_di.p, rp, nc, inner_iter, 1e-6, H2W_PREC_FP32, true, it.data(),
+                                ir.data());
+                int mx = 0;
+                for (int c = 0; c < nc; ++c) mx = std::max(mx, it[(size_t)c]);
+                *inner_total += mx;
+                CK(vec_axpby(1.0, xi, 1.0, h->m_di.p, xi, (int64_t)len, st));
+                *outer_iters = std::max(*outer_iters, o + 1);
+            }
+            if (!ok) rc = H2W_ERR_NOT_CONVERGED;
+        });
         return rc;
     });
 }

@@ -16,6 +16,7 @@
 #include <climits>
 
 #include "kernels.cuh"
+#include "sync.cuh"
 
 namespace h2w {
 
@@ -656,36 +657,6 @@ __global__ void __launch_bounds__(BRG_THREADS, 4)
                const int32_t *__restrict__ perm) {
     __shared__ BrgShared<T> sh;
     for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) brg_target<T>(sh, t, roff, blob, A, ws, xin, yout, perm);
-}
-
-// Grid-wide barrier for the cooperative matvec (all CTAs are co-resident by
-// construction of the cooperative launch). bar[0] counts arrivals, bar[1] is
-// the generation. The spin is bounded: a barrier that never completes sets
-// *err and lets the CTA continue, so the kernel always ends.
-__device__ void grid_barrier(unsigned *bar, unsigned nblocks, int32_t *err) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *vgen = bar + 1;
-        const unsigned gen = *vgen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            long long it = 0;
-            while (*vgen == gen) {
-                if (++it > (1LL << 26)) {
-                    atomicExch(err, 1);
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
 }
 
 // The whole matvec in one cooperative launch: phases separated by grid

@@ -86,4 +86,44 @@ cudaError_t vec_axpby(double a, const double *x, double b, const double *y, doub
 cudaError_t vec_f64_to_f32(const double *x, float *y, int64_t n, cudaStream_t st);
 cudaError_t vec_f32_to_f64(const float *x, double *y, int64_t n, cudaStream_t st);
 
+// ------------------------------------------------ multiple right-hand sides
+// Blocks of rp vectors are interleaved: element (t, c) at t*rp + c
+// (rp = 16, 32 or 64). The workspace holds ws_n rows of rp values.
+struct MrPhases {          // per-phase launches instead of one cooperative launch
+    const int64_t *t0, *t1;
+    int n;
+};
+cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                          const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                          unsigned *bar, int32_t *err, cudaStream_t st);
+cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                          const MrPhases *phased, const float *A, float *ws, const float *xin, double *yout,
+                          unsigned *bar, int32_t *err, cudaStream_t st);
+cudaError_t launch_mr_pack(const double *x, int64_t ldx, double *xi, const int32_t *perm, int64_t n, int nrhs,
+                           int rp, cudaStream_t st);
+cudaError_t launch_mr_unpack(const double *yi, double *y, int64_t ldy, const int32_t *perm, int64_t n, int nrhs,
+                             int rp, cudaStream_t st);
+cudaError_t launch_mr_widen_f64(const double *a, double *b, int64_t n, cudaStream_t st);
+cudaError_t launch_mr_widen_f32(const float *a, double *b, int64_t n, cudaStream_t st);
+
+// Batched GMRES state (rp interleaved systems, Krylov dimension m).
+struct GmresBatch {
+    double *V;               // (m+1) blocks of N*rp
+    double *w, *vcur;        // N*rp
+    double *H;               // per column c: (m+1) x m column-major at c*m*(m+1)
+    double *cs, *sn, *s;     // per column c: m+1 at c*(m+1)
+    double *part;            // nblk x (m+1) x rp block partial sums
+    double *hsum;            // (m+1) x rp reduced sums
+    double *normb, *resid;   // rp
+    double *y;               // (m+1) x rp back-substituted coefficients
+    int32_t *conv;           // rp: -1 running, k >= 0 converged at Arnoldi column k, -2 at the start, -3 padding
+    int32_t *iter;           // current Arnoldi column
+    int64_t N;
+    int m, rp, nrhs, nblk;
+};
+cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
+cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st);
+cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st);
+cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st);
+
 }  // namespace h2w

@@ -1,0 +1,614 @@
+// Multi-right-hand-side matvec and batched GMRES (sm_103a).
+//
+//  * mr_kernel / mr_coop_kernel  Y = A X for RP right-hand sides at once, over
+//      the same packed target records as the single-vector GEMV: a target is
+//      a small GEMM (rows x RP) = sum_p A_p (rows x w_p) X_p (w_p x RP). The
+//      operator panels and the gathered sources are staged through shared
+//      memory in 32-column chunks (the next chunk is loaded into registers
+//      while the current one is multiplied) and every thread keeps a 4-row x
+//      4-column block of the result, so each operator element read from HBM
+//      feeds RP fused multiply-adds. The input block is read in the
+//      kernel's precision (FP32 kernel: an FP32 copy). Vectors are interleaved: element (t, c)
+//      of a block of RP vectors sits at t*RP + c, so one source row is RP
+//      contiguous values.
+//  * mr_pack / mr_unpack  column-major vectors in the caller's point order
+//      <-> interleaved leaf-order blocks.
+//  * gmb_*  GMRES over RP systems in lockstep (the reference's unrestarted
+//      GMRES, */codes/gmres.hpp:92-200, per column): CGS2 Arnoldi, Givens
+//      rotations, per-column convergence; one column's numbers never mix
+//      with another's.
+#include <cfloat>
+
+#include "kernels.cuh"
+#include "sync.cuh"
+
+namespace h2w {
+
+constexpr int MR_MT = 64;  // result rows per tile
+constexpr int MR_KC = 32;  // operator columns per staged chunk
+
+template <class T> struct MrVec;
+template <> struct MrVec<double> { using type = double2; static constexpr int n = 2; };
+template <> struct MrVec<float> { using type = float4; static constexpr int n = 4; };
+
+template <class T, int RP> struct MrLayout {
+    static constexpr int NT = 4 * RP;                  // 16 row quads x RP/4 column quads
+    static constexpr int VN = MrVec<T>::n;             // elements per 16-byte vector
+    static constexpr int NA = MR_KC * MR_MT / VN / NT; // A vectors per thread per chunk
+    static constexpr int NX = MR_KC * RP / VN / NT;    // X vectors per thread per chunk
+    static constexpr size_t rec_bytes = (size_t)BRG_REC_WORDS * 8;
+    static constexpr size_t as_bytes = sizeof(T) * MR_KC * MR_MT;
+    static constexpr size_t xs_bytes = sizeof(T) * MR_KC * RP;
+    static constexpr size_t map_bytes = (size_t)4 * BRG_XS_ELEMS;
+    static constexpr size_t smem = rec_bytes + as_bytes + xs_bytes + map_bytes;
+    static_assert(NA >= 1 && NA * VN * NT == MR_KC * MR_MT, "A chunk split");
+    static_assert(NX >= 1 && NX * VN * NT == MR_KC * RP, "X chunk split");
+};
+
+__device__ __forceinline__ void mr_zero(double2 &v) { v = make_double2(0.0, 0.0); }
+__device__ __forceinline__ void mr_zero(float4 &v) { v = make_float4(0.f, 0.f, 0.f, 0.f); }
+__device__ __forceinline__ void mr_scalar(double2 &v, const double *p, int nv) {
+    v.x = nv > 0 ? p[0] : 0.0;
+    v.y = nv > 1 ? p[1] : 0.0;
+}
+__device__ __forceinline__ void mr_scalar(float4 &v, const float *p, int nv) {
+    v.x = nv > 0 ? p[0] : 0.f;
+    v.y = nv > 1 ? p[1] : 0.f;
+    v.z = nv > 2 ? p[2] : 0.f;
+    v.w = nv > 3 ? p[3] : 0.f;
+}
+__device__ __forceinline__ void mr_get4(double *o, const double *p) {
+    const double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+__device__ __forceinline__ void mr_get4(float *o, const float *p) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+}
+
+// One target of the packed record stream (record layout as the
+// single-vector GEMV: header, panels, segments).
+template <class T, int RP>
+__device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *__restrict__ roff,
+                                          const int64_t *__restrict__ blob, const T *__restrict__ A, T *ws,
+                                          const T *__restrict__ xin, double *yout) {
+    using Lay = MrLayout<T, RP>;
+    using V = typename MrVec<T>::type;
+    constexpr int NT = Lay::NT, VN = Lay::VN, NA = Lay::NA, NX = Lay::NX;
+    int64_t *rec = reinterpret_cast<int64_t *>(smem);
+    T *As = reinterpret_cast<T *>(smem + Lay::rec_bytes);
+    T *Xs = reinterpret_cast<T *>(smem + Lay::rec_bytes + Lay::as_bytes);
+    int32_t *map = reinterpret_cast<int32_t *>(smem + Lay::rec_bytes + Lay::as_bytes + Lay::xs_bytes);
+    const int tid = threadIdx.x;
+    const int ty = tid / (RP / 4), tx = tid % (RP / 4);
+
+    const int64_t o = roff[t];
+    const int nw = (int)(roff[t + 1] - o);
+    for (int q = tid; q < nw; q += NT) rec[q] = blob[o + q];
+    __syncthreads();
+    const int64_t dst = rec[0];
+    const int nrows = (int)(rec[1] & 0xffffffff), flags = (int)(rec[1] >> 32);
+    const int np = (int)(rec[2] & 0xffffffff), ns = (int)(rec[2] >> 32);
+    const int64_t *pan = rec + 3;
+    const int64_t *seg = pan + 3 * np;
+    // source map: gathered row e -> workspace row (>= 0), input row (-2 - pos) or none (-1)
+    int xend = 0;
+    for (int q = 0; q < np; ++q) {
+        const int e = (int)pan[3 * q + 2] + (int)(pan[3 * q + 1] >> 32);
+        xend = e > xend ? e : xend;
+    }
+    for (int e = tid; e < xend; e += NT) map[e] = -1;
+    __syncthreads();
+    for (int s = 0; s < ns; ++s) {
+        const int64_t src = seg[2 * s], w1 = seg[2 * s + 1];
+        const int len = (int)(w1 & 0xffffffff), code = (int)(w1 >> 32);
+        const int xo = code >> 1;
+        const bool g = code & 1;
+        for (int i = tid; i < len; i += NT) map[xo + i] = g ? -(2 + (int)(src + i)) : (int)(src + i);
+    }
+    __syncthreads();
+
+    V ra[NA], rx[NX];
+    // load chunk (panel q, columns c0 .. c0+KC) of row tile rt0 into registers
+    auto load = [&](int q, int c0, int rt0) {
+        const int64_t pa = pan[3 * q];
+        const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
+        const int xoff = (int)pan[3 * q + 2];
+        const bool vec = ((pa & 3) == 0) && ((lda & 3) == 0);  // the plan's 16-byte-row rule (4 elements)
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+            const int v = tid + NT * u;
+            const int col = v / (MR_MT / VN), r = rt0 + (v % (MR_MT / VN)) * VN;
+            const int c = c0 + col;
+            if (c < w && r < nrows) {
+                const T *p = A + pa + (int64_t)c * lda + r;
+                if (vec) ra[u] = *reinterpret_cast<const V *>(p);
+                else mr_scalar(ra[u], p, nrows - r);
+            } else {
+                mr_zero(ra[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < NX; ++u) {
+            const int v = tid + NT * u;
+            const int row = v / (RP / VN), cv = (v % (RP / VN)) * VN;
+            mr_zero(rx[u]);
+            if (c0 + row < w) {
+                const int m = map[xoff + c0 + row];
+                if (m >= 0) rx[u] = *reinterpret_cast<const V *>(ws + (int64_t)m * RP + cv);
+                else if (m <= -2) rx[u] = *reinterpret_cast<const V *>(xin + (int64_t)(-2 - m) * RP + cv);
+            }
+        }
+    };
+    auto store = [&]() {
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+            const int v = tid + NT * u;
+            *reinterpret_cast<V *>(As + (v / (MR_MT / VN)) * MR_MT + (v % (MR_MT / VN)) * VN) = ra[u];
+        }
+#pragma unroll
+        for (int u = 0; u < NX; ++u) {
+            const int v = tid + NT * u;
+            *reinterpret_cast<V *>(Xs + (v / (RP / VN)) * RP + (v % (RP / VN)) * VN) = rx[u];
+        }
+    };
+
+    for (int rt0 = 0; rt0 < nrows; rt0 += MR_MT) {
+        T acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+        int q = 0, c0 = 0;
+        if (np > 0) load(0, 0, rt0);
+        while (q < np) {
+            store();
+            __syncthreads();
+            int nq = q, nc0 = c0 + MR_KC;
+            if (nc0 >= (int)(pan[3 * q + 1] >> 32)) { nq = q + 1; nc0 = 0; }
+            if (nq < np) load(nq, nc0, rt0);
+#pragma unroll 8
+            for (int k = 0; k < MR_KC; ++k) {
+                T a4[4], x4[4];
+                mr_get4(a4, As + k * MR_MT + ty * 4);
+                mr_get4(x4, Xs + k * RP + tx * 4);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] += a4[i] * x4[j];
+            }
+            __syncthreads();
+            q = nq;
+            c0 = nc0;
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = rt0 + ty * 4 + i;
+            if (r >= nrows) continue;
+            const int64_t d = (dst + r) * RP + tx * 4;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const T v = acc[i][j];
+                if (flags & T_SCATTER) yout[d + j] = (double)((flags & T_ACCUM) ? ws[d + j] + v : v);
+                else if (flags & T_ATOMIC) atomicAdd(ws + d + j, v);
+                else if (flags & T_ACCUM) ws[d + j] += v;
+                else ws[d + j] = v;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <class T, int RP>
+__global__ void __launch_bounds__(4 * RP)
+    mr_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
+              const T *__restrict__ A, T *ws, const T *__restrict__ xin, double *yout) {
+    extern __shared__ __align__(16) char mr_smem[];
+    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) mr_target<T, RP>(mr_smem, t, roff, blob, A, ws, xin, yout);
+}
+
+template <class T, int RP>
+__global__ void __launch_bounds__(4 * RP)
+    mr_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
+                   const int64_t *__restrict__ pstart, int nphase, const T *__restrict__ A, T *ws,
+                   const T *__restrict__ xin, double *yout, unsigned *bar, int32_t *err) {
+    extern __shared__ __align__(16) char mr_smem[];
+    for (int p = 0; p < nphase; ++p) {
+        const int64_t t1 = pstart[p + 1];
+        for (int64_t t = pstart[p] + blockIdx.x; t < t1; t += gridDim.x)
+            mr_target<T, RP>(mr_smem, t, roff, blob, A, ws, xin, yout);
+        if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
+    }
+}
+
+static int mr_num_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <class T, int RP>
+static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                               const MrPhases *phased, const T *A, T *ws, const T *xin, double *yout,
+                               unsigned *bar, int32_t *err, cudaStream_t st) {
+    using Lay = MrLayout<T, RP>;
+    static int per_sm_coop = 0, per_sm = 0;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(mr_coop_kernel<T, RP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Lay::smem);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(mr_kernel<T, RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const int nsm = mr_num_sms();
+    if (phased) {
+        if (per_sm == 0) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_kernel<T, RP>, Lay::NT, Lay::smem);
+            if (per_sm <= 0) per_sm = 1;
+        }
+        for (int p = 0; p < phased->n; ++p) {
+            const int64_t t0 = phased->t0[p], t1 = phased->t1[p];
+            if (t1 <= t0) continue;
+            const int64_t cap = (int64_t)nsm * per_sm;
+            const int grid = (int)(t1 - t0 < cap ? t1 - t0 : cap);
+            mr_kernel<T, RP><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, A, ws, xin, yout);
+            count_launch();
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    if (per_sm_coop == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, mr_coop_kernel<T, RP>, Lay::NT, Lay::smem);
+        if (per_sm_coop <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    }
+    const int grid = nsm * per_sm_coop;
+    void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&A,
+                    (void *)&ws,   (void *)&xin,  (void *)&yout,   (void *)&bar,    (void *)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_coop_kernel<T, RP>, dim3(grid), dim3(Lay::NT), args,
+                                                Lay::smem, st);
+    count_launch();
+    return e;
+}
+
+template <class T>
+static cudaError_t mr_dispatch(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                               const MrPhases *phased, const T *A, T *ws, const T *xin, double *yout,
+                               unsigned *bar, int32_t *err, cudaStream_t st) {
+    switch (rp) {
+    case 16: return mr_launch_t<T, 16>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    case 32: return mr_launch_t<T, 32>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    case 64: return mr_launch_t<T, 64>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                          const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                          unsigned *bar, int32_t *err, cudaStream_t st) {
+    return mr_dispatch<double>(rp, roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+}
+cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                          const MrPhases *phased, const float *A, float *ws, const float *xin, double *yout,
+                          unsigned *bar, int32_t *err, cudaStream_t st) {
+    return mr_dispatch<float>(rp, roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+}
+
+// ------------------------------------------------------ pack / unpack ---
+// xi[t*rp + c] = x[perm[t] + c*ldx] for c < nrhs, 0 for the padding columns
+__global__ void mr_pack_kernel(const double *__restrict__ x, int64_t ldx, double *__restrict__ xi,
+                               const int32_t *__restrict__ perm, int64_t n, int nrhs, int rp) {
+    const int64_t tot = n * rp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = e / rp;
+        const int c = (int)(e % rp);
+        xi[e] = c < nrhs ? x[(perm ? (int64_t)perm[t] : t) + (int64_t)c * ldx] : 0.0;
+    }
+}
+__global__ void mr_unpack_kernel(const double *__restrict__ yi, double *__restrict__ y, int64_t ldy,
+                                 const int32_t *__restrict__ perm, int64_t n, int nrhs, int rp) {
+    const int64_t tot = n * rp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = e / rp;
+        const int c = (int)(e % rp);
+        if (c < nrhs) y[(perm ? (int64_t)perm[t] : t) + (int64_t)c * ldy] = yi[e];
+    }
+}
+template <class T>
+__global__ void mr_widen_kernel(const T *__restrict__ a, double *__restrict__ b, int64_t n) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        b[e] = (double)a[e];
+}
+cudaError_t launch_mr_pack(const double *x, int64_t ldx, double *xi, const int32_t *perm, int64_t n, int nrhs,
+                           int rp, cudaStream_t st) {
+    mr_pack_kernel<<<1216, 256, 0, st>>>(x, ldx, xi, perm, n, nrhs, rp);
+    count_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_mr_unpack(const double *yi, double *y, int64_t ldy, const int32_t *perm, int64_t n, int nrhs,
+                             int rp, cudaStream_t st) {
+    mr_unpack_kernel<<<1216, 256, 0, st>>>(yi, y, ldy, perm, n, nrhs, rp);
+    count_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_mr_widen_f64(const double *a, double *b, int64_t n, cudaStream_t st) {
+    mr_widen_kernel<double><<<1216, 256, 0, st>>>(a, b, n);
+    count_launch();
+    return cudaGetLastError();
+}
+cudaError_t launch_mr_widen_f32(const float *a, double *b, int64_t n, cudaStream_t st) {
+    mr_widen_kernel<float><<<1216, 256, 0, st>>>(a, b, n);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- batched GMRES ---
+constexpr int GMB_THREADS = 256;
+
+__device__ __forceinline__ void gmb_rows(const GmresBatch &g, int64_t &r0, int64_t &r1) {
+    const int64_t chunk = (g.N + g.nblk - 1) / g.nblk;
+    r0 = (int64_t)blockIdx.x * chunk;
+    r1 = r0 + chunk < g.N ? r0 + chunk : g.N;
+}
+__device__ __forceinline__ size_t gmb_h(const GmresBatch &g, int c, int row, int col) {
+    return ((size_t)c * g.m + col) * (g.m + 1) + row;
+}
+
+// out[(blk*(m+1) + k)*rp + c] = sum over the block's rows of a_k[t, c] * b[t, c],
+// k = 0..kn-1, a_k = a + k*N*rp (kn = 1: a itself)
+__device__ void gmb_block_dots(const GmresBatch &g, const double *a, const double *b, int kn, int64_t r0,
+                               int64_t r1, double *red, double *out) {
+    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
+    const size_t stride = (size_t)g.N * rp;
+    for (int k = 0; k < kn; ++k) {
+        const double *ak = a + k * stride;
+        double acc = 0.0;
+        for (int64_t t = r0 + rl; t < r1; t += RL) acc += ak[t * rp + c] * b[t * rp + c];
+        red[rl * rp + c] = acc;
+        __syncthreads();
+        if (rl == 0) {
+            double s = 0.0;
+            for (int q = 0; q < RL; ++q) s += red[q * rp + c];
+            out[((size_t)blockIdx.x * (g.m + 1) + k) * rp + c] = s;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void gmb_dots(GmresBatch g) {
+    __shared__ double red[GMB_THREADS];
+    int64_t r0, r1;
+    gmb_rows(g, r0, r1);
+    gmb_block_dots(g, g.V, g.w, *g.iter + 1, r0, r1, red, g.part);
+}
+
+// hsum[k*rp + c] = sum_b part[(b*(m+1) + k)*rp + c] for k <= i (all = 1) or k = 0 (all = 0)
+__global__ void gmb_reduce(GmresBatch g, int all) {
+    const int kn = all ? *g.iter + 1 : 1;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)kn * g.rp) return;
+    const int k = (int)(e / g.rp), c = (int)(e % g.rp);
+    double s = 0.0;
+    for (int b = 0; b < g.nblk; ++b) s += g.part[((size_t)b * (g.m + 1) + k) * g.rp + c];
+    g.hsum[e] = s;
+}
+
+// h = hsum; H(:, i) (=|+=) h; w -= V h; then new dots (pass 0) or ||w||^2 partials (pass 1)
+__global__ void gmb_update(GmresBatch g, int pass) {
+    extern __shared__ double gmb_sm[];
+    double *h = gmb_sm;
+    double *red = gmb_sm + (size_t)(g.m + 1) * g.rp;
+    const int i = *g.iter, rp = g.rp;
+    for (int e = threadIdx.x; e < (i + 1) * rp; e += blockDim.x) h[e] = g.hsum[e];
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int e = threadIdx.x; e < (i + 1) * rp; e += blockDim.x) {
+            const int k = e / rp, c = e % rp;
+            double *Hk = g.H + gmb_h(g, c, k, i);
+            *Hk = pass == 0 ? h[e] : *Hk + h[e];
+        }
+    int64_t r0, r1;
+    gmb_rows(g, r0, r1);
+    const int c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
+    const size_t stride = (size_t)g.N * rp;
+    for (int64_t t = r0 + rl; t < r1; t += RL) {
+        double v = g.w[t * rp + c];
+        for (int k = 0; k <= i; ++k) v -= g.V[k * stride + t * rp + c] * h[k * rp + c];
+        g.w[t * rp + c] = v;
+    }
+    __syncthreads();
+    if (pass == 0) gmb_block_dots(g, g.V, g.w, i + 1, r0, r1, red, g.part);
+    else gmb_block_dots(g, g.w, g.w, 1, r0, r1, red, g.part);
+}
+
+// H(i+1, i) = ||w||; V[:, i+1] = vcur = w / ||w|| (a zero column stays zero)
+__global__ void gmb_normalise(GmresBatch g) {
+    const int i = *g.iter, rp = g.rp;
+    const int c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
+    const double hn = sqrt(g.hsum[c]);
+    if (blockIdx.x == 0 && rl == 0) g.H[gmb_h(g, c, i + 1, i)] = hn;
+    const double ih = hn > 0.0 ? 1.0 / hn : 0.0;
+    int64_t r0, r1;
+    gmb_rows(g, r0, r1);
+    double *Vn = g.V + (size_t)(i + 1) * g.N * rp;
+    for (int64_t t = r0 + rl; t < r1; t += RL) {
+        const double v = ih * g.w[t * rp + c];
+        Vn[t * rp + c] = v;
+        g.vcur[t * rp + c] = v;
+    }
+}
+
+__device__ __forceinline__ void gmb_apply(double &dx, double &dy, double cs, double sn) {
+    const double temp = __dadd_rn(__dmul_rn(cs, dx), __dmul_rn(sn, dy));
+    dy = __dadd_rn(__dmul_rn(-sn, dx), __dmul_rn(cs, dy));
+    dx = temp;
+}
+
+// Givens rotations of column i for every running system
+// (*/codes/gmres.hpp:30-75,156-162); one thread per column.
+__global__ void gmb_givens(GmresBatch g, double tol) {
+    const int i = *g.iter, c = threadIdx.x;
+    if (c < g.rp && g.conv[c] == -1) {
+        double *cs = g.cs + (size_t)c * (g.m + 1), *sn = g.sn + (size_t)c * (g.m + 1), *s = g.s + (size_t)c * (g.m + 1);
+        double *Hc = g.H + gmb_h(g, c, 0, i);
+        for (int k = 0; k < i; ++k) gmb_apply(Hc[k], Hc[k + 1], cs[k], sn[k]);
+        double dx = Hc[i], dy = Hc[i + 1], c_, s_;
+        if (dy == 0.0) { c_ = 1.0; s_ = 0.0; }
+        else if (fabs(dy) > fabs(dx)) {
+            const double temp = dx / dy;
+            s_ = 1.0 / sqrt(1.0 + temp * temp);
+            c_ = temp * s_;
+        } else {
+            const double temp = dy / dx;
+            c_ = 1.0 / sqrt(1.0 + temp * temp);
+            s_ = temp * c_;
+        }
+        cs[i] = c_;
+        sn[i] = s_;
+        gmb_apply(Hc[i], Hc[i + 1], c_, s_);
+        gmb_apply(s[i], s[i + 1], c_, s_);
+        const double resid = fabs(s[i + 1]) / g.normb[c];
+        g.resid[c] = resid;
+        if (resid < tol) g.conv[c] = i;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && i + 1 < g.m) *g.iter = i + 1;
+}
+
+// w = b - Ax (Ax == NULL: w = b) and per-block partials of ||w||^2
+__global__ void gmb_resid(GmresBatch g, const double *__restrict__ b, const double *__restrict__ Ax) {
+    __shared__ double red[GMB_THREADS];
+    int64_t r0, r1;
+    gmb_rows(g, r0, r1);
+    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
+    for (int64_t t = r0 + rl; t < r1; t += RL) g.w[t * rp + c] = Ax ? b[t * rp + c] - Ax[t * rp + c] : b[t * rp + c];
+    __syncthreads();
+    gmb_block_dots(g, g.w, g.w, 1, r0, r1, red, g.part);
+}
+// partials of ||v[:, c]||^2
+__global__ void gmb_colnorm_part(GmresBatch g, const double *__restrict__ v) {
+    __shared__ double red[GMB_THREADS];
+    int64_t r0, r1;
+    gmb_rows(g, r0, r1);
+    gmb_block_dots(g, v, v, 1, r0, r1, red, g.part);
+}
+// out[c] = sqrt(sum of the partials); zero_to_one: a zero norm becomes 1
+__global__ void gmb_colnorm_fin(GmresBatch g, double *out, int zero_to_one) {
+    const int c = threadIdx.x;
+    if (c >= g.rp) return;
+    double s = 0.0;
+    for (int b = 0; b < g.nblk; ++b) s += g.part[((size_t)b * (g.m + 1)) * g.rp + c];
+    s = sqrt(s);
+    out[c] = (zero_to_one && s == 0.0) ? 1.0 : s;
+}
+// beta = ||w|| (hsum); V[:, 0] = vcur = w / beta; s = beta e1; per-column state
+__global__ void gmb_start_fin(GmresBatch g, double tol) {
+    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
+    const double beta = sqrt(g.hsum[c]);
+    if (blockIdx.x == 0 && rl == 0) {
+        double *cs = g.cs + (size_t)c * (g.m + 1), *sn = g.sn + (size_t)c * (g.m + 1), *s = g.s + (size_t)c * (g.m + 1);
+        for (int k = 0; k <= g.m; ++k) { s[k] = 0.0; cs[k] = 0.0; sn[k] = 0.0; }
+        s[0] = beta;
+        const double r = beta / g.normb[c];
+        g.resid[c] = r;
+        g.conv[c] = c >= g.nrhs ? -3 : (r <= tol ? -2 : -1);
+        if (c == 0) *g.iter = 0;
+    }
+    const double ib = beta > 0.0 ? 1.0 / beta : 0.0;
+    int64_t r0, r1;
+    gmb_rows(g, r0, r1);
+    for (int64_t t = r0 + rl; t < r1; t += RL) {
+        const double v = g.w[t * rp + c] * ib;
+        g.V[t * rp + c] = v;
+        g.vcur[t * rp + c] = v;
+    }
+}
+// y_c = H_c(0:k, 0:k) \ s_c(0:k), k = the column's last Arnoldi index
+// (converged: conv; still running: last; converged at the start / padding: none),
+// in the reference's back-substitution order (*/codes/gmres.hpp:77-90)
+__global__ void gmb_backsolve(GmresBatch g, int last) {
+    const int c = threadIdx.x;
+    if (c >= g.rp) return;
+    const int cv = g.conv[c];
+    const int k = cv >= 0 ? cv : (cv == -1 ? last : -1);
+    const double *s = g.s + (size_t)c * (g.m + 1);
+    for (int j = 0; j <= g.m; ++j) g.y[(size_t)j * g.rp + c] = j <= k ? s[j] : 0.0;
+    for (int i = k; i >= 0; --i) {
+        double *y = g.y;
+        const double yi = y[(size_t)i * g.rp + c] / g.H[gmb_h(g, c, i, i)];
+        y[(size_t)i * g.rp + c] = yi;
+        for (int j = i - 1; j >= 0; --j) y[(size_t)j * g.rp + c] -= g.H[gmb_h(g, c, j, i)] * yi;
+    }
+}
+// x += V y over Arnoldi columns 0..kmax
+__global__ void gmb_xupdate(GmresBatch g, double *__restrict__ x, int kmax) {
+    const int rp = g.rp;
+    const size_t stride = (size_t)g.N * rp;
+    const int64_t tot = g.N * rp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e % rp);
+        double v = x[e];
+        for (int j = 0; j <= kmax; ++j) v += g.V[j * stride + e] * g.y[(size_t)j * rp + c];
+        x[e] = v;
+    }
+}
+
+static bool gmb_attr(const GmresBatch &g) {
+    static int set = 0;
+    const size_t need = ((size_t)(g.m + 1) * g.rp + GMB_THREADS) * 8;
+    if ((int)need > set) {
+        if (cudaFuncSetAttribute(gmb_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) != cudaSuccess)
+            return false;
+        set = (int)need;
+    }
+    return true;
+}
+static unsigned gmb_rgrid(const GmresBatch &g) {
+    return (unsigned)(((size_t)(g.m + 1) * g.rp + GMB_THREADS - 1) / GMB_THREADS);
+}
+
+cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st) {
+    gmb_colnorm_part<<<g.nblk, GMB_THREADS, 0, st>>>(g, v);
+    gmb_colnorm_fin<<<1, 64, 0, st>>>(g, out, zero_to_one);
+    count_launch(2);
+    return cudaGetLastError();
+}
+cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st) {
+    gmb_resid<<<g.nblk, GMB_THREADS, 0, st>>>(g, b, Ax);
+    gmb_reduce<<<1, 64, 0, st>>>(g, 0);
+    gmb_start_fin<<<g.nblk, GMB_THREADS, 0, st>>>(g, tol);
+    count_launch(3);
+    return cudaGetLastError();
+}
+cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st) {
+    if (!gmb_attr(g)) return cudaErrorInvalidValue;
+    const size_t smu = ((size_t)(g.m + 1) * g.rp + GMB_THREADS) * 8;
+    gmb_dots<<<g.nblk, GMB_THREADS, 0, st>>>(g);
+    gmb_reduce<<<gmb_rgrid(g), GMB_THREADS, 0, st>>>(g, 1);
+    gmb_update<<<g.nblk, GMB_THREADS, smu, st>>>(g, 0);
+    gmb_reduce<<<gmb_rgrid(g), GMB_THREADS, 0, st>>>(g, 1);
+    gmb_update<<<g.nblk, GMB_THREADS, smu, st>>>(g, 1);
+    gmb_reduce<<<1, 64, 0, st>>>(g, 0);
+    gmb_normalise<<<g.nblk, GMB_THREADS, 0, st>>>(g);
+    gmb_givens<<<1, 64, 0, st>>>(g, tol);
+    count_launch(8);
+    return cudaGetLastError();
+}
+cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st) {
+    gmb_backsolve<<<1, 64, 0, st>>>(g, last);
+    count_launch();
+    if (kmax >= 0) {
+        gmb_xupdate<<<g.nblk, GMB_THREADS, 0, st>>>(g, x, kmax);
+        count_launch();
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace h2w

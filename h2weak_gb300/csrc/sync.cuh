@@ -1,0 +1,37 @@
+// Device-side synchronisation shared by the persistent matvec kernels.
+#pragma once
+#include <cstdint>
+
+namespace h2w {
+
+// Grid-wide barrier for cooperative launches (all CTAs are co-resident by
+// construction of the launch). bar[0] counts arrivals, bar[1] is the
+// generation. The spin is bounded: a barrier that never completes sets *err
+// and lets the CTA continue, so the kernel always ends.
+static __device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned nblocks, int32_t *err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == gen) {
+                if (++it > (1LL << 26)) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+}  // namespace h2w

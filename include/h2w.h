@@ -117,6 +117,26 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
 int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int inner_iter, int tol_pow, int where,
                  int *outer_iters, int *inner_total, double *resid);
 
+/* Many right-hand sides at once. b and x are column-major N x nrhs (leading
+ * dimension N, original point order); x holds the initial guesses on entry.
+ * Columns go through the solver in blocks of up to 64 that share every
+ * operator read (one multi-vector matvec per Arnoldi step); each column runs
+ * its own GMRES (the reference's iterative_solver::GMRES,
+ * {1D,2D,3D}/codes/gmres.hpp:92-200, applied per column: own Krylov basis,
+ * Givens rotations and stopping test) and stops updating when it converges.
+ * iters / resid: nrhs entries. max_iter <= 400. The reference solves one
+ * right-hand side per call; this replaces a loop of such calls. */
+int h2w_gmres_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max_iter, int tol_pow, int where,
+                    int *iters, double *resid);
+/* Mixed precision for many right-hand sides: per block of up to 64 columns,
+ * FP64 residuals (one multi-vector FP64 matvec per outer step) and a batched
+ * FP32-operator inner GMRES (relative tolerance 1e-6, x0 = 0). resid: final
+ * FP64 relative residual per column (nrhs entries); outer_iters: largest
+ * outer count over the blocks; inner_total: inner Arnoldi steps summed over
+ * outer steps and blocks (lockstep steps, not per column). */
+int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max_outer, int inner_iter,
+                       int tol_pow, int where, int *outer_iters, int *inner_total, double *resid);
+
 /* Launch statistics of the block-row GEMV kernel that performs every matvec
  * pass. While enabled, each phase launch is bracketed by CUDA events on its
  * own stream; enabling (or disabling) resets the record. (No counterpart in
