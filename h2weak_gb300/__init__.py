@@ -22,7 +22,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libh2w.so")
 
 OK = 0
-ERR_NOT_CONVERGED = -5
+ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_RANK, ERR_NOT_CONVERGED, ERR_STATE = -1, -2, -3, -4, -5, -6
 FORM_NESTED, FORM_SEMINESTED = 0, 1
 KERNEL_IE, KERNEL_RBF = 0, 1
 ASSEMBLE_NCA, ASSEMBLE_IMPORT, ASSEMBLE_LEARNED = 0, 1, 2
@@ -81,6 +81,7 @@ def lib():
         "h2w_storage_entries": [P, ctypes.POINTER(D)],
         "h2w_operator_bytes": [P, I, ctypes.POINTER(I64)],
         "h2w_matvec": [P, P, P, I, I, I, P],
+        "h2w_matvec_static": [P, P, P, I, P],
         "h2w_gmres": [P, P, P, I, I, I, ctypes.POINTER(I), ctypes.POINTER(D)],
         "h2w_gmres_ir": [P, P, P, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)],
         "h2w_gmres_batch": [P, P, P, I, I, I, I, P, P],

@@ -1732,6 +1732,58 @@ void require_op(h2w_handle *h) {
 
 }  // namespace
 
+// The product of h2w_matvec (x, y device pointers, original point order) with
+// a caller-provided workspace, barrier state and error word instead of the
+// handle's: used by the allocation-free entry point (noalloc.cu). Allocates
+// nothing: the FP32 form needs the FP32 operator copy to exist already.
+namespace h2w {
+int handle_device(const h2w_handle *h) { return h ? h->cfg.device : -1; }
+int handle_fail(h2w_handle *h, int code, const char *msg) { return h ? fail(h, code, msg) : code; }
+int matvec_external_ws(h2w_handle *h, const double *x, double *y, int precision, void *stream, double *ws,
+                       int64_t ws_cap, unsigned *bar, int32_t *err) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!x || !y || !ws || !bar || !err || (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32))
+            throw ApiError(H2W_ERR_ARG, "bad matvec arguments");
+        const bool f32 = precision == H2W_PREC_FP32;
+        if (f32 && !h->d_op32.p)
+            throw ApiError(H2W_ERR_STATE,
+                           "FP32 operator copy not materialised (one h2w_matvec call with H2W_PREC_FP32 creates it)");
+        const int64_t need = f32 ? (h->ws_n + 1) / 2 : h->ws_n;  // in doubles
+        if (need > ws_cap)
+            throw ApiError(H2W_ERR_ARG, "matvec workspace of " + std::to_string(h->ws_n) + (f32 ? " floats" : " doubles") +
+                                            " exceeds the static scratch maximum of " + std::to_string(ws_cap) +
+                                            " doubles");
+        cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+        CK(cudaMemsetAsync(ws, 0, (size_t)need * 8, st));
+        CK(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+        CK(cudaMemsetAsync(err, 0, sizeof(int32_t), st));
+        const int32_t *perm = h->d_perm.p;
+        const int nph = (int)h->phases.size();
+        if (h->coop) {
+            if (f32)
+                CK(launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op32.p, (float *)ws, x, y, perm,
+                                   bar, err, st));
+            else
+                CK(launch_coop_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op.p, ws, x, y, perm, bar, err,
+                                   st));
+        } else {
+            for (const Phase &ph : h->phases) {
+                if (f32)
+                    CK(launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, (float *)ws, x, y, perm, st));
+                else
+                    CK(launch_brg_f64(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op.p, ws, x, y, perm, st));
+            }
+        }
+        if (!h->fused_scatter) {
+            if (f32) CK(launch_scatter_f32((float *)ws + h->yperm_off, y, perm, h->tree.N, st));
+            else CK(launch_scatter_f64(ws + h->yperm_off, y, perm, h->tree.N, st));
+        }
+        return H2W_OK;
+    });
+}
+}  // namespace h2w
+
 // ================================================================ C ABI ===
 extern "C" {
 

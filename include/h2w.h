@@ -107,6 +107,24 @@ int h2w_operator_bytes(h2w_handle *h, int precision, int64_t *bytes);
  * where = H2W_HOST or H2W_DEVICE; stream = cudaStream_t or NULL (default). */
 int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precision, int where, void *stream);
 
+/* y = A x like h2w_matvec (one right-hand side, x and y DEVICE pointers in
+ * original point order), but allocating nothing on any call: the workspace
+ * is a fixed device array of 2^21 doubles (16 MiB) inside the library, not
+ * handle memory. No counterpart in the reference (its mat_vec_prod keeps its
+ * work vectors in the tree nodes). Limits and rules:
+ *  - an operator whose workspace exceeds the array (more than 2^21 doubles
+ *    FP64, 2^22 floats FP32) is rejected with H2W_ERR_ARG;
+ *  - H2W_PREC_FP32 needs the FP32 operator copy, which this call does not
+ *    create: one h2w_matvec FP32 call creates it, otherwise H2W_ERR_STATE;
+ *  - the first call on a device looks up the array's device address (set-up,
+ *    once per device); make that first call before any stream capture;
+ *  - every call and every handle on a device shares the array, which keeps
+ *    the last call's contents (each call clears what must start at zero):
+ *    calls that overlap on the GPU race on it;
+ *  - asynchronous on `stream` (NULL: the handle's stream), like the DEVICE
+ *    form of h2w_matvec. */
+int h2w_matvec_static(h2w_handle *h, const double *x, double *y, int precision, void *stream);
+
 /* GMRES, unrestarted, FP64, device-resident. Replaces iterative_solver::GMRES
  * ({1D,2D,3D}/codes/gmres.hpp:92-200): x0 = x on entry, stops when |s(i+1)|/||b|| < 10^-tol_pow. */
 int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_pow, int where, int *iters,
