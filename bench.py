@@ -1,14 +1,17 @@
 """Benchmark: GMRES time-to-1e-10 and matvec HBM GB/s of the GB300 H2*
-operator, mixed precision (FP32 inner GMRES + FP64 iterative refinement)
-against the plain FP64 GPU form, with the CPU oracle timed beside it.
+operator, mixed precision and batched right-hand sides against the plain
+FP64 GPU form, with the CPU oracle timed beside it.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME] [--rhs R]
 
-A step is one solve of A x = b to relative residual 1e-10 from x0 = 1, b =
-A_dense x_true (manufactured solution, FP64 dense product on the GPU), with
-the compressed operator resident in HBM. value = solves per second of the
-mixed form over all ranks. Multi-GPU runs are independent replicas (one
-problem per GPU, no collective on the data path).
+A step solves A X = B for R = 64 right-hand sides together (one multi-vector
+product per Arnoldi step) to relative residual 1e-10 per column from X0 = 1,
+with the compressed operator resident in HBM: FP32-operator inner GMRES and
+iterative refinement. value = solved right-hand sides per second over all
+ranks. Beside it: the same columns by batched FP64 GMRES, and one right-hand
+side b = A_dense x_true (manufactured solution) by the single-vector mixed and
+plain FP64 solvers. Multi-GPU runs are independent replicas (one problem per
+GPU, no collective on the data path).
 """
 import argparse
 import json
@@ -180,6 +183,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="2d_ie_65536", choices=sorted(WORKLOADS))
+    ap.add_argument("--rhs", type=int, default=64, help="right-hand sides solved together per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
@@ -195,6 +199,7 @@ def main():
     import torch
     import torch.distributed as dist
     import h2weak_gb300 as hw
+    from h2weak_gb300 import synth
     torch.cuda.set_device(local)
     if world > 1:
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
@@ -207,29 +212,53 @@ def main():
     hw.build()
     op, nlev, xt = make_problem(wl, local)
     N = op.N
+    R = max(1, min(64, args.rhs))
     torch.cuda.synchronize()
     t0 = time.time()
     op.assemble(hw.ASSEMBLE_NCA)
     t_asm = time.time() - t0
     storage = op.storage_entries()
     dev = torch.device("cuda", local)
+    gtol = wl["gtol"]
+    # single right-hand side: b = A_dense x_true (manufactured solution)
     xt_d = torch.from_numpy(xt).to(dev)
     b_d = torch.empty(N, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
     hw.lib().h2w_dense_matvec(op.h, xt_d.data_ptr(), b_d.data_ptr(), 0, N, hw.DEVICE)
-    ones_d = torch.ones(N, dtype=torch.float64, device=dev)
-    x_d = torch.empty_like(ones_d)
+    torch.cuda.synchronize()
+    x_d = torch.empty_like(b_d)
+    # R right-hand sides: columns x_true_c (column 0 = x_true), B = A X_true with
+    # the FP64 compressed operator (the dense O(N^2) product per column is left
+    # to the sampled-row check below); column-major N x R = rows of an R x N tensor
+    XT = np.stack([synth.normal(synth.config_seed(1, c), N) for c in range(R)], axis=0)
+    XT_d = torch.from_numpy(XT).to(dev)
+    B_d = torch.empty_like(XT_d)
+    torch.cuda.synchronize()
+    op.matvec_device(XT_d.data_ptr(), B_d.data_ptr(), nrhs=R, precision=hw.PREC_FP64)
+    torch.cuda.synchronize()
+    X_d = torch.empty_like(XT_d)
+    op.set_option(hw.OPT_IR_RESIDUAL, hw.PREC_DF64)
+
+    def solve_batched():
+        X_d.fill_(1.0)
+        torch.cuda.synchronize()  # the library runs on its own stream
+        return op.gmres_ir_batch_device(B_d.data_ptr(), X_d.data_ptr(), R, max_outer=20, inner_iter=200,
+                                        tol_pow=gtol)
+
+    def solve_batched_fp64():
+        X_d.fill_(1.0)
+        torch.cuda.synchronize()
+        return op.gmres_batch_device(B_d.data_ptr(), X_d.data_ptr(), R, max_iter=400, tol_pow=gtol)
 
     def solve_mixed():
-        x_d.copy_(ones_d)
+        x_d.fill_(1.0)
         torch.cuda.synchronize()
-        return op.gmres_ir_device(b_d.data_ptr(), x_d.data_ptr(), max_outer=20, inner_iter=200,
-                                  tol_pow=wl["gtol"])
+        return op.gmres_ir_device(b_d.data_ptr(), x_d.data_ptr(), max_outer=20, inner_iter=200, tol_pow=gtol)
 
     def solve_fp64():
-        x_d.copy_(ones_d)
+        x_d.fill_(1.0)
         torch.cuda.synchronize()
-        return op.gmres_device(b_d.data_ptr(), x_d.data_ptr(), max_iter=500, tol_pow=wl["gtol"])
+        return op.gmres_device(b_d.data_ptr(), x_d.data_ptr(), max_iter=500, tol_pow=gtol)
 
     def timed(fn, k):
         barrier()
@@ -252,97 +281,91 @@ def main():
             ms = float(tt.item())
         return ms, out, hw.launch_count() - l0, (t0w, t1w)
 
+    def col_err(X):
+        return float(torch.max(torch.linalg.norm(X - XT_d, dim=1) / torch.linalg.norm(XT_d, dim=1)))
+
     K, W = max(1, args.steps), max(3, args.warmup)
+    # ---- the timed step: R right-hand sides, mixed precision, batched
     clocks = ClockSampler(local)
     clocks.start()
     for _ in range(W):
-        solve_mixed()
-    ms_mixed, out_mixed, launches, win = timed(solve_mixed, K)
+        solve_batched()
+    ms_b, out_b, launches, win = timed(solve_batched, K)
     clocks.stop()
+    outer_b, inner_b, res_b = out_b
+    err_b = col_err(X_d)
+    # FP64 residual of the batched solution (host check) and the dense sampled rows
+    Yb = torch.empty_like(X_d)
+    op.matvec_device(X_d.data_ptr(), Yb.data_ptr(), nrhs=R, precision=hw.PREC_FP64)
+    torch.cuda.synchronize()
+    fp64_resid_b = float(torch.max(torch.linalg.norm(B_d - Yb, dim=1) / torch.linalg.norm(B_d, dim=1)))
+    nrow = min(1024, N)
+    yrows = torch.empty(nrow, dtype=torch.float64, device=dev)
+    x0c = X_d[0].contiguous()
+    hw.lib().h2w_dense_matvec(op.h, x0c.data_ptr(), yrows.data_ptr(), 0, nrow, hw.DEVICE)
+    brows = torch.empty_like(yrows)
+    xt0 = XT_d[0].contiguous()
+    hw.lib().h2w_dense_matvec(op.h, xt0.data_ptr(), brows.data_ptr(), 0, nrow, hw.DEVICE)
+    torch.cuda.synchronize()
+    dense_rows_err = float(torch.linalg.norm(yrows - brows) / torch.linalg.norm(brows))
+    # ---- beside it: batched FP64 GMRES, single-vector mixed and FP64 solves
+    for _ in range(W):
+        solve_batched_fp64()
+    ms_b64, out_b64, _, _ = timed(solve_batched_fp64, K)
+    it_b64 = int(np.max(out_b64[0]))
+    err_b64 = col_err(X_d)
+    for _ in range(W):
+        solve_mixed()
+    ms_mixed, out_mixed, _, _ = timed(solve_mixed, K)
     outer, inner, res_mixed = out_mixed
     err_mixed = float(torch.linalg.norm(x_d - xt_d) / torch.linalg.norm(xt_d))
-
     for _ in range(W):
         solve_fp64()
     ms_fp64, out_fp64, _, _ = timed(solve_fp64, K)
     it64, res64 = out_fp64
     err_fp64 = float(torch.linalg.norm(x_d - xt_d) / torch.linalg.norm(xt_d))
 
-    # end to end through the C ABI with pinned host buffers (b and x0 in, x out)
-    b_h = b_d.cpu().pin_memory()
-    x_h = torch.ones(N, dtype=torch.float64).pin_memory()
+    # ---- end to end through the C ABI with pinned host buffers (B, X0 in; X out)
+    B_h = B_d.cpu().pin_memory()
+    X_h = torch.ones_like(B_h).pin_memory()
 
     def solve_e2e():
-        x_h.fill_(1.0)
-        return op.gmres_ir_device(b_h.data_ptr(), x_h.data_ptr(), max_outer=20, inner_iter=200,
-                                  tol_pow=wl["gtol"], where=hw.HOST)
+        X_h.fill_(1.0)
+        return op.gmres_ir_batch_device(B_h.data_ptr(), X_h.data_ptr(), R, max_outer=20, inner_iter=200,
+                                        tol_pow=gtol, where=hw.HOST)
 
     for _ in range(W):
         solve_e2e()
     ms_e2e, _, _, _ = timed(solve_e2e, K)
 
-    # roofline: profiled repeat of the timed mixed steps; per phase of the
-    # block-row GEMV, algorithmic bytes per launch / mean launch time
+    # ---- roofline: profiled repeat of the timed steps (host-driven loop while
+    # profiling), per precision of the multi-vector kernel
+    peak, peak_kind = load_peaks()
     op.profile(True)
     for _ in range(K):
-        solve_mixed()
+        solve_batched()
     torch.cuda.synchronize()
-    prof = {}
-    for prec, nm in ((hw.PREC_FP32, "fp32"), (hw.PREC_FP64, "fp64")):
-        la, ms, by = op.profile_phases(prec)
-        prof[nm] = (la, ms, by)
+    kern = {}
+    for prec, nm in ((hw.PREC_FP32, "fp32"), (hw.PREC_DF64, "df64"), (hw.PREC_FP64, "fp64")):
+        la, ms, by = op.profile_multi(prec)
+        if la:
+            kern[nm] = dict(launches=la, ms=ms, bytes=by, us=ms / la * 1e3, gbs=by / (ms / la / 1e3) / 1e9)
     op.profile(False)
-    # isolated matvecs per precision: per-phase device time
-    phase_us = {}
-    y_d = torch.empty_like(x_d)
-    for prec, nm in ((hw.PREC_FP32, "fp32"), (hw.PREC_FP64, "fp64")):
-        for _ in range(3):
-            op.matvec_device(xt_d.data_ptr(), y_d.data_ptr(), precision=prec)
-        op.profile(True)
-        for _ in range(20):
-            op.matvec_device(xt_d.data_ptr(), y_d.data_ptr(), precision=prec)
-        torch.cuda.synchronize()
-        la, ms, by = op.profile_phases(prec)
-        op.profile(False)
-        phase_us[nm] = {"us": [round(float(m) / max(int(l), 1) * 1e3, 2) for m, l in zip(ms, la)],
-                        "MB": [round(float(b) / 1e6, 2) for b in by],
-                        "total_us": round(float(ms.sum()) / 20 * 1e3, 1)}
-    peak, peak_kind = load_peaks()
-    # entries 0..P-1: per-phase launches (phased mode); entry P: whole-matvec
-    # cooperative launches (default mode)
-    best = None
-    for nm, (la, ms, by) in prof.items():
-        for q in range(len(la)):
-            if la[q] == 0:
-                continue
-            if best is None or ms[q] > best[2]:
-                best = (nm, q, float(ms[q]), int(la[q]), float(by[q]))
-    nm, q, msq, laq, byq = best
-    whole = q == len(prof[nm][0]) - 1
-    tot_ms = sum(float(p[1].sum()) for p in prof.values())
-    achieved = byq / (msq / laq / 1e3) / 1e9
-    ctype = "float" if nm == "fp32" else "double"
-
-    def per_mv(p):
-        la, ms, by = p
-        n = int(la.max()) if la.size else 0
-        if n == 0:
-            return 0.0, 0.0
-        t = float(ms.sum()) / n
-        b = float(by[-1]) if la[-1] else float((by * (la > 0)).sum())
-        return t, b / (t / 1e3) / 1e9
-    mv32_ms, mv32_gbs = per_mv(prof["fp32"])
-    mv64_ms, mv64_gbs = per_mv(prof["fp64"])
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+    tot = sum(k["ms"] for k in kern.values())
+    top = max(kern, key=lambda k: kern[k]["ms"])
+    tk = kern[top]
+    ctype = {"fp32": "float, FP32", "df64": "double, double-FP32", "fp64": "double, FP64"}[top]
+    rp = 16 if R <= 16 else (32 if R <= 32 else 64)
+    roof = {"bound": "hbm", "achieved": tk["gbs"], "peak": peak, "unit": "GB/s", "frac": tk["gbs"] / peak,
             "traffic": None,
-            "kernel": ("brg_coop_kernel<%s> (one cooperative launch = one whole matvec, %d phases)"
-                       % (ctype, len(prof[nm][0]) - 1)) if whole else
-                      ("brg_kernel<%s> phase %d of %d" % (ctype, q, len(prof[nm][0]) - 1)),
-            "bytes_per_launch": byq, "launch_us": msq / laq * 1e3, "launches": laq,
-            "share_of_gemv_time": msq / tot_ms if tot_ms else None,
-            "peak_kind": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured" else peak_kind}
+            "kernel": "mr_coop_kernel<%s, %d> (one cooperative launch = one %d-vector matvec)" % (ctype, rp, R),
+            "bytes_per_launch": tk["bytes"], "launch_us": tk["us"], "launches": tk["launches"],
+            "share_of_matvec_time": tk["ms"] / tot if tot else None,
+            "peak_kind": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured" else peak_kind,
+            "per_precision": {k: {"launch_us": round(v["us"], 1), "GBs": round(v["gbs"], 1),
+                                  "share": round(v["ms"] / tot, 3)} for k, v in kern.items()}}
 
-    # CPU baseline: the oracle on this host's cores
+    # ---- CPU baseline: the oracle on this host's cores
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         r = cpu_oracle_solves(wl, 1, 0)
@@ -350,27 +373,37 @@ def main():
                "sample": "1 full FP64 GMRES solve to 1e-10 of the same workload (CPU oracle, assembly %.2fs untimed, "
                          "%d iterations, matvec %.1f ms)" % (r["t_asm"], r["iters"], r["t_mv"] * 1e3)}
 
-    value = K * world / (ms_mixed / 1e3)
+    value = K * R * world / (ms_b / 1e3)
+    ms_solve_b = ms_b / K / R
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": ms_mixed / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": ms_b / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*",
-                   "solver": "FP32-operator inner GMRES (FP64 Arnoldi) + FP64 iterative refinement",
+        "config": {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*", "rhs_per_step": R,
+                   "solver": "batched: FP32-operator inner GMRES (FP64 Arnoldi, %d columns in lockstep, one "
+                             "multi-vector matvec per step) + iterative refinement, residuals FP32 at x0 then "
+                             "double-FP32 on the FP64 operator; CUDA-graph Arnoldi loop" % R,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "no flush: FP64 operator %.0f MB, FP32 %.0f MB, both > 129 MB L2" %
                          (op.operator_bytes(hw.PREC_FP64) / 1e6, op.operator_bytes(hw.PREC_FP32) / 1e6)},
-        "e2e": {"value": K * world / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N,
-                "d2h_bytes_per_step": 8 * N},
+        "e2e": {"value": K * R * world / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N * R,
+                "d2h_bytes_per_step": 8 * N * R},
         "gpu_launches": int(launches),
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clocks.summary(*win),
-        "mixed": {"ms_per_solve": ms_mixed / K, "outer": outer, "inner_total": inner, "resid": res_mixed,
-                  "rel_err_vs_xtrue": err_mixed, "fp32_matvec_ms": mv32_ms, "fp32_matvec_gbs": mv32_gbs},
-        "fp64": {"ms_per_solve": ms_fp64 / K, "iters": it64, "resid": res64, "rel_err_vs_xtrue": err_fp64,
-                 "matvec_ms": mv64_ms, "matvec_gbs": mv64_gbs, "speedup_mixed_over_fp64": ms_fp64 / ms_mixed},
-        "assembly_s": t_asm, "storage_entries": storage, "phases": phase_us,
+        "batched_mixed": {"ms_per_step": ms_b / K, "ms_per_solve": ms_solve_b, "outer": outer_b,
+                          "inner_steps_total": inner_b, "max_resid": float(np.max(res_b)),
+                          "max_fp64_resid": fp64_resid_b, "max_rel_err_vs_xtrue": err_b,
+                          "dense_rows_rel_err_col0": dense_rows_err},
+        "batched_fp64": {"ms_per_solve": ms_b64 / K / R, "iters": it_b64, "max_rel_err_vs_xtrue": err_b64},
+        "single_mixed": {"ms_per_solve": ms_mixed / K, "outer": outer, "inner_total": inner, "resid": res_mixed,
+                         "rel_err_vs_xtrue": err_mixed},
+        "single_fp64": {"ms_per_solve": ms_fp64 / K, "iters": it64, "resid": res64, "rel_err_vs_xtrue": err_fp64},
+        "speedup_vs_plain_fp64": {"batched_mixed_over_single_fp64": (ms_fp64 / K) / ms_solve_b,
+                                  "batched_mixed_over_batched_fp64": (ms_b64 / K / R) / ms_solve_b,
+                                  "single_mixed_over_single_fp64": ms_fp64 / ms_mixed},
+        "assembly_s": t_asm, "storage_entries": storage,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

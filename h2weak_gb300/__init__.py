@@ -26,8 +26,9 @@ ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_RANK, ERR_NOT_CONVERGED, ERR_STATE = -1, -2, -
 FORM_NESTED, FORM_SEMINESTED = 0, 1
 KERNEL_IE, KERNEL_RBF = 0, 1
 ASSEMBLE_NCA, ASSEMBLE_IMPORT, ASSEMBLE_LEARNED = 0, 1, 2
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
 HOST, DEVICE = 0, 1
+OPT_GRAPH, OPT_COOP, OPT_IR_RESIDUAL = 0, 1, 2
 LISTS = {"charge": 0, "nbr": 1, "il": 2, "isvertex": 3, "far_check": 4, "far_charge": 5,
          "ver_check": 6, "ver_charge": 7, "sn_row": 8, "sn_col": 9}
 
@@ -88,6 +89,9 @@ def lib():
         "h2w_gmres_ir_batch": [P, P, P, I, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), P],
         "h2w_dense_matvec": [P, P, P, I64, I64, I],
         "h2w_profile": [P, I],
+        "h2w_profile_multi": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(D)],
+        "h2w_set_option": [P, I, I64],
+        "h2w_get_option": [P, I, ctypes.POINTER(I64)],
         "h2w_profile_phases": [P, I, I, P, P, P, ctypes.POINTER(I)],
     }
     for name, args in sig.items():
@@ -205,6 +209,20 @@ class H2Operator:
         return b.value
 
     # instrumentation
+    def set_option(self, option, value):
+        self._ck(lib().h2w_set_option(self.h, option, int(value)))
+
+    def get_option(self, option):
+        v = ctypes.c_int64()
+        self._ck(lib().h2w_get_option(self.h, option, ctypes.byref(v)))
+        return v.value
+
+    def profile_multi(self, precision=PREC_FP32):
+        """(launches, total ms, algorithmic bytes per launch) of the multi-vector kernel."""
+        la, ms, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+        self._ck(lib().h2w_profile_multi(self.h, precision, ctypes.byref(la), ctypes.byref(ms), ctypes.byref(by)))
+        return la.value, ms.value, by.value
+
     def profile(self, enable):
         self._ck(lib().h2w_profile(self.h, 1 if enable else 0))
 

@@ -1,6 +1,7 @@
 // C ABI of the GB300 H2* / (H2+H)* library: handle, tree, GPU assembly,
 // packed-operator plan, matvec launches and device-resident GMRES.
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -34,6 +35,10 @@ struct ApiError : std::runtime_error {
             throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));                    \
     } while (0)
 
+// Bumped by every device (re)allocation: a captured graph holds raw device
+// pointers and is rebuilt when the generation moved.
+std::atomic<uint64_t> g_alloc_gen{0};
+
 template <class T> struct DBuf {
     T *p = nullptr;
     size_t n = 0;
@@ -42,13 +47,17 @@ template <class T> struct DBuf {
     DBuf &operator=(const DBuf &) = delete;
     ~DBuf() { reset(); }
     void reset() {
-        if (p) cudaFree(p);
+        if (p) {
+            cudaFree(p);
+            g_alloc_gen.fetch_add(1);
+        }
         p = nullptr;
         n = 0;
     }
     void alloc(size_t cnt) {
         reset();
         if (cnt == 0) cnt = 1;
+        g_alloc_gen.fetch_add(1);
         cudaError_t e = cudaMalloc(&p, cnt * sizeof(T));
         if (e != cudaSuccess) {
             p = nullptr;
@@ -102,7 +111,7 @@ struct h2w_handle {
     std::vector<int64_t> ph_op, ph_vec;   // per phase: operator and vector elements moved
     // launch profiling of the block-row GEMV (events bracket every phase launch)
     bool prof = false;
-    struct ProfRec { cudaEvent_t a, b; int prec, phase; };
+    struct ProfRec { cudaEvent_t a, b; int prec, phase; int rp = 1; };  // prec + 2: multi-vector launch
     std::vector<ProfRec> prof_recs;
     std::vector<cudaEvent_t> ev_pool;
     bool fused_scatter = true;
@@ -113,6 +122,7 @@ struct h2w_handle {
     DBuf<double> g_V, g_w, g_vcur, g_H, g_cs, g_sn, g_s, g_part, g_scal, g_tmp, g_b, g_r, g_npart;
     DBuf<int32_t> g_iter;
     int g_m = -1;
+    DBuf<double> s_b, s_x, s_r, s_d;   // solver vectors in leaf order (kept between calls)
     // multiple right-hand sides: interleaved workspaces (ws_n x rp), staging, batched GMRES
     DBuf<double> m_wsd, m_xi, m_yi, m_ri, m_di, m_bi, m_stage_x, m_stage_y, m_onorm, m_ores;
     DBuf<float> m_wsf, m_xf;
@@ -120,6 +130,18 @@ struct h2w_handle {
     DBuf<double> gb_V, gb_w, gb_vcur, gb_H, gb_cs, gb_sn, gb_s, gb_part, gb_hsum, gb_normb, gb_resid, gb_y;
     DBuf<int32_t> gb_conv, gb_iter;
     int gb_m = -1, gb_rp = 0;
+    // graph-captured Arnoldi loops (a while node whose body is one step)
+    struct LoopGraph {
+        int kind, prec, m, rp, nrhs;
+        double tol;
+        uint64_t gen;
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+        int64_t kernels_per_step;
+    };
+    std::vector<LoopGraph> loops;
+    bool use_graphs = true, graph_failed = false;
+    int ir_resid_prec = H2W_PREC_FP64;   // refinement residuals after the first (batched IR)
     cudaStream_t stream = nullptr;
 
     KParams kparams() const {
@@ -1238,6 +1260,8 @@ void build_plan(h2w_handle *h) {
     {
         const char *m = getenv("H2W_MATVEC");
         h->coop = !(m && std::string(m) == "phased");
+        const char *g = getenv("H2W_GRAPH");
+        if (g && std::string(g) == "0") h->use_graphs = false;
     }
     CK(cudaStreamSynchronize(st));
     h->d_op32.reset();
@@ -1405,11 +1429,92 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     }
 }
 
+// ------------------------------------------------------- captured loops ---
+// The Arnoldi step as the body of a conditional while node: body(s, cond)
+// enqueues one step on s and ends with the kernel that sets cond. Cached per
+// (kind, precision, m, rp, nrhs, tol) and rebuilt when any device buffer was
+// reallocated since the capture. Returns nullptr when capture is unavailable
+// (the caller then runs the host loop). kps: kernels one step launches.
+template <class F>
+cudaGraphExec_t loop_graph(h2w_handle *h, int kind, int prec, int m, int rp, int nrhs, double tol, int64_t &kps,
+                           F &&body) {
+    if (!h->use_graphs || h->graph_failed || h->prof) return nullptr;
+    const uint64_t gen = g_alloc_gen.load();
+    for (size_t i = 0; i < h->loops.size(); ++i) {
+        h2w_handle::LoopGraph &L = h->loops[i];
+        if (L.kind == kind && L.prec == prec && L.m == m && L.rp == rp && L.nrhs == nrhs && L.tol == tol) {
+            if (L.gen == gen) {
+                kps = L.kernels_per_step;
+                return L.exec;
+            }
+            cudaGraphExecDestroy(L.exec);
+            cudaGraphDestroy(L.graph);
+            h->loops.erase(h->loops.begin() + (long)i);
+            break;
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int64_t c0 = launch_count();
+    bool capturing = false;
+    try {
+        CK(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle cond;
+        CK(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
+        // zero-initialised storage (the struct's union has no default constructor in C++)
+        alignas(cudaGraphNodeParams) unsigned char npbuf[sizeof(cudaGraphNodeParams)] = {};
+        cudaGraphNodeParams *np = reinterpret_cast<cudaGraphNodeParams *>(npbuf);
+        np->type = cudaGraphNodeTypeConditional;
+        np->conditional.handle = cond;
+        np->conditional.type = cudaGraphCondTypeWhile;
+        np->conditional.size = 1;
+        cudaGraphNode_t node;
+        CK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, np));
+        cudaGraph_t bodyg = np->conditional.phGraph_out[0];
+        CK(cudaStreamBeginCaptureToGraph(h->stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        capturing = true;
+        body(h->stream, cond);
+        cudaGraph_t out = nullptr;
+        capturing = false;
+        CK(cudaStreamEndCapture(h->stream, &out));
+        CK(cudaGraphInstantiate(&exec, graph, 0));
+    } catch (const std::exception &) {
+        if (capturing) {
+            cudaGraph_t out = nullptr;
+            cudaStreamEndCapture(h->stream, &out);
+        }
+        cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        count_launch(c0 - launch_count());
+        h->graph_failed = true;
+        return nullptr;
+    }
+    kps = launch_count() - c0;
+    count_launch(-kps);  // the captured launches run when the graph does
+    h->loops.push_back({kind, prec, m, rp, nrhs, tol, gen, graph, exec, kps});
+    return exec;
+}
+
 // ----------------------------------------------- multiple right-hand sides ---
 // Interleaved block width for nrhs columns (the multi-vector kernel is
 // compiled for 16, 32 and 64).
 int rp_for(int nrhs) { return nrhs <= 16 ? 16 : (nrhs <= 32 ? 32 : 64); }
 constexpr int MR_MAX = 64;
+
+// A multi-vector launch, bracketed by events while profiling is on.
+template <class F>
+void mr_prof(h2w_handle *h, int prec, int rp, cudaStream_t st, F &&launch) {
+    if (!h->prof) {
+        CK(launch());
+        return;
+    }
+    h2w_handle::ProfRec r{prof_event(h), prof_event(h), prec + 2, (int)h->mphases.size(), rp};
+    CK(cudaEventRecord(r.a, st));
+    CK(launch());
+    CK(cudaEventRecord(r.b, st));
+    h->prof_recs.push_back(r);
+}
 
 // Y = A X for an interleaved leaf-order block of rp vectors (xi, yi: N x rp).
 void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double *yi, cudaStream_t st) {
@@ -1426,14 +1531,21 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
         const size_t nx = (size_t)h->tree.N * (size_t)rp;
         if (h->m_xf.n < nx) h->m_xf.alloc(nx);
         CK(vec_f64_to_f32(xi, h->m_xf.p, (int64_t)nx, st));
-        CK(launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op32.p, h->m_wsf.p, h->m_xf.p, yi,
-                         h->d_bar.p, h->d_err.p, st));
+        mr_prof(h, prec, rp, st, [&] {
+            return launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op32.p,
+                                 h->m_wsf.p, h->m_xf.p, yi, h->d_bar.p, h->d_err.p, st);
+        });
         if (!h->fused_scatter) CK(launch_mr_widen_f32(h->m_wsf.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
     } else {
         if (h->m_wsd.n < wsz) h->m_wsd.alloc(wsz);
         CK(cudaMemsetAsync(h->m_wsd.p, 0, wsz * 8, st));
-        CK(launch_mr_f64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op.p, h->m_wsd.p, xi, yi,
-                         h->d_bar.p, h->d_err.p, st));
+        mr_prof(h, prec, rp, st, [&] {
+            if (prec == H2W_PREC_DF64)
+                return launch_mr_df64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op.p,
+                                      h->m_wsd.p, xi, yi, h->d_bar.p, h->d_err.p, st);
+            return launch_mr_f64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op.p,
+                                 h->m_wsd.p, xi, yi, h->d_bar.p, h->d_err.p, st);
+        });
         if (!h->fused_scatter) CK(launch_mr_widen_f64(h->m_wsd.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
     }
 }
@@ -1461,7 +1573,7 @@ GmresBatch gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
         h->gb_resid.alloc((size_t)rp);
         h->gb_y.alloc((size_t)(m + 1) * rp);
         h->gb_conv.alloc((size_t)rp);
-        h->gb_iter.alloc(1);
+        h->gb_iter.alloc(2);
         h->gb_m = m;
         h->gb_rp = rp;
     }
@@ -1514,7 +1626,28 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
     };
     bool done = read_conv();
     int last = -1;
-    for (int i = 0; i < max_iter && !done; ++i) {
+    bool looped = false;
+    if (!done && h->use_graphs && !h->graph_failed && !h->prof) {
+        // graph path: the batched Arnoldi steps as one while-loop graph launch
+        if (!gmb_attr(g)) throw ApiError(H2W_ERR_ARG, "batched GMRES: Krylov dimension too large for shared memory");
+        run_matvec_multi(h, prec, rp, g.vcur, g.w, st);  // one-time set-up outside the capture
+        int64_t kps = 0;
+        cudaGraphExec_t ex = loop_graph(h, 1, prec, max_iter, rp, nrhs, tol, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
+            run_matvec_multi(h, prec, rp, g.vcur, g.w, s);
+            CK(gmb_arnoldi(g, tol, s));
+            CK(gmb_loop(g, c, s));
+        });
+        if (ex) {
+            CK(cudaGraphLaunch(ex, st));
+            int32_t it2[2];
+            CK(cudaMemcpyAsync(it2, g.iter, 8, cudaMemcpyDeviceToHost, st));
+            read_conv();
+            count_launch(kps * it2[1]);
+            last = it2[1] - 1;
+            looped = true;
+        }
+    }
+    for (int i = 0; i < max_iter && !done && !looped; ++i) {
         run_matvec_multi(h, prec, rp, g.vcur, g.w, st);
         CK(gmb_arnoldi(g, tol, st));
         last = i;
@@ -1553,7 +1686,7 @@ GmresDev gmres_state(h2w_handle *h, int m) {
         h->g_s.alloc((size_t)m + 1);
         h->g_part.alloc((size_t)3 * nblk * (size_t)(m + 1));
         h->g_scal.alloc(8);
-        h->g_iter.alloc(1);
+        h->g_iter.alloc(2);
         h->g_tmp.alloc((size_t)N);
         h->g_r.alloc((size_t)N);
         h->g_m = m;
@@ -1603,11 +1736,25 @@ void gmres_xupdate(h2w_handle *h, const GmresDev &g, double *dx, int k) {
     CK(gmres_update(g, dx, h->g_tmp.p, k, h->stream));
 }
 
+// All max_iter steps taken without meeting the tolerance: x += V y over all
+// columns, then the true relative residual.
+int gmres_unconverged(h2w_handle *h, const GmresDev &g, const double *db, double *dx, int max_iter, double tol,
+                      int prec, double normb, int *iters, double *resid) {
+    cudaStream_t st = h->stream;
+    gmres_xupdate(h, g, dx, max_iter - 1);
+    if (prec == H2W_PREC_FP32) run_matvec_f32(h, dx, h->g_r.p, st, true);
+    else run_matvec_f64(h, dx, h->g_r.p, st, true);
+    CK(vec_axpby(1.0, db, -1.0, h->g_r.p, h->g_r.p, h->tree.N, st));
+    *resid = dnorm(h, h->g_r.p) / normb;
+    *iters = max_iter;
+    return *resid < tol ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+}
+
 // FP64 GMRES on device vectors in leaf order (the operator is applied as
 // P A P^T, which leaves GMRES unchanged up to rounding); matvec precision
 // chosen by prec.
 int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double tol, int prec, int *iters,
-              double *resid) {
+              double *resid, bool x0_zero = false) {
     GmresDev g = gmres_state(h, max_iter);
     cudaStream_t st = h->stream;
     const int64_t N = h->tree.N;
@@ -1617,8 +1764,12 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     };
     double normb = dnorm(h, db);
     if (normb == 0.0) normb = 1;
-    A(dx, h->g_r.p);
-    CK(gmres_start(g, db, h->g_r.p, normb, st));
+    if (x0_zero) {
+        CK(gmres_start(g, db, nullptr, normb, st));
+    } else {
+        A(dx, h->g_r.p);
+        CK(gmres_start(g, db, h->g_r.p, normb, st));
+    }
     double sc[4];
     CK(cudaMemcpyAsync(sc, g.scal, 32, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1626,6 +1777,36 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     if (sc[1] <= tol) {
         *iters = 0;
         return H2W_OK;
+    }
+    // graph path: the Arnoldi steps as one while-loop graph launch
+    if (h->use_graphs && !h->graph_failed && !h->prof) {
+        if (prec == H2W_PREC_FP32) ensure_f32(h);
+        gmres_prepare();
+        A(g.vcur, g.w);  // one-time launch set-up outside the capture; the step recomputes w
+        int64_t kps = 0;
+        cudaGraphExec_t ex = loop_graph(h, 0, prec, max_iter, 1, 1, tol, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
+            if (prec == H2W_PREC_FP32) run_matvec_f32(h, g.vcur, g.w, s, true);
+            else run_matvec_f64(h, g.vcur, g.w, s, true);
+            CK(gmres_cgs2(g, s));
+            CK(gmres_finish_iter(g, tol, s));
+            CK(gmres_loop_cond(g, c, s));
+        });
+        if (ex) {
+            CK(cudaGraphLaunch(ex, st));
+            int32_t it2[2];
+            CK(cudaMemcpyAsync(sc, g.scal, 32, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(it2, g.iter, 8, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            count_launch(kps * it2[1]);
+            *resid = sc[1];
+            if (sc[2] != 0.0) {
+                gmres_xupdate(h, g, dx, it2[0]);
+                CK(cudaStreamSynchronize(st));
+                *iters = it2[1];
+                return H2W_OK;
+            }
+            return gmres_unconverged(h, g, db, dx, max_iter, tol, prec, normb, iters, resid);
+        }
     }
     for (int i = 0; i < max_iter; ++i) {
         A(g.vcur, g.w);
@@ -1641,12 +1822,7 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
             return H2W_OK;
         }
     }
-    gmres_xupdate(h, g, dx, max_iter - 1);
-    A(dx, h->g_r.p);
-    CK(vec_axpby(1.0, db, -1.0, h->g_r.p, h->g_r.p, N, st));
-    *resid = dnorm(h, h->g_r.p) / normb;
-    *iters = max_iter;
-    return *resid < tol ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+    return gmres_unconverged(h, g, db, dx, max_iter, tol, prec, normb, iters, resid);
 }
 
 // Device-side failure flag of the cooperative matvec (a grid barrier whose
@@ -1823,6 +1999,10 @@ int h2w_destroy(h2w_handle *h) {
         cudaEventDestroy(r.b);
     }
     for (auto e : h->ev_pool) cudaEventDestroy(e);
+    for (auto &g : h->loops) {
+        cudaGraphExecDestroy(g.exec);
+        cudaGraphDestroy(g.graph);
+    }
     cudaStream_t st = h->stream;
     delete h;
     if (st) cudaStreamDestroy(st);
@@ -2123,7 +2303,9 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
         if (!x || !y || nrhs < 1 || (where != H2W_HOST && where != H2W_DEVICE)) throw ApiError(H2W_ERR_ARG, "bad matvec arguments");
         cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
         const int64_t N = h->tree.N;
-        if (nrhs > 1) {
+        if (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32 && precision != H2W_PREC_DF64)
+            throw ApiError(H2W_ERR_ARG, "unknown precision");
+        if (nrhs > 1 || precision == H2W_PREC_DF64) {
             // blocks of up to 64 columns through the multi-vector kernel
             ensure_multi_vectors(h);
             if (where == H2W_HOST) {
@@ -2139,8 +2321,7 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
                     xc = h->m_stage_x.p;
                 }
                 CK(launch_mr_pack(xc, N, h->m_xi.p, h->d_perm.p, N, nc, rp, st));
-                run_matvec_multi(h, precision == H2W_PREC_FP32 ? H2W_PREC_FP32 : H2W_PREC_FP64, rp, h->m_xi.p,
-                                 h->m_yi.p, st);
+                run_matvec_multi(h, precision, rp, h->m_xi.p, h->m_yi.p, st);
                 CK(launch_mr_unpack(h->m_yi.p, where == H2W_HOST ? h->m_stage_y.p : yc, N, h->d_perm.p, N, nc, rp,
                                     st));
                 if (where == H2W_HOST)
@@ -2196,9 +2377,9 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
             db = h->g_b.p;
             dx = h->d_x.p;
         }
-        DBuf<double> bp, xp;
-        bp.alloc((size_t)N);
-        xp.alloc((size_t)N);
+        DBuf<double> &bp = h->s_b, &xp = h->s_x;
+        if (bp.n < (size_t)N) bp.alloc((size_t)N);
+        if (xp.n < (size_t)N) xp.alloc((size_t)N);
         CK(launch_gather_f64(db, bp.p, h->d_perm.p, N, h->stream));
         CK(launch_gather_f64(dx, xp.p, h->d_perm.p, N, h->stream));
         int rc = gmres_run(h, bp.p, xp.p, max_iter, tol, H2W_PREC_FP64, iters, resid);
@@ -2234,11 +2415,9 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         }
         GmresDev g = gmres_state(h, inner_iter);
         (void)g;
-        DBuf<double> r, d, bp, xp;
-        r.alloc((size_t)N);
-        d.alloc((size_t)N);
-        bp.alloc((size_t)N);
-        xp.alloc((size_t)N);
+        DBuf<double> &r = h->s_r, &d = h->s_d, &bp = h->s_b, &xp = h->s_x;
+        for (DBuf<double> *v : {&r, &d, &bp, &xp})
+            if (v->n < (size_t)N) v->alloc((size_t)N);
         CK(launch_gather_f64(db, bp.p, h->d_perm.p, N, st));
         CK(launch_gather_f64(dx, xp.p, h->d_perm.p, N, st));
         const double *db_user = db;
@@ -2251,16 +2430,20 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         *outer_iters = 0;
         int rc = H2W_ERR_NOT_CONVERGED;
         for (int o = 0; o <= max_outer; ++o) {
-            run_matvec_f64(h, dx, r.p, st, true);
+            // residual: FP32 operator at x0 (a correction only), then FP64 (the stopping test)
+            if (o == 0) run_matvec_f32(h, dx, r.p, st, true);
+            else run_matvec_f64(h, dx, r.p, st, true);
             CK(vec_axpby(1.0, db, -1.0, r.p, r.p, N, st));
-            *resid = dnorm(h, r.p) / normb;
-            if (*resid < tol) { rc = H2W_OK; break; }
-            if (o == max_outer) break;
+            if (o > 0) {
+                *resid = dnorm(h, r.p) / normb;
+                if (*resid < tol) { rc = H2W_OK; break; }
+                if (o == max_outer) break;
+            }
             CK(cudaMemsetAsync(d.p, 0, (size_t)N * 8, st));
             int it = 0;
             double ires = 0;
             // inner: relative reduction 1e-6 of the current residual, FP32 operator
-            gmres_run(h, r.p, d.p, inner_iter, 1e-6, H2W_PREC_FP32, &it, &ires);
+            gmres_run(h, r.p, d.p, inner_iter, 1e-6, H2W_PREC_FP32, &it, &ires, true);
             *inner_total += it;
             CK(vec_axpby(1.0, dx, 1.0, d.p, dx, N, st));
             *outer_iters = o + 1;
@@ -2320,18 +2503,21 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
             std::vector<double> ir((size_t)rp);
             bool ok = false;
             for (int o = 0; o <= max_outer; ++o) {
-                // FP64 residual r = b - A x
-                run_matvec_multi(h, H2W_PREC_FP64, rp, xi, h->m_ri.p, st);
+                // residual r = b - A x: FP32 operator at x0 (a correction only), then
+                // FP64 (or double-FP32) products, which are the stopping test
+                run_matvec_multi(h, o == 0 ? H2W_PREC_FP32 : h->ir_resid_prec, rp, xi, h->m_ri.p, st);
                 CK(vec_axpby(1.0, bi, -1.0, h->m_ri.p, h->m_ri.p, (int64_t)len, st));
-                CK(gmb_norms(g, h->m_ri.p, h->m_ores.p, 0, st));
-                CK(cudaMemcpyAsync(nr.data(), h->m_ores.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
-                CK(cudaStreamSynchronize(st));
-                ok = true;
-                for (int c = 0; c < nc; ++c) {
-                    resid[c0 + c] = nr[(size_t)c] / nb[(size_t)c];
-                    if (!(resid[c0 + c] < tol)) ok = false;
+                if (o > 0) {
+                    CK(gmb_norms(g, h->m_ri.p, h->m_ores.p, 0, st));
+                    CK(cudaMemcpyAsync(nr.data(), h->m_ores.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
+                    CK(cudaStreamSynchronize(st));
+                    ok = true;
+                    for (int c = 0; c < nc; ++c) {
+                        resid[c0 + c] = nr[(size_t)c] / nb[(size_t)c];
+                        if (!(resid[c0 + c] < tol)) ok = false;
+                    }
+                    if (ok || o == max_outer) break;
                 }
-                if (ok || o == max_outer) break;
                 // FP32-operator inner GMRES on A d = r from d = 0, relative tolerance 1e-6
                 CK(cudaMemsetAsync(h->m_di.p, 0, len * 8, st));
                 gmres_batch_run(h, h->m_ri.p, h->m_di.p, rp, nc, inner_iter, 1e-6, H2W_PREC_FP32, true, it.data(),
@@ -2345,6 +2531,40 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
             if (!ok) rc = H2W_ERR_NOT_CONVERGED;
         });
         return rc;
+    });
+}
+
+int h2w_set_option(h2w_handle *h, int option, int64_t value) {
+    return guarded(h, [&] {
+        if (option == H2W_OPT_GRAPH) {
+            h->use_graphs = value != 0;
+            h->graph_failed = false;
+        } else if (option == H2W_OPT_IR_RESIDUAL) {
+            if (value != H2W_PREC_FP64 && value != H2W_PREC_DF64)
+                throw ApiError(H2W_ERR_ARG, "IR residual precision must be FP64 or DF64");
+            h->ir_resid_prec = (int)value;
+        } else if (option == H2W_OPT_COOP) {
+            h->coop = value != 0;
+            for (auto &g : h->loops) {  // captured steps hold the other launch form
+                cudaGraphExecDestroy(g.exec);
+                cudaGraphDestroy(g.graph);
+            }
+            h->loops.clear();
+        } else {
+            throw ApiError(H2W_ERR_ARG, "unknown option");
+        }
+        return H2W_OK;
+    });
+}
+
+int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
+    return guarded(h, [&] {
+        if (!value) throw ApiError(H2W_ERR_ARG, "null value");
+        if (option == H2W_OPT_GRAPH) *value = (h->use_graphs && !h->graph_failed) ? 1 : 0;
+        else if (option == H2W_OPT_COOP) *value = h->coop ? 1 : 0;
+        else if (option == H2W_OPT_IR_RESIDUAL) *value = h->ir_resid_prec;
+        else throw ApiError(H2W_ERR_ARG, "unknown option");
+        return H2W_OK;
     });
 }
 
@@ -2388,6 +2608,29 @@ int h2w_profile_phases(h2w_handle *h, int precision, int max_phases, int64_t *la
             launches[r.phase] += 1;
             ms[r.phase] += (double)t;
         }
+        return H2W_OK;
+    });
+}
+
+int h2w_profile_multi(h2w_handle *h, int precision, int64_t *launches, double *ms, double *bytes) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!launches || !ms || !bytes) throw ApiError(H2W_ERR_ARG, "null output");
+        CK(cudaDeviceSynchronize());
+        const double w = precision == H2W_PREC_FP32 ? 4.0 : 8.0;
+        *launches = 0;
+        *ms = 0.0;
+        double by = 0.0;
+        for (auto &r : h->prof_recs) {
+            if (r.prec != precision + 2) continue;
+            float t = 0.f;
+            CK(cudaEventElapsedTime(&t, r.a, r.b));
+            *launches += 1;
+            *ms += (double)t;
+            // operator once, the input block once (kernel precision), the FP64 result block once
+            by += (double)h->op_bytes_read * w + (double)h->tree.N * r.rp * (w + 8.0);
+        }
+        *bytes = *launches ? by / (double)*launches : 0.0;
         return H2W_OK;
     });
 }

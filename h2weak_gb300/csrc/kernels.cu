@@ -927,16 +927,22 @@ __global__ void gm_givens(GmresDev g, double tol) {
     else if (i + 1 < g.m) *g.iter = i + 1;
 }
 
-cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st) {
-    const int nw = GM_THREADS / 32;
-    size_t sm_dots = (size_t)(g.m + 1) * nw * sizeof(double);
-    size_t sm_upd = (size_t)(g.m + 1) * (nw + 1) * sizeof(double);
+// One-time function attributes of the Arnoldi kernels (done before any
+// stream capture of an Arnoldi step).
+void gmres_prepare() {
     static bool cfg = false;
     if (!cfg) {
         cudaFuncSetAttribute(gm_dots, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(gm_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cfg = true;
     }
+}
+
+cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st) {
+    const int nw = GM_THREADS / 32;
+    size_t sm_dots = (size_t)(g.m + 1) * nw * sizeof(double);
+    size_t sm_upd = (size_t)(g.m + 1) * (nw + 1) * sizeof(double);
+    gmres_prepare();
     gm_dots<<<g.nblk, GM_THREADS, sm_dots, st>>>(g);
     gm_update<<<g.nblk, GM_THREADS, sm_upd, st>>>(g, 0);
     gm_update<<<g.nblk, GM_THREADS, sm_upd, st>>>(g, 1);
@@ -949,14 +955,14 @@ cudaError_t gmres_finish_iter(const GmresDev &g, double tol, cudaStream_t st) {
     count_launch(2); return cudaGetLastError();
 }
 
-// r = b - Ax; beta = ||r||; V[:,0] = vcur = r / beta; s = beta e1; iter = 0
+// r = b - Ax (Ax NULL: r = b); beta = ||r||; V[:,0] = vcur = r / beta; s = beta e1; iter = 0
 __global__ void gm_resid_part(GmresDev g, const double *__restrict__ b, const double *__restrict__ Ax) {
     __shared__ double sh[32];
     int64_t r0, r1;
     gm_rows(g.N, g.nblk, r0, r1);
     double acc = 0.0;
     for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
-        double r = b[t] - Ax[t];
+        double r = Ax ? b[t] - Ax[t] : b[t];  // Ax == NULL: x0 = 0
         g.w[t] = r;
         acc += r * r;
     }
@@ -976,7 +982,8 @@ __global__ void gm_start_fin(GmresDev g, double normb) {
             g.scal[1] = beta / normb;
             g.scal[2] = 0.0;
             g.scal[3] = beta;
-            *g.iter = 0;
+            g.iter[0] = 0;
+            g.iter[1] = 0;  // Arnoldi steps taken (graph loop counter)
         }
     }
     __syncthreads();
@@ -989,6 +996,18 @@ __global__ void gm_start_fin(GmresDev g, double normb) {
         g.vcur[t] = v;
     }
 }
+// Loop condition of the graph-captured Arnoldi step: run another step while
+// not converged and fewer than m steps were taken.
+__global__ void gm_loop_cond(GmresDev g, cudaGraphConditionalHandle hnd) {
+    const int c = ++g.iter[1];
+    cudaGraphSetConditional(hnd, (g.scal[2] == 0.0 && c < g.m) ? 1u : 0u);
+}
+cudaError_t gmres_loop_cond(const GmresDev &g, cudaGraphConditionalHandle hnd, cudaStream_t st) {
+    gm_loop_cond<<<1, 1, 0, st>>>(g, hnd);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t gmres_start(const GmresDev &g, const double *b, const double *Ax, double normb, cudaStream_t st) {
     gm_resid_part<<<g.nblk, GM_THREADS, 0, st>>>(g, b, Ax);
     gm_start_fin<<<g.nblk, GM_THREADS, 0, st>>>(g, normb);

@@ -73,14 +73,17 @@ struct GmresDev {
     double *V, *w, *vcur, *H, *cs, *sn, *s;  // V: N x (m+1); H: (m+1) x m column-major
     double *part;                             // 3 * nblk * (m+1) partial sums
     double *scal;                             // [0] ||b||, [1] resid, [2] converged flag, [3] beta
-    int32_t *iter;                                          // current Arnoldi column i
+    int32_t *iter;                            // [0] current Arnoldi column i, [1] steps taken
     int64_t N;
     int m, nblk;
 };
+void gmres_prepare();                                             // one-time kernel attributes
 cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st);      // orthogonalise w against V[:, 0..i], H column
 cudaError_t gmres_finish_iter(const GmresDev &g, double tol, cudaStream_t st);  // normalise, Givens, residual
 cudaError_t gmres_start(const GmresDev &g, const double *b, const double *Ax, double normb, cudaStream_t st);
 cudaError_t gmres_update(const GmresDev &g, double *x, const double *y, int k, cudaStream_t st);
+// last node of a graph-captured Arnoldi step: sets the while-loop condition
+cudaError_t gmres_loop_cond(const GmresDev &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
 cudaError_t vec_norm(const double *x, int64_t n, double *part, int nblk, double *out, cudaStream_t st);
 cudaError_t vec_axpby(double a, const double *x, double b, const double *y, double *z, int64_t n, cudaStream_t st);
 cudaError_t vec_f64_to_f32(const double *x, float *y, int64_t n, cudaStream_t st);
@@ -99,6 +102,12 @@ cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, cons
 cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                           const MrPhases *phased, const float *A, float *ws, const float *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st);
+// FP64 operator and vectors, double-FP32 arithmetic on the FP32 pipes
+// (each product and sum carried as an FP32 pair; about 2^-44 relative per
+// term instead of FP64's 2^-53, at the FP32 pipes' rate).
+cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                           const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                           unsigned *bar, int32_t *err, cudaStream_t st);
 cudaError_t launch_mr_pack(const double *x, int64_t ldx, double *xi, const int32_t *perm, int64_t n, int nrhs,
                            int rp, cudaStream_t st);
 cudaError_t launch_mr_unpack(const double *yi, double *y, int64_t ldy, const int32_t *perm, int64_t n, int nrhs,
@@ -117,13 +126,15 @@ struct GmresBatch {
     double *normb, *resid;   // rp
     double *y;               // (m+1) x rp back-substituted coefficients
     int32_t *conv;           // rp: -1 running, k >= 0 converged at Arnoldi column k, -2 at the start, -3 padding
-    int32_t *iter;           // current Arnoldi column
+    int32_t *iter;           // [0] current Arnoldi column, [1] steps taken
     int64_t N;
     int m, rp, nrhs, nblk;
 };
 cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
 cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st);
+bool gmb_attr(const GmresBatch &g);   // one-time kernel attributes for Krylov dimension g.m
 cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st);
+cudaError_t gmb_loop(const GmresBatch &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
 cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st);
 
 }  // namespace h2w

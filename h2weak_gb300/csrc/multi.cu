@@ -66,9 +66,38 @@ __device__ __forceinline__ void mr_get4(float *o, const float *p) {
     o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
 }
 
+// Double-FP32 ("df64") arithmetic for an FP64-accurate product on the FP32
+// pipes: a double a is carried as hi = fl32(a), lo = fl32(a - hi) (2^-48
+// relative), a product a*x as p = hi_a*hi_x plus its exact FMA error and the
+// two cross terms, and a sum as an unevaluated pair (sh, sl) advanced by
+// Knuth's TwoSum, so every rounding of the FP32 sum is kept in sl. All
+// operations are explicitly rounded (no contraction may merge them).
+__device__ __forceinline__ float2 df_split(double a) {
+    const float h = __double2float_rn(a);
+    return make_float2(h, __double2float_rn(__dsub_rn(a, (double)h)));
+}
+__device__ __forceinline__ void df_fma(float &sh, float &sl, const float2 a, const float2 x) {
+    const float p = __fmul_rn(a.x, x.x);
+    float e = __fmaf_rn(a.x, x.x, -p);
+    e = __fmaf_rn(a.x, x.y, e);
+    e = __fmaf_rn(a.y, x.x, e);
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(t, e));
+}
+__device__ __forceinline__ void df_get4(float2 *o, const float2 *p) {
+    const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+    o[0] = make_float2(a.x, a.y); o[1] = make_float2(a.z, a.w);
+    o[2] = make_float2(b.x, b.y); o[3] = make_float2(b.z, b.w);
+}
+
 // One target of the packed record stream (record layout as the
-// single-vector GEMV: header, panels, segments).
-template <class T, int RP>
+// single-vector GEMV: header, panels, segments). DF (with T = double): the
+// FP64 operand tiles are split into FP32 pairs when staged and multiplied
+// with double-FP32 arithmetic.
+template <class T, int RP, bool DF = false>
 __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *__restrict__ roff,
                                           const int64_t *__restrict__ blob, const T *__restrict__ A, T *ws,
                                           const T *__restrict__ xin, double *yout) {
@@ -144,21 +173,38 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
             const int v = tid + NT * u;
-            *reinterpret_cast<V *>(As + (v / (MR_MT / VN)) * MR_MT + (v % (MR_MT / VN)) * VN) = ra[u];
+            T *d = As + (v / (MR_MT / VN)) * MR_MT + (v % (MR_MT / VN)) * VN;
+            if constexpr (DF) {
+                const float2 h0 = df_split(ra[u].x), h1 = df_split(ra[u].y);
+                *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
+            } else {
+                *reinterpret_cast<V *>(d) = ra[u];
+            }
         }
 #pragma unroll
         for (int u = 0; u < NX; ++u) {
             const int v = tid + NT * u;
-            *reinterpret_cast<V *>(Xs + (v / (RP / VN)) * RP + (v % (RP / VN)) * VN) = rx[u];
+            T *d = Xs + (v / (RP / VN)) * RP + (v % (RP / VN)) * VN;
+            if constexpr (DF) {
+                const float2 h0 = df_split(rx[u].x), h1 = df_split(rx[u].y);
+                *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
+            } else {
+                *reinterpret_cast<V *>(d) = rx[u];
+            }
         }
     };
 
     for (int rt0 = 0; rt0 < nrows; rt0 += MR_MT) {
         T acc[4][4];
+        float ah[4][4], al[4][4];  // DF: (hi, lo) pairs
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+            for (int j = 0; j < 4; ++j) {
+                acc[i][j] = T(0);
+                ah[i][j] = 0.f;
+                al[i][j] = 0.f;
+            }
         int q = 0, c0 = 0;
         if (np > 0) load(0, 0, rt0);
         while (q < np) {
@@ -167,15 +213,28 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
             int nq = q, nc0 = c0 + MR_KC;
             if (nc0 >= (int)(pan[3 * q + 1] >> 32)) { nq = q + 1; nc0 = 0; }
             if (nq < np) load(nq, nc0, rt0);
+            if constexpr (DF) {
+#pragma unroll 4
+                for (int k = 0; k < MR_KC; ++k) {
+                    float2 a4[4], x4[4];
+                    df_get4(a4, reinterpret_cast<const float2 *>(As) + k * MR_MT + ty * 4);
+                    df_get4(x4, reinterpret_cast<const float2 *>(Xs) + k * RP + tx * 4);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) df_fma(ah[i][j], al[i][j], a4[i], x4[j]);
+                }
+            } else {
 #pragma unroll 8
-            for (int k = 0; k < MR_KC; ++k) {
-                T a4[4], x4[4];
-                mr_get4(a4, As + k * MR_MT + ty * 4);
-                mr_get4(x4, Xs + k * RP + tx * 4);
+                for (int k = 0; k < MR_KC; ++k) {
+                    T a4[4], x4[4];
+                    mr_get4(a4, As + k * MR_MT + ty * 4);
+                    mr_get4(x4, Xs + k * RP + tx * 4);
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
+                    for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] += a4[i] * x4[j];
+                        for (int j = 0; j < 4; ++j) acc[i][j] += a4[i] * x4[j];
+                }
             }
             __syncthreads();
             q = nq;
@@ -188,7 +247,9 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
             const int64_t d = (dst + r) * RP + tx * 4;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const T v = acc[i][j];
+                T v;
+                if constexpr (DF) v = (T)((double)ah[i][j] + (double)al[i][j]);
+                else v = acc[i][j];
                 if (flags & T_SCATTER) yout[d + j] = (double)((flags & T_ACCUM) ? ws[d + j] + v : v);
                 else if (flags & T_ATOMIC) atomicAdd(ws + d + j, v);
                 else if (flags & T_ACCUM) ws[d + j] += v;
@@ -199,15 +260,16 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
     __syncthreads();
 }
 
-template <class T, int RP>
+template <class T, int RP, bool DF>
 __global__ void __launch_bounds__(4 * RP)
     mr_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
               const T *__restrict__ A, T *ws, const T *__restrict__ xin, double *yout) {
     extern __shared__ __align__(16) char mr_smem[];
-    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x) mr_target<T, RP>(mr_smem, t, roff, blob, A, ws, xin, yout);
+    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x)
+        mr_target<T, RP, DF>(mr_smem, t, roff, blob, A, ws, xin, yout);
 }
 
-template <class T, int RP>
+template <class T, int RP, bool DF>
 __global__ void __launch_bounds__(4 * RP)
     mr_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
                    const int64_t *__restrict__ pstart, int nphase, const T *__restrict__ A, T *ws,
@@ -216,7 +278,7 @@ __global__ void __launch_bounds__(4 * RP)
     for (int p = 0; p < nphase; ++p) {
         const int64_t t1 = pstart[p + 1];
         for (int64_t t = pstart[p] + blockIdx.x; t < t1; t += gridDim.x)
-            mr_target<T, RP>(mr_smem, t, roff, blob, A, ws, xin, yout);
+            mr_target<T, RP, DF>(mr_smem, t, roff, blob, A, ws, xin, yout);
         if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
     }
 }
@@ -232,7 +294,7 @@ static int mr_num_sms() {
     return n;
 }
 
-template <class T, int RP>
+template <class T, int RP, bool DF>
 static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                                const MrPhases *phased, const T *A, T *ws, const T *xin, double *yout,
                                unsigned *bar, int32_t *err, cudaStream_t st) {
@@ -240,17 +302,17 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
     static int per_sm_coop = 0, per_sm = 0;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(mr_coop_kernel<T, RP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(mr_coop_kernel<T, RP, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Lay::smem);
         if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(mr_kernel<T, RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::smem);
+        e = cudaFuncSetAttribute(mr_kernel<T, RP, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
     const int nsm = mr_num_sms();
     if (phased) {
         if (per_sm == 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_kernel<T, RP>, Lay::NT, Lay::smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_kernel<T, RP, DF>, Lay::NT, Lay::smem);
             if (per_sm <= 0) per_sm = 1;
         }
         for (int p = 0; p < phased->n; ++p) {
@@ -258,7 +320,7 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
             if (t1 <= t0) continue;
             const int64_t cap = (int64_t)nsm * per_sm;
             const int grid = (int)(t1 - t0 < cap ? t1 - t0 : cap);
-            mr_kernel<T, RP><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, A, ws, xin, yout);
+            mr_kernel<T, RP, DF><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, A, ws, xin, yout);
             count_launch();
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
@@ -266,26 +328,26 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
         return cudaSuccess;
     }
     if (per_sm_coop == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, mr_coop_kernel<T, RP>, Lay::NT, Lay::smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, mr_coop_kernel<T, RP, DF>, Lay::NT, Lay::smem);
         if (per_sm_coop <= 0) return cudaErrorCooperativeLaunchTooLarge;
     }
     const int grid = nsm * per_sm_coop;
     void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&A,
                     (void *)&ws,   (void *)&xin,  (void *)&yout,   (void *)&bar,    (void *)&err};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_coop_kernel<T, RP>, dim3(grid), dim3(Lay::NT), args,
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_coop_kernel<T, RP, DF>, dim3(grid), dim3(Lay::NT), args,
                                                 Lay::smem, st);
     count_launch();
     return e;
 }
 
-template <class T>
+template <class T, bool DF = false>
 static cudaError_t mr_dispatch(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                                const MrPhases *phased, const T *A, T *ws, const T *xin, double *yout,
                                unsigned *bar, int32_t *err, cudaStream_t st) {
     switch (rp) {
-    case 16: return mr_launch_t<T, 16>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
-    case 32: return mr_launch_t<T, 32>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
-    case 64: return mr_launch_t<T, 64>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    case 16: return mr_launch_t<T, 16, DF>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    case 32: return mr_launch_t<T, 32, DF>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    case 64: return mr_launch_t<T, 64, DF>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -294,6 +356,11 @@ cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, cons
                           const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st) {
     return mr_dispatch<double>(rp, roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+}
+cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                           const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                           unsigned *bar, int32_t *err, cudaStream_t st) {
+    return mr_dispatch<double, true>(rp, roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
 }
 cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                           const MrPhases *phased, const float *A, float *ws, const float *xin, double *yout,
@@ -519,7 +586,10 @@ __global__ void gmb_start_fin(GmresBatch g, double tol) {
         const double r = beta / g.normb[c];
         g.resid[c] = r;
         g.conv[c] = c >= g.nrhs ? -3 : (r <= tol ? -2 : -1);
-        if (c == 0) *g.iter = 0;
+        if (c == 0) {
+            g.iter[0] = 0;
+            g.iter[1] = 0;  // Arnoldi steps taken (graph loop counter)
+        }
     }
     const double ib = beta > 0.0 ? 1.0 / beta : 0.0;
     int64_t r0, r1;
@@ -560,7 +630,16 @@ __global__ void gmb_xupdate(GmresBatch g, double *__restrict__ x, int kmax) {
     }
 }
 
-static bool gmb_attr(const GmresBatch &g) {
+// Loop condition of the graph-captured batched Arnoldi step: run another
+// step while a column is still running and fewer than m steps were taken.
+__global__ void gmb_loop_cond(GmresBatch g, cudaGraphConditionalHandle hnd) {
+    const int c = ++g.iter[1];
+    int running = 0;
+    for (int q = 0; q < g.nrhs; ++q) running |= g.conv[q] == -1;
+    cudaGraphSetConditional(hnd, (running && c < g.m) ? 1u : 0u);
+}
+
+bool gmb_attr(const GmresBatch &g) {
     static int set = 0;
     const size_t need = ((size_t)(g.m + 1) * g.rp + GMB_THREADS) * 8;
     if ((int)need > set) {
@@ -599,6 +678,11 @@ cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st) {
     gmb_normalise<<<g.nblk, GMB_THREADS, 0, st>>>(g);
     gmb_givens<<<1, 64, 0, st>>>(g, tol);
     count_launch(8);
+    return cudaGetLastError();
+}
+cudaError_t gmb_loop(const GmresBatch &g, cudaGraphConditionalHandle hnd, cudaStream_t st) {
+    gmb_loop_cond<<<1, 1, 0, st>>>(g, hnd);
+    count_launch();
     return cudaGetLastError();
 }
 cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st) {

@@ -33,7 +33,12 @@ enum {
 enum { H2W_FORM_NESTED = 0, H2W_FORM_SEMINESTED = 1 };           /* -DUSE_nHODLRdD / -DUSE_snHODLRdD */
 enum { H2W_KERNEL_IE = 0, H2W_KERNEL_RBF = 1 };                 /* reference "choice" */
 enum { H2W_ASSEMBLE_NCA = 0, H2W_ASSEMBLE_IMPORT = 1, H2W_ASSEMBLE_LEARNED = 2 };
-enum { H2W_PREC_FP64 = 0, H2W_PREC_FP32 = 1 };
+/* FP64: FP64 operator and arithmetic. FP32: FP32 operator copy and arithmetic.
+ * DF64 (multi-vector products only: h2w_matvec with nrhs > 1 and the batched
+ * solvers): the FP64 operator with double-FP32 arithmetic (each operand split
+ * into an FP32 pair, products and sums carried as FP32 pairs), about 2^-44
+ * relative per term, on the FP32 pipes. */
+enum { H2W_PREC_FP64 = 0, H2W_PREC_FP32 = 1, H2W_PREC_DF64 = 2 };
 /* pointer-location flags for vectors */
 enum { H2W_HOST = 0, H2W_DEVICE = 1 };
 
@@ -129,9 +134,11 @@ int h2w_matvec_static(h2w_handle *h, const double *x, double *y, int precision, 
  * ({1D,2D,3D}/codes/gmres.hpp:92-200): x0 = x on entry, stops when |s(i+1)|/||b|| < 10^-tol_pow. */
 int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_pow, int where, int *iters,
               double *resid);
-/* Mixed precision: FP32 inner GMRES (FP32 operator) wrapped in FP64 iterative
- * refinement whose residual uses the FP64 operator; stops when the FP64
- * relative residual ||b - A x|| / ||b|| < 10^-tol_pow. */
+/* Mixed precision: FP32 inner GMRES (FP32 operator, from d = 0) wrapped in
+ * FP64 iterative refinement; the first residual (at the caller's x0) is formed
+ * with the FP32 operator and only corrects, every later residual uses the FP64
+ * operator and is the stopping test: FP64 relative residual
+ * ||b - A x|| / ||b|| < 10^-tol_pow. */
 int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int inner_iter, int tol_pow, int where,
                  int *outer_iters, int *inner_total, double *resid);
 
@@ -147,13 +154,34 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
 int h2w_gmres_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max_iter, int tol_pow, int where,
                     int *iters, double *resid);
 /* Mixed precision for many right-hand sides: per block of up to 64 columns,
- * FP64 residuals (one multi-vector FP64 matvec per outer step) and a batched
+ * refinement residuals from one multi-vector matvec per outer step (the first
+ * with the FP32 operator, the later ones FP64, or DF64 by H2W_OPT_IR_RESIDUAL,
+ * and only those tested against the tolerance) and a batched
  * FP32-operator inner GMRES (relative tolerance 1e-6, x0 = 0). resid: final
  * FP64 relative residual per column (nrhs entries); outer_iters: largest
  * outer count over the blocks; inner_total: inner Arnoldi steps summed over
  * outer steps and blocks (lockstep steps, not per column). */
 int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max_outer, int inner_iter,
                        int tol_pow, int where, int *outer_iters, int *inner_total, double *resid);
+
+/* Execution options of a handle (no counterpart in the reference, whose
+ * only switches are compile-time macros):
+ *  H2W_OPT_GRAPH  1 (default): GMRES runs its Arnoldi steps as one CUDA graph
+ *                 launch (a conditional while node whose body is one step:
+ *                 matvec + orthogonalisation + rotations + loop test), so
+ *                 the host does not wait on each step; 0: host-driven loop.
+ *                 Both run the same kernels in the same order.
+ *  H2W_OPT_COOP   1 (default): a matvec is one cooperative launch with grid
+ *                 barriers between its phases; 0: one launch per phase.
+ *  H2W_OPT_IR_RESIDUAL  precision of the refinement residuals after the
+ *                 first in h2w_gmres_ir_batch: H2W_PREC_FP64 (default) or
+ *                 H2W_PREC_DF64. (The first residual, at the caller's x0, is
+ *                 formed with the FP32 operator and is not tested for
+ *                 convergence; the inner solve only needs it to the inner
+ *                 tolerance.) */
+enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2 };
+int h2w_set_option(h2w_handle *h, int option, int64_t value);
+int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
 /* Launch statistics of the block-row GEMV kernel that performs every matvec
  * pass. While enabled, each phase launch is bracketed by CUDA events on its
@@ -165,6 +193,12 @@ int h2w_profile(h2w_handle *h, int enable);
  * destination rows) at the given precision. nphases receives the count. */
 int h2w_profile_phases(h2w_handle *h, int precision, int max_phases, int64_t *launches, double *ms, double *bytes,
                        int *nphases);
+/* Launch statistics of the multi-vector matvec kernel (h2w_matvec with
+ * nrhs > 1, batched solvers) at one precision while profiling is enabled:
+ * launches, total device ms and the algorithmic bytes of one launch (packed
+ * operator once, the input block in the kernel's precision, the FP64 result
+ * block). */
+int h2w_profile_multi(h2w_handle *h, int precision, int64_t *launches, double *ms, double *bytes);
 /* Kernel launches issued by this library since it was loaded. */
 int64_t h2w_launch_count(void);
 

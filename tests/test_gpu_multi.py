@@ -143,3 +143,44 @@ def test_gmres_ir_batch(gpu, k):
         e_ir = np.linalg.norm(X[:, c] - XT[:, c]) / np.linalg.norm(XT[:, c])
         e_64 = np.linalg.norm(x64 - XT[:, c]) / np.linalg.norm(XT[:, c])
         assert e_ir <= 10 * e_64 + 1e-12, (c, e_ir, e_64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [CASES[0], CASES[2], CASES[4]])
+def test_multi_matvec_df64(gpu, case):
+    """Double-FP32 products on the FP64 operator: within 1e-12 of the FP64
+    product per column (FP32 alone is ~1e-7), including one right-hand side."""
+    hw = gpu
+    op, _ = setup(hw, case)
+    op.assemble(hw.ASSEMBLE_NCA)
+    X = rhs(76, op.N, 40)
+    Y64 = op.matvec(X)
+    Ydf = op.matvec(X, precision=hw.PREC_DF64)
+    for c in range(40):
+        assert np.linalg.norm(Ydf[:, c] - Y64[:, c]) / np.linalg.norm(Y64[:, c]) < 1e-12, c
+    y1 = op.matvec(X[:, 3], precision=hw.PREC_DF64)
+    assert np.linalg.norm(y1 - Y64[:, 3]) / np.linalg.norm(Y64[:, 3]) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gmres_ir_batch_df64_residuals(gpu):
+    """Refinement residuals in double-FP32: same tolerance reached, solution
+    error within 10x of the FP64-residual refinement."""
+    hw = gpu
+    op, _ = setup(hw, CASES[1])
+    op.assemble(hw.ASSEMBLE_NCA)
+    N = op.N
+    XT = rhs(77, N, 16)
+    B = op.matvec(XT)
+    X64, o64, i64, r64 = op.gmres_ir_batch(B, max_outer=20, inner_iter=100, tol_pow=10)
+    op.set_option(hw.OPT_IR_RESIDUAL, hw.PREC_DF64)
+    assert op.get_option(hw.OPT_IR_RESIDUAL) == hw.PREC_DF64
+    Xdf, odf, idf, rdf = op.gmres_ir_batch(B, max_outer=20, inner_iter=100, tol_pow=10)
+    assert np.all(rdf < 1e-10)
+    # the FP64 residual of the DF64-refined solution
+    R = B - op.matvec(Xdf)
+    for c in range(16):
+        assert np.linalg.norm(R[:, c]) / np.linalg.norm(B[:, c]) < 1e-10
+        e_df = np.linalg.norm(Xdf[:, c] - XT[:, c]) / np.linalg.norm(XT[:, c])
+        e_64 = np.linalg.norm(X64[:, c] - XT[:, c]) / np.linalg.norm(XT[:, c])
+        assert e_df <= 10 * e_64 + 1e-12, (c, e_df, e_64)
