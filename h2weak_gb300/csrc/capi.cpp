@@ -100,6 +100,7 @@ struct h2w_handle {
     DBuf<float> d_op32;
     DBuf<int64_t> d_roff, d_blob;  // packed target records of the matvec
     DBuf<int64_t> d_roff_m, d_blob_m, d_pstart_m;  // the multi-vector stream (64-row targets)
+    DBuf<int32_t> d_mctr;                           // its per-phase target counters
     std::vector<Phase> mphases;
     DBuf<double> d_ws, d_x, d_y;
     DBuf<int32_t> d_ctr, d_err;
@@ -1251,6 +1252,7 @@ void build_plan(h2w_handle *h) {
     h->d_roff_m.upload(roff_m, st);
     h->d_blob_m.upload(blob_m, st);
     h->d_pstart_m.upload(pstart_m, st);
+    h->d_mctr.alloc(std::max<size_t>(h->mphases.size(), 1));
     h->d_ws.alloc((size_t)h->ws_n);
     h->d_ctr.alloc(h->phases.size() + 1);
     h->d_err.alloc(1);
@@ -1523,6 +1525,7 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
     if (h->ws_n >= (int64_t)INT32_MAX - 2 || h->tree.N >= (int64_t)INT32_MAX - 2)
         throw ApiError(H2W_ERR_ARG, "workspace too large for the multi-vector kernel's source map");
     MrPhases ph{h->ph_t0.data(), h->ph_t1.data(), nph};
+    CK(cudaMemsetAsync(h->d_mctr.p, 0, (size_t)std::max(nph, 1) * 4, st));
     const MrPhases *phased = h->coop ? nullptr : &ph;
     if (prec == H2W_PREC_FP32) {
         ensure_f32(h);
@@ -1532,7 +1535,7 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
         if (h->m_xf.n < nx) h->m_xf.alloc(nx);
         CK(vec_f64_to_f32(xi, h->m_xf.p, (int64_t)nx, st));
         mr_prof(h, prec, rp, st, [&] {
-            return launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op32.p,
+            return launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op32.p,
                                  h->m_wsf.p, h->m_xf.p, yi, h->d_bar.p, h->d_err.p, st);
         });
         if (!h->fused_scatter) CK(launch_mr_widen_f32(h->m_wsf.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
@@ -1541,9 +1544,9 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
         CK(cudaMemsetAsync(h->m_wsd.p, 0, wsz * 8, st));
         mr_prof(h, prec, rp, st, [&] {
             if (prec == H2W_PREC_DF64)
-                return launch_mr_df64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op.p,
+                return launch_mr_df64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op.p,
                                       h->m_wsd.p, xi, yi, h->d_bar.p, h->d_err.p, st);
-            return launch_mr_f64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_op.p,
+            return launch_mr_f64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op.p,
                                  h->m_wsd.p, xi, yi, h->d_bar.p, h->d_err.p, st);
         });
         if (!h->fused_scatter) CK(launch_mr_widen_f64(h->m_wsd.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));

@@ -92,21 +92,22 @@ cudaError_t vec_f32_to_f64(const float *x, double *y, int64_t n, cudaStream_t st
 // ------------------------------------------------ multiple right-hand sides
 // Blocks of rp vectors are interleaved: element (t, c) at t*rp + c
 // (rp = 16, 32 or 64). The workspace holds ws_n rows of rp values.
+// ctr: one int per phase, zero at launch (the phase's target counter).
 struct MrPhases {          // per-phase launches instead of one cooperative launch
     const int64_t *t0, *t1;
     int n;
 };
 cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                          const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                          const MrPhases *phased, int32_t *ctr, const double *A, double *ws, const double *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st);
 cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                          const MrPhases *phased, const float *A, float *ws, const float *xin, double *yout,
+                          const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st);
 // FP64 operator and vectors, double-FP32 arithmetic on the FP32 pipes
 // (each product and sum carried as an FP32 pair; about 2^-44 relative per
 // term instead of FP64's 2^-53, at the FP32 pipes' rate).
 cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                           const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                           const MrPhases *phased, int32_t *ctr, const double *A, double *ws, const double *xin, double *yout,
                            unsigned *bar, int32_t *err, cudaStream_t st);
 cudaError_t launch_mr_pack(const double *x, int64_t ldx, double *xi, const int32_t *perm, int64_t n, int nrhs,
                            int rp, cudaStream_t st);

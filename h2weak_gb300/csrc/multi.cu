@@ -40,7 +40,7 @@ template <class T, int RP> struct MrLayout {
     static constexpr size_t as_bytes = sizeof(T) * MR_KC * MR_MT;
     static constexpr size_t xs_bytes = sizeof(T) * MR_KC * RP;
     static constexpr size_t map_bytes = (size_t)4 * BRG_XS_ELEMS;
-    static constexpr size_t smem = rec_bytes + as_bytes + xs_bytes + map_bytes;
+    static constexpr size_t smem = rec_bytes + 2 * (as_bytes + xs_bytes) + map_bytes;  // two staging buffers
     static_assert(NA >= 1 && NA * VN * NT == MR_KC * MR_MT, "A chunk split");
     static_assert(NX >= 1 && NX * VN * NT == MR_KC * RP, "X chunk split");
 };
@@ -105,9 +105,10 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
     using V = typename MrVec<T>::type;
     constexpr int NT = Lay::NT, VN = Lay::VN, NA = Lay::NA, NX = Lay::NX;
     int64_t *rec = reinterpret_cast<int64_t *>(smem);
+    // staging buffer s: As + s * MR_KC * MR_MT, Xs + s * MR_KC * RP
     T *As = reinterpret_cast<T *>(smem + Lay::rec_bytes);
-    T *Xs = reinterpret_cast<T *>(smem + Lay::rec_bytes + Lay::as_bytes);
-    int32_t *map = reinterpret_cast<int32_t *>(smem + Lay::rec_bytes + Lay::as_bytes + Lay::xs_bytes);
+    T *Xs = reinterpret_cast<T *>(smem + Lay::rec_bytes + 2 * Lay::as_bytes);
+    int32_t *map = reinterpret_cast<int32_t *>(smem + Lay::rec_bytes + 2 * (Lay::as_bytes + Lay::xs_bytes));
     const int tid = threadIdx.x;
     const int ty = tid / (RP / 4), tx = tid % (RP / 4);
 
@@ -169,11 +170,11 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
             }
         }
     };
-    auto store = [&]() {
+    auto store = [&](int sb) {
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
             const int v = tid + NT * u;
-            T *d = As + (v / (MR_MT / VN)) * MR_MT + (v % (MR_MT / VN)) * VN;
+            T *d = As + sb * (MR_KC * MR_MT) + (v / (MR_MT / VN)) * MR_MT + (v % (MR_MT / VN)) * VN;
             if constexpr (DF) {
                 const float2 h0 = df_split(ra[u].x), h1 = df_split(ra[u].y);
                 *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
@@ -184,7 +185,7 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
 #pragma unroll
         for (int u = 0; u < NX; ++u) {
             const int v = tid + NT * u;
-            T *d = Xs + (v / (RP / VN)) * RP + (v % (RP / VN)) * VN;
+            T *d = Xs + sb * (MR_KC * RP) + (v / (RP / VN)) * RP + (v % (RP / VN)) * VN;
             if constexpr (DF) {
                 const float2 h0 = df_split(rx[u].x), h1 = df_split(rx[u].y);
                 *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
@@ -205,20 +206,31 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
                 ah[i][j] = 0.f;
                 al[i][j] = 0.f;
             }
-        int q = 0, c0 = 0;
-        if (np > 0) load(0, 0, rt0);
+        // Two staging buffers: chunk i is multiplied from buffer i&1 while the
+        // registers already hold chunk i+1, which then goes to the other buffer;
+        // one barrier per chunk. Warps whose rows are all past the target's
+        // last row skip the multiply.
+        int q = 0, c0 = 0, sb = 0;
+        if (np > 0) {
+            load(0, 0, rt0);
+            store(0);
+        }
+        __syncthreads();
+        const bool active = rt0 + ty * 4 < nrows;
         while (q < np) {
-            store();
-            __syncthreads();
             int nq = q, nc0 = c0 + MR_KC;
             if (nc0 >= (int)(pan[3 * q + 1] >> 32)) { nq = q + 1; nc0 = 0; }
-            if (nq < np) load(nq, nc0, rt0);
-            if constexpr (DF) {
+            const bool more = nq < np;
+            if (more) load(nq, nc0, rt0);
+            const T *Ab = As + sb * (MR_KC * MR_MT);
+            const T *Xb = Xs + sb * (MR_KC * RP);
+            if (!active) {
+            } else if constexpr (DF) {
 #pragma unroll 4
                 for (int k = 0; k < MR_KC; ++k) {
                     float2 a4[4], x4[4];
-                    df_get4(a4, reinterpret_cast<const float2 *>(As) + k * MR_MT + ty * 4);
-                    df_get4(x4, reinterpret_cast<const float2 *>(Xs) + k * RP + tx * 4);
+                    df_get4(a4, reinterpret_cast<const float2 *>(Ab) + k * MR_MT + ty * 4);
+                    df_get4(x4, reinterpret_cast<const float2 *>(Xb) + k * RP + tx * 4);
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -228,17 +240,19 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
 #pragma unroll 8
                 for (int k = 0; k < MR_KC; ++k) {
                     T a4[4], x4[4];
-                    mr_get4(a4, As + k * MR_MT + ty * 4);
-                    mr_get4(x4, Xs + k * RP + tx * 4);
+                    mr_get4(a4, Ab + k * MR_MT + ty * 4);
+                    mr_get4(x4, Xb + k * RP + tx * 4);
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
 #pragma unroll
                         for (int j = 0; j < 4; ++j) acc[i][j] += a4[i] * x4[j];
                 }
             }
+            if (more) store(sb ^ 1);
             __syncthreads();
             q = nq;
             c0 = nc0;
+            sb ^= 1;
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -260,25 +274,39 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
     __syncthreads();
 }
 
+// Targets [t0, t1) of one phase: a CTA takes t0 + blockIdx.x first, then
+// claims the next unstarted target from the phase's counter (zero at launch),
+// so CTAs that finish early take over the remaining work.
+template <class T, int RP, bool DF>
+__device__ __forceinline__ void mr_phase(char *smem, int64_t t0, int64_t t1, int32_t *ctr,
+                                         const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
+                                         const T *__restrict__ A, T *ws, const T *__restrict__ xin, double *yout) {
+    __shared__ int64_t s_next;
+    int64_t t = t0 + blockIdx.x;
+    while (t < t1) {
+        mr_target<T, RP, DF>(smem, t, roff, blob, A, ws, xin, yout);
+        if (threadIdx.x == 0) s_next = t0 + gridDim.x + atomicAdd(ctr, 1);
+        __syncthreads();
+        t = s_next;
+    }
+}
+
 template <class T, int RP, bool DF>
 __global__ void __launch_bounds__(4 * RP)
     mr_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
-              const T *__restrict__ A, T *ws, const T *__restrict__ xin, double *yout) {
+              int32_t *ctr, const T *__restrict__ A, T *ws, const T *__restrict__ xin, double *yout) {
     extern __shared__ __align__(16) char mr_smem[];
-    for (int64_t t = t0 + blockIdx.x; t < t1; t += gridDim.x)
-        mr_target<T, RP, DF>(mr_smem, t, roff, blob, A, ws, xin, yout);
+    mr_phase<T, RP, DF>(mr_smem, t0, t1, ctr, roff, blob, A, ws, xin, yout);
 }
 
 template <class T, int RP, bool DF>
 __global__ void __launch_bounds__(4 * RP)
     mr_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
-                   const int64_t *__restrict__ pstart, int nphase, const T *__restrict__ A, T *ws,
-                   const T *__restrict__ xin, double *yout, unsigned *bar, int32_t *err) {
+                   const int64_t *__restrict__ pstart, int nphase, int32_t *ctr, const T *__restrict__ A,
+                   T *ws, const T *__restrict__ xin, double *yout, unsigned *bar, int32_t *err) {
     extern __shared__ __align__(16) char mr_smem[];
     for (int p = 0; p < nphase; ++p) {
-        const int64_t t1 = pstart[p + 1];
-        for (int64_t t = pstart[p] + blockIdx.x; t < t1; t += gridDim.x)
-            mr_target<T, RP, DF>(mr_smem, t, roff, blob, A, ws, xin, yout);
+        mr_phase<T, RP, DF>(mr_smem, pstart[p], pstart[p + 1], ctr + p, roff, blob, A, ws, xin, yout);
         if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
     }
 }
@@ -296,8 +324,8 @@ static int mr_num_sms() {
 
 template <class T, int RP, bool DF>
 static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                               const MrPhases *phased, const T *A, T *ws, const T *xin, double *yout,
-                               unsigned *bar, int32_t *err, cudaStream_t st) {
+                               const MrPhases *phased, int32_t *ctr, const T *A, T *ws, const T *xin,
+                               double *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
     using Lay = MrLayout<T, RP>;
     static int per_sm_coop = 0, per_sm = 0;
     static bool attr = false;
@@ -320,7 +348,7 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
             if (t1 <= t0) continue;
             const int64_t cap = (int64_t)nsm * per_sm;
             const int grid = (int)(t1 - t0 < cap ? t1 - t0 : cap);
-            mr_kernel<T, RP, DF><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, A, ws, xin, yout);
+            mr_kernel<T, RP, DF><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, ctr + p, A, ws, xin, yout);
             count_launch();
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
@@ -332,7 +360,7 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
         if (per_sm_coop <= 0) return cudaErrorCooperativeLaunchTooLarge;
     }
     const int grid = nsm * per_sm_coop;
-    void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&A,
+    void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&ctr, (void *)&A,
                     (void *)&ws,   (void *)&xin,  (void *)&yout,   (void *)&bar,    (void *)&err};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_coop_kernel<T, RP, DF>, dim3(grid), dim3(Lay::NT), args,
                                                 Lay::smem, st);
@@ -342,30 +370,30 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
 
 template <class T, bool DF = false>
 static cudaError_t mr_dispatch(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                               const MrPhases *phased, const T *A, T *ws, const T *xin, double *yout,
-                               unsigned *bar, int32_t *err, cudaStream_t st) {
+                               const MrPhases *phased, int32_t *ctr, const T *A, T *ws, const T *xin,
+                               double *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
     switch (rp) {
-    case 16: return mr_launch_t<T, 16, DF>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
-    case 32: return mr_launch_t<T, 32, DF>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
-    case 64: return mr_launch_t<T, 64, DF>(roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    case 16: return mr_launch_t<T, 16, DF>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    case 32: return mr_launch_t<T, 32, DF>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    case 64: return mr_launch_t<T, 64, DF>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
     default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                          const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                          const MrPhases *phased, int32_t *ctr, const double *A, double *ws, const double *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st) {
-    return mr_dispatch<double>(rp, roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    return mr_dispatch<double>(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
 }
 cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                           const MrPhases *phased, const double *A, double *ws, const double *xin, double *yout,
+                           const MrPhases *phased, int32_t *ctr, const double *A, double *ws, const double *xin, double *yout,
                            unsigned *bar, int32_t *err, cudaStream_t st) {
-    return mr_dispatch<double, true>(rp, roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    return mr_dispatch<double, true>(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
 }
 cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                          const MrPhases *phased, const float *A, float *ws, const float *xin, double *yout,
+                          const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st) {
-    return mr_dispatch<float>(rp, roff, blob, pstart, nphase, phased, A, ws, xin, yout, bar, err, st);
+    return mr_dispatch<float>(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
 }
 
 // ------------------------------------------------------ pack / unpack ---
@@ -430,48 +458,70 @@ __device__ __forceinline__ size_t gmb_h(const GmresBatch &g, int c, int row, int
 
 // out[(blk*(m+1) + k)*rp + c] = sum over the block's rows of a_k[t, c] * b[t, c],
 // k = 0..kn-1, a_k = a + k*N*rp (kn = 1: a itself)
+// Four a_k per sweep over the rows (b read once per four); red: 4*GMB_THREADS.
 __device__ void gmb_block_dots(const GmresBatch &g, const double *a, const double *b, int kn, int64_t r0,
                                int64_t r1, double *red, double *out) {
     const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
     const size_t stride = (size_t)g.N * rp;
-    for (int k = 0; k < kn; ++k) {
-        const double *ak = a + k * stride;
-        double acc = 0.0;
-        for (int64_t t = r0 + rl; t < r1; t += RL) acc += ak[t * rp + c] * b[t * rp + c];
-        red[rl * rp + c] = acc;
-        __syncthreads();
-        if (rl == 0) {
-            double s = 0.0;
-            for (int q = 0; q < RL; ++q) s += red[q * rp + c];
-            out[((size_t)blockIdx.x * (g.m + 1) + k) * rp + c] = s;
+    for (int k0 = 0; k0 < kn; k0 += 4) {
+        const int kc = kn - k0 < 4 ? kn - k0 : 4;
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 2
+        for (int64_t t = r0 + rl; t < r1; t += RL) {
+            const double bv = b[t * rp + c];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j < kc) acc[j] += a[(k0 + j) * stride + t * rp + c] * bv;
         }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) red[(j * RL + rl) * rp + c] = acc[j];
+        __syncthreads();
+        if (rl == 0)
+            for (int j = 0; j < kc; ++j) {
+                double s2 = 0.0;
+                for (int q = 0; q < RL; ++q) s2 += red[(j * RL + q) * rp + c];
+                out[((size_t)blockIdx.x * (g.m + 1) + k0 + j) * rp + c] = s2;
+            }
         __syncthreads();
     }
 }
 
 __global__ void gmb_dots(GmresBatch g) {
-    __shared__ double red[GMB_THREADS];
+    __shared__ double red[4 * GMB_THREADS];
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
     gmb_block_dots(g, g.V, g.w, *g.iter + 1, r0, r1, red, g.part);
 }
 
-// hsum[k*rp + c] = sum_b part[(b*(m+1) + k)*rp + c] for k <= i (all = 1) or k = 0 (all = 0)
+// hsum[k*rp + c] = sum_b part[(b*(m+1) + k)*rp + c] for k <= i (all = 1) or k = 0 (all = 0);
+// block k, its threads split the blocks' partials, then meet in shared memory
 __global__ void gmb_reduce(GmresBatch g, int all) {
+    __shared__ double red[GMB_THREADS];
     const int kn = all ? *g.iter + 1 : 1;
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (int64_t)kn * g.rp) return;
-    const int k = (int)(e / g.rp), c = (int)(e % g.rp);
-    double s = 0.0;
-    for (int b = 0; b < g.nblk; ++b) s += g.part[((size_t)b * (g.m + 1) + k) * g.rp + c];
-    g.hsum[e] = s;
+    const int k = blockIdx.x;
+    if (k >= kn) return;
+    const int rp = g.rp, c = threadIdx.x % rp, bl = threadIdx.x / rp, BL = GMB_THREADS / rp;
+    double s0 = 0.0, s1 = 0.0;
+    int b = bl;
+    for (; b + BL < g.nblk; b += 2 * BL) {
+        s0 += g.part[((size_t)b * (g.m + 1) + k) * rp + c];
+        s1 += g.part[((size_t)(b + BL) * (g.m + 1) + k) * rp + c];
+    }
+    if (b < g.nblk) s0 += g.part[((size_t)b * (g.m + 1) + k) * rp + c];
+    red[threadIdx.x] = s0 + s1;
+    __syncthreads();
+    if (bl == 0) {
+        double s = 0.0;
+        for (int q = 0; q < BL; ++q) s += red[q * rp + c];
+        g.hsum[(size_t)k * rp + c] = s;
+    }
 }
 
 // h = hsum; H(:, i) (=|+=) h; w -= V h; then new dots (pass 0) or ||w||^2 partials (pass 1)
 __global__ void gmb_update(GmresBatch g, int pass) {
     extern __shared__ double gmb_sm[];
     double *h = gmb_sm;
-    double *red = gmb_sm + (size_t)(g.m + 1) * g.rp;
+    double *red = gmb_sm + (size_t)(g.m + 1) * g.rp;  // 4 * GMB_THREADS
     const int i = *g.iter, rp = g.rp;
     for (int e = threadIdx.x; e < (i + 1) * rp; e += blockDim.x) h[e] = g.hsum[e];
     __syncthreads();
@@ -551,7 +601,7 @@ __global__ void gmb_givens(GmresBatch g, double tol) {
 
 // w = b - Ax (Ax == NULL: w = b) and per-block partials of ||w||^2
 __global__ void gmb_resid(GmresBatch g, const double *__restrict__ b, const double *__restrict__ Ax) {
-    __shared__ double red[GMB_THREADS];
+    __shared__ double red[4 * GMB_THREADS];
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
     const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
@@ -561,7 +611,7 @@ __global__ void gmb_resid(GmresBatch g, const double *__restrict__ b, const doub
 }
 // partials of ||v[:, c]||^2
 __global__ void gmb_colnorm_part(GmresBatch g, const double *__restrict__ v) {
-    __shared__ double red[GMB_THREADS];
+    __shared__ double red[4 * GMB_THREADS];
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
     gmb_block_dots(g, v, v, 1, r0, r1, red, g.part);
@@ -641,16 +691,13 @@ __global__ void gmb_loop_cond(GmresBatch g, cudaGraphConditionalHandle hnd) {
 
 bool gmb_attr(const GmresBatch &g) {
     static int set = 0;
-    const size_t need = ((size_t)(g.m + 1) * g.rp + GMB_THREADS) * 8;
+    const size_t need = ((size_t)(g.m + 1) * g.rp + 4 * GMB_THREADS) * 8;
     if ((int)need > set) {
         if (cudaFuncSetAttribute(gmb_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) != cudaSuccess)
             return false;
         set = (int)need;
     }
     return true;
-}
-static unsigned gmb_rgrid(const GmresBatch &g) {
-    return (unsigned)(((size_t)(g.m + 1) * g.rp + GMB_THREADS - 1) / GMB_THREADS);
 }
 
 cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st) {
@@ -661,20 +708,20 @@ cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zer
 }
 cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st) {
     gmb_resid<<<g.nblk, GMB_THREADS, 0, st>>>(g, b, Ax);
-    gmb_reduce<<<1, 64, 0, st>>>(g, 0);
+    gmb_reduce<<<1, GMB_THREADS, 0, st>>>(g, 0);
     gmb_start_fin<<<g.nblk, GMB_THREADS, 0, st>>>(g, tol);
     count_launch(3);
     return cudaGetLastError();
 }
 cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st) {
     if (!gmb_attr(g)) return cudaErrorInvalidValue;
-    const size_t smu = ((size_t)(g.m + 1) * g.rp + GMB_THREADS) * 8;
+    const size_t smu = ((size_t)(g.m + 1) * g.rp + 4 * GMB_THREADS) * 8;
     gmb_dots<<<g.nblk, GMB_THREADS, 0, st>>>(g);
-    gmb_reduce<<<gmb_rgrid(g), GMB_THREADS, 0, st>>>(g, 1);
+    gmb_reduce<<<g.m + 1, GMB_THREADS, 0, st>>>(g, 1);
     gmb_update<<<g.nblk, GMB_THREADS, smu, st>>>(g, 0);
-    gmb_reduce<<<gmb_rgrid(g), GMB_THREADS, 0, st>>>(g, 1);
+    gmb_reduce<<<g.m + 1, GMB_THREADS, 0, st>>>(g, 1);
     gmb_update<<<g.nblk, GMB_THREADS, smu, st>>>(g, 1);
-    gmb_reduce<<<1, 64, 0, st>>>(g, 0);
+    gmb_reduce<<<1, GMB_THREADS, 0, st>>>(g, 0);
     gmb_normalise<<<g.nblk, GMB_THREADS, 0, st>>>(g);
     gmb_givens<<<1, 64, 0, st>>>(g, tol);
     count_launch(8);
