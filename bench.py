@@ -238,6 +238,11 @@ def main():
     torch.cuda.synchronize()
     X_d = torch.empty_like(XT_d)
     op.set_option(hw.OPT_IR_RESIDUAL, hw.PREC_DF64)
+    # target granularity picked by the autotuner on this operator and GPU
+    # (multi-vector stream on the refinement step's product mix: four FP32
+    # products per double-FP32 residual; single-vector stream on the FP32 product)
+    tuned_xw, tuned_xw_ms = op.autotune(nrhs=R, precision=hw.TUNE_IR_MIX, reps=2)
+    tuned_rs, tuned_rs_ms = op.autotune(nrhs=1, precision=hw.PREC_FP32, reps=5)
 
     def solve_batched():
         X_d.fill_(1.0)
@@ -383,6 +388,8 @@ def main():
                    "solver": "batched: FP32-operator inner GMRES (FP64 Arnoldi, %d columns in lockstep, one "
                              "multi-vector matvec per step) + iterative refinement, residuals FP32 at x0 then "
                              "double-FP32 on the FP64 operator; CUDA-graph Arnoldi loop" % R,
+                   "autotuned": {"multi_xw": tuned_xw, "multi_mix_ms": tuned_xw_ms, "single_row_split": tuned_rs,
+                                 "single_fp32_ms": tuned_rs_ms},
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "no flush: FP64 operator %.0f MB, FP32 %.0f MB, both > 129 MB L2" %
                          (op.operator_bytes(hw.PREC_FP64) / 1e6, op.operator_bytes(hw.PREC_FP32) / 1e6)},

@@ -28,7 +28,8 @@ KERNEL_IE, KERNEL_RBF = 0, 1
 ASSEMBLE_NCA, ASSEMBLE_IMPORT, ASSEMBLE_LEARNED = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
 HOST, DEVICE = 0, 1
-OPT_GRAPH, OPT_COOP, OPT_IR_RESIDUAL = 0, 1, 2
+OPT_GRAPH, OPT_COOP, OPT_IR_RESIDUAL, OPT_MULTI_XW, OPT_ROW_SPLIT = 0, 1, 2, 3, 4
+TUNE_IR_MIX = 16
 LISTS = {"charge": 0, "nbr": 1, "il": 2, "isvertex": 3, "far_check": 4, "far_charge": 5,
          "ver_check": 6, "ver_charge": 7, "sn_row": 8, "sn_col": 9}
 
@@ -91,6 +92,7 @@ def lib():
         "h2w_profile": [P, I],
         "h2w_profile_multi": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(D)],
         "h2w_set_option": [P, I, I64],
+        "h2w_autotune": [P, I, I, I, ctypes.POINTER(I64), ctypes.POINTER(D)],
         "h2w_get_option": [P, I, ctypes.POINTER(I64)],
         "h2w_profile_phases": [P, I, I, P, P, P, ctypes.POINTER(I)],
     }
@@ -209,6 +211,13 @@ class H2Operator:
         return b.value
 
     # instrumentation
+    def autotune(self, nrhs=64, precision=PREC_FP32, reps=3):
+        """Time each candidate target granularity and keep the fastest;
+        returns (chosen value, ms per repetition)."""
+        c, ms = ctypes.c_int64(), ctypes.c_double()
+        self._ck(lib().h2w_autotune(self.h, nrhs, precision, reps, ctypes.byref(c), ctypes.byref(ms)))
+        return c.value, ms.value
+
     def set_option(self, option, value):
         self._ck(lib().h2w_set_option(self.h, option, int(value)))
 

@@ -76,8 +76,13 @@ inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
 constexpr int XW_CAP = 4096;          // gathered source width per target (elements)
 constexpr int64_t ROW_SPLIT = 16384;  // rows * width above which a target is split (load balance)
 constexpr int64_t MR_ROWS = 64;      // rows per target of the multi-vector stream (its result tile)
+constexpr int64_t MR_XW_DEFAULT = 1024;  // gathered columns per multi-vector target before a column split
 
 }  // namespace
+
+namespace {
+struct PlanBuilder;
+}
 
 struct h2w_handle {
     h2w_config cfg{};
@@ -115,7 +120,11 @@ struct h2w_handle {
     struct ProfRec { cudaEvent_t a, b; int prec, phase; int rp = 1; };  // prec + 2: multi-vector launch
     std::vector<ProfRec> prof_recs;
     std::vector<cudaEvent_t> ev_pool;
-    bool fused_scatter = true;
+    bool fused_scatter = true, fused_scatter_m = true;  // per target stream
+    std::shared_ptr<PlanBuilder> plan;                  // logical targets (re-cut by the autotuner)
+    int nph_total = 0;
+    int64_t mr_xw = MR_XW_DEFAULT;                      // column cap of the multi-vector stream
+    int64_t row_split = ROW_SPLIT;                      // row split of the single-vector stream
     int64_t ws_n = 0, yperm_off = 0, op_n = 0;
     double storage = 0;
     int64_t op_bytes_read = 0;  // elements of operator data one matvec reads
@@ -563,6 +572,8 @@ struct PlanBuilder {
     // row chunks of max(min_rows, row_split / width) rows (multiples of 4)
     int64_t row_split = ROW_SPLIT;
     int64_t min_rows = 4;
+    int64_t xw_cap = XW_CAP;  // gathered columns per target before a column split
+    bool fused = true;        // no leaf (scatter) target was column-split
 
     // column-major block: element (i, c) at a + c*lda + i, lda = pad4(rows)
     int64_t alloc(int64_t rows, int64_t cols, int32_t &lda) {
@@ -598,27 +609,29 @@ struct PlanBuilder {
         logical.push_back({dst, nrows, flags, panels, lo, hi});
     }
     // Realise the logical targets with the given split parameters into T/P/S/win.
-    void realize(int64_t rs, int64_t mr) {
+    void realize(int64_t rs, int64_t mr, int64_t cap) {
         T.clear();
         P.clear();
         S.clear();
         win.clear();
         row_split = rs;
         min_rows = mr;
+        xw_cap = cap;
+        fused = true;
         for (const LTarget &l : logical) {
             lo = l.lo;
             hi = l.hi;
             split(l.dst, l.nrows, l.flags, l.panels);
         }
     }
-    // Cut a target into row chunks and, past XW_CAP gathered columns, into
+    // Cut a target into row chunks and, past xw_cap gathered columns, into
     // atomically accumulated column chunks.
     void split(int64_t dst, int32_t nrows, int32_t flags, const std::vector<PanelSpec> &panels) {
         if (nrows <= 0) return;
         int64_t xw = 0;
         for (auto &p : panels) xw += pad4(p.w);
         if (xw == 0) return;
-        if (xw <= XW_CAP) {
+        if (xw <= xw_cap) {
             // row chunks are multiples of 4 rows so the kernel's 16-byte column loads stay aligned
             int64_t rows_per =
                 std::max<int64_t>(min_rows, (row_split / std::max<int64_t>(xw, 1)) & ~int64_t(3));
@@ -653,11 +666,11 @@ struct PlanBuilder {
             }
             return;
         }
-        // column split: one sub-target per chunk of <= XW_CAP columns, atomically accumulated
-        if (flags & T_SCATTER) h->fused_scatter = false;
+        // column split: one sub-target per chunk of <= xw_cap columns, atomically accumulated
+        if (flags & T_SCATTER) fused = false;
         for (auto &p : panels) {
-            for (int64_t c0 = 0; c0 < p.w; c0 += XW_CAP) {
-                int64_t c1 = std::min<int64_t>(p.w, c0 + XW_CAP);
+            for (int64_t c0 = 0; c0 < p.w; c0 += xw_cap) {
+                int64_t c1 = std::min<int64_t>(p.w, c0 + xw_cap);
                 PanelSpec q;
                 q.a = p.a + c0 * p.lda;
                 q.lda = p.lda;
@@ -685,7 +698,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h, const std::vector
     auto bad = [](const char *what) { throw ApiError(H2W_ERR_STATE, std::string("internal plan check failed: ") + what); };
     const int64_t N = h->tree.N, wsn = h->ws_n, opn = pb.opn, nidx = (int64_t)pb.idx.size();
     for (const Phase &ph : phases)
-        if (ph.t0 < 0 || ph.t1 < ph.t0 || ph.t1 > (int64_t)pb.T.size() || ph.max_xw > XW_CAP) bad("phase");
+        if (ph.t0 < 0 || ph.t1 < ph.t0 || ph.t1 > (int64_t)pb.T.size() || ph.max_xw > pb.xw_cap) bad("phase");
     for (const Target &t : pb.T) {
         if (t.nrows < 1 || t.dst < 0 || t.dst + t.nrows > wsn) bad("target rows");
         if (t.p0 < 0 || t.p1 < t.p0 || t.p1 > (int32_t)pb.P.size() || t.p1 - t.p0 > BRG_MAX_PANELS) bad("target panels");
@@ -707,7 +720,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h, const std::vector
             }
             xw += pad4(p.w);
         }
-        if (xw != t.xw || xw > XW_CAP || xw > BRG_XS_ELEMS) bad("target width");
+        if (xw != t.xw || xw > pb.xw_cap || xw > BRG_XS_ELEMS) bad("target width");
     }
     for (const FactorJob &f : pb.factors)
         if (f.r < 1 || f.f < 0 || f.f + (int64_t)f.r * f.r > pb.fn || f.ii < 0 || f.ii + f.r > nidx || f.jj < 0 ||
@@ -735,7 +748,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h, const std::vector
 // Phase assignment of the realised targets: fixed targets at their phase,
 // flexible ones (largest first) into the least-loaded phase of their window;
 // targets sorted by phase, heaviest first within a phase.
-void assign_phases(h2w_handle *h, PlanBuilder &pb, int NPH, std::vector<Phase> &phases) {
+void assign_phases(h2w_handle *h, PlanBuilder &pb, int NPH, std::vector<Phase> &phases, bool &fused) {
     const size_t nt = pb.T.size();
     std::vector<int> ph(nt, 0);
     std::vector<double> load((size_t)NPH, 0.0);
@@ -779,8 +792,8 @@ void assign_phases(h2w_handle *h, PlanBuilder &pb, int NPH, std::vector<Phase> &
     const Phase &lp = phases.back();
     for (int64_t r = lp.t0; r < lp.t1; ++r)
         if (pb.T[(size_t)r].flags & T_SCATTER) covered += pb.T[(size_t)r].nrows;
-    if (covered != h->tree.N) h->fused_scatter = false;
-    if (!h->fused_scatter)
+    fused = pb.fused && covered == h->tree.N;
+    if (!fused)
         for (int64_t r = lp.t0; r < lp.t1; ++r)
             if (pb.T[(size_t)r].flags & T_SCATTER) pb.T[(size_t)r].flags = T_ACCUM;
     for (Phase &p2 : phases) {
@@ -793,7 +806,7 @@ void assign_phases(h2w_handle *h, PlanBuilder &pb, int NPH, std::vector<Phase> &
 // Packed records: header, panels, segments (layout documented at brg_kernel),
 // plus the phase starts.
 void pack_records(const PlanBuilder &pb, const std::vector<Phase> &phases, std::vector<int64_t> &roff,
-                  std::vector<int64_t> &blob, std::vector<int64_t> &pstart) {
+                  std::vector<int64_t> &blob, std::vector<int64_t> &pstart, size_t max_words = BRG_REC_WORDS) {
     roff.assign(1, 0);
     blob.clear();
     for (const Target &tg : pb.T) {
@@ -818,13 +831,81 @@ void pack_records(const PlanBuilder &pb, const std::vector<Phase> &phases, std::
                 blob.push_back((int64_t)(uint32_t)sg.len | (code << 32));
             }
         }
-        if (blob.size() - base > (size_t)BRG_REC_WORDS)
+        if (blob.size() - base > max_words)
             throw ApiError(H2W_ERR_STATE, "internal: target record exceeds the shared-memory record size");
         roff.push_back((int64_t)blob.size());
     }
     pstart.clear();
     for (auto &ph : phases) pstart.push_back(ph.t0);
     pstart.push_back(phases.empty() ? 0 : phases.back().t1);
+}
+
+// (Re)cut the single-vector target stream: row chunks of max(4,
+// row_split / width) rows, column splits past XW_CAP; per-phase byte counts
+// for the profiling statistics.
+void realize_single(h2w_handle *h, int64_t row_split) {
+    if (!h->plan) throw ApiError(H2W_ERR_STATE, "operator not assembled");
+    if (row_split < 256 || row_split > (int64_t(1) << 24)) throw ApiError(H2W_ERR_ARG, "row split out of range");
+    PlanBuilder &pb = *h->plan;
+    std::vector<int64_t> roff, blob, pstart;
+    pb.realize(row_split, 4, XW_CAP);
+    assign_phases(h, pb, h->nph_total, h->phases, h->fused_scatter);
+    h->ph_op.assign(h->phases.size(), 0);
+    h->ph_vec.assign(h->phases.size(), 0);
+    for (size_t pi = 0; pi < h->phases.size(); ++pi) {
+        const Phase &ph = h->phases[pi];
+        for (int64_t q = ph.t0; q < ph.t1; ++q) {
+            const Target &tg = pb.T[(size_t)q];
+            h->ph_vec[pi] += (int64_t)tg.nrows * ((tg.flags & (T_ACCUM | T_ATOMIC)) ? 2 : 1);
+            for (int32_t p = tg.p0; p < tg.p1; ++p) {
+                const Panel &pn = pb.P[(size_t)p];
+                h->ph_op[pi] += (int64_t)tg.nrows * pn.w;
+                for (int32_t e = pn.s0; e < pn.s1; ++e) h->ph_vec[pi] += pb.S[(size_t)e].len;
+            }
+        }
+    }
+    validate_plan(pb, h, h->phases);
+    pack_records(pb, h->phases, roff, blob, pstart);
+    cudaStream_t st = h->stream;
+    h->d_roff.upload(roff, st);
+    h->d_blob.upload(blob, st);
+    h->d_pstart.upload(pstart, st);
+    h->row_split = row_split;
+    pb.T = std::vector<Target>();
+    pb.P = std::vector<Panel>();
+    pb.S = std::vector<Seg>();
+    CK(cudaStreamSynchronize(st));
+}
+
+// (Re)cut the multi-vector target stream from the handle's logical targets:
+// 64-row targets of at most `cap` gathered columns; records, phase starts and
+// per-phase counters uploaded. Cheaper than a new assembly (host work and a
+// few small uploads); the operator itself is untouched.
+void realize_multi(h2w_handle *h, int64_t cap) {
+    if (!h->plan) throw ApiError(H2W_ERR_STATE, "operator not assembled");
+    if (cap < 32 || cap > MR_XS_ELEMS || cap % 4) throw ApiError(H2W_ERR_ARG, "multi-vector column cap out of range");
+    PlanBuilder &pb = *h->plan;
+    std::vector<int64_t> roff, blob, pstart;
+    pb.realize(0, MR_ROWS, cap);
+    assign_phases(h, pb, h->nph_total, h->mphases, h->fused_scatter_m);
+    validate_plan(pb, h, h->mphases);
+    pack_records(pb, h->mphases, roff, blob, pstart);
+    cudaStream_t st = h->stream;
+    h->d_roff_m.upload(roff, st);
+    h->d_blob_m.upload(blob, st);
+    h->d_pstart_m.upload(pstart, st);
+    h->d_mctr.alloc(std::max<size_t>(h->mphases.size(), 1));
+    h->ph_t0.clear();
+    h->ph_t1.clear();
+    for (const Phase &ph : h->mphases) {
+        h->ph_t0.push_back(ph.t0);
+        h->ph_t1.push_back(ph.t1);
+    }
+    h->mr_xw = cap;
+    pb.T = std::vector<Target>();
+    pb.P = std::vector<Panel>();
+    pb.S = std::vector<Seg>();
+    CK(cudaStreamSynchronize(st));
 }
 
 void build_plan(h2w_handle *h) {
@@ -834,9 +915,10 @@ void build_plan(h2w_handle *h) {
     const bool has_far = dim > 1;
     const bool has_ver = (dim == 1 && !sn) || (dim > 1 && !sn);
     const bool has_pairs = sn;
-    PlanBuilder pb;
+    auto pbp = std::make_shared<PlanBuilder>();
+    PlanBuilder &pb = *pbp;
     pb.h = h;
-    h->fused_scatter = true;
+    h->fused_scatter = h->fused_scatter_m = true;
 
     // ---- workspace layout
     int64_t wsn = 0;
@@ -1200,31 +1282,10 @@ void build_plan(h2w_handle *h) {
     }
     // ---- target streams. Single-vector: fine row chunks (load balance of a
     // GEMV); multi-vector: 64-row chunks, one result tile per target.
-    std::vector<int64_t> roff, blob, pstart, roff_m, blob_m, pstart_m;
-    pb.realize(ROW_SPLIT, 4);
-    assign_phases(h, pb, NPH, h->phases);
-    h->ph_op.assign(h->phases.size(), 0);
-    h->ph_vec.assign(h->phases.size(), 0);
-    for (size_t pi = 0; pi < h->phases.size(); ++pi) {
-        const Phase &ph = h->phases[pi];
-        for (int64_t q = ph.t0; q < ph.t1; ++q) {
-            const Target &tg = pb.T[(size_t)q];
-            h->ph_vec[pi] += (int64_t)tg.nrows * ((tg.flags & (T_ACCUM | T_ATOMIC)) ? 2 : 1);
-            for (int32_t p = tg.p0; p < tg.p1; ++p) {
-                const Panel &pn = pb.P[(size_t)p];
-                h->ph_op[pi] += (int64_t)tg.nrows * pn.w;
-                for (int32_t e = pn.s0; e < pn.s1; ++e) h->ph_vec[pi] += pb.S[(size_t)e].len;
-            }
-        }
-    }
+    h->nph_total = NPH;
     for (auto &x : pb.xfers)
         if (x.f < 0) throw ApiError(H2W_ERR_STATE, "internal: unresolved factor");
-    validate_plan(pb, h, h->phases);
-    pack_records(pb, h->phases, roff, blob, pstart);
-    pb.realize(0, MR_ROWS);
-    assign_phases(h, pb, NPH, h->mphases);
-    validate_plan(pb, h, h->mphases);
-    pack_records(pb, h->mphases, roff_m, blob_m, pstart_m);
+    validate_plan(pb, h, {});  // assembly jobs (no targets realised yet)
 
     // ---- device buffers and assembly kernels
     cudaStream_t st = h->stream;
@@ -1246,13 +1307,14 @@ void build_plan(h2w_handle *h) {
     CK(launch_factor(dfac.p, (int)pb.factors.size(), didx.p, kp, dF.p, st));
     CK(launch_xfer(dxf.p, (int)pb.xfers.size(), pb.max_xfer_n, didx.p, kp, dF.p, h->d_op.p, st));
     CK(launch_fill(dfill.p, (int)pb.fills.size(), didx.p, kp, h->d_op.p, st));
-    h->d_roff.upload(roff, st);
-    h->d_blob.upload(blob, st);
-    h->d_pstart.upload(pstart, st);
-    h->d_roff_m.upload(roff_m, st);
-    h->d_blob_m.upload(blob_m, st);
-    h->d_pstart_m.upload(pstart_m, st);
-    h->d_mctr.alloc(std::max<size_t>(h->mphases.size(), 1));
+    // the assembly's index and job lists are not needed again
+    pb.idx = std::vector<int32_t>();
+    pb.fills = std::vector<FillJob>();
+    pb.factors = std::vector<FactorJob>();
+    pb.xfers = std::vector<XferJob>();
+    h->plan = pbp;
+    realize_single(h, h->row_split);
+    realize_multi(h, h->mr_xw);
     h->d_ws.alloc((size_t)h->ws_n);
     h->d_ctr.alloc(h->phases.size() + 1);
     h->d_err.alloc(1);
@@ -1538,7 +1600,7 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
             return launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op32.p,
                                  h->m_wsf.p, h->m_xf.p, yi, h->d_bar.p, h->d_err.p, st);
         });
-        if (!h->fused_scatter) CK(launch_mr_widen_f32(h->m_wsf.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
+        if (!h->fused_scatter_m) CK(launch_mr_widen_f32(h->m_wsf.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
     } else {
         if (h->m_wsd.n < wsz) h->m_wsd.alloc(wsz);
         CK(cudaMemsetAsync(h->m_wsd.p, 0, wsz * 8, st));
@@ -1549,7 +1611,7 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
             return launch_mr_f64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op.p,
                                  h->m_wsd.p, xi, yi, h->d_bar.p, h->d_err.p, st);
         });
-        if (!h->fused_scatter) CK(launch_mr_widen_f64(h->m_wsd.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
+        if (!h->fused_scatter_m) CK(launch_mr_widen_f64(h->m_wsd.p + (size_t)h->yperm_off * rp, yi, h->tree.N * rp, st));
     }
 }
 
@@ -2270,12 +2332,6 @@ int h2w_assemble(h2w_handle *h, int mode) {
         h->has_op = true;
         h->g_m = -1;
         h->gb_m = -1;
-        h->ph_t0.clear();
-        h->ph_t1.clear();
-        for (const Phase &ph : h->mphases) {
-            h->ph_t0.push_back(ph.t0);
-            h->ph_t1.push_back(ph.t1);
-        }
         h->m_wsd.reset();
         h->m_wsf.reset();
         return H2W_OK;
@@ -2546,6 +2602,14 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
             if (value != H2W_PREC_FP64 && value != H2W_PREC_DF64)
                 throw ApiError(H2W_ERR_ARG, "IR residual precision must be FP64 or DF64");
             h->ir_resid_prec = (int)value;
+        } else if (option == H2W_OPT_MULTI_XW) {
+            if (h->has_op) realize_multi(h, value);
+            else if (value < 32 || value > MR_XS_ELEMS || value % 4) throw ApiError(H2W_ERR_ARG, "column cap out of range");
+            h->mr_xw = value;
+        } else if (option == H2W_OPT_ROW_SPLIT) {
+            if (h->has_op) realize_single(h, value);
+            else if (value < 256 || value > (int64_t(1) << 24)) throw ApiError(H2W_ERR_ARG, "row split out of range");
+            h->row_split = value;
         } else if (option == H2W_OPT_COOP) {
             h->coop = value != 0;
             for (auto &g : h->loops) {  // captured steps hold the other launch form
@@ -2566,7 +2630,81 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         if (option == H2W_OPT_GRAPH) *value = (h->use_graphs && !h->graph_failed) ? 1 : 0;
         else if (option == H2W_OPT_COOP) *value = h->coop ? 1 : 0;
         else if (option == H2W_OPT_IR_RESIDUAL) *value = h->ir_resid_prec;
+        else if (option == H2W_OPT_MULTI_XW) *value = h->mr_xw;
+        else if (option == H2W_OPT_ROW_SPLIT) *value = h->row_split;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
+        return H2W_OK;
+    });
+}
+
+int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chosen, double *best_ms) {
+    return guarded(h, [&] {
+        require_op(h);
+        const bool mix = precision == H2W_TUNE_IR_MIX;
+        if (nrhs < 1 || reps < 1 ||
+            (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32 && precision != H2W_PREC_DF64 && !mix) ||
+            (nrhs == 1 && (precision == H2W_PREC_DF64 || mix)))
+            throw ApiError(H2W_ERR_ARG, "bad autotune arguments");
+        cudaStream_t st = h->stream;
+        const int64_t N = h->tree.N;
+        const bool multi = nrhs > 1;
+        const int rp = rp_for(std::min(nrhs, MR_MAX));
+        // inputs: zeros (the products' cost does not depend on the values)
+        if (multi) {
+            ensure_multi_vectors(h);
+            CK(cudaMemsetAsync(h->m_xi.p, 0, (size_t)N * rp * 8, st));
+        } else {
+            if (h->d_x.n < (size_t)N) h->d_x.alloc((size_t)N);
+            if (h->d_y.n < (size_t)N) h->d_y.alloc((size_t)N);
+            CK(cudaMemsetAsync(h->d_x.p, 0, (size_t)N * 8, st));
+        }
+        const std::vector<int64_t> cand = multi ? std::vector<int64_t>{256, 512, 1024, 2048}
+                                                : std::vector<int64_t>{4096, 8192, 16384, 32768, 65536};
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        int64_t best = multi ? h->mr_xw : h->row_split;
+        double bms = 1e300;
+        const bool prof = h->prof;
+        h->prof = false;
+        try {
+            for (int64_t c : cand) {
+                if (multi) realize_multi(h, c);
+                else realize_single(h, c);
+                auto once = [&] {
+                    if (mix) {  // the batched refinement's mix: four FP32 products per DF64 residual
+                        for (int q = 0; q < 4; ++q) run_matvec_multi(h, H2W_PREC_FP32, rp, h->m_xi.p, h->m_yi.p, st);
+                        run_matvec_multi(h, H2W_PREC_DF64, rp, h->m_xi.p, h->m_yi.p, st);
+                    } else if (multi) run_matvec_multi(h, precision, rp, h->m_xi.p, h->m_yi.p, st);
+                    else if (precision == H2W_PREC_FP32) run_matvec_f32(h, h->d_x.p, h->d_y.p, st, true);
+                    else run_matvec_f64(h, h->d_x.p, h->d_y.p, st, true);
+                };
+                once();  // first use (workspace, attributes) outside the timing
+                CK(cudaEventRecord(e0, st));
+                for (int r = 0; r < reps; ++r) once();
+                CK(cudaEventRecord(e1, st));
+                CK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, e0, e1));
+                check_device_error(h);
+                if (ms / reps < bms) {
+                    bms = ms / reps;
+                    best = c;
+                }
+            }
+        } catch (...) {
+            h->prof = prof;
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        h->prof = prof;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (multi) realize_multi(h, best);
+        else realize_single(h, best);
+        if (chosen) *chosen = best;
+        if (best_ms) *best_ms = bms;
         return H2W_OK;
     });
 }

@@ -63,6 +63,7 @@ cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, 
 constexpr int BRG_XS_ELEMS = 4096;    // gathered source width per target (elements)
 constexpr int BRG_MAX_PANELS = 32;    // panels per target
 constexpr int BRG_REC_WORDS = 1024;   // packed record of one target (int64 words)
+constexpr int MR_XS_ELEMS = 2048;     // gathered source width per multi-vector target (elements)
 
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,

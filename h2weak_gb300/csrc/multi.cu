@@ -39,7 +39,7 @@ template <class T, int RP> struct MrLayout {
     static constexpr size_t rec_bytes = (size_t)BRG_REC_WORDS * 8;
     static constexpr size_t as_bytes = sizeof(T) * MR_KC * MR_MT;
     static constexpr size_t xs_bytes = sizeof(T) * MR_KC * RP;
-    static constexpr size_t map_bytes = (size_t)4 * BRG_XS_ELEMS;
+    static constexpr size_t map_bytes = (size_t)4 * MR_XS_ELEMS;
     static constexpr size_t smem = rec_bytes + 2 * (as_bytes + xs_bytes) + map_bytes;  // two staging buffers
     static_assert(NA >= 1 && NA * VN * NT == MR_KC * MR_MT, "A chunk split");
     static_assert(NX >= 1 && NX * VN * NT == MR_KC * RP, "X chunk split");

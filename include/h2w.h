@@ -173,15 +173,34 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 Both run the same kernels in the same order.
  *  H2W_OPT_COOP   1 (default): a matvec is one cooperative launch with grid
  *                 barriers between its phases; 0: one launch per phase.
+ *  H2W_OPT_MULTI_XW  gathered columns per target of the multi-vector
+ *                 stream before a target is split into atomically
+ *                 accumulated column chunks (multiple of 4, 32..2048;
+ *                 default 1024). Setting it after assembly re-cuts the
+ *                 stream (host work and small uploads; the operator is kept).
+ *  H2W_OPT_ROW_SPLIT  rows x width per target of the single-vector stream
+ *                 before it is cut into row chunks (default 16384); also
+ *                 re-cuts after assembly.
  *  H2W_OPT_IR_RESIDUAL  precision of the refinement residuals after the
  *                 first in h2w_gmres_ir_batch: H2W_PREC_FP64 (default) or
  *                 H2W_PREC_DF64. (The first residual, at the caller's x0, is
  *                 formed with the FP32 operator and is not tested for
  *                 convergence; the inner solve only needs it to the inner
  *                 tolerance.) */
-enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2 };
+enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
+
+/* Autotuner (no counterpart in the reference): times `reps` products per
+ * candidate target granularity on this operator and this GPU and keeps the
+ * fastest. nrhs > 1: the multi-vector stream's column cap (256, 512, 1024,
+ * 2048) at `precision` (FP32, FP64 or DF64) for blocks of nrhs columns;
+ * nrhs == 1: the single-vector stream's row split (4096 ... 65536) at FP32 or
+ * FP64. precision H2W_TUNE_IR_MIX (nrhs > 1): the batched refinement's mix,
+ * four FP32 products and one DF64 product per timed repetition. chosen /
+ * best_ms (may be NULL): the kept value and its ms per repetition. */
+enum { H2W_TUNE_IR_MIX = 16 };
+int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chosen, double *best_ms);
 
 /* Launch statistics of the block-row GEMV kernel that performs every matvec
  * pass. While enabled, each phase launch is bracketed by CUDA events on its

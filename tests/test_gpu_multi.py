@@ -77,7 +77,10 @@ def test_multi_matvec_device_pointers(gpu):
     yd = torch.empty_like(xd)
     op.matvec_device(xd.data_ptr(), yd.data_ptr(), nrhs=24)
     torch.cuda.synchronize()
-    assert np.array_equal(yd.cpu().numpy().T, Yh)
+    Yd = yd.cpu().numpy().T
+    # equal up to the order of atomically accumulated column splits
+    for c in range(24):
+        assert np.linalg.norm(Yd[:, c] - Yh[:, c]) / np.linalg.norm(Yh[:, c]) < 1e-14
 
 
 @pytest.mark.gpu
