@@ -92,6 +92,12 @@ def lib():
         "h2w_profile": [P, I],
         "h2w_profile_multi": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(D)],
         "h2w_set_option": [P, I, I64],
+        "h2w_batch_create": [P, I, ctypes.POINTER(P)],
+        "h2w_batch_destroy": [P],
+        "h2w_batch_offsets": [P, P],
+        "h2w_batch_matvec": [P, P, P, I, I],
+        "h2w_batch_gmres": [P, P, P, I, I, I, P, P],
+        "h2w_batch_gmres_ir": [P, P, P, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), P],
         "h2w_autotune": [P, I, I, I, ctypes.POINTER(I64), ctypes.POINTER(D)],
         "h2w_get_option": [P, I, ctypes.POINTER(I64)],
         "h2w_profile_phases": [P, I, I, P, P, P, ctypes.POINTER(I)],
@@ -102,6 +108,8 @@ def lib():
         f.restype = I
     L.h2w_launch_count.argtypes = []
     L.h2w_launch_count.restype = I64
+    L.h2w_batch_last_error.argtypes = [P]
+    L.h2w_batch_last_error.restype = ctypes.c_char_p
     L.h2w_last_error.argtypes = [P]
     L.h2w_last_error.restype = ctypes.c_char_p
     _lib = L
@@ -349,6 +357,74 @@ class H2Operator:
                                       inner_iter, tol_pow, where, ctypes.byref(oi), ctypes.byref(ii), _ptr(res))
         self._ck(rc, allow=(ERR_NOT_CONVERGED,))
         return oi.value, ii.value, res
+
+
+class Batch:
+    """Many assembled operators run together (one cooperative launch per
+    product, lockstep solvers over concatenated vectors)."""
+
+    def __init__(self, ops):
+        self.ops = list(ops)  # keeps the handles alive
+        arr = (ctypes.c_void_p * len(self.ops))(*[o.h.value for o in self.ops])
+        b = ctypes.c_void_p()
+        rc = lib().h2w_batch_create(arr, len(self.ops), ctypes.byref(b))
+        if rc != OK:
+            raise H2WError(rc, "h2w_batch_create failed (handles must be assembled, on one device)")
+        self.b = b
+        self.off = np.zeros(len(self.ops) + 1, dtype=np.int64)
+        self._ck(lib().h2w_batch_offsets(self.b, _ptr(self.off)))
+        self.N = int(self.off[-1])
+
+    def _ck(self, rc, allow=()):
+        if rc != OK and rc not in allow:
+            raise H2WError(rc, lib().h2w_batch_last_error(self.b).decode())
+
+    def close(self):
+        if getattr(self, "b", None):
+            lib().h2w_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def split(self, v):
+        return [v[self.off[p]:self.off[p + 1]] for p in range(len(self.ops))]
+
+    def matvec(self, x, precision=PREC_FP64):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        self._ck(lib().h2w_batch_matvec(self.b, _ptr(x), _ptr(y), precision, HOST))
+        return y
+
+    def matvec_device(self, x_ptr, y_ptr, precision=PREC_FP64):
+        self._ck(lib().h2w_batch_matvec(self.b, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), precision, DEVICE))
+
+    def gmres(self, b, x0=None, max_iter=200, tol_pow=10):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.ones(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        it = np.zeros(len(self.ops), dtype=np.int32)
+        res = np.zeros(len(self.ops))
+        rc = lib().h2w_batch_gmres(self.b, _ptr(b), _ptr(x), max_iter, tol_pow, HOST, _ptr(it), _ptr(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return x, it, res
+
+    def gmres_ir(self, b, x0=None, max_outer=20, inner_iter=100, tol_pow=10, where=HOST, b_ptr=None, x_ptr=None):
+        oi, ii = ctypes.c_int(), ctypes.c_int()
+        res = np.zeros(len(self.ops))
+        if b_ptr is not None:
+            rc = lib().h2w_batch_gmres_ir(self.b, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), max_outer,
+                                          inner_iter, tol_pow, where, ctypes.byref(oi), ctypes.byref(ii), _ptr(res))
+            self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+            return None, oi.value, ii.value, res
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.ones(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        rc = lib().h2w_batch_gmres_ir(self.b, _ptr(b), _ptr(x), max_outer, inner_iter, tol_pow, HOST,
+                                      ctypes.byref(oi), ctypes.byref(ii), _ptr(res))
+        self._ck(rc, allow=(ERR_NOT_CONVERGED,))
+        return x, oi.value, ii.value, res
 
 
 class _TreeView:

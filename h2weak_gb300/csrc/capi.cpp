@@ -1904,6 +1904,224 @@ void check_device_error(h2w_handle *h) {
     }
 }
 
+// ------------------------------------------------ many independent problems
+}  // namespace
+
+// A batch of assembled operators on one device, run together: one merged
+// record stream (every problem's single-vector targets, phase-aligned at the
+// leaf end, heaviest first within a merged phase) drives one cooperative
+// launch per product; the solvers run every problem's GMRES in lockstep over
+// concatenated vectors. The handles must outlive the batch and must not be
+// re-assembled while it exists.
+struct h2w_batch {
+    std::vector<h2w_handle *> hs;
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int64_t Ntot = 0;
+    std::vector<int64_t> off, wsoff;        // P+1: vector and workspace offsets
+    std::vector<int> unfused;               // problems whose leaf rows need an explicit scatter
+    DBuf<int64_t> roff, blob, pstart;
+    int nphase = 0;
+    DBuf<BatchProb> tab64_orig, tab64_leaf, tab32_orig, tab32_leaf;
+    DBuf<double> ws64;
+    DBuf<float> ws32;
+    DBuf<unsigned> bar;
+    DBuf<int32_t> errf;
+    DBuf<int64_t> perm_all;                 // global leaf position -> global original position
+    DBuf<double> sx, sy, bl, xl, r, d;      // staging and solver vectors (Ntot each)
+    // segmented GMRES state
+    DBuf<double> V, w, vcur, H, cs, sn, s, part, hsum, normb, resid, y, onorm, ores;
+    DBuf<int32_t> conv, iter, bprob, pblk;
+    DBuf<int64_t> brow;
+    int g_m = -1, nblk = 0;
+};
+
+namespace {
+
+template <class F>
+int bguarded(h2w_batch *b, F &&f) {
+    if (!b) return H2W_ERR_ARG;
+    try {
+        if (cudaSetDevice(b->device) != cudaSuccess) {
+            b->err = "cudaSetDevice failed";
+            return H2W_ERR_CUDA;
+        }
+        return f();
+    } catch (const ApiError &e) {
+        b->err = e.what();
+        return e.code;
+    } catch (const CudaError &e) {
+        b->err = e.what();
+        return H2W_ERR_CUDA;
+    } catch (const std::bad_alloc &) {
+        b->err = "host allocation failed";
+        return H2W_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        b->err = e.what();
+        return H2W_ERR_ARG;
+    }
+}
+
+void batch_check_error(h2w_batch *b) {
+    int32_t e = 0;
+    CK(cudaMemcpyAsync(&e, b->errf.p, 4, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    if (e) {
+        CK(cudaMemsetAsync(b->errf.p, 0, 4, b->stream));
+        CK(cudaMemsetAsync(b->bar.p, 0, 8, b->stream));
+        throw ApiError(H2W_ERR_CUDA, "batch matvec: a grid-barrier wait ran out (device error flag)");
+    }
+}
+
+// y = A x for every problem: x, y concatenated, leaf order (leaf) or each
+// problem's original point order.
+void run_batch(h2w_batch *b, int prec, const double *x, double *y, bool leaf, const int32_t *active = nullptr) {
+    cudaStream_t st = b->stream;
+    const bool f32 = prec == H2W_PREC_FP32;
+    const int P = (int)b->hs.size();
+    if (f32 && !b->tab32_orig.p) {
+        if (!b->ws32.p) b->ws32.alloc((size_t)b->wsoff[(size_t)P]);
+        std::vector<BatchProb> to(P), tl(P);
+        for (int p = 0; p < P; ++p) {
+            ensure_f32(b->hs[(size_t)p]);
+            to[(size_t)p] = {b->hs[(size_t)p]->d_op32.p, b->ws32.p + b->wsoff[(size_t)p], b->hs[(size_t)p]->d_perm.p,
+                             b->off[(size_t)p]};
+            tl[(size_t)p] = to[(size_t)p];
+            tl[(size_t)p].perm = nullptr;
+        }
+        b->tab32_orig.upload(to, st);
+        b->tab32_leaf.upload(tl, st);
+    }
+    const BatchProb *tab = f32 ? (leaf ? b->tab32_leaf.p : b->tab32_orig.p) : (leaf ? b->tab64_leaf.p : b->tab64_orig.p);
+    if (f32) CK(cudaMemsetAsync(b->ws32.p, 0, (size_t)b->wsoff[(size_t)P] * 4, st));
+    else CK(cudaMemsetAsync(b->ws64.p, 0, (size_t)b->wsoff[(size_t)P] * 8, st));
+    if (f32)
+        CK(launch_brgb_f32(b->roff.p, b->blob.p, b->pstart.p, b->nphase, tab, active, x, y, b->bar.p, b->errf.p, st));
+    else
+        CK(launch_brgb_f64(b->roff.p, b->blob.p, b->pstart.p, b->nphase, tab, active, x, y, b->bar.p, b->errf.p, st));
+    for (int p : b->unfused) {
+        h2w_handle *h = b->hs[(size_t)p];
+        const int64_t N = h->tree.N, o = b->off[(size_t)p], w0 = b->wsoff[(size_t)p] + h->yperm_off;
+        if (f32) {
+            if (leaf) CK(vec_f32_to_f64(b->ws32.p + w0, y + o, N, st));
+            else CK(launch_scatter_f32(b->ws32.p + w0, y + o, h->d_perm.p, N, st));
+        } else {
+            if (leaf) CK(cudaMemcpyAsync(y + o, b->ws64.p + w0, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+            else CK(launch_scatter_f64(b->ws64.p + w0, y + o, h->d_perm.p, N, st));
+        }
+    }
+}
+
+GmresSeg gms_state(h2w_batch *b, int m) {
+    const int P = (int)b->hs.size();
+    const int64_t N = b->Ntot;
+    if (b->g_m != m) {
+        b->V.alloc((size_t)N * (size_t)(m + 1));
+        b->w.alloc((size_t)N);
+        b->vcur.alloc((size_t)N);
+        b->H.alloc((size_t)P * (size_t)(m + 1) * (size_t)m);
+        b->cs.alloc((size_t)P * (m + 1));
+        b->sn.alloc((size_t)P * (m + 1));
+        b->s.alloc((size_t)P * (m + 1));
+        b->part.alloc((size_t)b->nblk * (m + 1));
+        b->hsum.alloc((size_t)P * (m + 1));
+        b->y.alloc((size_t)P * (m + 1));
+        b->g_m = m;
+    }
+    GmresSeg g;
+    g.V = b->V.p;
+    g.w = b->w.p;
+    g.vcur = b->vcur.p;
+    g.H = b->H.p;
+    g.cs = b->cs.p;
+    g.sn = b->sn.p;
+    g.s = b->s.p;
+    g.part = b->part.p;
+    g.hsum = b->hsum.p;
+    g.normb = b->normb.p;
+    g.resid = b->resid.p;
+    g.y = b->y.p;
+    g.conv = b->conv.p;
+    g.iter = b->iter.p;
+    g.bprob = b->bprob.p;
+    g.brow = b->brow.p;
+    g.pblk = b->pblk.p;
+    g.Ntot = N;
+    g.m = m;
+    g.P = P;
+    g.nblk = b->nblk;
+    return g;
+}
+
+// Every problem's GMRES in lockstep on concatenated leaf-order vectors: bl
+// right-hand sides, xl initial guesses (updated; x0_zero: no initial product).
+int gms_run(h2w_batch *b, const double *bl, double *xl, int max_iter, double tol, int prec, bool x0_zero, int *iters,
+            double *resid) {
+    if (max_iter < 1 || max_iter > 400) throw ApiError(H2W_ERR_ARG, "batch GMRES: max_iter must be in 1..400");
+    const int P = (int)b->hs.size();
+    GmresSeg g = gms_state(b, max_iter);
+    cudaStream_t st = b->stream;
+    CK(gms_norms(g, bl, g.normb, 1, st));
+    if (x0_zero) {
+        CK(gms_start(g, bl, nullptr, tol, st));
+    } else {
+        run_batch(b, prec, xl, b->r.p, true);
+        CK(gms_start(g, bl, b->r.p, tol, st));
+    }
+    std::vector<int32_t> conv((size_t)P);
+    auto read_conv = [&] {
+        CK(cudaMemcpyAsync(conv.data(), g.conv, (size_t)P * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int p = 0; p < P; ++p)
+            if (conv[(size_t)p] == -1) return false;
+        return true;
+    };
+    bool done = read_conv();
+    int last = -1;
+    for (int i = 0; i < max_iter && !done; ++i) {
+        run_batch(b, prec, g.vcur, g.w, true, g.conv);  // converged problems are skipped
+        CK(gms_arnoldi(g, tol, st));
+        last = i;
+        done = read_conv();
+    }
+    int kmax = -1;
+    for (int p = 0; p < P; ++p) {
+        const int cv = conv[(size_t)p];
+        kmax = std::max(kmax, cv >= 0 ? cv : (cv == -1 ? last : -1));
+    }
+    CK(gms_finish(g, xl, last, kmax, st));
+    std::vector<double> rs((size_t)P);
+    CK(cudaMemcpyAsync(rs.data(), g.resid, (size_t)P * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    batch_check_error(b);
+    bool all = true;
+    for (int p = 0; p < P; ++p) {
+        const int cv = conv[(size_t)p];
+        if (iters) iters[p] = cv >= 0 ? cv + 1 : (cv == -2 ? 0 : last + 1);
+        if (resid) resid[p] = rs[(size_t)p];
+        if (cv == -1) all = false;
+    }
+    return all ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+}
+
+// Concatenated vectors in (stage from host) and out, gathered to leaf order
+// for the solvers.
+void batch_in(h2w_batch *b, const double *v, double *leaf, int where) {
+    const double *src = v;
+    if (where == H2W_HOST) {
+        CK(cudaMemcpyAsync(b->sx.p, v, (size_t)b->Ntot * 8, cudaMemcpyHostToDevice, b->stream));
+        src = b->sx.p;
+    }
+    CK(launch_gather64(src, leaf, b->perm_all.p, b->Ntot, b->stream));
+}
+void batch_out(h2w_batch *b, const double *leaf, double *v, int where) {
+    double *dst = where == H2W_HOST ? b->sy.p : v;
+    CK(launch_scatter64(leaf, dst, b->perm_all.p, b->Ntot, b->stream));
+    if (where == H2W_HOST) CK(cudaMemcpyAsync(v, b->sy.p, (size_t)b->Ntot * 8, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+}
+
 // Column blocks of up to 64 right-hand sides: stage (host) and pack into
 // interleaved leaf order, run f on the block, unpack x back.
 template <class F>
@@ -2706,6 +2924,232 @@ int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chos
         if (chosen) *chosen = best;
         if (best_ms) *best_ms = bms;
         return H2W_OK;
+    });
+}
+
+int h2w_batch_create(h2w_handle *const *handles, int n, h2w_batch **out) {
+    if (!handles || n < 1 || !out) return H2W_ERR_ARG;
+    *out = nullptr;
+    if (n >= (1 << 22)) return H2W_ERR_ARG;
+    auto *b = new h2w_batch();
+    b->hs.assign(handles, handles + n);
+    for (h2w_handle *h : b->hs)
+        if (!h || !h->has_op || !h->plan || h->cfg.device != b->hs[0]->cfg.device) {
+            delete b;
+            return H2W_ERR_STATE;
+        }
+    b->device = b->hs[0]->cfg.device;
+    int rc = bguarded(b, [&] {
+        CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+        const int P = n;
+        b->off.assign((size_t)P + 1, 0);
+        b->wsoff.assign((size_t)P + 1, 0);
+        for (int p = 0; p < P; ++p) {
+            b->off[(size_t)p + 1] = b->off[(size_t)p] + b->hs[(size_t)p]->tree.N;
+            b->wsoff[(size_t)p + 1] = b->wsoff[(size_t)p] + b->hs[(size_t)p]->ws_n;
+        }
+        b->Ntot = b->off[(size_t)P];
+        // per problem: its single-vector stream with the problem index in the flags
+        struct Rec { int slot; double size; std::vector<int64_t> words; };
+        std::vector<std::vector<Rec>> per((size_t)P);
+        size_t maxph = 0;
+        std::vector<size_t> nph((size_t)P);
+        for (int p = 0; p < P; ++p) {
+            h2w_handle *h = b->hs[(size_t)p];
+            PlanBuilder &pb = *h->plan;
+            std::vector<Phase> ph;
+            bool fused = true;
+            pb.realize(h->row_split, 4, XW_CAP);
+            assign_phases(h, pb, h->nph_total, ph, fused);
+            validate_plan(pb, h, ph);
+            if (!fused) b->unfused.push_back(p);
+            for (Target &t : pb.T) t.flags |= (p << 8);
+            std::vector<int64_t> ro, bl, ps;
+            pack_records(pb, ph, ro, bl, ps);
+            nph[(size_t)p] = ph.size();
+            maxph = std::max(maxph, ph.size());
+            for (size_t j = 0; j < ph.size(); ++j)
+                for (int64_t t = ph[j].t0; t < ph[j].t1; ++t) {
+                    const Target &tg = pb.T[(size_t)t];
+                    Rec r;
+                    r.slot = (int)j;
+                    r.size = (double)tg.nrows * (double)tg.xw;
+                    r.words.assign(bl.begin() + ro[(size_t)t], bl.begin() + ro[(size_t)t + 1]);
+                    per[(size_t)p].push_back(std::move(r));
+                }
+            pb.T = std::vector<Target>();
+            pb.P = std::vector<Panel>();
+            pb.S = std::vector<Seg>();
+        }
+        // merged phases, aligned at the leaf end; heaviest first within a phase
+        std::vector<std::vector<std::pair<double, const Rec *>>> slots(maxph);
+        for (int p = 0; p < P; ++p)
+            for (const Rec &r : per[(size_t)p])
+                slots[(size_t)r.slot + (maxph - nph[(size_t)p])].push_back({r.size, &r});
+        std::vector<int64_t> roff{0}, blob, pstart;
+        for (auto &sl : slots) {
+            std::stable_sort(sl.begin(), sl.end(), [](const auto &a, const auto &c) { return a.first > c.first; });
+            pstart.push_back((int64_t)roff.size() - 1);
+            for (auto &e : sl) {
+                blob.insert(blob.end(), e.second->words.begin(), e.second->words.end());
+                roff.push_back((int64_t)blob.size());
+            }
+        }
+        pstart.push_back((int64_t)roff.size() - 1);
+        b->nphase = (int)maxph;
+        cudaStream_t st = b->stream;
+        b->roff.upload(roff, st);
+        b->blob.upload(blob, st);
+        b->pstart.upload(pstart, st);
+        b->ws64.alloc((size_t)b->wsoff[(size_t)P]);
+        std::vector<BatchProb> to((size_t)P), tl((size_t)P);
+        for (int p = 0; p < P; ++p) {
+            h2w_handle *h = b->hs[(size_t)p];
+            to[(size_t)p] = {h->d_op.p, b->ws64.p + b->wsoff[(size_t)p], h->d_perm.p, b->off[(size_t)p]};
+            tl[(size_t)p] = to[(size_t)p];
+            tl[(size_t)p].perm = nullptr;
+        }
+        b->tab64_orig.upload(to, st);
+        b->tab64_leaf.upload(tl, st);
+        std::vector<int64_t> pa((size_t)b->Ntot);
+        for (int p = 0; p < P; ++p) {
+            const auto &pm = b->hs[(size_t)p]->tree.perm;
+            for (size_t t = 0; t < pm.size(); ++t) pa[(size_t)b->off[(size_t)p] + t] = b->off[(size_t)p] + pm[t];
+        }
+        b->perm_all.upload(pa, st);
+        b->bar.alloc(2);
+        CK(cudaMemsetAsync(b->bar.p, 0, 8, st));
+        b->errf.alloc(1);
+        CK(cudaMemsetAsync(b->errf.p, 0, 4, st));
+        for (DBuf<double> *v : {&b->sx, &b->sy, &b->bl, &b->xl, &b->r, &b->d}) v->alloc((size_t)b->Ntot);
+        // segmented GMRES blocks: about 2048 rows each, never across problems
+        std::vector<int32_t> bprob, pblk{0};
+        std::vector<int64_t> brow{0};
+        for (int p = 0; p < P; ++p) {
+            const int64_t Np = b->hs[(size_t)p]->tree.N;
+            const int64_t nb = std::max<int64_t>(1, (Np + 2047) / 2048);
+            for (int64_t q = 0; q < nb; ++q) {
+                bprob.push_back(p);
+                brow.push_back(b->off[(size_t)p] + std::min(Np, (q + 1) * ((Np + nb - 1) / nb)));
+            }
+            pblk.push_back((int32_t)bprob.size());
+        }
+        b->nblk = (int)bprob.size();
+        b->bprob.upload(bprob, st);
+        b->brow.upload(brow, st);
+        b->pblk.upload(pblk, st);
+        for (DBuf<double> *v : {&b->normb, &b->resid, &b->onorm, &b->ores}) v->alloc((size_t)P);
+        b->conv.alloc((size_t)P);
+        b->iter.alloc(2);
+        CK(cudaStreamSynchronize(st));
+        return H2W_OK;
+    });
+    if (rc != H2W_OK) {
+        if (b->stream) cudaStreamDestroy(b->stream);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return H2W_OK;
+}
+
+int h2w_batch_destroy(h2w_batch *b) {
+    if (!b) return H2W_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    cudaStream_t st = b->stream;
+    delete b;
+    if (st) cudaStreamDestroy(st);
+    return H2W_OK;
+}
+
+const char *h2w_batch_last_error(const h2w_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int h2w_batch_offsets(h2w_batch *b, int64_t *offsets) {
+    return bguarded(b, [&] {
+        if (!offsets) throw ApiError(H2W_ERR_ARG, "null offsets");
+        for (size_t p = 0; p < b->off.size(); ++p) offsets[p] = b->off[p];
+        return H2W_OK;
+    });
+}
+
+int h2w_batch_matvec(h2w_batch *b, const double *x, double *y, int precision, int where) {
+    return bguarded(b, [&] {
+        if (!x || !y || (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32) ||
+            (where != H2W_HOST && where != H2W_DEVICE))
+            throw ApiError(H2W_ERR_ARG, "bad batch matvec arguments");
+        const double *dx = x;
+        double *dy = y;
+        if (where == H2W_HOST) {
+            CK(cudaMemcpyAsync(b->sx.p, x, (size_t)b->Ntot * 8, cudaMemcpyHostToDevice, b->stream));
+            dx = b->sx.p;
+            dy = b->sy.p;
+        }
+        run_batch(b, precision, dx, dy, false);
+        if (where == H2W_HOST) CK(cudaMemcpyAsync(y, b->sy.p, (size_t)b->Ntot * 8, cudaMemcpyDeviceToHost, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        batch_check_error(b);
+        return H2W_OK;
+    });
+}
+
+int h2w_batch_gmres(h2w_batch *b, const double *rhs, double *x, int max_iter, int tol_pow, int where, int *iters,
+                    double *resid) {
+    return bguarded(b, [&] {
+        if (!rhs || !x || (where != H2W_HOST && where != H2W_DEVICE)) throw ApiError(H2W_ERR_ARG, "bad arguments");
+        batch_in(b, rhs, b->bl.p, where);
+        batch_in(b, x, b->xl.p, where);
+        const int rc = gms_run(b, b->bl.p, b->xl.p, max_iter, std::pow(10, -1.0 * tol_pow), H2W_PREC_FP64, false,
+                               iters, resid);
+        batch_out(b, b->xl.p, x, where);
+        return rc;
+    });
+}
+
+int h2w_batch_gmres_ir(h2w_batch *b, const double *rhs, double *x, int max_outer, int inner_iter, int tol_pow,
+                       int where, int *outer_iters, int *inner_total, double *resid) {
+    return bguarded(b, [&] {
+        if (!rhs || !x || max_outer < 1 || inner_iter < 1 || !outer_iters || !inner_total || !resid ||
+            (where != H2W_HOST && where != H2W_DEVICE))
+            throw ApiError(H2W_ERR_ARG, "bad arguments");
+        const int P = (int)b->hs.size();
+        const double tol = std::pow(10, -1.0 * tol_pow);
+        cudaStream_t st = b->stream;
+        batch_in(b, rhs, b->bl.p, where);
+        batch_in(b, x, b->xl.p, where);
+        GmresSeg g = gms_state(b, inner_iter);
+        CK(gms_norms(g, b->bl.p, b->onorm.p, 1, st));
+        std::vector<double> nb((size_t)P), nr((size_t)P);
+        CK(cudaMemcpyAsync(nb.data(), b->onorm.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st));
+        *outer_iters = 0;
+        *inner_total = 0;
+        std::vector<int> it((size_t)P);
+        bool ok = false;
+        for (int o = 0; o <= max_outer; ++o) {
+            // residual: FP32 operators at x0 (a correction only), then FP64 (the stopping test)
+            run_batch(b, o == 0 ? H2W_PREC_FP32 : H2W_PREC_FP64, b->xl.p, b->r.p, true);
+            CK(vec_axpby(1.0, b->bl.p, -1.0, b->r.p, b->r.p, b->Ntot, st));
+            if (o > 0) {
+                CK(gms_norms(g, b->r.p, b->ores.p, 0, st));
+                CK(cudaMemcpyAsync(nr.data(), b->ores.p, (size_t)P * 8, cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                ok = true;
+                for (int p = 0; p < P; ++p) {
+                    resid[p] = nr[(size_t)p] / nb[(size_t)p];
+                    if (!(resid[p] < tol)) ok = false;
+                }
+                if (ok || o == max_outer) break;
+            }
+            CK(cudaMemsetAsync(b->d.p, 0, (size_t)b->Ntot * 8, st));
+            gms_run(b, b->r.p, b->d.p, inner_iter, 1e-6, H2W_PREC_FP32, true, it.data(), nullptr);
+            int mx = 0;
+            for (int p = 0; p < P; ++p) mx = std::max(mx, it[(size_t)p]);
+            *inner_total += mx;
+            CK(vec_axpby(1.0, b->xl.p, 1.0, b->d.p, b->xl.p, b->Ntot, st));
+            *outer_iters = o + 1;
+        }
+        batch_out(b, b->xl.p, x, where);
+        return ok ? H2W_OK : H2W_ERR_NOT_CONVERGED;
     });
 }
 

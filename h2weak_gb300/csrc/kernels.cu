@@ -676,6 +676,32 @@ __global__ void __launch_bounds__(BRG_THREADS, 4)
     }
 }
 
+// Many independent problems in one cooperative launch: the problem index of
+// a target sits in bits 8.. of its record's flag word, and the target runs
+// on that problem's operator, workspace, point permutation and vector
+// segment (xoff into the concatenated input and output vectors). active
+// (may be NULL): a problem whose entry is not -1 (a converged system of the
+// lockstep solver) is skipped.
+template <class T>
+__global__ void __launch_bounds__(BRG_THREADS, 4)
+    brgb_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
+                     const int64_t *__restrict__ pstart, int nphase, const BatchProb *__restrict__ probs,
+                     const int32_t *__restrict__ active, const double *__restrict__ xin, double *yout,
+                     unsigned *bar, int32_t *err) {
+    __shared__ BrgShared<T> sh;
+    for (int p = 0; p < nphase; ++p) {
+        const int64_t t1 = pstart[p + 1];
+        for (int64_t t = pstart[p] + blockIdx.x; t < t1; t += gridDim.x) {
+            const int pid = (int)(blob[roff[t] + 1] >> 40);
+            if (active && active[pid] != -1) continue;
+            const BatchProb pr = probs[pid];
+            brg_target<T>(sh, t, roff, blob, reinterpret_cast<const T *>(pr.A), reinterpret_cast<T *>(pr.ws),
+                          xin + pr.xoff, yout + pr.xoff, pr.perm);
+        }
+        if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
+    }
+}
+
 static int g_num_sms = 0;
 
 template <class T>
@@ -735,6 +761,41 @@ cudaError_t launch_coop_f32(const int64_t *roff, const int64_t *blob, const int6
                             const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
                             unsigned *bar, int32_t *err, cudaStream_t st) {
     return launch_coop_t<float>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, st);
+}
+
+template <class T>
+static cudaError_t launch_brgb_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                                 const BatchProb *probs, const int32_t *active, const double *xin, double *yout,
+                                 unsigned *bar, int32_t *err, cudaStream_t st) {
+    if (nphase <= 0) return cudaSuccess;
+    static int per_sm = 0;
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_num_sms <= 0) g_num_sms = 1;
+    }
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, brgb_coop_kernel<T>, BRG_THREADS, 0);
+        if (per_sm <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    }
+    const int grid = g_num_sms * per_sm;
+    void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&probs,
+                    (void *)&active, (void *)&xin, (void *)&yout,  (void *)&bar,    (void *)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)brgb_coop_kernel<T>, dim3(grid), dim3(BRG_THREADS), args,
+                                                0, st);
+    count_launch();
+    return e;
+}
+cudaError_t launch_brgb_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const BatchProb *probs, const int32_t *active, const double *xin, double *yout,
+                            unsigned *bar, int32_t *err, cudaStream_t st) {
+    return launch_brgb_t<double>(roff, blob, pstart, nphase, probs, active, xin, yout, bar, err, st);
+}
+cudaError_t launch_brgb_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const BatchProb *probs, const int32_t *active, const double *xin, double *yout,
+                            unsigned *bar, int32_t *err, cudaStream_t st) {
+    return launch_brgb_t<float>(roff, blob, pstart, nphase, probs, active, xin, yout, bar, err, st);
 }
 
 cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const double *A,

@@ -90,6 +90,58 @@ cudaError_t vec_axpby(double a, const double *x, double b, const double *y, doub
 cudaError_t vec_f64_to_f32(const double *x, float *y, int64_t n, cudaStream_t st);
 cudaError_t vec_f32_to_f64(const float *x, double *y, int64_t n, cudaStream_t st);
 
+// ------------------------------------------------ many independent problems
+// One problem of a batch: its packed operator (FP64 or FP32 copy), its
+// workspace, its leaf permutation (NULL: vectors in leaf order) and the
+// offset of its segment in the concatenated input / output vectors.
+struct BatchProb {
+    const void *A;
+    void *ws;
+    const int32_t *perm;
+    int64_t xoff;
+};
+// The single-vector matvec of every problem of a batch in one cooperative
+// launch; records carry the problem index in bits 8.. of their flag word.
+// active (may be NULL): problems whose entry is not -1 are skipped.
+cudaError_t launch_brgb_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const BatchProb *probs, const int32_t *active, const double *xin, double *yout,
+                            unsigned *bar, int32_t *err, cudaStream_t st);
+cudaError_t launch_brgb_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                            const BatchProb *probs, const int32_t *active, const double *xin, double *yout,
+                            unsigned *bar, int32_t *err, cudaStream_t st);
+
+// Segmented GMRES: P independent systems in lockstep over one concatenated
+// vector (problem p owns a contiguous row range); block b works on rows
+// [brow[b], brow[b+1]) of problem bprob[b], problem p owns blocks
+// [pblk[p], pblk[p+1]).
+struct GmresSeg {
+    double *V;               // (m+1) blocks of Ntot
+    double *w, *vcur;        // Ntot
+    double *H;               // per problem p: (m+1) x m column-major at p*m*(m+1)
+    double *cs, *sn, *s;     // per problem: m+1 at p*(m+1)
+    double *part;            // nblk x (m+1) block partial sums
+    double *hsum;            // P x (m+1) per-problem sums
+    double *normb, *resid;   // P
+    double *y;               // P x (m+1) back-substituted coefficients
+    int32_t *conv;           // P: -1 running, k >= 0 converged at column k, -2 at the start
+    int32_t *iter;           // [0] current Arnoldi column, [1] steps taken
+    const int32_t *bprob;    // nblk
+    const int64_t *brow;     // nblk + 1
+    const int32_t *pblk;     // P + 1
+    int64_t Ntot;
+    int m, P, nblk;
+};
+bool gms_attr(const GmresSeg &g);
+cudaError_t gms_norms(const GmresSeg &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
+cudaError_t gms_start(const GmresSeg &g, const double *b, const double *Ax, double tol, cudaStream_t st);
+cudaError_t gms_arnoldi(const GmresSeg &g, double tol, cudaStream_t st);
+cudaError_t gms_loop(const GmresSeg &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
+cudaError_t gms_finish(const GmresSeg &g, double *x, int last, int kmax, cudaStream_t st);
+// y[idx[t]] = x[t] (scatter) / y[t] = x[idx[t]] (gather) over n elements with
+// 64-bit indices (concatenated permutations of a batch)
+cudaError_t launch_gather64(const double *x, double *y, const int64_t *idx, int64_t n, cudaStream_t st);
+cudaError_t launch_scatter64(const double *x, double *y, const int64_t *idx, int64_t n, cudaStream_t st);
+
 // ------------------------------------------------ multiple right-hand sides
 // Blocks of rp vectors are interleaved: element (t, c) at t*rp + c
 // (rp = 16, 32 or 64). The workspace holds ws_n rows of rp values.

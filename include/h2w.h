@@ -191,6 +191,33 @@ enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MUL
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
+/* Many independent problems at once (no counterpart in the reference, which
+ * runs one problem per process): a batch groups assembled handles of one
+ * device; their single-vector products run as ONE cooperative launch over a
+ * merged target stream (every problem's levels, aligned at the leaf end), and
+ * the solvers run every problem's GMRES in lockstep over concatenated vectors
+ * (each problem with its own Krylov basis, rotations and stopping test).
+ * Vectors are the problems' vectors concatenated in handle order, each in its
+ * own original point order; h2w_batch_offsets gives the n+1 offsets. The
+ * handles must outlive the batch and must not be re-assembled meanwhile. */
+typedef struct h2w_batch h2w_batch;
+int h2w_batch_create(h2w_handle *const *handles, int n, h2w_batch **out);
+int h2w_batch_destroy(h2w_batch *b);
+const char *h2w_batch_last_error(const h2w_batch *b);
+int h2w_batch_offsets(h2w_batch *b, int64_t *offsets);
+/* y = A_p x for every problem p (mat_vec_prod of each), FP64 or FP32. */
+int h2w_batch_matvec(h2w_batch *b, const double *x, double *y, int precision, int where);
+/* FP64 GMRES of every problem (iterative_solver::GMRES of each), x0 = x on
+ * entry; iters / resid: n entries. max_iter <= 400. */
+int h2w_batch_gmres(h2w_batch *b, const double *rhs, double *x, int max_iter, int tol_pow, int where, int *iters,
+                    double *resid);
+/* Mixed precision for every problem: batched FP32-operator inner GMRES (x0 =
+ * 0, relative tolerance 1e-6) and FP64 refinement (first residual with the
+ * FP32 operators, the later ones FP64 and tested); resid: n final FP64
+ * relative residuals. */
+int h2w_batch_gmres_ir(h2w_batch *b, const double *rhs, double *x, int max_outer, int inner_iter, int tol_pow,
+                       int where, int *outer_iters, int *inner_total, double *resid);
+
 /* Autotuner (no counterpart in the reference): times `reps` products per
  * candidate target granularity on this operator and this GPU and keeps the
  * fastest. nrhs > 1: the multi-vector stream's column cap (256, 512, 1024,
