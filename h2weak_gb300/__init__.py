@@ -92,6 +92,14 @@ def lib():
         "h2w_profile": [P, I],
         "h2w_profile_multi": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(D)],
         "h2w_set_option": [P, I, I64],
+        "h2w_learn_record": [P, I],
+        "h2w_learn_data": [P, P, P, ctypes.POINTER(I64)],
+        "h2w_learn_set_model": [P, P, ctypes.c_float, I],
+        "h2w_learn_stats": [P, ctypes.POINTER(I64), ctypes.POINTER(I64)],
+        "h2w_learn_detail": [P, P, ctypes.POINTER(D), ctypes.POINTER(D)],
+        "h2w_mlp_forward": [P, P, I64, P, P],
+        "h2w_mlp_grad": [P, P, P, I64, ctypes.c_float, P, P, P],
+        "h2w_mlp_adam": [P, P, P, P, I, ctypes.c_float, P],
         "h2w_batch_create": [P, I, ctypes.POINTER(P)],
         "h2w_batch_destroy": [P],
         "h2w_batch_offsets": [P, P],
@@ -106,6 +114,8 @@ def lib():
         f = getattr(L, name)
         f.argtypes = args
         f.restype = I
+    L.h2w_mlp_nparam.argtypes = []
+    L.h2w_mlp_nparam.restype = I
     L.h2w_launch_count.argtypes = []
     L.h2w_launch_count.restype = I64
     L.h2w_batch_last_error.argtypes = [P]
@@ -219,6 +229,36 @@ class H2Operator:
         return b.value
 
     # instrumentation
+    # learned NCA proposals
+    def learn_record(self, enable=True):
+        self._ck(lib().h2w_learn_record(self.h, 1 if enable else 0))
+
+    def learn_data(self):
+        """Recorded (features n x 16 float32, labels n uint8) of plain NCA assemblies."""
+        n = ctypes.c_int64()
+        self._ck(lib().h2w_learn_data(self.h, None, None, ctypes.byref(n)))
+        X = np.empty((n.value, 16), dtype=np.float32)
+        y = np.empty(n.value, dtype=np.uint8)
+        self._ck(lib().h2w_learn_data(self.h, _ptr(X), _ptr(y), ctypes.byref(n)))
+        return X, y
+
+    def learn_set_model(self, params, calib=1.0, margin=2):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._ck(lib().h2w_learn_set_model(self.h, _ptr(p), float(calib), int(margin)))
+
+    def learn_detail(self):
+        """(rejections: no pivots / non-finite / test failed, mean proposal size, mean pivots kept)."""
+        r = np.zeros(3, dtype=np.int64)
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._ck(lib().h2w_learn_detail(self.h, _ptr(r), ctypes.byref(a), ctypes.byref(b)))
+        return r, a.value, b.value
+
+    def learn_stats(self):
+        """(blocks proposed, blocks accepted) since the last call."""
+        b, a = ctypes.c_int64(), ctypes.c_int64()
+        self._ck(lib().h2w_learn_stats(self.h, ctypes.byref(b), ctypes.byref(a)))
+        return b.value, a.value
+
     def autotune(self, nrhs=64, precision=PREC_FP32, reps=3):
         """Time each candidate target granularity and keep the fastest;
         returns (chosen value, ms per repetition)."""

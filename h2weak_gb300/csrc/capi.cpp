@@ -152,6 +152,17 @@ struct h2w_handle {
     std::vector<LoopGraph> loops;
     bool use_graphs = true, graph_failed = false;
     int ir_resid_prec = H2W_PREC_FP64;   // refinement residuals after the first (batched IR)
+    // learned NCA proposals: model, assembly switch, training-data recorder, statistics
+    DBuf<float> d_mlp;
+    float mlp_calib = 1.f;
+    int mlp_margin = 2;
+    bool learned = false, learn_rec = false;
+    std::vector<float> rec_X;
+    std::vector<uint8_t> rec_y;
+    int64_t learn_blocks = 0, learn_accepted = 0;
+    int64_t learn_reject[3] = {0, 0, 0};  // no usable pivots, non-finite, stopping test failed
+    double learn_rhat = 0.0, learn_r1 = 0.0;
+    double learn_ms = 0.0;
     cudaStream_t stream = nullptr;
 
     KParams kparams() const {
@@ -270,8 +281,14 @@ void append(std::vector<int32_t> &a, const int32_t *b, int64_t n) { a.insert(a.e
 
 // ------------------------------------------------------------ NCA runs ---
 // Run the batched NCA on problems (R[p], C[p]); returns local pivots.
-void run_nca(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
-             std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
+void record_blocks(h2w_handle *h, const std::vector<NcaProb> &probs, const DBuf<int32_t> &di,
+                   const std::vector<std::vector<int32_t>> &prow, const std::vector<std::vector<int32_t>> &pcol,
+                   size_t p0);
+
+// The NCA pivot search, one CTA per block (nca_kernel), in batches that fit
+// the scratch budget.
+void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+                   std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
     const size_t np = R.size();
     prow.assign(np, {});
     pcol.assign(np, {});
@@ -339,8 +356,167 @@ void run_nca(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const st
             prow[p0 + q].assign(hpr.begin() + pb.piv, hpr.begin() + pb.piv + rk[q]);
             pcol[p0 + q].assign(hpc.begin() + pb.piv, hpc.begin() + pb.piv + rk[q]);
         }
+        if (h->learn_rec) record_blocks(h, probs, di, prow, pcol, p0);
         p0 = p;
     }
+}
+
+// Training data: the learned model's features of every candidate point of
+// these blocks, labelled 1 where the NCA chose the point as a pivot.
+void record_blocks(h2w_handle *h, const std::vector<NcaProb> &probs, const DBuf<int32_t> &di,
+                   const std::vector<std::vector<int32_t>> &prow, const std::vector<std::vector<int32_t>> &pcol,
+                   size_t p0) {
+    std::vector<LearnProb> lp(probs.size());
+    int64_t xo = 0;
+    for (size_t q = 0; q < probs.size(); ++q) {
+        LearnProb &l = lp[q];
+        std::memset(&l, 0, sizeof(l));
+        l.ri = probs[q].ri;
+        l.ci = probs[q].ci;
+        l.n1 = probs[q].n1;
+        l.n2 = probs[q].n2;
+        l.xo = xo;
+        xo += l.n1 + l.n2;
+    }
+    DBuf<LearnProb> dl;
+    DBuf<float> dx;
+    dl.upload(lp, h->stream);
+    dx.alloc((size_t)xo * LRN_F);
+    CK(launch_learn_features(dl.p, (int)lp.size(), di.p, h->kparams(), h->cfg.tol_pow, dx.p, h->stream));
+    const size_t base = h->rec_y.size();
+    h->rec_X.resize((base + (size_t)xo) * LRN_F);
+    h->rec_y.resize(base + (size_t)xo, 0);
+    CK(cudaMemcpyAsync(h->rec_X.data() + base * LRN_F, dx.p, (size_t)xo * LRN_F * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t q = 0; q < lp.size(); ++q) {
+        for (int32_t i : prow[p0 + q]) h->rec_y[base + (size_t)lp[q].xo + (size_t)i] = 1;
+        for (int32_t j : pcol[p0 + q]) h->rec_y[base + (size_t)lp[q].xo + (size_t)lp[q].n1 + (size_t)j] = 1;
+    }
+}
+
+// Learned proposals for every block (see learn.cu); blocks the NCA stopping
+// test rejects go to the plain search.
+void run_nca_learned(h2w_handle *h, const std::vector<std::vector<int32_t>> &R,
+                     const std::vector<std::vector<int32_t>> &C, std::vector<std::vector<int32_t>> &prow,
+                     std::vector<std::vector<int32_t>> &pcol) {
+    const size_t np = R.size();
+    prow.assign(np, {});
+    pcol.assign(np, {});
+    const double tol = std::pow(10, -1.0 * h->cfg.tol_pow);
+    const size_t budget = (size_t)3 << 30;
+    KParams kp = h->kparams();
+    cudaStream_t st = h->stream;
+    std::vector<size_t> rejected;
+    size_t p0 = 0;
+    while (p0 < np) {
+        std::vector<LearnProb> probs;
+        std::vector<int32_t> idx;
+        std::vector<LearnTile> tiles;
+        int64_t scr = 0, xo = 0, piv = 0;
+        int mw1 = 1, mw2 = 1, mw3 = 1;
+        size_t p = p0;
+        for (; p < np; ++p) {
+            const int n1 = (int)R[p].size(), n2 = (int)C[p].size();
+            const int cap = std::min(std::min(n1, n2), LRN_CAP);
+            const int64_t need = 2 * (int64_t)cap * (n1 + n2) + 3 * (int64_t)cap * cap;
+            if (!probs.empty() && (size_t)(scr + need) * 8 + (size_t)(xo + n1 + n2) * (LRN_F + 1) * 4 > budget) break;
+            LearnProb l;
+            std::memset(&l, 0, sizeof(l));
+            l.ri = (int64_t)idx.size();
+            append(idx, R[p].data(), n1);
+            l.ci = (int64_t)idx.size();
+            append(idx, C[p].data(), n2);
+            l.xo = xo;
+            xo += n1 + n2;
+            l.ac = scr; scr += (int64_t)cap * n1;
+            l.ar = scr; scr += (int64_t)cap * n2;
+            l.uu = scr; scr += (int64_t)cap * n1;
+            l.vv = scr; scr += (int64_t)cap * n2;
+            l.ff = scr; scr += (int64_t)cap * cap;
+            l.gu = scr; scr += (int64_t)cap * cap;
+            l.gv = scr; scr += (int64_t)cap * cap;
+            l.piv = piv;
+            piv += cap + 1;
+            l.n1 = n1;
+            l.n2 = n2;
+            l.cap = cap;
+            const int b = (int)probs.size();
+            for (int64_t e = 0; e < (int64_t)n1 * cap; e += 8192)
+                tiles.push_back({b, 0, (int32_t)e, (int32_t)std::min<int64_t>(8192, (int64_t)n1 * cap - e)});
+            for (int64_t e = 0; e < (int64_t)n2 * cap; e += 8192)
+                tiles.push_back({b, 1, (int32_t)e, (int32_t)std::min<int64_t>(8192, (int64_t)n2 * cap - e)});
+            for (int e = 0; e < n1; e += 64) tiles.push_back({b, 2, e, std::min(64, n1 - e)});
+            for (int e = 0; e < n2; e += 64) tiles.push_back({b, 3, e, std::min(64, n2 - e)});
+            mw1 = std::max(mw1, (std::max(n1, n2) + 31) / 32);
+            mw2 = std::max(mw2, (n1 + 31) / 32 + (n2 + 31) / 32);
+            mw3 = std::max(mw3, (n2 + 31) / 32);
+            probs.push_back(l);
+        }
+        const int nb = (int)probs.size();
+        DBuf<LearnProb> dp;
+        DBuf<LearnTile> dt;
+        DBuf<int32_t> di, dpr, dpc, doi, doj, dor, doc;
+        DBuf<LearnState> dls;
+        DBuf<double> dscr;
+        DBuf<float> dx, dz;
+        dp.upload(probs, st);
+        dt.upload(tiles, st);
+        di.upload(idx, st);
+        for (DBuf<int32_t> *v : {&dpr, &dpc, &doi, &doj, &dor, &doc}) v->alloc((size_t)piv);
+        dls.alloc((size_t)nb);
+        dscr.alloc((size_t)scr);
+        CK(cudaMemsetAsync(dscr.p, 0, (size_t)scr * 8, st));
+        dx.alloc((size_t)xo * LRN_F);
+        dz.alloc((size_t)xo);
+        CK(launch_learn_features(dp.p, nb, di.p, kp, h->cfg.tol_pow, dx.p, st));
+        CK(launch_mlp_forward(h->d_mlp.p, dx.p, xo, dz.p, st));
+        CK(launch_learn_propose(dp.p, nb, dz.p, h->mlp_calib, h->mlp_margin, dpr.p, dpc.p, dls.p, mw1, st));
+        CK(launch_learn_fill(dt.p, (int)tiles.size(), dp.p, di.p, kp, dpr.p, doj.p, dls.p, dscr.p, 1, st));
+        CK(launch_learn_aca(dp.p, nb, tol, dscr.p, doi.p, doj.p, dls.p, mw3, st));
+        CK(launch_learn_fill(dt.p, (int)tiles.size(), dp.p, di.p, kp, dpr.p, doj.p, dls.p, dscr.p, 0, st));
+        CK(launch_learn_solve(dt.p, (int)tiles.size(), dp.p, doi.p, doj.p, dls.p, dscr.p, st));
+        CK(launch_learn_gram(dt.p, (int)tiles.size(), dp.p, dls.p, dscr.p, st));
+        CK(launch_learn_test(dp.p, nb, di.p, kp, tol, dpr.p, dpc.p, doi.p, doj.p, dls.p, dscr.p, dor.p, doc.p, mw2, st));
+        std::vector<LearnState> ls((size_t)nb);
+        std::vector<int32_t> hr((size_t)piv), hc((size_t)piv);
+        CK(cudaMemcpyAsync(ls.data(), dls.p, (size_t)nb * sizeof(LearnState), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hr.data(), dor.p, (size_t)piv * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hc.data(), doc.p, (size_t)piv * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int q = 0; q < nb; ++q) {
+            const LearnState &s = ls[(size_t)q];
+            h->learn_rhat += s.rhat;
+            h->learn_r1 += s.r1;
+            if (!s.accept) ++h->learn_reject[s.rank == -1 ? 0 : (s.rank == -2 ? 1 : 2)];
+            if (s.accept && s.rank > 0) {
+                prow[p0 + q].assign(hr.begin() + probs[(size_t)q].piv, hr.begin() + probs[(size_t)q].piv + s.rank);
+                pcol[p0 + q].assign(hc.begin() + probs[(size_t)q].piv, hc.begin() + probs[(size_t)q].piv + s.rank);
+                ++h->learn_accepted;
+            } else {
+                rejected.push_back(p0 + q);
+            }
+        }
+        h->learn_blocks += nb;
+        p0 = p;
+    }
+    if (!rejected.empty()) {
+        std::vector<std::vector<int32_t>> R2, C2, pr2, pc2;
+        for (size_t q : rejected) {
+            R2.push_back(R[q]);
+            C2.push_back(C[q]);
+        }
+        run_nca_plain(h, R2, C2, pr2, pc2);
+        for (size_t k = 0; k < rejected.size(); ++k) {
+            prow[rejected[k]] = std::move(pr2[k]);
+            pcol[rejected[k]] = std::move(pc2[k]);
+        }
+    }
+}
+
+void run_nca(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+             std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
+    if (h->learned) run_nca_learned(h, R, C, prow, pcol);
+    else run_nca_plain(h, R, C, prow, pcol);
 }
 
 void skel_from_pivots(Skel &s, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
@@ -2503,6 +2679,9 @@ int h2w_assemble(h2w_handle *h, int mode) {
         const bool sn = h->cfg.form == H2W_FORM_SEMINESTED;
         h->phases.clear();
         h->has_op = false;
+        if (mode == H2W_ASSEMBLE_LEARNED && !h->d_mlp.p)
+            throw ApiError(H2W_ERR_STATE, "learned assembly needs a model (h2w_learn_set_model)");
+        h->learned = mode == H2W_ASSEMBLE_LEARNED;
         if (mode == H2W_ASSEMBLE_NCA || mode == H2W_ASSEMBLE_LEARNED) {
             if (t.dim > 1) nca_far(h);
             if (!sn) nca_ver(h);
@@ -3151,6 +3330,82 @@ int h2w_batch_gmres_ir(h2w_batch *b, const double *rhs, double *x, int max_outer
         batch_out(b, b->xl.p, x, where);
         return ok ? H2W_OK : H2W_ERR_NOT_CONVERGED;
     });
+}
+
+int h2w_learn_record(h2w_handle *h, int enable) {
+    return guarded(h, [&] {
+        h->learn_rec = enable != 0;
+        h->rec_X.clear();
+        h->rec_y.clear();
+        return H2W_OK;
+    });
+}
+
+int h2w_learn_data(h2w_handle *h, float *X, uint8_t *y, int64_t *count) {
+    return guarded(h, [&] {
+        if (!count) throw ApiError(H2W_ERR_ARG, "null count");
+        *count = (int64_t)h->rec_y.size();
+        if (X) std::memcpy(X, h->rec_X.data(), h->rec_X.size() * 4);
+        if (y) std::memcpy(y, h->rec_y.data(), h->rec_y.size());
+        return H2W_OK;
+    });
+}
+
+int h2w_learn_set_model(h2w_handle *h, const float *params, float calib, int margin) {
+    return guarded(h, [&] {
+        if (!params || !(calib > 0.f) || margin < 0) throw ApiError(H2W_ERR_ARG, "bad model arguments");
+        if (h->cfg.device < 0) throw ApiError(H2W_ERR_STATE, "host-only handle");
+        std::vector<float> v(params, params + LRN_NPARAM);
+        h->d_mlp.upload(v, h->stream);
+        CK(cudaStreamSynchronize(h->stream));
+        h->mlp_calib = calib;
+        h->mlp_margin = margin;
+        return H2W_OK;
+    });
+}
+
+int h2w_learn_stats(h2w_handle *h, int64_t *blocks, int64_t *accepted) {
+    return guarded(h, [&] {
+        if (blocks) *blocks = h->learn_blocks;
+        if (accepted) *accepted = h->learn_accepted;
+        h->learn_blocks = h->learn_accepted = 0;
+        h->learn_reject[0] = h->learn_reject[1] = h->learn_reject[2] = 0;
+        h->learn_rhat = h->learn_r1 = 0.0;
+        return H2W_OK;
+    });
+}
+
+int h2w_learn_detail(h2w_handle *h, int64_t *rejects, double *mean_rhat, double *mean_r1) {
+    return guarded(h, [&] {
+        const double nb = (double)std::max<int64_t>(h->learn_blocks, 1);
+        if (rejects)
+            for (int k = 0; k < 3; ++k) rejects[k] = h->learn_reject[k];
+        if (mean_rhat) *mean_rhat = h->learn_rhat / nb;
+        if (mean_r1) *mean_r1 = h->learn_r1 / nb;
+        return H2W_OK;
+    });
+}
+
+int h2w_mlp_nparam(void) { return LRN_NPARAM; }
+
+int h2w_mlp_forward(const float *params, const float *X, int64_t n, float *logits, void *stream) {
+    if (!params || !X || !logits || n < 0) return H2W_ERR_ARG;
+    return launch_mlp_forward(params, X, n, logits, (cudaStream_t)stream) == cudaSuccess ? H2W_OK : H2W_ERR_CUDA;
+}
+
+int h2w_mlp_grad(const float *params, const float *X, const uint8_t *y, int64_t n, float pos_weight, float *grads,
+                 float *loss, void *stream) {
+    if (!params || !X || !y || !grads || !loss || n < 1 || !(pos_weight > 0.f)) return H2W_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(grads, 0, (size_t)LRN_NPARAM * 4, st) != cudaSuccess) return H2W_ERR_CUDA;
+    if (cudaMemsetAsync(loss, 0, 4, st) != cudaSuccess) return H2W_ERR_CUDA;
+    return launch_mlp_grad(params, X, y, n, pos_weight, grads, loss, st) == cudaSuccess ? H2W_OK : H2W_ERR_CUDA;
+}
+
+int h2w_mlp_adam(float *params, const float *grads, float *m, float *v, int step, float lr, void *stream) {
+    if (!params || !grads || !m || !v || step < 1 || !(lr > 0.f)) return H2W_ERR_ARG;
+    return launch_mlp_adam(params, grads, m, v, step, lr, (cudaStream_t)stream) == cudaSuccess ? H2W_OK
+                                                                                                : H2W_ERR_CUDA;
 }
 
 int h2w_profile(h2w_handle *h, int enable) {

@@ -90,6 +90,54 @@ cudaError_t vec_axpby(double a, const double *x, double b, const double *y, doub
 cudaError_t vec_f64_to_f32(const double *x, float *y, int64_t n, cudaStream_t st);
 cudaError_t vec_f32_to_f64(const float *x, double *y, int64_t n, cudaStream_t st);
 
+// ------------------------------------------------------- learned NCA
+// A per-point MLP (features -> 128 -> 128 -> logit, BF16 weights, FP32
+// accumulation) scores the candidate row and column points of NCA blocks;
+// the top-scored points form a cross-approximation proposal that the NCA's
+// own stopping test accepts or rejects.
+constexpr int LRN_F = 16, LRN_H = 128;
+constexpr int LRN_W1 = 0, LRN_B1 = LRN_F * LRN_H, LRN_W2 = LRN_B1 + LRN_H, LRN_B2 = LRN_W2 + LRN_H * LRN_H,
+              LRN_W3 = LRN_B2 + LRN_H, LRN_B3 = LRN_W3 + LRN_H, LRN_NPARAM = LRN_B3 + 1;
+constexpr int LRN_CAP = 128;  // most pivots a proposal holds
+
+struct LearnProb {
+    int64_t ri, ci;        // row / column point lists in the index buffer
+    int64_t xo;            // feature / logit offset: n1 rows then n2 columns
+    int64_t ac, ar;        // K(R, J): n1 x cap, column l at ac + l*n1; K(I, C): cap x n2, row l at ar + l*n2
+    int64_t uu, vv;        // U (n1 x cap), V (cap x n2), same layouts
+    int64_t ff, gu, gv;    // LU of K(I', J') and the Gram matrices U^T U, V V^T (cap x cap, row-major)
+    int64_t piv;           // proposal / pivot lists (cap + 1 entries)
+    int32_t n1, n2, cap, pad;
+};
+struct LearnState {
+    int32_t rhat, r1, accept, rank;  // proposal size, pivots kept, accepted, final rank
+};
+struct LearnTile {
+    int32_t b, kind, start, count;  // kind 0: K(R,J') entries, 1: K(I,C) entries, 2: U rows, 3: V columns
+};
+cudaError_t launch_learn_features(const LearnProb *probs, int nprob, const int32_t *idx, const KParams &kp,
+                                  int tol_pow, float *X, cudaStream_t st);
+cudaError_t launch_mlp_forward(const float *params, const float *X, int64_t n, float *logits, cudaStream_t st);
+cudaError_t launch_mlp_grad(const float *params, const float *X, const uint8_t *y, int64_t n, float pos_weight,
+                            float *grads, float *loss, cudaStream_t st);
+cudaError_t launch_mlp_adam(float *params, const float *grads, float *m, float *v, int step, float lr,
+                            cudaStream_t st);
+cudaError_t launch_learn_propose(const LearnProb *probs, int nprob, const float *logits, float calib, int margin,
+                                 int32_t *prop_r, int32_t *prop_c, LearnState *lst, int mask_words, cudaStream_t st);
+cudaError_t launch_learn_fill(const LearnTile *tiles, int ntiles, const LearnProb *probs, const int32_t *idx,
+                              const KParams &kp, const int32_t *prop_r, const int32_t *ordJ, const LearnState *lst,
+                              double *scr, int only, cudaStream_t st);
+cudaError_t launch_learn_aca(const LearnProb *probs, int nprob, double tol, double *scr, int32_t *ordI,
+                             int32_t *ordJ, LearnState *lst, int mask_words, cudaStream_t st);
+cudaError_t launch_learn_solve(const LearnTile *tiles, int ntiles, const LearnProb *probs, const int32_t *ordI,
+                               const int32_t *ordJ, const LearnState *lst, double *scr, cudaStream_t st);
+cudaError_t launch_learn_gram(const LearnTile *tiles, int ntiles, const LearnProb *probs, const LearnState *lst,
+                              double *scr, cudaStream_t st);
+cudaError_t launch_learn_test(const LearnProb *probs, int nprob, const int32_t *idx, const KParams &kp, double tol,
+                              const int32_t *prop_r, const int32_t *prop_c, const int32_t *ordI, const int32_t *ordJ,
+                              LearnState *lst, double *scr, int32_t *prow, int32_t *pcol, int mask_words,
+                              cudaStream_t st);
+
 // ------------------------------------------------ many independent problems
 // One problem of a batch: its packed operator (FP64 or FP32 copy), its
 // workspace, its leaf permutation (NULL: vectors in leaf order) and the

@@ -218,6 +218,41 @@ int h2w_batch_gmres(h2w_batch *b, const double *rhs, double *x, int max_iter, in
 int h2w_batch_gmres_ir(h2w_batch *b, const double *rhs, double *x, int max_outer, int inner_iter, int tol_pow,
                        int where, int *outer_iters, int *inner_total, double *resid);
 
+/* Learned NCA proposals (no counterpart in the reference). A small network
+ * (per candidate point: 16 geometric features -> 128 -> 128 -> 1, ReLU, BF16
+ * weights, FP32 accumulation) scores the row and column points of every NCA
+ * block; with H2W_ASSEMBLE_LEARNED the top-scored points form a cross
+ * approximation that the NCA's own stopping test (1D/codes/aca.hpp:363,
+ * 404-409) checks on the full block with one further ACA step; blocks that
+ * fail it get the plain pivot search, so every block meets the NCA tolerance.
+ * Parameters: h2w_mlp_nparam() floats, W1 (16 x 128, row-major), b1 (128),
+ * W2 (128 x 128), b2 (128), w3 (128), b3 (1).
+ *  h2w_learn_record     while enabled, plain NCA assembly records training
+ *                       data: features of every candidate point (16 floats)
+ *                       and a label (1 = chosen as a pivot); enabling clears it
+ *  h2w_learn_data       copies it out (NULL arrays: count only)
+ *  h2w_learn_set_model  installs a trained model; rank estimate per block =
+ *                       ceil(calib * sum of the rows' probabilities) + margin
+ *  h2w_learn_stats      blocks proposed / accepted since the last call
+ *  h2w_mlp_forward / h2w_mlp_grad / h2w_mlp_adam   the network's training
+ *                       kernels on device pointers: logits; the gradient of
+ *                       the mean weighted binary cross-entropy (positives
+ *                       weighted by pos_weight) into grads, and the loss; an
+ *                       Adam step (beta 0.9 / 0.999, eps 1e-8) */
+int h2w_learn_record(h2w_handle *h, int enable);
+int h2w_learn_data(h2w_handle *h, float *X, uint8_t *y, int64_t *count);
+int h2w_learn_set_model(h2w_handle *h, const float *params, float calib, int margin);
+int h2w_learn_stats(h2w_handle *h, int64_t *blocks, int64_t *accepted);
+/* Since the last h2w_learn_stats: rejections by cause (rejects[0] no usable
+ * pivots in the proposal, [1] non-finite factors, [2] the stopping test
+ * failed) and the mean proposal size and pivots kept per block. */
+int h2w_learn_detail(h2w_handle *h, int64_t *rejects, double *mean_rhat, double *mean_r1);
+int h2w_mlp_nparam(void);
+int h2w_mlp_forward(const float *params, const float *X, int64_t n, float *logits, void *stream);
+int h2w_mlp_grad(const float *params, const float *X, const uint8_t *y, int64_t n, float pos_weight, float *grads,
+                 float *loss, void *stream);
+int h2w_mlp_adam(float *params, const float *grads, float *m, float *v, int step, float lr, void *stream);
+
 /* Autotuner (no counterpart in the reference): times `reps` products per
  * candidate target granularity on this operator and this GPU and keeps the
  * fastest. nrhs > 1: the multi-vector stream's column cap (256, 512, 1024,
