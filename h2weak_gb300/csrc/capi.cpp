@@ -382,7 +382,7 @@ void record_blocks(h2w_handle *h, const std::vector<NcaProb> &probs, const DBuf<
     DBuf<float> dx;
     dl.upload(lp, h->stream);
     dx.alloc((size_t)xo * LRN_F);
-    CK(launch_learn_features(dl.p, (int)lp.size(), di.p, h->kparams(), h->cfg.tol_pow, dx.p, h->stream));
+    CK(launch_learn_features(dl.p, (int)lp.size(), di.p, h->kparams(), h->cfg.tol_pow, dx.p, 0, h->stream));
     const size_t base = h->rec_y.size();
     h->rec_X.resize((base + (size_t)xo) * LRN_F);
     h->rec_y.resize(base + (size_t)xo, 0);
@@ -419,7 +419,7 @@ void run_nca_learned(h2w_handle *h, const std::vector<std::vector<int32_t>> &R,
             const int n1 = (int)R[p].size(), n2 = (int)C[p].size();
             const int cap = std::min(std::min(n1, n2), LRN_CAP);
             const int64_t need = 2 * (int64_t)cap * (n1 + n2) + 3 * (int64_t)cap * cap;
-            if (!probs.empty() && (size_t)(scr + need) * 8 + (size_t)(xo + n1 + n2) * (LRN_F + 1) * 4 > budget) break;
+            if (!probs.empty() && (size_t)(scr + need) * 8 + (size_t)(xo + n1) * (LRN_F + 1) * 4 > budget) break;
             LearnProb l;
             std::memset(&l, 0, sizeof(l));
             l.ri = (int64_t)idx.size();
@@ -427,7 +427,7 @@ void run_nca_learned(h2w_handle *h, const std::vector<std::vector<int32_t>> &R,
             l.ci = (int64_t)idx.size();
             append(idx, C[p].data(), n2);
             l.xo = xo;
-            xo += n1 + n2;
+            xo += n1;  // rows only are scored
             l.ac = scr; scr += (int64_t)cap * n1;
             l.ar = scr; scr += (int64_t)cap * n2;
             l.uu = scr; scr += (int64_t)cap * n1;
@@ -468,7 +468,7 @@ void run_nca_learned(h2w_handle *h, const std::vector<std::vector<int32_t>> &R,
         CK(cudaMemsetAsync(dscr.p, 0, (size_t)scr * 8, st));
         dx.alloc((size_t)xo * LRN_F);
         dz.alloc((size_t)xo);
-        CK(launch_learn_features(dp.p, nb, di.p, kp, h->cfg.tol_pow, dx.p, st));
+        CK(launch_learn_features(dp.p, nb, di.p, kp, h->cfg.tol_pow, dx.p, 1, st));
         CK(launch_mlp_forward(h->d_mlp.p, dx.p, xo, dz.p, st));
         CK(launch_learn_propose(dp.p, nb, dz.p, h->mlp_calib, h->mlp_margin, dpr.p, dpc.p, dls.p, mw1, st));
         CK(launch_learn_fill(dt.p, (int)tiles.size(), dp.p, di.p, kp, dpr.p, doj.p, dls.p, dscr.p, 1, st));

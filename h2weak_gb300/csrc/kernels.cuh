@@ -115,8 +115,9 @@ struct LearnState {
 struct LearnTile {
     int32_t b, kind, start, count;  // kind 0: K(R,J') entries, 1: K(I,C) entries, 2: U rows, 3: V columns
 };
+// rows_only: features of the rows alone (inference scores rows only)
 cudaError_t launch_learn_features(const LearnProb *probs, int nprob, const int32_t *idx, const KParams &kp,
-                                  int tol_pow, float *X, cudaStream_t st);
+                                  int tol_pow, float *X, int rows_only, cudaStream_t st);
 cudaError_t launch_mlp_forward(const float *params, const float *X, int64_t n, float *logits, cudaStream_t st);
 cudaError_t launch_mlp_grad(const float *params, const float *X, const uint8_t *y, int64_t n, float pos_weight,
                             float *grads, float *loss, cudaStream_t st);

@@ -38,7 +38,7 @@ __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__floa
 // ------------------------------------------------------------ features ---
 __global__ void __launch_bounds__(LT)
     learn_features_kernel(const LearnProb *__restrict__ probs, const int32_t *__restrict__ idx, KParams kp,
-                          int tol_pow, float *__restrict__ X) {
+                          int tol_pow, float *__restrict__ X, int rows_only) {
     __shared__ double part[LT][12];
     __shared__ double st[12];  // row: min[3] max[3]; col: min[3] max[3]
     __shared__ double cen[6];  // row centroid, col centroid
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(LT)
         __syncthreads();
     }
     const float lg1 = log2f((float)pb.n1 + 1.f) / 16.f, lg2 = log2f((float)pb.n2 + 1.f) / 16.f;
-    for (int e = tid; e < pb.n1 + pb.n2; e += LT) {
+    for (int e = tid; e < pb.n1 + (rows_only ? 0 : pb.n2); e += LT) {
         const bool row = e < pb.n1;
         const int set = row ? 0 : 1;
         const int gp = row ? R[e] : C[e - pb.n1];
@@ -118,10 +118,10 @@ __global__ void __launch_bounds__(LT)
 }
 
 cudaError_t launch_learn_features(const LearnProb *probs, int nprob, const int32_t *idx, const KParams &kp,
-                                  int tol_pow, float *X, cudaStream_t st) {
+                                  int tol_pow, float *X, int rows_only, cudaStream_t st) {
     for (int b0 = 0; b0 < nprob; b0 += 65535) {
         const int nb = nprob - b0 < 65535 ? nprob - b0 : 65535;
-        learn_features_kernel<<<nb, LT, 0, st>>>(probs + b0, idx, kp, tol_pow, X);
+        learn_features_kernel<<<nb, LT, 0, st>>>(probs + b0, idx, kp, tol_pow, X, rows_only);
         count_launch();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -468,7 +468,8 @@ cudaError_t launch_learn_fill(const LearnTile *tiles, int ntiles, const LearnPro
 // pivots by argmax of the residual row over every column, row pivots by argmax
 // of the residual column over the proposed rows, the stopping test with
 // normS over these vectors; at most cap - 1 pivots (one column is kept for the
-// full-block test). ordI: pivot rows as proposal indices, ordJ: pivot columns
+// full-block test; normS here only trims, without the cross terms). ordI:
+// pivot rows as proposal indices, ordJ: pivot columns
 // as local column indices, both in pivot order; then the LU (no pivoting) of
 // K(I', J') in that order at ff (L unit lower / R upper, row-major cap x cap).
 // Scratch: the residual rows at vv, the restricted residual columns at gu
@@ -581,23 +582,9 @@ __global__ void __launch_bounds__(LT)
             crow[row] = 1;
             acm[cj >> 5] |= 1u << (cj & 31);
         }
-        // normS with the cross terms of the new term against the kept ones
-        double cross = 0.0;
-        for (int l = 0; l < r1; ++l) {
-            double du = 0.0, dv = 0.0;
-            for (int m = tid; m < rh; m += LT) du += Ur[(int64_t)l * cap + m] * u[m];
-            for (int s2 = tid; s2 < n2; s2 += LT) dv += Vr[(int64_t)l * n2 + s2] * v[s2];
-            for (int o = 16; o > 0; o >>= 1) {
-                du += __shfl_xor_sync(0xffffffffu, du, o);
-                dv += __shfl_xor_sync(0xffffffffu, dv, o);
-            }
-            if (lane == 0) { shd[2 * warp] = du; shd[2 * warp + 1] = dv; }
-            __syncthreads();
-            double a = 0.0, b2 = 0.0;
-            for (int q = 0; q < nw; ++q) { a += shd[2 * q]; b2 += shd[2 * q + 1]; }
-            cross += 2.0 * fabs(a * b2);
-            __syncthreads();
-        }
+        // normS for trimming the proposal (the full-block test recomputes it
+        // exactly from the Gram matrices)
+        const double cross = 0.0;
         ++r1;
         const double uv = nu * nv;
         normS = sqrt(normS * normS + uv * uv + cross);
