@@ -284,10 +284,150 @@ void append(std::vector<int32_t> &a, const int32_t *b, int64_t n) { a.insert(a.e
 void record_blocks(h2w_handle *h, const std::vector<NcaProb> &probs, const DBuf<int32_t> &di,
                    const std::vector<std::vector<int32_t>> &prow, const std::vector<std::vector<int32_t>> &pcol,
                    size_t p0);
+void record_lists(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+                  const std::vector<std::vector<int32_t>> &prow, const std::vector<std::vector<int32_t>> &pcol);
+void run_nca_small(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+                   std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol);
 
-// The NCA pivot search, one CTA per block (nca_kernel), in batches that fit
-// the scratch budget.
+constexpr int64_t NCA_BIG = 8192;  // rows + columns from which a block gets a group of CTAs
+
+// Large blocks: groups of CTAs of one cooperative launch per block
+// (ncabig.cu), in batches within the scratch budget.
+void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+                 const std::vector<size_t> &big, std::vector<std::vector<int32_t>> &prow,
+                 std::vector<std::vector<int32_t>> &pcol) {
+    const double tol = std::pow(10, -1.0 * h->cfg.tol_pow);
+    const int cap = h->cfg.rank_cap > 0 ? h->cfg.rank_cap : 1024;
+    const size_t budget = (size_t)40 << 30;
+    KParams kp = h->kparams();
+    cudaStream_t st = h->stream;
+    size_t q0 = 0;
+    while (q0 < big.size()) {
+        std::vector<NcaProb> probs;
+        std::vector<int64_t> moff;
+        std::vector<int32_t> idx;
+        size_t scr = 0;
+        int64_t piv = 0, mw = 0;
+        int dcap = 1;
+        size_t q = q0;
+        for (; q < big.size(); ++q) {
+            const size_t p = big[q];
+            const int n1 = (int)R[p].size(), n2 = (int)C[p].size();
+            const int rc = std::min(std::min(n1, n2), cap);
+            const size_t need = (size_t)rc * (size_t)(n1 + n2);
+            if (!probs.empty() && (scr + need) * 8 > budget) break;
+            NcaProb pb{};
+            pb.ri = (int64_t)idx.size();
+            append(idx, R[p].data(), n1);
+            pb.ci = (int64_t)idx.size();
+            append(idx, C[p].data(), n2);
+            pb.u = (int64_t)scr;
+            pb.v = (int64_t)(scr + (size_t)rc * n1);
+            scr += need;
+            pb.piv = piv;
+            piv += rc;
+            pb.n1 = n1;
+            pb.n2 = n2;
+            pb.rcap = rc;
+            probs.push_back(pb);
+            moff.push_back(mw);
+            mw += (n1 + 31) / 32 + (n2 + 31) / 32;
+            dcap = std::max(dcap, rc);
+        }
+        const int grid = nca_group_grid(dcap);
+        if (grid <= 0) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: no co-resident grid");
+        const int nb = (int)probs.size();
+        const int G = std::max(1, std::min(nb, grid / 32));
+        DBuf<NcaProb> dp;
+        DBuf<int64_t> dm;
+        DBuf<int32_t> di, drank, dpr, dpc, dst, derr;
+        DBuf<uint32_t> dmask;
+        DBuf<unsigned> dbar;
+        DBuf<double> dscr, ddots;
+        DBuf<char> dpartr, dpartc;
+        dp.upload(probs, st);
+        dm.upload(moff, st);
+        di.upload(idx, st);
+        dscr.alloc(scr);
+        dmask.alloc((size_t)mw);
+        drank.alloc((size_t)nb);
+        dpr.alloc((size_t)piv);
+        dpc.alloc((size_t)piv);
+        dst.alloc(1);
+        derr.alloc(1);
+        dbar.alloc((size_t)2 * G);
+        dpartr.alloc(nca_group_part_bytes() * (size_t)grid);
+        dpartc.alloc(nca_group_part_bytes() * (size_t)grid);
+        ddots.alloc((size_t)grid * 2 * dcap);
+        CK(cudaMemsetAsync(dst.p, 0, 4, st));
+        CK(cudaMemsetAsync(derr.p, 0, 4, st));
+        CK(cudaMemsetAsync(dbar.p, 0, (size_t)2 * G * sizeof(unsigned), st));
+        CK(launch_nca_group(dp.p, dm.p, nb, G, grid, di.p, kp, tol, dscr.p, dmask.p, drank.p, dpr.p, dpc.p, dst.p,
+                            dbar.p, derr.p, dpartr.p, dpartc.p, ddots.p, dcap, st));
+        std::vector<int32_t> rk((size_t)nb), hpr((size_t)piv), hpc((size_t)piv);
+        int32_t status = 0, errf = 0;
+        CK(cudaMemcpyAsync(rk.data(), drank.p, rk.size() * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hpr.data(), dpr.p, hpr.size() * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(hpc.data(), dpc.p, hpc.size() * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&errf, derr.p, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (errf) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: a group-barrier wait ran out");
+        if (status & 1) throw ApiError(H2W_ERR_RANK, "an NCA block needed more than rank_cap pivots");
+        if (status & 2) throw ApiError(H2W_ERR_ARG, "non-finite kernel entries (coincident points?) in an NCA block");
+        for (int k = 0; k < nb; ++k) {
+            const size_t p = big[q0 + (size_t)k];
+            prow[p].assign(hpr.begin() + probs[(size_t)k].piv, hpr.begin() + probs[(size_t)k].piv + rk[(size_t)k]);
+            pcol[p].assign(hpc.begin() + probs[(size_t)k].piv, hpc.begin() + probs[(size_t)k].piv + rk[(size_t)k]);
+        }
+        q0 = q;
+    }
+}
+
+// The NCA pivot search: one CTA per block (nca_kernel) in batches that fit
+// the scratch budget; blocks of NCA_BIG or more rows + columns get groups of
+// CTAs (run_nca_big). H2W_NCA_BIG=0 keeps every block on one CTA.
 void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+                   std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
+    prow.assign(R.size(), {});
+    pcol.assign(R.size(), {});
+    std::vector<size_t> big, small;
+    const char *eb = getenv("H2W_NCA_BIG");
+    const bool use_big = !(eb && std::string(eb) == "0");
+    for (size_t p = 0; p < R.size(); ++p)
+        ((use_big && (int64_t)(R[p].size() + C[p].size()) >= NCA_BIG) ? big : small).push_back(p);
+    if (!big.empty()) {
+        run_nca_big(h, R, C, big, prow, pcol);
+        if (h->learn_rec) {  // training data of the large blocks: recorded through the small path's recorder
+            std::vector<std::vector<int32_t>> R2, C2, pr2, pc2;
+            for (size_t p : big) {
+                R2.push_back(R[p]);
+                C2.push_back(C[p]);
+                pr2.push_back(prow[p]);
+                pc2.push_back(pcol[p]);
+            }
+            record_lists(h, R2, C2, pr2, pc2);
+        }
+    }
+    if (small.empty()) return;
+    std::vector<std::vector<int32_t>> Rs, Cs, prs, pcs;
+    const bool all_small = small.size() == R.size();
+    if (!all_small)
+        for (size_t p : small) {
+            Rs.push_back(R[p]);
+            Cs.push_back(C[p]);
+        }
+    const std::vector<std::vector<int32_t>> &RR = all_small ? R : Rs, &CC = all_small ? C : Cs;
+    std::vector<std::vector<int32_t>> &PR = all_small ? prow : prs, &PC = all_small ? pcol : pcs;
+    run_nca_small(h, RR, CC, PR, PC);
+    if (!all_small)
+        for (size_t k = 0; k < small.size(); ++k) {
+            prow[small[k]] = std::move(prs[k]);
+            pcol[small[k]] = std::move(pcs[k]);
+        }
+}
+
+void run_nca_small(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
                    std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
     const size_t np = R.size();
     prow.assign(np, {});
@@ -392,6 +532,24 @@ void record_blocks(h2w_handle *h, const std::vector<NcaProb> &probs, const DBuf<
         for (int32_t i : prow[p0 + q]) h->rec_y[base + (size_t)lp[q].xo + (size_t)i] = 1;
         for (int32_t j : pcol[p0 + q]) h->rec_y[base + (size_t)lp[q].xo + (size_t)lp[q].n1 + (size_t)j] = 1;
     }
+}
+
+// Training data of blocks given as lists (the large-block path).
+void record_lists(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
+                  const std::vector<std::vector<int32_t>> &prow, const std::vector<std::vector<int32_t>> &pcol) {
+    std::vector<NcaProb> probs(R.size());
+    std::vector<int32_t> idx;
+    for (size_t q = 0; q < R.size(); ++q) {
+        probs[q].ri = (int64_t)idx.size();
+        append(idx, R[q].data(), (int64_t)R[q].size());
+        probs[q].ci = (int64_t)idx.size();
+        append(idx, C[q].data(), (int64_t)C[q].size());
+        probs[q].n1 = (int32_t)R[q].size();
+        probs[q].n2 = (int32_t)C[q].size();
+    }
+    DBuf<int32_t> di;
+    di.upload(idx, h->stream);
+    record_blocks(h, probs, di, prow, pcol, 0);
 }
 
 // Learned proposals for every block (see learn.cu); blocks the NCA stopping

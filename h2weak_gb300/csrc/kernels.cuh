@@ -34,6 +34,17 @@ struct NcaProb {
 cudaError_t launch_nca(const NcaProb *probs, int nprob, const int32_t *idx, const KParams &kp, double tol,
                        double *scratch, int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status,
                        int max_n1, int max_n2, int max_rcap, cudaStream_t st);
+// The NCA for large blocks: the CTAs of one cooperative launch in G groups,
+// each group on one block at a time (same pivots as launch_nca). moff: per
+// block, offset of its row+column pivot masks (uint32 words) in masks;
+// partial buffers of nca_group_part_bytes() x grid each; dots: grid x 2*dcap.
+int nca_group_grid(int dcap);
+size_t nca_group_part_bytes();
+cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int nprob, int G, int grid,
+                             const int32_t *idx, const KParams &kp, double tol, double *scr, uint32_t *masks,
+                             int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status, unsigned *bars,
+                             int32_t *err, void *prow_part, void *pcol_part, double *dots, int dcap,
+                             cudaStream_t st);
 cudaError_t launch_factor(const FactorJob *jobs, int njobs, const int32_t *idx, const KParams &kp, double *F,
                           cudaStream_t st);
 cudaError_t launch_xfer(const XferJob *jobs, int njobs, int max_n, const int32_t *idx, const KParams &kp,

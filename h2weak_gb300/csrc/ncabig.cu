@@ -1,0 +1,333 @@
+// The NCA pivot search for large blocks on many SMs at once (sm_103a).
+//
+// The reference's ACA (1D/codes/aca.hpp:296-446) is sequential in its
+// pivots, and one CTA per block (nca_kernel) leaves a block of tens of
+// thousands of rows and columns on a single SM. Here the CTAs of one
+// cooperative launch form G groups; a group works on one large block at a
+// time, its CTAs striding over the block's columns (residual rows) and rows
+// (residual columns), with a bounded group barrier after each pass. Every
+// entry and residual is computed by one thread in the reference's operation
+// order (separately rounded multiply and subtract), the argmax keeps the
+// lowest index among equal magnitudes, and every CTA of the group reduces the
+// per-CTA partials in the same CTA order, so all CTAs agree on every pivot
+// and on the stopping test without further communication.
+#include <climits>
+
+#include "entry.cuh"
+
+namespace h2w {
+
+constexpr int NG_THREADS = 256;
+
+struct NgPart {             // per-CTA partials of one pass
+    double v, s;            // best |value| (argmax), sum of squares
+    int32_t i, pad;
+};
+
+// Group barrier: ctr[0] arrivals, ctr[1] generation; bounded spin sets *err.
+__device__ __forceinline__ void ng_barrier(unsigned *ctr, unsigned members, int32_t *err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = ctr + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(ctr, 1u);
+        if (arrived == members - 1) {
+            atomicExch(ctr, 0u);
+            __threadfence();
+            atomicAdd(ctr + 1, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == gen) {
+                if (++it > (1LL << 26)) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool ng_better(double a, int ia, double b, int ib) { return a > b || (a == b && ia < ib); }
+
+// CTA-local argmax / sum, then written as this CTA's partial
+__device__ void ng_cta_part(double v, int i, double s, NgPart *out, double *shv, int *shi, double *shs) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+        if (ng_better(ov, oi, v, i)) { v = ov; i = oi; }
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) { shv[w] = v; shi[w] = i; shs[w] = s; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bv = shv[0], ss = shs[0];
+        int bi = shi[0];
+        for (int q = 1; q < NG_THREADS / 32; ++q) {
+            if (ng_better(shv[q], shi[q], bv, bi)) { bv = shv[q]; bi = shi[q]; }
+            ss += shs[q];
+        }
+        *out = {bv, ss, bi, 0};
+    }
+    __syncthreads();
+}
+// the group's result from its members' partials, in member order
+__device__ void ng_group(const NgPart *part, int g, int G, int S, double &v, int &i, double &s) {
+    v = -1.0;
+    i = INT_MAX;
+    s = 0.0;
+    for (int k = 0; k < S; ++k) {
+        const NgPart p = part[g + k * G];
+        if (ng_better(p.v, p.i, v, i)) { v = p.v; i = p.i; }
+        s += p.s;
+    }
+}
+__device__ __forceinline__ bool ng_bit(const uint32_t *m, int i) { return (m[i >> 5] >> (i & 31)) & 1u; }
+
+__global__ void __launch_bounds__(NG_THREADS)
+    nca_group_kernel(const NcaProb *__restrict__ probs, const int64_t *__restrict__ moff, int nprob, int G,
+                     const int32_t *__restrict__ idx, KParams kp, double tol, double *__restrict__ scr,
+                     uint32_t *__restrict__ masks, int32_t *__restrict__ rank_out, int32_t *__restrict__ prow,
+                     int32_t *__restrict__ pcol, int32_t *status, unsigned *bars, int32_t *err, NgPart *prow_part,
+                     NgPart *pcol_part, double *dots, int dcap) {
+    extern __shared__ double ng_coef[];  // dcap doubles
+    __shared__ double shv[32], shs[32];
+    __shared__ int shi[32];
+    const int g = blockIdx.x % G, gi = blockIdx.x / G;
+    const int S = (gridDim.x - g + G - 1) / G;  // members of group g
+    unsigned *bar = bars + 2 * g;
+    const int tid = threadIdx.x;
+    const int cstride = S * NG_THREADS;
+    const double tiny = 1e-36;
+    for (int b = g; b < nprob; b += G) {
+        const NcaProb pb = probs[b];
+        const int n1 = pb.n1, n2 = pb.n2, rcap = pb.rcap;
+        const int32_t *I = idx + pb.ri, *J = idx + pb.ci;
+        double *U = scr + pb.u, *V = scr + pb.v;
+        uint32_t *rm = masks + moff[b], *cm = rm + (n1 + 31) / 32;
+        for (int q = gi * NG_THREADS + tid; q < (n1 + 31) / 32 + (n2 + 31) / 32; q += cstride) rm[q] = 0u;
+        if (gi == 0 && tid == 0) rank_out[b] = 0;
+        ng_barrier(bar, S, err);
+        const int mn = n1 < n2 ? n1 : n2;
+        if (mn == 0 || rcap == 0) continue;
+        // first pivot row: the first row whose largest |entry| exceeds 1e-36
+        int ri = -1, ci = -1;
+        double bv, ss;
+        int bi;
+        for (int l = 0; l < n1 && ri < 0; ++l) {
+            double v0 = -1.0;
+            int i0 = INT_MAX;
+            for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) {
+                const double v = kentry(kp, I[l], J[s2]);
+                V[s2] = v;
+                const double a = fabs(v);
+                if (ng_better(a, s2, v0, i0)) { v0 = a; i0 = s2; }
+            }
+            ng_cta_part(v0, i0, 0.0, prow_part + blockIdx.x, shv, shi, shs);
+            ng_barrier(bar, S, err);
+            ng_group(prow_part, g, G, S, bv, bi, ss);
+            if (bv > tiny) { ri = l; ci = bi; }
+            ng_barrier(bar, S, err);  // the partials are read before the next row overwrites them
+        }
+        if (ri < 0) continue;
+        const double piv0 = V[ci];
+        // first column; the first row's squares
+        {
+            double v0 = -1.0, us = 0.0, vs = 0.0;
+            int i0 = INT_MAX;
+            for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) {
+                const double c = kentry(kp, I[t], J[ci]);
+                const double u = __ddiv_rn(c, piv0);
+                U[t] = u;
+                us += u * u;
+                if (t != ri) {
+                    const double a = fabs(c);
+                    if (ng_better(a, t, v0, i0)) { v0 = a; i0 = t; }
+                }
+            }
+            for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) vs += V[s2] * V[s2];
+            ng_cta_part(v0, i0, us, pcol_part + blockIdx.x, shv, shi, shs);
+            ng_cta_part(-1.0, INT_MAX, vs, prow_part + blockIdx.x, shv, shi, shs);
+        }
+        ng_barrier(bar, S, err);
+        double nu, nv;
+        {
+            double a;
+            int nri;
+            ng_group(pcol_part, g, G, S, a, nri, nu);
+            nu = sqrt(nu);
+            double dummy;
+            int di;
+            ng_group(prow_part, g, G, S, dummy, di, nv);
+            nv = sqrt(nv);
+            if (gi == 0 && tid == 0) {
+                prow[pb.piv] = ri;
+                pcol[pb.piv] = ci;
+                rm[ri >> 5] |= 1u << (ri & 31);
+                cm[ci >> 5] |= 1u << (ci & 31);
+            }
+            ri = nri;
+        }
+        int rank = 1;
+        double normS = 0.0;
+        ng_barrier(bar, S, err);
+        while (nu * nv > tol * normS && rank < mn) {
+            if (rank >= rcap) {
+                if (gi == 0 && tid == 0) atomicOr(status, 1);
+                break;
+            }
+            if (ri < 0 || ri >= n1) {
+                if (gi == 0 && tid == 0) atomicOr(status, 2);
+                break;
+            }
+            // residual row ri over this CTA's columns; column pivot
+            for (int l = tid; l < rank; l += NG_THREADS) ng_coef[l] = U[(size_t)l * n1 + ri];
+            __syncthreads();
+            double *Vr = V + (size_t)rank * n2;
+            double v0 = -1.0, vs = 0.0;
+            int i0 = INT_MAX;
+            for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) {
+                double v = kentry(kp, I[ri], J[s2]);
+                for (int l = 0; l < rank; ++l) v = __dsub_rn(v, __dmul_rn(ng_coef[l], V[(size_t)l * n2 + s2]));
+                Vr[s2] = v;
+                vs += v * v;
+                if (!ng_bit(cm, s2)) {
+                    const double a = fabs(v);
+                    if (ng_better(a, s2, v0, i0)) { v0 = a; i0 = s2; }
+                }
+            }
+            ng_cta_part(v0, i0, vs, prow_part + blockIdx.x, shv, shi, shs);
+            ng_barrier(bar, S, err);
+            ng_group(prow_part, g, G, S, bv, bi, ss);
+            if (bi < 0 || bi >= n2) {
+                if (gi == 0 && tid == 0) atomicOr(status, 2);
+                break;
+            }
+            ci = bi;
+            nv = sqrt(ss);
+            const double piv = Vr[ci];
+            // residual column ci over this CTA's rows; next row pivot
+            for (int l = tid; l < rank; l += NG_THREADS) ng_coef[l] = V[(size_t)l * n2 + ci];
+            __syncthreads();
+            double *Ur = U + (size_t)rank * n1;
+            double u0 = -1.0, us = 0.0;
+            int j0 = INT_MAX;
+            for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) {
+                double c = kentry(kp, I[t], J[ci]);
+                for (int l = 0; l < rank; ++l) c = __dsub_rn(c, __dmul_rn(ng_coef[l], U[(size_t)l * n1 + t]));
+                const double u = __ddiv_rn(c, piv);
+                Ur[t] = u;
+                us += u * u;
+                if (t != ri && !ng_bit(rm, t)) {
+                    const double a = fabs(c);
+                    if (ng_better(a, t, u0, j0)) { u0 = a; j0 = t; }
+                }
+            }
+            ng_cta_part(u0, j0, us, pcol_part + blockIdx.x, shv, shi, shs);
+            ng_barrier(bar, S, err);
+            int nri;
+            ng_group(pcol_part, g, G, S, bv, nri, ss);
+            nu = sqrt(ss);
+            if (nu < 1e-36 || nv < 1e-36) break;
+            if (gi == 0 && tid == 0) {
+                prow[pb.piv + rank] = ri;
+                pcol[pb.piv + rank] = ci;
+                rm[ri >> 5] |= 1u << (ri & 31);
+                cm[ci >> 5] |= 1u << (ci & 31);
+            }
+            ++rank;
+            // normS: partial dots of every kept u, v with the new ones (the new term included)
+            double *dme = dots + (size_t)blockIdx.x * 2 * dcap;
+            for (int l = 0; l < rank; ++l) {
+                const double *Ul = U + (size_t)l * n1, *Vl = V + (size_t)l * n2;
+                double du = 0.0, dv = 0.0;
+                for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) du += Ul[t] * Ur[t];
+                for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) dv += Vl[s2] * Vr[s2];
+                for (int o = 16; o > 0; o >>= 1) {
+                    du += __shfl_xor_sync(0xffffffffu, du, o);
+                    dv += __shfl_xor_sync(0xffffffffu, dv, o);
+                }
+                if ((tid & 31) == 0) { shv[tid >> 5] = du; shs[tid >> 5] = dv; }
+                __syncthreads();
+                if (tid == 0) {
+                    double a = 0.0, c = 0.0;
+                    for (int q = 0; q < NG_THREADS / 32; ++q) { a += shv[q]; c += shs[q]; }
+                    dme[2 * l] = a;
+                    dme[2 * l + 1] = c;
+                }
+                __syncthreads();
+            }
+            ng_barrier(bar, S, err);
+            {
+                // 2 sum_l |<U_l, u><V_l, v>|: the terms split over the CTA's threads
+                // (each term summed over the members in member order), then one
+                // block sum in a fixed order, so every CTA gets the same normS
+                double part = 0.0;
+                for (int l = tid; l < rank; l += NG_THREADS) {
+                    double du = 0.0, dv = 0.0;
+                    for (int k = 0; k < S; ++k) {
+                        const double *dk = dots + (size_t)(g + k * G) * 2 * dcap;
+                        du += dk[2 * l];
+                        dv += dk[2 * l + 1];
+                    }
+                    part += 2.0 * fabs(du * dv);
+                }
+                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                if ((tid & 31) == 0) shs[tid >> 5] = part;
+                __syncthreads();
+                double ns = normS * normS + (nu * nv) * (nu * nv);
+                for (int q = 0; q < NG_THREADS / 32; ++q) ns += shs[q];
+                normS = sqrt(ns);
+                __syncthreads();
+            }
+            ri = nri;
+            ng_barrier(bar, S, err);  // the dots are read before the next step overwrites them
+        }
+        if (gi == 0 && tid == 0) rank_out[b] = rank;
+        ng_barrier(bar, S, err);
+    }
+}
+
+static int ng_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+int nca_group_grid(int dcap) {
+    int per_sm = 0;
+    const size_t sm = (size_t)dcap * 8;
+    if (sm > 48 * 1024) cudaFuncSetAttribute(nca_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nca_group_kernel, NG_THREADS, sm);
+    return per_sm > 0 ? ng_sms() * per_sm : 0;
+}
+
+cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int nprob, int G, int grid,
+                             const int32_t *idx, const KParams &kp, double tol, double *scr, uint32_t *masks,
+                             int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status, unsigned *bars,
+                             int32_t *err, void *prow_part, void *pcol_part, double *dots, int dcap,
+                             cudaStream_t st) {
+    if (nprob <= 0) return cudaSuccess;
+    NgPart *pr = reinterpret_cast<NgPart *>(prow_part), *pc = reinterpret_cast<NgPart *>(pcol_part);
+    void *args[] = {(void *)&probs, (void *)&moff, (void *)&nprob, (void *)&G,    (void *)&idx,  (void *)&kp,
+                    (void *)&tol,   (void *)&scr,  (void *)&masks, (void *)&rank, (void *)&prow, (void *)&pcol,
+                    (void *)&status, (void *)&bars, (void *)&err, (void *)&pr,   (void *)&pc,   (void *)&dots,
+                    (void *)&dcap};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)nca_group_kernel, dim3(grid), dim3(NG_THREADS), args,
+                                                (size_t)dcap * 8, st);
+    count_launch();
+    return e;
+}
+
+size_t nca_group_part_bytes() { return sizeof(NgPart); }
+
+}  // namespace h2w
