@@ -136,6 +136,7 @@ struct h2w_handle {
     // multiple right-hand sides: interleaved workspaces (ws_n x rp), staging, batched GMRES
     DBuf<double> m_wsd, m_xi, m_yi, m_ri, m_di, m_bi, m_stage_x, m_stage_y, m_onorm, m_ores;
     DBuf<float> m_wsf, m_xf;
+    DBuf<double> d_opdf, m_xdf;  // (hi, lo) FP32 pairs (8 bytes each) of the operator and of an input block
     std::vector<int64_t> ph_t0, ph_t1;   // phase target ranges (per-phase launches)
     DBuf<double> gb_V, gb_w, gb_vcur, gb_H, gb_cs, gb_sn, gb_s, gb_part, gb_hsum, gb_normb, gb_resid, gb_y;
     DBuf<int32_t> gb_conv, gb_iter;
@@ -1663,6 +1664,7 @@ void build_plan(h2w_handle *h) {
     }
     CK(cudaStreamSynchronize(st));
     h->d_op32.reset();
+    h->d_opdf.reset();
     h->d_ws32.reset();
 }
 
@@ -1938,10 +1940,19 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
     } else {
         if (h->m_wsd.n < wsz) h->m_wsd.alloc(wsz);
         CK(cudaMemsetAsync(h->m_wsd.p, 0, wsz * 8, st));
+        if (prec == H2W_PREC_DF64) {  // operator split once; the input block split per product
+            if (!h->d_opdf.p) {
+                h->d_opdf.alloc((size_t)h->op_n);
+                CK(launch_mr_split(h->d_op.p, h->d_opdf.p, h->op_n, st));
+            }
+            const size_t nx = (size_t)h->tree.N * (size_t)rp;
+            if (h->m_xdf.n < nx) h->m_xdf.alloc(nx);
+            CK(launch_mr_split(xi, h->m_xdf.p, (int64_t)nx, st));
+        }
         mr_prof(h, prec, rp, st, [&] {
             if (prec == H2W_PREC_DF64)
-                return launch_mr_df64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op.p,
-                                      h->m_wsd.p, xi, yi, h->d_bar.p, h->d_err.p, st);
+                return launch_mr_df64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p,
+                                      h->d_opdf.p, h->m_wsd.p, h->m_xdf.p, yi, h->d_bar.p, h->d_err.p, st);
             return launch_mr_f64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op.p,
                                  h->m_wsd.p, xi, yi, h->d_bar.p, h->d_err.p, st);
         });

@@ -216,12 +216,16 @@ cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, cons
 cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st);
-// FP64 operator and vectors, double-FP32 arithmetic on the FP32 pipes
-// (each product and sum carried as an FP32 pair; about 2^-44 relative per
-// term instead of FP64's 2^-53, at the FP32 pipes' rate).
+// Double-FP32 arithmetic on the FP32 pipes (each product and sum carried as
+// an FP32 pair; about 2^-44 relative per term instead of FP64's 2^-53): A and
+// xin are (hi, lo) pairs (launch_mr_split of the FP64 operator and input),
+// the workspace and the result FP64.
 cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                            const MrPhases *phased, int32_t *ctr, const double *A, double *ws, const double *xin, double *yout,
                            unsigned *bar, int32_t *err, cudaStream_t st);
+// (hi, lo) FP32 pairs of n doubles (8 bytes each, the double-FP32 product's
+// operator and input formats)
+cudaError_t launch_mr_split(const double *a, void *b, int64_t n, cudaStream_t st);
 cudaError_t launch_mr_pack(const double *x, int64_t ldx, double *xi, const int32_t *perm, int64_t n, int nrhs,
                            int rp, cudaStream_t st);
 cudaError_t launch_mr_unpack(const double *yi, double *y, int64_t ldy, const int32_t *perm, int64_t n, int nrhs,

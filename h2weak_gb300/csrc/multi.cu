@@ -94,9 +94,10 @@ __device__ __forceinline__ void df_get4(float2 *o, const float2 *p) {
 }
 
 // One target of the packed record stream (record layout as the
-// single-vector GEMV: header, panels, segments). DF (with T = double): the
-// FP64 operand tiles are split into FP32 pairs when staged and multiplied
-// with double-FP32 arithmetic.
+// single-vector GEMV: header, panels, segments). DF (with T = double): A and
+// xin hold (hi, lo) FP32 pairs in place of doubles (split once, mr_split),
+// workspace values are split when staged, and the tiles are multiplied with
+// double-FP32 arithmetic.
 template <class T, int RP, bool DF = false>
 __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *__restrict__ roff,
                                           const int64_t *__restrict__ blob, const T *__restrict__ A, T *ws,
@@ -139,6 +140,7 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
     __syncthreads();
 
     V ra[NA], rx[NX];
+    bool xws[NX];  // DF: the source row came from the FP64 workspace (split on staging)
     // load chunk (panel q, columns c0 .. c0+KC) of row tile rt0 into registers
     auto load = [&](int q, int c0, int rt0) {
         const int64_t pa = pan[3 * q];
@@ -163,8 +165,10 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
             const int v = tid + NT * u;
             const int row = v / (RP / VN), cv = (v % (RP / VN)) * VN;
             mr_zero(rx[u]);
+            xws[u] = false;
             if (c0 + row < w) {
                 const int m = map[xoff + c0 + row];
+                xws[u] = m >= 0;
                 if (m >= 0) rx[u] = *reinterpret_cast<const V *>(ws + (int64_t)m * RP + cv);
                 else if (m <= -2) rx[u] = *reinterpret_cast<const V *>(xin + (int64_t)(-2 - m) * RP + cv);
             }
@@ -175,20 +179,20 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
         for (int u = 0; u < NA; ++u) {
             const int v = tid + NT * u;
             T *d = As + sb * (MR_KC * MR_MT) + (v / (MR_MT / VN)) * MR_MT + (v % (MR_MT / VN)) * VN;
-            if constexpr (DF) {
-                const float2 h0 = df_split(ra[u].x), h1 = df_split(ra[u].y);
-                *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
-            } else {
-                *reinterpret_cast<V *>(d) = ra[u];
-            }
+            // DF: the operator is stored pre-split (hi, lo FP32 pairs): the bits go as they are
+            *reinterpret_cast<V *>(d) = ra[u];
         }
 #pragma unroll
         for (int u = 0; u < NX; ++u) {
             const int v = tid + NT * u;
             T *d = Xs + sb * (MR_KC * RP) + (v / (RP / VN)) * RP + (v % (RP / VN)) * VN;
             if constexpr (DF) {
-                const float2 h0 = df_split(rx[u].x), h1 = df_split(rx[u].y);
-                *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
+                if (xws[u]) {  // FP64 workspace values: split here
+                    const float2 h0 = df_split(rx[u].x), h1 = df_split(rx[u].y);
+                    *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
+                } else {  // the input block is pre-split
+                    *reinterpret_cast<V *>(d) = rx[u];
+                }
             } else {
                 *reinterpret_cast<V *>(d) = rx[u];
             }
@@ -394,6 +398,18 @@ cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, cons
                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st) {
     return mr_dispatch<float>(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+}
+
+// b[i] = (hi, lo) FP32 pair of a[i] (df_split), for the double-FP32 product
+__global__ void mr_split_kernel(const double *__restrict__ a, float2 *__restrict__ b, int64_t n) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        b[e] = df_split(a[e]);
+}
+cudaError_t launch_mr_split(const double *a, void *b, int64_t n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    mr_split_kernel<<<1216, 256, 0, st>>>(a, reinterpret_cast<float2 *>(b), n);
+    count_launch();
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------ pack / unpack ---
