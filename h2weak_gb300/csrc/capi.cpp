@@ -153,6 +153,11 @@ struct h2w_handle {
     std::vector<LoopGraph> loops;
     bool use_graphs = true, graph_failed = false;
     int ir_resid_prec = H2W_PREC_FP64;   // refinement residuals after the first (batched IR)
+    // refinement residual updating r <- r - A32 d (H2W_OPT_IR_UPDATE) and the calibrated
+    // error of the FP32 products per unit input norm (< 0: not measured for this operator)
+    bool ir_update = true;
+    double eta_multi = -1.0, eta_single = -1.0;
+    DBuf<double> m_ti, m_dn, s_t;
     // learned NCA proposals: model, assembly switch, training-data recorder, statistics
     DBuf<float> d_mlp;
     float mlp_calib = 1.f;
@@ -1180,6 +1185,7 @@ void pack_records(const PlanBuilder &pb, const std::vector<Phase> &phases, std::
 // for the profiling statistics.
 void realize_single(h2w_handle *h, int64_t row_split) {
     if (!h->plan) throw ApiError(H2W_ERR_STATE, "operator not assembled");
+    h->eta_single = -1.0;  // new cuts, new rounding: calibrate again
     if (row_split < 256 || row_split > (int64_t(1) << 24)) throw ApiError(H2W_ERR_ARG, "row split out of range");
     PlanBuilder &pb = *h->plan;
     std::vector<int64_t> roff, blob, pstart;
@@ -1218,6 +1224,7 @@ void realize_single(h2w_handle *h, int64_t row_split) {
 // few small uploads); the operator itself is untouched.
 void realize_multi(h2w_handle *h, int64_t cap) {
     if (!h->plan) throw ApiError(H2W_ERR_STATE, "operator not assembled");
+    h->eta_multi = -1.0;
     if (cap < 32 || cap > MR_XS_ELEMS || cap % 4) throw ApiError(H2W_ERR_ARG, "multi-vector column cap out of range");
     PlanBuilder &pb = *h->plan;
     std::vector<int64_t> roff, blob, pstart;
@@ -1666,6 +1673,7 @@ void build_plan(h2w_handle *h) {
     h->d_op32.reset();
     h->d_opdf.reset();
     h->d_ws32.reset();
+    h->eta_multi = h->eta_single = -1.0;
 }
 
 // Stored-entry count of the reference (findMemory_n / findMemory_sn).
@@ -2039,7 +2047,6 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
     bool looped = false;
     if (!done && h->use_graphs && !h->graph_failed && !h->prof) {
         // graph path: the batched Arnoldi steps as one while-loop graph launch
-        if (!gmb_attr(g)) throw ApiError(H2W_ERR_ARG, "batched GMRES: Krylov dimension too large for shared memory");
         run_matvec_multi(h, prec, rp, g.vcur, g.w, st);  // one-time set-up outside the capture
         int64_t kps = 0;
         cudaGraphExec_t ex = loop_graph(h, 1, prec, max_iter, rp, nrhs, tol, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
@@ -2126,6 +2133,66 @@ double dnorm(h2w_handle *h, const double *x) {
     CK(cudaMemcpyAsync(&v, h->g_scal.p + 4, 8, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return v;
+}
+
+// Refinement residual updating. After an accurate residual r_k = b - A x_k,
+// the next one is r_{k+1} = r_k - A d_k in exact arithmetic; forming A d_k
+// with the FP32 operator costs an error of about eta * ||d_k||, eta being the
+// FP32 product's error per unit input norm. That update replaces the FP64
+// (or double-FP32) product while the summed bound since the last accurate
+// residual, IR_UPDATE_SAFETY * eta * ||d||, stays below IR_UPDATE_SHARE of
+// the stopping tolerance times ||b||; the stopping test and the reported
+// residual add that bound to ||r||, so they bound the true residual. Updates
+// also need the accurate residual's own rounding error, estimated as
+// IR_UPDATE_SAFETY * eta * 2^-29 * ||x|| (FP64 unit roundoff in place of
+// FP32's), to be below IR_UPDATE_FLOOR of the tolerance times ||b||: near the
+// FP64 floor an updated residual would keep falling while the true one
+// cannot. eta is measured once per operator: max over calibration vectors z
+// (pseudo-random and smooth) of ||A32 z - A z|| / ||z||.
+constexpr double IR_UPDATE_SAFETY = 10.0, IR_UPDATE_SHARE = 0.25, IR_UPDATE_FLOOR = 0.01;
+constexpr double IR_U64_OVER_U32 = 0x1.0p-29;
+
+double fp32_error_single(h2w_handle *h, cudaStream_t st) {
+    if (h->eta_single >= 0) return h->eta_single;
+    const int64_t N = h->tree.N;
+    for (DBuf<double> *v : {&h->s_d, &h->s_r, &h->s_t})
+        if (v->n < (size_t)N) v->alloc((size_t)N);
+    double eta = 0.0;
+    for (int c = 0; c < 2; ++c) {
+        CK(launch_calib_fill(h->s_d.p, N, 1, c, st));
+        run_matvec_f32(h, h->s_d.p, h->s_r.p, st, true);
+        run_matvec_f64(h, h->s_d.p, h->s_t.p, st, true);
+        CK(vec_axpby(1.0, h->s_r.p, -1.0, h->s_t.p, h->s_r.p, N, st));
+        const double nz = dnorm(h, h->s_d.p);
+        if (nz > 0) eta = std::max(eta, dnorm(h, h->s_r.p) / nz);
+    }
+    h->eta_single = eta;
+    return eta;
+}
+
+// The same for the multi-vector product: rp calibration columns at once, the
+// accurate product in the refinement's residual precision. Uses m_ri, m_di, m_ti.
+double fp32_error_multi(h2w_handle *h, const GmresBatch &g, int rp, cudaStream_t st) {
+    if (h->eta_multi >= 0) return h->eta_multi;
+    const int64_t N = h->tree.N;
+    const size_t len = (size_t)N * rp;
+    if (h->m_ti.n < (size_t)N * MR_MAX) h->m_ti.alloc((size_t)N * MR_MAX);
+    if (h->m_dn.n < (size_t)2 * MR_MAX) h->m_dn.alloc((size_t)2 * MR_MAX);
+    double *z = h->m_di.p, *y32 = h->m_ri.p, *y = h->m_ti.p;
+    CK(launch_calib_fill(z, N, rp, 0, st));
+    run_matvec_multi(h, H2W_PREC_FP32, rp, z, y32, st);
+    run_matvec_multi(h, h->ir_resid_prec, rp, z, y, st);
+    CK(vec_axpby(1.0, y32, -1.0, y, y32, (int64_t)len, st));
+    CK(gmb_norms(g, y32, h->m_dn.p, 0, st));
+    CK(gmb_norms(g, z, h->m_dn.p + MR_MAX, 0, st));
+    std::vector<double> n((size_t)2 * MR_MAX);
+    CK(cudaMemcpyAsync(n.data(), h->m_dn.p, n.size() * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double eta = 0.0;
+    for (int c = 0; c < rp; ++c)
+        if (n[(size_t)(MR_MAX + c)] > 0) eta = std::max(eta, n[(size_t)c] / n[(size_t)(MR_MAX + c)]);
+    h->eta_multi = eta;
+    return eta;
 }
 
 // Solve the upper-triangular least-squares system H(0:k,0:k) y = s(0:k) on
@@ -3041,7 +3108,7 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         GmresDev g = gmres_state(h, inner_iter);
         (void)g;
         DBuf<double> &r = h->s_r, &d = h->s_d, &bp = h->s_b, &xp = h->s_x;
-        for (DBuf<double> *v : {&r, &d, &bp, &xp})
+        for (DBuf<double> *v : {&r, &d, &bp, &xp, &h->s_t})
             if (v->n < (size_t)N) v->alloc((size_t)N);
         CK(launch_gather_f64(db, bp.p, h->d_perm.p, N, st));
         CK(launch_gather_f64(dx, xp.p, h->d_perm.p, N, st));
@@ -3054,13 +3121,28 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         *inner_total = 0;
         *outer_iters = 0;
         int rc = H2W_ERR_NOT_CONVERGED;
+        const double eta = h->ir_update ? fp32_error_single(h, st) : 0.0;
+        double drift = HUGE_VAL;  // error bound of r since the last accurate residual
+        bool above_floor = false;  // the accurate residual's own error is far below the tolerance
         for (int o = 0; o <= max_outer; ++o) {
-            // residual: FP32 operator at x0 (a correction only), then FP64 (the stopping test)
-            if (o == 0) run_matvec_f32(h, dx, r.p, st, true);
-            else run_matvec_f64(h, dx, r.p, st, true);
-            CK(vec_axpby(1.0, db, -1.0, r.p, r.p, N, st));
+            // residual: FP32 operator at x0 (a correction only), then FP64 (the
+            // stopping test), or r -= A32 d while its error bound allows
+            double add = HUGE_VAL;
+            if (h->ir_update && o >= 2 && above_floor) add = IR_UPDATE_SAFETY * eta * dnorm(h, d.p);
+            if (drift + add <= IR_UPDATE_SHARE * tol * normb) {
+                run_matvec_f32(h, d.p, h->s_t.p, st, true);
+                CK(vec_axpby(1.0, r.p, -1.0, h->s_t.p, r.p, N, st));
+                drift += add;
+            } else {
+                if (o == 0) run_matvec_f32(h, dx, r.p, st, true);
+                else run_matvec_f64(h, dx, r.p, st, true);
+                CK(vec_axpby(1.0, db, -1.0, r.p, r.p, N, st));
+                drift = o == 0 ? HUGE_VAL : 0.0;
+                if (o == 1 && h->ir_update)
+                    above_floor = IR_UPDATE_SAFETY * eta * IR_U64_OVER_U32 * dnorm(h, dx) <= IR_UPDATE_FLOOR * tol * normb;
+            }
             if (o > 0) {
-                *resid = dnorm(h, r.p) / normb;
+                *resid = (dnorm(h, r.p) + drift) / normb;
                 if (*resid < tol) { rc = H2W_OK; break; }
                 if (o == max_outer) break;
             }
@@ -3118,6 +3200,8 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
         if (h->m_di.n < (size_t)N * MR_MAX) h->m_di.alloc((size_t)N * MR_MAX);
         if (!h->m_onorm.p) h->m_onorm.alloc(MR_MAX);
         if (!h->m_ores.p) h->m_ores.alloc(MR_MAX);
+        if (h->m_ti.n < (size_t)N * MR_MAX) h->m_ti.alloc((size_t)N * MR_MAX);
+        if (h->m_dn.n < (size_t)2 * MR_MAX) h->m_dn.alloc((size_t)2 * MR_MAX);
         for_rhs_blocks(h, b, x, nrhs, where, [&](int c0, int nc, int rp, double *bi, double *xi) {
             GmresBatch g = gmb_state(h, inner_iter, rp, nc);
             const size_t len = (size_t)N * rp;
@@ -3125,20 +3209,51 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
             std::vector<double> nb((size_t)rp), nr((size_t)rp);
             CK(cudaMemcpyAsync(nb.data(), h->m_onorm.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
             std::vector<int> it((size_t)rp);
-            std::vector<double> ir((size_t)rp);
+            std::vector<double> ir((size_t)rp), nd((size_t)rp);
+            std::vector<double> drift((size_t)rp, HUGE_VAL);  // error bound of r since the last accurate residual
+            bool above_floor = false;  // every column's accurate-residual error far below its tolerance
+            const double eta = h->ir_update ? fp32_error_multi(h, g, rp, st) : 0.0;
             bool ok = false;
             for (int o = 0; o <= max_outer; ++o) {
                 // residual r = b - A x: FP32 operator at x0 (a correction only), then
-                // FP64 (or double-FP32) products, which are the stopping test
-                run_matvec_multi(h, o == 0 ? H2W_PREC_FP32 : h->ir_resid_prec, rp, xi, h->m_ri.p, st);
-                CK(vec_axpby(1.0, bi, -1.0, h->m_ri.p, h->m_ri.p, (int64_t)len, st));
+                // FP64 (or double-FP32) products, which are the stopping test, or
+                // r -= A32 d while every column's error bound allows it
+                bool upd = h->ir_update && o >= 2 && above_floor;
+                if (upd) {
+                    CK(gmb_norms(g, h->m_di.p, h->m_dn.p, 0, st));
+                    CK(cudaMemcpyAsync(nd.data(), h->m_dn.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
+                    CK(cudaStreamSynchronize(st));
+                    for (int c = 0; c < nc; ++c)
+                        if (!(drift[(size_t)c] + IR_UPDATE_SAFETY * eta * nd[(size_t)c] <=
+                              IR_UPDATE_SHARE * tol * nb[(size_t)c]))
+                            upd = false;
+                }
+                if (upd) {
+                    run_matvec_multi(h, H2W_PREC_FP32, rp, h->m_di.p, h->m_ti.p, st);
+                    CK(vec_axpby(1.0, h->m_ri.p, -1.0, h->m_ti.p, h->m_ri.p, (int64_t)len, st));
+                    for (int c = 0; c < nc; ++c) drift[(size_t)c] += IR_UPDATE_SAFETY * eta * nd[(size_t)c];
+                } else {
+                    run_matvec_multi(h, o == 0 ? H2W_PREC_FP32 : h->ir_resid_prec, rp, xi, h->m_ri.p, st);
+                    CK(vec_axpby(1.0, bi, -1.0, h->m_ri.p, h->m_ri.p, (int64_t)len, st));
+                    std::fill(drift.begin(), drift.end(), o == 0 ? HUGE_VAL : 0.0);
+                    if (o == 1 && h->ir_update) {
+                        CK(gmb_norms(g, xi, h->m_dn.p, 0, st));
+                        CK(cudaMemcpyAsync(nd.data(), h->m_dn.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
+                        CK(cudaStreamSynchronize(st));
+                        above_floor = true;
+                        for (int c = 0; c < nc; ++c)
+                            if (!(IR_UPDATE_SAFETY * eta * IR_U64_OVER_U32 * nd[(size_t)c] <=
+                                  IR_UPDATE_FLOOR * tol * nb[(size_t)c]))
+                                above_floor = false;
+                    }
+                }
                 if (o > 0) {
                     CK(gmb_norms(g, h->m_ri.p, h->m_ores.p, 0, st));
                     CK(cudaMemcpyAsync(nr.data(), h->m_ores.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
                     CK(cudaStreamSynchronize(st));
                     ok = true;
                     for (int c = 0; c < nc; ++c) {
-                        resid[c0 + c] = nr[(size_t)c] / nb[(size_t)c];
+                        resid[c0 + c] = (nr[(size_t)c] + drift[(size_t)c]) / nb[(size_t)c];
                         if (!(resid[c0 + c] < tol)) ok = false;
                     }
                     if (ok || o == max_outer) break;
@@ -3176,6 +3291,8 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
             if (h->has_op) realize_single(h, value);
             else if (value < 256 || value > (int64_t(1) << 24)) throw ApiError(H2W_ERR_ARG, "row split out of range");
             h->row_split = value;
+        } else if (option == H2W_OPT_IR_UPDATE) {
+            h->ir_update = value != 0;
         } else if (option == H2W_OPT_COOP) {
             h->coop = value != 0;
             for (auto &g : h->loops) {  // captured steps hold the other launch form
@@ -3198,6 +3315,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_IR_RESIDUAL) *value = h->ir_resid_prec;
         else if (option == H2W_OPT_MULTI_XW) *value = h->mr_xw;
         else if (option == H2W_OPT_ROW_SPLIT) *value = h->row_split;
+        else if (option == H2W_OPT_IR_UPDATE) *value = h->ir_update ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });

@@ -226,6 +226,8 @@ cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, con
 // (hi, lo) FP32 pairs of n doubles (8 bytes each, the double-FP32 product's
 // operator and input formats)
 cudaError_t launch_mr_split(const double *a, void *b, int64_t n, cudaStream_t st);
+// calibration vectors (even columns pseudo-random, odd columns smooth), n x rp interleaved
+cudaError_t launch_calib_fill(double *z, int64_t n, int rp, int c0, cudaStream_t st);
 cudaError_t launch_mr_pack(const double *x, int64_t ldx, double *xi, const int32_t *perm, int64_t n, int nrhs,
                            int rp, cudaStream_t st);
 cudaError_t launch_mr_unpack(const double *yi, double *y, int64_t ldy, const int32_t *perm, int64_t n, int nrhs,
@@ -250,7 +252,6 @@ struct GmresBatch {
 };
 cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
 cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st);
-bool gmb_attr(const GmresBatch &g);   // one-time kernel attributes for Krylov dimension g.m
 cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st);
 cudaError_t gmb_loop(const GmresBatch &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
 cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st);

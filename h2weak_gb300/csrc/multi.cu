@@ -412,6 +412,33 @@ cudaError_t launch_mr_split(const double *a, void *b, int64_t n, cudaStream_t st
     return cudaGetLastError();
 }
 
+// Calibration vectors of the FP32 product's error (interleaved, rp columns,
+// column index c0 + e % rp): even columns pseudo-random in [-1, 1) (splitmix64
+// of the element index), odd columns smooth, cos(pi * k * (t + 0.5) / n).
+__global__ void mr_calib_fill_kernel(double *__restrict__ z, int64_t n, int rp, int c0) {
+    const int64_t tot = n * rp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = e / rp;
+        const int c = c0 + (int)(e % rp);
+        double v;
+        if (c % 2 == 0) {
+            uint64_t x = (uint64_t)t * 64u + (uint64_t)c + 0x9E3779B97F4A7C15ull;
+            x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+            x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+            x ^= x >> 31;
+            v = 2.0 * ((double)(x >> 11) * 0x1.0p-53) - 1.0;
+        } else {
+            v = cospi((double)(c / 2 + 1) * ((double)t + 0.5) / (double)n);
+        }
+        z[e] = v;
+    }
+}
+cudaError_t launch_calib_fill(double *z, int64_t n, int rp, int c0, cudaStream_t st) {
+    mr_calib_fill_kernel<<<1216, 256, 0, st>>>(z, n, rp, c0);
+    count_launch();
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------ pack / unpack ---
 // xi[t*rp + c] = x[perm[t] + c*ldx] for c < nrhs, 0 for the padding columns
 __global__ void mr_pack_kernel(const double *__restrict__ x, int64_t ldx, double *__restrict__ xi,
@@ -474,31 +501,53 @@ __device__ __forceinline__ size_t gmb_h(const GmresBatch &g, int c, int row, int
 
 // out[(blk*(m+1) + k)*rp + c] = sum over the block's rows of a_k[t, c] * b[t, c],
 // k = 0..kn-1, a_k = a + k*N*rp (kn = 1: a itself)
-// Four a_k per sweep over the rows (b read once per four); red: 4*GMB_THREADS.
+// Four a_k per sweep over the rows (b read once per four), four rows per
+// iteration so that 20 loads per thread are in flight; red: 4*GMB_THREADS.
+__device__ __forceinline__ void gmb_block_sum(const GmresBatch &g, const double *acc, int nout, double *red,
+                                              double *out) {
+    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) red[(j * RL + rl) * rp + c] = acc[j];
+    __syncthreads();
+    if (rl == 0)
+        for (int j = 0; j < nout; ++j) {
+            double s2 = 0.0;
+            for (int q = 0; q < RL; ++q) s2 += red[(j * RL + q) * rp + c];
+            out[((size_t)blockIdx.x * (g.m + 1) + j) * rp + c] = s2;
+        }
+    __syncthreads();
+}
 __device__ void gmb_block_dots(const GmresBatch &g, const double *a, const double *b, int kn, int64_t r0,
                                int64_t r1, double *red, double *out) {
     const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
     const size_t stride = (size_t)g.N * rp;
+    const int64_t step = (int64_t)RL * rp;
     for (int k0 = 0; k0 < kn; k0 += 4) {
         const int kc = kn - k0 < 4 ? kn - k0 : 4;
+        const double *ak = a + (size_t)k0 * stride;
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll 2
-        for (int64_t t = r0 + rl; t < r1; t += RL) {
+        int64_t t = r0 + rl;
+        for (; t + 3 * RL < r1; t += 4 * RL) {
+            const int64_t o = t * rp + c;
+            double bv[4], av[4][4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) bv[u] = b[o + u * step];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) av[u][j] = j < kc ? ak[j * stride + o + u * step] : 0.0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[j] += av[u][j] * bv[u];
+        }
+        for (; t < r1; t += RL) {
             const double bv = b[t * rp + c];
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                if (j < kc) acc[j] += a[(k0 + j) * stride + t * rp + c] * bv;
+                if (j < kc) acc[j] += ak[j * stride + t * rp + c] * bv;
         }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) red[(j * RL + rl) * rp + c] = acc[j];
-        __syncthreads();
-        if (rl == 0)
-            for (int j = 0; j < kc; ++j) {
-                double s2 = 0.0;
-                for (int q = 0; q < RL; ++q) s2 += red[(j * RL + q) * rp + c];
-                out[((size_t)blockIdx.x * (g.m + 1) + k0 + j) * rp + c] = s2;
-            }
-        __syncthreads();
+        gmb_block_sum(g, acc, kc, red, out + (size_t)k0 * rp);
     }
 }
 
@@ -533,31 +582,85 @@ __global__ void gmb_reduce(GmresBatch g, int all) {
     }
 }
 
-// h = hsum; H(:, i) (=|+=) h; w -= V h; then new dots (pass 0) or ||w||^2 partials (pass 1)
+// h = hsum; H(:, i) (=|+=) h; w -= V h; then new dots (pass 0) or ||w||^2 partials (pass 1).
+// With at most four basis vectors the dots are formed in the same sweep from
+// the basis values already in registers (the basis is read once); with more,
+// w is updated four basis vectors at a time and a second sweep forms the dots.
 __global__ void gmb_update(GmresBatch g, int pass) {
-    extern __shared__ double gmb_sm[];
-    double *h = gmb_sm;
-    double *red = gmb_sm + (size_t)(g.m + 1) * g.rp;  // 4 * GMB_THREADS
-    const int i = *g.iter, rp = g.rp;
-    for (int e = threadIdx.x; e < (i + 1) * rp; e += blockDim.x) h[e] = g.hsum[e];
-    __syncthreads();
+    __shared__ double red[4 * GMB_THREADS];
+    const int i = *g.iter, rp = g.rp, kn = i + 1;
     if (blockIdx.x == 0)
-        for (int e = threadIdx.x; e < (i + 1) * rp; e += blockDim.x) {
+        for (int e = threadIdx.x; e < kn * rp; e += blockDim.x) {
             const int k = e / rp, c = e % rp;
             double *Hk = g.H + gmb_h(g, c, k, i);
-            *Hk = pass == 0 ? h[e] : *Hk + h[e];
+            *Hk = pass == 0 ? g.hsum[e] : *Hk + g.hsum[e];
         }
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
     const int c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
     const size_t stride = (size_t)g.N * rp;
-    for (int64_t t = r0 + rl; t < r1; t += RL) {
-        double v = g.w[t * rp + c];
-        for (int k = 0; k <= i; ++k) v -= g.V[k * stride + t * rp + c] * h[k * rp + c];
-        g.w[t * rp + c] = v;
+    const int64_t step = (int64_t)RL * rp;
+    double *w = g.w;
+    for (int k0 = 0; k0 < kn; k0 += 4) {
+        const int kc = kn - k0 < 4 ? kn - k0 : 4;
+        const bool fused = kn <= 4;
+        const double *Vk = g.V + (size_t)k0 * stride;
+        double hk[4], acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) hk[j] = j < kc ? g.hsum[(size_t)(k0 + j) * rp + c] : 0.0;
+        int64_t t = r0 + rl;
+        for (; t + 3 * RL < r1; t += 4 * RL) {
+            const int64_t o = t * rp + c;
+            double wv[4], vk[4][4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) wv[u] = w[o + u * step];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) vk[u][j] = j < kc ? Vk[j * stride + o + u * step] : 0.0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                double v = wv[u];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j < kc) v -= vk[u][j] * hk[j];
+                w[o + u * step] = v;
+                if (fused) {
+                    if (pass == 0) {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[j] += vk[u][j] * v;
+                    } else {
+                        acc[0] += v * v;
+                    }
+                }
+            }
+        }
+        for (; t < r1; t += RL) {
+            const int64_t o = t * rp + c;
+            double vk[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) vk[j] = j < kc ? Vk[j * stride + o] : 0.0;
+            double v = w[o];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j < kc) v -= vk[j] * hk[j];
+            w[o] = v;
+            if (fused) {
+                if (pass == 0) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[j] += vk[j] * v;
+                } else {
+                    acc[0] += v * v;
+                }
+            }
+        }
+        if (fused) {
+            gmb_block_sum(g, acc, pass == 0 ? kn : 1, red, g.part);
+            return;
+        }
     }
     __syncthreads();
-    if (pass == 0) gmb_block_dots(g, g.V, g.w, i + 1, r0, r1, red, g.part);
+    if (pass == 0) gmb_block_dots(g, g.V, g.w, kn, r0, r1, red, g.part);
     else gmb_block_dots(g, g.w, g.w, 1, r0, r1, red, g.part);
 }
 
@@ -571,7 +674,20 @@ __global__ void gmb_normalise(GmresBatch g) {
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
     double *Vn = g.V + (size_t)(i + 1) * g.N * rp;
-    for (int64_t t = r0 + rl; t < r1; t += RL) {
+    const int64_t step = (int64_t)RL * rp;
+    int64_t t = r0 + rl;
+    for (; t + 3 * RL < r1; t += 4 * RL) {
+        const int64_t o = t * rp + c;
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = ih * g.w[o + u * step];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            Vn[o + u * step] = v[u];
+            g.vcur[o + u * step] = v[u];
+        }
+    }
+    for (; t < r1; t += RL) {
         const double v = ih * g.w[t * rp + c];
         Vn[t * rp + c] = v;
         g.vcur[t * rp + c] = v;
@@ -705,17 +821,6 @@ __global__ void gmb_loop_cond(GmresBatch g, cudaGraphConditionalHandle hnd) {
     cudaGraphSetConditional(hnd, (running && c < g.m) ? 1u : 0u);
 }
 
-bool gmb_attr(const GmresBatch &g) {
-    static int set = 0;
-    const size_t need = ((size_t)(g.m + 1) * g.rp + 4 * GMB_THREADS) * 8;
-    if ((int)need > set) {
-        if (cudaFuncSetAttribute(gmb_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) != cudaSuccess)
-            return false;
-        set = (int)need;
-    }
-    return true;
-}
-
 cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st) {
     gmb_colnorm_part<<<g.nblk, GMB_THREADS, 0, st>>>(g, v);
     gmb_colnorm_fin<<<1, 64, 0, st>>>(g, out, zero_to_one);
@@ -730,13 +835,11 @@ cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, do
     return cudaGetLastError();
 }
 cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st) {
-    if (!gmb_attr(g)) return cudaErrorInvalidValue;
-    const size_t smu = ((size_t)(g.m + 1) * g.rp + 4 * GMB_THREADS) * 8;
     gmb_dots<<<g.nblk, GMB_THREADS, 0, st>>>(g);
     gmb_reduce<<<g.m + 1, GMB_THREADS, 0, st>>>(g, 1);
-    gmb_update<<<g.nblk, GMB_THREADS, smu, st>>>(g, 0);
+    gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 0);
     gmb_reduce<<<g.m + 1, GMB_THREADS, 0, st>>>(g, 1);
-    gmb_update<<<g.nblk, GMB_THREADS, smu, st>>>(g, 1);
+    gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 1);
     gmb_reduce<<<1, GMB_THREADS, 0, st>>>(g, 0);
     gmb_normalise<<<g.nblk, GMB_THREADS, 0, st>>>(g);
     gmb_givens<<<1, 64, 0, st>>>(g, tol);

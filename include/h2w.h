@@ -186,8 +186,20 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 H2W_PREC_DF64. (The first residual, at the caller's x0, is
  *                 formed with the FP32 operator and is not tested for
  *                 convergence; the inner solve only needs it to the inner
- *                 tolerance.) */
-enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4 };
+ *                 tolerance.)
+ *  H2W_OPT_IR_UPDATE  1 (default): in the refinement solvers, after an
+ *                 accurate residual r = b - A x, later residuals may be
+ *                 updated as r - A32 d (d the last correction, A32 the FP32
+ *                 operator) while the error bound of those updates,
+ *                 10 * eta * ||d|| summed, stays below 25 % of
+ *                 tol * ||b|| per column; eta = ||A32 z - A z|| / ||z||,
+ *                 measured once per operator on pseudo-random and smooth z.
+ *                 The stopping test and the reported residual add that
+ *                 bound to ||r||. Not used near the FP64 floor (where
+ *                 10 * eta * 2^-29 * ||x|| exceeds 1 % of tol * ||b||).
+ *                 0: every residual after the first is formed from x. */
+enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
+       H2W_OPT_IR_UPDATE = 5 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
