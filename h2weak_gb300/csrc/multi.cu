@@ -559,27 +559,36 @@ __global__ void gmb_dots(GmresBatch g) {
 }
 
 // hsum[k*rp + c] = sum_b part[(b*(m+1) + k)*rp + c] for k <= i (all = 1) or k = 0 (all = 0);
-// block k, its threads split the blocks' partials, then meet in shared memory
+// block k of GMB_RED threads: 1024 / rp lanes per column split the blocks'
+// partials (four loads in flight each), then meet in shared memory
+constexpr int GMB_RED = 1024;
+__device__ __forceinline__ double gmb_sum_parts(const GmresBatch &g, int k, double *red) {
+    const int rp = g.rp, c = threadIdx.x % rp, bl = threadIdx.x / rp, BL = GMB_RED / rp;
+    const size_t st = (size_t)(g.m + 1) * rp;
+    const double *p = g.part + (size_t)k * rp + c;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int b = bl;
+    for (; b + 3 * BL < g.nblk; b += 4 * BL) {
+        s0 += p[(size_t)b * st];
+        s1 += p[(size_t)(b + BL) * st];
+        s2 += p[(size_t)(b + 2 * BL) * st];
+        s3 += p[(size_t)(b + 3 * BL) * st];
+    }
+    for (; b < g.nblk; b += BL) s0 += p[(size_t)b * st];
+    red[threadIdx.x] = (s0 + s1) + (s2 + s3);
+    __syncthreads();
+    double s = 0.0;
+    if (bl == 0)
+        for (int q = 0; q < BL; ++q) s += red[q * rp + c];
+    return s;  // valid in the threads with bl == 0
+}
 __global__ void gmb_reduce(GmresBatch g, int all) {
-    __shared__ double red[GMB_THREADS];
+    __shared__ double red[GMB_RED];
     const int kn = all ? *g.iter + 1 : 1;
     const int k = blockIdx.x;
     if (k >= kn) return;
-    const int rp = g.rp, c = threadIdx.x % rp, bl = threadIdx.x / rp, BL = GMB_THREADS / rp;
-    double s0 = 0.0, s1 = 0.0;
-    int b = bl;
-    for (; b + BL < g.nblk; b += 2 * BL) {
-        s0 += g.part[((size_t)b * (g.m + 1) + k) * rp + c];
-        s1 += g.part[((size_t)(b + BL) * (g.m + 1) + k) * rp + c];
-    }
-    if (b < g.nblk) s0 += g.part[((size_t)b * (g.m + 1) + k) * rp + c];
-    red[threadIdx.x] = s0 + s1;
-    __syncthreads();
-    if (bl == 0) {
-        double s = 0.0;
-        for (int q = 0; q < BL; ++q) s += red[q * rp + c];
-        g.hsum[(size_t)k * rp + c] = s;
-    }
+    const double s = gmb_sum_parts(g, k, red);
+    if (threadIdx.x < g.rp) g.hsum[(size_t)k * g.rp + threadIdx.x] = s;
 }
 
 // h = hsum; H(:, i) (=|+=) h; w -= V h; then new dots (pass 0) or ||w||^2 partials (pass 1).
@@ -750,12 +759,9 @@ __global__ void gmb_colnorm_part(GmresBatch g, const double *__restrict__ v) {
 }
 // out[c] = sqrt(sum of the partials); zero_to_one: a zero norm becomes 1
 __global__ void gmb_colnorm_fin(GmresBatch g, double *out, int zero_to_one) {
-    const int c = threadIdx.x;
-    if (c >= g.rp) return;
-    double s = 0.0;
-    for (int b = 0; b < g.nblk; ++b) s += g.part[((size_t)b * (g.m + 1)) * g.rp + c];
-    s = sqrt(s);
-    out[c] = (zero_to_one && s == 0.0) ? 1.0 : s;
+    __shared__ double red[GMB_RED];
+    const double s = sqrt(gmb_sum_parts(g, 0, red));
+    if (threadIdx.x < g.rp) out[threadIdx.x] = (zero_to_one && s == 0.0) ? 1.0 : s;
 }
 // beta = ||w|| (hsum); V[:, 0] = vcur = w / beta; s = beta e1; per-column state
 __global__ void gmb_start_fin(GmresBatch g, double tol) {
@@ -823,24 +829,24 @@ __global__ void gmb_loop_cond(GmresBatch g, cudaGraphConditionalHandle hnd) {
 
 cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st) {
     gmb_colnorm_part<<<g.nblk, GMB_THREADS, 0, st>>>(g, v);
-    gmb_colnorm_fin<<<1, 64, 0, st>>>(g, out, zero_to_one);
+    gmb_colnorm_fin<<<1, GMB_RED, 0, st>>>(g, out, zero_to_one);
     count_launch(2);
     return cudaGetLastError();
 }
 cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st) {
     gmb_resid<<<g.nblk, GMB_THREADS, 0, st>>>(g, b, Ax);
-    gmb_reduce<<<1, GMB_THREADS, 0, st>>>(g, 0);
+    gmb_reduce<<<1, GMB_RED, 0, st>>>(g, 0);
     gmb_start_fin<<<g.nblk, GMB_THREADS, 0, st>>>(g, tol);
     count_launch(3);
     return cudaGetLastError();
 }
 cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st) {
     gmb_dots<<<g.nblk, GMB_THREADS, 0, st>>>(g);
-    gmb_reduce<<<g.m + 1, GMB_THREADS, 0, st>>>(g, 1);
+    gmb_reduce<<<g.m + 1, GMB_RED, 0, st>>>(g, 1);
     gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 0);
-    gmb_reduce<<<g.m + 1, GMB_THREADS, 0, st>>>(g, 1);
+    gmb_reduce<<<g.m + 1, GMB_RED, 0, st>>>(g, 1);
     gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 1);
-    gmb_reduce<<<1, GMB_THREADS, 0, st>>>(g, 0);
+    gmb_reduce<<<1, GMB_RED, 0, st>>>(g, 0);
     gmb_normalise<<<g.nblk, GMB_THREADS, 0, st>>>(g);
     gmb_givens<<<1, 64, 0, st>>>(g, tol);
     count_launch(8);
