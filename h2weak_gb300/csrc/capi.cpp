@@ -156,6 +156,7 @@ struct h2w_handle {
     // refinement residual updating r <- r - A32 d (H2W_OPT_IR_UPDATE) and the calibrated
     // error of the FP32 products per unit input norm (< 0: not measured for this operator)
     bool ir_update = true;
+    bool tensor = false;  // FP32 multi-vector products on the tensor cores (H2W_OPT_TENSOR)
     double eta_multi = -1.0, eta_single = -1.0;
     DBuf<double> m_ti, m_dn, s_t;
     // learned NCA proposals: model, assembly switch, training-data recorder, statistics
@@ -1941,6 +1942,9 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
         if (h->m_xf.n < nx) h->m_xf.alloc(nx);
         CK(vec_f64_to_f32(xi, h->m_xf.p, (int64_t)nx, st));
         mr_prof(h, prec, rp, st, [&] {
+            if (h->tensor)
+                return launch_mrt_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p,
+                                      h->d_op32.p, h->m_wsf.p, h->m_xf.p, yi, h->d_bar.p, h->d_err.p, st);
             return launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op32.p,
                                  h->m_wsf.p, h->m_xf.p, yi, h->d_bar.p, h->d_err.p, st);
         });
@@ -3293,6 +3297,14 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
             h->row_split = value;
         } else if (option == H2W_OPT_IR_UPDATE) {
             h->ir_update = value != 0;
+        } else if (option == H2W_OPT_TENSOR) {
+            h->tensor = value != 0;
+            h->eta_multi = -1.0;
+            for (auto &g : h->loops) {  // captured steps hold the other kernel
+                cudaGraphExecDestroy(g.exec);
+                cudaGraphDestroy(g.graph);
+            }
+            h->loops.clear();
         } else if (option == H2W_OPT_COOP) {
             h->coop = value != 0;
             for (auto &g : h->loops) {  // captured steps hold the other launch form
@@ -3316,6 +3328,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_MULTI_XW) *value = h->mr_xw;
         else if (option == H2W_OPT_ROW_SPLIT) *value = h->row_split;
         else if (option == H2W_OPT_IR_UPDATE) *value = h->ir_update ? 1 : 0;
+        else if (option == H2W_OPT_TENSOR) *value = h->tensor ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });

@@ -220,6 +220,11 @@ cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, cons
 // an FP32 pair; about 2^-44 relative per term instead of FP64's 2^-53): A and
 // xin are (hi, lo) pairs (launch_mr_split of the FP64 operator and input),
 // the workspace and the result FP64.
+// FP32 multi-vector product on the tensor cores (tcgen05 kind::tf32 with
+// hi/lo operand splitting), same records and arguments as launch_mr_f32
+cudaError_t launch_mrt_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin,
+                           double *yout, unsigned *bar, int32_t *err, cudaStream_t st);
 cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                            const MrPhases *phased, int32_t *ctr, const double *A, double *ws, const double *xin, double *yout,
                            unsigned *bar, int32_t *err, cudaStream_t st);

@@ -52,6 +52,7 @@ def main(argv=None):
     ap.add_argument("--ir-residual", default="df64", choices=["fp64", "df64"])
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--tensor", action="store_true", help="FP32 multi-vector products on the tensor cores")
     a = ap.parse_args(argv)
 
     import torch
@@ -66,6 +67,8 @@ def main(argv=None):
     out = {"what": a.what, "N": N, "assembly_s": time.time() - t0, "storage_entries": op.storage_entries()}
     if a.no_graph:
         op.set_option(hw.OPT_GRAPH, 0)
+    if a.tensor:
+        op.set_option(hw.OPT_TENSOR, 1)
     op.set_option(hw.OPT_IR_RESIDUAL, PREC[a.ir_residual])
     R = max(1, min(64, a.rhs))
     # column-major N x R blocks = rows of R x N tensors

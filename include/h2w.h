@@ -197,9 +197,16 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 The stopping test and the reported residual add that
  *                 bound to ||r||. Not used near the FP64 floor (where
  *                 10 * eta * 2^-29 * ||x|| exceeds 1 % of tol * ||b||).
- *                 0: every residual after the first is formed from x. */
+ *                 0: every residual after the first is formed from x.
+ *  H2W_OPT_TENSOR  1: FP32 multi-vector products (nrhs > 1) run on the tensor
+ *                 cores: tcgen05 TF32 MMAs on hi/lo-split operands
+ *                 (a = tf32(a) + rest; all four partial products), FP32
+ *                 accuracy; 0 (default): the FP32 FMA kernel, which is
+ *                 faster on the operators measured (one tensor-memory CTA
+ *                 per SM; targets of 20-64 rows fill half of an M = 128
+ *                 MMA at best). */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
-       H2W_OPT_IR_UPDATE = 5 };
+       H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
