@@ -361,8 +361,24 @@ def main():
     tk = kern[top]
     ctype = {"fp32": "float, FP32", "df64": "double, double-FP32", "fp64": "double, FP64"}[top]
     rp = 16 if R <= 16 else (32 if R <= 32 else 64)
+    # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu captures of the
+    # same launches on this workload: profiles/mr_coop_fp32_2d_ie_65536.md, mr_coop_df64_2d_ie_65536.md
+    ncu_traffic = {"fp32": 432.656e6 + 74.567e6, "df64": 1032.532e6 + 187.731e6}
+    # the multi-vector kernel multiplies every packed operator entry by R vectors: one FMA per
+    # term (FP32), about twelve FP32 operations per term (double-FP32); nominal FP32 peak of
+    # 152 SMs x 128 lanes x 2 flop x 2.07 GHz
+    entries = op.operator_bytes(hw.PREC_FP32) / 4
+    fp32_nominal = 152 * 128 * 2 * 2.07e9
+    ops_per_term = {"fp32": 2.0, "df64": 12.0, "fp64": 2.0}[top]
+    achieved_ops = ops_per_term * entries * R / (tk["us"] / 1e6)
     roof = {"bound": "hbm", "achieved": tk["gbs"], "peak": peak, "unit": "GB/s", "frac": tk["gbs"] / peak,
-            "traffic": None,
+            "traffic": ncu_traffic.get(top) if args.workload == "2d_ie_65536" and R == 64 else None,
+            "compute": {"pipe": "fp64" if top == "fp64" else "fp32",
+                        "ops_per_launch": ops_per_term * entries * R,
+                        "achieved_tops": achieved_ops / 1e12,
+                        "nominal_fp32_tops": fp32_nominal / 1e12,
+                        "frac_of_nominal": achieved_ops / fp32_nominal if top != "fp64" else None,
+                        "note": "each operator element feeds R FMAs: the pipe, not HBM, bounds this kernel"},
             "kernel": "mr_coop_kernel<%s, %d> (one cooperative launch = one %d-vector matvec)" % (ctype, rp, R),
             "bytes_per_launch": tk["bytes"], "launch_us": tk["us"], "launches": tk["launches"],
             "share_of_matvec_time": tk["ms"] / tot if tot else None,
@@ -387,7 +403,8 @@ def main():
         "config": {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*", "rhs_per_step": R,
                    "solver": "batched: FP32-operator inner GMRES (FP64 Arnoldi, %d columns in lockstep, one "
                              "multi-vector matvec per step) + iterative refinement, residuals FP32 at x0 then "
-                             "double-FP32 on the FP64 operator; CUDA-graph Arnoldi loop" % R,
+                             "double-FP32 on the FP64 operator, later ones updated as r - A32 d under a calibrated "
+                             "error bound; CUDA-graph Arnoldi loop" % R,
                    "autotuned": {"multi_xw": tuned_xw, "multi_mix_ms": tuned_xw_ms, "single_row_split": tuned_rs,
                                  "single_fp32_ms": tuned_rs_ms},
                    "parallelism": "replicas" if world > 1 else "single",
