@@ -2156,6 +2156,14 @@ double dnorm(h2w_handle *h, const double *x) {
 constexpr double IR_UPDATE_SAFETY = 10.0, IR_UPDATE_SHARE = 0.25, IR_UPDATE_FLOOR = 0.01;
 constexpr double IR_U64_OVER_U32 = 0x1.0p-29;
 
+// Relative tolerance of a refinement step's inner solve: enough to bring the
+// residual ||r|| to a tenth of the outer target tol * ||b||, within
+// [1e-6, 0.1]; 1e-6 when ||r|| is not known (the first step).
+double inner_tol(double tol, double nb, double nr) {
+    if (!(nr > 0) || !(nb > 0)) return 1e-6;
+    return std::min(0.1, std::max(1e-6, 0.1 * tol * nb / nr));
+}
+
 double fp32_error_single(h2w_handle *h, cudaStream_t st) {
     if (h->eta_single >= 0) return h->eta_single;
     const int64_t N = h->tree.N;
@@ -3153,8 +3161,10 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
             CK(cudaMemsetAsync(d.p, 0, (size_t)N * 8, st));
             int it = 0;
             double ires = 0;
-            // inner: relative reduction 1e-6 of the current residual, FP32 operator
-            gmres_run(h, r.p, d.p, inner_iter, 1e-6, H2W_PREC_FP32, &it, &ires, true);
+            // inner: FP32 operator, relative reduction of the current residual to a
+            // tenth of the target (1e-6 in the first step)
+            gmres_run(h, r.p, d.p, inner_iter, o == 0 ? 1e-6 : inner_tol(tol, 1.0, *resid), H2W_PREC_FP32, &it, &ires,
+                      true);
             *inner_total += it;
             CK(vec_axpby(1.0, dx, 1.0, d.p, dx, N, st));
             *outer_iters = o + 1;
@@ -3262,9 +3272,14 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
                     }
                     if (ok || o == max_outer) break;
                 }
-                // FP32-operator inner GMRES on A d = r from d = 0, relative tolerance 1e-6
+                // FP32-operator inner GMRES on A d = r from d = 0; relative tolerance: the
+                // strictest column's need (1e-6 in the first step)
+                double tin = o == 0 ? 1e-6 : 0.1;
+                if (o > 0)
+                    for (int c = 0; c < nc; ++c)
+                        tin = std::min(tin, inner_tol(tol, 1.0, resid[c0 + c]));
                 CK(cudaMemsetAsync(h->m_di.p, 0, len * 8, st));
-                gmres_batch_run(h, h->m_ri.p, h->m_di.p, rp, nc, inner_iter, 1e-6, H2W_PREC_FP32, true, it.data(),
+                gmres_batch_run(h, h->m_ri.p, h->m_di.p, rp, nc, inner_iter, tin, H2W_PREC_FP32, true, it.data(),
                                 ir.data());
                 int mx = 0;
                 for (int c = 0; c < nc; ++c) mx = std::max(mx, it[(size_t)c]);
@@ -3619,8 +3634,11 @@ int h2w_batch_gmres_ir(h2w_batch *b, const double *rhs, double *x, int max_outer
                 }
                 if (ok || o == max_outer) break;
             }
+            double tin = o == 0 ? 1e-6 : 0.1;  // the strictest problem's need (1e-6 in the first step)
+            if (o > 0)
+                for (int p = 0; p < P; ++p) tin = std::min(tin, inner_tol(tol, 1.0, resid[p]));
             CK(cudaMemsetAsync(b->d.p, 0, (size_t)b->Ntot * 8, st));
-            gms_run(b, b->r.p, b->d.p, inner_iter, 1e-6, H2W_PREC_FP32, true, it.data(), nullptr);
+            gms_run(b, b->r.p, b->d.p, inner_iter, tin, H2W_PREC_FP32, true, it.data(), nullptr);
             int mx = 0;
             for (int p = 0; p < P; ++p) mx = std::max(mx, it[(size_t)p]);
             *inner_total += mx;

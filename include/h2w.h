@@ -134,10 +134,12 @@ int h2w_matvec_static(h2w_handle *h, const double *x, double *y, int precision, 
  * ({1D,2D,3D}/codes/gmres.hpp:92-200): x0 = x on entry, stops when |s(i+1)|/||b|| < 10^-tol_pow. */
 int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_pow, int where, int *iters,
               double *resid);
-/* Mixed precision: FP32 inner GMRES (FP32 operator, from d = 0) wrapped in
- * FP64 iterative refinement; the first residual (at the caller's x0) is formed
- * with the FP32 operator and only corrects, every later residual uses the FP64
- * operator and is the stopping test: FP64 relative residual
+/* Mixed precision: FP32 inner GMRES (FP32 operator, from d = 0; relative
+ * tolerance 1e-6 in the first step, later a tenth of tol * ||b|| / ||r||,
+ * within [1e-6, 0.1]) wrapped in FP64 iterative refinement; the first
+ * residual (at the caller's x0) is formed with the FP32 operator and only
+ * corrects, later residuals use the FP64 operator (or an update under
+ * H2W_OPT_IR_UPDATE) and are the stopping test: FP64 relative residual
  * ||b - A x|| / ||b|| < 10^-tol_pow. */
 int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int inner_iter, int tol_pow, int where,
                  int *outer_iters, int *inner_total, double *resid);
@@ -157,7 +159,9 @@ int h2w_gmres_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max
  * refinement residuals from one multi-vector matvec per outer step (the first
  * with the FP32 operator, the later ones FP64, or DF64 by H2W_OPT_IR_RESIDUAL,
  * and only those tested against the tolerance) and a batched
- * FP32-operator inner GMRES (relative tolerance 1e-6, x0 = 0). resid: final
+ * FP32-operator inner GMRES (x0 = 0; relative tolerance 1e-6 in the first
+ * step, later the strictest column's need: a tenth of tol * ||b|| / ||r||,
+ * within [1e-6, 0.1]). resid: final
  * FP64 relative residual per column (nrhs entries); outer_iters: largest
  * outer count over the blocks; inner_total: inner Arnoldi steps summed over
  * outer steps and blocks (lockstep steps, not per column). */
@@ -231,7 +235,8 @@ int h2w_batch_matvec(h2w_batch *b, const double *x, double *y, int precision, in
 int h2w_batch_gmres(h2w_batch *b, const double *rhs, double *x, int max_iter, int tol_pow, int where, int *iters,
                     double *resid);
 /* Mixed precision for every problem: batched FP32-operator inner GMRES (x0 =
- * 0, relative tolerance 1e-6) and FP64 refinement (first residual with the
+ * 0; relative tolerance 1e-6 in the first step, later the strictest
+ * problem's need, as in h2w_gmres_ir_batch) and FP64 refinement (first residual with the
  * FP32 operators, the later ones FP64 and tested); resid: n final FP64
  * relative residuals. */
 int h2w_batch_gmres_ir(h2w_batch *b, const double *rhs, double *x, int max_outer, int inner_iter, int tol_pow,
