@@ -138,13 +138,12 @@ struct h2w_handle {
     DBuf<float> m_wsf, m_xf;
     DBuf<double> d_opdf, m_xdf;  // (hi, lo) FP32 pairs (8 bytes each) of the operator and of an input block
     std::vector<int64_t> ph_t0, ph_t1;   // phase target ranges (per-phase launches)
-    DBuf<double> gb_V, gb_w, gb_vcur, gb_H, gb_cs, gb_sn, gb_s, gb_part, gb_hsum, gb_normb, gb_resid, gb_y;
+    DBuf<double> gb_V, gb_w, gb_vcur, gb_H, gb_cs, gb_sn, gb_s, gb_part, gb_hsum, gb_normb, gb_resid, gb_y, gb_tol;
     DBuf<int32_t> gb_conv, gb_iter;
     int gb_m = -1, gb_rp = 0;
     // graph-captured Arnoldi loops (a while node whose body is one step)
     struct LoopGraph {
         int kind, prec, m, rp, nrhs;
-        double tol;
         uint64_t gen;
         cudaGraph_t graph;
         cudaGraphExec_t exec;
@@ -1844,14 +1843,22 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
 // (kind, precision, m, rp, nrhs, tol) and rebuilt when any device buffer was
 // reallocated since the capture. Returns nullptr when capture is unavailable
 // (the caller then runs the host loop). kps: kernels one step launches.
+// Whether loop_graph holds a valid captured step for this key (no capture needed).
+bool loop_graph_cached(h2w_handle *h, int kind, int prec, int m, int rp, int nrhs) {
+    if (!h->use_graphs || h->graph_failed || h->prof) return false;
+    const uint64_t gen = g_alloc_gen.load();
+    for (const h2w_handle::LoopGraph &L : h->loops)
+        if (L.kind == kind && L.prec == prec && L.m == m && L.rp == rp && L.nrhs == nrhs) return L.gen == gen;
+    return false;
+}
+
 template <class F>
-cudaGraphExec_t loop_graph(h2w_handle *h, int kind, int prec, int m, int rp, int nrhs, double tol, int64_t &kps,
-                           F &&body) {
+cudaGraphExec_t loop_graph(h2w_handle *h, int kind, int prec, int m, int rp, int nrhs, int64_t &kps, F &&body) {
     if (!h->use_graphs || h->graph_failed || h->prof) return nullptr;
     const uint64_t gen = g_alloc_gen.load();
     for (size_t i = 0; i < h->loops.size(); ++i) {
         h2w_handle::LoopGraph &L = h->loops[i];
-        if (L.kind == kind && L.prec == prec && L.m == m && L.rp == rp && L.nrhs == nrhs && L.tol == tol) {
+        if (L.kind == kind && L.prec == prec && L.m == m && L.rp == rp && L.nrhs == nrhs) {
             if (L.gen == gen) {
                 kps = L.kernels_per_step;
                 return L.exec;
@@ -1901,7 +1908,7 @@ cudaGraphExec_t loop_graph(h2w_handle *h, int kind, int prec, int m, int rp, int
     }
     kps = launch_count() - c0;
     count_launch(-kps);  // the captured launches run when the graph does
-    h->loops.push_back({kind, prec, m, rp, nrhs, tol, gen, graph, exec, kps});
+    h->loops.push_back({kind, prec, m, rp, nrhs, gen, graph, exec, kps});
     return exec;
 }
 
@@ -1980,7 +1987,7 @@ void ensure_multi_vectors(h2w_handle *h) {
 
 GmresBatch gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
     const int64_t N = h->tree.N;
-    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(2 * 152, (N + 255) / 256));
+    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(3 * 152, (N + 255) / 256));
     if (h->gb_m != m || h->gb_rp != rp) {
         h->gb_V.alloc((size_t)N * rp * (size_t)(m + 1));
         h->gb_w.alloc((size_t)N * rp);
@@ -1995,6 +2002,7 @@ GmresBatch gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
         h->gb_resid.alloc((size_t)rp);
         h->gb_y.alloc((size_t)(m + 1) * rp);
         h->gb_conv.alloc((size_t)rp);
+        h->gb_tol.alloc(1);
         h->gb_iter.alloc(2);
         h->gb_m = m;
         h->gb_rp = rp;
@@ -2013,6 +2021,7 @@ GmresBatch gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
     g.resid = h->gb_resid.p;
     g.y = h->gb_y.p;
     g.conv = h->gb_conv.p;
+    g.tolp = h->gb_tol.p;
     g.iter = h->gb_iter.p;
     g.N = N;
     g.m = m;
@@ -2030,6 +2039,7 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
     if (max_iter < 1 || max_iter > 400) throw ApiError(H2W_ERR_ARG, "batched GMRES: max_iter must be in 1..400");
     GmresBatch g = gmb_state(h, max_iter, rp, nrhs);
     cudaStream_t st = h->stream;
+    CK(cudaMemcpyAsync(g.tolp, &tol, 8, cudaMemcpyHostToDevice, st));  // read by the Givens step
     CK(gmb_norms(g, bi, g.normb, 1, st));
     if (x0_zero) {
         CK(gmb_start(g, bi, nullptr, tol, st));
@@ -2051,11 +2061,12 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
     bool looped = false;
     if (!done && h->use_graphs && !h->graph_failed && !h->prof) {
         // graph path: the batched Arnoldi steps as one while-loop graph launch
-        run_matvec_multi(h, prec, rp, g.vcur, g.w, st);  // one-time set-up outside the capture
+        // before a capture, one product outside it makes its buffers and launch attributes
+        if (!loop_graph_cached(h, 1, prec, max_iter, rp, nrhs)) run_matvec_multi(h, prec, rp, g.vcur, g.w, st);
         int64_t kps = 0;
-        cudaGraphExec_t ex = loop_graph(h, 1, prec, max_iter, rp, nrhs, tol, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
+        cudaGraphExec_t ex = loop_graph(h, 1, prec, max_iter, rp, nrhs, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
             run_matvec_multi(h, prec, rp, g.vcur, g.w, s);
-            CK(gmb_arnoldi(g, tol, s));
+            CK(gmb_arnoldi(g, s));
             CK(gmb_loop(g, c, s));
         });
         if (ex) {
@@ -2070,7 +2081,7 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
     }
     for (int i = 0; i < max_iter && !done && !looped; ++i) {
         run_matvec_multi(h, prec, rp, g.vcur, g.w, st);
-        CK(gmb_arnoldi(g, tol, st));
+        CK(gmb_arnoldi(g, st));
         last = i;
         done = read_conv();
     }
@@ -2247,6 +2258,7 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     GmresDev g = gmres_state(h, max_iter);
     cudaStream_t st = h->stream;
     const int64_t N = h->tree.N;
+    CK(cudaMemcpyAsync(g.scal + 6, &tol, 8, cudaMemcpyHostToDevice, st));  // read by the Givens step
     auto A = [&](const double *in, double *out) {
         if (prec == H2W_PREC_FP32) run_matvec_f32(h, in, out, st, true);
         else run_matvec_f64(h, in, out, st, true);
@@ -2271,13 +2283,15 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     if (h->use_graphs && !h->graph_failed && !h->prof) {
         if (prec == H2W_PREC_FP32) ensure_f32(h);
         gmres_prepare();
-        A(g.vcur, g.w);  // one-time launch set-up outside the capture; the step recomputes w
+        // before a capture, one product outside it makes its buffers and launch
+        // attributes (the step recomputes w)
+        if (!loop_graph_cached(h, 0, prec, max_iter, 1, 1)) A(g.vcur, g.w);
         int64_t kps = 0;
-        cudaGraphExec_t ex = loop_graph(h, 0, prec, max_iter, 1, 1, tol, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
+        cudaGraphExec_t ex = loop_graph(h, 0, prec, max_iter, 1, 1, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
             if (prec == H2W_PREC_FP32) run_matvec_f32(h, g.vcur, g.w, s, true);
             else run_matvec_f64(h, g.vcur, g.w, s, true);
             CK(gmres_cgs2(g, s));
-            CK(gmres_finish_iter(g, tol, s));
+            CK(gmres_finish_iter(g, s));
             CK(gmres_loop_cond(g, c, s));
         });
         if (ex) {
@@ -2300,7 +2314,7 @@ int gmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double 
     for (int i = 0; i < max_iter; ++i) {
         A(g.vcur, g.w);
         CK(gmres_cgs2(g, st));
-        CK(gmres_finish_iter(g, tol, st));
+        CK(gmres_finish_iter(g, st));
         CK(cudaMemcpyAsync(sc, g.scal, 32, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         *resid = sc[1];

@@ -935,8 +935,9 @@ __device__ void gm_apply(double &dx, double &dy, double cs, double sn) {
 }
 
 // Givens rotations on column i (*/codes/gmres.hpp:30-75,156-162); resid = |s(i+1)| / ||b||.
-__global__ void gm_givens(GmresDev g, double tol) {
+__global__ void gm_givens(GmresDev g) {
     const int i = *g.iter;
+    const double tol = g.scal[6];
     double *Hc = g.H + (size_t)i * (g.m + 1);
     if (g.scal[2] != 0.0) return;  // already converged: leave state untouched
     for (int k = 0; k < i; ++k) gm_apply(Hc[k], Hc[k + 1], g.cs[k], g.sn[k]);
@@ -983,9 +984,9 @@ cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st) {
     count_launch(3); return cudaGetLastError();
 }
 
-cudaError_t gmres_finish_iter(const GmresDev &g, double tol, cudaStream_t st) {
+cudaError_t gmres_finish_iter(const GmresDev &g, cudaStream_t st) {
     gm_normalise<<<g.nblk, GM_THREADS, 0, st>>>(g);
-    gm_givens<<<1, 1, 0, st>>>(g, tol);
+    gm_givens<<<1, 1, 0, st>>>(g);
     count_launch(2); return cudaGetLastError();
 }
 

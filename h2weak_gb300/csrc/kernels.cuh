@@ -84,14 +84,15 @@ cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, d
 struct GmresDev {
     double *V, *w, *vcur, *H, *cs, *sn, *s;  // V: N x (m+1); H: (m+1) x m column-major
     double *part;                             // 3 * nblk * (m+1) partial sums
-    double *scal;                             // [0] ||b||, [1] resid, [2] converged flag, [3] beta
+    double *scal;                             // [0] ||b||, [1] resid, [2] converged flag, [3] beta,
+                                              // [6] stopping tolerance (read by the Givens step)
     int32_t *iter;                            // [0] current Arnoldi column i, [1] steps taken
     int64_t N;
     int m, nblk;
 };
 void gmres_prepare();                                             // one-time kernel attributes
 cudaError_t gmres_cgs2(const GmresDev &g, cudaStream_t st);      // orthogonalise w against V[:, 0..i], H column
-cudaError_t gmres_finish_iter(const GmresDev &g, double tol, cudaStream_t st);  // normalise, Givens, residual
+cudaError_t gmres_finish_iter(const GmresDev &g, cudaStream_t st);  // normalise, Givens, residual (tol: scal[6])
 cudaError_t gmres_start(const GmresDev &g, const double *b, const double *Ax, double normb, cudaStream_t st);
 cudaError_t gmres_update(const GmresDev &g, double *x, const double *y, int k, cudaStream_t st);
 // last node of a graph-captured Arnoldi step: sets the while-loop condition
@@ -252,12 +253,13 @@ struct GmresBatch {
     double *y;               // (m+1) x rp back-substituted coefficients
     int32_t *conv;           // rp: -1 running, k >= 0 converged at Arnoldi column k, -2 at the start, -3 padding
     int32_t *iter;           // [0] current Arnoldi column, [1] steps taken
+    double *tolp;            // stopping tolerance (device, so that captured steps do not hold it)
     int64_t N;
     int m, rp, nrhs, nblk;
 };
 cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
 cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st);
-cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st);
+cudaError_t gmb_arnoldi(const GmresBatch &g, cudaStream_t st);
 cudaError_t gmb_loop(const GmresBatch &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
 cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st);
 

@@ -551,7 +551,7 @@ __device__ void gmb_block_dots(const GmresBatch &g, const double *a, const doubl
     }
 }
 
-__global__ void gmb_dots(GmresBatch g) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_dots(GmresBatch g) {
     __shared__ double red[4 * GMB_THREADS];
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
@@ -595,7 +595,7 @@ __global__ void gmb_reduce(GmresBatch g, int all) {
 // With at most four basis vectors the dots are formed in the same sweep from
 // the basis values already in registers (the basis is read once); with more,
 // w is updated four basis vectors at a time and a second sweep forms the dots.
-__global__ void gmb_update(GmresBatch g, int pass) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_update(GmresBatch g, int pass) {
     __shared__ double red[4 * GMB_THREADS];
     const int i = *g.iter, rp = g.rp, kn = i + 1;
     if (blockIdx.x == 0)
@@ -674,7 +674,7 @@ __global__ void gmb_update(GmresBatch g, int pass) {
 }
 
 // H(i+1, i) = ||w||; V[:, i+1] = vcur = w / ||w|| (a zero column stays zero)
-__global__ void gmb_normalise(GmresBatch g) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_normalise(GmresBatch g) {
     const int i = *g.iter, rp = g.rp;
     const int c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
     const double hn = sqrt(g.hsum[c]);
@@ -711,8 +711,9 @@ __device__ __forceinline__ void gmb_apply(double &dx, double &dy, double cs, dou
 
 // Givens rotations of column i for every running system
 // (*/codes/gmres.hpp:30-75,156-162); one thread per column.
-__global__ void gmb_givens(GmresBatch g, double tol) {
+__global__ void gmb_givens(GmresBatch g) {
     const int i = *g.iter, c = threadIdx.x;
+    const double tol = *g.tolp;
     if (c < g.rp && g.conv[c] == -1) {
         double *cs = g.cs + (size_t)c * (g.m + 1), *sn = g.sn + (size_t)c * (g.m + 1), *s = g.s + (size_t)c * (g.m + 1);
         double *Hc = g.H + gmb_h(g, c, 0, i);
@@ -741,7 +742,7 @@ __global__ void gmb_givens(GmresBatch g, double tol) {
 }
 
 // w = b - Ax (Ax == NULL: w = b) and per-block partials of ||w||^2
-__global__ void gmb_resid(GmresBatch g, const double *__restrict__ b, const double *__restrict__ Ax) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_resid(GmresBatch g, const double *__restrict__ b, const double *__restrict__ Ax) {
     __shared__ double red[4 * GMB_THREADS];
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
@@ -751,7 +752,7 @@ __global__ void gmb_resid(GmresBatch g, const double *__restrict__ b, const doub
     gmb_block_dots(g, g.w, g.w, 1, r0, r1, red, g.part);
 }
 // partials of ||v[:, c]||^2
-__global__ void gmb_colnorm_part(GmresBatch g, const double *__restrict__ v) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_colnorm_part(GmresBatch g, const double *__restrict__ v) {
     __shared__ double red[4 * GMB_THREADS];
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
@@ -764,7 +765,7 @@ __global__ void gmb_colnorm_fin(GmresBatch g, double *out, int zero_to_one) {
     if (threadIdx.x < g.rp) out[threadIdx.x] = (zero_to_one && s == 0.0) ? 1.0 : s;
 }
 // beta = ||w|| (hsum); V[:, 0] = vcur = w / beta; s = beta e1; per-column state
-__global__ void gmb_start_fin(GmresBatch g, double tol) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_start_fin(GmresBatch g, double tol) {
     const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
     const double beta = sqrt(g.hsum[c]);
     if (blockIdx.x == 0 && rl == 0) {
@@ -806,7 +807,7 @@ __global__ void gmb_backsolve(GmresBatch g, int last) {
     }
 }
 // x += V y over Arnoldi columns 0..kmax
-__global__ void gmb_xupdate(GmresBatch g, double *__restrict__ x, int kmax) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_xupdate(GmresBatch g, double *__restrict__ x, int kmax) {
     const int rp = g.rp;
     const size_t stride = (size_t)g.N * rp;
     const int64_t tot = g.N * rp;
@@ -840,7 +841,7 @@ cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, do
     count_launch(3);
     return cudaGetLastError();
 }
-cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st) {
+cudaError_t gmb_arnoldi(const GmresBatch &g, cudaStream_t st) {
     gmb_dots<<<g.nblk, GMB_THREADS, 0, st>>>(g);
     gmb_reduce<<<g.m + 1, GMB_RED, 0, st>>>(g, 1);
     gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 0);
@@ -848,7 +849,7 @@ cudaError_t gmb_arnoldi(const GmresBatch &g, double tol, cudaStream_t st) {
     gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 1);
     gmb_reduce<<<1, GMB_RED, 0, st>>>(g, 0);
     gmb_normalise<<<g.nblk, GMB_THREADS, 0, st>>>(g);
-    gmb_givens<<<1, 64, 0, st>>>(g, tol);
+    gmb_givens<<<1, 64, 0, st>>>(g);
     count_launch(8);
     return cudaGetLastError();
 }
