@@ -1,3 +1,4 @@
+#include <type_traits>
 // C ABI of the GB300 H2* / (H2+H)* library: handle, tree, GPU assembly,
 // packed-operator plan, matvec launches and device-resident GMRES.
 #include <algorithm>
@@ -71,6 +72,14 @@ template <class T> struct DBuf {
     }
 };
 
+// Device state of the lockstep GMRES for one Krylov-vector type T
+template <class T> struct GmbStore {
+    DBuf<T> V, w, vcur;
+    DBuf<double> H, cs, sn, s, part, hsum, normb, resid, y, tol;
+    DBuf<int32_t> conv, iter;
+    int m = -1, rp = 0;
+};
+
 inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
 
 constexpr int XW_CAP = 4096;          // gathered source width per target (elements)
@@ -138,9 +147,9 @@ struct h2w_handle {
     DBuf<float> m_wsf, m_xf;
     DBuf<double> d_opdf, m_xdf;  // (hi, lo) FP32 pairs (8 bytes each) of the operator and of an input block
     std::vector<int64_t> ph_t0, ph_t1;   // phase target ranges (per-phase launches)
-    DBuf<double> gb_V, gb_w, gb_vcur, gb_H, gb_cs, gb_sn, gb_s, gb_part, gb_hsum, gb_normb, gb_resid, gb_y, gb_tol;
-    DBuf<int32_t> gb_conv, gb_iter;
-    int gb_m = -1, gb_rp = 0;
+    GmbStore<double> gbd;  // FP64 Krylov vectors (FP64 solves)
+    GmbStore<float> gbf;   // FP32 Krylov vectors (inner solves of the refinement, H2W_OPT_F32_BASIS)
+    bool f32_basis = true;
     // graph-captured Arnoldi loops (a while node whose body is one step)
     struct LoopGraph {
         int kind, prec, m, rp, nrhs;
@@ -1979,50 +1988,79 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
     }
 }
 
+// y = A32 x for an FP32 interleaved block, FP32 result (no conversions)
+void run_matvec_multi_f32io(h2w_handle *h, int rp, const float *xf, float *yf, cudaStream_t st) {
+    const int nph = (int)h->mphases.size();
+    const size_t wsz = (size_t)h->ws_n * (size_t)rp;
+    if (h->ws_n >= (int64_t)INT32_MAX - 2 || h->tree.N >= (int64_t)INT32_MAX - 2)
+        throw ApiError(H2W_ERR_ARG, "workspace too large for the multi-vector kernel's source map");
+    MrPhases ph{h->ph_t0.data(), h->ph_t1.data(), nph};
+    CK(cudaMemsetAsync(h->d_mctr.p, 0, (size_t)std::max(nph, 1) * 4, st));
+    const MrPhases *phased = h->coop ? nullptr : &ph;
+    ensure_f32(h);
+    if (h->m_wsf.n < wsz) h->m_wsf.alloc(wsz);
+    CK(cudaMemsetAsync(h->m_wsf.p, 0, wsz * 4, st));
+    mr_prof(h, H2W_PREC_FP32, rp, st, [&] {
+        if (h->tensor)
+            return launch_mrt_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p,
+                                  h->d_op32.p, h->m_wsf.p, xf, yf, h->d_bar.p, h->d_err.p, st);
+        return launch_mr_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p, h->d_op32.p,
+                             h->m_wsf.p, xf, yf, h->d_bar.p, h->d_err.p, st);
+    });
+    if (!h->fused_scatter_m)
+        CK(cudaMemcpyAsync(yf, h->m_wsf.p + (size_t)h->yperm_off * rp, (size_t)h->tree.N * rp * 4,
+                           cudaMemcpyDeviceToDevice, st));
+}
+
 void ensure_multi_vectors(h2w_handle *h) {
     const size_t n = (size_t)h->tree.N * MR_MAX;
     if (h->m_xi.n < n) h->m_xi.alloc(n);
     if (h->m_yi.n < n) h->m_yi.alloc(n);
 }
 
-GmresBatch gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
+inline GmbStore<double> &gmb_store(h2w_handle *h, double *) { return h->gbd; }
+inline GmbStore<float> &gmb_store(h2w_handle *h, float *) { return h->gbf; }
+
+template <class T>
+GmbT<T> gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
     const int64_t N = h->tree.N;
     const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(3 * 152, (N + 255) / 256));
-    if (h->gb_m != m || h->gb_rp != rp) {
-        h->gb_V.alloc((size_t)N * rp * (size_t)(m + 1));
-        h->gb_w.alloc((size_t)N * rp);
-        h->gb_vcur.alloc((size_t)N * rp);
-        h->gb_H.alloc((size_t)rp * (size_t)(m + 1) * (size_t)m);
-        h->gb_cs.alloc((size_t)rp * (m + 1));
-        h->gb_sn.alloc((size_t)rp * (m + 1));
-        h->gb_s.alloc((size_t)rp * (m + 1));
-        h->gb_part.alloc((size_t)nblk * (m + 1) * rp);
-        h->gb_hsum.alloc((size_t)(m + 1) * rp);
-        h->gb_normb.alloc((size_t)rp);
-        h->gb_resid.alloc((size_t)rp);
-        h->gb_y.alloc((size_t)(m + 1) * rp);
-        h->gb_conv.alloc((size_t)rp);
-        h->gb_tol.alloc(1);
-        h->gb_iter.alloc(2);
-        h->gb_m = m;
-        h->gb_rp = rp;
+    GmbStore<T> &S = gmb_store(h, (T *)nullptr);
+    if (S.m != m || S.rp != rp) {
+        S.V.alloc((size_t)N * rp * (size_t)(m + 1));
+        S.w.alloc((size_t)N * rp);
+        S.vcur.alloc((size_t)N * rp);
+        S.H.alloc((size_t)rp * (size_t)(m + 1) * (size_t)m);
+        S.cs.alloc((size_t)rp * (m + 1));
+        S.sn.alloc((size_t)rp * (m + 1));
+        S.s.alloc((size_t)rp * (m + 1));
+        S.part.alloc((size_t)nblk * (m + 1) * rp);
+        S.hsum.alloc((size_t)(m + 1) * rp);
+        S.normb.alloc((size_t)rp);
+        S.resid.alloc((size_t)rp);
+        S.y.alloc((size_t)(m + 1) * rp);
+        S.conv.alloc((size_t)rp);
+        S.tol.alloc(1);
+        S.iter.alloc(2);
+        S.m = m;
+        S.rp = rp;
     }
-    GmresBatch g;
-    g.V = h->gb_V.p;
-    g.w = h->gb_w.p;
-    g.vcur = h->gb_vcur.p;
-    g.H = h->gb_H.p;
-    g.cs = h->gb_cs.p;
-    g.sn = h->gb_sn.p;
-    g.s = h->gb_s.p;
-    g.part = h->gb_part.p;
-    g.hsum = h->gb_hsum.p;
-    g.normb = h->gb_normb.p;
-    g.resid = h->gb_resid.p;
-    g.y = h->gb_y.p;
-    g.conv = h->gb_conv.p;
-    g.tolp = h->gb_tol.p;
-    g.iter = h->gb_iter.p;
+    GmbT<T> g;
+    g.V = S.V.p;
+    g.w = S.w.p;
+    g.vcur = S.vcur.p;
+    g.H = S.H.p;
+    g.cs = S.cs.p;
+    g.sn = S.sn.p;
+    g.s = S.s.p;
+    g.part = S.part.p;
+    g.hsum = S.hsum.p;
+    g.normb = S.normb.p;
+    g.resid = S.resid.p;
+    g.y = S.y.p;
+    g.conv = S.conv.p;
+    g.tolp = S.tol.p;
+    g.iter = S.iter.p;
     g.N = N;
     g.m = m;
     g.rp = rp;
@@ -2034,16 +2072,25 @@ GmresBatch gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
 // Lockstep GMRES over the nrhs <= rp systems of an interleaved leaf-order
 // block: bi right-hand sides, xi initial guesses (updated in place; x0_zero:
 // skip the initial product). iters / resid per column (nrhs entries).
-int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrhs, int max_iter, double tol, int prec,
-                    bool x0_zero, int *iters, double *resid) {
+template <class T>
+int gmres_batch_run_t(h2w_handle *h, const double *bi, double *xi, int rp, int nrhs, int max_iter, double tol,
+                      int prec, bool x0_zero, int *iters, double *resid) {
     if (max_iter < 1 || max_iter > 400) throw ApiError(H2W_ERR_ARG, "batched GMRES: max_iter must be in 1..400");
-    GmresBatch g = gmb_state(h, max_iter, rp, nrhs);
+    constexpr bool F32 = std::is_same<T, float>::value;
+    GmbT<T> g = gmb_state<T>(h, max_iter, rp, nrhs);
+    // w = A vcur: the FP32 basis feeds the FP32 product directly (no conversions)
+    auto product = [&](cudaStream_t s) {
+        if constexpr (F32) run_matvec_multi_f32io(h, rp, g.vcur, g.w, s);
+        else run_matvec_multi(h, prec, rp, g.vcur, g.w, s);
+    };
+    const int kind = F32 ? 2 : 1;
     cudaStream_t st = h->stream;
     CK(cudaMemcpyAsync(g.tolp, &tol, 8, cudaMemcpyHostToDevice, st));  // read by the Givens step
     CK(gmb_norms(g, bi, g.normb, 1, st));
     if (x0_zero) {
         CK(gmb_start(g, bi, nullptr, tol, st));
     } else {
+        if (F32) throw ApiError(H2W_ERR_ARG, "batched GMRES: the FP32 basis starts from x0 = 0");
         if (h->m_ri.n < (size_t)h->tree.N * rp) h->m_ri.alloc((size_t)h->tree.N * MR_MAX);
         run_matvec_multi(h, prec, rp, xi, h->m_ri.p, st);
         CK(gmb_start(g, bi, h->m_ri.p, tol, st));
@@ -2062,10 +2109,10 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
     if (!done && h->use_graphs && !h->graph_failed && !h->prof) {
         // graph path: the batched Arnoldi steps as one while-loop graph launch
         // before a capture, one product outside it makes its buffers and launch attributes
-        if (!loop_graph_cached(h, 1, prec, max_iter, rp, nrhs)) run_matvec_multi(h, prec, rp, g.vcur, g.w, st);
+        if (!loop_graph_cached(h, kind, prec, max_iter, rp, nrhs)) product(st);
         int64_t kps = 0;
-        cudaGraphExec_t ex = loop_graph(h, 1, prec, max_iter, rp, nrhs, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
-            run_matvec_multi(h, prec, rp, g.vcur, g.w, s);
+        cudaGraphExec_t ex = loop_graph(h, kind, prec, max_iter, rp, nrhs, kps, [&](cudaStream_t s, cudaGraphConditionalHandle c) {
+            product(s);
             CK(gmb_arnoldi(g, s));
             CK(gmb_loop(g, c, s));
         });
@@ -2080,7 +2127,7 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
         }
     }
     for (int i = 0; i < max_iter && !done && !looped; ++i) {
-        run_matvec_multi(h, prec, rp, g.vcur, g.w, st);
+        product(st);
         CK(gmb_arnoldi(g, st));
         last = i;
         done = read_conv();
@@ -2102,6 +2149,15 @@ int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrh
         if (cv == -1) all = false;
     }
     return all ? H2W_OK : H2W_ERR_NOT_CONVERGED;
+}
+
+// FP32-operator solves from x0 = 0 run on the FP32 basis (H2W_OPT_F32_BASIS),
+// everything else on the FP64 basis
+int gmres_batch_run(h2w_handle *h, const double *bi, double *xi, int rp, int nrhs, int max_iter, double tol, int prec,
+                    bool x0_zero, int *iters, double *resid) {
+    if (prec == H2W_PREC_FP32 && x0_zero && h->f32_basis)
+        return gmres_batch_run_t<float>(h, bi, xi, rp, nrhs, max_iter, tol, prec, x0_zero, iters, resid);
+    return gmres_batch_run_t<double>(h, bi, xi, rp, nrhs, max_iter, tol, prec, x0_zero, iters, resid);
 }
 
 // --------------------------------------------------------------- GMRES ---
@@ -2195,7 +2251,8 @@ double fp32_error_single(h2w_handle *h, cudaStream_t st) {
 
 // The same for the multi-vector product: rp calibration columns at once, the
 // accurate product in the refinement's residual precision. Uses m_ri, m_di, m_ti.
-double fp32_error_multi(h2w_handle *h, const GmresBatch &g, int rp, cudaStream_t st) {
+template <class T>
+double fp32_error_multi(h2w_handle *h, const GmbT<T> &g, int rp, cudaStream_t st) {
     if (h->eta_multi >= 0) return h->eta_multi;
     const int64_t N = h->tree.N;
     const size_t len = (size_t)N * rp;
@@ -2990,7 +3047,8 @@ int h2w_assemble(h2w_handle *h, int mode) {
         h->storage = storage_entries(h);
         h->has_op = true;
         h->g_m = -1;
-        h->gb_m = -1;
+        h->gbd.m = -1;
+        h->gbf.m = -1;
         h->m_wsd.reset();
         h->m_wsf.reset();
         return H2W_OK;
@@ -3230,8 +3288,8 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
         if (!h->m_ores.p) h->m_ores.alloc(MR_MAX);
         if (h->m_ti.n < (size_t)N * MR_MAX) h->m_ti.alloc((size_t)N * MR_MAX);
         if (h->m_dn.n < (size_t)2 * MR_MAX) h->m_dn.alloc((size_t)2 * MR_MAX);
-        for_rhs_blocks(h, b, x, nrhs, where, [&](int c0, int nc, int rp, double *bi, double *xi) {
-            GmresBatch g = gmb_state(h, inner_iter, rp, nc);
+        // g: the inner solves' state (FP32 or FP64 basis), here for its reductions
+        auto block = [&](auto g, int c0, int nc, int rp, double *bi, double *xi) {
             const size_t len = (size_t)N * rp;
             CK(gmb_norms(g, bi, h->m_onorm.p, 1, st));
             std::vector<double> nb((size_t)rp), nr((size_t)rp);
@@ -3302,6 +3360,10 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
                 *outer_iters = std::max(*outer_iters, o + 1);
             }
             if (!ok) rc = H2W_ERR_NOT_CONVERGED;
+        };
+        for_rhs_blocks(h, b, x, nrhs, where, [&](int c0, int nc, int rp, double *bi, double *xi) {
+            if (h->f32_basis) block(gmb_state<float>(h, inner_iter, rp, nc), c0, nc, rp, bi, xi);
+            else block(gmb_state<double>(h, inner_iter, rp, nc), c0, nc, rp, bi, xi);
         });
         return rc;
     });
@@ -3326,6 +3388,8 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
             h->row_split = value;
         } else if (option == H2W_OPT_IR_UPDATE) {
             h->ir_update = value != 0;
+        } else if (option == H2W_OPT_F32_BASIS) {
+            h->f32_basis = value != 0;
         } else if (option == H2W_OPT_TENSOR) {
             h->tensor = value != 0;
             h->eta_multi = -1.0;
@@ -3358,6 +3422,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_ROW_SPLIT) *value = h->row_split;
         else if (option == H2W_OPT_IR_UPDATE) *value = h->ir_update ? 1 : 0;
         else if (option == H2W_OPT_TENSOR) *value = h->tensor ? 1 : 0;
+        else if (option == H2W_OPT_F32_BASIS) *value = h->f32_basis ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });

@@ -217,6 +217,10 @@ cudaError_t launch_mr_f64(int rp, const int64_t *roff, const int64_t *blob, cons
 cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st);
+// the same with a float result (interleaved FP32 blocks)
+cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                          const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, float *yout,
+                          unsigned *bar, int32_t *err, cudaStream_t st);
 // Double-FP32 arithmetic on the FP32 pipes (each product and sum carried as
 // an FP32 pair; about 2^-44 relative per term instead of FP64's 2^-53): A and
 // xin are (hi, lo) pairs (launch_mr_split of the FP64 operator and input),
@@ -226,6 +230,9 @@ cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, cons
 cudaError_t launch_mrt_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                            const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin,
                            double *yout, unsigned *bar, int32_t *err, cudaStream_t st);
+cudaError_t launch_mrt_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin,
+                           float *yout, unsigned *bar, int32_t *err, cudaStream_t st);
 cudaError_t launch_mr_df64(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                            const MrPhases *phased, int32_t *ctr, const double *A, double *ws, const double *xin, double *yout,
                            unsigned *bar, int32_t *err, cudaStream_t st);
@@ -242,9 +249,13 @@ cudaError_t launch_mr_widen_f64(const double *a, double *b, int64_t n, cudaStrea
 cudaError_t launch_mr_widen_f32(const float *a, double *b, int64_t n, cudaStream_t st);
 
 // Batched GMRES state (rp interleaved systems, Krylov dimension m).
-struct GmresBatch {
-    double *V;               // (m+1) blocks of N*rp
-    double *w, *vcur;        // N*rp
+// Lockstep GMRES state for RP systems (gmbatch.cu). T: type of the Krylov
+// vectors (double for FP64 solves, float for FP32-operator inner solves);
+// Hessenberg, rotations and reductions are double.
+template <class T>
+struct GmbT {
+    T *V;                    // (m+1) blocks of N*rp
+    T *w, *vcur;             // N*rp
     double *H;               // per column c: (m+1) x m column-major at c*m*(m+1)
     double *cs, *sn, *s;     // per column c: m+1 at c*(m+1)
     double *part;            // nblk x (m+1) x rp block partial sums
@@ -257,10 +268,16 @@ struct GmresBatch {
     int64_t N;
     int m, rp, nrhs, nblk;
 };
-cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
-cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st);
-cudaError_t gmb_arnoldi(const GmresBatch &g, cudaStream_t st);
-cudaError_t gmb_loop(const GmresBatch &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
-cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st);
+using GmresBatch = GmbT<double>;
+template <class T>
+cudaError_t gmb_norms(const GmbT<T> &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
+template <class T>
+cudaError_t gmb_start(const GmbT<T> &g, const double *b, const double *Ax, double tol, cudaStream_t st);
+template <class T>
+cudaError_t gmb_arnoldi(const GmbT<T> &g, cudaStream_t st);
+template <class T>
+cudaError_t gmb_loop(const GmbT<T> &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
+template <class T>
+cudaError_t gmb_finish(const GmbT<T> &g, double *x, int last, int kmax, cudaStream_t st);
 
 }  // namespace h2w

@@ -115,11 +115,11 @@ __device__ __forceinline__ void tc_wait(TcPipe &pp, uint64_t *bars, int s, int32
     }
 }
 
-template <int RP>
+template <int RP, class YT>
 __device__ __forceinline__ void tc_target(char *smem, uint32_t tmem, TcPipe &pp, int64_t t,
                                           const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
                                           const float *__restrict__ A, float *ws, const float *__restrict__ xin,
-                                          double *yout, int32_t *err) {
+                                          YT *yout, int32_t *err) {
     using L = TcLayout<RP>;
     int64_t *rec = reinterpret_cast<int64_t *>(smem);
     int32_t *map = reinterpret_cast<int32_t *>(smem + L::map_off);
@@ -330,7 +330,7 @@ __device__ __forceinline__ void tc_target(char *smem, uint32_t tmem, TcPipe &pp,
             const int64_t d = (dst + rt0 + r) * RP + n4;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                if (flags & T_SCATTER) yout[d + j] = (double)((flags & T_ACCUM) ? ws[d + j] + vv[j] : vv[j]);
+                if (flags & T_SCATTER) yout[d + j] = (YT)((flags & T_ACCUM) ? ws[d + j] + vv[j] : vv[j]);
                 else if (flags & T_ATOMIC) atomicAdd(ws + d + j, vv[j]);
                 else if (flags & T_ACCUM) ws[d + j] += vv[j];
                 else ws[d + j] = vv[j];
@@ -340,15 +340,15 @@ __device__ __forceinline__ void tc_target(char *smem, uint32_t tmem, TcPipe &pp,
     }
 }
 
-template <int RP>
+template <int RP, class YT>
 __device__ __forceinline__ void tc_phase(char *smem, uint32_t tmem, TcPipe &pp, int64_t t0, int64_t t1,
                                          int32_t *ctr, const int64_t *__restrict__ roff,
                                          const int64_t *__restrict__ blob, const float *__restrict__ A, float *ws,
-                                         const float *__restrict__ xin, double *yout, int32_t *err) {
+                                         const float *__restrict__ xin, YT *yout, int32_t *err) {
     __shared__ int64_t s_next;
     int64_t t = t0 + blockIdx.x;
     while (t < t1) {
-        tc_target<RP>(smem, tmem, pp, t, roff, blob, A, ws, xin, yout, err);
+        tc_target<RP, YT>(smem, tmem, pp, t, roff, blob, A, ws, xin, yout, err);
         if (threadIdx.x == 0) s_next = t0 + gridDim.x + atomicAdd(ctr, 1);
         __syncthreads();
         t = s_next;
@@ -384,27 +384,27 @@ __device__ __forceinline__ void tc_teardown(uint32_t tmem) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TcLayout<RP>::tmem_cols));
 }
 
-template <int RP>
+template <int RP, class YT>
 __global__ void __launch_bounds__(TC_NT, 1)
     mrt_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1, int32_t *ctr,
-               const float *__restrict__ A, float *ws, const float *__restrict__ xin, double *yout, int32_t *err) {
+               const float *__restrict__ A, float *ws, const float *__restrict__ xin, YT *yout, int32_t *err) {
     extern __shared__ __align__(1024) char tc_smem[];
     const uint32_t tmem = tc_setup<RP>(tc_smem);
     TcPipe pp{0u, 0u, false};
-    tc_phase<RP>(tc_smem, tmem, pp, t0, t1, ctr, roff, blob, A, ws, xin, yout, err);
+    tc_phase<RP, YT>(tc_smem, tmem, pp, t0, t1, ctr, roff, blob, A, ws, xin, yout, err);
     tc_teardown<RP>(tmem);
 }
 
-template <int RP>
+template <int RP, class YT>
 __global__ void __launch_bounds__(TC_NT, 1)
     mrt_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
                     const int64_t *__restrict__ pstart, int nphase, int32_t *ctr, const float *__restrict__ A,
-                    float *ws, const float *__restrict__ xin, double *yout, unsigned *bar, int32_t *err) {
+                    float *ws, const float *__restrict__ xin, YT *yout, unsigned *bar, int32_t *err) {
     extern __shared__ __align__(1024) char tc_smem[];
     const uint32_t tmem = tc_setup<RP>(tc_smem);
     TcPipe pp{0u, 0u, false};
     for (int p = 0; p < nphase; ++p) {
-        tc_phase<RP>(tc_smem, tmem, pp, pstart[p], pstart[p + 1], ctr + p, roff, blob, A, ws, xin, yout, err);
+        tc_phase<RP, YT>(tc_smem, tmem, pp, pstart[p], pstart[p + 1], ctr + p, roff, blob, A, ws, xin, yout, err);
         if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
     }
     tc_teardown<RP>(tmem);
@@ -421,27 +421,27 @@ int tc_num_sms() {
     return n;
 }
 
-template <int RP>
+template <int RP, class YT>
 cudaError_t mrt_launch(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
-                       const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, double *yout,
+                       const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, YT *yout,
                        unsigned *bar, int32_t *err, cudaStream_t st) {
     using L = TcLayout<RP>;
     static int per_sm_coop = 0, per_sm = 0;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(mrt_coop_kernel<RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::smem);
+        cudaError_t e = cudaFuncSetAttribute(mrt_coop_kernel<RP, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::smem);
         if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(mrt_kernel<RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::smem);
+        e = cudaFuncSetAttribute(mrt_kernel<RP, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::smem);
         if (e != cudaSuccess) return e;
         // all of the unified L1 / shared memory as shared memory: two CTAs per SM
-        cudaFuncSetAttribute(mrt_coop_kernel<RP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cudaFuncSetAttribute(mrt_kernel<RP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(mrt_coop_kernel<RP, YT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(mrt_kernel<RP, YT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         attr = true;
     }
     const int nsm = tc_num_sms();
     if (phased) {
         if (per_sm == 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mrt_kernel<RP>, TC_NT, L::smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mrt_kernel<RP, YT>, TC_NT, L::smem);
             if (per_sm <= 0) per_sm = 1;
         }
         for (int p = 0; p < phased->n; ++p) {
@@ -449,7 +449,7 @@ cudaError_t mrt_launch(const int64_t *roff, const int64_t *blob, const int64_t *
             if (t1 <= t0) continue;
             const int64_t cap = (int64_t)nsm * per_sm;
             const int grid = (int)(t1 - t0 < cap ? t1 - t0 : cap);
-            mrt_kernel<RP><<<grid, TC_NT, L::smem, st>>>(roff, blob, t0, t1, ctr + p, A, ws, xin, yout, err);
+            mrt_kernel<RP, YT><<<grid, TC_NT, L::smem, st>>>(roff, blob, t0, t1, ctr + p, A, ws, xin, yout, err);
             count_launch();
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
@@ -466,7 +466,7 @@ cudaError_t mrt_launch(const int64_t *roff, const int64_t *blob, const int64_t *
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
         cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-        if (cudaFuncGetAttributes(&fa, mrt_coop_kernel<RP>) != cudaSuccess) return cudaErrorInvalidValue;
+        if (cudaFuncGetAttributes(&fa, mrt_coop_kernel<RP, YT>) != cudaSuccess) return cudaErrorInvalidValue;
         const int per_block_smem = L::smem + (int)fa.sharedSizeBytes + 1024;
         const int per_block_regs = ((fa.numRegs + 7) / 8 * 8) * TC_NT;
         int n = per_block_smem > 0 ? smem_sm / per_block_smem : 1;
@@ -477,7 +477,7 @@ cudaError_t mrt_launch(const int64_t *roff, const int64_t *blob, const int64_t *
                     (void *)&ws,   (void *)&xin,  (void *)&yout,   (void *)&bar,    (void *)&err};
     while (true) {
         const int grid = nsm * per_sm_coop;
-        cudaError_t e = cudaLaunchCooperativeKernel((const void *)mrt_coop_kernel<RP>, dim3(grid), dim3(TC_NT), args,
+        cudaError_t e = cudaLaunchCooperativeKernel((const void *)mrt_coop_kernel<RP, YT>, dim3(grid), dim3(TC_NT), args,
                                                     L::smem, st);
         if (e == cudaErrorCooperativeLaunchTooLarge && per_sm_coop > 1) {
             cudaGetLastError();
@@ -491,15 +491,26 @@ cudaError_t mrt_launch(const int64_t *roff, const int64_t *blob, const int64_t *
 
 }  // namespace
 
+template <class YT>
+static cudaError_t mrt_dispatch(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                                const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin,
+                                YT *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
+    switch (rp) {
+    case 16: return mrt_launch<16, YT>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    case 32: return mrt_launch<32, YT>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    case 64: return mrt_launch<64, YT>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
 cudaError_t launch_mrt_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                            const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin,
                            double *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
-    switch (rp) {
-    case 16: return mrt_launch<16>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
-    case 32: return mrt_launch<32>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
-    case 64: return mrt_launch<64>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
-    default: return cudaErrorInvalidValue;
-    }
+    return mrt_dispatch(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+}
+cudaError_t launch_mrt_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin,
+                           float *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
+    return mrt_dispatch(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
 }
 
 }  // namespace h2w

@@ -13,10 +13,7 @@
 //      contiguous values.
 //  * mr_pack / mr_unpack  column-major vectors in the caller's point order
 //      <-> interleaved leaf-order blocks.
-//  * gmb_*  GMRES over RP systems in lockstep (the reference's unrestarted
-//      GMRES, */codes/gmres.hpp:92-200, per column): CGS2 Arnoldi, Givens
-//      rotations, per-column convergence; one column's numbers never mix
-//      with another's.
+//  (The lockstep GMRES over these blocks is in gmbatch.cu.)
 #include <cfloat>
 
 #include "kernels.cuh"
@@ -98,10 +95,10 @@ __device__ __forceinline__ void df_get4(float2 *o, const float2 *p) {
 // xin hold (hi, lo) FP32 pairs in place of doubles (split once, mr_split),
 // workspace values are split when staged, and the tiles are multiplied with
 // double-FP32 arithmetic.
-template <class T, int RP, bool DF = false>
+template <class T, int RP, bool DF = false, class YT = double>
 __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *__restrict__ roff,
                                           const int64_t *__restrict__ blob, const T *__restrict__ A, T *ws,
-                                          const T *__restrict__ xin, double *yout) {
+                                          const T *__restrict__ xin, YT *yout) {
     using Lay = MrLayout<T, RP>;
     using V = typename MrVec<T>::type;
     constexpr int NT = Lay::NT, VN = Lay::VN, NA = Lay::NA, NX = Lay::NX;
@@ -268,7 +265,7 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
                 T v;
                 if constexpr (DF) v = (T)((double)ah[i][j] + (double)al[i][j]);
                 else v = acc[i][j];
-                if (flags & T_SCATTER) yout[d + j] = (double)((flags & T_ACCUM) ? ws[d + j] + v : v);
+                if (flags & T_SCATTER) yout[d + j] = (YT)((flags & T_ACCUM) ? ws[d + j] + v : v);
                 else if (flags & T_ATOMIC) atomicAdd(ws + d + j, v);
                 else if (flags & T_ACCUM) ws[d + j] += v;
                 else ws[d + j] = v;
@@ -281,36 +278,36 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
 // Targets [t0, t1) of one phase: a CTA takes t0 + blockIdx.x first, then
 // claims the next unstarted target from the phase's counter (zero at launch),
 // so CTAs that finish early take over the remaining work.
-template <class T, int RP, bool DF>
+template <class T, int RP, bool DF, class YT>
 __device__ __forceinline__ void mr_phase(char *smem, int64_t t0, int64_t t1, int32_t *ctr,
                                          const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
-                                         const T *__restrict__ A, T *ws, const T *__restrict__ xin, double *yout) {
+                                         const T *__restrict__ A, T *ws, const T *__restrict__ xin, YT *yout) {
     __shared__ int64_t s_next;
     int64_t t = t0 + blockIdx.x;
     while (t < t1) {
-        mr_target<T, RP, DF>(smem, t, roff, blob, A, ws, xin, yout);
+        mr_target<T, RP, DF, YT>(smem, t, roff, blob, A, ws, xin, yout);
         if (threadIdx.x == 0) s_next = t0 + gridDim.x + atomicAdd(ctr, 1);
         __syncthreads();
         t = s_next;
     }
 }
 
-template <class T, int RP, bool DF>
+template <class T, int RP, bool DF, class YT>
 __global__ void __launch_bounds__(4 * RP)
     mr_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t t1,
-              int32_t *ctr, const T *__restrict__ A, T *ws, const T *__restrict__ xin, double *yout) {
+              int32_t *ctr, const T *__restrict__ A, T *ws, const T *__restrict__ xin, YT *yout) {
     extern __shared__ __align__(16) char mr_smem[];
-    mr_phase<T, RP, DF>(mr_smem, t0, t1, ctr, roff, blob, A, ws, xin, yout);
+    mr_phase<T, RP, DF, YT>(mr_smem, t0, t1, ctr, roff, blob, A, ws, xin, yout);
 }
 
-template <class T, int RP, bool DF>
+template <class T, int RP, bool DF, class YT>
 __global__ void __launch_bounds__(4 * RP)
     mr_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
                    const int64_t *__restrict__ pstart, int nphase, int32_t *ctr, const T *__restrict__ A,
-                   T *ws, const T *__restrict__ xin, double *yout, unsigned *bar, int32_t *err) {
+                   T *ws, const T *__restrict__ xin, YT *yout, unsigned *bar, int32_t *err) {
     extern __shared__ __align__(16) char mr_smem[];
     for (int p = 0; p < nphase; ++p) {
-        mr_phase<T, RP, DF>(mr_smem, pstart[p], pstart[p + 1], ctr + p, roff, blob, A, ws, xin, yout);
+        mr_phase<T, RP, DF, YT>(mr_smem, pstart[p], pstart[p + 1], ctr + p, roff, blob, A, ws, xin, yout);
         if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
     }
 }
@@ -326,25 +323,25 @@ static int mr_num_sms() {
     return n;
 }
 
-template <class T, int RP, bool DF>
+template <class T, int RP, bool DF, class YT>
 static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                                const MrPhases *phased, int32_t *ctr, const T *A, T *ws, const T *xin,
-                               double *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
+                               YT *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
     using Lay = MrLayout<T, RP>;
     static int per_sm_coop = 0, per_sm = 0;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(mr_coop_kernel<T, RP, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(mr_coop_kernel<T, RP, DF, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Lay::smem);
         if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(mr_kernel<T, RP, DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::smem);
+        e = cudaFuncSetAttribute(mr_kernel<T, RP, DF, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
     const int nsm = mr_num_sms();
     if (phased) {
         if (per_sm == 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_kernel<T, RP, DF>, Lay::NT, Lay::smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_kernel<T, RP, DF, YT>, Lay::NT, Lay::smem);
             if (per_sm <= 0) per_sm = 1;
         }
         for (int p = 0; p < phased->n; ++p) {
@@ -352,7 +349,7 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
             if (t1 <= t0) continue;
             const int64_t cap = (int64_t)nsm * per_sm;
             const int grid = (int)(t1 - t0 < cap ? t1 - t0 : cap);
-            mr_kernel<T, RP, DF><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, ctr + p, A, ws, xin, yout);
+            mr_kernel<T, RP, DF, YT><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, ctr + p, A, ws, xin, yout);
             count_launch();
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
@@ -360,26 +357,26 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
         return cudaSuccess;
     }
     if (per_sm_coop == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, mr_coop_kernel<T, RP, DF>, Lay::NT, Lay::smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, mr_coop_kernel<T, RP, DF, YT>, Lay::NT, Lay::smem);
         if (per_sm_coop <= 0) return cudaErrorCooperativeLaunchTooLarge;
     }
     const int grid = nsm * per_sm_coop;
     void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&ctr, (void *)&A,
                     (void *)&ws,   (void *)&xin,  (void *)&yout,   (void *)&bar,    (void *)&err};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_coop_kernel<T, RP, DF>, dim3(grid), dim3(Lay::NT), args,
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_coop_kernel<T, RP, DF, YT>, dim3(grid), dim3(Lay::NT), args,
                                                 Lay::smem, st);
     count_launch();
     return e;
 }
 
-template <class T, bool DF = false>
+template <class T, bool DF = false, class YT = double>
 static cudaError_t mr_dispatch(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                                const MrPhases *phased, int32_t *ctr, const T *A, T *ws, const T *xin,
-                               double *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
+                               YT *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
     switch (rp) {
-    case 16: return mr_launch_t<T, 16, DF>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
-    case 32: return mr_launch_t<T, 32, DF>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
-    case 64: return mr_launch_t<T, 64, DF>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    case 16: return mr_launch_t<T, 16, DF, YT>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    case 32: return mr_launch_t<T, 32, DF, YT>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+    case 64: return mr_launch_t<T, 64, DF, YT>(roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -398,6 +395,12 @@ cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, cons
                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, double *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st) {
     return mr_dispatch<float>(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err, st);
+}
+cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
+                          const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, float *yout,
+                          unsigned *bar, int32_t *err, cudaStream_t st) {
+    return mr_dispatch<float, false, float>(rp, roff, blob, pstart, nphase, phased, ctr, A, ws, xin, yout, bar, err,
+                                            st);
 }
 
 // b[i] = (hi, lo) FP32 pair of a[i] (df_split), for the double-FP32 product
@@ -484,387 +487,6 @@ cudaError_t launch_mr_widen_f64(const double *a, double *b, int64_t n, cudaStrea
 cudaError_t launch_mr_widen_f32(const float *a, double *b, int64_t n, cudaStream_t st) {
     mr_widen_kernel<float><<<1216, 256, 0, st>>>(a, b, n);
     count_launch();
-    return cudaGetLastError();
-}
-
-// ------------------------------------------------------- batched GMRES ---
-constexpr int GMB_THREADS = 256;
-
-__device__ __forceinline__ void gmb_rows(const GmresBatch &g, int64_t &r0, int64_t &r1) {
-    const int64_t chunk = (g.N + g.nblk - 1) / g.nblk;
-    r0 = (int64_t)blockIdx.x * chunk;
-    r1 = r0 + chunk < g.N ? r0 + chunk : g.N;
-}
-__device__ __forceinline__ size_t gmb_h(const GmresBatch &g, int c, int row, int col) {
-    return ((size_t)c * g.m + col) * (g.m + 1) + row;
-}
-
-// out[(blk*(m+1) + k)*rp + c] = sum over the block's rows of a_k[t, c] * b[t, c],
-// k = 0..kn-1, a_k = a + k*N*rp (kn = 1: a itself)
-// Four a_k per sweep over the rows (b read once per four), four rows per
-// iteration so that 20 loads per thread are in flight; red: 4*GMB_THREADS.
-__device__ __forceinline__ void gmb_block_sum(const GmresBatch &g, const double *acc, int nout, double *red,
-                                              double *out) {
-    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) red[(j * RL + rl) * rp + c] = acc[j];
-    __syncthreads();
-    if (rl == 0)
-        for (int j = 0; j < nout; ++j) {
-            double s2 = 0.0;
-            for (int q = 0; q < RL; ++q) s2 += red[(j * RL + q) * rp + c];
-            out[((size_t)blockIdx.x * (g.m + 1) + j) * rp + c] = s2;
-        }
-    __syncthreads();
-}
-__device__ void gmb_block_dots(const GmresBatch &g, const double *a, const double *b, int kn, int64_t r0,
-                               int64_t r1, double *red, double *out) {
-    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
-    const size_t stride = (size_t)g.N * rp;
-    const int64_t step = (int64_t)RL * rp;
-    for (int k0 = 0; k0 < kn; k0 += 4) {
-        const int kc = kn - k0 < 4 ? kn - k0 : 4;
-        const double *ak = a + (size_t)k0 * stride;
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
-        int64_t t = r0 + rl;
-        for (; t + 3 * RL < r1; t += 4 * RL) {
-            const int64_t o = t * rp + c;
-            double bv[4], av[4][4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) bv[u] = b[o + u * step];
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) av[u][j] = j < kc ? ak[j * stride + o + u * step] : 0.0;
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[j] += av[u][j] * bv[u];
-        }
-        for (; t < r1; t += RL) {
-            const double bv = b[t * rp + c];
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (j < kc) acc[j] += ak[j * stride + t * rp + c] * bv;
-        }
-        gmb_block_sum(g, acc, kc, red, out + (size_t)k0 * rp);
-    }
-}
-
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_dots(GmresBatch g) {
-    __shared__ double red[4 * GMB_THREADS];
-    int64_t r0, r1;
-    gmb_rows(g, r0, r1);
-    gmb_block_dots(g, g.V, g.w, *g.iter + 1, r0, r1, red, g.part);
-}
-
-// hsum[k*rp + c] = sum_b part[(b*(m+1) + k)*rp + c] for k <= i (all = 1) or k = 0 (all = 0);
-// block k of GMB_RED threads: 1024 / rp lanes per column split the blocks'
-// partials (four loads in flight each), then meet in shared memory
-constexpr int GMB_RED = 1024;
-__device__ __forceinline__ double gmb_sum_parts(const GmresBatch &g, int k, double *red) {
-    const int rp = g.rp, c = threadIdx.x % rp, bl = threadIdx.x / rp, BL = GMB_RED / rp;
-    const size_t st = (size_t)(g.m + 1) * rp;
-    const double *p = g.part + (size_t)k * rp + c;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    int b = bl;
-    for (; b + 3 * BL < g.nblk; b += 4 * BL) {
-        s0 += p[(size_t)b * st];
-        s1 += p[(size_t)(b + BL) * st];
-        s2 += p[(size_t)(b + 2 * BL) * st];
-        s3 += p[(size_t)(b + 3 * BL) * st];
-    }
-    for (; b < g.nblk; b += BL) s0 += p[(size_t)b * st];
-    red[threadIdx.x] = (s0 + s1) + (s2 + s3);
-    __syncthreads();
-    double s = 0.0;
-    if (bl == 0)
-        for (int q = 0; q < BL; ++q) s += red[q * rp + c];
-    return s;  // valid in the threads with bl == 0
-}
-__global__ void gmb_reduce(GmresBatch g, int all) {
-    __shared__ double red[GMB_RED];
-    const int kn = all ? *g.iter + 1 : 1;
-    const int k = blockIdx.x;
-    if (k >= kn) return;
-    const double s = gmb_sum_parts(g, k, red);
-    if (threadIdx.x < g.rp) g.hsum[(size_t)k * g.rp + threadIdx.x] = s;
-}
-
-// h = hsum; H(:, i) (=|+=) h; w -= V h; then new dots (pass 0) or ||w||^2 partials (pass 1).
-// With at most four basis vectors the dots are formed in the same sweep from
-// the basis values already in registers (the basis is read once); with more,
-// w is updated four basis vectors at a time and a second sweep forms the dots.
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_update(GmresBatch g, int pass) {
-    __shared__ double red[4 * GMB_THREADS];
-    const int i = *g.iter, rp = g.rp, kn = i + 1;
-    if (blockIdx.x == 0)
-        for (int e = threadIdx.x; e < kn * rp; e += blockDim.x) {
-            const int k = e / rp, c = e % rp;
-            double *Hk = g.H + gmb_h(g, c, k, i);
-            *Hk = pass == 0 ? g.hsum[e] : *Hk + g.hsum[e];
-        }
-    int64_t r0, r1;
-    gmb_rows(g, r0, r1);
-    const int c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
-    const size_t stride = (size_t)g.N * rp;
-    const int64_t step = (int64_t)RL * rp;
-    double *w = g.w;
-    for (int k0 = 0; k0 < kn; k0 += 4) {
-        const int kc = kn - k0 < 4 ? kn - k0 : 4;
-        const bool fused = kn <= 4;
-        const double *Vk = g.V + (size_t)k0 * stride;
-        double hk[4], acc[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) hk[j] = j < kc ? g.hsum[(size_t)(k0 + j) * rp + c] : 0.0;
-        int64_t t = r0 + rl;
-        for (; t + 3 * RL < r1; t += 4 * RL) {
-            const int64_t o = t * rp + c;
-            double wv[4], vk[4][4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) wv[u] = w[o + u * step];
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) vk[u][j] = j < kc ? Vk[j * stride + o + u * step] : 0.0;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                double v = wv[u];
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (j < kc) v -= vk[u][j] * hk[j];
-                w[o + u * step] = v;
-                if (fused) {
-                    if (pass == 0) {
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) acc[j] += vk[u][j] * v;
-                    } else {
-                        acc[0] += v * v;
-                    }
-                }
-            }
-        }
-        for (; t < r1; t += RL) {
-            const int64_t o = t * rp + c;
-            double vk[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) vk[j] = j < kc ? Vk[j * stride + o] : 0.0;
-            double v = w[o];
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (j < kc) v -= vk[j] * hk[j];
-            w[o] = v;
-            if (fused) {
-                if (pass == 0) {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[j] += vk[j] * v;
-                } else {
-                    acc[0] += v * v;
-                }
-            }
-        }
-        if (fused) {
-            gmb_block_sum(g, acc, pass == 0 ? kn : 1, red, g.part);
-            return;
-        }
-    }
-    __syncthreads();
-    if (pass == 0) gmb_block_dots(g, g.V, g.w, kn, r0, r1, red, g.part);
-    else gmb_block_dots(g, g.w, g.w, 1, r0, r1, red, g.part);
-}
-
-// H(i+1, i) = ||w||; V[:, i+1] = vcur = w / ||w|| (a zero column stays zero)
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_normalise(GmresBatch g) {
-    const int i = *g.iter, rp = g.rp;
-    const int c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
-    const double hn = sqrt(g.hsum[c]);
-    if (blockIdx.x == 0 && rl == 0) g.H[gmb_h(g, c, i + 1, i)] = hn;
-    const double ih = hn > 0.0 ? 1.0 / hn : 0.0;
-    int64_t r0, r1;
-    gmb_rows(g, r0, r1);
-    double *Vn = g.V + (size_t)(i + 1) * g.N * rp;
-    const int64_t step = (int64_t)RL * rp;
-    int64_t t = r0 + rl;
-    for (; t + 3 * RL < r1; t += 4 * RL) {
-        const int64_t o = t * rp + c;
-        double v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = ih * g.w[o + u * step];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            Vn[o + u * step] = v[u];
-            g.vcur[o + u * step] = v[u];
-        }
-    }
-    for (; t < r1; t += RL) {
-        const double v = ih * g.w[t * rp + c];
-        Vn[t * rp + c] = v;
-        g.vcur[t * rp + c] = v;
-    }
-}
-
-__device__ __forceinline__ void gmb_apply(double &dx, double &dy, double cs, double sn) {
-    const double temp = __dadd_rn(__dmul_rn(cs, dx), __dmul_rn(sn, dy));
-    dy = __dadd_rn(__dmul_rn(-sn, dx), __dmul_rn(cs, dy));
-    dx = temp;
-}
-
-// Givens rotations of column i for every running system
-// (*/codes/gmres.hpp:30-75,156-162); one thread per column.
-__global__ void gmb_givens(GmresBatch g) {
-    const int i = *g.iter, c = threadIdx.x;
-    const double tol = *g.tolp;
-    if (c < g.rp && g.conv[c] == -1) {
-        double *cs = g.cs + (size_t)c * (g.m + 1), *sn = g.sn + (size_t)c * (g.m + 1), *s = g.s + (size_t)c * (g.m + 1);
-        double *Hc = g.H + gmb_h(g, c, 0, i);
-        for (int k = 0; k < i; ++k) gmb_apply(Hc[k], Hc[k + 1], cs[k], sn[k]);
-        double dx = Hc[i], dy = Hc[i + 1], c_, s_;
-        if (dy == 0.0) { c_ = 1.0; s_ = 0.0; }
-        else if (fabs(dy) > fabs(dx)) {
-            const double temp = dx / dy;
-            s_ = 1.0 / sqrt(1.0 + temp * temp);
-            c_ = temp * s_;
-        } else {
-            const double temp = dy / dx;
-            c_ = 1.0 / sqrt(1.0 + temp * temp);
-            s_ = temp * c_;
-        }
-        cs[i] = c_;
-        sn[i] = s_;
-        gmb_apply(Hc[i], Hc[i + 1], c_, s_);
-        gmb_apply(s[i], s[i + 1], c_, s_);
-        const double resid = fabs(s[i + 1]) / g.normb[c];
-        g.resid[c] = resid;
-        if (resid < tol) g.conv[c] = i;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && i + 1 < g.m) *g.iter = i + 1;
-}
-
-// w = b - Ax (Ax == NULL: w = b) and per-block partials of ||w||^2
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_resid(GmresBatch g, const double *__restrict__ b, const double *__restrict__ Ax) {
-    __shared__ double red[4 * GMB_THREADS];
-    int64_t r0, r1;
-    gmb_rows(g, r0, r1);
-    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
-    for (int64_t t = r0 + rl; t < r1; t += RL) g.w[t * rp + c] = Ax ? b[t * rp + c] - Ax[t * rp + c] : b[t * rp + c];
-    __syncthreads();
-    gmb_block_dots(g, g.w, g.w, 1, r0, r1, red, g.part);
-}
-// partials of ||v[:, c]||^2
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_colnorm_part(GmresBatch g, const double *__restrict__ v) {
-    __shared__ double red[4 * GMB_THREADS];
-    int64_t r0, r1;
-    gmb_rows(g, r0, r1);
-    gmb_block_dots(g, v, v, 1, r0, r1, red, g.part);
-}
-// out[c] = sqrt(sum of the partials); zero_to_one: a zero norm becomes 1
-__global__ void gmb_colnorm_fin(GmresBatch g, double *out, int zero_to_one) {
-    __shared__ double red[GMB_RED];
-    const double s = sqrt(gmb_sum_parts(g, 0, red));
-    if (threadIdx.x < g.rp) out[threadIdx.x] = (zero_to_one && s == 0.0) ? 1.0 : s;
-}
-// beta = ||w|| (hsum); V[:, 0] = vcur = w / beta; s = beta e1; per-column state
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_start_fin(GmresBatch g, double tol) {
-    const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
-    const double beta = sqrt(g.hsum[c]);
-    if (blockIdx.x == 0 && rl == 0) {
-        double *cs = g.cs + (size_t)c * (g.m + 1), *sn = g.sn + (size_t)c * (g.m + 1), *s = g.s + (size_t)c * (g.m + 1);
-        for (int k = 0; k <= g.m; ++k) { s[k] = 0.0; cs[k] = 0.0; sn[k] = 0.0; }
-        s[0] = beta;
-        const double r = beta / g.normb[c];
-        g.resid[c] = r;
-        g.conv[c] = c >= g.nrhs ? -3 : (r <= tol ? -2 : -1);
-        if (c == 0) {
-            g.iter[0] = 0;
-            g.iter[1] = 0;  // Arnoldi steps taken (graph loop counter)
-        }
-    }
-    const double ib = beta > 0.0 ? 1.0 / beta : 0.0;
-    int64_t r0, r1;
-    gmb_rows(g, r0, r1);
-    for (int64_t t = r0 + rl; t < r1; t += RL) {
-        const double v = g.w[t * rp + c] * ib;
-        g.V[t * rp + c] = v;
-        g.vcur[t * rp + c] = v;
-    }
-}
-// y_c = H_c(0:k, 0:k) \ s_c(0:k), k = the column's last Arnoldi index
-// (converged: conv; still running: last; converged at the start / padding: none),
-// in the reference's back-substitution order (*/codes/gmres.hpp:77-90)
-__global__ void gmb_backsolve(GmresBatch g, int last) {
-    const int c = threadIdx.x;
-    if (c >= g.rp) return;
-    const int cv = g.conv[c];
-    const int k = cv >= 0 ? cv : (cv == -1 ? last : -1);
-    const double *s = g.s + (size_t)c * (g.m + 1);
-    for (int j = 0; j <= g.m; ++j) g.y[(size_t)j * g.rp + c] = j <= k ? s[j] : 0.0;
-    for (int i = k; i >= 0; --i) {
-        double *y = g.y;
-        const double yi = y[(size_t)i * g.rp + c] / g.H[gmb_h(g, c, i, i)];
-        y[(size_t)i * g.rp + c] = yi;
-        for (int j = i - 1; j >= 0; --j) y[(size_t)j * g.rp + c] -= g.H[gmb_h(g, c, j, i)] * yi;
-    }
-}
-// x += V y over Arnoldi columns 0..kmax
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_xupdate(GmresBatch g, double *__restrict__ x, int kmax) {
-    const int rp = g.rp;
-    const size_t stride = (size_t)g.N * rp;
-    const int64_t tot = g.N * rp;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(e % rp);
-        double v = x[e];
-        for (int j = 0; j <= kmax; ++j) v += g.V[j * stride + e] * g.y[(size_t)j * rp + c];
-        x[e] = v;
-    }
-}
-
-// Loop condition of the graph-captured batched Arnoldi step: run another
-// step while a column is still running and fewer than m steps were taken.
-__global__ void gmb_loop_cond(GmresBatch g, cudaGraphConditionalHandle hnd) {
-    const int c = ++g.iter[1];
-    int running = 0;
-    for (int q = 0; q < g.nrhs; ++q) running |= g.conv[q] == -1;
-    cudaGraphSetConditional(hnd, (running && c < g.m) ? 1u : 0u);
-}
-
-cudaError_t gmb_norms(const GmresBatch &g, const double *v, double *out, int zero_to_one, cudaStream_t st) {
-    gmb_colnorm_part<<<g.nblk, GMB_THREADS, 0, st>>>(g, v);
-    gmb_colnorm_fin<<<1, GMB_RED, 0, st>>>(g, out, zero_to_one);
-    count_launch(2);
-    return cudaGetLastError();
-}
-cudaError_t gmb_start(const GmresBatch &g, const double *b, const double *Ax, double tol, cudaStream_t st) {
-    gmb_resid<<<g.nblk, GMB_THREADS, 0, st>>>(g, b, Ax);
-    gmb_reduce<<<1, GMB_RED, 0, st>>>(g, 0);
-    gmb_start_fin<<<g.nblk, GMB_THREADS, 0, st>>>(g, tol);
-    count_launch(3);
-    return cudaGetLastError();
-}
-cudaError_t gmb_arnoldi(const GmresBatch &g, cudaStream_t st) {
-    gmb_dots<<<g.nblk, GMB_THREADS, 0, st>>>(g);
-    gmb_reduce<<<g.m + 1, GMB_RED, 0, st>>>(g, 1);
-    gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 0);
-    gmb_reduce<<<g.m + 1, GMB_RED, 0, st>>>(g, 1);
-    gmb_update<<<g.nblk, GMB_THREADS, 0, st>>>(g, 1);
-    gmb_reduce<<<1, GMB_RED, 0, st>>>(g, 0);
-    gmb_normalise<<<g.nblk, GMB_THREADS, 0, st>>>(g);
-    gmb_givens<<<1, 64, 0, st>>>(g);
-    count_launch(8);
-    return cudaGetLastError();
-}
-cudaError_t gmb_loop(const GmresBatch &g, cudaGraphConditionalHandle hnd, cudaStream_t st) {
-    gmb_loop_cond<<<1, 1, 0, st>>>(g, hnd);
-    count_launch();
-    return cudaGetLastError();
-}
-cudaError_t gmb_finish(const GmresBatch &g, double *x, int last, int kmax, cudaStream_t st) {
-    gmb_backsolve<<<1, 64, 0, st>>>(g, last);
-    count_launch();
-    if (kmax >= 0) {
-        gmb_xupdate<<<g.nblk, GMB_THREADS, 0, st>>>(g, x, kmax);
-        count_launch();
-    }
     return cudaGetLastError();
 }
 

@@ -208,9 +208,13 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 accuracy; 0 (default): the FP32 FMA kernel, which is
  *                 faster on the operators measured (one tensor-memory CTA
  *                 per SM; targets of 20-64 rows fill half of an M = 128
- *                 MMA at best). */
+ *                 MMA at best).
+ *  H2W_OPT_F32_BASIS  1 (default): the inner solves of h2w_gmres_ir_batch
+ *                 (FP32 operator, x0 = 0) keep their Krylov vectors and do
+ *                 their orthogonalisation in FP32 (Hessenberg, rotations and
+ *                 block sums in FP64); 0: FP64 Krylov vectors. */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
-       H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6 };
+       H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
