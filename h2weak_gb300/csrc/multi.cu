@@ -15,6 +15,7 @@
 //      <-> interleaved leaf-order blocks.
 //  (The lockstep GMRES over these blocks is in gmbatch.cu.)
 #include <cfloat>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "sync.cuh"
@@ -23,6 +24,19 @@ namespace h2w {
 
 constexpr int MR_MT = 64;  // result rows per tile
 constexpr int MR_KC = 32;  // operator columns per staged chunk
+constexpr int MR_NSA = 3;  // staging buffers of the FP32 kernel (two chunks in flight)
+
+// 16-byte asynchronous global -> shared copy; bytes < 16 zero-fills the rest
+// (bytes = 0: no global read, src may be any valid address)
+__device__ __forceinline__ void mr_cp16(void *dst, const void *src, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mr_cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void mr_cp_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 template <class T> struct MrVec;
 template <> struct MrVec<double> { using type = double2; static constexpr int n = 2; };
@@ -38,6 +52,8 @@ template <class T, int RP> struct MrLayout {
     static constexpr size_t xs_bytes = sizeof(T) * MR_KC * RP;
     static constexpr size_t map_bytes = (size_t)4 * MR_XS_ELEMS;
     static constexpr size_t smem = rec_bytes + 2 * (as_bytes + xs_bytes) + map_bytes;  // two staging buffers
+    // FP32 kernel: MR_NSA staging buffers filled by asynchronous copies
+    static constexpr size_t smem_async = rec_bytes + MR_NSA * (as_bytes + xs_bytes) + map_bytes;
     static_assert(NA >= 1 && NA * VN * NT == MR_KC * MR_MT, "A chunk split");
     static_assert(NX >= 1 && NX * VN * NT == MR_KC * RP, "X chunk split");
 };
@@ -275,6 +291,165 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
     __syncthreads();
 }
 
+// FP32 form of mr_target with the chunks staged by asynchronous copies
+// (cp.async, zero-filled past a target's rows or a panel's columns) into
+// MR_NSA buffers: the copies of chunks i+1 and i+2 are in flight while chunk
+// i is multiplied, with no staging registers; one barrier per chunk.
+template <int RP, class YT>
+__device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int64_t *__restrict__ roff,
+                                                const int64_t *__restrict__ blob, const float *__restrict__ A,
+                                                float *ws, const float *__restrict__ xin, YT *yout) {
+    using Lay = MrLayout<float, RP>;
+    constexpr int NT = Lay::NT, NA = Lay::NA, NX = Lay::NX;
+    int64_t *rec = reinterpret_cast<int64_t *>(smem);
+    float *As = reinterpret_cast<float *>(smem + Lay::rec_bytes);
+    float *Xs = reinterpret_cast<float *>(smem + Lay::rec_bytes + MR_NSA * Lay::as_bytes);
+    int32_t *map = reinterpret_cast<int32_t *>(smem + Lay::rec_bytes + MR_NSA * (Lay::as_bytes + Lay::xs_bytes));
+    const int tid = threadIdx.x;
+    const int ty = tid / (RP / 4), tx = tid % (RP / 4);
+
+    const int64_t o = roff[t];
+    const int nw = (int)(roff[t + 1] - o);
+    for (int q = tid; q < nw; q += NT) rec[q] = blob[o + q];
+    __syncthreads();
+    const int64_t dst = rec[0];
+    const int nrows = (int)(rec[1] & 0xffffffff), flags = (int)(rec[1] >> 32);
+    const int np = (int)(rec[2] & 0xffffffff), ns = (int)(rec[2] >> 32);
+    const int64_t *pan = rec + 3;
+    const int64_t *seg = pan + 3 * np;
+    int xend = 0;
+    for (int q = 0; q < np; ++q) {
+        const int e = (int)pan[3 * q + 2] + (int)(pan[3 * q + 1] >> 32);
+        xend = e > xend ? e : xend;
+    }
+    for (int e = tid; e < xend; e += NT) map[e] = -1;
+    __syncthreads();
+    for (int s = 0; s < ns; ++s) {
+        const int64_t src = seg[2 * s], w1 = seg[2 * s + 1];
+        const int len = (int)(w1 & 0xffffffff), code = (int)(w1 >> 32);
+        const int xo = code >> 1;
+        const bool g = code & 1;
+        for (int i = tid; i < len; i += NT) map[xo + i] = g ? -(2 + (int)(src + i)) : (int)(src + i);
+    }
+    __syncthreads();
+
+    auto advance = [&](int &q, int &c0) {
+        if (q >= np) return;
+        c0 += MR_KC;
+        if (c0 >= (int)(pan[3 * q + 1] >> 32)) {
+            ++q;
+            c0 = 0;
+        }
+    };
+    // copies of chunk (panel q, columns c0 .. c0+KC) of rows rt0 .. into buffer sb
+    // (q >= np: none), committed as one group
+    auto issue = [&](int q, int c0, int rt0, int sb) {
+        if (q < np) {
+            const int64_t pa = pan[3 * q];
+            const int lda = (int)(pan[3 * q + 1] & 0xffffffff), w = (int)(pan[3 * q + 1] >> 32);
+            const int xoff = (int)pan[3 * q + 2];
+            const bool vec = ((pa & 3) == 0) && ((lda & 3) == 0);  // the plan's 16-byte-row rule (4 elements)
+#pragma unroll
+            for (int u = 0; u < NA; ++u) {
+                const int v = tid + NT * u;
+                const int col = v / (MR_MT / 4), r = rt0 + (v % (MR_MT / 4)) * 4;
+                const int c = c0 + col;
+                float *d = As + sb * (MR_KC * MR_MT) + col * MR_MT + (v % (MR_MT / 4)) * 4;
+                if (c < w && r < nrows) {
+                    const float *p = A + pa + (int64_t)c * lda + r;
+                    const int nv = nrows - r < 4 ? nrows - r : 4;
+                    if (vec) {
+                        mr_cp16(d, p, 4 * nv);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) d[j] = j < nv ? p[j] : 0.f;
+                    }
+                } else {
+                    mr_cp16(d, A, 0);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < NX; ++u) {
+                const int v = tid + NT * u;
+                const int row = v / (RP / 4), cv = (v % (RP / 4)) * 4;
+                const float *src = xin;
+                int bytes = 0;
+                if (c0 + row < w) {
+                    const int m = map[xoff + c0 + row];
+                    if (m >= 0) {
+                        src = ws + (int64_t)m * RP + cv;
+                        bytes = 16;
+                    } else if (m <= -2) {
+                        src = xin + (int64_t)(-2 - m) * RP + cv;
+                        bytes = 16;
+                    }
+                }
+                mr_cp16(Xs + sb * (MR_KC * RP) + row * RP + cv, src, bytes);
+            }
+        }
+        mr_cp_commit();
+    };
+
+    for (int rt0 = 0; rt0 < nrows; rt0 += MR_MT) {
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+        int q0 = 0, c00 = 0;  // the chunk multiplied next, then the two in flight behind it
+        int q1 = 0, c01 = 0;
+        advance(q1, c01);
+        int q2 = q1, c02 = c01;
+        advance(q2, c02);
+        issue(q0, c00, rt0, 0);
+        issue(q1, c01, rt0, 1);
+        const bool active = rt0 + ty * 4 < nrows;
+        int sb = 0;
+        while (q0 < np) {
+            mr_cp_wait<1>();   // this thread's copies of chunk q0 have landed
+            __syncthreads();   // everyone's have; the buffer of the previous chunk is free
+            issue(q2, c02, rt0, sb == 0 ? MR_NSA - 1 : sb - 1);
+            if (active) {
+                const float *Ab = As + sb * (MR_KC * MR_MT);
+                const float *Xb = Xs + sb * (MR_KC * RP);
+#pragma unroll 8
+                for (int k = 0; k < MR_KC; ++k) {
+                    float a4[4], x4[4];
+                    mr_get4(a4, Ab + k * MR_MT + ty * 4);
+                    mr_get4(x4, Xb + k * RP + tx * 4);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] += a4[i] * x4[j];
+                }
+            }
+            q0 = q1;
+            c00 = c01;
+            q1 = q2;
+            c01 = c02;
+            advance(q2, c02);
+            sb = sb + 1 == MR_NSA ? 0 : sb + 1;
+        }
+        mr_cp_wait<0>();
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = rt0 + ty * 4 + i;
+            if (r >= nrows) continue;
+            const int64_t d = (dst + r) * RP + tx * 4;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float v = acc[i][j];
+                if (flags & T_SCATTER) yout[d + j] = (YT)((flags & T_ACCUM) ? ws[d + j] + v : v);
+                else if (flags & T_ATOMIC) atomicAdd(ws + d + j, v);
+                else if (flags & T_ACCUM) ws[d + j] += v;
+                else ws[d + j] = v;
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+}
+
 // Targets [t0, t1) of one phase: a CTA takes t0 + blockIdx.x first, then
 // claims the next unstarted target from the phase's counter (zero at launch),
 // so CTAs that finish early take over the remaining work.
@@ -285,7 +460,10 @@ __device__ __forceinline__ void mr_phase(char *smem, int64_t t0, int64_t t1, int
     __shared__ int64_t s_next;
     int64_t t = t0 + blockIdx.x;
     while (t < t1) {
-        mr_target<T, RP, DF, YT>(smem, t, roff, blob, A, ws, xin, yout);
+        if constexpr (std::is_same<T, float>::value && !DF)
+            mr_target_async<RP, YT>(smem, t, roff, blob, A, ws, xin, yout);
+        else
+            mr_target<T, RP, DF, YT>(smem, t, roff, blob, A, ws, xin, yout);
         if (threadIdx.x == 0) s_next = t0 + gridDim.x + atomicAdd(ctr, 1);
         __syncthreads();
         t = s_next;
@@ -328,20 +506,21 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
                                const MrPhases *phased, int32_t *ctr, const T *A, T *ws, const T *xin,
                                YT *yout, unsigned *bar, int32_t *err, cudaStream_t st) {
     using Lay = MrLayout<T, RP>;
+    constexpr size_t SMEM = (std::is_same<T, float>::value && !DF) ? Lay::smem_async : Lay::smem;
     static int per_sm_coop = 0, per_sm = 0;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(mr_coop_kernel<T, RP, DF, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Lay::smem);
+                                             (int)SMEM);
         if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(mr_kernel<T, RP, DF, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::smem);
+        e = cudaFuncSetAttribute(mr_kernel<T, RP, DF, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
         if (e != cudaSuccess) return e;
         attr = true;
     }
     const int nsm = mr_num_sms();
     if (phased) {
         if (per_sm == 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_kernel<T, RP, DF, YT>, Lay::NT, Lay::smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_kernel<T, RP, DF, YT>, Lay::NT, SMEM);
             if (per_sm <= 0) per_sm = 1;
         }
         for (int p = 0; p < phased->n; ++p) {
@@ -349,7 +528,7 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
             if (t1 <= t0) continue;
             const int64_t cap = (int64_t)nsm * per_sm;
             const int grid = (int)(t1 - t0 < cap ? t1 - t0 : cap);
-            mr_kernel<T, RP, DF, YT><<<grid, Lay::NT, Lay::smem, st>>>(roff, blob, t0, t1, ctr + p, A, ws, xin, yout);
+            mr_kernel<T, RP, DF, YT><<<grid, Lay::NT, SMEM, st>>>(roff, blob, t0, t1, ctr + p, A, ws, xin, yout);
             count_launch();
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
@@ -357,14 +536,14 @@ static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const i
         return cudaSuccess;
     }
     if (per_sm_coop == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, mr_coop_kernel<T, RP, DF, YT>, Lay::NT, Lay::smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_coop, mr_coop_kernel<T, RP, DF, YT>, Lay::NT, SMEM);
         if (per_sm_coop <= 0) return cudaErrorCooperativeLaunchTooLarge;
     }
     const int grid = nsm * per_sm_coop;
     void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&ctr, (void *)&A,
                     (void *)&ws,   (void *)&xin,  (void *)&yout,   (void *)&bar,    (void *)&err};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_coop_kernel<T, RP, DF, YT>, dim3(grid), dim3(Lay::NT), args,
-                                                Lay::smem, st);
+                                                SMEM, st);
     count_launch();
     return e;
 }
