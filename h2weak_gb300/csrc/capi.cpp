@@ -2024,7 +2024,7 @@ inline GmbStore<float> &gmb_store(h2w_handle *h, float *) { return h->gbf; }
 template <class T>
 GmbT<T> gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
     const int64_t N = h->tree.N;
-    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(3 * 152, (N + 255) / 256));
+    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(3 * 152, (N + 127) / 128));
     GmbStore<T> &S = gmb_store(h, (T *)nullptr);
     if (S.m != m || S.rp != rp) {
         S.V.alloc((size_t)N * rp * (size_t)(m + 1));

@@ -12,6 +12,7 @@
 // double, and over blocks in a fixed order (deterministic). The number of
 // basis vectors a sweep handles (1-4) is a template parameter, so no
 // multiply-add is issued for an empty slot.
+#include <algorithm>
 #include <type_traits>
 
 #include "kernels.cuh"
@@ -330,7 +331,24 @@ __global__ void __launch_bounds__(GMB_THREADS, 3)
     gmb_rows(g, r0, r1);
     const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
     T acc[4] = {T(0), T(0), T(0), T(0)};
-    for (int64_t t = r0 + rl; t < r1; t += RL) {
+    const int64_t step = (int64_t)RL * rp;
+    int64_t t = r0 + rl;
+    for (; t + 3 * RL < r1; t += 4 * RL) {  // four rows per iteration: the loads of all four in flight
+        const int64_t o = t * rp + c;
+        double bv[4], av[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            bv[u] = b[o + u * step];
+            av[u] = Ax ? Ax[o + u * step] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const T v = (T)(Ax ? bv[u] - av[u] : bv[u]);
+            g.w[o + u * step] = v;
+            acc[0] += v * v;
+        }
+    }
+    for (; t < r1; t += RL) {
         const T v = (T)(Ax ? b[t * rp + c] - Ax[t * rp + c] : b[t * rp + c]);
         g.w[t * rp + c] = v;
         acc[0] += v * v;
@@ -372,7 +390,20 @@ __global__ void __launch_bounds__(GMB_THREADS, 3) gmb_start_fin(GmbT<T> g, doubl
     const T ib = beta > 0.0 ? (T)(1.0 / beta) : T(0);
     int64_t r0, r1;
     gmb_rows(g, r0, r1);
-    for (int64_t t = r0 + rl; t < r1; t += RL) {
+    const int64_t step = (int64_t)RL * rp;
+    int64_t t = r0 + rl;
+    for (; t + 3 * RL < r1; t += 4 * RL) {
+        const int64_t o = t * rp + c;
+        T v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = g.w[o + u * step] * ib;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            g.V[o + u * step] = v[u];
+            g.vcur[o + u * step] = v[u];
+        }
+    }
+    for (; t < r1; t += RL) {
         const T v = g.w[t * rp + c] * ib;
         g.V[t * rp + c] = v;
         g.vcur[t * rp + c] = v;
@@ -397,9 +428,10 @@ __global__ void gmb_backsolve(GmbT<T> g, int last) {
     }
 }
 // x += V y over Arnoldi columns 0..kmax (x double; with a float basis the
-// combination V y is formed in float and added in double)
+// combination V y is formed in float and added in double); launched with
+// about one element per thread (GMB_XU_BLOCKS)
 template <class T>
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_xupdate(GmbT<T> g, double *__restrict__ x, int kmax) {
+__global__ void __launch_bounds__(GMB_THREADS) gmb_xupdate(GmbT<T> g, double *__restrict__ x, int kmax) {
     const int rp = g.rp;
     const size_t stride = (size_t)g.N * rp;
     const int64_t tot = g.N * rp;
@@ -467,7 +499,9 @@ cudaError_t gmb_finish(const GmbT<T> &g, double *x, int last, int kmax, cudaStre
     gmb_backsolve<T><<<1, 64, 0, st>>>(g, last);
     count_launch();
     if (kmax >= 0) {
-        gmb_xupdate<T><<<g.nblk, GMB_THREADS, 0, st>>>(g, x, kmax);
+        const int64_t tot = g.N * g.rp;
+        const int nb = (int)std::min<int64_t>((tot + GMB_THREADS - 1) / GMB_THREADS, 152 * 64);
+        gmb_xupdate<T><<<nb, GMB_THREADS, 0, st>>>(g, x, kmax);
         count_launch();
     }
     return cudaGetLastError();
