@@ -75,9 +75,10 @@ template <class T> struct DBuf {
 // Device state of the lockstep GMRES for one Krylov-vector type T
 template <class T> struct GmbStore {
     DBuf<T> V, w, vcur;
-    DBuf<double> H, cs, sn, s, part, hsum, normb, resid, y, tol;
+    DBuf<double> H, cs, sn, s, part, hsum, normb, resid, y, z, tol;
     DBuf<int32_t> conv, iter;
     int m = -1, rp = 0;
+    int jres = -1;  // the last solve from x0 = 0: largest Arnoldi index + 1 (its residual is V z), else -1
 };
 
 inline int64_t pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
@@ -2039,6 +2040,7 @@ GmbT<T> gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
         S.normb.alloc((size_t)rp);
         S.resid.alloc((size_t)rp);
         S.y.alloc((size_t)(m + 1) * rp);
+        S.z.alloc((size_t)(m + 2) * rp);
         S.conv.alloc((size_t)rp);
         S.tol.alloc(1);
         S.iter.alloc(2);
@@ -2058,6 +2060,7 @@ GmbT<T> gmb_state(h2w_handle *h, int m, int rp, int nrhs) {
     g.normb = S.normb.p;
     g.resid = S.resid.p;
     g.y = S.y.p;
+    g.z = S.z.p;
     g.conv = S.conv.p;
     g.tolp = S.tol.p;
     g.iter = S.iter.p;
@@ -2138,6 +2141,8 @@ int gmres_batch_run_t(h2w_handle *h, const double *bi, double *xi, int rp, int n
         kmax = std::max(kmax, cv >= 0 ? cv : (cv == -1 ? last : -1));
     }
     CK(gmb_finish(g, xi, last, kmax, st));
+    // the solved system's residual bi - A d is V z (Arnoldi relation) from x0 = 0
+    gmb_store(h, (T *)nullptr).jres = (x0_zero && kmax + 1 <= max_iter) ? kmax + 1 : -1;
     std::vector<double> rs((size_t)rp);
     CK(cudaMemcpyAsync(rs.data(), g.resid, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -2221,6 +2226,14 @@ double dnorm(h2w_handle *h, const double *x) {
 // cannot. eta is measured once per operator: max over calibration vectors z
 // (pseudo-random and smooth) of ||A32 z - A z|| / ||z||.
 constexpr double IR_UPDATE_SAFETY = 10.0, IR_UPDATE_SHARE = 0.25, IR_UPDATE_FLOOR = 0.01;
+// The update may instead be read from the inner solve: with d = V y from
+// GMRES on A32 d = r (r rounded to the basis precision, r_f), the Arnoldi
+// relation gives r_f - A32 d = V_{k+1} (beta e1 - Hbar y), so
+// r - A32 d = (r - r_f) + V_{k+1} z costs a basis combination, no product. Its
+// error adds the rounding of the Arnoldi relation (each basis vector's
+// product and the orthogonalisation) to that of the product; it is charged
+// IR_UPDATE_ARNOLDI times the product's bound.
+constexpr double IR_UPDATE_ARNOLDI = 4.0;
 constexpr double IR_U64_OVER_U32 = 0x1.0p-29;
 
 // Relative tolerance of a refinement step's inner solve: enough to bring the
@@ -3303,18 +3316,30 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
             for (int o = 0; o <= max_outer; ++o) {
                 // residual r = b - A x: FP32 operator at x0 (a correction only), then
                 // FP64 (or double-FP32) products, which are the stopping test, or
-                // r -= A32 d while every column's error bound allows it
-                bool upd = h->ir_update && o >= 2 && above_floor;
+                // r - A32 d while every column's error bound allows it: from the inner
+                // solve's Arnoldi relation (no product) or from an FP32 product
+                using BT = typename std::remove_pointer<decltype(g.V)>::type;
+                const int jres = gmb_store(h, (BT *)nullptr).jres;  // the inner state is g's
+                bool upd = h->ir_update && o >= 2 && above_floor, arn = upd && jres >= 0;
                 if (upd) {
                     CK(gmb_norms(g, h->m_di.p, h->m_dn.p, 0, st));
                     CK(cudaMemcpyAsync(nd.data(), h->m_dn.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
                     CK(cudaStreamSynchronize(st));
-                    for (int c = 0; c < nc; ++c)
-                        if (!(drift[(size_t)c] + IR_UPDATE_SAFETY * eta * nd[(size_t)c] <=
-                              IR_UPDATE_SHARE * tol * nb[(size_t)c]))
-                            upd = false;
+                    for (int c = 0; c < nc; ++c) {
+                        const double budget = IR_UPDATE_SHARE * tol * nb[(size_t)c];
+                        if (!(drift[(size_t)c] + IR_UPDATE_SAFETY * IR_UPDATE_ARNOLDI * eta * nd[(size_t)c] <= budget))
+                            arn = false;
+                        if (!(drift[(size_t)c] + IR_UPDATE_SAFETY * eta * nd[(size_t)c] <= budget)) upd = false;
+                    }
+                    arn = arn && upd;
                 }
-                if (upd) {
+                if (arn) {  // r - A32 d = (r - r_f) + V z of the last inner solve
+                    CK(gmb_residual(g, h->m_ri.p, h->m_ti.p, jres, st));
+                    std::swap(h->m_ri.p, h->m_ti.p);
+                    std::swap(h->m_ri.n, h->m_ti.n);
+                    for (int c = 0; c < nc; ++c)
+                        drift[(size_t)c] += IR_UPDATE_SAFETY * IR_UPDATE_ARNOLDI * eta * nd[(size_t)c];
+                } else if (upd) {
                     run_matvec_multi(h, H2W_PREC_FP32, rp, h->m_di.p, h->m_ti.p, st);
                     CK(vec_axpby(1.0, h->m_ri.p, -1.0, h->m_ti.p, h->m_ri.p, (int64_t)len, st));
                     for (int c = 0; c < nc; ++c) drift[(size_t)c] += IR_UPDATE_SAFETY * eta * nd[(size_t)c];

@@ -411,7 +411,9 @@ __global__ void __launch_bounds__(GMB_THREADS, 3) gmb_start_fin(GmbT<T> g, doubl
 }
 // y_c = H_c(0:k, 0:k) \ s_c(0:k), k = the column's last Arnoldi index
 // (converged: conv; still running: last; converged at the start / padding: none),
-// in the reference's back-substitution order (*/codes/gmres.hpp:77-90)
+// in the reference's back-substitution order (*/codes/gmres.hpp:77-90). Also
+// z_c = beta e1 - Hbar y = Q^T (s_{k+1} e_{k+1}): the rotations undone on the
+// last rotated residual entry (padding: z = 0).
 template <class T>
 __global__ void gmb_backsolve(GmbT<T> g, int last) {
     const int c = threadIdx.x;
@@ -425,6 +427,16 @@ __global__ void gmb_backsolve(GmbT<T> g, int last) {
         const double yi = y[(size_t)i * g.rp + c] / g.H[gmb_h(g, c, i, i)];
         y[(size_t)i * g.rp + c] = yi;
         for (int j = i - 1; j >= 0; --j) y[(size_t)j * g.rp + c] -= g.H[gmb_h(g, c, j, i)] * yi;
+    }
+    double *z = g.z;
+    const double *cs = g.cs + (size_t)c * (g.m + 1), *sn = g.sn + (size_t)c * (g.m + 1);
+    for (int j = 0; j <= g.m + 1; ++j) z[(size_t)j * g.rp + c] = 0.0;
+    if (cv == -3 || k + 1 > g.m) return;
+    z[(size_t)(k + 1) * g.rp + c] = s[k + 1];
+    for (int i = k; i >= 0; --i) {  // (z_i, z_{i+1}) <- G_i^T (z_i, z_{i+1})
+        const double a = z[(size_t)i * g.rp + c], b = z[(size_t)(i + 1) * g.rp + c];
+        z[(size_t)i * g.rp + c] = cs[i] * a - sn[i] * b;
+        z[(size_t)(i + 1) * g.rp + c] = sn[i] * a + cs[i] * b;
     }
 }
 // x += V y over Arnoldi columns 0..kmax (x double; with a float basis the
@@ -447,6 +459,24 @@ __global__ void __launch_bounds__(GMB_THREADS) gmb_xupdate(GmbT<T> g, double *__
             for (int j = 0; j <= kmax; ++j) v += V[j * stride + e] * g.y[(size_t)j * rp + c];
             x[e] = v;
         }
+    }
+}
+
+// rout = (rin - T(rin)) + sum_{j <= jmax} V_j z_j: the residual of the solved
+// system rin - A d (the right-hand side was rin rounded to T), one element per thread
+template <class T>
+__global__ void __launch_bounds__(GMB_THREADS)
+    gmb_resvec(GmbT<T> g, const double *__restrict__ rin, double *__restrict__ rout, int jmax) {
+    const int rp = g.rp;
+    const size_t stride = (size_t)g.N * rp;
+    const int64_t tot = g.N * rp;
+    const T *__restrict__ V = g.V;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e % rp);
+        T v = T(0);
+        for (int j = 0; j <= jmax; ++j) v += V[j * stride + e] * (T)g.z[(size_t)j * rp + c];
+        const double r = rin[e];
+        rout[e] = (r - (double)(T)r) + (double)v;
     }
 }
 
@@ -506,13 +536,23 @@ cudaError_t gmb_finish(const GmbT<T> &g, double *x, int last, int kmax, cudaStre
     }
     return cudaGetLastError();
 }
+template <class T>
+cudaError_t gmb_residual(const GmbT<T> &g, const double *rin, double *rout, int jmax, cudaStream_t st) {
+    if (jmax < 0 || jmax > g.m) return cudaErrorInvalidValue;
+    const int64_t tot = g.N * g.rp;
+    const int nb = (int)std::min<int64_t>((tot + GMB_THREADS - 1) / GMB_THREADS, 152 * 64);
+    gmb_resvec<T><<<nb, GMB_THREADS, 0, st>>>(g, rin, rout, jmax);
+    count_launch();
+    return cudaGetLastError();
+}
 
 #define GMB_INSTANTIATE(T)                                                                                         \
     template cudaError_t gmb_norms<T>(const GmbT<T> &, const double *, double *, int, cudaStream_t);              \
     template cudaError_t gmb_start<T>(const GmbT<T> &, const double *, const double *, double, cudaStream_t);     \
     template cudaError_t gmb_arnoldi<T>(const GmbT<T> &, cudaStream_t);                                           \
     template cudaError_t gmb_loop<T>(const GmbT<T> &, cudaGraphConditionalHandle, cudaStream_t);                  \
-    template cudaError_t gmb_finish<T>(const GmbT<T> &, double *, int, int, cudaStream_t);
+    template cudaError_t gmb_finish<T>(const GmbT<T> &, double *, int, int, cudaStream_t);                       \
+    template cudaError_t gmb_residual<T>(const GmbT<T> &, const double *, double *, int, cudaStream_t);
 GMB_INSTANTIATE(double)
 GMB_INSTANTIATE(float)
 #undef GMB_INSTANTIATE

@@ -262,6 +262,7 @@ struct GmbT {
     double *hsum;            // (m+1) x rp reduced sums
     double *normb, *resid;   // rp
     double *y;               // (m+1) x rp back-substituted coefficients
+    double *z;               // (m+2) x rp: beta e1 - Hbar y of each column (its residual in the basis)
     int32_t *conv;           // rp: -1 running, k >= 0 converged at Arnoldi column k, -2 at the start, -3 padding
     int32_t *iter;           // [0] current Arnoldi column, [1] steps taken
     double *tolp;            // stopping tolerance (device, so that captured steps do not hold it)
@@ -277,7 +278,13 @@ template <class T>
 cudaError_t gmb_arnoldi(const GmbT<T> &g, cudaStream_t st);
 template <class T>
 cudaError_t gmb_loop(const GmbT<T> &g, cudaGraphConditionalHandle hnd, cudaStream_t st);
+// x += V y (and z = beta e1 - Hbar y per column)
 template <class T>
 cudaError_t gmb_finish(const GmbT<T> &g, double *x, int last, int kmax, cudaStream_t st);
+// after gmb_finish: rout = (rin - T(rin)) + sum_{j <= jmax} V_j z_j, the solved system's
+// residual rin - A d from the Arnoldi relation (rin: the right-hand side the solve started
+// from at x0 = 0; jmax: the largest Arnoldi index + 1 over the columns)
+template <class T>
+cudaError_t gmb_residual(const GmbT<T> &g, const double *rin, double *rout, int jmax, cudaStream_t st);
 
 }  // namespace h2w

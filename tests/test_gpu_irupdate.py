@@ -2,7 +2,8 @@
 the solvers reach the same tolerance on the TRUE FP64 residual, the reported
 residual (||r|| plus the update's error bound) bounds the true one and stays
 within the bound's budget (25 % of the tolerance) of it, and the update does
-replace accurate products."""
+replace accurate products (taking r - A32 d from the inner solve's Arnoldi
+relation, without a product)."""
 import numpy as np
 import pytest
 
@@ -38,6 +39,7 @@ def test_ir_batch_residual_update(gpu, tol_pow):
     op.profile(True)
     X1, o1, i1, r1 = op.gmres_ir_batch(B, max_outer=20, inner_iter=100, tol_pow=tol_pow)
     acc_on = op.profile_multi(hw.PREC_FP64)[0]
+    f32_on = op.profile_multi(hw.PREC_FP32)[0]
     op.profile(False)
     assert np.all(r0 < tol) and np.all(r1 < tol)
     t1 = true_resid(op, B, X1)
@@ -54,6 +56,9 @@ def test_ir_batch_residual_update(gpu, tol_pow):
     assert acc_off == o0
     if o0 >= 2 and tol_pow == 8:
         assert acc_on < acc_off, (acc_on, acc_off)
+        # the updated residual came from the inner solve's Arnoldi relation: FP32
+        # products = the residual at x0 + one per inner Arnoldi step, none for the update
+        assert f32_on == 1 + i1, (f32_on, i1)
     print("accurate residual products: %d without updating, %d with" % (acc_off, acc_on))
 
 
