@@ -151,6 +151,12 @@ struct h2w_handle {
     GmbStore<double> gbd;  // FP64 Krylov vectors (FP64 solves)
     GmbStore<float> gbf;   // FP32 Krylov vectors (inner solves of the refinement, H2W_OPT_F32_BASIS)
     bool f32_basis = true;
+    // dataflow launch of the multi-vector stream (H2W_OPT_DATAFLOW): producer counts
+    // (initial and working copy) and consumer lists
+    bool dataflow = false;
+    DBuf<int32_t> d_mdep0, d_mdep, d_mcidx;
+    DBuf<int64_t> d_mcoff;
+    int64_t mflow_edges = 0;
     // graph-captured Arnoldi loops (a while node whose body is one step)
     struct LoopGraph {
         int kind, prec, m, rp, nrhs;
@@ -1192,6 +1198,82 @@ void pack_records(const PlanBuilder &pb, const std::vector<Phase> &phases, std::
 
 // (Re)cut the single-vector target stream: row chunks of max(4,
 // row_split / width) rows, column splits past XW_CAP; per-phase byte counts
+// Producer -> consumer dependencies between the targets of a stream, over the
+// workspace rows they touch, for the dataflow launch (no grid barriers). In
+// target order (the phase order, a topological order of the tree passes):
+// a target that reads rows (gathered sources, or its destination when it
+// accumulates) depends on the earlier writers of those rows since the last
+// overwrite; a target that writes rows depends on the earlier writers (an
+// atomic writer: only on the last non-atomic one, atomic additions commute)
+// and on the earlier readers since the last overwrite. Output: cnt[t]
+// producers, and the consumers of each target in CSR (coff, cidx). Every
+// dependency points from a lower target index to a higher one.
+void build_deps(const PlanBuilder &pb, int64_t ws_n, std::vector<int32_t> &cnt, std::vector<int64_t> &coff,
+                std::vector<int32_t> &cidx) {
+    const size_t nt = pb.T.size();
+    std::vector<int32_t> last_nw((size_t)ws_n, -1);
+    std::vector<std::vector<int32_t>> atom((size_t)ws_n), rd((size_t)ws_n);
+    std::vector<std::vector<int32_t>> prod(nt);
+    std::vector<int32_t> deps, rows_read;
+    for (size_t t = 0; t < nt; ++t) {
+        const Target &tg = pb.T[t];
+        const bool scatter = tg.flags & T_SCATTER, atomic = tg.flags & T_ATOMIC, accum = tg.flags & T_ACCUM;
+        deps.clear();
+        rows_read.clear();
+        auto read_row = [&](int64_t r) {
+            if (last_nw[(size_t)r] >= 0) deps.push_back(last_nw[(size_t)r]);
+            for (int32_t a : atom[(size_t)r]) deps.push_back(a);
+            rows_read.push_back((int32_t)r);
+        };
+        for (int32_t q = tg.p0; q < tg.p1; ++q) {
+            const Panel &pn = pb.P[(size_t)q];
+            for (int32_t e = pn.s0; e < pn.s1; ++e) {
+                const Seg &sg = pb.S[(size_t)e];
+                if (sg.flags & S_GATHER) continue;  // the input vector: no producer
+                for (int64_t r = sg.src; r < sg.src + sg.len; ++r) read_row(r);
+            }
+        }
+        if (accum)
+            for (int64_t r = tg.dst; r < tg.dst + tg.nrows; ++r) read_row(r);
+        if (!scatter)
+            for (int64_t r = tg.dst; r < tg.dst + tg.nrows; ++r) {
+                if (last_nw[(size_t)r] >= 0) deps.push_back(last_nw[(size_t)r]);
+                if (!atomic)
+                    for (int32_t a : atom[(size_t)r]) deps.push_back(a);
+                for (int32_t a : rd[(size_t)r]) deps.push_back(a);
+            }
+        std::sort(deps.begin(), deps.end());
+        deps.erase(std::unique(deps.begin(), deps.end()), deps.end());
+        deps.erase(std::remove(deps.begin(), deps.end(), (int32_t)t), deps.end());
+        prod[t] = deps;
+        for (int32_t r : rows_read) rd[(size_t)r].push_back((int32_t)t);
+        if (!scatter)
+            for (int64_t r = tg.dst; r < tg.dst + tg.nrows; ++r) {
+                if (atomic) {
+                    atom[(size_t)r].push_back((int32_t)t);
+                } else {
+                    last_nw[(size_t)r] = (int32_t)t;
+                    atom[(size_t)r].clear();
+                    rd[(size_t)r].clear();
+                }
+            }
+    }
+    cnt.assign(nt, 0);
+    coff.assign(nt + 1, 0);
+    for (size_t t = 0; t < nt; ++t) {
+        cnt[t] = (int32_t)prod[t].size();
+        for (int32_t u : prod[t]) {
+            if (u < 0 || (size_t)u >= t) throw ApiError(H2W_ERR_STATE, "dataflow dependency against the target order");
+            ++coff[(size_t)u + 1];
+        }
+    }
+    for (size_t t = 0; t < nt; ++t) coff[t + 1] += coff[t];
+    cidx.assign((size_t)coff[nt], 0);
+    std::vector<int64_t> fill(coff.begin(), coff.end() - 1);
+    for (size_t t = 0; t < nt; ++t)
+        for (int32_t u : prod[t]) cidx[(size_t)fill[(size_t)u]++] = (int32_t)t;
+}
+
 // for the profiling statistics.
 void realize_single(h2w_handle *h, int64_t row_split) {
     if (!h->plan) throw ApiError(H2W_ERR_STATE, "operator not assembled");
@@ -1242,6 +1324,16 @@ void realize_multi(h2w_handle *h, int64_t cap) {
     assign_phases(h, pb, h->nph_total, h->mphases, h->fused_scatter_m);
     validate_plan(pb, h, h->mphases);
     pack_records(pb, h->mphases, roff, blob, pstart);
+    {
+        std::vector<int32_t> cnt, cidx;
+        std::vector<int64_t> coff;
+        build_deps(pb, h->ws_n, cnt, coff, cidx);
+        h->d_mdep0.upload(cnt, h->stream);
+        h->d_mdep.alloc(cnt.size());
+        h->d_mcoff.upload(coff, h->stream);
+        h->d_mcidx.upload(cidx, h->stream);
+        h->mflow_edges = (int64_t)cidx.size();
+    }
     cudaStream_t st = h->stream;
     h->d_roff_m.upload(roff, st);
     h->d_blob_m.upload(blob, st);
@@ -1958,7 +2050,13 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
         const size_t nx = (size_t)h->tree.N * (size_t)rp;
         if (h->m_xf.n < nx) h->m_xf.alloc(nx);
         CK(vec_f64_to_f32(xi, h->m_xf.p, (int64_t)nx, st));
+        const bool flow = h->dataflow && h->coop && !h->tensor;
+        if (flow) CK(cudaMemcpyAsync(h->d_mdep.p, h->d_mdep0.p, h->d_mdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         mr_prof(h, prec, rp, st, [&] {
+            if (flow)
+                return launch_mr_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
+                                          h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, h->m_xf.p,
+                                          yi, h->d_err.p, st);
             if (h->tensor)
                 return launch_mrt_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p,
                                       h->d_op32.p, h->m_wsf.p, h->m_xf.p, yi, h->d_bar.p, h->d_err.p, st);
@@ -2001,7 +2099,13 @@ void run_matvec_multi_f32io(h2w_handle *h, int rp, const float *xf, float *yf, c
     ensure_f32(h);
     if (h->m_wsf.n < wsz) h->m_wsf.alloc(wsz);
     CK(cudaMemsetAsync(h->m_wsf.p, 0, wsz * 4, st));
+    const bool flow = h->dataflow && h->coop && !h->tensor;
+    if (flow) CK(cudaMemcpyAsync(h->d_mdep.p, h->d_mdep0.p, h->d_mdep0.n * 4, cudaMemcpyDeviceToDevice, st));
     mr_prof(h, H2W_PREC_FP32, rp, st, [&] {
+        if (flow)
+            return launch_mr_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
+                                      h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, xf, yf, h->d_err.p,
+                                      st);
         if (h->tensor)
             return launch_mrt_f32(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p,
                                   h->d_op32.p, h->m_wsf.p, xf, yf, h->d_bar.p, h->d_err.p, st);
@@ -3415,6 +3519,14 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
             h->ir_update = value != 0;
         } else if (option == H2W_OPT_F32_BASIS) {
             h->f32_basis = value != 0;
+        } else if (option == H2W_OPT_DATAFLOW) {
+            h->dataflow = value != 0;
+            h->eta_multi = -1.0;
+            for (auto &g : h->loops) {  // captured steps hold the other launch form
+                cudaGraphExecDestroy(g.exec);
+                cudaGraphDestroy(g.graph);
+            }
+            h->loops.clear();
         } else if (option == H2W_OPT_TENSOR) {
             h->tensor = value != 0;
             h->eta_multi = -1.0;
@@ -3448,6 +3560,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_IR_UPDATE) *value = h->ir_update ? 1 : 0;
         else if (option == H2W_OPT_TENSOR) *value = h->tensor ? 1 : 0;
         else if (option == H2W_OPT_F32_BASIS) *value = h->f32_basis ? 1 : 0;
+        else if (option == H2W_OPT_DATAFLOW) *value = h->dataflow ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });

@@ -221,6 +221,16 @@ cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, cons
 cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                           const MrPhases *phased, int32_t *ctr, const float *A, float *ws, const float *xin, float *yout,
                           unsigned *bar, int32_t *err, cudaStream_t st);
+// Dataflow launch of the FP32 multi-vector stream (no grid barriers): nt
+// targets in stored order, ctr a zeroed claim counter, rem the targets'
+// producer counts (reset before every launch), consumers of target t in
+// cidx[coff[t] .. coff[t+1]); err = 3 if a wait timed out
+cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+                               const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
+                               double *yout, int32_t *err, cudaStream_t st);
+cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+                               const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
+                               float *yout, int32_t *err, cudaStream_t st);
 // Double-FP32 arithmetic on the FP32 pipes (each product and sum carried as
 // an FP32 pair; about 2^-44 relative per term instead of FP64's 2^-53): A and
 // xin are (hi, lo) pairs (launch_mr_split of the FP64 operator and input),

@@ -295,7 +295,7 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
 // (cp.async, zero-filled past a target's rows or a panel's columns) into
 // MR_NSA buffers: the copies of chunks i+1 and i+2 are in flight while chunk
 // i is multiplied, with no staging registers; one barrier per chunk.
-template <int RP, class YT>
+template <int RP, class YT, bool FLOW = false>
 __device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int64_t *__restrict__ roff,
                                                 const int64_t *__restrict__ blob, const float *__restrict__ A,
                                                 float *ws, const float *__restrict__ xin, YT *yout) {
@@ -439,9 +439,12 @@ __device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const float v = acc[i][j];
-                if (flags & T_SCATTER) yout[d + j] = (YT)((flags & T_ACCUM) ? ws[d + j] + v : v);
+                // dataflow launch: accumulated rows are read from L2 (__ldcg), as
+                // another SM may have produced them after this one cached the line
+                const float prev = (flags & T_ACCUM) ? (FLOW ? __ldcg(ws + d + j) : ws[d + j]) : 0.f;
+                if (flags & T_SCATTER) yout[d + j] = (YT)((flags & T_ACCUM) ? prev + v : v);
                 else if (flags & T_ATOMIC) atomicAdd(ws + d + j, v);
-                else if (flags & T_ACCUM) ws[d + j] += v;
+                else if (flags & T_ACCUM) ws[d + j] = prev + v;
                 else ws[d + j] = v;
             }
         }
@@ -500,6 +503,91 @@ static int mr_num_sms() {
     }
     return n;
 }
+
+// Dataflow form of mr_coop_kernel (FP32): no grid barriers. Targets are
+// claimed in their stored order (a topological order: every producer of a
+// target precedes it), first blockIdx.x, then from a global counter; a CTA
+// waits until its target's producer count rem[t] reaches zero (bounded spin:
+// on timeout it sets *err = 3 and proceeds, so the kernel always ends), runs
+// it, and decrements the counts of its consumers cidx[coff[t] .. coff[t+1]).
+// The launch is cooperative, so every CTA is resident: a waiting target's
+// producers have all been claimed by running CTAs.
+template <int RP, class YT>
+__global__ void __launch_bounds__(4 * RP)
+    mr_flow_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t nt, int32_t *ctr,
+                   int32_t *rem, const int64_t *__restrict__ coff, const int32_t *__restrict__ cidx,
+                   const float *__restrict__ A, float *ws, const float *__restrict__ xin, YT *yout, int32_t *err) {
+    extern __shared__ __align__(16) char mr_smem[];
+    __shared__ int64_t s_next;
+    int64_t t = blockIdx.x;
+    while (t < nt) {
+        if (threadIdx.x == 0) {
+            long long it = 0;
+            while (*((volatile int32_t *)(rem + t)) > 0) {
+                if (++it > (1LL << 20)) {  // about 0.1 s
+                    atomicExch(err, 3);
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        mr_target_async<RP, YT, true>(mr_smem, t, roff, blob, A, ws, xin, yout);  // ends with a barrier
+        if (threadIdx.x < 32) {
+            __threadfence();  // this CTA's results are visible before its consumers are released
+            for (int64_t e = coff[t] + threadIdx.x; e < coff[t + 1]; e += 32) atomicSub(rem + cidx[e], 1);
+            if (threadIdx.x == 0) s_next = gridDim.x + atomicAdd(ctr, 1);
+        }
+        __syncthreads();
+        t = s_next;
+    }
+}
+
+template <int RP, class YT>
+static cudaError_t mr_flow_launch(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+                                  const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
+                                  YT *yout, int32_t *err, cudaStream_t st) {
+    using Lay = MrLayout<float, RP>;
+    constexpr size_t SMEM = Lay::smem_async;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        if (cudaFuncSetAttribute(mr_flow_kernel<RP, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) !=
+            cudaSuccess)
+            return cudaErrorInvalidValue;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_flow_kernel<RP, YT>, Lay::NT, SMEM);
+        if (per_sm <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    }
+    const int grid = mr_num_sms() * per_sm;
+    void *args[] = {(void *)&roff, (void *)&blob, (void *)&nt, (void *)&ctr, (void *)&rem, (void *)&coff,
+                    (void *)&cidx, (void *)&A, (void *)&ws, (void *)&xin, (void *)&yout, (void *)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_flow_kernel<RP, YT>, dim3(grid), dim3(Lay::NT), args,
+                                                SMEM, st);
+    count_launch();
+    return e;
+}
+template <class YT>
+static cudaError_t mr_flow_dispatch(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
+                                    int32_t *rem, const int64_t *coff, const int32_t *cidx, const float *A, float *ws,
+                                    const float *xin, YT *yout, int32_t *err, cudaStream_t st) {
+    switch (rp) {
+    case 16: return mr_flow_launch<16, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    case 32: return mr_flow_launch<32, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    case 64: return mr_flow_launch<64, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+                               const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
+                               double *yout, int32_t *err, cudaStream_t st) {
+    return mr_flow_dispatch(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+}
+cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+                               const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
+                               float *yout, int32_t *err, cudaStream_t st) {
+    return mr_flow_dispatch(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+}
+
 
 template <class T, int RP, bool DF, class YT>
 static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,

@@ -53,6 +53,7 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--tensor", action="store_true", help="FP32 multi-vector products on the tensor cores")
+    ap.add_argument("--no-dataflow", action="store_true", help="FP32 multi-vector products with grid barriers")
     a = ap.parse_args(argv)
 
     import torch
@@ -69,6 +70,8 @@ def main(argv=None):
         op.set_option(hw.OPT_GRAPH, 0)
     if a.tensor:
         op.set_option(hw.OPT_TENSOR, 1)
+    if a.no_dataflow:
+        op.set_option(hw.OPT_DATAFLOW, 0)
     op.set_option(hw.OPT_IR_RESIDUAL, PREC[a.ir_residual])
     R = max(1, min(64, a.rhs))
     # column-major N x R blocks = rows of R x N tensors
