@@ -153,7 +153,7 @@ struct h2w_handle {
     bool f32_basis = true;
     // dataflow launch of the multi-vector stream (H2W_OPT_DATAFLOW): producer counts
     // (initial and working copy) and consumer lists
-    bool dataflow = false;
+    bool dataflow = true;
     DBuf<int32_t> d_mdep0, d_mdep, d_mcidx;
     DBuf<int64_t> d_mcoff;
     int64_t mflow_edges = 0;

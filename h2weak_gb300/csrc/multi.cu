@@ -295,7 +295,7 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
 // (cp.async, zero-filled past a target's rows or a panel's columns) into
 // MR_NSA buffers: the copies of chunks i+1 and i+2 are in flight while chunk
 // i is multiplied, with no staging registers; one barrier per chunk.
-template <int RP, class YT, bool FLOW = false>
+template <int RP, class YT>
 __device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int64_t *__restrict__ roff,
                                                 const int64_t *__restrict__ blob, const float *__restrict__ A,
                                                 float *ws, const float *__restrict__ xin, YT *yout) {
@@ -439,9 +439,7 @@ __device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const float v = acc[i][j];
-                // dataflow launch: accumulated rows are read from L2 (__ldcg), as
-                // another SM may have produced them after this one cached the line
-                const float prev = (flags & T_ACCUM) ? (FLOW ? __ldcg(ws + d + j) : ws[d + j]) : 0.f;
+                const float prev = (flags & T_ACCUM) ? ws[d + j] : 0.f;
                 if (flags & T_SCATTER) yout[d + j] = (YT)((flags & T_ACCUM) ? prev + v : v);
                 else if (flags & T_ATOMIC) atomicAdd(ws + d + j, v);
                 else if (flags & T_ACCUM) ws[d + j] = prev + v;
@@ -511,7 +509,11 @@ static int mr_num_sms() {
 // on timeout it sets *err = 3 and proceeds, so the kernel always ends), runs
 // it, and decrements the counts of its consumers cidx[coff[t] .. coff[t+1]).
 // The launch is cooperative, so every CTA is resident: a waiting target's
-// producers have all been claimed by running CTAs.
+// producers have all been claimed by running CTAs. Workspace reads are as in
+// the barrier launch (gathered sources by cp.async.cg from L2, an
+// accumulating target's own rows by plain loads); the dependencies order
+// every writer of a row before its readers, and each producer fences its
+// writes before releasing its consumers.
 template <int RP, class YT>
 __global__ void __launch_bounds__(4 * RP)
     mr_flow_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t nt, int32_t *ctr,
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(4 * RP)
             __threadfence();
         }
         __syncthreads();
-        mr_target_async<RP, YT, true>(mr_smem, t, roff, blob, A, ws, xin, yout);  // ends with a barrier
+        mr_target_async<RP, YT>(mr_smem, t, roff, blob, A, ws, xin, yout);  // ends with a barrier
         if (threadIdx.x < 32) {
             __threadfence();  // this CTA's results are visible before its consumers are released
             for (int64_t e = coff[t] + threadIdx.x; e < coff[t + 1]; e += 32) atomicSub(rem + cidx[e], 1);

@@ -213,13 +213,12 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 (FP32 operator, x0 = 0) keep their Krylov vectors and do
  *                 their orthogonalisation in FP32 (Hessenberg, rotations and
  *                 block sums in FP64); 0: FP64 Krylov vectors.
- *  H2W_OPT_DATAFLOW  1: the FP32 multi-vector product runs as one
+ *  H2W_OPT_DATAFLOW  1 (default): the FP32 multi-vector product runs as one
  *                 cooperative launch without grid barriers: each target waits
  *                 for the targets that produce the workspace rows it uses
  *                 (dependencies derived on the host from the rows each target
- *                 reads and writes) and releases its consumers; 0 (default):
- *                 phases separated by grid barriers, which measured faster
- *                 (the dataflow form must read accumulated rows from L2). */
+ *                 reads and writes) and releases its consumers; 0: phases
+ *                 separated by grid barriers. */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
        H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);

@@ -1,5 +1,5 @@
-"""Dataflow launch of the FP32 multi-vector product (opt-in; targets wait for
-the targets producing their workspace rows, no grid barriers) against the
+"""Dataflow launch of the FP32 multi-vector product (targets wait for the
+targets producing their workspace rows, no grid barriers) against the
 barrier-phased launch and the FP64 product, on 1D/2D/3D operators of both
 forms and blocks of 7/16/32/64 columns, and inside the batched mixed solve."""
 import numpy as np
@@ -19,8 +19,7 @@ def test_dataflow_product(gpu, case):
     hw = gpu
     op, _ = setup(hw, case)
     op.assemble(hw.ASSEMBLE_NCA)
-    assert op.get_option(hw.OPT_DATAFLOW) == 0
-    op.set_option(hw.OPT_DATAFLOW, 1)
+    assert op.get_option(hw.OPT_DATAFLOW) == 1
     for k in (7, 16, 32, 64):
         X = rhs(110 + k, op.N, k)
         Y64 = op.matvec(X)
