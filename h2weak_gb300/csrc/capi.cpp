@@ -2076,7 +2076,16 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
             if (h->m_xdf.n < nx) h->m_xdf.alloc(nx);
             CK(launch_mr_split(xi, h->m_xdf.p, (int64_t)nx, st));
         }
+        const bool flow = h->dataflow && h->coop;
+        if (flow) CK(cudaMemcpyAsync(h->d_mdep.p, h->d_mdep0.p, h->d_mdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         mr_prof(h, prec, rp, st, [&] {
+            if (flow) {
+                const bool df = prec == H2W_PREC_DF64;
+                return launch_mr_f64_flow(rp, df, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1,
+                                          h->d_mctr.p, h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p,
+                                          df ? h->d_opdf.p : h->d_op.p, h->m_wsd.p, df ? h->m_xdf.p : xi, yi,
+                                          h->d_err.p, st);
+            }
             if (prec == H2W_PREC_DF64)
                 return launch_mr_df64(rp, h->d_roff_m.p, h->d_blob_m.p, h->d_pstart_m.p, nph, phased, h->d_mctr.p,
                                       h->d_opdf.p, h->m_wsd.p, h->m_xdf.p, yi, h->d_bar.p, h->d_err.p, st);

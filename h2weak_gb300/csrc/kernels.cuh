@@ -231,6 +231,11 @@ cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob,
 cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
                                const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
                                float *yout, int32_t *err, cudaStream_t st);
+// the same for the FP64 (df = false) and double-FP32 (df = true, A and xin
+// pre-split pairs as for launch_mr_df64) products
+cudaError_t launch_mr_f64_flow(int rp, bool df, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
+                               int32_t *rem, const int64_t *coff, const int32_t *cidx, const double *A, double *ws,
+                               const double *xin, double *yout, int32_t *err, cudaStream_t st);
 // Double-FP32 arithmetic on the FP32 pipes (each product and sum carried as
 // an FP32 pair; about 2^-44 relative per term instead of FP64's 2^-53): A and
 // xin are (hi, lo) pairs (launch_mr_split of the FP64 operator and input),

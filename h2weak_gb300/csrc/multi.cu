@@ -502,23 +502,23 @@ static int mr_num_sms() {
     return n;
 }
 
-// Dataflow form of mr_coop_kernel (FP32): no grid barriers. Targets are
-// claimed in their stored order (a topological order: every producer of a
-// target precedes it), first blockIdx.x, then from a global counter; a CTA
-// waits until its target's producer count rem[t] reaches zero (bounded spin:
-// on timeout it sets *err = 3 and proceeds, so the kernel always ends), runs
-// it, and decrements the counts of its consumers cidx[coff[t] .. coff[t+1]).
+// Dataflow form of mr_coop_kernel: no grid barriers. Targets are claimed in
+// their stored order (a topological order: every producer of a target
+// precedes it), first blockIdx.x, then from a global counter; a CTA waits
+// until its target's producer count rem[t] reaches zero (bounded spin: on
+// timeout it sets *err = 3 and proceeds, so the kernel always ends), runs it,
+// and decrements the counts of its consumers cidx[coff[t] .. coff[t+1]).
 // The launch is cooperative, so every CTA is resident: a waiting target's
 // producers have all been claimed by running CTAs. Workspace reads are as in
-// the barrier launch (gathered sources by cp.async.cg from L2, an
-// accumulating target's own rows by plain loads); the dependencies order
-// every writer of a row before its readers, and each producer fences its
-// writes before releasing its consumers.
-template <int RP, class YT>
+// the barrier launch (gathered sources by cp.async.cg from L2 or by plain
+// loads, an accumulating target's own rows by plain loads); the dependencies
+// order every writer of a row before its readers, and each producer fences
+// its writes before releasing its consumers.
+template <class T, int RP, bool DF, class YT>
 __global__ void __launch_bounds__(4 * RP)
     mr_flow_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t nt, int32_t *ctr,
                    int32_t *rem, const int64_t *__restrict__ coff, const int32_t *__restrict__ cidx,
-                   const float *__restrict__ A, float *ws, const float *__restrict__ xin, YT *yout, int32_t *err) {
+                   const T *__restrict__ A, T *ws, const T *__restrict__ xin, YT *yout, int32_t *err) {
     extern __shared__ __align__(16) char mr_smem[];
     __shared__ int64_t s_next;
     int64_t t = blockIdx.x;
@@ -535,7 +535,10 @@ __global__ void __launch_bounds__(4 * RP)
             __threadfence();
         }
         __syncthreads();
-        mr_target_async<RP, YT>(mr_smem, t, roff, blob, A, ws, xin, yout);  // ends with a barrier
+        if constexpr (std::is_same<T, float>::value && !DF)
+            mr_target_async<RP, YT>(mr_smem, t, roff, blob, A, ws, xin, yout);  // ends with a barrier
+        else
+            mr_target<T, RP, DF, YT>(mr_smem, t, roff, blob, A, ws, xin, yout);  // ends with a barrier
         if (threadIdx.x < 32) {
             __threadfence();  // this CTA's results are visible before its consumers are released
             for (int64_t e = coff[t] + threadIdx.x; e < coff[t + 1]; e += 32) atomicSub(rem + cidx[e], 1);
@@ -546,50 +549,55 @@ __global__ void __launch_bounds__(4 * RP)
     }
 }
 
-template <int RP, class YT>
+template <class T, int RP, bool DF, class YT>
 static cudaError_t mr_flow_launch(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
-                                  const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
+                                  const int64_t *coff, const int32_t *cidx, const T *A, T *ws, const T *xin,
                                   YT *yout, int32_t *err, cudaStream_t st) {
-    using Lay = MrLayout<float, RP>;
-    constexpr size_t SMEM = Lay::smem_async;
+    using Lay = MrLayout<T, RP>;
+    constexpr size_t SMEM = (std::is_same<T, float>::value && !DF) ? Lay::smem_async : Lay::smem;
     static int per_sm = 0;
     if (per_sm == 0) {
-        if (cudaFuncSetAttribute(mr_flow_kernel<RP, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(mr_flow_kernel<T, RP, DF, YT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SMEM) != cudaSuccess)
             return cudaErrorInvalidValue;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_flow_kernel<RP, YT>, Lay::NT, SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mr_flow_kernel<T, RP, DF, YT>, Lay::NT, SMEM);
         if (per_sm <= 0) return cudaErrorCooperativeLaunchTooLarge;
     }
     const int grid = mr_num_sms() * per_sm;
     void *args[] = {(void *)&roff, (void *)&blob, (void *)&nt, (void *)&ctr, (void *)&rem, (void *)&coff,
                     (void *)&cidx, (void *)&A, (void *)&ws, (void *)&xin, (void *)&yout, (void *)&err};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_flow_kernel<RP, YT>, dim3(grid), dim3(Lay::NT), args,
-                                                SMEM, st);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)mr_flow_kernel<T, RP, DF, YT>, dim3(grid), dim3(Lay::NT),
+                                                args, SMEM, st);
     count_launch();
     return e;
 }
-template <class YT>
+template <class T, bool DF, class YT>
 static cudaError_t mr_flow_dispatch(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
-                                    int32_t *rem, const int64_t *coff, const int32_t *cidx, const float *A, float *ws,
-                                    const float *xin, YT *yout, int32_t *err, cudaStream_t st) {
+                                    int32_t *rem, const int64_t *coff, const int32_t *cidx, const T *A, T *ws,
+                                    const T *xin, YT *yout, int32_t *err, cudaStream_t st) {
     switch (rp) {
-    case 16: return mr_flow_launch<16, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
-    case 32: return mr_flow_launch<32, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
-    case 64: return mr_flow_launch<64, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    case 16: return mr_flow_launch<T, 16, DF, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    case 32: return mr_flow_launch<T, 32, DF, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    case 64: return mr_flow_launch<T, 64, DF, YT>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
     default: return cudaErrorInvalidValue;
     }
 }
 cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
                                const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
                                double *yout, int32_t *err, cudaStream_t st) {
-    return mr_flow_dispatch(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    return mr_flow_dispatch<float, false>(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
 }
 cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
                                const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
                                float *yout, int32_t *err, cudaStream_t st) {
-    return mr_flow_dispatch(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    return mr_flow_dispatch<float, false>(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
 }
-
+cudaError_t launch_mr_f64_flow(int rp, bool df, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
+                               int32_t *rem, const int64_t *coff, const int32_t *cidx, const double *A, double *ws,
+                               const double *xin, double *yout, int32_t *err, cudaStream_t st) {
+    if (df) return mr_flow_dispatch<double, true>(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+    return mr_flow_dispatch<double, false>(rp, roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, err, st);
+}
 
 template <class T, int RP, bool DF, class YT>
 static cudaError_t mr_launch_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,

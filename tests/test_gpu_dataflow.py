@@ -1,6 +1,6 @@
-"""Dataflow launch of the FP32 multi-vector product (targets wait for the
+"""Dataflow launch of the multi-vector products (targets wait for the
 targets producing their workspace rows, no grid barriers) against the
-barrier-phased launch and the FP64 product, on 1D/2D/3D operators of both
+barrier-phased launch and the FP64 product, for FP32, FP64 and double-FP32, on 1D/2D/3D operators of both
 forms and blocks of 7/16/32/64 columns, and inside the batched mixed solve."""
 import numpy as np
 import pytest
@@ -30,6 +30,15 @@ def test_dataflow_product(gpu, case):
         # same per-target arithmetic; only the order of atomically accumulated column splits differs
         assert np.all(colerr(Yf, Yb) < 1e-6), (k, colerr(Yf, Yb).max())
         assert np.all(colerr(Yf, Y64) < 1e-5), (k, colerr(Yf, Y64).max())
+        # FP64 and double-FP32 products on the dataflow launch against the barrier launch
+        Ydf = op.matvec(X, precision=hw.PREC_DF64)
+        op.set_option(hw.OPT_DATAFLOW, 0)
+        Y64b = op.matvec(X)
+        Ydfb = op.matvec(X, precision=hw.PREC_DF64)
+        op.set_option(hw.OPT_DATAFLOW, 1)
+        assert np.all(colerr(Y64, Y64b) < 1e-14), (k, colerr(Y64, Y64b).max())
+        assert np.all(colerr(Ydf, Ydfb) < 1e-13), (k, colerr(Ydf, Ydfb).max())
+        assert np.all(colerr(Ydf, Y64) < 1e-12), (k, colerr(Ydf, Y64).max())
     # repeated launches give the same result (counters reset per launch)
     X = rhs(120, op.N, 64)
     Y1 = op.matvec(X, precision=hw.PREC_FP32)
