@@ -156,6 +156,8 @@ struct h2w_handle {
     bool dataflow = true;
     DBuf<int32_t> d_mdep0, d_mdep, d_mcidx;
     DBuf<int64_t> d_mcoff;
+    DBuf<int32_t> d_sdep0, d_sdep, d_scidx, d_sctr;  // the same for the single-vector stream
+    DBuf<int64_t> d_scoff;
     int64_t mflow_edges = 0;
     // graph-captured Arnoldi loops (a while node whose body is one step)
     struct LoopGraph {
@@ -1299,6 +1301,16 @@ void realize_single(h2w_handle *h, int64_t row_split) {
     }
     validate_plan(pb, h, h->phases);
     pack_records(pb, h->phases, roff, blob, pstart);
+    {
+        std::vector<int32_t> cnt, cidx;
+        std::vector<int64_t> coff;
+        build_deps(pb, h->ws_n, cnt, coff, cidx);
+        h->d_sdep0.upload(cnt, h->stream);
+        h->d_sdep.alloc(cnt.size());
+        h->d_scoff.upload(coff, h->stream);
+        h->d_scidx.upload(cidx, h->stream);
+        if (!h->d_sctr.p) h->d_sctr.alloc(1);
+    }
     cudaStream_t st = h->stream;
     h->d_roff.upload(roff, st);
     h->d_blob.upload(blob, st);
@@ -1883,7 +1895,14 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
-    if (h->coop) {
+    if (h->coop && h->dataflow) {
+        CK(cudaMemcpyAsync(h->d_sdep.p, h->d_sdep0.p, h->d_sdep0.n * 4, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemsetAsync(h->d_sctr.p, 0, 4, st));
+        prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
+            return launch_brg_flow_f64(h->d_roff.p, h->d_blob.p, (int64_t)h->d_roff.n - 1, h->d_sctr.p, h->d_sdep.p,
+                                       h->d_scoff.p, h->d_scidx.p, h->d_op.p, h->d_ws.p, dx, dy, perm, h->d_err.p, st);
+        });
+    } else if (h->coop) {
         prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
             return launch_coop_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op.p, h->d_ws.p, dx, dy, perm,
                                    h->d_bar.p, h->d_err.p, st);
@@ -1919,7 +1938,15 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
-    if (h->coop) {
+    if (h->coop && h->dataflow) {
+        CK(cudaMemcpyAsync(h->d_sdep.p, h->d_sdep0.p, h->d_sdep0.n * 4, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemsetAsync(h->d_sctr.p, 0, 4, st));
+        prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
+            return launch_brg_flow_f32(h->d_roff.p, h->d_blob.p, (int64_t)h->d_roff.n - 1, h->d_sctr.p, h->d_sdep.p,
+                                       h->d_scoff.p, h->d_scidx.p, h->d_op32.p, h->d_ws32.p, dx, dy, perm, h->d_err.p,
+                                       st);
+        });
+    } else if (h->coop) {
         prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
             return launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op32.p, h->d_ws32.p, dx, dy,
                                    perm, h->d_bar.p, h->d_err.p, st);

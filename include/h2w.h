@@ -213,9 +213,9 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 (FP32 operator, x0 = 0) keep their Krylov vectors and do
  *                 their orthogonalisation in FP32 (Hessenberg, rotations and
  *                 block sums in FP64); 0: FP64 Krylov vectors.
- *  H2W_OPT_DATAFLOW  1 (default): the multi-vector products (FP32, FP64,
- *                 double-FP32) run as one cooperative launch without grid
- *                 barriers: each target waits
+ *  H2W_OPT_DATAFLOW  1 (default): the products (single-vector FP64 / FP32,
+ *                 multi-vector FP32 / FP64 / double-FP32) run as one
+ *                 cooperative launch without grid barriers: each target waits
  *                 for the targets that produce the workspace rows it uses
  *                 (dependencies derived on the host from the rows each target
  *                 reads and writes) and releases its consumers; 0: phases

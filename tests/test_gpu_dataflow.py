@@ -61,3 +61,22 @@ def test_dataflow_in_batched_mixed_solve(gpu, graph):
     assert np.all(res < 1e-10)
     t = colerr(op.matvec(X), B)
     assert np.all(t < 1e-10), t.max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_dataflow_single_vector_product(gpu, case):
+    """One right-hand side (the single-vector stream) on the dataflow launch
+    against the barrier launch, FP64 and FP32."""
+    hw = gpu
+    op, _ = setup(hw, case)
+    op.assemble(hw.ASSEMBLE_NCA)
+    x = rhs(130, op.N, 1)[:, 0]
+    y64 = op.matvec(x)
+    y32 = op.matvec(x, precision=hw.PREC_FP32)
+    op.set_option(hw.OPT_DATAFLOW, 0)
+    b64 = op.matvec(x)
+    b32 = op.matvec(x, precision=hw.PREC_FP32)
+    op.set_option(hw.OPT_DATAFLOW, 1)
+    assert np.linalg.norm(y64 - b64) / np.linalg.norm(b64) < 1e-14
+    assert np.linalg.norm(y32 - b32) / np.linalg.norm(b32) < 1e-6
