@@ -89,6 +89,22 @@ __device__ __forceinline__ float2 df_split(double a) {
     const float h = __double2float_rn(a);
     return make_float2(h, __double2float_rn(__dsub_rn(a, (double)h)));
 }
+// The same pair without FP64 instructions (GB300 runs those at 1/64 rate):
+// hi = the double's top 24 significand bits as a float (truncated), lo = the
+// remaining 29 bits, converted to float (rounded to 24 bits) and scaled by the
+// exact power of two 2^(E-52); hi + lo carries 47 bits. Used when both parts
+// are normal floats (exponent E in [-74, 127]); otherwise (zero, tiny or huge
+// values) the FP64 split.
+__device__ __forceinline__ float2 df_split_fast(double a) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(a);
+    const int e = (int)((u >> 52) & 0x7ff);
+    if (e < 1023 - 74 || e > 1023 + 127) return df_split(a);
+    const unsigned sign = (unsigned)(u >> 63) << 31;
+    const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((u >> 29) & 0x7fffffu));
+    const float scale = __uint_as_float((unsigned)(e - 1023 - 52 + 127) << 23);
+    const float lo = __fmul_rn(__uint2float_rn((unsigned)(u & 0x1fffffffu)), scale);
+    return make_float2(hi, sign ? -lo : lo);
+}
 __device__ __forceinline__ void df_fma(float &sh, float &sl, const float2 a, const float2 x) {
     const float p = __fmul_rn(a.x, x.x);
     float e = __fmaf_rn(a.x, x.x, -p);
@@ -201,7 +217,7 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
             T *d = Xs + sb * (MR_KC * RP) + (v / (RP / VN)) * RP + (v % (RP / VN)) * VN;
             if constexpr (DF) {
                 if (xws[u]) {  // FP64 workspace values: split here
-                    const float2 h0 = df_split(rx[u].x), h1 = df_split(rx[u].y);
+                    const float2 h0 = df_split_fast(rx[u].x), h1 = df_split_fast(rx[u].y);
                     *reinterpret_cast<float4 *>(d) = make_float4(h0.x, h0.y, h1.x, h1.y);
                 } else {  // the input block is pre-split
                     *reinterpret_cast<V *>(d) = rx[u];
@@ -680,10 +696,10 @@ cudaError_t launch_mr_f32(int rp, const int64_t *roff, const int64_t *blob, cons
                                             st);
 }
 
-// b[i] = (hi, lo) FP32 pair of a[i] (df_split), for the double-FP32 product
+// b[i] = (hi, lo) FP32 pair of a[i] (df_split_fast), for the double-FP32 product
 __global__ void mr_split_kernel(const double *__restrict__ a, float2 *__restrict__ b, int64_t n) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-        b[e] = df_split(a[e]);
+        b[e] = df_split_fast(a[e]);
 }
 cudaError_t launch_mr_split(const double *a, void *b, int64_t n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
