@@ -2229,11 +2229,11 @@ int gmres_batch_run_t(h2w_handle *h, const double *bi, double *xi, int rp, int n
     const int kind = F32 ? 2 : 1;
     cudaStream_t st = h->stream;
     CK(cudaMemcpyAsync(g.tolp, &tol, 8, cudaMemcpyHostToDevice, st));  // read by the Givens step
-    CK(gmb_norms(g, bi, g.normb, 1, st));
     if (x0_zero) {
-        CK(gmb_start(g, bi, nullptr, tol, st));
+        CK(gmb_start(g, bi, nullptr, tol, st));  // also sets normb = ||bi||
     } else {
         if (F32) throw ApiError(H2W_ERR_ARG, "batched GMRES: the FP32 basis starts from x0 = 0");
+        CK(gmb_norms(g, bi, g.normb, 1, st));
         if (h->m_ri.n < (size_t)h->tree.N * rp) h->m_ri.alloc((size_t)h->tree.N * MR_MAX);
         run_matvec_multi(h, prec, rp, xi, h->m_ri.p, st);
         CK(gmb_start(g, bi, h->m_ri.p, tol, st));

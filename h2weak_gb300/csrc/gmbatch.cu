@@ -370,12 +370,14 @@ __global__ void gmb_colnorm_fin(GmbT<T> g, double *out, int zero_to_one) {
     const double s = sqrt(gmb_sum_parts(g, 0, red));
     if (threadIdx.x < g.rp) out[threadIdx.x] = (zero_to_one && s == 0.0) ? 1.0 : s;
 }
-// beta = ||w|| (hsum); V[:, 0] = vcur = w / beta; s = beta e1; per-column state
+// beta = ||w|| (hsum); V[:, 0] = vcur = w / beta; s = beta e1; per-column state.
+// set_normb (x0 = 0, where w = b): ||b|| = beta (a zero norm becomes 1)
 template <class T>
-__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_start_fin(GmbT<T> g, double tol) {
+__global__ void __launch_bounds__(GMB_THREADS, 3) gmb_start_fin(GmbT<T> g, double tol, int set_normb) {
     const int rp = g.rp, c = threadIdx.x % rp, rl = threadIdx.x / rp, RL = GMB_THREADS / rp;
     const double beta = sqrt(g.hsum[c]);
     if (blockIdx.x == 0 && rl == 0) {
+        if (set_normb) g.normb[c] = beta == 0.0 ? 1.0 : beta;
         double *cs = g.cs + (size_t)c * (g.m + 1), *sn = g.sn + (size_t)c * (g.m + 1), *s = g.s + (size_t)c * (g.m + 1);
         for (int k = 0; k <= g.m; ++k) { s[k] = 0.0; cs[k] = 0.0; sn[k] = 0.0; }
         s[0] = beta;
@@ -501,7 +503,7 @@ template <class T>
 cudaError_t gmb_start(const GmbT<T> &g, const double *b, const double *Ax, double tol, cudaStream_t st) {
     gmb_resid<T><<<g.nblk, GMB_THREADS, 0, st>>>(g, b, Ax);
     gmb_reduce<T><<<1, GMB_RED, 0, st>>>(g, 0);
-    gmb_start_fin<T><<<g.nblk, GMB_THREADS, 0, st>>>(g, tol);
+    gmb_start_fin<T><<<g.nblk, GMB_THREADS, 0, st>>>(g, tol, Ax == nullptr ? 1 : 0);
     count_launch(3);
     return cudaGetLastError();
 }

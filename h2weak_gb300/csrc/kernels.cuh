@@ -296,6 +296,7 @@ struct GmbT {
 using GmresBatch = GmbT<double>;
 template <class T>
 cudaError_t gmb_norms(const GmbT<T> &g, const double *v, double *out, int zero_to_one, cudaStream_t st);
+// w = b - Ax (Ax NULL: w = b, and normb = ||b|| is set here), V[:, 0], rotations, state
 template <class T>
 cudaError_t gmb_start(const GmbT<T> &g, const double *b, const double *Ax, double tol, cudaStream_t st);
 template <class T>
