@@ -31,11 +31,11 @@ sys.path.insert(0, ROOT)
 METRIC = "GMRES time-to-1e-10 & matvec HBM GB/s: mixed+batched+learned vs plain FP64 GPU"
 
 WORKLOADS = {
-    # configs[1]: 2D H2* integral equation, 256^2 grid, nmax 64, NCA tol 1e-10
+    # the workload the metric is quoted on: 2D H2* integral equation, 256^2 grid, nmax 64, NCA tol 1e-10
     "2d_ie_65536": dict(dim=2, form=0, choice=0, tol=10, grid=256, leaf=8, gtol=10,
                         desc="2D H2* IE (choice 0), N=65536 (256^2 grid on [-1,1]^2), nmax=64, NCA tol 1e-10, "
                              "GMRES to 1e-10"),
-    # configs[0]: 1D H2* (HSS) RBF, N=32768, nmax 64
+    # the CPU-sized case: 1D H2* (HSS) RBF, N=32768, nmax 64
     "1d_rbf_32768": dict(dim=1, form=0, choice=1, tol=10, grid=32768, leaf=64, gtol=10,
                          desc="1D H2* RBF (choice 1), N=32768 grid on [-1,1], nmax=64, NCA tol 1e-10, GMRES to 1e-10"),
 }
