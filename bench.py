@@ -371,6 +371,8 @@ def main():
     fp32_nominal = 152 * 128 * 2 * 2.07e9
     ops_per_term = {"fp32": 2.0, "df64": 12.0, "fp64": 2.0}[top]
     achieved_ops = ops_per_term * entries * R / (tk["us"] / 1e6)
+    plan = op.plan_stats()
+    plan["padding_overhead"] = plan["multiplied"] / plan["entries"] - 1.0 if plan["entries"] else None
     roof = {"bound": "hbm", "achieved": tk["gbs"], "peak": peak, "unit": "GB/s", "frac": tk["gbs"] / peak,
             "traffic": ncu_traffic.get(top) if args.workload == "2d_ie_65536" and R == 64 else None,
             "compute": {"pipe": "fp64" if top == "fp64" else "fp32",
@@ -378,8 +380,11 @@ def main():
                         "achieved_tops": achieved_ops / 1e12,
                         "nominal_fp32_tops": fp32_nominal / 1e12,
                         "frac_of_nominal": achieved_ops / fp32_nominal if top != "fp64" else None,
-                        "note": "each operator element feeds R FMAs: the pipe, not HBM, bounds this kernel"},
-            "kernel": "mr_coop_kernel<%s, %d> (one cooperative launch = one %d-vector matvec)" % (ctype, rp, R),
+                        "note": "each operator element feeds R FMAs: the pipe, not HBM, bounds this kernel",
+                        # entries multiplied per column with the kernel's row and column padding
+                        "plan": plan},
+            "kernel": "%s<%s, %d> (one cooperative launch = one %d-vector matvec)" % (
+                "mr_flow_kernel" if op.get_option(hw.OPT_DATAFLOW) else "mr_coop_kernel", ctype, rp, R),
             "bytes_per_launch": tk["bytes"], "launch_us": tk["us"], "launches": tk["launches"],
             "share_of_matvec_time": tk["ms"] / tot if tot else None,
             "peak_kind": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured" else peak_kind,

@@ -93,6 +93,7 @@ def lib():
         "h2w_dense_matvec": [P, P, P, I64, I64, I],
         "h2w_profile": [P, I],
         "h2w_profile_multi": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(D)],
+        "h2w_plan_stats": [P, P, I],
         "h2w_set_option": [P, I, I64],
         "h2w_learn_record": [P, I],
         "h2w_learn_data": [P, P, P, ctypes.POINTER(I64)],
@@ -281,6 +282,14 @@ class H2Operator:
         la, ms, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
         self._ck(lib().h2w_profile_multi(self.h, precision, ctypes.byref(la), ctypes.byref(ms), ctypes.byref(by)))
         return la.value, ms.value, by.value
+
+    def plan_stats(self):
+        """Multi-vector plan: targets, panels, operator entries per column, entries
+        the kernel multiplies per column (with its row and column padding),
+        atomically accumulated targets, entries spanned by the 64-row tiles."""
+        st = np.zeros(6, dtype=np.int64)
+        self._ck(lib().h2w_plan_stats(self.h, _ptr(st), 6))
+        return dict(zip(("targets", "panels", "entries", "multiplied", "atomic_targets", "tile_span"), st.tolist()))
 
     def profile(self, enable):
         self._ck(lib().h2w_profile(self.h, 1 if enable else 0))

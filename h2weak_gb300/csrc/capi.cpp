@@ -159,6 +159,10 @@ struct h2w_handle {
     DBuf<int32_t> d_sdep0, d_sdep, d_scidx, d_sctr;  // the same for the single-vector stream
     DBuf<int64_t> d_scoff;
     int64_t mflow_edges = 0;
+    // multi-vector plan: targets, panels, operator entries per column, entries
+    // the kernel multiplies (rows to warp granularity, each panel's columns to
+    // chunks), atomically accumulated targets, entries spanned by the row tiles
+    int64_t mstats[6] = {0, 0, 0, 0, 0, 0};
     // graph-captured Arnoldi loops (a while node whose body is one step)
     struct LoopGraph {
         int kind, prec, m, rp, nrhs;
@@ -1024,9 +1028,31 @@ struct PlanBuilder {
             }
             return;
         }
-        // column split: one sub-target per chunk of <= xw_cap columns, atomically accumulated
+        // column split, atomically accumulated sub-targets: whole panels in
+        // groups of <= xw_cap gathered columns (as many groups as the width
+        // needs, filled evenly), panels wider than xw_cap in chunks of xw_cap
         if (flags & T_SCATTER) fused = false;
+        int64_t narrow = 0;
+        for (auto &p : panels)
+            if (pad4(p.w) <= xw_cap) narrow += pad4(p.w);
+        if (narrow > 0) {
+            const int64_t ng = (narrow + xw_cap - 1) / xw_cap, share = (narrow + ng - 1) / ng;
+            std::vector<PanelSpec> grp;
+            int64_t gw = 0;
+            for (auto &p : panels) {
+                if (pad4(p.w) > xw_cap) continue;
+                if (!grp.empty() && (gw + pad4(p.w) > xw_cap || gw >= share)) {
+                    split(dst, nrows, T_ATOMIC, grp);
+                    grp.clear();
+                    gw = 0;
+                }
+                grp.push_back(p);
+                gw += pad4(p.w);
+            }
+            if (!grp.empty()) split(dst, nrows, T_ATOMIC, grp);
+        }
         for (auto &p : panels) {
+            if (pad4(p.w) <= xw_cap) continue;
             for (int64_t c0 = 0; c0 < p.w; c0 += xw_cap) {
                 int64_t c1 = std::min<int64_t>(p.w, c0 + xw_cap);
                 PanelSpec q;
@@ -1336,6 +1362,26 @@ void realize_multi(h2w_handle *h, int64_t cap) {
     assign_phases(h, pb, h->nph_total, h->mphases, h->fused_scatter_m);
     validate_plan(pb, h, h->mphases);
     pack_records(pb, h->mphases, roff, blob, pstart);
+    {
+        const int64_t mt = 64, kc = 32, wr = 8;  // the kernel's row tile, column chunk and rows per warp
+        int64_t *ms = h->mstats;
+        std::fill(ms, ms + 6, int64_t(0));
+        ms[0] = (int64_t)pb.T.size();
+        for (const Target &t : pb.T) {
+            const int64_t rows = (int64_t)t.nrows / mt * mt + ((int64_t)t.nrows % mt + wr - 1) / wr * wr;
+            int64_t w = 0, chunked = 0;
+            for (int32_t q = t.p0; q < t.p1; ++q) {
+                const Panel &p = pb.P[(size_t)q];
+                w += p.w;
+                chunked += ((int64_t)p.w + kc - 1) / kc * kc;
+            }
+            ms[1] += t.p1 - t.p0;
+            ms[2] += (int64_t)t.nrows * w;
+            ms[3] += rows * chunked;
+            ms[4] += (t.flags & T_ATOMIC) ? 1 : 0;
+            ms[5] += ((int64_t)t.nrows + mt - 1) / mt * mt * chunked;
+        }
+    }
     {
         std::vector<int32_t> cnt, cidx;
         std::vector<int64_t> coff;
@@ -3355,6 +3401,7 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
         dx = xp.p;
         double normb = dnorm(h, db);
         if (normb == 0.0) normb = 1;
+        const bool x0_zero = dnorm(h, dx) == 0.0;
         *inner_total = 0;
         *outer_iters = 0;
         int rc = H2W_ERR_NOT_CONVERGED;
@@ -3370,6 +3417,9 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
                 run_matvec_f32(h, d.p, h->s_t.p, st, true);
                 CK(vec_axpby(1.0, r.p, -1.0, h->s_t.p, r.p, N, st));
                 drift += add;
+            } else if (o == 0 && x0_zero) {  // r = b without a product
+                CK(cudaMemcpyAsync(r.p, db, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+                drift = HUGE_VAL;
             } else {
                 if (o == 0) run_matvec_f32(h, dx, r.p, st, true);
                 else run_matvec_f64(h, dx, r.p, st, true);
@@ -3451,6 +3501,13 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
             std::vector<double> ir((size_t)rp), nd((size_t)rp);
             std::vector<double> drift((size_t)rp, HUGE_VAL);  // error bound of r since the last accurate residual
             bool above_floor = false;  // every column's accurate-residual error far below its tolerance
+            // a zero start block (the usual x0) has r = b without a product
+            CK(gmb_norms(g, xi, h->m_dn.p, 0, st));
+            CK(cudaMemcpyAsync(nd.data(), h->m_dn.p, (size_t)rp * 8, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            bool x0_zero = true;
+            for (int c = 0; c < rp; ++c)
+                if (nd[(size_t)c] != 0.0) x0_zero = false;
             const double eta = h->ir_update ? fp32_error_multi(h, g, rp, st) : 0.0;
             bool ok = false;
             for (int o = 0; o <= max_outer; ++o) {
@@ -3483,6 +3540,8 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
                     run_matvec_multi(h, H2W_PREC_FP32, rp, h->m_di.p, h->m_ti.p, st);
                     CK(vec_axpby(1.0, h->m_ri.p, -1.0, h->m_ti.p, h->m_ri.p, (int64_t)len, st));
                     for (int c = 0; c < nc; ++c) drift[(size_t)c] += IR_UPDATE_SAFETY * eta * nd[(size_t)c];
+                } else if (o == 0 && x0_zero) {
+                    CK(cudaMemcpyAsync(h->m_ri.p, bi, len * 8, cudaMemcpyDeviceToDevice, st));
                 } else {
                     run_matvec_multi(h, o == 0 ? H2W_PREC_FP32 : h->ir_resid_prec, rp, xi, h->m_ri.p, st);
                     CK(vec_axpby(1.0, bi, -1.0, h->m_ri.p, h->m_ri.p, (int64_t)len, st));
@@ -4042,6 +4101,15 @@ int h2w_profile_multi(h2w_handle *h, int precision, int64_t *launches, double *m
             by += (double)h->op_bytes_read * w + (double)h->tree.N * r.rp * (w + 8.0);
         }
         *bytes = *launches ? by / (double)*launches : 0.0;
+        return H2W_OK;
+    });
+}
+
+int h2w_plan_stats(h2w_handle *h, int64_t *stats, int n) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!stats || n < 1 || n > 6) throw ApiError(H2W_ERR_ARG, "bad plan stats arguments");
+        std::copy(h->mstats, h->mstats + n, stats);
         return H2W_OK;
     });
 }

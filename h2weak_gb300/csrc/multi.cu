@@ -116,6 +116,11 @@ __device__ __forceinline__ void df_fma(float &sh, float &sl, const float2 a, con
     sh = s;
     sl = __fadd_rn(sl, __fadd_rn(t, e));
 }
+// k-parts of a row tile: a tile of at most 32 (16) rows leaves half (three
+// quarters) of the 16 row groups without rows, so the row groups split each
+// chunk's columns into 2 (4) parts instead, summed through shared memory
+// after the last chunk
+__device__ __forceinline__ int mr_kparts(int rows) { return rows > 32 ? 1 : (rows > 16 ? 2 : 4); }
 __device__ __forceinline__ void df_get4(float2 *o, const float2 *p) {
     const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
     o[0] = make_float2(a.x, a.y); o[1] = make_float2(a.z, a.w);
@@ -242,7 +247,9 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
         // Two staging buffers: chunk i is multiplied from buffer i&1 while the
         // registers already hold chunk i+1, which then goes to the other buffer;
         // one barrier per chunk. Warps whose rows are all past the target's
-        // last row skip the multiply.
+        // last row skip the multiply (the SM's other CTA keeps the pipes busy:
+        // this kernel is issue-bound, and splitting a short tile's chunks over
+        // the idle warps, as the FP32 kernel does, measured no faster).
         int q = 0, c0 = 0, sb = 0;
         if (np > 0) {
             load(0, 0, rt0);
@@ -419,7 +426,10 @@ __device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int
         advance(q2, c02);
         issue(q0, c00, rt0, 0);
         issue(q1, c01, rt0, 1);
-        const bool active = rt0 + ty * 4 < nrows;
+        // row group tyr of k-part kp: rows rt0 + 4 tyr .. + 3, columns kp kn .. + kn of each chunk
+        const int S = mr_kparts(nrows - rt0), G = 16 / S, kn = MR_KC / S;
+        const int tyr = ty % G, kp = ty / G;
+        const bool active = rt0 + tyr * 4 < nrows;
         int sb = 0;
         while (q0 < np) {
             mr_cp_wait<1>();   // this thread's copies of chunk q0 have landed
@@ -429,9 +439,10 @@ __device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int
                 const float *Ab = As + sb * (MR_KC * MR_MT);
                 const float *Xb = Xs + sb * (MR_KC * RP);
 #pragma unroll 8
-                for (int k = 0; k < MR_KC; ++k) {
+                for (int kk = 0; kk < kn; ++kk) {
+                    const int k = kp * kn + kk;
                     float a4[4], x4[4];
-                    mr_get4(a4, Ab + k * MR_MT + ty * 4);
+                    mr_get4(a4, Ab + k * MR_MT + tyr * 4);
                     mr_get4(x4, Xb + k * RP + tx * 4);
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
@@ -447,10 +458,27 @@ __device__ __forceinline__ void mr_target_async(char *smem, int64_t t, const int
             sb = sb + 1 == MR_NSA ? 0 : sb + 1;
         }
         mr_cp_wait<0>();
+        if (S > 1) {  // k-parts 1 .. S-1 add into part 0 through the staging buffers
+            __syncthreads();  // every group is done with the last chunk's buffer
+            if (kp > 0 && active) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) As[(((kp - 1) * G + tyr) * 4 + i) * RP + tx * 4 + j] = acc[i][j];
+            }
+            __syncthreads();
+            if (kp == 0 && active) {
+                for (int p = 1; p < S; ++p)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] += As[(((p - 1) * G + tyr) * 4 + i) * RP + tx * 4 + j];
+            }
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int r = rt0 + ty * 4 + i;
-            if (r >= nrows) continue;
+            const int r = rt0 + tyr * 4 + i;
+            if (kp > 0 || r >= nrows) continue;
             const int64_t d = (dst + r) * RP + tx * 4;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {

@@ -107,6 +107,8 @@ def main(argv=None):
     out["ms_per_rep"] = (time.time() - t0) / max(a.reps, 1) * 1e3
     if res is not None:
         out["result"] = [float(np.max(r)) if hasattr(r, "tolist") else r for r in res]
+    if R > 1:
+        out["plan"] = op.plan_stats()
     print(json.dumps(out), flush=True)
 
 

@@ -315,6 +315,14 @@ int h2w_profile_phases(h2w_handle *h, int precision, int max_phases, int64_t *la
  * operator once, the input block in the kernel's precision, the FP64 result
  * block). */
 int h2w_profile_multi(h2w_handle *h, int precision, int64_t *launches, double *ms, double *bytes);
+/* Shape of the multi-vector product's plan (host-side figures, no device
+ * work): stats[0] targets, [1] operator panels, [2] operator entries read per
+ * column, [3] entries the kernel multiplies per column (rows rounded to the
+ * 8 rows of a warp, each panel's columns to 32-column chunks), [4] targets
+ * accumulated atomically (column-split block rows), [5] entries spanned by
+ * the kernel's 64-row tiles (the share of [3] in [5] is the share of busy
+ * warps). n (1..6) entries are written. */
+int h2w_plan_stats(h2w_handle *h, int64_t *stats, int n);
 /* Kernel launches issued by this library since it was loaded. */
 int64_t h2w_launch_count(void);
 

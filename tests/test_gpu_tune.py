@@ -26,9 +26,17 @@ def test_recut_streams_same_products(gpu, case):
     Y0 = op.matvec(X)
     y0 = op.matvec(X[:, 0])
     assert op.get_option(hw.OPT_MULTI_XW) == 1024
+    st0 = op.plan_stats()
+    assert st0["entries"] == op.storage_entries()
     for cap in (256, 512, 2048, 32):
         op.set_option(hw.OPT_MULTI_XW, cap)
         assert op.get_option(hw.OPT_MULTI_XW) == cap
+        st = op.plan_stats()
+        # a re-cut moves entries between targets, never adds or drops any
+        assert st["entries"] == st0["entries"]
+        assert st["entries"] <= st["multiplied"] <= st["tile_span"]
+        if cap == 32:
+            assert st["atomic_targets"] > 0 and st["targets"] > st0["targets"]
         Y = op.matvec(X)
         for c in range(20):
             assert rel(Y[:, c], Y0[:, c]) < 1e-13, (cap, c)
