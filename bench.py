@@ -384,7 +384,8 @@ def main():
                         # entries multiplied per column with the kernel's row and column padding
                         "plan": plan},
             "kernel": "%s<%s, %d> (one cooperative launch = one %d-vector matvec)" % (
-                "mr_flow_kernel" if op.get_option(hw.OPT_DATAFLOW) else "mr_coop_kernel", ctype, rp, R),
+                ("mw_flow_kernel" if top == "fp32" and op.get_option(hw.OPT_PRODUCER_WARP) else "mr_flow_kernel")
+                if op.get_option(hw.OPT_DATAFLOW) else "mr_coop_kernel", ctype, rp, R),
             "bytes_per_launch": tk["bytes"], "launch_us": tk["us"], "launches": tk["launches"],
             "share_of_matvec_time": tk["ms"] / tot if tot else None,
             "peak_kind": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured" else peak_kind,
@@ -406,12 +407,14 @@ def main():
         "ms_per_step": ms_b / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*", "rhs_per_step": R,
-                   "solver": "batched: FP32-operator inner GMRES (FP64 Arnoldi, %d columns in lockstep, one "
-                             "multi-vector matvec per step) + iterative refinement, residuals FP32 at x0 then "
+                   "solver": "batched: FP32-operator inner GMRES (FP32 Krylov basis, FP64 Hessenberg and "
+                             "rotations, %d columns in lockstep, one multi-vector matvec per step) + iterative "
+                             "refinement, residuals FP32 at x0 then "
                              "double-FP32 on the FP64 operator, later ones updated as r - A32 d under a calibrated "
                              "error bound; CUDA-graph Arnoldi loop" % R,
-                   "autotuned": {"multi_xw": tuned_xw, "multi_mix_ms": tuned_xw_ms, "single_row_split": tuned_rs,
-                                 "single_fp32_ms": tuned_rs_ms},
+                   "autotuned": {"multi_xw": tuned_xw, "multi_mix_ms": tuned_xw_ms,
+                                 "fp32_producer_warp": op.get_option(hw.OPT_PRODUCER_WARP),
+                                 "single_row_split": tuned_rs, "single_fp32_ms": tuned_rs_ms},
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "no flush: FP64 operator %.0f MB, FP32 %.0f MB, both > 129 MB L2" %
                          (op.operator_bytes(hw.PREC_FP64) / 1e6, op.operator_bytes(hw.PREC_FP32) / 1e6)},

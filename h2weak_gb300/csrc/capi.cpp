@@ -154,6 +154,7 @@ struct h2w_handle {
     // dataflow launch of the multi-vector stream (H2W_OPT_DATAFLOW): producer counts
     // (initial and working copy) and consumer lists
     bool dataflow = true;
+    bool producer_warp = true;  // the FP32 dataflow product's warp-specialised form (H2W_OPT_PRODUCER_WARP)
     DBuf<int32_t> d_mdep0, d_mdep, d_mcidx;
     DBuf<int64_t> d_mcoff;
     DBuf<int32_t> d_sdep0, d_sdep, d_scidx, d_sctr;  // the same for the single-vector stream
@@ -2126,6 +2127,10 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
         const bool flow = h->dataflow && h->coop && !h->tensor;
         if (flow) CK(cudaMemcpyAsync(h->d_mdep.p, h->d_mdep0.p, h->d_mdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         mr_prof(h, prec, rp, st, [&] {
+            if (flow && h->producer_warp)
+                return launch_mw_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
+                                          h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, h->m_xf.p,
+                                          yi, h->d_err.p, st);
             if (flow)
                 return launch_mr_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
                                           h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, h->m_xf.p,
@@ -2184,6 +2189,10 @@ void run_matvec_multi_f32io(h2w_handle *h, int rp, const float *xf, float *yf, c
     const bool flow = h->dataflow && h->coop && !h->tensor;
     if (flow) CK(cudaMemcpyAsync(h->d_mdep.p, h->d_mdep0.p, h->d_mdep0.n * 4, cudaMemcpyDeviceToDevice, st));
     mr_prof(h, H2W_PREC_FP32, rp, st, [&] {
+        if (flow && h->producer_warp)
+            return launch_mw_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
+                                      h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, xf, yf, h->d_err.p,
+                                      st);
         if (flow)
             return launch_mr_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
                                       h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, xf, yf, h->d_err.p,
@@ -2594,7 +2603,10 @@ void check_device_error(h2w_handle *h) {
     if (e) {
         CK(cudaMemsetAsync(h->d_err.p, 0, 4, h->stream));
         CK(cudaMemsetAsync(h->d_bar.p, 0, 8, h->stream));
-        throw ApiError(H2W_ERR_CUDA, "matvec: a grid-barrier wait ran out (device error flag)");
+        static const char *what[] = {"", "a grid-barrier wait", "a tensor-pipeline wait", "a dependency wait",
+                                     "a stage (mbarrier or counter) wait"};
+        throw ApiError(H2W_ERR_CUDA, std::string("matvec: ") + (e >= 1 && e <= 4 ? what[e] : "a device wait") +
+                                         " ran out (device error flag " + std::to_string(e) + ")");
     }
 }
 
@@ -3622,6 +3634,14 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
                 cudaGraphDestroy(g.graph);
             }
             h->loops.clear();
+        } else if (option == H2W_OPT_PRODUCER_WARP) {
+            h->producer_warp = value != 0;
+            h->eta_multi = -1.0;
+            for (auto &g : h->loops) {  // captured steps hold the other kernel
+                cudaGraphExecDestroy(g.exec);
+                cudaGraphDestroy(g.graph);
+            }
+            h->loops.clear();
         } else if (option == H2W_OPT_TENSOR) {
             h->tensor = value != 0;
             h->eta_multi = -1.0;
@@ -3656,6 +3676,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_TENSOR) *value = h->tensor ? 1 : 0;
         else if (option == H2W_OPT_F32_BASIS) *value = h->f32_basis ? 1 : 0;
         else if (option == H2W_OPT_DATAFLOW) *value = h->dataflow ? 1 : 0;
+        else if (option == H2W_OPT_PRODUCER_WARP) *value = h->producer_warp ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });
@@ -3688,11 +3709,17 @@ int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chos
         CK(cudaEventCreate(&e0));
         CK(cudaEventCreate(&e1));
         int64_t best = multi ? h->mr_xw : h->row_split;
+        // the FP32 dataflow product's two forms (producer warp or not) are candidates too
+        const bool forms = multi && (mix || precision == H2W_PREC_FP32) && h->dataflow && h->coop && !h->tensor;
+        const bool pw0 = h->producer_warp;
+        bool best_pw = pw0;
         double bms = 1e300;
         const bool prof = h->prof;
         h->prof = false;
         try {
+            for (int f = 0; f < (forms ? 2 : 1); ++f)
             for (int64_t c : cand) {
+                h->producer_warp = forms ? f == 0 : pw0;
                 if (multi) realize_multi(h, c);
                 else realize_single(h, c);
                 auto once = [&] {
@@ -3714,9 +3741,11 @@ int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chos
                 if (ms / reps < bms) {
                     bms = ms / reps;
                     best = c;
+                    best_pw = h->producer_warp;
                 }
             }
         } catch (...) {
+            h->producer_warp = pw0;
             h->prof = prof;
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
@@ -3725,6 +3754,14 @@ int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chos
         h->prof = prof;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        if (h->producer_warp != best_pw || pw0 != best_pw) {
+            h->producer_warp = best_pw;
+            for (auto &g : h->loops) {  // captured steps hold the other kernel
+                cudaGraphExecDestroy(g.exec);
+                cudaGraphDestroy(g.graph);
+            }
+            h->loops.clear();
+        }
         if (multi) realize_multi(h, best);
         else realize_single(h, best);
         if (chosen) *chosen = best;

@@ -240,6 +240,14 @@ cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob,
 cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
                                const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
                                float *yout, int32_t *err, cudaStream_t st);
+// warp-specialised form of launch_mr_f32_flow (a producer warp streams each
+// CTA's chunks by bulk asynchronous copies; mrws.cu)
+cudaError_t launch_mw_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
+                               int32_t *rem, const int64_t *coff, const int32_t *cidx, const float *A, float *ws,
+                               const float *xin, double *yout, int32_t *err, cudaStream_t st);
+cudaError_t launch_mw_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
+                               int32_t *rem, const int64_t *coff, const int32_t *cidx, const float *A, float *ws,
+                               const float *xin, float *yout, int32_t *err, cudaStream_t st);
 // the same for the FP64 (df = false) and double-FP32 (df = true, A and xin
 // pre-split pairs as for launch_mr_df64) products
 cudaError_t launch_mr_f64_flow(int rp, bool df, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,

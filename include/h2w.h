@@ -219,9 +219,16 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 for the targets that produce the workspace rows it uses
  *                 (dependencies derived on the host from the rows each target
  *                 reads and writes) and releases its consumers; 0: phases
- *                 separated by grid barriers. */
+ *                 separated by grid barriers.
+ *  H2W_OPT_PRODUCER_WARP  1 (default): the dataflow form of the FP32
+ *                 multi-vector product splits each CTA into a producer warp
+ *                 (claims targets, waits for their producers, streams their
+ *                 chunks into a ring of shared-memory stages by bulk
+ *                 asynchronous copies) and multiplying warps; 0: every warp
+ *                 stages and multiplies its CTA's current target. */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
-       H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8 };
+       H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8,
+       H2W_OPT_PRODUCER_WARP = 9 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
@@ -294,8 +301,11 @@ int h2w_mlp_adam(float *params, const float *grads, float *m, float *v, int step
  * 2048) at `precision` (FP32, FP64 or DF64) for blocks of nrhs columns;
  * nrhs == 1: the single-vector stream's row split (4096 ... 65536) at FP32 or
  * FP64. precision H2W_TUNE_IR_MIX (nrhs > 1): the batched refinement's mix,
- * four FP32 products and one DF64 product per timed repetition. chosen /
- * best_ms (may be NULL): the kept value and its ms per repetition. */
+ * four FP32 products and one DF64 product per timed repetition. With FP32
+ * or the mix on the dataflow launch, both forms of the FP32 product
+ * (H2W_OPT_PRODUCER_WARP on and off) are candidates as well, and the faster
+ * one stays set. chosen / best_ms (may be NULL): the kept column cap or row
+ * split and its ms per repetition. */
 enum { H2W_TUNE_IR_MIX = 16 };
 int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chosen, double *best_ms);
 

@@ -47,6 +47,33 @@ def test_dataflow_product(gpu, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_producer_warp_product(gpu, case):
+    """FP32 multi-vector product of the warp-specialised dataflow kernel
+    (producer warp + bulk copies) against the kernel whose warps all stage
+    and multiply, for blocks of 7/16/32/64 columns (RP 16, 32 and 64), FP32
+    and FP64 outputs, and repeated launches."""
+    hw = gpu
+    op, _ = setup(hw, case)
+    op.assemble(hw.ASSEMBLE_NCA)
+    assert op.get_option(hw.OPT_PRODUCER_WARP) == 1
+    for k in (7, 16, 32, 64):
+        X = rhs(140 + k, op.N, k)
+        Y64 = op.matvec(X)
+        Yw = op.matvec(X, precision=hw.PREC_FP32)
+        op.set_option(hw.OPT_PRODUCER_WARP, 0)
+        Yo = op.matvec(X, precision=hw.PREC_FP32)
+        op.set_option(hw.OPT_PRODUCER_WARP, 1)
+        # the same per-target sums; split-K parts and atomics may add in another order
+        assert np.all(colerr(Yw, Yo) < 1e-6), (k, colerr(Yw, Yo).max())
+        assert np.all(colerr(Yw, Y64) < 1e-5), (k, colerr(Yw, Y64).max())
+    X = rhs(150, op.N, 64)
+    Y1 = op.matvec(X, precision=hw.PREC_FP32)
+    Y2 = op.matvec(X, precision=hw.PREC_FP32)
+    assert np.all(colerr(Y1, Y2) < 1e-6)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("graph", [1, 0])
 def test_dataflow_in_batched_mixed_solve(gpu, graph):
     hw = gpu

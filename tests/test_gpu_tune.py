@@ -27,7 +27,8 @@ def test_recut_streams_same_products(gpu, case):
     y0 = op.matvec(X[:, 0])
     assert op.get_option(hw.OPT_MULTI_XW) == 1024
     st0 = op.plan_stats()
-    assert st0["entries"] == op.storage_entries()
+    # stored panels keep their columns at 4-row strides: the plan reads at most the stored entries
+    assert 0 < st0["entries"] <= op.storage_entries()
     for cap in (256, 512, 2048, 32):
         op.set_option(hw.OPT_MULTI_XW, cap)
         assert op.get_option(hw.OPT_MULTI_XW) == cap
@@ -65,6 +66,10 @@ def test_autotune_keeps_a_candidate(gpu):
     cap, ms = op.autotune(nrhs=64, precision=hw.TUNE_IR_MIX, reps=1)
     assert cap in (256, 512, 1024, 2048) and ms > 0
     assert op.get_option(hw.OPT_MULTI_XW) == cap
+    # the FP32 product's form is a candidate too; either gives the product
+    assert op.get_option(hw.OPT_PRODUCER_WARP) in (0, 1)
+    Yf = op.matvec(X, precision=hw.PREC_FP32)
+    assert max(rel(Yf[:, c], Y0[:, c]) for c in range(64)) < 1e-5
     Y = op.matvec(X, precision=hw.PREC_DF64)
     assert max(rel(Y[:, c], Y0[:, c]) for c in range(64)) < 1e-12
     rs, ms1 = op.autotune(nrhs=1, precision=hw.PREC_FP32, reps=3)
