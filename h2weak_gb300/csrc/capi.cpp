@@ -115,6 +115,13 @@ struct h2w_handle {
     DBuf<float> d_op32;
     DBuf<int64_t> d_roff, d_blob;  // packed target records of the matvec
     DBuf<int64_t> d_roff_m, d_blob_m, d_pstart_m;  // the multi-vector stream (64-row targets)
+    // the warp-specialised FP32 product's operator copy: every (target, panel)
+    // slice contiguous at its padded height, records pointing into it, and the
+    // slices to copy (6 words each: source offset, lda, rows, width, offset, lda)
+    DBuf<float> d_op32m;
+    DBuf<int64_t> d_blob_mw, d_mslices;
+    int64_t op32m_n = 0;
+    bool op32m_ready = false;
     DBuf<int32_t> d_mctr;                           // its per-phase target counters
     std::vector<Phase> mphases;
     DBuf<double> d_ws, d_x, d_y;
@@ -1397,6 +1404,31 @@ void realize_multi(h2w_handle *h, int64_t cap) {
     h->d_roff_m.upload(roff, st);
     h->d_blob_m.upload(blob, st);
     h->d_pstart_m.upload(pstart, st);
+    {
+        // slice-contiguous copy for the warp-specialised FP32 product: each
+        // target's panel slice (its <= 64 rows of a stored block) moves to its
+        // own column-major block at leading dimension pad4(rows), so a chunk of
+        // 32 columns is one contiguous copy
+        std::vector<int64_t> bw = blob, sl;
+        int64_t off = 0;
+        for (size_t t = 0; t + 1 < roff.size(); ++t) {
+            const int64_t o = roff[t];
+            const int64_t rows = blob[(size_t)o + 1] & 0xffffffff, np = blob[(size_t)o + 2] & 0xffffffff;
+            const int64_t ld = pad4(rows);
+            for (int64_t q = 0; q < np; ++q) {
+                const size_t pw = (size_t)(o + 3 + 3 * q);
+                const int64_t a = blob[pw], lda = blob[pw + 1] & 0xffffffff, w = blob[pw + 1] >> 32;
+                sl.insert(sl.end(), {a, lda, rows, w, off, ld});
+                bw[pw] = off;
+                bw[pw + 1] = ld | (w << 32);
+                off += ld * w;
+            }
+        }
+        h->d_blob_mw.upload(bw, st);
+        h->d_mslices.upload(sl, st);
+        h->op32m_n = off;
+        h->op32m_ready = false;
+    }
     h->d_mctr.alloc(std::max<size_t>(h->mphases.size(), 1));
     h->ph_t0.clear();
     h->ph_t1.clear();
@@ -1834,6 +1866,8 @@ void build_plan(h2w_handle *h) {
     h->d_op32.reset();
     h->d_opdf.reset();
     h->d_ws32.reset();
+    h->d_op32m.reset();
+    h->op32m_ready = false;
     h->eta_multi = h->eta_single = -1.0;
 }
 
@@ -1976,6 +2010,16 @@ void ensure_f32(h2w_handle *h) {
     CK(launch_convert_f32(h->d_op.p, h->d_op32.p, h->op_n, h->stream));
     h->d_ws32.alloc((size_t)h->ws_n);
     CK(cudaStreamSynchronize(h->stream));
+}
+
+// the slice-contiguous FP32 operator of the warp-specialised product
+void ensure_f32m(h2w_handle *h) {
+    ensure_f32(h);
+    if (h->op32m_ready) return;
+    h->d_op32m.reset();
+    h->d_op32m.alloc((size_t)std::max<int64_t>(h->op32m_n, 4));
+    CK(launch_slice_copy_f32(h->d_op32.p, h->d_mslices.p, (int64_t)h->d_mslices.n / 6, h->d_op32m.p, h->stream));
+    h->op32m_ready = true;
 }
 
 // FP32 operator and workspace; x and y stay FP64 in original order (the
@@ -2125,11 +2169,12 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
         if (h->m_xf.n < nx) h->m_xf.alloc(nx);
         CK(vec_f64_to_f32(xi, h->m_xf.p, (int64_t)nx, st));
         const bool flow = h->dataflow && h->coop && !h->tensor;
+        if (flow && h->producer_warp) ensure_f32m(h);
         if (flow) CK(cudaMemcpyAsync(h->d_mdep.p, h->d_mdep0.p, h->d_mdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         mr_prof(h, prec, rp, st, [&] {
             if (flow && h->producer_warp)
-                return launch_mw_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
-                                          h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, h->m_xf.p,
+                return launch_mw_f32_flow(rp, h->d_roff_m.p, h->d_blob_mw.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
+                                          h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32m.p, h->m_wsf.p, h->m_xf.p,
                                           yi, h->d_err.p, st);
             if (flow)
                 return launch_mr_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
@@ -2187,12 +2232,13 @@ void run_matvec_multi_f32io(h2w_handle *h, int rp, const float *xf, float *yf, c
     if (h->m_wsf.n < wsz) h->m_wsf.alloc(wsz);
     CK(cudaMemsetAsync(h->m_wsf.p, 0, wsz * 4, st));
     const bool flow = h->dataflow && h->coop && !h->tensor;
+    if (flow && h->producer_warp) ensure_f32m(h);
     if (flow) CK(cudaMemcpyAsync(h->d_mdep.p, h->d_mdep0.p, h->d_mdep0.n * 4, cudaMemcpyDeviceToDevice, st));
     mr_prof(h, H2W_PREC_FP32, rp, st, [&] {
         if (flow && h->producer_warp)
-            return launch_mw_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
-                                      h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, xf, yf, h->d_err.p,
-                                      st);
+            return launch_mw_f32_flow(rp, h->d_roff_m.p, h->d_blob_mw.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
+                                      h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32m.p, h->m_wsf.p, xf, yf,
+                                      h->d_err.p, st);
         if (flow)
             return launch_mr_f32_flow(rp, h->d_roff_m.p, h->d_blob_m.p, (int64_t)h->d_roff_m.n - 1, h->d_mctr.p,
                                       h->d_mdep.p, h->d_mcoff.p, h->d_mcidx.p, h->d_op32.p, h->m_wsf.p, xf, yf, h->d_err.p,

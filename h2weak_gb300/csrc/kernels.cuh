@@ -240,8 +240,13 @@ cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob,
 cudaError_t launch_mr_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
                                const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const float *xin,
                                float *yout, int32_t *err, cudaStream_t st);
+// the slices of an FP32 operator, 6 words each (source offset, leading
+// dimension, rows, columns, destination offset, destination leading
+// dimension), copied to dst with zeros in the destination's padding rows
+cudaError_t launch_slice_copy_f32(const float *src, const int64_t *slices, int64_t n, float *dst, cudaStream_t st);
 // warp-specialised form of launch_mr_f32_flow (a producer warp streams each
-// CTA's chunks by bulk asynchronous copies; mrws.cu)
+// CTA's chunks by bulk asynchronous copies; mrws.cu); A and blob: the
+// slice-contiguous operator copy and its records
 cudaError_t launch_mw_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
                                int32_t *rem, const int64_t *coff, const int32_t *cidx, const float *A, float *ws,
                                const float *xin, double *yout, int32_t *err, cudaStream_t st);

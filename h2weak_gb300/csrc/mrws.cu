@@ -24,11 +24,13 @@
 // the record reads, dependency waits and copy latency of the next target
 // overlap the current target's multiply, epilogue and release.
 //
-// Copies: an operator column is 4 * pad4(rows) bytes at a 16-byte aligned
-// address (the plan's 16-byte-row rule: panel offsets, leading dimensions
-// and tile starts are multiples of 4 elements); panels that break the rule,
-// and gathered columns without a source, are written by the producer's own
-// stores. Rows past a tile's last row and columns past a chunk's width are
+// Copies: the kernel reads a slice-contiguous copy of the FP32 operator
+// (each target's panel slice stored on its own at leading dimension
+// pad4(rows), launch_slice_copy_f32), so a chunk is one copy of
+// 4 * pad4(rows) * 32 bytes at a 16-byte aligned address; given any other
+// layout it falls back to one copy per column (tiles of a target of more
+// than 64 rows) or, for panels off the 16-byte rule, the producer's own
+// stores, as it does for gathered columns without a source. Rows past a tile's last row and columns past a chunk's width are
 // never used: a row's result reads only its own operator row, and the
 // consumers' column loop stops at the chunk width.
 //
@@ -445,6 +447,23 @@ cudaError_t mw_dispatch(int rp, const int64_t *roff, const int64_t *blob, int64_
 }
 
 }  // namespace
+
+// one CTA per slice
+__global__ void slice_copy_kernel(const float *__restrict__ src, const int64_t *__restrict__ sl, float *dst) {
+    const int64_t *d = sl + 6 * (int64_t)blockIdx.x;
+    const int64_t a = d[0], lda = d[1], rows = d[2], w = d[3], o = d[4], ld = d[5];
+    for (int64_t e = threadIdx.x; e < ld * w; e += blockDim.x) {
+        const int64_t c = e / ld, r = e - c * ld;
+        dst[o + e] = r < rows ? src[a + c * lda + r] : 0.f;
+    }
+}
+cudaError_t launch_slice_copy_f32(const float *src, const int64_t *slices, int64_t n, float *dst, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (n > (int64_t)INT32_MAX) return cudaErrorInvalidValue;
+    slice_copy_kernel<<<(unsigned)n, 256, 0, st>>>(src, slices, dst);
+    count_launch();
+    return cudaGetLastError();
+}
 
 cudaError_t launch_mw_f32_flow(int rp, const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr,
                                int32_t *rem, const int64_t *coff, const int32_t *cidx, const float *A, float *ws,
