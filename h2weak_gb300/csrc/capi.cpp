@@ -1371,6 +1371,28 @@ void realize_multi(h2w_handle *h, int64_t cap) {
     validate_plan(pb, h, h->mphases);
     pack_records(pb, h->mphases, roff, blob, pstart);
     {
+        // An accumulating target that is the first (in stored order) to write
+        // its rows adds onto the zeroed workspace: it becomes an overwrite and
+        // its epilogue reads nothing. Scatter targets write the result, not the
+        // workspace; atomic parts of a column-split row keep their atomics.
+        std::vector<uint8_t> written((size_t)h->ws_n, 0);
+        for (size_t t = 0; t + 1 < roff.size(); ++t) {
+            const size_t o = (size_t)roff[t];
+            const int64_t dst = blob[o], nrows = blob[o + 1] & 0xffffffff;
+            int64_t flags = blob[o + 1] >> 32;
+            if ((flags & T_ACCUM) && !(flags & T_ATOMIC)) {
+                bool any = false;
+                for (int64_t r = dst; r < dst + nrows && !any; ++r) any = written[(size_t)r] != 0;
+                if (!any) {
+                    flags &= ~(int64_t)T_ACCUM;
+                    blob[o + 1] = nrows | (flags << 32);
+                }
+            }
+            if (!(flags & T_SCATTER))
+                for (int64_t r = dst; r < dst + nrows; ++r) written[(size_t)r] = 1;
+        }
+    }
+    {
         const int64_t mt = 64, kc = 32, wr = 8;  // the kernel's row tile, column chunk and rows per warp
         int64_t *ms = h->mstats;
         std::fill(ms, ms + 6, int64_t(0));
