@@ -1232,6 +1232,30 @@ void pack_records(const PlanBuilder &pb, const std::vector<Phase> &phases, std::
     pstart.push_back(phases.empty() ? 0 : phases.back().t1);
 }
 
+// An accumulating target that is the first (in stored order, the order of
+// the dependencies and phases) to write its rows adds onto the zeroed
+// workspace: it becomes an overwrite and its epilogue reads nothing. Scatter
+// targets write the result, not the workspace; atomic parts of a
+// column-split row keep their atomics.
+void first_writers_overwrite(const std::vector<int64_t> &roff, std::vector<int64_t> &blob, int64_t ws_n) {
+    std::vector<uint8_t> written((size_t)ws_n, 0);
+    for (size_t t = 0; t + 1 < roff.size(); ++t) {
+        const size_t o = (size_t)roff[t];
+        const int64_t dst = blob[o], nrows = blob[o + 1] & 0xffffffff;
+        int64_t flags = blob[o + 1] >> 32;
+        if ((flags & T_ACCUM) && !(flags & T_ATOMIC)) {
+            bool any = false;
+            for (int64_t r = dst; r < dst + nrows && !any; ++r) any = written[(size_t)r] != 0;
+            if (!any) {
+                flags &= ~(int64_t)T_ACCUM;
+                blob[o + 1] = nrows | (flags << 32);
+            }
+        }
+        if (!(flags & T_SCATTER))
+            for (int64_t r = dst; r < dst + nrows; ++r) written[(size_t)r] = 1;
+    }
+}
+
 // (Re)cut the single-vector target stream: row chunks of max(4,
 // row_split / width) rows, column splits past XW_CAP; per-phase byte counts
 // Producer -> consumer dependencies between the targets of a stream, over the
@@ -1335,6 +1359,7 @@ void realize_single(h2w_handle *h, int64_t row_split) {
     }
     validate_plan(pb, h, h->phases);
     pack_records(pb, h->phases, roff, blob, pstart);
+    first_writers_overwrite(roff, blob, h->ws_n);
     {
         std::vector<int32_t> cnt, cidx;
         std::vector<int64_t> coff;
@@ -1370,28 +1395,8 @@ void realize_multi(h2w_handle *h, int64_t cap) {
     assign_phases(h, pb, h->nph_total, h->mphases, h->fused_scatter_m);
     validate_plan(pb, h, h->mphases);
     pack_records(pb, h->mphases, roff, blob, pstart);
-    {
-        // An accumulating target that is the first (in stored order) to write
-        // its rows adds onto the zeroed workspace: it becomes an overwrite and
-        // its epilogue reads nothing. Scatter targets write the result, not the
-        // workspace; atomic parts of a column-split row keep their atomics.
-        std::vector<uint8_t> written((size_t)h->ws_n, 0);
-        for (size_t t = 0; t + 1 < roff.size(); ++t) {
-            const size_t o = (size_t)roff[t];
-            const int64_t dst = blob[o], nrows = blob[o + 1] & 0xffffffff;
-            int64_t flags = blob[o + 1] >> 32;
-            if ((flags & T_ACCUM) && !(flags & T_ATOMIC)) {
-                bool any = false;
-                for (int64_t r = dst; r < dst + nrows && !any; ++r) any = written[(size_t)r] != 0;
-                if (!any) {
-                    flags &= ~(int64_t)T_ACCUM;
-                    blob[o + 1] = nrows | (flags << 32);
-                }
-            }
-            if (!(flags & T_SCATTER))
-                for (int64_t r = dst; r < dst + nrows; ++r) written[(size_t)r] = 1;
-        }
-    }
+    if (roff.size() != pb.T.size() + 1) throw ApiError(H2W_ERR_STATE, "internal: multi-vector records not packed");
+    first_writers_overwrite(roff, blob, h->ws_n);
     {
         const int64_t mt = 64, kc = 32, wr = 8;  // the kernel's row tile, column chunk and rows per warp
         int64_t *ms = h->mstats;
@@ -2041,6 +2046,7 @@ void ensure_f32m(h2w_handle *h) {
     h->d_op32m.reset();
     h->d_op32m.alloc((size_t)std::max<int64_t>(h->op32m_n, 4));
     CK(launch_slice_copy_f32(h->d_op32.p, h->d_mslices.p, (int64_t)h->d_mslices.n / 6, h->d_op32m.p, h->stream));
+    CK(cudaStreamSynchronize(h->stream));  // products may run on a caller's stream
     h->op32m_ready = true;
 }
 
@@ -3877,6 +3883,7 @@ int h2w_batch_create(h2w_handle *const *handles, int n, h2w_batch **out) {
             for (Target &t : pb.T) t.flags |= (p << 8);
             std::vector<int64_t> ro, bl, ps;
             pack_records(pb, ph, ro, bl, ps);
+            first_writers_overwrite(ro, bl, h->ws_n);
             nph[(size_t)p] = ph.size();
             maxph = std::max(maxph, ph.size());
             for (size_t j = 0; j < ph.size(); ++j)
