@@ -266,8 +266,10 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
             const T *Xb = Xs + sb * (MR_KC * RP);
             if (!active) {
             } else if constexpr (DF) {
+                // columns past the panel's width are zero: the 12-operation terms stop at the width
+                const int kw = min(MR_KC, (int)(pan[3 * q + 1] >> 32) - c0);
 #pragma unroll 4
-                for (int k = 0; k < MR_KC; ++k) {
+                for (int k = 0; k < kw; ++k) {
                     float2 a4[4], x4[4];
                     df_get4(a4, reinterpret_cast<const float2 *>(Ab) + k * MR_MT + ty * 4);
                     df_get4(x4, reinterpret_cast<const float2 *>(Xb) + k * RP + tx * 4);
@@ -277,8 +279,9 @@ __device__ __forceinline__ void mr_target(char *smem, int64_t t, const int64_t *
                         for (int j = 0; j < 4; ++j) df_fma(ah[i][j], al[i][j], a4[i], x4[j]);
                 }
             } else {
+                const int kw = min(MR_KC, (int)(pan[3 * q + 1] >> 32) - c0);
 #pragma unroll 8
-                for (int k = 0; k < MR_KC; ++k) {
+                for (int k = 0; k < kw; ++k) {
                     T a4[4], x4[4];
                     mr_get4(a4, Ab + k * MR_MT + ty * 4);
                     mr_get4(x4, Xb + k * RP + tx * 4);
