@@ -8,9 +8,8 @@
 //    (32 operator columns x the tile's rows, and the 32 gathered source rows
 //    of RP vectors) into a ring of MW_NS shared-memory stages with bulk
 //    asynchronous copies (cp.async.bulk, completing on the stage's "full"
-//    mbarrier): one copy for a chunk whose columns are contiguous in the
-//    operator (a single-tile target stored at its padded height), else one
-//    per column; one copy per run of consecutive source rows;
+//    mbarrier): one copy per operator chunk, one per run of consecutive
+//    source rows;
 //  * 4 RP consumer threads (8 warps at RP = 64) multiply each stage as it
 //    lands (4 rows x 4 vectors per thread; a tile of at most 32 or 16 rows
 //    splits the stage's columns over the otherwise idle row groups, whose
@@ -27,12 +26,13 @@
 // Copies: the kernel reads a slice-contiguous copy of the FP32 operator
 // (each target's panel slice stored on its own at leading dimension
 // pad4(rows), launch_slice_copy_f32), so a chunk is one copy of
-// 4 * pad4(rows) * 32 bytes at a 16-byte aligned address; given any other
+// 4 * pad4(rows) * 32 bytes at a 16-byte aligned address. Given any other
 // layout it falls back to one copy per column (tiles of a target of more
-// than 64 rows) or, for panels off the 16-byte rule, the producer's own
-// stores, as it does for gathered columns without a source. Rows past a tile's last row and columns past a chunk's width are
-// never used: a row's result reads only its own operator row, and the
-// consumers' column loop stops at the chunk width.
+// than 64 rows) or, for panels off the 16-byte rule, to the producer's own
+// stores, as it does for gathered columns without a source. Rows past a
+// tile's last row and columns past a chunk's width are never used: a row's
+// result reads only its own operator row, and the consumers' column loop
+// stops at the chunk width.
 //
 // Every wait is bounded: a dependency wait that runs out sets *err = 3, an
 // mbarrier wait *err = 4, and the thread carries on, so the kernel always
