@@ -112,10 +112,11 @@ __device__ __forceinline__ void mw_until(volatile int32_t *c, int32_t want, vola
     }
     __syncwarp();
 }
-// k-parts of a tile of `rows` rows: the idle row groups of a short tile take
-// a share of each chunk's columns (parts stay warp-uniform: at most 2 for RP 16)
-template <int RP> __device__ __forceinline__ int mw_kparts(int rows) {
-    return rows > 32 ? 1 : ((rows > 16 || RP == 16) ? 2 : 4);
+// log2 of the k-parts of a tile of `rows` rows: the idle row groups of a
+// short tile take a share of each chunk's columns (parts stay warp-uniform:
+// at most 2 for RP 16)
+template <int RP> __device__ __forceinline__ int mw_kparts_log2(int rows) {
+    return rows > 32 ? 0 : ((rows > 16 || RP == 16) ? 1 : 2);
 }
 
 template <int RP>
@@ -291,9 +292,9 @@ __device__ __forceinline__ void mw_consume(char *sm, const int64_t *__restrict__
         if (m.t < 0) break;
         const float *As = reinterpret_cast<const float *>(sm + s * Lay::stage);
         const float *Xs = As + MW_KC * MW_MT;
-        const int S = mw_kparts<RP>(min(MW_MT, m.nrows - m.rt0)), G = 16 / S;
-        const int tyr = ty % G, kp = ty / G;
-        const int kn = (m.kw + S - 1) / S, k0 = kp * kn, k1 = min(m.kw, k0 + kn);
+        const int ls = mw_kparts_log2<RP>(min(MW_MT, m.nrows - m.rt0)), S = 1 << ls, G = 16 >> ls;
+        const int tyr = ty & (G - 1), kp = ty >> (4 - ls);
+        const int kn = (m.kw + S - 1) >> ls, k0 = kp * kn, k1 = min(m.kw, k0 + kn);
         const bool active = m.rt0 + tyr * 4 < m.nrows;
         if (active) {
 #pragma unroll 4
@@ -311,7 +312,7 @@ __device__ __forceinline__ void mw_consume(char *sm, const int64_t *__restrict__
         if (lane == 0) mw_arrive(empty + s);
         if (!(m.last & 1)) continue;
         if (S > 1) {  // k-parts 1 .. S-1 add into part 0 through shared memory
-            const int nr = RP / (8 * S), nw = NWARP - nr;  // warps of part 0, of the other parts
+            const int nr = RP >> (3 + ls), nw = NWARP - nr;  // warps of part 0, of the other parts
             if (kp > 0) {
                 mw_until(rd, rd_want, fail, err);  // the previous short tile's partials are read
                 if (active) {
