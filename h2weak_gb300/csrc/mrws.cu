@@ -296,16 +296,22 @@ __device__ __forceinline__ void mw_consume(char *sm, const int64_t *__restrict__
         const int tyr = ty & (G - 1), kp = ty >> (4 - ls);
         const int kn = (m.kw + S - 1) >> ls, k0 = kp * kn, k1 = min(m.kw, k0 + kn);
         const bool active = m.rt0 + tyr * 4 < m.nrows;
+        auto term = [&](int k) {
+            const float4 a = *reinterpret_cast<const float4 *>(As + k * m.astride + tyr * 4);
+            const float4 x = *reinterpret_cast<const float4 *>(Xs + k * RP + tx * 4);
+            const float a4[4] = {a.x, a.y, a.z, a.w}, x4[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = __fmaf_rn(a4[i], x4[j], acc[i][j]);
+        };
         if (active) {
+            if (k1 - k0 == MW_KC) {  // a full chunk of a tall tile: compile-time trip count
+#pragma unroll 8
+                for (int k = 0; k < MW_KC; ++k) term(k);
+            } else {
 #pragma unroll 4
-            for (int k = k0; k < k1; ++k) {
-                const float4 a = *reinterpret_cast<const float4 *>(As + k * m.astride + tyr * 4);
-                const float4 x = *reinterpret_cast<const float4 *>(Xs + k * RP + tx * 4);
-                const float a4[4] = {a.x, a.y, a.z, a.w}, x4[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = __fmaf_rn(a4[i], x4[j], acc[i][j]);
+                for (int k = k0; k < k1; ++k) term(k);
             }
         }
         __syncwarp();
