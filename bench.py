@@ -363,7 +363,7 @@ def main():
     rp = 16 if R <= 16 else (32 if R <= 32 else 64)
     # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu captures of the
     # same launches on this workload: profiles/mw_flow_fp32_2d_ie_65536.md, mr_flow_df64_2d_ie_65536.md
-    ncu_traffic = {"fp32": 361.941e6 + 71.802e6, "df64": 896.444e6 + 188.591e6}
+    ncu_traffic = {"fp32": 361.970e6 + 72.415e6, "df64": 896.444e6 + 188.591e6}
     # the multi-vector kernel multiplies every packed operator entry by R vectors: one FMA per
     # term (FP32), about twelve FP32 operations per term (double-FP32); nominal FP32 peak of
     # 152 SMs x 128 lanes x 2 flop x 2.07 GHz
