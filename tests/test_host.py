@@ -47,6 +47,21 @@ def test_state_errors():
         op.build_tree()  # no points yet
     with pytest.raises(hw.H2WError):
         op.set_points(np.array([[0.0, np.nan]]))
+    with pytest.raises(hw.H2WError):
+        op.plan_stats()  # no operator, no plan
+
+
+def test_options_on_a_host_only_handle():
+    """Kernel-form options are plain handle state: set and read back without a device."""
+    op = hw.H2Operator(2, 0, 1, 8, 2, device=-1)
+    for opt in (hw.OPT_PRODUCER_WARP, hw.OPT_DATAFLOW, hw.OPT_F32_BASIS, hw.OPT_IR_UPDATE):
+        assert op.get_option(opt) == 1
+        op.set_option(opt, 0)
+        assert op.get_option(opt) == 0
+        op.set_option(opt, 1)
+        assert op.get_option(opt) == 1
+    with pytest.raises(hw.H2WError):
+        op.set_option(99, 1)
 
 
 @pytest.mark.parametrize("name", golden_names())
