@@ -129,6 +129,7 @@ struct h2w_handle {
     DBuf<int64_t> d_pstart;
     DBuf<unsigned> d_bar;
     bool coop = true;  // one cooperative launch per matvec (else one launch per phase)
+    int64_t spin_limit = 0;  // polls per grid-barrier wait of the single-vector cooperative launch (0: built-in)
     DBuf<float> d_ws32;
     std::vector<Phase> phases;
     std::vector<int64_t> ph_op, ph_vec;   // per phase: operator and vector elements moved
@@ -2013,7 +2014,7 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     } else if (h->coop) {
         prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
             return launch_coop_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op.p, h->d_ws.p, dx, dy, perm,
-                                   h->d_bar.p, h->d_err.p, st);
+                                   h->d_bar.p, h->d_err.p, st, h->spin_limit);
         });
     } else {
         for (size_t q = 0; q < h->phases.size(); ++q) {
@@ -2068,7 +2069,7 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     } else if (h->coop) {
         prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
             return launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op32.p, h->d_ws32.p, dx, dy,
-                                   perm, h->d_bar.p, h->d_err.p, st);
+                                   perm, h->d_bar.p, h->d_err.p, st, h->spin_limit);
         });
     } else {
         for (size_t q = 0; q < h->phases.size(); ++q) {
@@ -2975,6 +2976,28 @@ void require_op(h2w_handle *h) {
 // a caller-provided workspace, barrier state and error word instead of the
 // handle's: used by the allocation-free entry point (noalloc.cu). Allocates
 // nothing: the FP32 form needs the FP32 operator copy to exist already.
+// x and y must be device (or managed) memory that this handle's device can
+// address; cudaPointerGetAttributes checks that before any launch, so a host
+// pointer is refused instead of faulting the kernel. The call waits for its
+// launches and reads the error word back: a grid-barrier wait that ran out
+// (the result is then wrong) returns H2W_ERR_CUDA on this call.
+namespace {
+void require_device_vector(const h2w_handle *h, const void *p, const char *name) {
+    cudaPointerAttributes a{};
+    const cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw ApiError(H2W_ERR_ARG, std::string(name) + ": not a CUDA pointer");
+    }
+    if (a.type == cudaMemoryTypeManaged) return;
+    if (a.type != cudaMemoryTypeDevice)
+        throw ApiError(H2W_ERR_ARG, std::string(name) + " is not device memory (host or unregistered pointer)");
+    if (a.device != h->cfg.device)
+        throw ApiError(H2W_ERR_ARG, std::string(name) + " lives on device " + std::to_string(a.device) +
+                                        ", the operator on device " + std::to_string(h->cfg.device));
+}
+}  // namespace
+
 namespace h2w {
 int handle_device(const h2w_handle *h) { return h ? h->cfg.device : -1; }
 int handle_fail(h2w_handle *h, int code, const char *msg) { return h ? fail(h, code, msg) : code; }
@@ -2993,6 +3016,8 @@ int matvec_external_ws(h2w_handle *h, const double *x, double *y, int precision,
             throw ApiError(H2W_ERR_ARG, "matvec workspace of " + std::to_string(h->ws_n) + (f32 ? " floats" : " doubles") +
                                             " exceeds the static scratch maximum of " + std::to_string(ws_cap) +
                                             " doubles");
+        require_device_vector(h, x, "x");
+        require_device_vector(h, y, "y");
         cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
         CK(cudaMemsetAsync(ws, 0, (size_t)need * 8, st));
         CK(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
@@ -3002,10 +3027,10 @@ int matvec_external_ws(h2w_handle *h, const double *x, double *y, int precision,
         if (h->coop) {
             if (f32)
                 CK(launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op32.p, (float *)ws, x, y, perm,
-                                   bar, err, st));
+                                   bar, err, st, h->spin_limit));
             else
                 CK(launch_coop_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op.p, ws, x, y, perm, bar, err,
-                                   st));
+                                   st, h->spin_limit));
         } else {
             for (const Phase &ph : h->phases) {
                 if (f32)
@@ -3018,6 +3043,12 @@ int matvec_external_ws(h2w_handle *h, const double *x, double *y, int precision,
             if (f32) CK(launch_scatter_f32((float *)ws + h->yperm_off, y, perm, h->tree.N, st));
             else CK(launch_scatter_f64(ws + h->yperm_off, y, perm, h->tree.N, st));
         }
+        int32_t flag = 0;
+        CK(cudaMemcpyAsync(&flag, err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (flag)
+            throw ApiError(H2W_ERR_CUDA, "a grid-barrier wait of the product ran out (device error " +
+                                             std::to_string(flag) + "); y is not valid");
         return H2W_OK;
     });
 }
@@ -3724,6 +3755,9 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
                 cudaGraphDestroy(g.graph);
             }
             h->loops.clear();
+        } else if (option == H2W_OPT_SPIN_LIMIT) {
+            if (value < 0) throw ApiError(H2W_ERR_ARG, "spin limit must be >= 0");
+            h->spin_limit = value;
         } else if (option == H2W_OPT_COOP) {
             h->coop = value != 0;
             for (auto &g : h->loops) {  // captured steps hold the other launch form
@@ -3751,6 +3785,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_F32_BASIS) *value = h->f32_basis ? 1 : 0;
         else if (option == H2W_OPT_DATAFLOW) *value = h->dataflow ? 1 : 0;
         else if (option == H2W_OPT_PRODUCER_WARP) *value = h->producer_warp ? 1 : 0;
+        else if (option == H2W_OPT_SPIN_LIMIT) *value = h->spin_limit;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });

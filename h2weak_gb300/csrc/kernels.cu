@@ -639,13 +639,13 @@ __global__ void __launch_bounds__(BRG_THREADS, 4)
     brg_coop_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob,
                     const int64_t *__restrict__ pstart, int nphase, const T *__restrict__ A, T *ws,
                     const double *__restrict__ xin, double *yout, const int32_t *__restrict__ perm, unsigned *bar,
-                    int32_t *err) {
+                    int32_t *err, long long spin) {
     __shared__ BrgShared<T> sh;
     for (int p = 0; p < nphase; ++p) {
         const int64_t t1 = pstart[p + 1];
         for (int64_t t = pstart[p] + blockIdx.x; t < t1; t += gridDim.x)
             brg_target<T>(sh, t, roff, blob, A, ws, xin, yout, perm);
-        if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err);
+        if (p + 1 < nphase) grid_barrier(bar, gridDim.x, err, spin);
     }
 }
 
@@ -743,8 +743,9 @@ static cudaError_t launch_brg_t(const int64_t *roff, const int64_t *blob, int64_
 template <class T>
 static cudaError_t launch_coop_t(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                                  const T *A, T *ws, const double *xin, double *yout, const int32_t *perm,
-                                 unsigned *bar, int32_t *err, cudaStream_t st) {
+                                 unsigned *bar, int32_t *err, long long spin, cudaStream_t st) {
     if (nphase <= 0) return cudaSuccess;
+    if (spin <= 0) spin = GRID_SPIN_LIMIT;
     static int per_sm = 0;
     if (g_num_sms == 0) {
         int dev = 0;
@@ -758,7 +759,7 @@ static cudaError_t launch_coop_t(const int64_t *roff, const int64_t *blob, const
     }
     const int grid = g_num_sms * per_sm;
     void *args[] = {(void *)&roff, (void *)&blob, (void *)&pstart, (void *)&nphase, (void *)&A, (void *)&ws,
-                    (void *)&xin, (void *)&yout, (void *)&perm, (void *)&bar, (void *)&err};
+                    (void *)&xin, (void *)&yout, (void *)&perm, (void *)&bar, (void *)&err, (void *)&spin};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)brg_coop_kernel<T>, dim3(grid), dim3(BRG_THREADS), args,
                                                 0, st);
     count_launch();
@@ -803,13 +804,13 @@ cudaError_t launch_brg_flow_f32(const int64_t *roff, const int64_t *blob, int64_
 
 cudaError_t launch_coop_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                             const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
-                            unsigned *bar, int32_t *err, cudaStream_t st) {
-    return launch_coop_t<double>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, st);
+                            unsigned *bar, int32_t *err, cudaStream_t st, long long spin) {
+    return launch_coop_t<double>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, spin, st);
 }
 cudaError_t launch_coop_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                             const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
-                            unsigned *bar, int32_t *err, cudaStream_t st) {
-    return launch_coop_t<float>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, st);
+                            unsigned *bar, int32_t *err, cudaStream_t st, long long spin) {
+    return launch_coop_t<float>(roff, blob, pstart, nphase, A, ws, xin, yout, perm, bar, err, spin, st);
 }
 
 template <class T>

@@ -60,8 +60,6 @@ cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0,
                            double *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
 cudaError_t launch_brg_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const float *A,
                            float *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
-// The whole matvec as one cooperative launch: phase p covers targets
-// [pstart[p], pstart[p+1]); bar (2 unsigned, zero) is the grid barrier state.
 // Dataflow form of the single-vector product (see launch_mr_f32_flow):
 // nt targets in stored order, ctr a zeroed claim counter, rem the producer
 // counts (reset before every launch), consumers in cidx[coff[t] .. coff[t+1])
@@ -71,12 +69,15 @@ cudaError_t launch_brg_flow_f64(const int64_t *roff, const int64_t *blob, int64_
 cudaError_t launch_brg_flow_f32(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
                                 const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const double *xin,
                                 double *yout, const int32_t *perm, int32_t *err, cudaStream_t st);
+// The whole matvec as one cooperative launch: phase p covers targets
+// [pstart[p], pstart[p+1]); bar (2 unsigned, zero) is the grid barrier state;
+// spin bounds each grid-barrier wait in polls (<= 0: the built-in limit).
 cudaError_t launch_coop_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                             const double *A, double *ws, const double *xin, double *yout, const int32_t *perm,
-                            unsigned *bar, int32_t *err, cudaStream_t st);
+                            unsigned *bar, int32_t *err, cudaStream_t st, long long spin = 0);
 cudaError_t launch_coop_f32(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,
                             const float *A, float *ws, const double *xin, double *yout, const int32_t *perm,
-                            unsigned *bar, int32_t *err, cudaStream_t st);
+                            unsigned *bar, int32_t *err, cudaStream_t st, long long spin = 0);
 cudaError_t launch_scatter_f64(const double *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_gather_f64(const double *x, double *xp, const int32_t *perm, int64_t n, cudaStream_t st);
 cudaError_t launch_scatter_f32(const float *yp, double *y, const int32_t *perm, int64_t n, cudaStream_t st);

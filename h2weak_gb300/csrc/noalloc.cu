@@ -5,11 +5,14 @@
 // (an FP32 product uses them as twice as many floats), followed by the grid
 // barrier state and the barrier's error word. Its device address is looked
 // up once per device, on the first call on that device, with that device
-// current (cudaGetSymbolAddress); later calls reuse it. Every call clears
-// the workspace rows it uses, the barrier state and the error word before
-// its launch. All handles and all calls on a device share the one array and
-// it keeps the last call's contents, so calls whose kernels overlap on the
-// GPU (two streams, two host threads) race on it: serialise them.
+// current (cudaGetSymbolAddress); later calls reuse it (the cached address
+// does not survive a cudaDeviceReset of that device). Every call clears the
+// workspace rows it uses, the barrier state and the error word before its
+// launch, and reads the error word back once the product has finished, so a
+// grid-barrier wait that ran out fails that call with H2W_ERR_CUDA. All
+// handles and all calls on a device share the one array and it keeps the
+// last call's contents, so calls whose kernels overlap on the GPU (two
+// streams, two host threads) race on it: serialise them.
 #include <mutex>
 #include <string>
 

@@ -6,9 +6,12 @@ namespace h2w {
 
 // Grid-wide barrier for cooperative launches (all CTAs are co-resident by
 // construction of the launch). bar[0] counts arrivals, bar[1] is the
-// generation. The spin is bounded: a barrier that never completes sets *err
-// and lets the CTA continue, so the kernel always ends.
-static __device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned nblocks, int32_t *err) {
+// generation. The spin is bounded by `limit` polls: a barrier that does not
+// complete in time sets *err and lets the CTA continue, so the kernel always
+// ends (with wrong results, which the error word reports).
+constexpr long long GRID_SPIN_LIMIT = 1LL << 26;
+static __device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned nblocks, int32_t *err,
+                                                    long long limit = GRID_SPIN_LIMIT) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *vgen = bar + 1;
@@ -22,7 +25,7 @@ static __device__ __forceinline__ void grid_barrier(unsigned *bar, unsigned nblo
         } else {
             long long it = 0;
             while (*vgen == gen) {
-                if (++it > (1LL << 26)) {
+                if (++it > limit) {
                     atomicExch(err, 1);
                     break;
                 }

@@ -126,8 +126,15 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
  *  - every call and every handle on a device shares the array, which keeps
  *    the last call's contents (each call clears what must start at zero):
  *    calls that overlap on the GPU race on it;
- *  - asynchronous on `stream` (NULL: the handle's stream), like the DEVICE
- *    form of h2w_matvec. */
+ *  - x and y must be device (or managed) memory of the handle's device;
+ *    anything else (a host pointer) is refused with H2W_ERR_ARG before any
+ *    launch;
+ *  - the product is enqueued on `stream` (NULL: the handle's stream) and the
+ *    call returns once it has finished: it reads the product's device error
+ *    word back, so a grid-barrier wait that ran out (y then invalid) returns
+ *    H2W_ERR_CUDA from this call rather than H2W_OK;
+ *  - the array's cached device address does not survive cudaDeviceReset
+ *    (or a new primary context) on that device: do not call it after one. */
 int h2w_matvec_static(h2w_handle *h, const double *x, double *y, int precision, void *stream);
 
 /* GMRES, unrestarted, FP64, device-resident. Replaces iterative_solver::GMRES
@@ -225,10 +232,17 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 (claims targets, waits for their producers, streams their
  *                 chunks into a ring of shared-memory stages by bulk
  *                 asynchronous copies) and multiplying warps; 0: every warp
- *                 stages and multiplies its CTA's current target. */
+ *                 stages and multiplies its CTA's current target.
+ *  H2W_OPT_SPIN_LIMIT  polls allowed per grid-barrier wait of the
+ *                 single-vector product's cooperative launch with grid
+ *                 barriers (H2W_OPT_DATAFLOW 0, and h2w_matvec_static);
+ *                 0 (default): the built-in limit (2^26 polls, seconds). A
+ *                 wait that runs out lets the kernel finish with an invalid
+ *                 result and makes the call fail with H2W_ERR_CUDA; a tiny
+ *                 limit is how that error path is exercised. */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
        H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8,
-       H2W_OPT_PRODUCER_WARP = 9 };
+       H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
