@@ -107,11 +107,58 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def nlevels_for(dim, n_param, leaf_param):
+    """Tree depth as the reference's drivers compute it (1D/codes/main.cpp:13,
+    2D/codes/main.cpp:13, 3D/codes/main.cpp:11)."""
+    import math
+    if dim == 1:
+        return int(math.ceil(math.log(float(n_param) / leaf_param) / math.log(2)))
+    if dim == 2:
+        return int(math.ceil(2.0 * math.log(float(n_param) / leaf_param) / math.log(4)))
+    return int(math.ceil(3 * math.log(float(n_param) / leaf_param) / math.log(8)))
+
+
+def grid_points(dim, n):
+    """The reference's uniform grid (set_Uniform_Nodes, 1D/codes/HODLR1Dtree.hpp:59-66,
+    2D/codes/HODLR2Dtree.hpp:75-91, 3D/codes/HODLR3Dtree.hpp:82-102) with its
+    point numbering, in numpy: node k = -1 + 2(k+1)/(n+1), the same operations
+    in the same order as the library's h2w_gen_grid, so the points are bitwise
+    the same. The CPU arm builds its points here and never loads the GPU library."""
+    k = np.arange(n, dtype=np.float64)
+    node = -1.0 + 2.0 * (k + 1.0) / (n + 1.0)
+    if dim == 1:
+        return node.reshape(n, 1)
+    if dim == 2:
+        j, kk = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        return np.stack([node[kk.ravel()], node[j.ravel()]], axis=1)
+    j, kk, i = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    return np.stack([node[kk.ravel()], node[j.ravel()], node[i.ravel()]], axis=1)
+
+
+def load_synth():
+    """The seeded generators (h2weak_gb300/synth.py, pure numpy) loaded by
+    path, without importing the GPU package."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("h2w_synth", os.path.join(ROOT, "h2weak_gb300", "synth.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def common_config(wl, N, nlev, R):
+    """The workload, identical in both arms' lines."""
+    return {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*", "rhs_per_step": R,
+            "rhs": "columns N(0,1) from seeded splitmix64 streams, B = A X_true with the FP64 compressed "
+                   "operator, X0 = 1", "tolerance": "relative residual 1e-%d per column" % wl["gtol"],
+            "parallelism": "replicas (one problem per GPU)",
+            "l2": "no flush: the compressed operator exceeds the 129 MB L2 (inputs larger than L2)"}
+
+
 def make_problem(wl, device):
     import h2weak_gb300 as hw
     from h2weak_gb300 import synth
     dim = wl["dim"]
-    nlev = hw.levels_for(dim, wl["grid"], wl["leaf"])
+    nlev = nlevels_for(dim, wl["grid"], wl["leaf"])
     N = wl["grid"] ** dim
     op = hw.H2Operator(dim, wl["form"], wl["choice"], wl["tol"], nlev, kernel_n=N,
                        diag_n=2 * N if dim == 1 else N, device=device)
@@ -121,58 +168,70 @@ def make_problem(wl, device):
     return op, nlev, xt
 
 
-def cpu_oracle_solves(wl, steps, warmup):
-    """The CPU oracle (restatement of the reference's algorithm) on the host
-    cores: assembly, then `warmup` + `steps` FP64 GMRES solves."""
+def cpu_oracle_solves(wl, R, steps, warmup, budget_s=150.0):
+    """The CPU oracle (the reference's algorithm restated in C++, OpenMP on
+    every host core) on the same workload: assembly, then per step the FP64
+    GMRES solves of the step's right-hand sides one after another (the
+    reference solves one right-hand side per call). Every step solves all R
+    columns when warmup + steps fit in budget_s, else the same number of
+    columns from each step's sample (stated in the result)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import h2weak_gb300 as hw
-    from h2weak_gb300 import synth
     from oracle import Oracle
+    synth = load_synth()
     dim = wl["dim"]
-    nlev = hw.levels_for(dim, wl["grid"], wl["leaf"])
-    hop = hw.H2Operator(dim, wl["form"], wl["choice"], wl["tol"], nlev, device=-1)
-    hop.gen_grid(wl["grid"])
-    pts = hop.points()
+    nlev = nlevels_for(dim, wl["grid"], wl["leaf"])
+    pts = grid_points(dim, wl["grid"])
     N = len(pts)
     t0 = time.time()
     o = Oracle(dim, wl["form"], pts, nlev, wl["tol"], wl["choice"], N, 2 * N if dim == 1 else N)
     t_asm = time.time() - t0
-    xt = synth.normal(synth.config_seed(1, 0), N)
-    # right-hand side from the compressed operator (the dense O(N^2) product is
-    # the GPU's job; the timed quantity here is the solve)
-    b = o.matvec(xt)
-    for _ in range(warmup):
-        o.gmres(b, max_iter=500, tol_pow=wl["gtol"])
+    cols = [synth.normal(synth.config_seed(1, c), N) for c in range(R)]
+    rhs = [o.matvec(x) for x in cols]
     t0 = time.time()
-    its = []
-    for _ in range(steps):
-        _, it, res = o.gmres(b, max_iter=500, tol_pow=wl["gtol"])
-        its.append(it)
+    _, it0, _ = o.gmres(rhs[0], max_iter=500, tol_pow=wl["gtol"])
+    t_col = time.time() - t0
+    per_step = max(1, min(R, int(budget_s / max(t_col * (steps + warmup), 1e-9))))
+    for w in range(warmup):
+        for c in range(per_step):
+            o.gmres(rhs[(w * per_step + c) % R], max_iter=500, tol_pow=wl["gtol"])
+    its, errs = [], []
+    t0 = time.time()
+    for k in range(steps):
+        for c in range(per_step):
+            q = (k * per_step + c) % R
+            x, it, res = o.gmres(rhs[q], max_iter=500, tol_pow=wl["gtol"])
+            its.append(it)
     t = time.time() - t0
+    errs.append(float(np.linalg.norm(x - cols[q]) / np.linalg.norm(cols[q])))
     t0 = time.time()
     nmv = 5
     for _ in range(nmv):
-        o.matvec(xt)
+        o.matvec(cols[0])
     t_mv = (time.time() - t0) / nmv
-    return dict(t_solve=t / steps, iters=its[-1], t_asm=t_asm, t_mv=t_mv, mem=o.memory(), N=N,
+    return dict(t_step=t / steps, cols_per_step=per_step, t_solve=t / (steps * per_step), iters=max(its),
+                t_asm=t_asm, t_mv=t_mv, mem=o.memory(), N=N, nlev=nlev, err=errs[-1],
                 cores=int(os.environ.get("OMP_NUM_THREADS", os.cpu_count())))
 
 
 def run_reference(args, wl):
     steps = max(1, args.steps)
-    r = cpu_oracle_solves(wl, steps, max(0, min(args.warmup, 1)))
+    R = max(1, min(64, args.rhs))
+    r = cpu_oracle_solves(wl, R, steps, max(0, min(args.warmup, 1)))
     v = 1.0 / r["t_solve"]
+    sample = ("%d of the step's %d right-hand sides per step (%s), each a full FP64 GMRES solve to 1e-%d on the "
+              "host cores by the CPU oracle restating the reference's algorithm; assembly %.2fs untimed" %
+              (r["cols_per_step"], R, "the whole step" if r["cols_per_step"] == R else "a bounded sample",
+               wl["gtol"], r["t_asm"]))
     line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": steps,
-            "warmup": args.warmup, "ms_per_step": r["t_solve"] * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": wl["desc"], "N": r["N"], "form": "H2*", "l2": "n/a (CPU)"},
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": r["cores"], "kind": "port",
-                             "sample": "%d full FP64 GMRES solves to 1e-10 of the workload on the host cores "
-                                       "(CPU oracle restating the reference's algorithm; assembly %.2fs untimed)"
-                                       % (steps, r["t_asm"])},
+            "warmup": args.warmup, "ms_per_step": r["t_solve"] * R * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": common_config(wl, r["N"], r["nlev"], R),
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": r["cores"], "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "gmres_iters": r["iters"], "matvec_ms": r["t_mv"] * 1e3,
-            "matvec_gbs": 8.0 * r["mem"] / r["t_mv"] / 1e9}
+            "solver": "unrestarted FP64 GMRES per right-hand side (iterative_solver::GMRES, "
+                      "1D/codes/gmres.hpp:92-200), compressed operator matvec (OpenMP)",
+            "gmres_iters": r["iters"], "rel_err_vs_xtrue": r["err"], "matvec_ms": r["t_mv"] * 1e3,
+            "matvec_gbs": 8.0 * r["mem"] / r["t_mv"] / 1e9, "assembly_s": r["t_asm"], "storage_entries": r["mem"]}
     print(json.dumps(line), flush=True)
 
 
@@ -363,7 +422,9 @@ def main():
     rp = 16 if R <= 16 else (32 if R <= 32 else 64)
     # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu captures of the
     # same launches on this workload: profiles/mw_flow_fp32_2d_ie_65536.md, mr_flow_df64_2d_ie_65536.md
-    ncu_traffic = {"fp32": 361.970e6 + 72.415e6, "df64": 896.444e6 + 188.591e6}
+    kname = (("mw_flow_kernel" if top == "fp32" and op.get_option(hw.OPT_PRODUCER_WARP) else "mr_flow_kernel")
+             if op.get_option(hw.OPT_DATAFLOW) else "mr_coop_kernel")
+    ncu_traffic = {("mw_flow_kernel", "fp32"): 361.970e6 + 72.415e6, ("mr_flow_kernel", "df64"): 896.444e6 + 188.591e6}
     # the multi-vector kernel multiplies every packed operator entry by R vectors: one FMA per
     # term (FP32), about twelve FP32 operations per term (double-FP32); nominal FP32 peak of
     # 152 SMs x 128 lanes x 2 flop x 2.07 GHz
@@ -374,7 +435,8 @@ def main():
     plan = op.plan_stats()
     plan["padding_overhead"] = plan["multiplied"] / plan["entries"] - 1.0 if plan["entries"] else None
     roof = {"bound": "hbm", "achieved": tk["gbs"], "peak": peak, "unit": "GB/s", "frac": tk["gbs"] / peak,
-            "traffic": ncu_traffic.get(top) if args.workload == "2d_ie_65536" and R == 64 else None,
+            # the captured kernel's DRAM bytes, only when that kernel is the one reported here
+            "traffic": ncu_traffic.get((kname, top)) if args.workload == "2d_ie_65536" and R == 64 else None,
             "compute": {"pipe": "fp64" if top == "fp64" else "fp32",
                         "ops_per_launch": ops_per_term * entries * R,
                         "achieved_tops": achieved_ops / 1e12,
@@ -383,22 +445,49 @@ def main():
                         "note": "each operator element feeds R FMAs: the pipe, not HBM, bounds this kernel",
                         # entries multiplied per column with the kernel's row and column padding
                         "plan": plan},
-            "kernel": "%s<%s, %d> (one cooperative launch = one %d-vector matvec)" % (
-                ("mw_flow_kernel" if top == "fp32" and op.get_option(hw.OPT_PRODUCER_WARP) else "mr_flow_kernel")
-                if op.get_option(hw.OPT_DATAFLOW) else "mr_coop_kernel", ctype, rp, R),
+            "kernel": "%s<%s, %d> (one cooperative launch = one %d-vector matvec)" % (kname, ctype, rp, R),
             "bytes_per_launch": tk["bytes"], "launch_us": tk["us"], "launches": tk["launches"],
             "share_of_matvec_time": tk["ms"] / tot if tot else None,
             "peak_kind": (peak_kind + " (MEASURED_PEAKS.json hbm_gbs)") if peak_kind == "measured" else peak_kind,
             "per_precision": {k: {"launch_us": round(v["us"], 1), "GBs": round(v["gbs"], 1),
                                   "share": round(v["ms"] / tot, 3)} for k, v in kern.items()}}
 
-    # ---- CPU baseline: the oracle on this host's cores
+    # ---- CPU baseline: the oracle on this host's cores, a bounded sample of the same workload
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        r = cpu_oracle_solves(wl, 1, 0)
+        r = cpu_oracle_solves(wl, R, 1, 0, budget_s=20.0)
         cpu = {"value": 1.0 / r["t_solve"], "unit": "solves/s", "cores": r["cores"], "kind": "port",
-               "sample": "1 full FP64 GMRES solve to 1e-10 of the same workload (CPU oracle, assembly %.2fs untimed, "
-                         "%d iterations, matvec %.1f ms)" % (r["t_asm"], r["iters"], r["t_mv"] * 1e3)}
+               "sample": "%d of the %d right-hand sides, each a full FP64 GMRES solve to 1e-%d (CPU oracle, "
+                         "assembly %.2fs untimed, %d iterations, matvec %.1f ms)"
+                         % (r["cols_per_step"], R, gtol, r["t_asm"], r["iters"], r["t_mv"] * 1e3)}
+
+    # ---- assembly: plain NCA (timed again, warm) against learned proposals (the
+    # shipped model; blocks the NCA stopping test rejects fall back to the plain
+    # search), with each operator's error on the same exact dense rows
+    def rows_err():
+        y = op.matvec(xt)
+        return float(np.linalg.norm(y[:nrow] - b_rows_xt) / np.linalg.norm(b_rows_xt))
+
+    b_rows_xt = b_d[:nrow].cpu().numpy()
+    asm = {}
+    torch.cuda.synchronize()
+    t0 = time.time()
+    op.assemble(hw.ASSEMBLE_NCA)
+    torch.cuda.synchronize()
+    asm["plain"] = {"s": time.time() - t0, "storage_entries": op.storage_entries(), "dense_rows_rel_err": rows_err()}
+    from h2weak_gb300 import learned
+    params, calib, margin = learned.load()
+    op.learn_set_model(params, calib, margin)
+    op.learn_stats()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    op.assemble(hw.ASSEMBLE_LEARNED)
+    torch.cuda.synchronize()
+    t_l = time.time() - t0
+    blocks, acc = op.learn_stats()
+    asm["learned"] = {"s": t_l, "storage_entries": op.storage_entries(), "dense_rows_rel_err": rows_err(),
+                      "blocks": blocks, "accepted": acc}
+    asm["learned_speedup"] = asm["plain"]["s"] / t_l
 
     value = K * R * world / (ms_b / 1e3)
     ms_solve_b = ms_b / K / R
@@ -406,18 +495,15 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms_b / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*", "rhs_per_step": R,
-                   "solver": "batched: FP32-operator inner GMRES (FP32 Krylov basis, FP64 Hessenberg and "
-                             "rotations, %d columns in lockstep, one multi-vector matvec per step) + iterative "
-                             "refinement, residuals FP32 at x0 then "
-                             "double-FP32 on the FP64 operator, later ones updated as r - A32 d under a calibrated "
-                             "error bound; CUDA-graph Arnoldi loop" % R,
-                   "autotuned": {"multi_xw": tuned_xw, "multi_mix_ms": tuned_xw_ms,
-                                 "fp32_producer_warp": op.get_option(hw.OPT_PRODUCER_WARP),
-                                 "single_row_split": tuned_rs, "single_fp32_ms": tuned_rs_ms},
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "no flush: FP64 operator %.0f MB, FP32 %.0f MB, both > 129 MB L2" %
-                         (op.operator_bytes(hw.PREC_FP64) / 1e6, op.operator_bytes(hw.PREC_FP32) / 1e6)},
+        "config": common_config(wl, N, nlev, R),
+        "solver": "batched: FP32-operator inner GMRES (FP32 Krylov basis, FP64 Hessenberg and rotations, %d "
+                  "columns in lockstep, one multi-vector matvec per step) + iterative refinement, residuals FP32 "
+                  "at x0 then double-FP32 on the FP64 operator, later ones updated as r - A32 d under a "
+                  "calibrated error bound; CUDA-graph Arnoldi loop" % R,
+        "autotuned": {"multi_xw": tuned_xw, "multi_mix_ms": tuned_xw_ms,
+                      "fp32_producer_warp": op.get_option(hw.OPT_PRODUCER_WARP),
+                      "single_row_split": tuned_rs, "single_fp32_ms": tuned_rs_ms},
+        "operator_mb": {"fp64": op.operator_bytes(hw.PREC_FP64) / 1e6, "fp32": op.operator_bytes(hw.PREC_FP32) / 1e6},
         "e2e": {"value": K * R * world / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N * R,
                 "d2h_bytes_per_step": 8 * N * R},
         "gpu_launches": int(launches),
@@ -432,10 +518,10 @@ def main():
         "single_mixed": {"ms_per_solve": ms_mixed / K, "outer": outer, "inner_total": inner, "resid": res_mixed,
                          "rel_err_vs_xtrue": err_mixed},
         "single_fp64": {"ms_per_solve": ms_fp64 / K, "iters": it64, "resid": res64, "rel_err_vs_xtrue": err_fp64},
-        "speedup_vs_plain_fp64": {"batched_mixed_over_single_fp64": (ms_fp64 / K) / ms_solve_b,
-                                  "batched_mixed_over_batched_fp64": (ms_b64 / K / R) / ms_solve_b,
+        # same workload on both sides of each ratio: the R columns (batched), one column (single)
+        "speedup_vs_plain_fp64": {"batched_mixed_over_batched_fp64": (ms_b64 / K / R) / ms_solve_b,
                                   "single_mixed_over_single_fp64": ms_fp64 / ms_mixed},
-        "assembly_s": t_asm, "storage_entries": storage,
+        "assembly_s": t_asm, "storage_entries": storage, "assembly": asm,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

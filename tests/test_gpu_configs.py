@@ -1,0 +1,289 @@
+"""Parity at the full sizes of the benchmark configurations, GPU against the
+CPU oracle (the reference's algorithm restated, pinned to the reference's own
+outputs by the golden fixtures):
+
+* 1D H2* RBF, N = 32768 grid, 9 levels, NCA tol 1e-10, diagonal sqrt(2N)
+  (1D/codes/main.cpp:29-34 with ./test 32768 64 1 10 1): tree lists, pivots
+  and storage bit-exact (every entry is built from IEEE-exact operations),
+  matvec <= 1e-13 on two vectors, GMRES iterations +-1 and solution error
+  within 10x of the oracle's (1D/codes/gmres.hpp:92-200).
+* 2D H2* IE, 256^2 grid, 5 levels, tol 1e-10: the oracle's pivots imported
+  and the matvec <= 1e-13 on two vectors; the GPU's own pivots agree on
+  >= 90 % of the boxes (CUDA's and glibc's log may differ in the last bit)
+  with storage within 1 %; GMRES iterations +-1.
+* The GPU dense product (getTruePoten, 3D/codes/HODLR3Dtree.hpp:2630-2643)
+  against the reference's own dense product in every golden file and against
+  oracle entries on sampled rows at full size.
+* 3D (H2+H)* RBF 64^3, 4 levels, tol 1e-8, 64 right-hand sides: the FP64
+  product against exact dense rows, the FP32 and double-FP32 64-vector
+  products against the FP64 one, and the mixed-precision 64-column solve to
+  a relative residual of 1e-10 checked with FP64 products.
+* The many-problem batch (2D, uniform random points, log-uniform sizes,
+  alternating kernels) on the oracle's pivots: every problem's product and
+  GMRES iteration count against the oracle's.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from h2weak_gb300 import synth
+
+
+def relerr(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def sampled_rows(N, k, seed):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(N, size=min(k, N), replace=False)).astype(np.int32)
+
+
+def oracle_rows(o, rows, x):
+    """Exact dense rows from the oracle's kernel entries, in blocks."""
+    out = np.empty(len(rows))
+    cols = np.arange(o.N, dtype=np.int32)
+    for s in range(0, len(rows), 64):
+        out[s:s + 64] = o.entries(rows[s:s + 64], cols) @ x
+    return out
+
+
+def gpu_op(hw, dim, form, choice, tol, nlev, N, pts=None, grid=None):
+    op = hw.H2Operator(dim, form, choice, tol, nlev, kernel_n=N, diag_n=2 * N if dim == 1 else N, device=0)
+    if grid is not None:
+        op.gen_grid(grid)
+    else:
+        op.set_points(pts)
+    op.build_tree()
+    return op
+
+
+# ------------------------------------------------------------------ cfg 1 ---
+@pytest.fixture(scope="module")
+def cfg1(gpu):
+    from oracle import Oracle
+    hw = gpu
+    N = 32768
+    op = gpu_op(hw, 1, hw.FORM_NESTED, hw.KERNEL_RBF, 10, 9, N, grid=N)
+    o = Oracle(1, 0, op.points(), 9, 10, 1, N, 2 * N)
+    op.assemble(hw.ASSEMBLE_NCA)
+    return hw, op, o
+
+
+@pytest.mark.gpu
+def test_cfg1_tree_pivots_storage_bit_exact(cfg1):
+    hw, op, o = cfg1
+    for nm in ("charge", "nbr", "il", "isvertex", "far_check", "far_charge"):
+        p, v = op.get_list(nm)
+        po, vo = o.csr(nm)
+        assert np.array_equal(p, po) and np.array_equal(v, vo), nm
+    assert op.storage_entries() == o.memory()
+
+
+@pytest.mark.gpu
+def test_cfg1_matvec_two_vectors(cfg1):
+    hw, op, o = cfg1
+    for k in range(2):
+        x = synth.normal(synth.config_seed(1, 10 + k), op.N)
+        assert relerr(op.matvec(x), o.matvec(x)) <= 1e-13, k
+
+
+@pytest.mark.gpu
+def test_cfg1_gmres_vs_oracle(cfg1):
+    hw, op, o = cfg1
+    N = op.N
+    xt = synth.normal(synth.config_seed(1), N)
+    b = op.dense_matvec(xt)
+    rows = sampled_rows(N, 256, 11)
+    assert relerr(b[rows], oracle_rows(o, rows, xt)) <= 1e-13
+    x, it, res = op.gmres(b, max_iter=500, tol_pow=10)
+    xo, ito, reso = o.gmres(b, max_iter=500, tol_pow=10)
+    assert abs(it - ito) <= 1, (it, ito)
+    assert res < 1e-10
+    err, err_o = relerr(x, xt), relerr(xo, xt)
+    assert err <= 10 * err_o + 1e-13, (err, err_o)
+    print("cfg1: iterations %d (oracle %d), residual %.2e (oracle %.2e), error %.2e (oracle %.2e)"
+          % (it, ito, res, reso, err, err_o))
+
+
+# ------------------------------------------------------------------ cfg 2 ---
+@pytest.fixture(scope="module")
+def cfg2(gpu):
+    from oracle import Oracle
+    hw = gpu
+    N = 256 * 256
+    op = gpu_op(hw, 2, hw.FORM_NESTED, hw.KERNEL_IE, 10, 5, N, grid=256)
+    o = Oracle(2, 0, op.points(), 5, 10, 0, N, N)
+    return hw, op, o
+
+
+@pytest.mark.gpu
+def test_cfg2_matvec_on_oracle_pivots(cfg2):
+    hw, op, o = cfg2
+    for nm in ("far_check", "far_charge", "ver_check", "ver_charge"):
+        p, v = o.csr(nm)
+        op.import_list(nm, p, v)
+    op.assemble(hw.ASSEMBLE_IMPORT)
+    assert op.storage_entries() == o.memory()
+    for k in range(2):
+        x = synth.normal(synth.config_seed(2, 10 + k), op.N)
+        assert relerr(op.matvec(x), o.matvec(x)) <= 1e-13, k
+
+
+@pytest.mark.gpu
+def test_cfg2_own_pivots_agreement(cfg2):
+    hw, op, o = cfg2
+    op.assemble(hw.ASSEMBLE_NCA)
+    agree = total = 0
+    for nm in ("far_check", "far_charge", "ver_check", "ver_charge"):
+        p, v = op.get_list(nm)
+        po, vo = o.csr(nm)
+        assert len(p) == len(po), nm
+        for i in range(len(po) - 1):
+            if po[i + 1] == po[i] and p[i + 1] == p[i]:
+                continue
+            total += 1
+            agree += int(np.array_equal(v[p[i]:p[i + 1]], vo[po[i]:po[i + 1]]))
+    ds = (op.storage_entries() - o.memory()) / o.memory()
+    print("cfg2 own NCA: %d/%d box pivot lists equal (%.1f %%), storage delta %+.3f %%"
+          % (agree, total, 100.0 * agree / total, 100.0 * ds))
+    assert agree >= 0.9 * total, (agree, total)
+    assert abs(ds) <= 0.01
+    # the own operator is as accurate as the oracle's on exact dense rows
+    x = synth.normal(synth.config_seed(2, 12), op.N)
+    rows = sampled_rows(op.N, 256, 12)
+    yd = oracle_rows(o, rows, x)
+    e_g = relerr(op.matvec(x)[rows], yd)
+    e_o = relerr(o.matvec(x)[rows], yd)
+    assert e_g <= 10 * e_o + 1e-14, (e_g, e_o)
+
+
+@pytest.mark.gpu
+def test_cfg2_gmres_vs_oracle(cfg2):
+    hw, op, o = cfg2
+    for nm in ("far_check", "far_charge", "ver_check", "ver_charge"):
+        p, v = o.csr(nm)
+        op.import_list(nm, p, v)
+    op.assemble(hw.ASSEMBLE_IMPORT)
+    N = op.N
+    xt = synth.normal(synth.config_seed(2), N)
+    b = op.dense_matvec(xt)
+    rows = sampled_rows(N, 256, 13)
+    assert relerr(b[rows], oracle_rows(o, rows, xt)) <= 1e-13
+    x, it, res = op.gmres(b, max_iter=500, tol_pow=10)
+    xo, ito, reso = o.gmres(b, max_iter=500, tol_pow=10)
+    assert abs(it - ito) <= 1, (it, ito)
+    err, err_o = relerr(x, xt), relerr(xo, xt)
+    assert err <= 10 * err_o + 1e-13, (err, err_o)
+    # the mixed-precision form reaches the same FP64 tolerance
+    xm, outer, inner, resm = op.gmres_ir(b, max_outer=20, inner_iter=200, tol_pow=10)
+    assert resm < 1e-10
+    assert relerr(o.matvec(xm), b) < 1e-10
+    print("cfg2: GMRES %d iterations (oracle %d), error %.2e (oracle %.2e); mixed %d outer / %d inner, error %.2e"
+          % (it, ito, err, err_o, outer, inner, relerr(xm, xt)))
+
+
+# ------------------------------------------------------ dense product -------
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", golden_names())
+def test_dense_matvec_vs_reference_golden(gpu, name):
+    hw = gpu
+    g = load_golden(name)
+    N, dim = g["N"], g["dim"]
+    op = gpu_op(hw, dim, g["form"], g["choice"], g["tol_pow"], g["nlevels"], N, pts=g["points"])
+    y = op.dense_matvec(g["vecs"][0])
+    assert relerr(y, g["dense_matvec"]) <= 1e-13
+    # a row range alone gives the same rows
+    r0, nr = N // 3, min(97, N - N // 3)
+    assert relerr(op.dense_matvec(g["vecs"][0], row0=r0, nrows=nr), y[r0:r0 + nr]) <= 1e-15
+
+
+# ------------------------------------------------------------------ cfg 3 ---
+@pytest.mark.gpu
+def test_cfg3_products_and_64_column_solve(gpu):
+    """3D semi-nested RBF 64^3 (5.4e9 stored entries): products against
+    exact dense rows, the 64-vector FP32 / DF64 products against FP64, and
+    the batched mixed-precision solve of 64 right-hand sides."""
+    import torch
+    hw = gpu
+    N = 64 ** 3
+    op = gpu_op(hw, 3, hw.FORM_SEMINESTED, hw.KERNEL_RBF, 8, 4, N, grid=64)
+    op.assemble(hw.ASSEMBLE_NCA)
+    R = 64
+    X = torch.from_numpy(np.stack([synth.normal(synth.config_seed(3, c), N) for c in range(R)])).cuda()
+    Y64, Y32, Ydf, B = (torch.empty_like(X) for _ in range(4))
+    op.matvec_device(X.data_ptr(), Y64.data_ptr(), nrhs=R, precision=hw.PREC_FP64)
+    op.matvec_device(X.data_ptr(), Y32.data_ptr(), nrhs=R, precision=hw.PREC_FP32)
+    op.matvec_device(X.data_ptr(), Ydf.data_ptr(), nrhs=R, precision=hw.PREC_DF64)
+    torch.cuda.synchronize()
+    y64, y32, ydf = Y64.cpu().numpy(), Y32.cpu().numpy(), Ydf.cpu().numpy()
+    x0 = X[0].cpu().numpy()
+    # single-vector FP64 product = column 0 of the multi-vector one
+    assert relerr(op.matvec(x0), y64[0]) <= 1e-13
+    # compression error on exact dense rows (GPU dense kernel, FP64)
+    starts = sampled_rows(N - 256, 4, 14)
+    rows = np.concatenate([np.arange(r, r + 256) for r in starts])
+    yd = np.concatenate([op.dense_matvec(x0, row0=int(r), nrows=256) for r in starts])
+    e_c = relerr(y64[0][rows], yd)
+    assert e_c < 1e-6, e_c
+    for c in range(R):
+        assert relerr(y32[c], y64[c]) < 1e-5, c
+        assert relerr(ydf[c], y64[c]) < 1e-12, c
+    # 64 right-hand sides B = A X, solved together from x0 = 1
+    B.copy_(Y64)
+    Xs = torch.ones_like(X)
+    outer, inner, res = op.gmres_ir_batch_device(B.data_ptr(), Xs.data_ptr(), R, 20, 200, 10)
+    assert np.all(res < 1e-10), res.max()
+    AX = torch.empty_like(X)
+    op.matvec_device(Xs.data_ptr(), AX.data_ptr(), nrhs=R, precision=hw.PREC_FP64)
+    torch.cuda.synchronize()
+    Bh, AXh = B.cpu().numpy(), AX.cpu().numpy()
+    rt = max(relerr(AXh[c], Bh[c]) for c in range(R))
+    assert rt < 1e-10, rt
+    ex = max(relerr(Xs[c].cpu().numpy(), X[c].cpu().numpy()) for c in range(R))
+    print("cfg3: storage %.3g entries; compression error %.2e on 1024 dense rows; 64 columns solved in %d outer / "
+          "%d inner steps, worst FP64 residual %.2e, worst error vs X %.2e" % (op.storage_entries(), e_c, outer, inner,
+                                                                               rt, ex))
+
+
+# ------------------------------------------------------------------ cfg 4 ---
+def cfg4_sizes(count, lo, hi):
+    """N_i = floor(exp(U(ln lo, ln hi))) per instance seed (the many-problem
+    configuration's size law, at reduced bounds so that the oracle runs in
+    seconds)."""
+    out = []
+    for i in range(count):
+        u = synth.uniform01(synth.config_seed(4, 1000 + i), 1)[0]
+        out.append(int(np.floor(np.exp(np.log(lo) + u * (np.log(hi) - np.log(lo))))))
+    return out
+
+
+@pytest.mark.gpu
+def test_cfg4_batch_vs_oracle(gpu):
+    from oracle import Oracle
+    hw = gpu
+    sizes = cfg4_sizes(12, 1024, 8192)
+    ops, oracles = [], []
+    for i, n in enumerate(sizes):
+        nl = max(1, int(np.ceil(np.log(n / 64.0) / np.log(4.0))))
+        pts = synth.uniform_points(synth.config_seed(4, i), n, 2)
+        op = gpu_op(hw, 2, hw.FORM_NESTED, i % 2, 8, nl, n, pts=pts)
+        o = Oracle(2, 0, pts, nl, 8, i % 2, n, n)
+        for nm in ("far_check", "far_charge", "ver_check", "ver_charge"):
+            p, v = o.csr(nm)
+            op.import_list(nm, p, v)
+        op.assemble(hw.ASSEMBLE_IMPORT)
+        assert op.storage_entries() == o.memory(), i
+        ops.append(op)
+        oracles.append(o)
+    B = hw.Batch(ops)
+    x = synth.normal(synth.config_seed(4, 77), B.N)
+    y = B.matvec(x)
+    for p, (o, xs, ys) in enumerate(zip(oracles, B.split(x), B.split(y))):
+        assert relerr(ys, o.matvec(xs)) <= 1e-13, p
+    xt = synth.normal(synth.config_seed(4, 78), B.N)
+    rhs = np.concatenate([op.dense_matvec(xs) for op, xs in zip(ops, B.split(xt))])
+    xb, it, res = B.gmres(rhs, max_iter=400, tol_pow=10)
+    for p, (o, bs) in enumerate(zip(oracles, B.split(rhs))):
+        _, ito, _ = o.gmres(bs, max_iter=400, tol_pow=10)
+        assert abs(int(it[p]) - ito) <= 1, (p, sizes[p], it[p], ito)
+    assert np.all(res < 1e-10)
