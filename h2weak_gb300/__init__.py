@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libh2w.so")
 
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_RANK, ERR_NOT_CONVERGED, ERR_STATE = -1, -2, -3, -4, -5, -6
-FORM_NESTED, FORM_SEMINESTED = 0, 1
+FORM_NESTED, FORM_SEMINESTED, FORM_NONNESTED = 0, 1, 2
 KERNEL_IE, KERNEL_RBF = 0, 1
 ASSEMBLE_NCA, ASSEMBLE_IMPORT, ASSEMBLE_LEARNED = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
@@ -40,7 +40,7 @@ LISTS = {"charge": 0, "nbr": 1, "il": 2, "isvertex": 3, "far_check": 4, "far_cha
 EXPORTS = ["h2w_create", "h2w_destroy", "h2w_last_error", "h2w_set_points", "h2w_gen_grid", "h2w_gen_uniform",
            "h2w_get_points", "h2w_num_points", "h2w_build_tree", "h2w_get_list", "h2w_import_list",
            "h2w_assemble", "h2w_storage_entries", "h2w_operator_bytes", "h2w_matvec", "h2w_gmres",
-           "h2w_gmres_ir", "h2w_dense_matvec", "h2w_profile", "h2w_profile_phases", "h2w_launch_count"]
+           "h2w_gmres_ir", "h2w_dense_matvec", "h2w_total_error", "h2w_profile", "h2w_profile_phases", "h2w_launch_count"]
 
 
 class H2WError(RuntimeError):
@@ -93,6 +93,10 @@ def lib():
         "h2w_gmres_batch": [P, P, P, I, I, I, I, P, P],
         "h2w_gmres_ir_batch": [P, P, P, I, I, I, I, I, ctypes.POINTER(I), ctypes.POINTER(I), P],
         "h2w_dense_matvec": [P, P, P, I64, I64, I],
+        "h2w_total_error": [P, P, I64, I, ctypes.POINTER(D)],
+        "h2w_save_operator": [P, ctypes.c_char_p],
+        "h2w_open_operator": [ctypes.c_char_p, I, ctypes.POINTER(P)],
+        "h2w_get_config": [P, ctypes.POINTER(_Config)],
         "h2w_profile": [P, I],
         "h2w_profile_multi": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(D)],
         "h2w_plan_stats": [P, P, I],
@@ -162,6 +166,26 @@ class H2Operator:
             raise H2WError(rc, "h2w_create failed (no CUDA device or bad configuration)")
         self.h = h
         self.dim, self.form, self.choice, self.tol_pow, self.nlevels = dim, form, choice, tol_pow, nlevels
+
+    @classmethod
+    def open(cls, path, device=0):
+        """A handle from an operator file (h2w_open_operator): the saved
+        operator formed from its pivots on `device` (-1: host-only)."""
+        h = ctypes.c_void_p()
+        rc = lib().h2w_open_operator(os.fsencode(path), device, ctypes.byref(h))
+        if rc != OK:
+            raise H2WError(rc, "h2w_open_operator failed for %s (missing, corrupted or not an operator file)" % path)
+        self = cls.__new__(cls)
+        self.h = h
+        cfg = _Config()
+        self._ck(lib().h2w_get_config(self.h, ctypes.byref(cfg)))
+        self.dim, self.form, self.choice, self.tol_pow, self.nlevels = (cfg.dim, cfg.form, cfg.choice, cfg.tol_pow,
+                                                                        cfg.nlevels)
+        return self
+
+    def save(self, path):
+        """Write the operator file of this assembled operator (h2w_save_operator)."""
+        self._ck(lib().h2w_save_operator(self.h, os.fsencode(path)))
 
     def close(self):
         if getattr(self, "h", None):
@@ -326,6 +350,14 @@ class H2Operator:
         self._ck(lib().h2w_dense_matvec(self.h, _ptr(x), _ptr(y), row0, n, HOST))
         return y
 
+    def total_error(self, x, nrows=0):
+        """||y_dense - A x|| / ||y_dense|| with the exact dense product on the
+        GPU (compute_total_error); nrows > 0 samples that many evenly spaced rows."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        e = ctypes.c_double()
+        self._ck(lib().h2w_total_error(self.h, _ptr(x), int(nrows), HOST, ctypes.byref(e)))
+        return e.value
+
     def gmres_device(self, b_ptr, x_ptr, max_iter=500, tol_pow=10):
         it, res = ctypes.c_int(), ctypes.c_double()
         rc = lib().h2w_gmres(self.h, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), max_iter, tol_pow, DEVICE,
@@ -488,6 +520,7 @@ class _TreeView:
         self._op = op
         self.N = op.N
         self.memory = 0.0
+        self.collective_charge = None  # the charge of the last mat_vec_prod
 
     def findMemory(self):
         self.memory = self._op.storage_entries()
@@ -498,6 +531,13 @@ class _TreeView:
 
     def getTruePoten(self, charge):
         return self._op.dense_matvec(charge)
+
+    def compute_total_error(self, nrows=0):
+        """Error of the last mat_vec_prod against the exact dense product
+        (compute_total_error, 3D/codes/HODLR3Dtree.hpp:2645-2662)."""
+        if self.collective_charge is None:
+            raise RuntimeError("no mat_vec_prod has run yet")
+        return self._op.total_error(self.collective_charge, nrows)
 
 
 class initialisation:
@@ -544,6 +584,7 @@ class initialisation:
 
     def mat_vec_prod(self, charge, output=None):
         y = self.op.matvec(charge)
+        self.K.collective_charge = np.array(charge, dtype=np.float64)
         if output is not None:
             output.resize(y.shape, refcheck=False)
             output[...] = y

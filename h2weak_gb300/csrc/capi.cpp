@@ -324,106 +324,144 @@ void record_blocks(h2w_handle *h, const std::vector<NcaProb> &probs, const DBuf<
 void record_lists(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
                   const std::vector<std::vector<int32_t>> &prow, const std::vector<std::vector<int32_t>> &pcol);
 void run_nca_small(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
-                   std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol);
+                   std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol,
+                   std::vector<size_t> &over);
 
 constexpr int64_t NCA_BIG = 8192;  // rows + columns from which a block gets a group of CTAs
+constexpr int NCA_SMALL_CAP = 512;   // pivots one CTA per block holds; larger blocks move to the groups
+
+// Scratch bytes a batch of NCA blocks may take: most of the free device
+// memory (nothing else of the operator is resident while pivots are searched).
+size_t nca_budget() {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return (size_t)8 << 30;
+    }
+    const size_t keep = (size_t)4 << 30;
+    return fr > keep + ((size_t)2 << 30) ? (fr - keep) * 3 / 4 : (size_t)1 << 30;
+}
 
 // Large blocks: groups of CTAs of one cooperative launch per block
-// (ncabig.cu), in batches within the scratch budget.
+// (ncabig.cu), in batches within the scratch budget. There is no built-in
+// rank limit (the reference's loop bound is min(rows, columns),
+// 1D/codes/aca.hpp:363): each block starts with scratch for `start` pivots
+// (at most min(rows, columns)), and a block that fills it runs again with
+// twice as much until it fits; only an explicit rank_cap stops it
+// (H2W_ERR_RANK).
 void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
                  const std::vector<size_t> &big, std::vector<std::vector<int32_t>> &prow,
-                 std::vector<std::vector<int32_t>> &pcol) {
+                 std::vector<std::vector<int32_t>> &pcol, int start = 1024) {
     const double tol = std::pow(10, -1.0 * h->cfg.tol_pow);
-    const int cap = h->cfg.rank_cap > 0 ? h->cfg.rank_cap : 1024;
-    const size_t budget = (size_t)40 << 30;
+    const int cap = h->cfg.rank_cap > 0 ? h->cfg.rank_cap : INT32_MAX;
     KParams kp = h->kparams();
     cudaStream_t st = h->stream;
-    size_t q0 = 0;
-    while (q0 < big.size()) {
-        std::vector<NcaProb> probs;
-        std::vector<int64_t> moff;
-        std::vector<int32_t> idx;
-        size_t scr = 0;
-        int64_t piv = 0, mw = 0;
-        int dcap = 1;
-        size_t q = q0;
-        for (; q < big.size(); ++q) {
-            const size_t p = big[q];
-            const int n1 = (int)R[p].size(), n2 = (int)C[p].size();
-            const int rc = std::min(std::min(n1, n2), cap);
-            const size_t need = (size_t)rc * (size_t)(n1 + n2);
-            if (!probs.empty() && (scr + need) * 8 > budget) break;
-            NcaProb pb{};
-            pb.ri = (int64_t)idx.size();
-            append(idx, R[p].data(), n1);
-            pb.ci = (int64_t)idx.size();
-            append(idx, C[p].data(), n2);
-            pb.u = (int64_t)scr;
-            pb.v = (int64_t)(scr + (size_t)rc * n1);
-            scr += need;
-            pb.piv = piv;
-            piv += rc;
-            pb.n1 = n1;
-            pb.n2 = n2;
-            pb.rcap = rc;
-            probs.push_back(pb);
-            moff.push_back(mw);
-            mw += (n1 + 31) / 32 + (n2 + 31) / 32;
-            dcap = std::max(dcap, rc);
+    std::vector<std::pair<size_t, int>> pend;  // (problem, scratch pivots)
+    for (size_t p : big) {
+        const int mn = (int)std::min(R[p].size(), C[p].size());
+        pend.push_back({p, std::min(std::min(mn, cap), std::max(start, 1))});
+    }
+    while (!pend.empty()) {
+        const size_t budget = nca_budget();
+        std::vector<std::pair<size_t, int>> again;
+        size_t q0 = 0;
+        while (q0 < pend.size()) {
+            std::vector<NcaProb> probs;
+            std::vector<int64_t> moff;
+            std::vector<int32_t> idx;
+            size_t scr = 0;
+            int64_t piv = 0, mw = 0;
+            int dcap = 1;
+            size_t q = q0;
+            for (; q < pend.size(); ++q) {
+                const size_t p = pend[q].first;
+                const int n1 = (int)R[p].size(), n2 = (int)C[p].size();
+                const int rc = pend[q].second;
+                const size_t need = (size_t)rc * (size_t)(n1 + n2);
+                if (!probs.empty() && (scr + need) * 8 > budget) break;
+                NcaProb pb{};
+                pb.ri = (int64_t)idx.size();
+                append(idx, R[p].data(), n1);
+                pb.ci = (int64_t)idx.size();
+                append(idx, C[p].data(), n2);
+                pb.u = (int64_t)scr;
+                pb.v = (int64_t)(scr + (size_t)rc * n1);
+                scr += need;
+                pb.piv = piv;
+                piv += rc;
+                pb.n1 = n1;
+                pb.n2 = n2;
+                pb.rcap = rc;
+                probs.push_back(pb);
+                moff.push_back(mw);
+                mw += (n1 + 31) / 32 + (n2 + 31) / 32;
+                dcap = std::max(dcap, rc);
+            }
+            const int grid = nca_group_grid(dcap);
+            if (grid <= 0) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: no co-resident grid");
+            const int nb = (int)probs.size();
+            const int G = std::max(1, std::min(nb, grid / 32));
+            DBuf<NcaProb> dp;
+            DBuf<int64_t> dm;
+            DBuf<int32_t> di, drank, dpr, dpc, dst, derr;
+            DBuf<uint32_t> dmask;
+            DBuf<unsigned> dbar;
+            DBuf<double> dscr, ddots;
+            DBuf<char> dpartr, dpartc;
+            dp.upload(probs, st);
+            dm.upload(moff, st);
+            di.upload(idx, st);
+            dscr.alloc(scr);
+            dmask.alloc((size_t)mw);
+            drank.alloc((size_t)nb);
+            dpr.alloc((size_t)piv);
+            dpc.alloc((size_t)piv);
+            dst.alloc(1);
+            derr.alloc(1);
+            dbar.alloc((size_t)2 * G);
+            dpartr.alloc(nca_group_part_bytes() * (size_t)grid);
+            dpartc.alloc(nca_group_part_bytes() * (size_t)grid);
+            ddots.alloc((size_t)grid * 2 * dcap + (size_t)G * dcap);
+            CK(cudaMemsetAsync(dst.p, 0, 4, st));
+            CK(cudaMemsetAsync(derr.p, 0, 4, st));
+            CK(cudaMemsetAsync(dbar.p, 0, (size_t)2 * G * sizeof(unsigned), st));
+            CK(launch_nca_group(dp.p, dm.p, nb, G, grid, di.p, kp, tol, dscr.p, dmask.p, drank.p, dpr.p, dpc.p, dst.p,
+                                dbar.p, derr.p, dpartr.p, dpartc.p, ddots.p, dcap, st));
+            std::vector<int32_t> rk((size_t)nb), hpr((size_t)piv), hpc((size_t)piv);
+            int32_t status = 0, errf = 0;
+            CK(cudaMemcpyAsync(rk.data(), drank.p, rk.size() * 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(hpr.data(), dpr.p, hpr.size() * 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(hpc.data(), dpc.p, hpc.size() * 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(&errf, derr.p, 4, cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (errf) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: a group-barrier wait ran out");
+            if (status & 2) throw ApiError(H2W_ERR_ARG, "non-finite kernel entries (coincident points?) in an NCA block");
+            for (int k = 0; k < nb; ++k) {
+                const auto &pq = pend[q0 + (size_t)k];
+                const size_t p = pq.first;
+                if (rk[(size_t)k] < 0) {  // scratch full: again with twice the pivots
+                    const int mn = (int)std::min(R[p].size(), C[p].size());
+                    const int lim = std::min(mn, cap);
+                    if (pq.second >= lim)
+                        throw ApiError(H2W_ERR_RANK, "an NCA block needed more than rank_cap = " +
+                                                         std::to_string(h->cfg.rank_cap) + " pivots");
+                    again.push_back({p, (int)std::min<int64_t>((int64_t)pq.second * 2, lim)});
+                    continue;
+                }
+                prow[p].assign(hpr.begin() + probs[(size_t)k].piv, hpr.begin() + probs[(size_t)k].piv + rk[(size_t)k]);
+                pcol[p].assign(hpc.begin() + probs[(size_t)k].piv, hpc.begin() + probs[(size_t)k].piv + rk[(size_t)k]);
+            }
+            q0 = q;
         }
-        const int grid = nca_group_grid(dcap);
-        if (grid <= 0) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: no co-resident grid");
-        const int nb = (int)probs.size();
-        const int G = std::max(1, std::min(nb, grid / 32));
-        DBuf<NcaProb> dp;
-        DBuf<int64_t> dm;
-        DBuf<int32_t> di, drank, dpr, dpc, dst, derr;
-        DBuf<uint32_t> dmask;
-        DBuf<unsigned> dbar;
-        DBuf<double> dscr, ddots;
-        DBuf<char> dpartr, dpartc;
-        dp.upload(probs, st);
-        dm.upload(moff, st);
-        di.upload(idx, st);
-        dscr.alloc(scr);
-        dmask.alloc((size_t)mw);
-        drank.alloc((size_t)nb);
-        dpr.alloc((size_t)piv);
-        dpc.alloc((size_t)piv);
-        dst.alloc(1);
-        derr.alloc(1);
-        dbar.alloc((size_t)2 * G);
-        dpartr.alloc(nca_group_part_bytes() * (size_t)grid);
-        dpartc.alloc(nca_group_part_bytes() * (size_t)grid);
-        ddots.alloc((size_t)grid * 2 * dcap);
-        CK(cudaMemsetAsync(dst.p, 0, 4, st));
-        CK(cudaMemsetAsync(derr.p, 0, 4, st));
-        CK(cudaMemsetAsync(dbar.p, 0, (size_t)2 * G * sizeof(unsigned), st));
-        CK(launch_nca_group(dp.p, dm.p, nb, G, grid, di.p, kp, tol, dscr.p, dmask.p, drank.p, dpr.p, dpc.p, dst.p,
-                            dbar.p, derr.p, dpartr.p, dpartc.p, ddots.p, dcap, st));
-        std::vector<int32_t> rk((size_t)nb), hpr((size_t)piv), hpc((size_t)piv);
-        int32_t status = 0, errf = 0;
-        CK(cudaMemcpyAsync(rk.data(), drank.p, rk.size() * 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hpr.data(), dpr.p, hpr.size() * 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(hpc.data(), dpc.p, hpc.size() * 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&errf, derr.p, 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (errf) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: a group-barrier wait ran out");
-        if (status & 1) throw ApiError(H2W_ERR_RANK, "an NCA block needed more than rank_cap pivots");
-        if (status & 2) throw ApiError(H2W_ERR_ARG, "non-finite kernel entries (coincident points?) in an NCA block");
-        for (int k = 0; k < nb; ++k) {
-            const size_t p = big[q0 + (size_t)k];
-            prow[p].assign(hpr.begin() + probs[(size_t)k].piv, hpr.begin() + probs[(size_t)k].piv + rk[(size_t)k]);
-            pcol[p].assign(hpc.begin() + probs[(size_t)k].piv, hpc.begin() + probs[(size_t)k].piv + rk[(size_t)k]);
-        }
-        q0 = q;
+        pend.swap(again);
     }
 }
 
 // The NCA pivot search: one CTA per block (nca_kernel) in batches that fit
-// the scratch budget; blocks of NCA_BIG or more rows + columns get groups of
-// CTAs (run_nca_big). H2W_NCA_BIG=0 keeps every block on one CTA.
+// the scratch budget; blocks of NCA_BIG or more rows + columns, and blocks
+// whose rank outgrows one CTA's scratch, get groups of CTAs (run_nca_big).
+// H2W_NCA_BIG=0 keeps every block that fits on one CTA.
 void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
                    std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
     prow.assign(R.size(), {});
@@ -433,11 +471,35 @@ void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, co
     const bool use_big = !(eb && std::string(eb) == "0");
     for (size_t p = 0; p < R.size(); ++p)
         ((use_big && (int64_t)(R[p].size() + C[p].size()) >= NCA_BIG) ? big : small).push_back(p);
-    if (!big.empty()) {
-        run_nca_big(h, R, C, big, prow, pcol);
-        if (h->learn_rec) {  // training data of the large blocks: recorded through the small path's recorder
+    if (!big.empty()) run_nca_big(h, R, C, big, prow, pcol);
+    std::vector<size_t> over;
+    if (!small.empty()) {
+        std::vector<std::vector<int32_t>> Rs, Cs, prs, pcs;
+        const bool all_small = small.size() == R.size();
+        if (!all_small)
+            for (size_t p : small) {
+                Rs.push_back(R[p]);
+                Cs.push_back(C[p]);
+            }
+        const std::vector<std::vector<int32_t>> &RR = all_small ? R : Rs, &CC = all_small ? C : Cs;
+        std::vector<std::vector<int32_t>> &PR = all_small ? prow : prs, &PC = all_small ? pcol : pcs;
+        std::vector<size_t> ov;
+        run_nca_small(h, RR, CC, PR, PC, ov);
+        for (size_t k : ov) over.push_back(all_small ? k : small[k]);
+        if (!all_small)
+            for (size_t k = 0; k < small.size(); ++k) {
+                prow[small[k]] = std::move(prs[k]);
+                pcol[small[k]] = std::move(pcs[k]);
+            }
+        // blocks whose rank outgrew one CTA: the group search from twice that scratch
+        if (!over.empty()) run_nca_big(h, R, C, over, prow, pcol, 2 * NCA_SMALL_CAP);
+    }
+    if (h->learn_rec) {  // training data of the large blocks: recorded through the small path's recorder
+        std::vector<size_t> rec = big;
+        rec.insert(rec.end(), over.begin(), over.end());
+        if (!rec.empty()) {
             std::vector<std::vector<int32_t>> R2, C2, pr2, pc2;
-            for (size_t p : big) {
+            for (size_t p : rec) {
                 R2.push_back(R[p]);
                 C2.push_back(C[p]);
                 pr2.push_back(prow[p]);
@@ -446,31 +508,20 @@ void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, co
             record_lists(h, R2, C2, pr2, pc2);
         }
     }
-    if (small.empty()) return;
-    std::vector<std::vector<int32_t>> Rs, Cs, prs, pcs;
-    const bool all_small = small.size() == R.size();
-    if (!all_small)
-        for (size_t p : small) {
-            Rs.push_back(R[p]);
-            Cs.push_back(C[p]);
-        }
-    const std::vector<std::vector<int32_t>> &RR = all_small ? R : Rs, &CC = all_small ? C : Cs;
-    std::vector<std::vector<int32_t>> &PR = all_small ? prow : prs, &PC = all_small ? pcol : pcs;
-    run_nca_small(h, RR, CC, PR, PC);
-    if (!all_small)
-        for (size_t k = 0; k < small.size(); ++k) {
-            prow[small[k]] = std::move(prs[k]);
-            pcol[small[k]] = std::move(pcs[k]);
-        }
 }
 
+// One CTA per block. over: blocks whose rank outgrew the CTA's scratch
+// (NCA_SMALL_CAP pivots, or rank_cap when smaller); their pivots are left
+// empty for the caller to search with groups of CTAs.
 void run_nca_small(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
-                   std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
+                   std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol,
+                   std::vector<size_t> &over) {
     const size_t np = R.size();
     prow.assign(np, {});
     pcol.assign(np, {});
+    over.clear();
     const double tol = std::pow(10, -1.0 * h->cfg.tol_pow);
-    const int cap = h->cfg.rank_cap > 0 ? h->cfg.rank_cap : 512;
+    const int cap = h->cfg.rank_cap > 0 ? std::min(h->cfg.rank_cap, NCA_SMALL_CAP) : NCA_SMALL_CAP;
     const size_t budget = (size_t)3 << 30;  // scratch bytes per batch
     KParams kp = h->kparams();
     size_t p0 = 0;
@@ -526,14 +577,33 @@ void run_nca_small(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, co
         }
         CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
-        if (status & 1) throw ApiError(H2W_ERR_RANK, "an NCA block needed more than rank_cap pivots");
         if (status & 2) throw ApiError(H2W_ERR_ARG, "non-finite kernel entries (coincident points?) in an NCA block");
+        bool any_over = false;
         for (size_t q = 0; q < probs.size(); ++q) {
             const NcaProb &pb = probs[q];
+            if (rk[q] < 0) {
+                if (h->cfg.rank_cap > 0 && h->cfg.rank_cap <= NCA_SMALL_CAP)
+                    throw ApiError(H2W_ERR_RANK, "an NCA block needed more than rank_cap = " +
+                                                     std::to_string(h->cfg.rank_cap) + " pivots");
+                over.push_back(p0 + q);
+                any_over = true;
+                continue;
+            }
             prow[p0 + q].assign(hpr.begin() + pb.piv, hpr.begin() + pb.piv + rk[q]);
             pcol[p0 + q].assign(hpc.begin() + pb.piv, hpc.begin() + pb.piv + rk[q]);
         }
-        if (h->learn_rec) record_blocks(h, probs, di, prow, pcol, p0);
+        if (h->learn_rec && !any_over) record_blocks(h, probs, di, prow, pcol, p0);
+        else if (h->learn_rec) {  // the finished blocks only (the others are recorded after the group search)
+            std::vector<std::vector<int32_t>> R2, C2, pr2, pc2;
+            for (size_t q = 0; q < probs.size(); ++q)
+                if (rk[q] >= 0) {
+                    R2.push_back(R[p0 + q]);
+                    C2.push_back(C[p0 + q]);
+                    pr2.push_back(prow[p0 + q]);
+                    pc2.push_back(pcol[p0 + q]);
+                }
+            if (!R2.empty()) record_lists(h, R2, C2, pr2, pc2);
+        }
         p0 = p;
     }
 }
@@ -824,7 +894,10 @@ void pair_layout(h2w_handle *h) {
                 }
             } else {
                 for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e) {
-                    if (!t.ilv[(size_t)j][(size_t)e]) continue;
+                    // (H2+H)*: vertex pairs (getUVtTree_sn); H*: every interaction-list
+                    // pair (getUVtTree_nn, 2D/codes/HODLR2Dtree.hpp:971-980,
+                    // 3D/codes/HODLR3Dtree.hpp:2239-2280)
+                    if (!t.ilv[(size_t)j][(size_t)e] && h->cfg.form != H2W_FORM_NONNESTED) continue;
                     P.box.push_back((int32_t)k);
                     P.slot.push_back((int32_t)(e - t.ilp[(size_t)j][(size_t)k]));
                     P.other.push_back(t.il[(size_t)j][(size_t)e]);
@@ -1474,10 +1547,11 @@ void realize_multi(h2w_handle *h, int64_t cap) {
 void build_plan(h2w_handle *h) {
     Tree &t = h->tree;
     const int L = t.nL, dim = t.dim;
-    const bool sn = h->cfg.form == H2W_FORM_SEMINESTED;
-    const bool has_far = dim > 1;
-    const bool has_ver = (dim == 1 && !sn) || (dim > 1 && !sn);
-    const bool has_pairs = sn;
+    const bool nested = h->cfg.form == H2W_FORM_NESTED;
+    // H* (non-nested) has no nested far field: every interaction-list pair is a pair
+    const bool has_far = dim > 1 && h->cfg.form != H2W_FORM_NONNESTED;
+    const bool has_ver = nested;
+    const bool has_pairs = !nested;
     auto pbp = std::make_shared<PlanBuilder>();
     PlanBuilder &pb = *pbp;
     pb.h = h;
@@ -1899,11 +1973,11 @@ void build_plan(h2w_handle *h) {
     h->eta_multi = h->eta_single = -1.0;
 }
 
-// Stored-entry count of the reference (findMemory_n / findMemory_sn).
+// Stored-entry count of the reference (findMemory_n / findMemory_sn / findMemory_nn).
 double storage_entries(h2w_handle *h) {
     const Tree &t = h->tree;
     const int L = t.nL, dim = t.dim;
-    const bool sn = h->cfg.form == H2W_FORM_SEMINESTED;
+    const bool sn = h->cfg.form != H2W_FORM_NESTED;  // per-pair factors: (H2+H)* and H*
     double mem = 0;
     auto nrank = [](const Skel &s, int64_t k) { return (double)s.rank(k); };
     if (dim == 1) {
@@ -1932,7 +2006,9 @@ double storage_entries(h2w_handle *h) {
             }
         return mem;
     }
-    for (int j = 2; j <= L; ++j)
+    // findMemory_nn (2D/codes/HODLR2Dtree.hpp:1307-1328, 3D/codes/HODLR3Dtree.hpp:2561-2583): pairs and near field only
+    const bool nn = h->cfg.form == H2W_FORM_NONNESTED;
+    for (int j = 2; j <= L && !nn; ++j)
         for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
             const Skel &s = h->far[(size_t)j];
             double r = nrank(s, k);
@@ -3060,7 +3136,7 @@ extern "C" {
 int h2w_create(const h2w_config *cfg, h2w_handle **out) {
     if (!cfg || !out) return H2W_ERR_ARG;
     *out = nullptr;
-    if (cfg->dim < 1 || cfg->dim > 3 || (cfg->form != 0 && cfg->form != 1) || (cfg->choice != 0 && cfg->choice != 1) ||
+    if (cfg->dim < 1 || cfg->dim > 3 || (cfg->form != 0 && cfg->form != 1 && cfg->form != 2) || (cfg->form == 2 && cfg->dim == 1) || (cfg->choice != 0 && cfg->choice != 1) ||
         cfg->nlevels < 1 || cfg->tol_pow < 0 || cfg->rank_cap < 0)
         return H2W_ERR_ARG;
     h2w_handle *h = nullptr;
@@ -3252,6 +3328,7 @@ int h2w_get_list(h2w_handle *h, int which, int64_t *ptr, int32_t *val, int64_t *
                     const std::vector<Skel> *S = nullptr;
                     if (op) {
                         if (t.dim == 1) S = farl && h->cfg.form == 0 ? &h->ver : nullptr;
+                        else if (h->cfg.form == H2W_FORM_NONNESTED) S = nullptr;
                         else S = farl ? &h->far : (h->cfg.form == 0 ? &h->ver : nullptr);
                     }
                     if (!S || S->empty() || (*S)[(size_t)j].ptr.empty()) { add(nullptr, 0); break; }
@@ -3266,10 +3343,13 @@ int h2w_get_list(h2w_handle *h, int which, int64_t *ptr, int32_t *val, int64_t *
                     if (t.dim == 1 && j == 0) break;
                     for (int sl = 0; sl < nslot; ++sl) {
                         bool done = false;
-                        if (op && h->cfg.form == 1 && j >= 1) {
+                        if (op && h->cfg.form != H2W_FORM_NESTED && j >= 1) {
+                            // the box's pairs are contiguous, in slot order
                             const Pairs &Pp = h->pairs[(size_t)j];
-                            for (size_t p = 0; p < Pp.box.size(); ++p)
-                                if (Pp.box[p] == k && Pp.slot[p] == sl) {
+                            const size_t p0 = (size_t)(std::lower_bound(Pp.box.begin(), Pp.box.end(), (int32_t)k) -
+                                                       Pp.box.begin());
+                            for (size_t p = p0; p < Pp.box.size() && Pp.box[p] == k; ++p)
+                                if (Pp.slot[p] == sl) {
                                     const auto &src = which == H2W_LIST_SN_ROW ? Pp.row : Pp.col;
                                     add(src.data() + Pp.ptr[p], Pp.ptr[p + 1] - Pp.ptr[p]);
                                     done = true;
@@ -3311,21 +3391,23 @@ int h2w_assemble(h2w_handle *h, int mode) {
         require_tree(h);
         if (h->cfg.device < 0) throw ApiError(H2W_ERR_STATE, "host-only handle (device < 0) cannot assemble");
         const Tree &t = h->tree;
-        const bool sn = h->cfg.form == H2W_FORM_SEMINESTED;
+        // (H2+H)* and H* both keep per-pair factors; H* has no nested far field
+        const bool sn = h->cfg.form != H2W_FORM_NESTED;
+        const bool nn = h->cfg.form == H2W_FORM_NONNESTED;
         h->phases.clear();
         h->has_op = false;
         if (mode == H2W_ASSEMBLE_LEARNED && !h->d_mlp.p)
             throw ApiError(H2W_ERR_STATE, "learned assembly needs a model (h2w_learn_set_model)");
         h->learned = mode == H2W_ASSEMBLE_LEARNED;
         if (mode == H2W_ASSEMBLE_NCA || mode == H2W_ASSEMBLE_LEARNED) {
-            if (t.dim > 1) nca_far(h);
+            if (t.dim > 1 && !nn) nca_far(h);
             if (!sn) nca_ver(h);
             if (sn) {
                 pair_layout(h);
                 nca_pairs(h);
             }
         } else if (mode == H2W_ASSEMBLE_IMPORT) {
-            if (t.dim > 1) {
+            if (t.dim > 1 && !nn) {
                 if (!h->imp[H2W_LIST_FAR_CHECK] || !h->imp[H2W_LIST_FAR_CHARGE])
                     throw ApiError(H2W_ERR_STATE, "far pivots not imported");
                 import_skel(h, H2W_LIST_FAR_CHECK, H2W_LIST_FAR_CHARGE, h->far, 2);
@@ -3348,6 +3430,7 @@ int h2w_assemble(h2w_handle *h, int mode) {
         } else {
             throw ApiError(H2W_ERR_ARG, "unknown assembly mode");
         }
+        if (nn) h->far.clear();
         if (t.dim == 1 || sn) {
             if (h->far.empty()) {
                 h->far.assign((size_t)t.nL + 1, Skel{});
@@ -4282,6 +4365,220 @@ int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, in
         CK(launch_dense_matvec(h->kparams(), N, dx, dy, row0, nrows, st));
         if (where == H2W_HOST) CK(cudaMemcpyAsync(y, by.p, (size_t)nrows * 8, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        return H2W_OK;
+    });
+}
+
+// ------------------------------------------------------- operator files ---
+// An operator file holds what determines the compressed operator: the
+// configuration, the points, and every pivot list of the NCA (the skeletons
+// of each level and the pair pivots), little-endian, closed by an FNV-1a
+// checksum of everything before it. Opening rebuilds the tree from the
+// points, imports the pivots and forms the operator from them on the GPU
+// (H2W_ASSEMBLE_IMPORT): the pivot search, the costly part of assembly, is
+// skipped, and the operator is bitwise the one that was saved.
+}  // extern "C"
+
+namespace {
+constexpr char H2W_OPFILE_MAGIC[8] = {'H', '2', 'W', 'O', 'P', 'E', 'R', '1'};
+
+struct OpWriter {
+    std::vector<unsigned char> buf;
+    template <class T> void put(const T &v) {
+        const unsigned char *c = reinterpret_cast<const unsigned char *>(&v);
+        buf.insert(buf.end(), c, c + sizeof(T));
+    }
+    template <class T> void put_n(const T *v, size_t n) {
+        const unsigned char *c = reinterpret_cast<const unsigned char *>(v);
+        buf.insert(buf.end(), c, c + n * sizeof(T));
+    }
+};
+struct OpReader {
+    const std::vector<unsigned char> &buf;
+    size_t pos = 0, end;
+    template <class T> T get() {
+        if (pos + sizeof(T) > end) throw ApiError(H2W_ERR_ARG, "operator file is truncated");
+        T v;
+        std::memcpy(&v, buf.data() + pos, sizeof(T));
+        pos += sizeof(T);
+        return v;
+    }
+    template <class T> void get_n(T *v, size_t n) {
+        if (n > (end - pos) / sizeof(T)) throw ApiError(H2W_ERR_ARG, "operator file is truncated");
+        std::memcpy(v, buf.data() + pos, n * sizeof(T));
+        pos += n * sizeof(T);
+    }
+};
+uint64_t fnv1a(const unsigned char *p, size_t n) {
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+}  // namespace
+
+extern "C" {
+
+int h2w_get_config(h2w_handle *h, h2w_config *out) {
+    return guarded(h, [&] {
+        if (!out) throw ApiError(H2W_ERR_ARG, "null output");
+        *out = h->cfg;
+        return H2W_OK;
+    });
+}
+
+int h2w_save_operator(h2w_handle *h, const char *path) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!path) throw ApiError(H2W_ERR_ARG, "null path");
+        OpWriter w;
+        w.put_n(H2W_OPFILE_MAGIC, 8);
+        const h2w_config &c = h->cfg;
+        for (int32_t v : {c.dim, c.form, c.choice, c.tol_pow, c.nlevels, c.rank_cap}) w.put(v);
+        w.put(c.kernel_n);
+        w.put(c.diag_n);
+        const int64_t N = h->tree.N;
+        w.put(N);
+        w.put_n(h->pts.data(), h->pts.size());
+        std::vector<int32_t> lists;
+        for (int which = H2W_LIST_FAR_CHECK; which <= H2W_LIST_SN_COL; ++which) lists.push_back(which);
+        w.put((int32_t)lists.size());
+        for (int which : lists) {
+            int64_t np = 0, nv = 0;
+            if (h2w_get_list(h, which, nullptr, nullptr, &np, &nv) != H2W_OK) throw ApiError(H2W_ERR_STATE, h->err);
+            std::vector<int64_t> ptr((size_t)np);
+            std::vector<int32_t> val((size_t)std::max<int64_t>(nv, 1));
+            if (h2w_get_list(h, which, ptr.data(), val.data(), nullptr, nullptr) != H2W_OK)
+                throw ApiError(H2W_ERR_STATE, h->err);
+            w.put((int32_t)which);
+            w.put(np);
+            w.put_n(ptr.data(), ptr.size());
+            w.put(nv);
+            w.put_n(val.data(), (size_t)nv);
+        }
+        w.put(h->storage);
+        w.put(fnv1a(w.buf.data(), w.buf.size()));
+        FILE *f = std::fopen(path, "wb");
+        if (!f) throw ApiError(H2W_ERR_ARG, std::string("cannot write ") + path);
+        const size_t n = std::fwrite(w.buf.data(), 1, w.buf.size(), f);
+        const bool ok = n == w.buf.size() && std::fclose(f) == 0;
+        if (!ok) throw ApiError(H2W_ERR_ARG, std::string("write to ") + path + " failed");
+        return H2W_OK;
+    });
+}
+
+int h2w_open_operator(const char *path, int device, h2w_handle **out) {
+    if (!path || !out) return H2W_ERR_ARG;
+    *out = nullptr;
+    std::vector<unsigned char> buf;
+    {
+        FILE *f = std::fopen(path, "rb");
+        if (!f) return H2W_ERR_ARG;
+        unsigned char tmp[1 << 16];
+        size_t n;
+        while ((n = std::fread(tmp, 1, sizeof(tmp), f)) > 0) buf.insert(buf.end(), tmp, tmp + n);
+        std::fclose(f);
+    }
+    if (buf.size() < 8 + 8 || std::memcmp(buf.data(), H2W_OPFILE_MAGIC, 8) != 0) return H2W_ERR_ARG;
+    uint64_t sum;
+    std::memcpy(&sum, buf.data() + buf.size() - 8, 8);
+    if (fnv1a(buf.data(), buf.size() - 8) != sum) return H2W_ERR_ARG;
+    OpReader r{buf, 8, buf.size() - 8};
+    h2w_config c{};
+    try {
+        c.dim = r.get<int32_t>();
+        c.form = r.get<int32_t>();
+        c.choice = r.get<int32_t>();
+        c.tol_pow = r.get<int32_t>();
+        c.nlevels = r.get<int32_t>();
+        c.rank_cap = r.get<int32_t>();
+        c.kernel_n = r.get<int64_t>();
+        c.diag_n = r.get<int64_t>();
+    } catch (const ApiError &) {
+        return H2W_ERR_ARG;
+    }
+    c.device = device;
+    h2w_handle *h = nullptr;
+    int rc = h2w_create(&c, &h);
+    if (rc != H2W_OK) return rc;
+    rc = guarded(h, [&] {
+        const int64_t N = r.get<int64_t>();
+        if (N < 1 || N > INT32_MAX - 1) throw ApiError(H2W_ERR_ARG, "operator file: bad point count");
+        std::vector<double> pts((size_t)N * (size_t)c.dim);
+        r.get_n(pts.data(), pts.size());
+        if (h2w_set_points(h, pts.data(), N) != H2W_OK || h2w_build_tree(h) != H2W_OK) throw ApiError(H2W_ERR_ARG, h->err);
+        const int32_t nl = r.get<int32_t>();
+        for (int32_t q = 0; q < nl; ++q) {
+            const int32_t which = r.get<int32_t>();
+            const int64_t np = r.get<int64_t>();
+            if (np < 1 || np > (int64_t)buf.size()) throw ApiError(H2W_ERR_ARG, "operator file: bad list");
+            std::vector<int64_t> ptr((size_t)np);
+            r.get_n(ptr.data(), ptr.size());
+            const int64_t nv = r.get<int64_t>();
+            if (nv < 0 || nv != ptr.back() || nv > (int64_t)buf.size()) throw ApiError(H2W_ERR_ARG, "operator file: bad list");
+            std::vector<int32_t> val((size_t)std::max<int64_t>(nv, 1));
+            r.get_n(val.data(), (size_t)nv);
+            for (int64_t i = 1; i < np; ++i)
+                if (ptr[(size_t)i] < ptr[(size_t)i - 1]) throw ApiError(H2W_ERR_ARG, "operator file: bad list");
+            if (h2w_import_list(h, which, ptr.data(), val.data(), np) != H2W_OK) throw ApiError(H2W_ERR_ARG, h->err);
+        }
+        const double storage = r.get<double>();
+        if (device >= 0) {
+            if (h2w_assemble(h, H2W_ASSEMBLE_IMPORT) != H2W_OK) throw ApiError(H2W_ERR_ARG, h->err);
+            if (h->storage != storage)
+                throw ApiError(H2W_ERR_ARG, "operator file: the formed operator's storage differs from the saved one");
+        }
+        return H2W_OK;
+    });
+    if (rc != H2W_OK) {
+        h2w_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return H2W_OK;
+}
+
+int h2w_total_error(h2w_handle *h, const double *x, int64_t nrows, int where, double *err) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!x || !err || (where != H2W_HOST && where != H2W_DEVICE)) throw ApiError(H2W_ERR_ARG, "bad error arguments");
+        const int64_t N = h->tree.N;
+        cudaStream_t st = h->stream;
+        DBuf<double> bx, byh, byd;
+        DBuf<int64_t> brows;
+        const double *dx = x;
+        if (where == H2W_HOST) {
+            bx.alloc((size_t)N);
+            CK(cudaMemcpyAsync(bx.p, x, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+            dx = bx.p;
+        }
+        byh.alloc((size_t)N);
+        run_matvec_f64(h, dx, byh.p, st);
+        const bool all = nrows <= 0 || nrows >= N;
+        const int64_t nr = all ? N : nrows;
+        std::vector<int64_t> rows((size_t)nr);
+        for (int64_t i = 0; i < nr; ++i) rows[(size_t)i] = all ? i : (int64_t)((__int128)i * N / nr);
+        byd.alloc((size_t)nr);
+        if (all) {
+            CK(launch_dense_matvec(h->kparams(), N, dx, byd.p, 0, N, st));
+        } else {
+            brows.upload(rows, st);
+            CK(launch_dense_rows(h->kparams(), N, dx, brows.p, nr, byd.p, st));
+        }
+        std::vector<double> yh((size_t)N), yd((size_t)nr);
+        CK(cudaMemcpyAsync(yh.data(), byh.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(yd.data(), byd.p, (size_t)nr * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        check_device_error(h);
+        long double num = 0.0L, den = 0.0L;
+        for (int64_t i = 0; i < nr; ++i) {
+            const long double d = (long double)yd[(size_t)i] - (long double)yh[(size_t)rows[(size_t)i]];
+            num += d * d;
+            den += (long double)yd[(size_t)i] * (long double)yd[(size_t)i];
+        }
+        *err = den > 0.0L ? (double)std::sqrt(num / den) : 0.0;
         return H2W_OK;
     });
 }

@@ -73,7 +73,8 @@ __device__ __forceinline__ bool bit_get(const uint32_t *m, int i) { return (m[i 
 // first row with a non-negligible entry, column pivot = first largest |.|
 // among unused columns of the residual row, row pivot = first largest |.|
 // among unused rows of the residual column, stop when ||u|| ||v|| <= tol
-// normS or the rank reaches min(n1, n2). Residual rows and columns are
+// normS or the rank reaches min(n1, n2) (a block whose rank reaches its
+// scratch capacity rcap first reports -rcap). Residual rows and columns are
 // formed entry by entry in pivot order with separate multiply and subtract,
 // so for identical entries they are bitwise those of the reference; norms
 // and dot products are tree reductions (they only enter the stopping test).
@@ -163,9 +164,10 @@ __global__ void __launch_bounds__(NCA_THREADS) nca_kernel(const NcaProb *__restr
     ri = nri;
     __syncthreads();
 
+    bool over = false;  // the block needs more pivots than its scratch holds
     while (nu * nv > tol * normS && rank < mn) {
         if (rank >= rcap) {
-            if (tid == 0) atomicOr(status, 1);
+            over = true;
             break;
         }
         if (ri < 0 || ri >= n1) {  // no finite candidate row
@@ -266,7 +268,8 @@ __global__ void __launch_bounds__(NCA_THREADS) nca_kernel(const NcaProb *__restr
         ri = nri;
         __syncthreads();
     }
-    if (tid == 0) rank_out[blockIdx.x] = rank;
+    // an overflowing block reports -rank: the host runs it again with more scratch
+    if (tid == 0) rank_out[blockIdx.x] = over ? -rank : rank;
 }
 
 cudaError_t launch_nca(const NcaProb *probs, int nprob, const int32_t *idx, const KParams &kp, double tol,
@@ -890,6 +893,25 @@ __global__ void dense_kernel(KParams kp, int64_t N, const double *__restrict__ x
     for (int64_t j = threadIdx.x; j < N; j += blockDim.x) acc += kentry(kp, (int)r, (int)j) * x[j];
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) y[blockIdx.x] = acc;
+}
+// Dense FP64 rows y[i] = sum_j K(rows[i], j) x[j] for a list of rows.
+__global__ void dense_rows_kernel(KParams kp, int64_t N, const double *__restrict__ x,
+                                  const int64_t *__restrict__ rows, double *__restrict__ y) {
+    __shared__ double sh[32];
+    const int64_t r = rows[blockIdx.x];
+    double acc = 0.0;
+    for (int64_t j = threadIdx.x; j < N; j += blockDim.x) acc += kentry(kp, (int)r, (int)j) * x[j];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) y[blockIdx.x] = acc;
+}
+cudaError_t launch_dense_rows(const KParams &kp, int64_t N, const double *x, const int64_t *rows, int64_t nrows,
+                              double *y, cudaStream_t st) {
+    for (int64_t b = 0; b < nrows; b += 2147483647LL) {
+        int64_t nb = nrows - b < 2147483647LL ? nrows - b : 2147483647LL;
+        dense_rows_kernel<<<(unsigned)nb, 256, 0, st>>>(kp, N, x, rows + b, y + b);
+        count_launch();
+    }
+    return cudaGetLastError();
 }
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0, int64_t nrows,
                                 cudaStream_t st) {

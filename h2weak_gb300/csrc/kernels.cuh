@@ -37,7 +37,9 @@ cudaError_t launch_nca(const NcaProb *probs, int nprob, const int32_t *idx, cons
 // The NCA for large blocks: the CTAs of one cooperative launch in G groups,
 // each group on one block at a time (same pivots as launch_nca). moff: per
 // block, offset of its row+column pivot masks (uint32 words) in masks;
-// partial buffers of nca_group_part_bytes() x grid each; dots: grid x 2*dcap.
+// partial buffers of nca_group_part_bytes() x grid each; dots: grid x 2*dcap
+// + G x dcap doubles (dcap >= every block's rcap). A block whose rank reaches
+// its rcap reports -rank in rank (launch_nca does the same).
 int nca_group_grid(int dcap);
 size_t nca_group_part_bytes();
 cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int nprob, int G, int grid,
@@ -89,6 +91,9 @@ constexpr int MR_XS_ELEMS = 2048;     // gathered source width per multi-vector 
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,
                                 int64_t nrows, cudaStream_t st);
+// The same for a list of rows (each in [0, N)): y[i] = sum_j K(rows[i], j) x[j].
+cudaError_t launch_dense_rows(const KParams &kp, int64_t N, const double *x, const int64_t *rows, int64_t nrows,
+                              double *y, cudaStream_t st);
 
 // GMRES building blocks (FP64). V is column-major N x (m+1).
 struct GmresDev {

@@ -11,6 +11,13 @@
 // lowest index among equal magnitudes, and every CTA of the group reduces the
 // per-CTA partials in the same CTA order, so all CTAs agree on every pivot
 // and on the stopping test without further communication.
+//
+// No rank limit is built in: the residual updates stream the coefficients of
+// the kept terms through a fixed shared-memory chunk (the subtraction order
+// stays the pivot order), and a block whose rank reaches the capacity of its
+// scratch (rcap terms of U and V) stops and reports -rank, so that the host
+// runs it again with more scratch (the search is deterministic: the same
+// pivots come out, the earlier ones unchanged).
 #include <climits>
 
 #include "entry.cuh"
@@ -18,6 +25,7 @@
 namespace h2w {
 
 constexpr int NG_THREADS = 256;
+constexpr int NG_COEF = 1024;  // coefficients of kept terms staged per chunk (8 KB)
 
 struct NgPart {             // per-CTA partials of one pass
     double v, s;            // best |value| (argmax), sum of squares
@@ -94,15 +102,16 @@ __global__ void __launch_bounds__(NG_THREADS)
                      uint32_t *__restrict__ masks, int32_t *__restrict__ rank_out, int32_t *__restrict__ prow,
                      int32_t *__restrict__ pcol, int32_t *status, unsigned *bars, int32_t *err, NgPart *prow_part,
                      NgPart *pcol_part, double *dots, int dcap) {
-    extern __shared__ double ng_coef[];  // dcap doubles
+    __shared__ double ng_coef[NG_COEF];
     __shared__ double shv[32], shs[32];
     __shared__ int shi[32];
     const int g = blockIdx.x % G, gi = blockIdx.x / G;
     const int S = (gridDim.x - g + G - 1) / G;  // members of group g
     unsigned *bar = bars + 2 * g;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int cstride = S * NG_THREADS;
     const double tiny = 1e-36;
+    double *gterm = dots + (size_t)gridDim.x * 2 * dcap + (size_t)g * dcap;  // the group's normS terms
     for (int b = g; b < nprob; b += G) {
         const NcaProb pb = probs[b];
         const int n1 = pb.n1, n2 = pb.n2, rcap = pb.rcap;
@@ -174,30 +183,40 @@ __global__ void __launch_bounds__(NG_THREADS)
         }
         int rank = 1;
         double normS = 0.0;
+        bool over = false;
         ng_barrier(bar, S, err);
         while (nu * nv > tol * normS && rank < mn) {
             if (rank >= rcap) {
-                if (gi == 0 && tid == 0) atomicOr(status, 1);
+                over = true;
                 break;
             }
             if (ri < 0 || ri >= n1) {
                 if (gi == 0 && tid == 0) atomicOr(status, 2);
                 break;
             }
-            // residual row ri over this CTA's columns; column pivot
-            for (int l = tid; l < rank; l += NG_THREADS) ng_coef[l] = U[(size_t)l * n1 + ri];
-            __syncthreads();
+            // residual row ri over this CTA's columns (kept terms subtracted in
+            // pivot order, chunk by chunk); column pivot
             double *Vr = V + (size_t)rank * n2;
             double v0 = -1.0, vs = 0.0;
             int i0 = INT_MAX;
-            for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) {
-                double v = kentry(kp, I[ri], J[s2]);
-                for (int l = 0; l < rank; ++l) v = __dsub_rn(v, __dmul_rn(ng_coef[l], V[(size_t)l * n2 + s2]));
-                Vr[s2] = v;
-                vs += v * v;
-                if (!ng_bit(cm, s2)) {
-                    const double a = fabs(v);
-                    if (ng_better(a, s2, v0, i0)) { v0 = a; i0 = s2; }
+            for (int l0 = 0; l0 < rank; l0 += NG_COEF) {
+                const int l1 = rank - l0 < NG_COEF ? rank : l0 + NG_COEF;
+                const bool last = l1 == rank;
+                __syncthreads();
+                for (int l = l0 + tid; l < l1; l += NG_THREADS) ng_coef[l - l0] = U[(size_t)l * n1 + ri];
+                __syncthreads();
+                for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) {
+                    double v = l0 == 0 ? kentry(kp, I[ri], J[s2]) : Vr[s2];
+                    for (int l = l0; l < l1; ++l)
+                        v = __dsub_rn(v, __dmul_rn(ng_coef[l - l0], V[(size_t)l * n2 + s2]));
+                    Vr[s2] = v;
+                    if (last) {
+                        vs += v * v;
+                        if (!ng_bit(cm, s2)) {
+                            const double a = fabs(v);
+                            if (ng_better(a, s2, v0, i0)) { v0 = a; i0 = s2; }
+                        }
+                    }
                 }
             }
             ng_cta_part(v0, i0, vs, prow_part + blockIdx.x, shv, shi, shs);
@@ -210,21 +229,33 @@ __global__ void __launch_bounds__(NG_THREADS)
             ci = bi;
             nv = sqrt(ss);
             const double piv = Vr[ci];
-            // residual column ci over this CTA's rows; next row pivot
-            for (int l = tid; l < rank; l += NG_THREADS) ng_coef[l] = V[(size_t)l * n2 + ci];
-            __syncthreads();
+            // residual column ci over this CTA's rows; next row pivot. The
+            // unscaled residual is kept in Ur across chunks, scaled by the
+            // pivot after the last one.
             double *Ur = U + (size_t)rank * n1;
             double u0 = -1.0, us = 0.0;
             int j0 = INT_MAX;
-            for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) {
-                double c = kentry(kp, I[t], J[ci]);
-                for (int l = 0; l < rank; ++l) c = __dsub_rn(c, __dmul_rn(ng_coef[l], U[(size_t)l * n1 + t]));
-                const double u = __ddiv_rn(c, piv);
-                Ur[t] = u;
-                us += u * u;
-                if (t != ri && !ng_bit(rm, t)) {
-                    const double a = fabs(c);
-                    if (ng_better(a, t, u0, j0)) { u0 = a; j0 = t; }
+            for (int l0 = 0; l0 < rank; l0 += NG_COEF) {
+                const int l1 = rank - l0 < NG_COEF ? rank : l0 + NG_COEF;
+                const bool last = l1 == rank;
+                __syncthreads();
+                for (int l = l0 + tid; l < l1; l += NG_THREADS) ng_coef[l - l0] = V[(size_t)l * n2 + ci];
+                __syncthreads();
+                for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) {
+                    double c = l0 == 0 ? kentry(kp, I[t], J[ci]) : Ur[t];
+                    for (int l = l0; l < l1; ++l)
+                        c = __dsub_rn(c, __dmul_rn(ng_coef[l - l0], U[(size_t)l * n1 + t]));
+                    if (!last) {
+                        Ur[t] = c;
+                        continue;
+                    }
+                    const double u = __ddiv_rn(c, piv);
+                    Ur[t] = u;
+                    us += u * u;
+                    if (t != ri && !ng_bit(rm, t)) {
+                        const double a = fabs(c);
+                        if (ng_better(a, t, u0, j0)) { u0 = a; j0 = t; }
+                    }
                 }
             }
             ng_cta_part(u0, j0, us, pcol_part + blockIdx.x, shv, shi, shs);
@@ -240,44 +271,45 @@ __global__ void __launch_bounds__(NG_THREADS)
                 cm[ci >> 5] |= 1u << (ci & 31);
             }
             ++rank;
-            // normS: partial dots of every kept u, v with the new ones (the new term included)
+            // normS: this CTA's partial dots of every kept u, v with the new
+            // ones (the new term included), one warp per term, over the CTA's
+            // rows and columns in a fixed order
             double *dme = dots + (size_t)blockIdx.x * 2 * dcap;
-            for (int l = 0; l < rank; ++l) {
+            for (int l = warp; l < rank; l += NG_THREADS / 32) {
                 const double *Ul = U + (size_t)l * n1, *Vl = V + (size_t)l * n2;
                 double du = 0.0, dv = 0.0;
-                for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) du += Ul[t] * Ur[t];
-                for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) dv += Vl[s2] * Vr[s2];
+                for (int t0 = gi * NG_THREADS; t0 < n1; t0 += cstride)
+                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n1; t += 32) du += Ul[t] * Ur[t];
+                for (int t0 = gi * NG_THREADS; t0 < n2; t0 += cstride)
+                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n2; t += 32) dv += Vl[t] * Vr[t];
                 for (int o = 16; o > 0; o >>= 1) {
                     du += __shfl_xor_sync(0xffffffffu, du, o);
                     dv += __shfl_xor_sync(0xffffffffu, dv, o);
                 }
-                if ((tid & 31) == 0) { shv[tid >> 5] = du; shs[tid >> 5] = dv; }
-                __syncthreads();
-                if (tid == 0) {
-                    double a = 0.0, c = 0.0;
-                    for (int q = 0; q < NG_THREADS / 32; ++q) { a += shv[q]; c += shs[q]; }
-                    dme[2 * l] = a;
-                    dme[2 * l + 1] = c;
+                if (lane == 0) {
+                    dme[2 * l] = du;
+                    dme[2 * l + 1] = dv;
                 }
-                __syncthreads();
+            }
+            ng_barrier(bar, S, err);
+            // 2 |<U_l, u><V_l, v>| per term: the members' partials summed in
+            // member order, the terms split over the group's CTAs
+            for (int l = gi * NG_THREADS + tid; l < rank; l += cstride) {
+                double du = 0.0, dv = 0.0;
+                for (int k = 0; k < S; ++k) {
+                    const double *dk = dots + (size_t)(g + k * G) * 2 * dcap;
+                    du += dk[2 * l];
+                    dv += dk[2 * l + 1];
+                }
+                gterm[l] = 2.0 * fabs(du * dv);
             }
             ng_barrier(bar, S, err);
             {
-                // 2 sum_l |<U_l, u><V_l, v>|: the terms split over the CTA's threads
-                // (each term summed over the members in member order), then one
-                // block sum in a fixed order, so every CTA gets the same normS
+                // every CTA sums the terms in the same fixed order: the same normS everywhere
                 double part = 0.0;
-                for (int l = tid; l < rank; l += NG_THREADS) {
-                    double du = 0.0, dv = 0.0;
-                    for (int k = 0; k < S; ++k) {
-                        const double *dk = dots + (size_t)(g + k * G) * 2 * dcap;
-                        du += dk[2 * l];
-                        dv += dk[2 * l + 1];
-                    }
-                    part += 2.0 * fabs(du * dv);
-                }
+                for (int l = tid; l < rank; l += NG_THREADS) part += gterm[l];
                 for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-                if ((tid & 31) == 0) shs[tid >> 5] = part;
+                if (lane == 0) shs[warp] = part;
                 __syncthreads();
                 double ns = normS * normS + (nu * nv) * (nu * nv);
                 for (int q = 0; q < NG_THREADS / 32; ++q) ns += shs[q];
@@ -285,9 +317,10 @@ __global__ void __launch_bounds__(NG_THREADS)
                 __syncthreads();
             }
             ri = nri;
-            ng_barrier(bar, S, err);  // the dots are read before the next step overwrites them
+            ng_barrier(bar, S, err);  // the terms are read before the next step overwrites them
         }
-        if (gi == 0 && tid == 0) rank_out[b] = rank;
+        // an overflowing block reports -rank: the host runs it again with more scratch
+        if (gi == 0 && tid == 0) rank_out[b] = over ? -rank : rank;
         ng_barrier(bar, S, err);
     }
 }
@@ -304,10 +337,9 @@ static int ng_sms() {
 }
 
 int nca_group_grid(int dcap) {
+    (void)dcap;  // shared memory no longer depends on the rank
     int per_sm = 0;
-    const size_t sm = (size_t)dcap * 8;
-    if (sm > 48 * 1024) cudaFuncSetAttribute(nca_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nca_group_kernel, NG_THREADS, sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nca_group_kernel, NG_THREADS, 0);
     return per_sm > 0 ? ng_sms() * per_sm : 0;
 }
 
@@ -323,7 +355,7 @@ cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int npro
                     (void *)&status, (void *)&bars, (void *)&err, (void *)&pr,   (void *)&pc,   (void *)&dots,
                     (void *)&dcap};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)nca_group_kernel, dim3(grid), dim3(NG_THREADS), args,
-                                                (size_t)dcap * 8, st);
+                                                0, st);
     count_launch();
     return e;
 }

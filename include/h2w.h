@@ -30,7 +30,10 @@ enum {
     H2W_ERR_STATE = -6       /* call needs an earlier step (tree, assembly) */
 };
 
-enum { H2W_FORM_NESTED = 0, H2W_FORM_SEMINESTED = 1 };           /* -DUSE_nHODLRdD / -DUSE_snHODLRdD */
+/* -DUSE_nHODLRdD (H2*), -DUSE_snHODLRdD ((H2+H)*), -DUSE_HODLRdD (H*, non-nested:
+ * every interaction-list pair compressed on its own, 2D and 3D only,
+ * 2D/codes/matvec.hpp:136-172, 3D/codes/matvec.hpp:138-180) */
+enum { H2W_FORM_NESTED = 0, H2W_FORM_SEMINESTED = 1, H2W_FORM_NONNESTED = 2 };
 enum { H2W_KERNEL_IE = 0, H2W_KERNEL_RBF = 1 };                 /* reference "choice" */
 enum { H2W_ASSEMBLE_NCA = 0, H2W_ASSEMBLE_IMPORT = 1, H2W_ASSEMBLE_LEARNED = 2 };
 /* FP64: FP64 operator and arithmetic. FP32: FP32 operator copy and arithmetic.
@@ -353,6 +356,28 @@ int64_t h2w_launch_count(void);
 /* Dense FP64 product with the exact kernel matrix (getTruePoten,
  * 1D/codes/HODLR1Dtree.hpp:590-604), on the GPU, rows [row0, row0 + nrows). */
 int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, int64_t nrows, int where);
+/* Operator files (no counterpart in the reference, which re-assembles on
+ * every run, 3D/codes/main.cpp:21-25). h2w_save_operator writes the
+ * configuration, the points and every NCA pivot list of an assembled handle,
+ * closed by a checksum. h2w_open_operator creates a handle on `device` from
+ * such a file, rebuilds the tree and forms the operator from the saved pivots
+ * (H2W_ASSEMBLE_IMPORT: the pivot search is skipped; the operator is bitwise
+ * the saved one, its storage count checked); device = -1 gives a host-only
+ * handle with the points, tree and imported lists. A missing, truncated or
+ * corrupted file is refused with H2W_ERR_ARG. */
+int h2w_save_operator(h2w_handle *h, const char *path);
+/* The configuration a handle was created with (e.g. one opened from a file). */
+int h2w_get_config(h2w_handle *h, h2w_config *out);
+int h2w_open_operator(const char *path, int device, h2w_handle **out);
+
+/* Relative error of the compressed FP64 product against the exact dense
+ * product on the same vector, ||y_dense - A x|| / ||y_dense||: the reference's
+ * compute_total_error (3D/codes/HODLR3Dtree.hpp:2645-2662, 2D/codes/HODLR2Dtree.hpp:1347,
+ * on the charge of the last mat_vec_prod), on the GPU.
+ * nrows <= 0 or >= N: every row (O(N^2) kernel entries, as the reference);
+ * otherwise nrows rows evenly spaced in original point order
+ * (row i * N / nrows), the sampled form for large N. x host or device (where). */
+int h2w_total_error(h2w_handle *h, const double *x, int64_t nrows, int where, double *err);
 
 #ifdef __cplusplus
 }

@@ -703,8 +703,9 @@ struct Oracle {
                 b.Ac.assign(n, Mat());
                 b.Ar.assign(n, Mat());
             }
-        // far field, bottom-up NCA: getNodes + getNodes_incoming_box (2D :552-597, 3D :1872-1939)
-        for (int j = nL; j >= 2; --j) {
+        // far field, bottom-up NCA: getNodes + getNodes_incoming_box (2D :552-597, 3D :1872-1939);
+        // H* (form 2) has no nested far field (2D/codes/matvec.hpp:136-160)
+        for (int j = nL; j >= 2 && form != 2; --j) {
             auto &lv = T[(size_t)j];
 #pragma omp parallel for schedule(dynamic, 1)
             for (long k = 0; k < (long)lv.size(); ++k) {
@@ -727,7 +728,7 @@ struct Oracle {
             }
         }
         // M2L far: assemble_M2L_far (2D :655-675, 3D :1978-1998)
-        for (int j = 2; j <= nL; ++j) {
+        for (int j = 2; j <= nL && form != 2; ++j) {
             auto &lv = T[(size_t)j];
 #pragma omp parallel for schedule(dynamic, 4)
             for (long k = 0; k < (long)lv.size(); ++k) {
@@ -776,14 +777,15 @@ struct Oracle {
                 }
             }
         } else {
-            // semi-nested vertex pairs: getUVtTree_sn + assembleAcAr_sn (2D :953-1005, 3D :2250-2321)
+            // semi-nested vertex pairs: getUVtTree_sn + assembleAcAr_sn (2D :953-1005, 3D :2250-2321);
+            // H*: every interaction-list pair, getUVtTree_nn + assembleAcAr_nn (2D :971-1021, 3D :2239-2321)
             for (int j = 1; j <= nL; ++j) {
                 auto &lv = T[(size_t)j];
 #pragma omp parallel for schedule(dynamic, 1)
                 for (long k = 0; k < (long)lv.size(); ++k) {
                     Box &b = lv[(size_t)k];
                     for (size_t i = 0; i < b.il.size(); ++i) {
-                        if (!b.ilv[i]) continue;
+                        if (!b.ilv[i] && form == 1) continue;
                         const auto &qp = lv[(size_t)b.il[i]].pts;
                         ACA a = aca(b.pts, qp, false, false);
                         b.Lc[i] = a.L;
@@ -895,7 +897,49 @@ struct Oracle {
         reorder(yp, y);
     }
 
+    // H* (USE_HODLRdD): evaluateFarField_nn (2D :1053-1071, 3D :2353-2373) sets every
+    // box's potential from its pairs, evaluate_NearField adds the leaf blocks,
+    // collect_all_potentials_nn (2D :1175-1189, 3D :2473-2487) sums the levels.
+    void matvec_nn(const double *x, double *y) {
+        assign_charges(x);
+        for (int j = 1; j <= nL; ++j) {
+            auto &lv = T[(size_t)j];
+#pragma omp parallel for schedule(dynamic, 4)
+            for (long k = 0; k < (long)lv.size(); ++k) {
+                Box &b = lv[(size_t)k];
+                b.pot.assign(b.q.size(), 0.0);
+                for (size_t i = 0; i < b.il.size(); ++i) {
+                    if (b.colb[i].empty()) continue;
+                    Vec t = gemv(b.Ar[i], lv[(size_t)b.il[i]].q);
+                    int r = b.Lc[i].r;
+                    trsv_lower(b.Lc[i], false, t.data(), r);
+                    trsv_upper(b.Rc[i], false, t.data(), r);
+                    addto(b.pot, gemv(b.Ac[i], t));
+                }
+            }
+        }
+        auto &lf = T[(size_t)nL];
+#pragma omp parallel for
+        for (long k = 0; k < (long)lf.size(); ++k) {
+            Box &b = lf[(size_t)k];
+            for (int n = 0; n < nnb; ++n)
+                if (b.nb[n] != -1) addto(b.pot, gemv(b.dense[n], lf[(size_t)b.nb[n]].q));
+            addto(b.pot, gemv(b.dense[nnb], b.q));
+        }
+        Vec yp((size_t)N, 0.0);
+        for (int j = 1; j <= nL; ++j) {
+            size_t cnt = 0;
+            for (auto &b : T[(size_t)j])
+                for (double v : b.pot) { yp[cnt] += v; ++cnt; }
+        }
+        reorder(yp, y);
+    }
+
     void matvec_nd(const double *x, double *y) {
+        if (form == 2) {
+            matvec_nn(x, y);
+            return;
+        }
         assign_charges(x);
         // evaluate_M2M_far (2D :617-653, 3D :1941-1976)
         for (int j = nL; j >= 2; --j) {
@@ -1032,7 +1076,7 @@ struct Oracle {
         reorder(yp, y);
     }
 
-    // ---- storage: findMemory_n / _sn (1D :535-588, 2D :1207-1305, 3D :2505-2628)
+    // ---- storage: findMemory_n / _sn / _nn (1D :535-588, 2D :1207-1328, 3D :2505-2628)
     double memory() const {
         double mem = 0.0;
         if (dim == 1) {
@@ -1065,7 +1109,7 @@ struct Oracle {
                     else for (int c = 0; c < nch; ++c) mem += 2.0 * (double)b.M2M[c].size();
                 }
                 for (size_t i = 0; i < b.il.size(); ++i) {
-                    if (!b.ilv[i]) continue;
+                    if (!b.ilv[i] && form != 2) continue;  // findMemory_nn counts every pair
                     if (form == 0) mem += (double)b.m2l[i].size();
                     else mem += (double)(b.Lc[i].size() + b.Rc[i].size() + b.Ac[i].size() + b.Ar[i].size());
                 }
@@ -1183,7 +1227,7 @@ extern "C" {
 
 h2wo *h2wo_create(int dim, int form, int64_t n, const double *pts, int nlevels, int tol_pow, int choice,
                   int64_t kernel_n, int64_t diag_n) {
-    if (dim < 1 || dim > 3 || n < 1 || nlevels < 1 || (form != 0 && form != 1) || (choice != 0 && choice != 1))
+    if (dim < 1 || dim > 3 || n < 1 || nlevels < 1 || (form != 0 && form != 1 && form != 2) || (form == 2 && dim == 1) || (choice != 0 && choice != 1))
         return nullptr;
     h2wo *h = new h2wo;
     Oracle &o = h->o;

@@ -170,6 +170,10 @@ int main(int argc, char **argv) {
         K->assemble_M2L_ver();
         K->assemble_M2M_ver();
         K->assemble_NearField();
+#elif defined(USE_HODLRdD)
+        K->getUVtTree_nn();
+        K->assembleAcAr_nn();
+        K->assemble_NearField();
 #else
         K->getNodes();
         K->assemble_M2L_far();
@@ -195,8 +199,10 @@ int main(int argc, char **argv) {
     g_out = fopen(out_path, "wb");
     if (!g_out) { fprintf(stderr, "cannot open %s\n", out_path); return 2; }
     put_i64("meta", {H2W_DIM, N, nL, tol_pow, choice,
-#ifdef USE_nHODLRdD
+#if defined(USE_nHODLRdD)
                      0
+#elif defined(USE_HODLRdD)
+                     2
 #else
                      1
 #endif
@@ -230,7 +236,7 @@ int main(int argc, char **argv) {
             chkv.add(b->incoming_checkPoints_ver);
             chgv.add(b->incoming_chargePoints_ver);
             for (size_t i = 0; i < b->interactionList.size(); ++i) {
-#ifdef USE_snHODLRdD
+#if defined(USE_snHODLRdD) || defined(USE_HODLRdD)
                 rowb.add(b->row_basis[i]);
                 colb.add(b->col_basis[i]);
 #else
@@ -263,8 +269,10 @@ int main(int argc, char **argv) {
     put_i32("uv_rank", uvr);
 #endif
 
-#ifdef USE_nHODLRdD
+#if defined(USE_nHODLRdD)
     K->findMemory_n();
+#elif defined(USE_HODLRdD)
+    K->findMemory_nn();
 #else
     K->findMemory_sn();
 #endif

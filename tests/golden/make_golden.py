@@ -6,7 +6,7 @@ stores points, tree lists, NCA pivots, storage counts, matvec outputs, the
 dense product and GMRES results. Needs the reference tree; the committed
 .npz files are what the tests read (no test reads the reference).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <reference checkout> [case ...]
 """
 import os
 import subprocess
@@ -31,7 +31,12 @@ CASES = {
     "g3d_sn_ie": (3, "sn", 16, 2, 4, 8, 0, None, 10),
     "g2d_n_rand": (2, "n", 0, 3, 0, 8, 1, ("uniform", 2, 3000), 10),
     "g3d_n_rand": (3, "n", 0, 2, 0, 8, 1, ("uniform", 3, 4000), 10),
+    # non-nested H* (USE_HODLRdD)
+    "g2d_nn_rbf": (2, "nn", 48, 3, 6, 10, 1, None, 10),
+    "g3d_nn_ie": (3, "nn", 16, 2, 4, 8, 0, None, 10),
+    "g2d_nn_rand": (2, "nn", 0, 3, 0, 8, 0, ("uniform", 2, 3000), 10),
 }
+FORMS = {"n": 0, "sn": 1, "nn": 2}
 LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge", "sn_row", "sn_col"]
 
 
@@ -50,7 +55,7 @@ def run_case(name, spec):
     r = subprocess.run([exe, str(npar), str(nlev), str(leaf), "1", str(tol), str(ch), inp, out, "500", str(gtol)],
                        capture_output=True, text=True, check=True)
     d = read_dump(out)
-    rec = {"spec": np.array([dim, 0 if form == "n" else 1, npar, nlev, leaf, tol, ch, gtol, N], dtype=np.int64),
+    rec = {"spec": np.array([dim, FORMS[form], npar, nlev, leaf, tol, ch, gtol, N], dtype=np.int64),
            "points": d["points"].reshape(N, dim), "vecs": np.stack(vecs), "xtrue": xtrue,
            "memory": d["memory"], "matvec": d["matvec"].reshape(2, N), "dense_matvec": d["dense_matvec"],
            "gmres_rhs": d["gmres_rhs"], "gmres_x": d["gmres_x"], "gmres_stats": d["gmres_stats"]}
@@ -64,6 +69,8 @@ def run_case(name, spec):
 
 
 if __name__ == "__main__":
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
-    for name, spec in CASES.items():
-        print(name, run_case(name, spec))
+    # python tests/golden/make_golden.py <reference checkout> [case ...]
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + sys.argv[1]], check=True)
+    names = sys.argv[2:] or list(CASES)
+    for name in names:
+        print(name, run_case(name, CASES[name]))
