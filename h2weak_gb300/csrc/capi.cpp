@@ -130,6 +130,19 @@ struct h2w_handle {
     DBuf<unsigned> d_bar;
     bool coop = true;  // one cooperative launch per matvec (else one launch per phase)
     int64_t spin_limit = 0;  // polls per grid-barrier wait of the single-vector cooperative launch (0: built-in)
+    // far-field M2L evaluated during each single-vector product instead of stored
+    // (H2W_OPT_FAR_ON_THE_FLY, applies at assembly): work items, row / column
+    // point ids, source workspace rows, claim counter, FP32 coordinates, and the
+    // phase at which the product's stored stream is split around the kernel
+    bool far_fly = false, fly_active = false;
+    DBuf<FlyItem> d_fly_items;
+    DBuf<int32_t> d_fly_rowpid, d_fly_cpid, d_fly_cws;
+    DBuf<unsigned long long> d_fly_ctr;
+    DBuf<float> d_pts4;
+    int fly_split = 0;
+    int64_t fly_entries = 0;  // kernel entries one product evaluates
+    std::vector<std::pair<int64_t, int64_t>> fly_rows;  // workspace rows the kernel writes
+    FlyK32 k32{};
     DBuf<float> d_ws32;
     std::vector<Phase> phases;
     std::vector<int64_t> ph_op, ph_vec;   // per phase: operator and vector elements moved
@@ -1250,7 +1263,7 @@ void assign_phases(h2w_handle *h, PlanBuilder &pb, int NPH, std::vector<Phase> &
     for (int p2 = 0; p2 < NPH; ++p2) {
         size_t q0 = q;
         while (q < nt && ph[order[q]] == p2) ++q;
-        if (q > q0) phases.push_back({(int64_t)q0, (int64_t)q, 0});
+        if (q > q0) phases.push_back({(int64_t)q0, (int64_t)q, 0, p2});
     }
     // leaves without any far contribution would never be scattered by the
     // fused path; fall back to an explicit scatter then.
@@ -1311,8 +1324,12 @@ void pack_records(const PlanBuilder &pb, const std::vector<Phase> &phases, std::
 // workspace: it becomes an overwrite and its epilogue reads nothing. Scatter
 // targets write the result, not the workspace; atomic parts of a
 // column-split row keep their atomics.
-void first_writers_overwrite(const std::vector<int64_t> &roff, std::vector<int64_t> &blob, int64_t ws_n) {
+void first_writers_overwrite(const std::vector<int64_t> &roff, std::vector<int64_t> &blob, int64_t ws_n,
+                             const std::vector<std::pair<int64_t, int64_t>> *prewritten = nullptr) {
     std::vector<uint8_t> written((size_t)ws_n, 0);
+    if (prewritten)  // rows written before the stream runs (the far M2L kernel)
+        for (const auto &r : *prewritten)
+            for (int64_t q = r.first; q < r.second; ++q) written[(size_t)q] = 1;
     for (size_t t = 0; t + 1 < roff.size(); ++t) {
         const size_t o = (size_t)roff[t];
         const int64_t dst = blob[o], nrows = blob[o + 1] & 0xffffffff;
@@ -1433,7 +1450,15 @@ void realize_single(h2w_handle *h, int64_t row_split) {
     }
     validate_plan(pb, h, h->phases);
     pack_records(pb, h->phases, roff, blob, pstart);
-    first_writers_overwrite(roff, blob, h->ws_n);
+    first_writers_overwrite(roff, blob, h->ws_n, h->fly_active ? &h->fly_rows : nullptr);
+    // the far M2L kernel runs between the upward passes (logical phases <= L)
+    // and the downward ones (>= L + 1)
+    h->fly_split = (int)h->phases.size();
+    for (size_t q = 0; q < h->phases.size(); ++q)
+        if (h->phases[q].logical >= h->tree.nL + 1) {
+            h->fly_split = (int)q;
+            break;
+        }
     {
         std::vector<int32_t> cnt, cidx;
         std::vector<int64_t> coff;
@@ -1676,12 +1701,73 @@ void build_plan(h2w_handle *h) {
 
     // ---- coupling phase: M2L (far, vertex), near field, pair phase A
     std::vector<std::vector<int64_t>> pfac((size_t)L + 1);
+    // far M2L on the fly: its work items instead of stored blocks
+    const bool fly = h->far_fly && has_far && L >= 2;
+    h->fly_active = fly;
+    h->fly_rows.clear();
+    h->fly_entries = 0;
+    std::vector<FlyItem> fitems;
+    std::vector<int32_t> frow, fcpid, fcws;
+    if (fly) {
+        for (int j = 2; j <= L; ++j) {
+            const Skel &s = h->far[(size_t)j];
+            for (int64_t k = 0; k < t.nbox[(size_t)j]; ++k) {
+                const int32_t r = (int32_t)s.rank(k);
+                if (r == 0) continue;
+                const int64_t cbeg = (int64_t)fcpid.size();
+                for (int64_t e = t.ilp[(size_t)j][(size_t)k]; e < t.ilp[(size_t)j][(size_t)k + 1]; ++e) {
+                    if (t.ilv[(size_t)j][(size_t)e]) continue;
+                    const int32_t q = t.il[(size_t)j][(size_t)e];
+                    for (int64_t i = s.ptr[(size_t)q]; i < s.ptr[(size_t)q + 1]; ++i) {
+                        fcpid.push_back(s.chk[(size_t)i]);
+                        const int64_t w = fo[(size_t)j] + i;
+                        if (w > INT32_MAX) throw ApiError(H2W_ERR_STATE, "workspace too large for the far M2L kernel");
+                        fcws.push_back((int32_t)w);
+                    }
+                }
+                const int64_t nc = (int64_t)fcpid.size() - cbeg;
+                if (nc == 0) continue;
+                if (nc > INT32_MAX) throw ApiError(H2W_ERR_STATE, "far M2L source set too large");
+                const int64_t rbeg = (int64_t)frow.size();
+                append(frow, s.chk.data() + s.ptr[(size_t)k], r);
+                const int nb = (r + 127) / 128, per = (r + nb - 1) / nb;
+                for (int32_t r0 = 0; r0 < r; r0 += per) {
+                    FlyItem it{};
+                    it.dst = fi[(size_t)j] + s.ptr[(size_t)k] + r0;
+                    it.rows = rbeg + r0;
+                    it.cbeg = cbeg;
+                    it.nrows = std::min(per, r - r0);
+                    it.ncols = (int32_t)nc;
+                    fitems.push_back(it);
+                }
+                h->fly_rows.push_back({fi[(size_t)j] + s.ptr[(size_t)k], fi[(size_t)j] + s.ptr[(size_t)k] + r});
+                h->fly_entries += (int64_t)r * nc;
+            }
+        }
+        // bounds of every item against its buffers before any upload
+        for (const FlyItem &it : fitems) {
+            if (it.nrows < 1 || it.nrows > 128 || it.ncols < 1 || it.dst < 0 || it.dst + it.nrows > wsn ||
+                it.rows < 0 || it.rows + it.nrows > (int64_t)frow.size() || it.cbeg < 0 ||
+                it.cbeg + it.ncols > (int64_t)fcpid.size())
+                throw ApiError(H2W_ERR_STATE, "internal: far M2L work item out of range");
+        }
+        for (int32_t v : frow)
+            if (v < 0 || v >= t.N) throw ApiError(H2W_ERR_STATE, "internal: far M2L row point out of range");
+        for (size_t i = 0; i < fcpid.size(); ++i)
+            if (fcpid[i] < 0 || fcpid[i] >= t.N || fcws[i] < 0 || fcws[i] >= wsn)
+                throw ApiError(H2W_ERR_STATE, "internal: far M2L source out of range");
+        // largest first for the persistent grid
+        std::stable_sort(fitems.begin(), fitems.end(), [](const FlyItem &a, const FlyItem &b) {
+            return (int64_t)a.nrows * a.ncols > (int64_t)b.nrows * b.ncols;
+        });
+    }
     {
         for (int j = 1; j <= L; ++j) {
             pb.lo = L - j + 1;
             pb.hi = j == 1 ? L : L + j - 2;
             for (int kind = 0; kind < 2; ++kind) {
                 if (kind == 0 && !(has_far && j >= 2)) continue;
+                if (kind == 0 && fly) continue;  // evaluated by the far M2L kernel
                 if (kind == 1 && !has_ver) continue;
                 const Skel &s = kind == 0 ? h->far[(size_t)j] : h->ver[(size_t)j];
                 const int64_t outb = kind == 0 ? fo[(size_t)j] : vo[(size_t)j];
@@ -1926,6 +2012,29 @@ void build_plan(h2w_handle *h) {
 
     // ---- device buffers and assembly kernels
     cudaStream_t st = h->stream;
+    if (fly) {
+        h->d_fly_items.upload(fitems, st);
+        h->d_fly_rowpid.upload(frow, st);
+        h->d_fly_cpid.upload(fcpid, st);
+        h->d_fly_cws.upload(fcws, st);
+        if (!h->d_fly_ctr.p) h->d_fly_ctr.alloc(1);
+        h->d_pts4.alloc((size_t)t.N * 4);
+        CK(launch_pts4(h->d_pts.p, dim, t.N, h->d_pts4.p, st));
+        const double a = 0.0001;
+        h->k32.c2d = (float)h->c2d;
+        h->k32.inv4pi = (float)(1.0 / h->four_pi);
+        h->k32.inv_loga = (float)(1.0 / h->loga);
+        h->k32.inv_den = (float)(1.0 / h->den_small);
+        h->k32.a = (float)a;
+        h->k32.a2 = (float)(a * a);
+        h->k32.inv_a = (float)(1.0 / a);
+    } else {
+        h->d_fly_items.reset();
+        h->d_fly_rowpid.reset();
+        h->d_fly_cpid.reset();
+        h->d_fly_cws.reset();
+        h->d_pts4.reset();
+    }
     h->op_n = pb.opn;
     h->op_bytes_read = pb.read_elems;
     h->d_op.alloc((size_t)pb.opn);
@@ -2080,7 +2189,32 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
-    if (h->coop && h->dataflow) {
+    if (h->fly_active) {
+        // stored passes up to the upward ones, the far M2L kernel, the rest
+        auto stored = [&](int a, int b) {
+            if (b <= a) return;
+            if (h->coop) {
+                prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
+                    return launch_coop_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p + a, b - a, h->d_op.p, h->d_ws.p,
+                                           dx, dy, perm, h->d_bar.p, h->d_err.p, st, h->spin_limit);
+                });
+            } else {
+                for (int q = a; q < b; ++q) {
+                    const Phase &ph = h->phases[(size_t)q];
+                    prof_launch(h, H2W_PREC_FP64, q, st, [&] {
+                        return launch_brg_f64(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op.p, h->d_ws.p, dx, dy,
+                                              perm, st);
+                    });
+                }
+            }
+        };
+        stored(0, h->fly_split);
+        prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
+            return launch_fly_f64(h->d_fly_items.p, (int64_t)h->d_fly_items.n, h->d_fly_ctr.p, h->d_fly_rowpid.p,
+                                  h->d_fly_cpid.p, h->d_fly_cws.p, h->d_ws.p, h->kparams(), st);
+        });
+        stored(h->fly_split, nph);
+    } else if (h->coop && h->dataflow) {
         CK(cudaMemcpyAsync(h->d_sdep.p, h->d_sdep0.p, h->d_sdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemsetAsync(h->d_sctr.p, 0, 4, st));
         prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
@@ -2134,7 +2268,31 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
-    if (h->coop && h->dataflow) {
+    if (h->fly_active) {
+        auto stored = [&](int a, int b) {
+            if (b <= a) return;
+            if (h->coop) {
+                prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
+                    return launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p + a, b - a, h->d_op32.p,
+                                           h->d_ws32.p, dx, dy, perm, h->d_bar.p, h->d_err.p, st, h->spin_limit);
+                });
+            } else {
+                for (int q = a; q < b; ++q) {
+                    const Phase &ph = h->phases[(size_t)q];
+                    prof_launch(h, H2W_PREC_FP32, q, st, [&] {
+                        return launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, h->d_ws32.p, dx, dy,
+                                              perm, st);
+                    });
+                }
+            }
+        };
+        stored(0, h->fly_split);
+        prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
+            return launch_fly_f32(h->d_fly_items.p, (int64_t)h->d_fly_items.n, h->d_fly_ctr.p, h->d_fly_rowpid.p,
+                                  h->d_fly_cpid.p, h->d_fly_cws.p, h->d_pts4.p, h->d_ws32.p, h->kparams(), h->k32, st);
+        });
+        stored(h->fly_split, nph);
+    } else if (h->coop && h->dataflow) {
         CK(cudaMemcpyAsync(h->d_sdep.p, h->d_sdep0.p, h->d_sdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemsetAsync(h->d_sctr.p, 0, 4, st));
         prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
@@ -2259,6 +2417,8 @@ void mr_prof(h2w_handle *h, int prec, int rp, cudaStream_t st, F &&launch) {
 
 // Y = A X for an interleaved leaf-order block of rp vectors (xi, yi: N x rp).
 void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double *yi, cudaStream_t st) {
+    if (h->fly_active)
+        throw ApiError(H2W_ERR_STATE, "multi-vector products need the stored far field (H2W_OPT_FAR_ON_THE_FLY is on)");
     const int nph = (int)h->mphases.size();
     const size_t wsz = (size_t)h->ws_n * (size_t)rp;
     if (h->ws_n >= (int64_t)INT32_MAX - 2 || h->tree.N >= (int64_t)INT32_MAX - 2)
@@ -2326,6 +2486,8 @@ void run_matvec_multi(h2w_handle *h, int prec, int rp, const double *xi, double 
 
 // y = A32 x for an FP32 interleaved block, FP32 result (no conversions)
 void run_matvec_multi_f32io(h2w_handle *h, int rp, const float *xf, float *yf, cudaStream_t st) {
+    if (h->fly_active)
+        throw ApiError(H2W_ERR_STATE, "multi-vector products need the stored far field (H2W_OPT_FAR_ON_THE_FLY is on)");
     const int nph = (int)h->mphases.size();
     const size_t wsz = (size_t)h->ws_n * (size_t)rp;
     if (h->ws_n >= (int64_t)INT32_MAX - 2 || h->tree.N >= (int64_t)INT32_MAX - 2)
@@ -3087,6 +3249,9 @@ int matvec_external_ws(h2w_handle *h, const double *x, double *y, int precision,
         if (f32 && !h->d_op32.p)
             throw ApiError(H2W_ERR_STATE,
                            "FP32 operator copy not materialised (one h2w_matvec call with H2W_PREC_FP32 creates it)");
+        if (h->fly_active)
+            throw ApiError(H2W_ERR_STATE, "the far field is evaluated on the fly (H2W_OPT_FAR_ON_THE_FLY): "
+                                          "this entry point needs the stored operator");
         const int64_t need = f32 ? (h->ws_n + 1) / 2 : h->ws_n;  // in doubles
         if (need > ws_cap)
             throw ApiError(H2W_ERR_ARG, "matvec workspace of " + std::to_string(h->ws_n) + (f32 ? " floats" : " doubles") +
@@ -3841,6 +4006,8 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
         } else if (option == H2W_OPT_SPIN_LIMIT) {
             if (value < 0) throw ApiError(H2W_ERR_ARG, "spin limit must be >= 0");
             h->spin_limit = value;
+        } else if (option == H2W_OPT_FAR_ON_THE_FLY) {
+            h->far_fly = value != 0;  // takes effect at the next h2w_assemble
         } else if (option == H2W_OPT_COOP) {
             h->coop = value != 0;
             for (auto &g : h->loops) {  // captured steps hold the other launch form
@@ -3869,6 +4036,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_DATAFLOW) *value = h->dataflow ? 1 : 0;
         else if (option == H2W_OPT_PRODUCER_WARP) *value = h->producer_warp ? 1 : 0;
         else if (option == H2W_OPT_SPIN_LIMIT) *value = h->spin_limit;
+        else if (option == H2W_OPT_FAR_ON_THE_FLY) *value = h->far_fly ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });
@@ -3969,7 +4137,7 @@ int h2w_batch_create(h2w_handle *const *handles, int n, h2w_batch **out) {
     auto *b = new h2w_batch();
     b->hs.assign(handles, handles + n);
     for (h2w_handle *h : b->hs)
-        if (!h || !h->has_op || !h->plan || h->cfg.device != b->hs[0]->cfg.device) {
+        if (!h || !h->has_op || !h->plan || h->cfg.device != b->hs[0]->cfg.device || h->fly_active) {
             delete b;
             return H2W_ERR_STATE;
         }

@@ -6,10 +6,9 @@
 namespace h2w {
 
 // ------------------------------------------------------------ entries ---
-static __device__ __forceinline__ double kentry(const KParams &k, int i, int j) {
-    if (i == j) return k.diag;
-    const double *a = k.pts + (size_t)i * k.dim;
-    const double *b = k.pts + (size_t)j * k.dim;
+// The entry between two distinct points given by their coordinates a, b
+// (getMatrixEntry off the diagonal, in the reference's operation order).
+static __device__ __forceinline__ double kentry_ab(const KParams &k, const double *a, const double *b) {
     if (k.dim == 1) {
         double R = fabs(__dsub_rn(a[0], b[0]));
         if (k.choice == 0) return log(R);
@@ -31,6 +30,11 @@ static __device__ __forceinline__ double kentry(const KParams &k, int i, int j) 
     const double aa = 0.0001;
     if (R < aa) return __ddiv_rn(__dsub_rn(__dmul_rn(R, log(R)), 1.0), k.den_small);
     return __ddiv_rn(log(R), k.loga);
+}
+
+static __device__ __forceinline__ double kentry(const KParams &k, int i, int j) {
+    if (i == j) return k.diag;
+    return kentry_ab(k, k.pts + (size_t)i * k.dim, k.pts + (size_t)j * k.dim);
 }
 
 }  // namespace h2w

@@ -69,6 +69,7 @@ struct Seg {
 struct Phase {
     int64_t t0, t1;   // target range
     int max_xw;       // shared-memory words needed
+    int logical = 0;  // the pass it belongs to (0 .. 2L; empty passes have no Phase)
 };
 
 // Assembly jobs.

@@ -88,6 +88,25 @@ constexpr int BRG_MAX_PANELS = 32;    // panels per target
 constexpr int BRG_REC_WORDS = 1024;   // packed record of one target (int64 words)
 constexpr int MR_XS_ELEMS = 2048;     // gathered source width per multi-vector target (elements)
 
+// Far-field M2L evaluated during the product (m2lfly.cu). One work item: a
+// block of <= 128 rows of one target box: rows[i] (point ids at rowpid[rows
+// + i]) get ws[dst + i] = sum_c K(row point, cpid[cbeg + c]) ws[cws[cbeg + c]].
+struct FlyItem {
+    int64_t dst, rows, cbeg;
+    int32_t nrows, ncols;
+};
+// FP32 constants of the kernel functions (3D/2D, choice 0/1)
+struct FlyK32 {
+    float c2d, inv4pi, inv_loga, inv_den, a, a2, inv_a, pad;
+};
+cudaError_t launch_fly_f64(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                           const int32_t *cpid, const int32_t *cws, double *ws, const KParams &kp, cudaStream_t st);
+cudaError_t launch_fly_f32(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                           const int32_t *cpid, const int32_t *cws, const float *pts4, float *ws, const KParams &kp,
+                           const FlyK32 &k32, cudaStream_t st);
+// (x, y, z, 0) FP32 coordinates of the FP64 points (N x dim) for the FP32 form.
+cudaError_t launch_pts4(const double *pts, int dim, int64_t n, float *out, cudaStream_t st);
+
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,
                                 int64_t nrows, cudaStream_t st);

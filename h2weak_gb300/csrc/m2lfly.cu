@@ -1,0 +1,172 @@
+// Far-field M2L evaluated during the product (sm_103a).
+//
+// The far M2L blocks of the nested form are plain kernel entries between
+// skeleton points: M2L[k][q] = K(check_k, check_q) (assemble_M2L_far,
+// 2D/codes/HODLR2Dtree.hpp:655-675, 3D/codes/HODLR3Dtree.hpp:1978-1998), and
+// they are most of the stored entries of a 3D operator (about 80 % for
+// uniform random points at tol 1e-10). When the stored operator would not fit
+// in device memory, the handle keeps the far check points instead and this
+// kernel forms in_k = sum_q K(check_k, check_q) out_q (evaluate_M2L_far,
+// 2D :678-699, 3D :2000-2021) from the point coordinates on every product.
+//
+// Work items are row blocks (<= 128 rows) of one target box; a persistent
+// grid claims them largest first from a counter. A CTA stages the item's
+// source columns 256 at a time in shared memory (coordinates and the
+// workspace value out_q), each thread owns one row (or a quarter / half row
+// when the block is short, the partial sums met by shuffles) and writes the
+// row once: the target's rows are written by no other item, and this kernel
+// is the first writer of them in the product. The FP64 form evaluates every
+// entry with the same operations as the stored operator's (bitwise the same
+// entries); the FP32 form evaluates them in FP32 from FP32 coordinates.
+#include "entry.cuh"
+
+namespace h2w {
+
+constexpr int FLY_THREADS = 128;
+constexpr int FLY_TILE = 256;
+
+template <int DIM, int CH>
+__device__ __forceinline__ float fly_entry32(const FlyK32 &k, float dx, float dy, float dz) {
+    const float R2 = DIM == 3 ? fmaf(dz, dz, fmaf(dy, dy, dx * dx)) : fmaf(dy, dy, dx * dx);
+    if (DIM == 2) {
+        if (CH == 0) return k.c2d * __logf(R2);
+        return R2 < k.a2 ? sqrtf(R2) * k.inv_a : k.a * rsqrtf(R2);
+    }
+    if (CH == 0) return k.inv4pi * rsqrtf(R2);
+    if (R2 < k.a2) {
+        const float R = sqrtf(R2);
+        return (R * __logf(R) - 1.f) * k.inv_den;
+    }
+    return (0.5f * __logf(R2)) * k.inv_loga;
+}
+
+template <class T, int DIM, int CH>
+__global__ void __launch_bounds__(FLY_THREADS)
+    m2l_fly_kernel(const FlyItem *__restrict__ items, int64_t nitems, unsigned long long *ctr,
+                   const int32_t *__restrict__ rowpid, const int32_t *__restrict__ cpid,
+                   const int32_t *__restrict__ cws, const T *__restrict__ pts, T *ws, KParams kp, FlyK32 k32) {
+    __shared__ T sx[FLY_TILE], sy[FLY_TILE], sz[FLY_TILE], sv[FLY_TILE];
+    __shared__ long long s_it;
+    // coordinates: FP32 as (x, y, z, 0) quadruples, FP64 as the points array (N x DIM)
+    constexpr int PS = sizeof(T) == 4 ? 4 : DIM;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_it = (long long)atomicAdd(ctr, 1ull);
+        __syncthreads();
+        const long long it = s_it;
+        if (it >= nitems) return;
+        const FlyItem m = items[it];
+        const int tpr = m.nrows <= 32 ? 4 : (m.nrows <= 64 ? 2 : 1);
+        const int row = threadIdx.x / tpr, sub = threadIdx.x - row * tpr;
+        const bool has = row < m.nrows;
+        T a[3] = {T(0), T(0), T(0)};
+        if (has) {
+            const int64_t p = rowpid[m.rows + row];
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) a[d] = pts[p * PS + d];
+        }
+        T acc = T(0);
+        for (int c0 = 0; c0 < m.ncols; c0 += FLY_TILE) {
+            const int nc = m.ncols - c0 < FLY_TILE ? m.ncols - c0 : FLY_TILE;
+            __syncthreads();
+            for (int c = threadIdx.x; c < nc; c += FLY_THREADS) {
+                const int64_t e = m.cbeg + c0 + c;
+                const int64_t p = cpid[e];
+                sx[c] = pts[p * PS];
+                sy[c] = pts[p * PS + 1];
+                if (DIM == 3) sz[c] = pts[p * PS + 2];
+                sv[c] = ws[cws[e]];
+            }
+            __syncthreads();
+            if (has) {
+                if constexpr (sizeof(T) == 4) {
+                    for (int c = sub; c < nc; c += tpr)
+                        acc = fmaf(fly_entry32<DIM, CH>(k32, (float)a[0] - (float)sx[c], (float)a[1] - (float)sy[c],
+                                                        DIM == 3 ? (float)a[2] - (float)sz[c] : 0.f),
+                                   (float)sv[c], (float)acc);
+                } else {
+                    for (int c = sub; c < nc; c += tpr) {
+                        const double b[3] = {(double)sx[c], (double)sy[c], DIM == 3 ? (double)sz[c] : 0.0};
+                        const double aa[3] = {(double)a[0], (double)a[1], (double)a[2]};
+                        acc += (T)(kentry_ab(kp, aa, b) * (double)sv[c]);
+                    }
+                }
+            }
+        }
+        // partial sums of a row's threads (adjacent lanes)
+        if (tpr > 1) acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        if (tpr > 2) acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        if (has && sub == 0) ws[m.dst + row] = acc;
+    }
+}
+
+static int fly_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <class T, int DIM, int CH>
+static cudaError_t fly_launch_t(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                                const int32_t *cpid, const int32_t *cws, const T *pts, T *ws, const KParams &kp,
+                                const FlyK32 &k32, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, m2l_fly_kernel<T, DIM, CH>, FLY_THREADS, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    const int64_t cap = (int64_t)fly_sms() * per_sm;
+    const int grid = (int)(nitems < cap ? nitems : cap);
+    cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    m2l_fly_kernel<T, DIM, CH><<<grid, FLY_THREADS, 0, st>>>(items, nitems, ctr, rowpid, cpid, cws, pts, ws, kp, k32);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t fly_dispatch(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                                const int32_t *cpid, const int32_t *cws, const T *pts, T *ws, const KParams &kp,
+                                const FlyK32 &k32, cudaStream_t st) {
+    if (nitems <= 0) return cudaSuccess;
+    if (kp.dim == 2)
+        return kp.choice == 0 ? fly_launch_t<T, 2, 0>(items, nitems, ctr, rowpid, cpid, cws, pts, ws, kp, k32, st)
+                              : fly_launch_t<T, 2, 1>(items, nitems, ctr, rowpid, cpid, cws, pts, ws, kp, k32, st);
+    if (kp.dim == 3)
+        return kp.choice == 0 ? fly_launch_t<T, 3, 0>(items, nitems, ctr, rowpid, cpid, cws, pts, ws, kp, k32, st)
+                              : fly_launch_t<T, 3, 1>(items, nitems, ctr, rowpid, cpid, cws, pts, ws, kp, k32, st);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fly_f64(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                           const int32_t *cpid, const int32_t *cws, double *ws, const KParams &kp, cudaStream_t st) {
+    return fly_dispatch<double>(items, nitems, ctr, rowpid, cpid, cws, kp.pts, ws, kp, FlyK32{}, st);
+}
+
+cudaError_t launch_fly_f32(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                           const int32_t *cpid, const int32_t *cws, const float *pts4, float *ws, const KParams &kp,
+                           const FlyK32 &k32, cudaStream_t st) {
+    return fly_dispatch<float>(items, nitems, ctr, rowpid, cpid, cws, pts4, ws, kp, k32, st);
+}
+
+// (x, y, z, 0) FP32 quadruples of the FP64 points (N x dim).
+__global__ void pts4_kernel(const double *__restrict__ pts, int dim, int64_t n, float *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float q[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int d = 0; d < dim; ++d) q[d] = (float)pts[i * dim + d];
+        reinterpret_cast<float4 *>(out)[i] = make_float4(q[0], q[1], q[2], q[3]);
+    }
+}
+
+cudaError_t launch_pts4(const double *pts, int dim, int64_t n, float *out, cudaStream_t st) {
+    pts4_kernel<<<fly_sms() * 4, 256, 0, st>>>(pts, dim, n, out);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace h2w

@@ -242,10 +242,22 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 0 (default): the built-in limit (2^26 polls, seconds). A
  *                 wait that runs out lets the kernel finish with an invalid
  *                 result and makes the call fail with H2W_ERR_CUDA; a tiny
- *                 limit is how that error path is exercised. */
+ *                 limit is how that error path is exercised.
+ *  H2W_OPT_FAR_ON_THE_FLY  1: the far-field M2L blocks (kernel entries between
+ *                 the check points of interacting boxes, assemble_M2L_far,
+ *                 3D/codes/HODLR3Dtree.hpp:1978-1998) are not stored; every
+ *                 single-vector product evaluates them from the point
+ *                 coordinates (FP64: the stored entries bitwise; FP32: FP32
+ *                 entries from FP32 coordinates) between its upward and
+ *                 downward passes. For operators whose stored form exceeds
+ *                 device memory (3D, tight tolerances: the far M2L blocks
+ *                 are most of the entries). Takes effect at the next
+ *                 h2w_assemble; multi-vector products and many-problem
+ *                 batches need the stored form (H2W_ERR_STATE). 0 (default):
+ *                 stored. The storage count stays the reference's. */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
        H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8,
-       H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10 };
+       H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10, H2W_OPT_FAR_ON_THE_FLY = 11 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
