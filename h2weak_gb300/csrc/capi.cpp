@@ -1347,6 +1347,29 @@ void first_writers_overwrite(const std::vector<int64_t> &roff, std::vector<int64
     }
 }
 
+// Within a phase (and in the dataflow launch, between targets with no
+// dependency) targets run concurrently, so non-atomic writers of the same
+// workspace rows in one phase would race, and one that first_writers_overwrite
+// turned into an overwrite would drop the other's terms. The tree passes never
+// produce such a pair; this check makes a plan that did fail loudly.
+void check_phase_writers(const std::vector<int64_t> &roff, const std::vector<int64_t> &blob,
+                         const std::vector<Phase> &phases) {
+    std::vector<std::pair<int64_t, int64_t>> w;
+    for (const Phase &ph : phases) {
+        w.clear();
+        for (int64_t t = ph.t0; t < ph.t1; ++t) {
+            const size_t o = (size_t)roff[(size_t)t];
+            const int64_t dst = blob[o], nrows = blob[o + 1] & 0xffffffff, flags = blob[o + 1] >> 32;
+            if ((flags & T_ATOMIC) || (flags & T_SCATTER)) continue;
+            w.push_back({dst, dst + nrows});
+        }
+        std::sort(w.begin(), w.end());
+        for (size_t q = 1; q < w.size(); ++q)
+            if (w[q].first < w[q - 1].second)
+                throw ApiError(H2W_ERR_STATE, "internal: two non-atomic targets of one phase write the same rows");
+    }
+}
+
 // (Re)cut the single-vector target stream: row chunks of max(4,
 // row_split / width) rows, column splits past XW_CAP; per-phase byte counts
 // Producer -> consumer dependencies between the targets of a stream, over the
@@ -1451,6 +1474,7 @@ void realize_single(h2w_handle *h, int64_t row_split) {
     validate_plan(pb, h, h->phases);
     pack_records(pb, h->phases, roff, blob, pstart);
     first_writers_overwrite(roff, blob, h->ws_n, h->fly_active ? &h->fly_rows : nullptr);
+    check_phase_writers(roff, blob, h->phases);
     // the far M2L kernel runs between the upward passes (logical phases <= L)
     // and the downward ones (>= L + 1)
     h->fly_split = (int)h->phases.size();
@@ -1496,6 +1520,7 @@ void realize_multi(h2w_handle *h, int64_t cap) {
     pack_records(pb, h->mphases, roff, blob, pstart);
     if (roff.size() != pb.T.size() + 1) throw ApiError(H2W_ERR_STATE, "internal: multi-vector records not packed");
     first_writers_overwrite(roff, blob, h->ws_n);
+    check_phase_writers(roff, blob, h->mphases);
     {
         const int64_t mt = 64, kc = 32, wr = 8;  // the kernel's row tile, column chunk and rows per warp
         int64_t *ms = h->mstats;
