@@ -1755,7 +1755,7 @@ void build_plan(h2w_handle *h) {
                 if (nc > INT32_MAX) throw ApiError(H2W_ERR_STATE, "far M2L source set too large");
                 const int64_t rbeg = (int64_t)frow.size();
                 append(frow, s.chk.data() + s.ptr[(size_t)k], r);
-                const int nb = (r + 127) / 128, per = (r + nb - 1) / nb;
+                const int nb = (r + FLY_ROWS - 1) / FLY_ROWS, per = (r + nb - 1) / nb;
                 for (int32_t r0 = 0; r0 < r; r0 += per) {
                     FlyItem it{};
                     it.dst = fi[(size_t)j] + s.ptr[(size_t)k] + r0;
@@ -1771,7 +1771,7 @@ void build_plan(h2w_handle *h) {
         }
         // bounds of every item against its buffers before any upload
         for (const FlyItem &it : fitems) {
-            if (it.nrows < 1 || it.nrows > 128 || it.ncols < 1 || it.dst < 0 || it.dst + it.nrows > wsn ||
+            if (it.nrows < 1 || it.nrows > FLY_ROWS || it.ncols < 1 || it.dst < 0 || it.dst + it.nrows > wsn ||
                 it.rows < 0 || it.rows + it.nrows > (int64_t)frow.size() || it.cbeg < 0 ||
                 it.cbeg + it.ncols > (int64_t)fcpid.size())
                 throw ApiError(H2W_ERR_STATE, "internal: far M2L work item out of range");

@@ -89,8 +89,9 @@ constexpr int BRG_REC_WORDS = 1024;   // packed record of one target (int64 word
 constexpr int MR_XS_ELEMS = 2048;     // gathered source width per multi-vector target (elements)
 
 // Far-field M2L evaluated during the product (m2lfly.cu). One work item: a
-// block of <= 128 rows of one target box: rows[i] (point ids at rowpid[rows
+// block of <= FLY_ROWS rows of one target box: rows[i] (point ids at rowpid[rows
 // + i]) get ws[dst + i] = sum_c K(row point, cpid[cbeg + c]) ws[cws[cbeg + c]].
+constexpr int FLY_ROWS = 32;  // rows per work item
 struct FlyItem {
     int64_t dst, rows, cbeg;
     int32_t nrows, ncols;

@@ -9,21 +9,24 @@
 // kernel forms in_k = sum_q K(check_k, check_q) out_q (evaluate_M2L_far,
 // 2D :678-699, 3D :2000-2021) from the point coordinates on every product.
 //
-// Work items are row blocks (<= 128 rows) of one target box; a persistent
-// grid claims them largest first from a counter. A CTA stages the item's
-// source columns 256 at a time in shared memory (coordinates and the
-// workspace value out_q), each thread owns one row (or a quarter / half row
-// when the block is short, the partial sums met by shuffles) and writes the
-// row once: the target's rows are written by no other item, and this kernel
-// is the first writer of them in the product. The FP64 form evaluates every
-// entry with the same operations as the stored operator's (bitwise the same
-// entries); the FP32 form evaluates them in FP32 from FP32 coordinates.
+// Work items are blocks of <= 32 rows of one target box (enough items to
+// fill every SM); a persistent grid claims them largest first from a
+// counter. A CTA stages the item's source columns 256 at a time in shared
+// memory (coordinates and the workspace value out_q); four threads share a
+// row, each over every fourth column with two independent accumulation
+// chains, their partial sums met by shuffles, and the row is written once:
+// the target's rows are written by no other item, and this kernel is the
+// first writer of them in the product. The FP64 form evaluates the entries
+// with a few ulps of the stored ones (fly_entry64); the FP32 form evaluates
+// them in FP32 from FP32 coordinates.
 #include "entry.cuh"
 
 namespace h2w {
 
 constexpr int FLY_THREADS = 128;
 constexpr int FLY_TILE = 256;
+constexpr int FLY_TPR = 4;  // threads per row; FLY_ROWS = FLY_THREADS / FLY_TPR rows per work item
+static_assert(FLY_ROWS * FLY_TPR == FLY_THREADS, "work item shape");
 
 template <int DIM, int CH>
 __device__ __forceinline__ float fly_entry32(const FlyK32 &k, float dx, float dy, float dz) {
@@ -40,12 +43,36 @@ __device__ __forceinline__ float fly_entry32(const FlyK32 &k, float dx, float dy
     return (0.5f * __logf(R2)) * k.inv_loga;
 }
 
+// one staged source column: coordinates and the workspace value out_q
+template <class T> struct FlyCol { T x, y, z, v; };
+
+// FP64 entries for the far field: the same functions with fewer FP64
+// operations than the exact getMatrixEntry order (log R = log(R^2) / 2, a
+// product by 1/log a, an rsqrt instead of a division by a square root);
+// they differ from the stored entries by a few ulps. Far pairs never meet
+// the R < a branch of the RBF kernels (boxes are separated by a box), which
+// keeps the exact form.
+template <int DIM, int CH>
+__device__ __forceinline__ double fly_entry64(const KParams &k, const double *a, const double *b) {
+    const double dx = a[0] - b[0], dy = a[1] - b[1];
+    const double R2 = DIM == 3 ? fma(a[2] - b[2], a[2] - b[2], fma(dy, dy, dx * dx)) : fma(dy, dy, dx * dx);
+    const double aa = 0.0001;
+    if (DIM == 2) {
+        if (CH == 0) return k.c2d * log(R2);
+        if (R2 < aa * aa) return kentry_ab(k, a, b);
+        return aa * rsqrt(R2);
+    }
+    if (CH == 0) return rsqrt(R2) / k.four_pi;
+    if (R2 < aa * aa) return kentry_ab(k, a, b);
+    return log(R2) * (0.5 / k.loga);
+}
+
 template <class T, int DIM, int CH>
 __global__ void __launch_bounds__(FLY_THREADS)
     m2l_fly_kernel(const FlyItem *__restrict__ items, int64_t nitems, unsigned long long *ctr,
                    const int32_t *__restrict__ rowpid, const int32_t *__restrict__ cpid,
                    const int32_t *__restrict__ cws, const T *__restrict__ pts, T *ws, KParams kp, FlyK32 k32) {
-    __shared__ T sx[FLY_TILE], sy[FLY_TILE], sz[FLY_TILE], sv[FLY_TILE];
+    __shared__ __align__(16) FlyCol<T> sc[FLY_TILE];
     __shared__ long long s_it;
     // coordinates: FP32 as (x, y, z, 0) quadruples, FP64 as the points array (N x DIM)
     constexpr int PS = sizeof(T) == 4 ? 4 : DIM;
@@ -56,7 +83,8 @@ __global__ void __launch_bounds__(FLY_THREADS)
         const long long it = s_it;
         if (it >= nitems) return;
         const FlyItem m = items[it];
-        const int tpr = m.nrows <= 32 ? 4 : (m.nrows <= 64 ? 2 : 1);
+        // FLY_ROWS rows per item, FLY_TPR threads per row over interleaved columns
+        const int tpr = FLY_TPR;
         const int row = threadIdx.x / tpr, sub = threadIdx.x - row * tpr;
         const bool has = row < m.nrows;
         T a[3] = {T(0), T(0), T(0)};
@@ -65,37 +93,67 @@ __global__ void __launch_bounds__(FLY_THREADS)
 #pragma unroll
             for (int d = 0; d < DIM; ++d) a[d] = pts[p * PS + d];
         }
-        T acc = T(0);
+        (void)PS;
+        T acc = T(0), acc2 = T(0);  // two chains: the multiply-adds of neighbouring columns overlap
         for (int c0 = 0; c0 < m.ncols; c0 += FLY_TILE) {
             const int nc = m.ncols - c0 < FLY_TILE ? m.ncols - c0 : FLY_TILE;
             __syncthreads();
             for (int c = threadIdx.x; c < nc; c += FLY_THREADS) {
                 const int64_t e = m.cbeg + c0 + c;
                 const int64_t p = cpid[e];
-                sx[c] = pts[p * PS];
-                sy[c] = pts[p * PS + 1];
-                if (DIM == 3) sz[c] = pts[p * PS + 2];
-                sv[c] = ws[cws[e]];
+                FlyCol<T> q;
+                if constexpr (sizeof(T) == 4) {
+                    const float4 f = reinterpret_cast<const float4 *>(pts)[p];
+                    q.x = f.x;
+                    q.y = f.y;
+                    q.z = f.z;
+                } else {
+                    q.x = pts[p * PS];
+                    q.y = pts[p * PS + 1];
+                    q.z = DIM == 3 ? pts[p * PS + 2] : T(0);
+                }
+                q.v = ws[cws[e]];
+                sc[c] = q;
             }
             __syncthreads();
             if (has) {
                 if constexpr (sizeof(T) == 4) {
-                    for (int c = sub; c < nc; c += tpr)
-                        acc = fmaf(fly_entry32<DIM, CH>(k32, (float)a[0] - (float)sx[c], (float)a[1] - (float)sy[c],
-                                                        DIM == 3 ? (float)a[2] - (float)sz[c] : 0.f),
-                                   (float)sv[c], (float)acc);
+                    int c = sub;
+                    for (; c + tpr < nc; c += 2 * tpr) {
+                        const float4 q = reinterpret_cast<const float4 *>(sc)[c];
+                        const float4 r = reinterpret_cast<const float4 *>(sc)[c + tpr];
+                        acc = fmaf(fly_entry32<DIM, CH>(k32, a[0] - q.x, a[1] - q.y, DIM == 3 ? a[2] - q.z : 0.f), q.w,
+                                   acc);
+                        acc2 = fmaf(fly_entry32<DIM, CH>(k32, a[0] - r.x, a[1] - r.y, DIM == 3 ? a[2] - r.z : 0.f),
+                                    r.w, acc2);
+                    }
+                    if (c < nc) {
+                        const float4 q = reinterpret_cast<const float4 *>(sc)[c];
+                        acc = fmaf(fly_entry32<DIM, CH>(k32, a[0] - q.x, a[1] - q.y, DIM == 3 ? a[2] - q.z : 0.f), q.w,
+                                   acc);
+                    }
                 } else {
-                    for (int c = sub; c < nc; c += tpr) {
-                        const double b[3] = {(double)sx[c], (double)sy[c], DIM == 3 ? (double)sz[c] : 0.0};
-                        const double aa[3] = {(double)a[0], (double)a[1], (double)a[2]};
-                        acc += (T)(kentry_ab(kp, aa, b) * (double)sv[c]);
+                    const double aa[3] = {(double)a[0], (double)a[1], (double)a[2]};
+                    int c = sub;
+                    for (; c + tpr < nc; c += 2 * tpr) {
+                        const FlyCol<T> q = sc[c], r = sc[c + tpr];
+                        const double b[3] = {(double)q.x, (double)q.y, (double)q.z};
+                        const double e[3] = {(double)r.x, (double)r.y, (double)r.z};
+                        acc = fma(fly_entry64<DIM, CH>(kp, aa, b), (double)q.v, (double)acc);
+                        acc2 = fma(fly_entry64<DIM, CH>(kp, aa, e), (double)r.v, (double)acc2);
+                    }
+                    if (c < nc) {
+                        const FlyCol<T> q = sc[c];
+                        const double b[3] = {(double)q.x, (double)q.y, (double)q.z};
+                        acc = fma(fly_entry64<DIM, CH>(kp, aa, b), (double)q.v, (double)acc);
                     }
                 }
             }
         }
         // partial sums of a row's threads (adjacent lanes)
-        if (tpr > 1) acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        if (tpr > 2) acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        acc += acc2;
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
         if (has && sub == 0) ws[m.dst + row] = acc;
     }
 }
