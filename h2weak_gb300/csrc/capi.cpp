@@ -139,6 +139,7 @@ struct h2w_handle {
     DBuf<int32_t> d_fly_rowpid, d_fly_cpid, d_fly_cws;
     DBuf<unsigned long long> d_fly_ctr;
     DBuf<float> d_pts4;
+    DBuf<float> d_ptsdf, d_logtab;  // (hi, lo) points and the log table of the double-FP32 form
     int fly_split = 0;
     int64_t fly_entries = 0;  // kernel entries one product evaluates
     std::vector<std::pair<int64_t, int64_t>> fly_rows;  // workspace rows the kernel writes
@@ -2045,6 +2046,12 @@ void build_plan(h2w_handle *h) {
         if (!h->d_fly_ctr.p) h->d_fly_ctr.alloc(1);
         h->d_pts4.alloc((size_t)t.N * 4);
         CK(launch_pts4(h->d_pts.p, dim, t.N, h->d_pts4.p, st));
+        h->d_ptsdf.alloc((size_t)t.N * 8);
+        CK(launch_ptsdf(h->d_pts.p, dim, t.N, h->d_ptsdf.p, st));
+        std::vector<float> lt(128 * 8);
+        fly_df_logtab(lt.data());
+        h->d_logtab.upload(lt, st);
+        CK(cudaStreamSynchronize(st));
         const double a = 0.0001;
         h->k32.c2d = (float)h->c2d;
         h->k32.inv4pi = (float)(1.0 / h->four_pi);
@@ -2053,12 +2060,16 @@ void build_plan(h2w_handle *h) {
         h->k32.a = (float)a;
         h->k32.a2 = (float)(a * a);
         h->k32.inv_a = (float)(1.0 / a);
+        // far boxes are not adjacent: their points are at least the deepest box width apart
+        h->k32.sep = 2.0 / std::ldexp(1.0, L) > 2.0 * a ? 1 : 0;
     } else {
         h->d_fly_items.reset();
         h->d_fly_rowpid.reset();
         h->d_fly_cpid.reset();
         h->d_fly_cws.reset();
         h->d_pts4.reset();
+        h->d_ptsdf.reset();
+        h->d_logtab.reset();
     }
     h->op_n = pb.opn;
     h->op_bytes_read = pb.read_elems;
@@ -2210,7 +2221,11 @@ void prof_launch(h2w_handle *h, int prec, int phase, cudaStream_t st, F &&launch
 
 // y = A x. permuted: x and y in leaf order (GMRES works there: no gather or
 // scatter per product); otherwise original point order.
-void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st, bool permuted = false) {
+// df: with the far field on the fly, its M2L in double-FP32 arithmetic
+// (FP64-accurate on the FP32 pipes) where that form exists; the stored passes
+// stay FP64.
+void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st, bool permuted = false,
+                    bool df = false) {
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
@@ -2235,6 +2250,10 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
         };
         stored(0, h->fly_split);
         prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
+            if (df)
+                return launch_fly_df64(h->d_fly_items.p, (int64_t)h->d_fly_items.n, h->d_fly_ctr.p, h->d_fly_rowpid.p,
+                                       h->d_fly_cpid.p, h->d_fly_cws.p, h->d_ptsdf.p, h->d_logtab.p, h->d_ws.p,
+                                       h->kparams(), h->k32, st);
             return launch_fly_f64(h->d_fly_items.p, (int64_t)h->d_fly_items.n, h->d_fly_ctr.p, h->d_fly_rowpid.p,
                                   h->d_fly_cpid.p, h->d_fly_cws.p, h->d_ws.p, h->kparams(), st);
         });
@@ -2786,7 +2805,7 @@ double fp32_error_single(h2w_handle *h, cudaStream_t st) {
     for (int c = 0; c < 2; ++c) {
         CK(launch_calib_fill(h->s_d.p, N, 1, c, st));
         run_matvec_f32(h, h->s_d.p, h->s_r.p, st, true);
-        run_matvec_f64(h, h->s_d.p, h->s_t.p, st, true);
+        run_matvec_f64(h, h->s_d.p, h->s_t.p, st, true, h->ir_resid_prec == H2W_PREC_DF64);
         CK(vec_axpby(1.0, h->s_r.p, -1.0, h->s_t.p, h->s_r.p, N, st));
         const double nz = dnorm(h, h->s_d.p);
         if (nz > 0) eta = std::max(eta, dnorm(h, h->s_r.p) / nz);
@@ -3670,7 +3689,8 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
         const int64_t N = h->tree.N;
         if (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32 && precision != H2W_PREC_DF64)
             throw ApiError(H2W_ERR_ARG, "unknown precision");
-        if (nrhs > 1 || precision == H2W_PREC_DF64) {
+        const bool df_single = nrhs == 1 && precision == H2W_PREC_DF64 && h->fly_active;
+        if (nrhs > 1 || (precision == H2W_PREC_DF64 && !df_single)) {
             // blocks of up to 64 columns through the multi-vector kernel
             ensure_multi_vectors(h);
             if (where == H2W_HOST) {
@@ -3713,7 +3733,7 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
             if (precision == H2W_PREC_FP32) {
                 run_matvec_f32(h, dx, dy, st);
             } else {
-                run_matvec_f64(h, dx, dy, st);
+                run_matvec_f64(h, dx, dy, st, false, df_single);
             }
             if (where == H2W_HOST) CK(cudaMemcpyAsync(yc, h->d_y.p, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
         }
@@ -3812,7 +3832,7 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
                 drift = HUGE_VAL;
             } else {
                 if (o == 0) run_matvec_f32(h, dx, r.p, st, true);
-                else run_matvec_f64(h, dx, r.p, st, true);
+                else run_matvec_f64(h, dx, r.p, st, true, h->ir_resid_prec == H2W_PREC_DF64);
                 CK(vec_axpby(1.0, db, -1.0, r.p, r.p, N, st));
                 drift = o == 0 ? HUGE_VAL : 0.0;
                 if (o == 1 && h->ir_update)

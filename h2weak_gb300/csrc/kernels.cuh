@@ -98,7 +98,8 @@ struct FlyItem {
 };
 // FP32 constants of the kernel functions (3D/2D, choice 0/1)
 struct FlyK32 {
-    float c2d, inv4pi, inv_loga, inv_den, a, a2, inv_a, pad;
+    float c2d, inv4pi, inv_loga, inv_den, a, a2, inv_a;
+    int32_t sep;  // every far pair is farther apart than a (deepest box wider than a)
 };
 cudaError_t launch_fly_f64(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
                            const int32_t *cpid, const int32_t *cws, double *ws, const KParams &kp, cudaStream_t st);
@@ -107,6 +108,16 @@ cudaError_t launch_fly_f32(const FlyItem *items, int64_t nitems, unsigned long l
                            const FlyK32 &k32, cudaStream_t st);
 // (x, y, z, 0) FP32 coordinates of the FP64 points (N x dim) for the FP32 form.
 cudaError_t launch_pts4(const double *pts, int dim, int64_t n, float *out, cudaStream_t st);
+// The FP64-accurate form on the FP32 pipes (double-FP32 arithmetic) for the
+// kernels built on log(R^2) when every far pair is farther apart than a (else
+// the FP64 form): ptsdf = (hi, lo) FP32 quadruples of the points
+// (launch_ptsdf, 8 floats per point), logtab = fly_df_logtab's 128 x 8 floats.
+bool fly_df_supported(const KParams &kp, const FlyK32 &k32);
+cudaError_t launch_fly_df64(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                            const int32_t *cpid, const int32_t *cws, const float *ptsdf, const void *logtab,
+                            double *ws, const KParams &kp, const FlyK32 &k32, cudaStream_t st);
+void fly_df_logtab(float *out);
+cudaError_t launch_ptsdf(const double *pts, int dim, int64_t n, float *out, cudaStream_t st);
 
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,

@@ -19,6 +19,8 @@
 // first writer of them in the product. The FP64 form evaluates the entries
 // with a few ulps of the stored ones (fly_entry64); the FP32 form evaluates
 // them in FP32 from FP32 coordinates.
+#include <cmath>
+
 #include "entry.cuh"
 
 namespace h2w {
@@ -158,6 +160,226 @@ __global__ void __launch_bounds__(FLY_THREADS)
     }
 }
 
+// FP32 form for far pairs separated by more than the RBF kernels' radius a
+// (every far pair of a tree whose deepest boxes are wider than a: a far pair's
+// boxes are not adjacent, so its points are at least a box width apart). The
+// entry is then one function of R^2 times a constant: log2(R^2) (3D RBF,
+// 2D IE) or 1/sqrt(R^2) (3D IE, 2D RBF); the constant multiplies the row's
+// sum once. Eight threads share a row pair (rows r and r + 16 of the item),
+// each over every eighth staged column: one shared-memory load feeds two
+// entries, and the two rows' sums are independent chains.
+template <int DIM, int CH>
+__device__ __forceinline__ float fly_g32(float R2) {
+    if ((DIM == 3 && CH == 1) || (DIM == 2 && CH == 0)) return __log2f(R2);
+    return rsqrtf(R2);
+}
+
+template <int DIM, int CH>
+__global__ void __launch_bounds__(FLY_THREADS)
+    m2l_fly32_sep_kernel(const FlyItem *__restrict__ items, int64_t nitems, unsigned long long *ctr,
+                         const int32_t *__restrict__ rowpid, const int32_t *__restrict__ cpid,
+                         const int32_t *__restrict__ cws, const float *__restrict__ pts4, float *ws, float scale) {
+    constexpr int TPR = 8, HALF = FLY_ROWS / 2;
+    static_assert(HALF * TPR == FLY_THREADS, "two rows per thread");
+    __shared__ __align__(16) float4 sc[FLY_TILE];
+    __shared__ long long s_it;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_it = (long long)atomicAdd(ctr, 1ull);
+        __syncthreads();
+        const long long it = s_it;
+        if (it >= nitems) return;
+        const FlyItem m = items[it];
+        const int row = threadIdx.x / TPR, sub = threadIdx.x - row * TPR;
+        const bool h0 = row < m.nrows, h1 = row + HALF < m.nrows;
+        float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+        if (h0) a0 = reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + row]];
+        if (h1) a1 = reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + row + HALF]];
+        float acc0 = 0.f, acc1 = 0.f;
+        for (int c0 = 0; c0 < m.ncols; c0 += FLY_TILE) {
+            const int nc = m.ncols - c0 < FLY_TILE ? m.ncols - c0 : FLY_TILE;
+            __syncthreads();
+            for (int c = threadIdx.x; c < nc; c += FLY_THREADS) {
+                const int64_t e = m.cbeg + c0 + c;
+                float4 q = reinterpret_cast<const float4 *>(pts4)[cpid[e]];
+                q.w = ws[cws[e]];
+                sc[c] = q;
+            }
+            __syncthreads();
+            if (h0) {
+#pragma unroll 4
+                for (int c = sub; c < nc; c += TPR) {
+                    const float4 q = sc[c];
+                    const float x0 = a0.x - q.x, y0 = a0.y - q.y, x1 = a1.x - q.x, y1 = a1.y - q.y;
+                    float r0 = fmaf(y0, y0, x0 * x0), r1 = fmaf(y1, y1, x1 * x1);
+                    if (DIM == 3) {
+                        const float z0 = a0.z - q.z, z1 = a1.z - q.z;
+                        r0 = fmaf(z0, z0, r0);
+                        r1 = fmaf(z1, z1, r1);
+                    }
+                    acc0 = fmaf(fly_g32<DIM, CH>(r0), q.w, acc0);
+                    // a row past the item's last reads distance 0 to nothing useful: its sum is dropped
+                    acc1 = fmaf(fly_g32<DIM, CH>(h1 ? r1 : 1.f), q.w, acc1);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 1; o < TPR; o <<= 1) {
+            acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
+            acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
+        }
+        if (sub == 0) {
+            if (h0) ws[m.dst + row] = acc0 * scale;
+            if (h1) ws[m.dst + row + HALF] = acc1 * scale;
+        }
+    }
+}
+
+// ---- double-FP32 form (FP64-accurate far M2L on the FP32 pipes) ---------
+//
+// GB300 runs FP64 at 1/64 of its FP32 rate, and the FP64 entries spend it on
+// the logarithm. Here every value is an unevaluated pair of floats (hi + lo,
+// about 2^-48 relative) and every operation an error-free transformation:
+// TwoSum (Knuth), TwoProduct with the FMA (Ogita, Rump and Oishi 2005), the
+// pair arithmetic of Dekker (1971). The points are split once into (hi, lo)
+// pairs; R^2 is formed from pair differences; log(R^2) follows Tang's
+// table-driven method (ACM TOMS 16(4), 1990): R^2 = 2^e m, m in [1, 2),
+// c_k the centre of the 1/128-wide bin of m (exact in FP32), log m =
+// log c_k + log(1 + u) with u = (m - c_k) / c_k, |u| <= 2^-8, log c_k and
+// 1 / c_k from a table of pairs computed on the host in FP64, and
+// log(1 + u) = u - u^2/2 + u^3 (1/3 - u/4 + u^2/5) (the u^6 term is below
+// 2^-50); e log 2 with log 2 split so that e * hi is exact. Each row's sum
+// is a pair; the kernel's constant multiplies it once. For the kernels built
+// on log(R^2) (3D RBF, 2D integral equation) with every far pair farther
+// apart than a; the others keep the FP64 form.
+struct Df { float h, l; };
+__device__ __forceinline__ Df df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ Df df_fast(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ Df df_add(Df a, Df b) {
+    const Df s = df_two_sum(a.h, b.h);
+    return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ Df df_sub(Df a, Df b) { return df_add(a, Df{-b.h, -b.l}); }
+// (a.h + a.l)^2, not renormalised: hi and a correction below 2^-22 |hi|
+__device__ __forceinline__ Df df_sqr(Df a) {
+    const float p = __fmul_rn(a.h, a.h);
+    return {p, __fmaf_rn(__fadd_rn(a.h, a.h), a.l, __fmaf_rn(a.h, a.h, -p))};
+}
+__device__ __forceinline__ Df df_mul(Df a, Df b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return df_fast(p, e);
+}
+
+struct DfLogTab { float c, lh, ll, ih, il, pad0, pad1, pad2; };  // bin centre, log c (pair), 1/c (pair)
+
+// log(R^2) as a pair, R^2 = r.h + r.l > 0 and normal
+__device__ __forceinline__ Df df_log(Df r, const DfLogTab *tab) {
+    const int bits = __float_as_int(r.h);
+    const int e = (bits >> 23) - 127;
+    const int k = (bits >> 16) & 0x7f;
+    const float m = __int_as_float((bits & 0x7fffff) | 0x3f800000);
+    const DfLogTab t = tab[k];
+    const float d = __fsub_rn(m, t.c);                                   // exact (Sterbenz)
+    const float lm = __fmul_rn(r.l, __int_as_float((127 - e) << 23));   // r.l / 2^e, exact
+    const Df dd = df_two_sum(d, lm);
+    // u = dd / c as a pair
+    const float uh = __fmul_rn(dd.h, t.ih);
+    float ue = __fmaf_rn(dd.h, t.ih, -uh);
+    ue = __fmaf_rn(dd.h, t.il, ue);
+    ue = __fmaf_rn(dd.l, t.ih, ue);
+    const Df u = df_fast(uh, ue);
+    // log(1 + u) = u - u^2/2 + u^3 (1/3 - u/4 + u^2/5)
+    const Df u2 = df_sqr(u);
+    const float poly = __fmaf_rn(u.h, __fmaf_rn(u.h, 0.2f, -0.25f), 0.33333334f);
+    const float tail = __fmul_rn(__fmul_rn(u2.h, u.h), poly);
+    Df l1 = df_add(u, Df{-0.5f * u2.h, __fmaf_rn(-0.5f, u2.l, tail)});
+    // + e log 2 (hi exact for |e| < 128) + log c
+    const float ln2h = 0.693145751953125f, ln2l = 1.42860676533018704e-6f;
+    const Df el = df_fast(__fmul_rn((float)e, ln2h), __fmul_rn((float)e, ln2l));
+    const Df lc = Df{t.lh, t.ll};
+    return df_add(df_add(el, lc), l1);
+}
+
+// the FP64-accurate far M2L: rows' sums as pairs times `scale`, into an FP64 workspace
+template <int DIM>
+__global__ void __launch_bounds__(FLY_THREADS)
+    m2l_flydf_kernel(const FlyItem *__restrict__ items, int64_t nitems, unsigned long long *ctr,
+                     const int32_t *__restrict__ rowpid, const int32_t *__restrict__ cpid,
+                     const int32_t *__restrict__ cws, const float *__restrict__ ptsdf, double *ws,
+                     const DfLogTab *__restrict__ gtab, double scale) {
+    __shared__ __align__(16) float sc[FLY_TILE][8];  // x, y, z hi; x, y, z lo; value hi, lo
+    __shared__ __align__(16) DfLogTab tab[128];
+    __shared__ long long s_it;
+    for (int i = threadIdx.x; i < 128; i += FLY_THREADS) tab[i] = gtab[i];
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_it = (long long)atomicAdd(ctr, 1ull);
+        __syncthreads();
+        const long long it = s_it;
+        if (it >= nitems) return;
+        const FlyItem m = items[it];
+        const int row = threadIdx.x / FLY_TPR, sub = threadIdx.x - row * FLY_TPR;
+        const bool has = row < m.nrows;
+        float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (has) {
+            const float4 *q = reinterpret_cast<const float4 *>(ptsdf) + 2 * (int64_t)rowpid[m.rows + row];
+            const float4 hi = q[0], lo = q[1];
+            a[0] = hi.x; a[1] = hi.y; a[2] = hi.z; a[4] = lo.x; a[5] = lo.y; a[6] = lo.z;
+        }
+        Df acc{0.f, 0.f};
+        for (int c0 = 0; c0 < m.ncols; c0 += FLY_TILE) {
+            const int nc = m.ncols - c0 < FLY_TILE ? m.ncols - c0 : FLY_TILE;
+            __syncthreads();
+            for (int c = threadIdx.x; c < nc; c += FLY_THREADS) {
+                const int64_t e = m.cbeg + c0 + c;
+                const float4 *q = reinterpret_cast<const float4 *>(ptsdf) + 2 * (int64_t)cpid[e];
+                const float4 hi = q[0], lo = q[1];
+                const double v = ws[cws[e]];
+                const float vh = (float)v;
+                const float vl = (float)(v - (double)vh);
+                reinterpret_cast<float4 *>(sc[c])[0] = make_float4(hi.x, hi.y, hi.z, lo.x);
+                reinterpret_cast<float4 *>(sc[c])[1] = make_float4(lo.y, lo.z, vh, vl);
+            }
+            __syncthreads();
+            if (has) {
+                for (int c = sub; c < nc; c += FLY_TPR) {
+                    const float4 p0 = reinterpret_cast<const float4 *>(sc[c])[0];
+                    const float4 p1 = reinterpret_cast<const float4 *>(sc[c])[1];
+                    const Df dx = df_sub(Df{a[0], a[4]}, Df{p0.x, p0.w});
+                    const Df dy = df_sub(Df{a[1], a[5]}, Df{p0.y, p1.x});
+                    const Df sx = df_sqr(dx), sy = df_sqr(dy);
+                    Df r2 = df_add(sx, sy);
+                    if (DIM == 3) r2 = df_add(r2, df_sqr(df_sub(Df{a[2], a[6]}, Df{p0.z, p1.y})));
+                    const Df lg = df_log(r2, tab);
+                    // acc += lg * v
+                    const float ph = __fmul_rn(lg.h, p1.z);
+                    float pe = __fmaf_rn(lg.h, p1.z, -ph);
+                    pe = __fmaf_rn(lg.h, p1.w, pe);
+                    pe = __fmaf_rn(lg.l, p1.z, pe);
+                    const Df s2 = df_two_sum(acc.h, ph);
+                    acc = df_fast(s2.h, __fadd_rn(s2.l, __fadd_rn(acc.l, pe)));
+                }
+            }
+        }
+        // partial sums of a row's four threads (pairs)
+#pragma unroll
+        for (int o = 1; o < FLY_TPR; o <<= 1) {
+            const Df b{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
+            acc = df_add(acc, b);
+        }
+        if (has && sub == 0) ws[m.dst + row] = ((double)acc.h + (double)acc.l) * scale;
+    }
+}
+
 static int fly_sms() {
     static int n = 0;
     if (n == 0) {
@@ -206,10 +428,112 @@ cudaError_t launch_fly_f64(const FlyItem *items, int64_t nitems, unsigned long l
     return fly_dispatch<double>(items, nitems, ctr, rowpid, cpid, cws, kp.pts, ws, kp, FlyK32{}, st);
 }
 
+template <int DIM, int CH>
+static cudaError_t fly32_sep_launch(const FlyItem *items, int64_t nitems, unsigned long long *ctr,
+                                    const int32_t *rowpid, const int32_t *cpid, const int32_t *cws, const float *pts4,
+                                    float *ws, float scale, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, m2l_fly32_sep_kernel<DIM, CH>, FLY_THREADS, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    const int64_t cap = (int64_t)fly_sms() * per_sm;
+    const int grid = (int)(nitems < cap ? nitems : cap);
+    cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    m2l_fly32_sep_kernel<DIM, CH><<<grid, FLY_THREADS, 0, st>>>(items, nitems, ctr, rowpid, cpid, cws, pts4, ws, scale);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fly_f32(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
                            const int32_t *cpid, const int32_t *cws, const float *pts4, float *ws, const KParams &kp,
                            const FlyK32 &k32, cudaStream_t st) {
+    if (nitems <= 0) return cudaSuccess;
+    if (k32.sep) {  // every far pair farther apart than a: one function of R^2 times a constant
+        const double ln2 = 0.69314718055994530942;
+        if (kp.dim == 3 && kp.choice == 1)
+            return fly32_sep_launch<3, 1>(items, nitems, ctr, rowpid, cpid, cws, pts4, ws,
+                                          (float)(0.5 * ln2 / kp.loga), st);
+        if (kp.dim == 3 && kp.choice == 0)
+            return fly32_sep_launch<3, 0>(items, nitems, ctr, rowpid, cpid, cws, pts4, ws, (float)(1.0 / kp.four_pi),
+                                          st);
+        if (kp.dim == 2 && kp.choice == 0)
+            return fly32_sep_launch<2, 0>(items, nitems, ctr, rowpid, cpid, cws, pts4, ws, (float)(kp.c2d * ln2), st);
+        if (kp.dim == 2 && kp.choice == 1)
+            return fly32_sep_launch<2, 1>(items, nitems, ctr, rowpid, cpid, cws, pts4, ws, k32.a, st);
+    }
     return fly_dispatch<float>(items, nitems, ctr, rowpid, cpid, cws, pts4, ws, kp, k32, st);
+}
+
+template <int DIM>
+static cudaError_t flydf_launch(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                                const int32_t *cpid, const int32_t *cws, const float *ptsdf, double *ws,
+                                const DfLogTab *tab, double scale, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, m2l_flydf_kernel<DIM>, FLY_THREADS, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    const int64_t cap = (int64_t)fly_sms() * per_sm;
+    const int grid = (int)(nitems < cap ? nitems : cap);
+    cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    m2l_flydf_kernel<DIM><<<grid, FLY_THREADS, 0, st>>>(items, nitems, ctr, rowpid, cpid, cws, ptsdf, ws, tab, scale);
+    count_launch();
+    return cudaGetLastError();
+}
+
+bool fly_df_supported(const KParams &kp, const FlyK32 &k32) {
+    return k32.sep && ((kp.dim == 3 && kp.choice == 1) || (kp.dim == 2 && kp.choice == 0));
+}
+
+cudaError_t launch_fly_df64(const FlyItem *items, int64_t nitems, unsigned long long *ctr, const int32_t *rowpid,
+                            const int32_t *cpid, const int32_t *cws, const float *ptsdf, const void *logtab,
+                            double *ws, const KParams &kp, const FlyK32 &k32, cudaStream_t st) {
+    if (nitems <= 0) return cudaSuccess;
+    if (!fly_df_supported(kp, k32))
+        return fly_dispatch<double>(items, nitems, ctr, rowpid, cpid, cws, kp.pts, ws, kp, FlyK32{}, st);
+    const DfLogTab *tab = reinterpret_cast<const DfLogTab *>(logtab);
+    if (kp.dim == 3) return flydf_launch<3>(items, nitems, ctr, rowpid, cpid, cws, ptsdf, ws, tab, 0.5 / kp.loga, st);
+    return flydf_launch<2>(items, nitems, ctr, rowpid, cpid, cws, ptsdf, ws, tab, kp.c2d, st);
+}
+
+// The log table of the double-FP32 form: 128 bins of [1, 2), centre
+// c_k = 1 + (2k + 1) / 256 (exact in FP32), log c_k and 1 / c_k as (hi, lo)
+// pairs of their FP64 values. 8 floats per entry.
+void fly_df_logtab(float *out) {
+    for (int k = 0; k < 128; ++k) {
+        const double c = 1.0 + (2.0 * k + 1.0) / 256.0, l = std::log(c), i = 1.0 / c;
+        const float lh = (float)l, ih = (float)i;
+        float *t = out + 8 * k;
+        t[0] = (float)c;
+        t[1] = lh;
+        t[2] = (float)(l - (double)lh);
+        t[3] = ih;
+        t[4] = (float)(i - (double)ih);
+        t[5] = t[6] = t[7] = 0.f;
+    }
+}
+
+// (x, y, z, 0) hi and lo FP32 quadruples of the FP64 points (N x dim): x = hi + lo to 2^-48.
+__global__ void ptsdf_kernel(const double *__restrict__ pts, int dim, int64_t n, float *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int d = 0; d < dim; ++d) {
+            const double v = pts[i * dim + d];
+            h[d] = (float)v;
+            l[d] = (float)(v - (double)h[d]);
+        }
+        reinterpret_cast<float4 *>(out)[2 * i] = make_float4(h[0], h[1], h[2], h[3]);
+        reinterpret_cast<float4 *>(out)[2 * i + 1] = make_float4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+cudaError_t launch_ptsdf(const double *pts, int dim, int64_t n, float *out, cudaStream_t st) {
+    ptsdf_kernel<<<fly_sms() * 4, 256, 0, st>>>(pts, dim, n, out);
+    count_launch();
+    return cudaGetLastError();
 }
 
 // (x, y, z, 0) FP32 quadruples of the FP64 points (N x dim).

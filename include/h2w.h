@@ -196,7 +196,8 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 before it is cut into row chunks (default 16384); also
  *                 re-cuts after assembly.
  *  H2W_OPT_IR_RESIDUAL  precision of the refinement residuals after the
- *                 first in h2w_gmres_ir_batch: H2W_PREC_FP64 (default) or
+ *                 first in h2w_gmres_ir_batch (and in h2w_gmres_ir with the
+ *                 far field on the fly): H2W_PREC_FP64 (default) or
  *                 H2W_PREC_DF64. (The first residual, at the caller's x0, is
  *                 formed with the FP32 operator and is not tested for
  *                 convergence; the inner solve only needs it to the inner
@@ -254,7 +255,12 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 are most of the entries). Takes effect at the next
  *                 h2w_assemble; multi-vector products and many-problem
  *                 batches need the stored form (H2W_ERR_STATE). 0 (default):
- *                 stored. The storage count stays the reference's. */
+ *                 stored. The storage count stays the reference's. In this
+ *                 mode one-column products also take H2W_PREC_DF64 (the far
+ *                 M2L in double-FP32 arithmetic on the FP32 pipes, FP64
+ *                 accuracy, for the kernels built on log(R^2); the stored
+ *                 passes in FP64), and h2w_gmres_ir forms its accurate
+ *                 residuals that way when H2W_OPT_IR_RESIDUAL is DF64. */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
        H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8,
        H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10, H2W_OPT_FAR_ON_THE_FLY = 11 };

@@ -1,7 +1,8 @@
 """The far-field M2L evaluated during the product (H2W_OPT_FAR_ON_THE_FLY)
 against the stored operator on the same pivots: FP64 products equal to
 1e-13 (the same entries, summed in another order), FP32 products within FP32
-accuracy, GMRES and the mixed-precision solve reaching the same tolerance;
+accuracy, the double-FP32 form within 1e-12, GMRES and the mixed-precision
+solve (FP64 or double-FP32 residuals) reaching the same tolerance;
 the storage count stays the reference's; multi-vector products refuse."""
 import numpy as np
 import pytest
@@ -63,5 +64,12 @@ def test_far_on_the_fly_matches_stored(gpu, case):
     xm, outer, inner, rm = fl.gmres_ir(b, max_outer=20, inner_iter=200, tol_pow=10)
     assert rm < 1e-10
     assert relerr(st.matvec(xm), b) < 1e-10
+    # the FP64-accurate double-FP32 form of the far field (FP64 where it has none)
+    x = synth.normal(synth.config_seed(74, 2), st.N)
+    assert relerr(fl.matvec(x, precision=hw.PREC_DF64), st.matvec(x)) <= 1e-12
+    fl.set_option(hw.OPT_IR_RESIDUAL, hw.PREC_DF64)
+    xd, outer, inner, rd = fl.gmres_ir(b, max_outer=20, inner_iter=200, tol_pow=10)
+    assert rd < 1e-10
+    assert relerr(st.matvec(xd), b) < 1e-10
     with pytest.raises(hw.H2WError):
         fl.matvec(np.stack([x1, x2], axis=1))
