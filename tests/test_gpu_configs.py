@@ -287,3 +287,43 @@ def test_cfg4_batch_vs_oracle(gpu):
         _, ito, _ = o.gmres(bs, max_iter=400, tol_pow=10)
         assert abs(int(it[p]) - ito) <= 1, (p, sizes[p], it[p], ito)
     assert np.all(res < 1e-10)
+
+
+@pytest.mark.gpu
+def test_cfg4_all_256_problems(gpu):
+    """The many-problem configuration at its full size: 256 2D problems, N
+    log-uniform in [1024, 65536] (3.7 M points), uniform random points,
+    choices alternating, tol 1e-8, one batch (one launch per product for all
+    of them) solved by the mixed-precision lockstep GMRES to 1e-10. Every
+    problem's FP64 residual is checked with its own handle's product; the
+    RBF problems (IEEE-exact entries) among the smallest ones are checked
+    against the oracle: storage bit-exact, batched product <= 1e-13."""
+    from oracle import Oracle
+    hw = gpu
+    sizes = cfg4_sizes(256, 1024, 65536)
+    ops = []
+    for i, n in enumerate(sizes):
+        nl = max(1, int(np.ceil(np.log(n / 64.0) / np.log(4.0))))
+        op = gpu_op(hw, 2, hw.FORM_NESTED, i % 2, 8, nl, n,
+                    pts=synth.uniform_points(synth.config_seed(4, 2000 + i), n, 2))
+        op.assemble(hw.ASSEMBLE_NCA)
+        ops.append(op)
+    B = hw.Batch(ops)
+    assert B.N == sum(sizes)
+    x = synth.normal(synth.config_seed(4, 79), B.N)
+    y = B.matvec(x)
+    small = sorted((n, i) for i, n in enumerate(sizes) if i % 2 == 1)[:4]
+    for n, i in small:
+        op = ops[i]
+        nl = max(1, int(np.ceil(np.log(n / 64.0) / np.log(4.0))))
+        o = Oracle(2, 0, op.points(), nl, 8, 1, n, n)
+        assert op.storage_entries() == o.memory(), i
+        assert relerr(B.split(y)[i], o.matvec(B.split(x)[i])) <= 1e-13, i
+    xt = synth.normal(synth.config_seed(4, 80), B.N)
+    rhs = B.matvec(xt)
+    xs, outer, inner, res = B.gmres_ir(rhs, max_outer=20, inner_iter=200, tol_pow=10)
+    assert np.all(res < 1e-10), res.max()
+    worst = max(relerr(op.matvec(xp), bp) for op, xp, bp in zip(ops, B.split(xs), B.split(rhs)))
+    assert worst < 1e-10, worst
+    print("cfg4: 256 problems, %d points; mixed solve %d outer / %d inner lockstep steps, worst FP64 residual %.2e"
+          % (B.N, outer, inner, worst))
