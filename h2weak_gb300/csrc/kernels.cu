@@ -660,13 +660,13 @@ __global__ void __launch_bounds__(BRG_THREADS, 4)
 // resident, so the producers of a waiting target are all claimed and running.
 template <class T>
 __global__ void __launch_bounds__(BRG_THREADS, 4)
-    brg_flow_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t nt, int32_t *ctr,
-                    int32_t *rem, const int64_t *__restrict__ coff, const int32_t *__restrict__ cidx,
+    brg_flow_kernel(const int64_t *__restrict__ roff, const int64_t *__restrict__ blob, int64_t t0, int64_t nt,
+                    int32_t *ctr, int32_t *rem, const int64_t *__restrict__ coff, const int32_t *__restrict__ cidx,
                     const T *__restrict__ A, T *ws, const double *__restrict__ xin, double *yout,
                     const int32_t *__restrict__ perm, int32_t *err) {
     __shared__ BrgShared<T> sh;
     __shared__ int64_t s_next;
-    int64_t t = blockIdx.x;
+    int64_t t = t0 + blockIdx.x;
     while (t < nt) {
         if (threadIdx.x == 0) {
             long long it = 0;
@@ -685,7 +685,7 @@ __global__ void __launch_bounds__(BRG_THREADS, 4)
         if (threadIdx.x < 32) {
             __threadfence();  // this CTA's results are visible before its consumers are released
             for (int64_t e = coff[t] + threadIdx.x; e < coff[t + 1]; e += 32) atomicSub(rem + cidx[e], 1);
-            if (threadIdx.x == 0) s_next = gridDim.x + atomicAdd(ctr, 1);
+            if (threadIdx.x == 0) s_next = t0 + gridDim.x + atomicAdd(ctr, 1);
         }
         __syncthreads();
         t = s_next;
@@ -770,10 +770,11 @@ static cudaError_t launch_coop_t(const int64_t *roff, const int64_t *blob, const
 }
 
 template <class T>
-static cudaError_t launch_brg_flow_t(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+static cudaError_t launch_brg_flow_t(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t nt, int32_t *ctr,
+                                     int32_t *rem,
                                      const int64_t *coff, const int32_t *cidx, const T *A, T *ws, const double *xin,
                                      double *yout, const int32_t *perm, int32_t *err, cudaStream_t st) {
-    if (nt <= 0) return cudaSuccess;
+    if (nt <= t0) return cudaSuccess;
     static int per_sm = 0;
     if (g_num_sms == 0) {
         int dev = 0;
@@ -786,7 +787,7 @@ static cudaError_t launch_brg_flow_t(const int64_t *roff, const int64_t *blob, i
         if (per_sm <= 0) return cudaErrorCooperativeLaunchTooLarge;
     }
     const int grid = g_num_sms * per_sm;
-    void *args[] = {(void *)&roff, (void *)&blob, (void *)&nt,   (void *)&ctr,  (void *)&rem,
+    void *args[] = {(void *)&roff, (void *)&blob, (void *)&t0, (void *)&nt,   (void *)&ctr,  (void *)&rem,
                     (void *)&coff, (void *)&cidx, (void *)&A,    (void *)&ws,   (void *)&xin,
                     (void *)&yout, (void *)&perm, (void *)&err};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)brg_flow_kernel<T>, dim3(grid), dim3(BRG_THREADS), args,
@@ -794,15 +795,15 @@ static cudaError_t launch_brg_flow_t(const int64_t *roff, const int64_t *blob, i
     count_launch();
     return e;
 }
-cudaError_t launch_brg_flow_f64(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+cudaError_t launch_brg_flow_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t nt, int32_t *ctr, int32_t *rem,
                                 const int64_t *coff, const int32_t *cidx, const double *A, double *ws,
                                 const double *xin, double *yout, const int32_t *perm, int32_t *err, cudaStream_t st) {
-    return launch_brg_flow_t<double>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, perm, err, st);
+    return launch_brg_flow_t<double>(roff, blob, t0, nt, ctr, rem, coff, cidx, A, ws, xin, yout, perm, err, st);
 }
-cudaError_t launch_brg_flow_f32(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+cudaError_t launch_brg_flow_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t nt, int32_t *ctr, int32_t *rem,
                                 const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const double *xin,
                                 double *yout, const int32_t *perm, int32_t *err, cudaStream_t st) {
-    return launch_brg_flow_t<float>(roff, blob, nt, ctr, rem, coff, cidx, A, ws, xin, yout, perm, err, st);
+    return launch_brg_flow_t<float>(roff, blob, t0, nt, ctr, rem, coff, cidx, A, ws, xin, yout, perm, err, st);
 }
 
 cudaError_t launch_coop_f64(const int64_t *roff, const int64_t *blob, const int64_t *pstart, int nphase,

@@ -63,12 +63,12 @@ cudaError_t launch_brg_f64(const int64_t *roff, const int64_t *blob, int64_t t0,
 cudaError_t launch_brg_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t t1, const float *A,
                            float *ws, const double *xin, double *yout, const int32_t *perm, cudaStream_t st);
 // Dataflow form of the single-vector product (see launch_mr_f32_flow):
-// nt targets in stored order, ctr a zeroed claim counter, rem the producer
+// targets [t0, nt) in stored order, ctr a zeroed claim counter, rem the producer
 // counts (reset before every launch), consumers in cidx[coff[t] .. coff[t+1])
-cudaError_t launch_brg_flow_f64(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+cudaError_t launch_brg_flow_f64(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t nt, int32_t *ctr, int32_t *rem,
                                 const int64_t *coff, const int32_t *cidx, const double *A, double *ws,
                                 const double *xin, double *yout, const int32_t *perm, int32_t *err, cudaStream_t st);
-cudaError_t launch_brg_flow_f32(const int64_t *roff, const int64_t *blob, int64_t nt, int32_t *ctr, int32_t *rem,
+cudaError_t launch_brg_flow_f32(const int64_t *roff, const int64_t *blob, int64_t t0, int64_t nt, int32_t *ctr, int32_t *rem,
                                 const int64_t *coff, const int32_t *cidx, const float *A, float *ws, const double *xin,
                                 double *yout, const int32_t *perm, int32_t *err, cudaStream_t st);
 // The whole matvec as one cooperative launch: phase p covers targets
