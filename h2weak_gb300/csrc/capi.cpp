@@ -2,6 +2,7 @@
 // C ABI of the GB300 H2* / (H2+H)* library: handle, tree, GPU assembly,
 // packed-operator plan, matvec launches and device-resident GMRES.
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <climits>
 #include <cmath>
@@ -130,6 +131,7 @@ struct h2w_handle {
     DBuf<unsigned> d_bar;
     bool coop = true;  // one cooperative launch per matvec (else one launch per phase)
     int64_t spin_limit = 0;  // polls per grid-barrier wait of the single-vector cooperative launch (0: built-in)
+    bool nca_df = true;      // group NCA of log kernels in double-FP32 arithmetic (H2W_OPT_NCA_DF)
     // far-field M2L evaluated during each single-vector product instead of stored
     // (H2W_OPT_FAR_ON_THE_FLY, applies at assembly): work items, row / column
     // point ids, source workspace rows, claim counter, FP32 coordinates, and the
@@ -411,7 +413,9 @@ void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, cons
                 mw += (n1 + 31) / 32 + (n2 + 31) / 32;
                 dcap = std::max(dcap, rc);
             }
-            const int grid = nca_group_grid(dcap);
+            // kernels built on log: residuals in double-FP32 arithmetic on the FP32 pipes
+            const bool df = h->nca_df && ((h->cfg.dim < 3 && h->cfg.choice == 0) || (h->cfg.dim == 3 && h->cfg.choice == 1));
+            const int grid = nca_group_grid(dcap, df);
             if (grid <= 0) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: no co-resident grid");
             const int nb = (int)probs.size();
             const int G = std::max(1, std::min(nb, grid / 32));
@@ -440,7 +444,7 @@ void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, cons
             CK(cudaMemsetAsync(derr.p, 0, 4, st));
             CK(cudaMemsetAsync(dbar.p, 0, (size_t)2 * G * sizeof(unsigned), st));
             CK(launch_nca_group(dp.p, dm.p, nb, G, grid, di.p, kp, tol, dscr.p, dmask.p, drank.p, dpr.p, dpc.p, dst.p,
-                                dbar.p, derr.p, dpartr.p, dpartc.p, ddots.p, dcap, st));
+                                dbar.p, derr.p, dpartr.p, dpartc.p, ddots.p, dcap, df, st));
             std::vector<int32_t> rk((size_t)nb), hpr((size_t)piv), hpc((size_t)piv);
             int32_t status = 0, errf = 0;
             CK(cudaMemcpyAsync(rk.data(), drank.p, rk.size() * 4, cudaMemcpyDeviceToHost, st));
@@ -485,7 +489,12 @@ void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, co
     const bool use_big = !(eb && std::string(eb) == "0");
     for (size_t p = 0; p < R.size(); ++p)
         ((use_big && (int64_t)(R[p].size() + C[p].size()) >= NCA_BIG) ? big : small).push_back(p);
+    // H2W_TIMING=1: the time of each part of the search on stderr (diagnostic)
+    static const bool timing = getenv("H2W_TIMING") && std::string(getenv("H2W_TIMING")) == "1";
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto t0 = now();
     if (!big.empty()) run_nca_big(h, R, C, big, prow, pcol);
+    auto t1 = now();
     std::vector<size_t> over;
     if (!small.empty()) {
         std::vector<std::vector<int32_t>> Rs, Cs, prs, pcs;
@@ -505,8 +514,21 @@ void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, co
                 prow[small[k]] = std::move(prs[k]);
                 pcol[small[k]] = std::move(pcs[k]);
             }
+        auto t2 = now();
         // blocks whose rank outgrew one CTA: the group search from twice that scratch
         if (!over.empty()) run_nca_big(h, R, C, over, prow, pcol, 2 * NCA_SMALL_CAP);
+        if (timing) {
+            int64_t rb = 0, rs = 0;
+            for (size_t p : big) rb += (int64_t)prow[p].size();
+            for (size_t p : small) rs += (int64_t)prow[p].size();
+            fprintf(stderr, "h2w nca: %zu group blocks %.3f s (pivots %lld); %zu one-CTA blocks %.3f s (pivots %lld); "
+                            "%zu outgrew one CTA %.3f s\n", big.size(),
+                    std::chrono::duration<double>(t1 - t0).count(), (long long)rb, small.size(),
+                    std::chrono::duration<double>(t2 - t1).count(), (long long)rs, over.size(),
+                    std::chrono::duration<double>(now() - t2).count());
+        }
+    } else if (timing) {
+        fprintf(stderr, "h2w nca: %zu group blocks %.3f s\n", big.size(), std::chrono::duration<double>(t1 - t0).count());
     }
     if (h->learn_rec) {  // training data of the large blocks: recorded through the small path's recorder
         std::vector<size_t> rec = big;
@@ -3608,6 +3630,8 @@ int h2w_assemble(h2w_handle *h, int mode) {
         if (mode == H2W_ASSEMBLE_LEARNED && !h->d_mlp.p)
             throw ApiError(H2W_ERR_STATE, "learned assembly needs a model (h2w_learn_set_model)");
         h->learned = mode == H2W_ASSEMBLE_LEARNED;
+        static const bool timing = getenv("H2W_TIMING") && std::string(getenv("H2W_TIMING")) == "1";
+        const auto ta = std::chrono::steady_clock::now();
         if (mode == H2W_ASSEMBLE_NCA || mode == H2W_ASSEMBLE_LEARNED) {
             if (t.dim > 1 && !nn) nca_far(h);
             if (!sn) nca_ver(h);
@@ -3651,7 +3675,12 @@ int h2w_assemble(h2w_handle *h, int mode) {
             for (int j = 0; j <= t.nL; ++j) h->ver[(size_t)j].ptr.assign((size_t)t.nbox[(size_t)j] + 1, 0);
         }
         if (!sn && h->pairs.empty()) h->pairs.assign((size_t)t.nL + 1, Pairs{});
+        const auto tb = std::chrono::steady_clock::now();
         build_plan(h);
+        if (timing)
+            fprintf(stderr, "h2w assembly: pivots %.3f s, operator formation %.3f s\n",
+                    std::chrono::duration<double>(tb - ta).count(),
+                    std::chrono::duration<double>(std::chrono::steady_clock::now() - tb).count());
         h->storage = storage_entries(h);
         h->has_op = true;
         h->g_m = -1;
@@ -4051,6 +4080,8 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
         } else if (option == H2W_OPT_SPIN_LIMIT) {
             if (value < 0) throw ApiError(H2W_ERR_ARG, "spin limit must be >= 0");
             h->spin_limit = value;
+        } else if (option == H2W_OPT_NCA_DF) {
+            h->nca_df = value != 0;
         } else if (option == H2W_OPT_FAR_ON_THE_FLY) {
             h->far_fly = value != 0;  // takes effect at the next h2w_assemble
         } else if (option == H2W_OPT_COOP) {
@@ -4082,6 +4113,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_PRODUCER_WARP) *value = h->producer_warp ? 1 : 0;
         else if (option == H2W_OPT_SPIN_LIMIT) *value = h->spin_limit;
         else if (option == H2W_OPT_FAR_ON_THE_FLY) *value = h->far_fly ? 1 : 0;
+        else if (option == H2W_OPT_NCA_DF) *value = h->nca_df ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });

@@ -38,14 +38,16 @@ cudaError_t launch_nca(const NcaProb *probs, int nprob, const int32_t *idx, cons
 // each group on one block at a time (same pivots as launch_nca). moff: per
 // block, offset of its row+column pivot masks (uint32 words) in masks;
 // partial buffers of nca_group_part_bytes() x grid each; dots: grid x 2*dcap
+// (df: the scratch holds double-FP32 pairs and the residuals are formed in
+// double-FP32 arithmetic, for kernels built on log, see ncabig.cu)
 // + G x dcap doubles (dcap >= every block's rcap). A block whose rank reaches
 // its rcap reports -rank in rank (launch_nca does the same).
-int nca_group_grid(int dcap);
+int nca_group_grid(int dcap, bool df);
 size_t nca_group_part_bytes();
 cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int nprob, int G, int grid,
                              const int32_t *idx, const KParams &kp, double tol, double *scr, uint32_t *masks,
                              int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status, unsigned *bars,
-                             int32_t *err, void *prow_part, void *pcol_part, double *dots, int dcap,
+                             int32_t *err, void *prow_part, void *pcol_part, double *dots, int dcap, bool df,
                              cudaStream_t st);
 cudaError_t launch_factor(const FactorJob *jobs, int njobs, const int32_t *idx, const KParams &kp, double *F,
                           cudaStream_t st);

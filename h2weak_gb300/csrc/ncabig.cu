@@ -96,13 +96,72 @@ __device__ void ng_group(const NgPart *part, int g, int G, int S, double &v, int
 }
 __device__ __forceinline__ bool ng_bit(const uint32_t *m, int i) { return (m[i >> 5] >> (i & 31)) & 1u; }
 
+// Scratch element types of the group search. double: the reference's FP64
+// operations in its order (bitwise its residuals for equal entries). float2:
+// double-FP32 pairs (hi + lo, about 2^-48 relative; TwoSum / TwoProduct
+// error-free transformations) on the FP32 pipes, for the kernels whose
+// entries already differ from the reference's in the last bit (they use log):
+// GB300 runs FP64 at 1/64 of the FP32 rate, and the residual updates, a
+// product and a subtraction per kept term and entry, are the search's work.
+// The squares and the stopping test's dots only need FP32 there.
+template <class E> struct NgOps;
+template <> struct NgOps<double> {
+    using Acc = double;
+    static __device__ __forceinline__ double from(double d) { return d; }
+    static __device__ __forceinline__ double mag(double e) { return fabs(e); }
+    static __device__ __forceinline__ double submul(double v, double c, double x) {
+        return __dsub_rn(v, __dmul_rn(c, x));
+    }
+    static __device__ __forceinline__ double inv(double p) { return p; }  // divided exactly below
+    static __device__ __forceinline__ double div(double c, double p) { return __ddiv_rn(c, p); }
+    static __device__ __forceinline__ double sq(double e) { return e * e; }
+    static __device__ __forceinline__ double dot(double a, double b) { return a * b; }
+};
+template <> struct NgOps<float2> {
+    using Acc = float;
+    static __device__ __forceinline__ float2 from(double d) {
+        const float h = __double2float_rn(d);
+        return make_float2(h, __double2float_rn(d - (double)h));
+    }
+    static __device__ __forceinline__ double mag(float2 e) { return (double)fabsf(e.x); }
+    // renormalised pair of a + b (TwoSum of the high parts, the lows added)
+    static __device__ __forceinline__ float2 add(float ah, float al, float bh, float bl) {
+        const float s = __fadd_rn(ah, bh), bb = __fsub_rn(s, ah);
+        const float e = __fadd_rn(__fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb)), __fadd_rn(al, bl));
+        const float h = __fadd_rn(s, e);
+        return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+    }
+    static __device__ __forceinline__ float2 mul(float2 a, float2 b) {
+        const float p = __fmul_rn(a.x, b.x);
+        float e = __fmaf_rn(a.x, b.x, -p);
+        e = __fmaf_rn(a.x, b.y, e);
+        e = __fmaf_rn(a.y, b.x, e);
+        const float h = __fadd_rn(p, e);
+        return make_float2(h, __fsub_rn(e, __fsub_rn(h, p)));
+    }
+    static __device__ __forceinline__ float2 submul(float2 v, float2 c, float2 x) {
+        const float p = __fmul_rn(c.x, x.x);
+        float e = __fmaf_rn(c.x, x.x, -p);
+        e = __fmaf_rn(c.x, x.y, e);
+        e = __fmaf_rn(c.y, x.x, e);
+        return add(v.x, v.y, -p, -e);
+    }
+    static __device__ __forceinline__ float2 inv(float2 p) { return from(1.0 / ((double)p.x + (double)p.y)); }
+    static __device__ __forceinline__ float2 div(float2 c, float2 ip) { return mul(c, ip); }
+    static __device__ __forceinline__ float sq(float2 e) { return e.x * e.x; }
+    static __device__ __forceinline__ float dot(float2 a, float2 b) { return a.x * b.x; }
+};
+
+template <class E>
 __global__ void __launch_bounds__(NG_THREADS)
     nca_group_kernel(const NcaProb *__restrict__ probs, const int64_t *__restrict__ moff, int nprob, int G,
-                     const int32_t *__restrict__ idx, KParams kp, double tol, double *__restrict__ scr,
+                     const int32_t *__restrict__ idx, KParams kp, double tol, E *__restrict__ scr,
                      uint32_t *__restrict__ masks, int32_t *__restrict__ rank_out, int32_t *__restrict__ prow,
                      int32_t *__restrict__ pcol, int32_t *status, unsigned *bars, int32_t *err, NgPart *prow_part,
                      NgPart *pcol_part, double *dots, int dcap) {
-    __shared__ double ng_coef[NG_COEF];
+    using Op = NgOps<E>;
+    using Acc = typename Op::Acc;
+    __shared__ E ng_coef[NG_COEF];
     __shared__ double shv[32], shs[32];
     __shared__ int shi[32];
     const int g = blockIdx.x % G, gi = blockIdx.x / G;
@@ -116,7 +175,7 @@ __global__ void __launch_bounds__(NG_THREADS)
         const NcaProb pb = probs[b];
         const int n1 = pb.n1, n2 = pb.n2, rcap = pb.rcap;
         const int32_t *I = idx + pb.ri, *J = idx + pb.ci;
-        double *U = scr + pb.u, *V = scr + pb.v;
+        E *U = scr + pb.u, *V = scr + pb.v;
         uint32_t *rm = masks + moff[b], *cm = rm + (n1 + 31) / 32;
         for (int q = gi * NG_THREADS + tid; q < (n1 + 31) / 32 + (n2 + 31) / 32; q += cstride) rm[q] = 0u;
         if (gi == 0 && tid == 0) rank_out[b] = 0;
@@ -132,7 +191,7 @@ __global__ void __launch_bounds__(NG_THREADS)
             int i0 = INT_MAX;
             for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) {
                 const double v = kentry(kp, I[l], J[s2]);
-                V[s2] = v;
+                V[s2] = Op::from(v);
                 const double a = fabs(v);
                 if (ng_better(a, s2, v0, i0)) { v0 = a; i0 = s2; }
             }
@@ -143,24 +202,25 @@ __global__ void __launch_bounds__(NG_THREADS)
             ng_barrier(bar, S, err);  // the partials are read before the next row overwrites them
         }
         if (ri < 0) continue;
-        const double piv0 = V[ci];
+        const E piv0 = Op::inv(V[ci]);
         // first column; the first row's squares
         {
-            double v0 = -1.0, us = 0.0, vs = 0.0;
+            double v0 = -1.0;
+            Acc us = 0, vs = 0;
             int i0 = INT_MAX;
             for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) {
                 const double c = kentry(kp, I[t], J[ci]);
-                const double u = __ddiv_rn(c, piv0);
+                const E u = Op::div(Op::from(c), piv0);
                 U[t] = u;
-                us += u * u;
+                us += Op::sq(u);
                 if (t != ri) {
                     const double a = fabs(c);
                     if (ng_better(a, t, v0, i0)) { v0 = a; i0 = t; }
                 }
             }
-            for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) vs += V[s2] * V[s2];
-            ng_cta_part(v0, i0, us, pcol_part + blockIdx.x, shv, shi, shs);
-            ng_cta_part(-1.0, INT_MAX, vs, prow_part + blockIdx.x, shv, shi, shs);
+            for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) vs += Op::sq(V[s2]);
+            ng_cta_part(v0, i0, (double)us, pcol_part + blockIdx.x, shv, shi, shs);
+            ng_cta_part(-1.0, INT_MAX, (double)vs, prow_part + blockIdx.x, shv, shi, shs);
         }
         ng_barrier(bar, S, err);
         double nu, nv;
@@ -196,8 +256,9 @@ __global__ void __launch_bounds__(NG_THREADS)
             }
             // residual row ri over this CTA's columns (kept terms subtracted in
             // pivot order, chunk by chunk); column pivot
-            double *Vr = V + (size_t)rank * n2;
-            double v0 = -1.0, vs = 0.0;
+            E *Vr = V + (size_t)rank * n2;
+            double v0 = -1.0;
+            Acc vs = 0;
             int i0 = INT_MAX;
             for (int l0 = 0; l0 < rank; l0 += NG_COEF) {
                 const int l1 = rank - l0 < NG_COEF ? rank : l0 + NG_COEF;
@@ -206,20 +267,19 @@ __global__ void __launch_bounds__(NG_THREADS)
                 for (int l = l0 + tid; l < l1; l += NG_THREADS) ng_coef[l - l0] = U[(size_t)l * n1 + ri];
                 __syncthreads();
                 for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) {
-                    double v = l0 == 0 ? kentry(kp, I[ri], J[s2]) : Vr[s2];
-                    for (int l = l0; l < l1; ++l)
-                        v = __dsub_rn(v, __dmul_rn(ng_coef[l - l0], V[(size_t)l * n2 + s2]));
+                    E v = l0 == 0 ? Op::from(kentry(kp, I[ri], J[s2])) : Vr[s2];
+                    for (int l = l0; l < l1; ++l) v = Op::submul(v, ng_coef[l - l0], V[(size_t)l * n2 + s2]);
                     Vr[s2] = v;
                     if (last) {
-                        vs += v * v;
+                        vs += Op::sq(v);
                         if (!ng_bit(cm, s2)) {
-                            const double a = fabs(v);
+                            const double a = Op::mag(v);
                             if (ng_better(a, s2, v0, i0)) { v0 = a; i0 = s2; }
                         }
                     }
                 }
             }
-            ng_cta_part(v0, i0, vs, prow_part + blockIdx.x, shv, shi, shs);
+            ng_cta_part(v0, i0, (double)vs, prow_part + blockIdx.x, shv, shi, shs);
             ng_barrier(bar, S, err);
             ng_group(prow_part, g, G, S, bv, bi, ss);
             if (bi < 0 || bi >= n2) {
@@ -228,12 +288,13 @@ __global__ void __launch_bounds__(NG_THREADS)
             }
             ci = bi;
             nv = sqrt(ss);
-            const double piv = Vr[ci];
+            const E piv = Op::inv(Vr[ci]);
             // residual column ci over this CTA's rows; next row pivot. The
             // unscaled residual is kept in Ur across chunks, scaled by the
             // pivot after the last one.
-            double *Ur = U + (size_t)rank * n1;
-            double u0 = -1.0, us = 0.0;
+            E *Ur = U + (size_t)rank * n1;
+            double u0 = -1.0;
+            Acc us = 0;
             int j0 = INT_MAX;
             for (int l0 = 0; l0 < rank; l0 += NG_COEF) {
                 const int l1 = rank - l0 < NG_COEF ? rank : l0 + NG_COEF;
@@ -242,23 +303,22 @@ __global__ void __launch_bounds__(NG_THREADS)
                 for (int l = l0 + tid; l < l1; l += NG_THREADS) ng_coef[l - l0] = V[(size_t)l * n2 + ci];
                 __syncthreads();
                 for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) {
-                    double c = l0 == 0 ? kentry(kp, I[t], J[ci]) : Ur[t];
-                    for (int l = l0; l < l1; ++l)
-                        c = __dsub_rn(c, __dmul_rn(ng_coef[l - l0], U[(size_t)l * n1 + t]));
+                    E c = l0 == 0 ? Op::from(kentry(kp, I[t], J[ci])) : Ur[t];
+                    for (int l = l0; l < l1; ++l) c = Op::submul(c, ng_coef[l - l0], U[(size_t)l * n1 + t]);
                     if (!last) {
                         Ur[t] = c;
                         continue;
                     }
-                    const double u = __ddiv_rn(c, piv);
+                    const E u = Op::div(c, piv);
                     Ur[t] = u;
-                    us += u * u;
+                    us += Op::sq(u);
                     if (t != ri && !ng_bit(rm, t)) {
-                        const double a = fabs(c);
+                        const double a = Op::mag(c);
                         if (ng_better(a, t, u0, j0)) { u0 = a; j0 = t; }
                     }
                 }
             }
-            ng_cta_part(u0, j0, us, pcol_part + blockIdx.x, shv, shi, shs);
+            ng_cta_part(u0, j0, (double)us, pcol_part + blockIdx.x, shv, shi, shs);
             ng_barrier(bar, S, err);
             int nri;
             ng_group(pcol_part, g, G, S, bv, nri, ss);
@@ -276,19 +336,19 @@ __global__ void __launch_bounds__(NG_THREADS)
             // rows and columns in a fixed order
             double *dme = dots + (size_t)blockIdx.x * 2 * dcap;
             for (int l = warp; l < rank; l += NG_THREADS / 32) {
-                const double *Ul = U + (size_t)l * n1, *Vl = V + (size_t)l * n2;
-                double du = 0.0, dv = 0.0;
+                const E *Ul = U + (size_t)l * n1, *Vl = V + (size_t)l * n2;
+                Acc du = 0, dv = 0;
                 for (int t0 = gi * NG_THREADS; t0 < n1; t0 += cstride)
-                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n1; t += 32) du += Ul[t] * Ur[t];
+                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n1; t += 32) du += Op::dot(Ul[t], Ur[t]);
                 for (int t0 = gi * NG_THREADS; t0 < n2; t0 += cstride)
-                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n2; t += 32) dv += Vl[t] * Vr[t];
+                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n2; t += 32) dv += Op::dot(Vl[t], Vr[t]);
                 for (int o = 16; o > 0; o >>= 1) {
                     du += __shfl_xor_sync(0xffffffffu, du, o);
                     dv += __shfl_xor_sync(0xffffffffu, dv, o);
                 }
                 if (lane == 0) {
-                    dme[2 * l] = du;
-                    dme[2 * l + 1] = dv;
+                    dme[2 * l] = (double)du;
+                    dme[2 * l + 1] = (double)dv;
                 }
             }
             ng_barrier(bar, S, err);
@@ -336,17 +396,18 @@ static int ng_sms() {
     return n;
 }
 
-int nca_group_grid(int dcap) {
+int nca_group_grid(int dcap, bool df) {
     (void)dcap;  // shared memory no longer depends on the rank
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nca_group_kernel, NG_THREADS, 0);
+    if (df) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nca_group_kernel<float2>, NG_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nca_group_kernel<double>, NG_THREADS, 0);
     return per_sm > 0 ? ng_sms() * per_sm : 0;
 }
 
 cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int nprob, int G, int grid,
                              const int32_t *idx, const KParams &kp, double tol, double *scr, uint32_t *masks,
                              int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status, unsigned *bars,
-                             int32_t *err, void *prow_part, void *pcol_part, double *dots, int dcap,
+                             int32_t *err, void *prow_part, void *pcol_part, double *dots, int dcap, bool df,
                              cudaStream_t st) {
     if (nprob <= 0) return cudaSuccess;
     NgPart *pr = reinterpret_cast<NgPart *>(prow_part), *pc = reinterpret_cast<NgPart *>(pcol_part);
@@ -354,8 +415,8 @@ cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int npro
                     (void *)&tol,   (void *)&scr,  (void *)&masks, (void *)&rank, (void *)&prow, (void *)&pcol,
                     (void *)&status, (void *)&bars, (void *)&err, (void *)&pr,   (void *)&pc,   (void *)&dots,
                     (void *)&dcap};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)nca_group_kernel, dim3(grid), dim3(NG_THREADS), args,
-                                                0, st);
+    const void *fn = df ? (const void *)nca_group_kernel<float2> : (const void *)nca_group_kernel<double>;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(NG_THREADS), args, 0, st);
     count_launch();
     return e;
 }

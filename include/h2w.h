@@ -260,10 +260,17 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 M2L in double-FP32 arithmetic on the FP32 pipes, FP64
  *                 accuracy, for the kernels built on log(R^2); the stored
  *                 passes in FP64), and h2w_gmres_ir forms its accurate
- *                 residuals that way when H2W_OPT_IR_RESIDUAL is DF64. */
+ *                 residuals that way when H2W_OPT_IR_RESIDUAL is DF64.
+ *  H2W_OPT_NCA_DF  1 (default): the pivot search of large blocks (groups of
+ *                 CTAs) for the kernels built on log (1D and 2D integral
+ *                 equation, 3D RBF), whose entries already differ from the
+ *                 reference's in the last bit, forms its residuals in
+ *                 double-FP32 arithmetic (about 2^-48 relative) on the FP32
+ *                 pipes instead of FP64; 0: FP64. The other kernels always
+ *                 search in FP64 (their pivots are bitwise the reference's). */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
        H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8,
-       H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10, H2W_OPT_FAR_ON_THE_FLY = 11 };
+       H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10, H2W_OPT_FAR_ON_THE_FLY = 11, H2W_OPT_NCA_DF = 12 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 
