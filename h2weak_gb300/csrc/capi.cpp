@@ -344,6 +344,7 @@ void run_nca_small(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, co
                    std::vector<size_t> &over);
 
 constexpr int64_t NCA_BIG = 8192;  // rows + columns from which a block gets a group of CTAs
+constexpr int64_t NCA_MED = 2048;  // ... and from which it does when one CTA per block would leave SMs idle
 constexpr int NCA_SMALL_CAP = 512;   // pivots one CTA per block holds; larger blocks move to the groups
 
 // Scratch bytes a batch of NCA blocks may take: most of the free device
@@ -418,7 +419,13 @@ void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, cons
             const int grid = nca_group_grid(dcap, df);
             if (grid <= 0) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: no co-resident grid");
             const int nb = (int)probs.size();
-            const int G = std::max(1, std::min(nb, grid / 32));
+            // groups sized to the widest block (about four residual entries per
+            // thread and pass, at least two CTAs, at most 32), as many groups
+            // as blocks while the grid allows
+            int64_t wmax = 0;
+            for (const NcaProb &pb : probs) wmax = std::max<int64_t>(wmax, (int64_t)pb.n1 + pb.n2);
+            const int smin = (int)std::min<int64_t>(32, std::max<int64_t>(2, (wmax + 2047) / 2048));
+            const int G = std::max(1, std::min(nb, grid / smin));
             DBuf<NcaProb> dp;
             DBuf<int64_t> dm;
             DBuf<int32_t> di, drank, dpr, dpc, dst, derr;
@@ -479,21 +486,38 @@ void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, cons
 // The NCA pivot search: one CTA per block (nca_kernel) in batches that fit
 // the scratch budget; blocks of NCA_BIG or more rows + columns, and blocks
 // whose rank outgrows one CTA's scratch, get groups of CTAs (run_nca_big).
+// Blocks of NCA_MED or more rows + columns get groups too when there are no
+// more of them than SMs (one CTA each would leave SMs idle), and always for
+// the kernels whose group search runs in double-FP32 arithmetic.
 // H2W_NCA_BIG=0 keeps every block that fits on one CTA.
 void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
                    std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
     prow.assign(R.size(), {});
     pcol.assign(R.size(), {});
-    std::vector<size_t> big, small;
+    std::vector<size_t> big, med, small;
     const char *eb = getenv("H2W_NCA_BIG");
     const bool use_big = !(eb && std::string(eb) == "0");
-    for (size_t p = 0; p < R.size(); ++p)
-        ((use_big && (int64_t)(R[p].size() + C[p].size()) >= NCA_BIG) ? big : small).push_back(p);
+    for (size_t p = 0; p < R.size(); ++p) {
+        const int64_t w = (int64_t)(R[p].size() + C[p].size());
+        (use_big && w >= NCA_BIG ? big : use_big && w >= NCA_MED ? med : small).push_back(p);
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, std::max(0, h->cfg.device)) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 0;
+    }
+    // kernels built on log search in double-FP32 arithmetic on the groups,
+    // faster than one CTA's FP64 whatever the count
+    const bool df = h->nca_df && ((h->cfg.dim < 3 && h->cfg.choice == 0) || (h->cfg.dim == 3 && h->cfg.choice == 1));
+    if (!df && (int64_t)med.size() > (int64_t)sms) small.insert(small.end(), med.begin(), med.end()), med.clear();
+    std::sort(small.begin(), small.end());
     // H2W_TIMING=1: the time of each part of the search on stderr (diagnostic)
     static const bool timing = getenv("H2W_TIMING") && std::string(getenv("H2W_TIMING")) == "1";
     auto now = [] { return std::chrono::steady_clock::now(); };
     auto t0 = now();
     if (!big.empty()) run_nca_big(h, R, C, big, prow, pcol);
+    auto tm = now();
+    if (!med.empty()) run_nca_big(h, R, C, med, prow, pcol, NCA_SMALL_CAP);
     auto t1 = now();
     std::vector<size_t> over;
     if (!small.empty()) {
@@ -521,17 +545,22 @@ void run_nca_plain(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, co
             int64_t rb = 0, rs = 0;
             for (size_t p : big) rb += (int64_t)prow[p].size();
             for (size_t p : small) rs += (int64_t)prow[p].size();
-            fprintf(stderr, "h2w nca: %zu group blocks %.3f s (pivots %lld); %zu one-CTA blocks %.3f s (pivots %lld); "
-                            "%zu outgrew one CTA %.3f s\n", big.size(),
-                    std::chrono::duration<double>(t1 - t0).count(), (long long)rb, small.size(),
+            int64_t rm = 0;
+            for (size_t p : med) rm += (int64_t)prow[p].size();
+            fprintf(stderr, "h2w nca: %zu group blocks %.3f s (pivots %lld); %zu medium blocks on groups %.3f s (pivots "
+                            "%lld); %zu one-CTA blocks %.3f s (pivots %lld); %zu outgrew one CTA %.3f s\n", big.size(),
+                    std::chrono::duration<double>(tm - t0).count(), (long long)rb, med.size(),
+                    std::chrono::duration<double>(t1 - tm).count(), (long long)rm, small.size(),
                     std::chrono::duration<double>(t2 - t1).count(), (long long)rs, over.size(),
                     std::chrono::duration<double>(now() - t2).count());
         }
     } else if (timing) {
-        fprintf(stderr, "h2w nca: %zu group blocks %.3f s\n", big.size(), std::chrono::duration<double>(t1 - t0).count());
+        fprintf(stderr, "h2w nca: %zu group blocks %.3f s, %zu medium blocks on groups %.3f s\n", big.size(),
+                std::chrono::duration<double>(tm - t0).count(), med.size(), std::chrono::duration<double>(t1 - tm).count());
     }
     if (h->learn_rec) {  // training data of the large blocks: recorded through the small path's recorder
         std::vector<size_t> rec = big;
+        rec.insert(rec.end(), med.begin(), med.end());
         rec.insert(rec.end(), over.begin(), over.end());
         if (!rec.empty()) {
             std::vector<std::vector<int32_t>> R2, C2, pr2, pc2;

@@ -152,8 +152,73 @@ template <> struct NgOps<float2> {
     static __device__ __forceinline__ float dot(float2 a, float2 b) { return a.x * b.x; }
 };
 
+// Subtracts the kept terms l0..l1-1 (coefficients in shared memory) from the
+// residual entries a (column base[0]) and b (base[off], when hb), in pivot
+// order; NG_UNROLL terms are loaded before their subtractions.
+constexpr int NG_UNROLL = 8;
+template <class Op, class E>
+__device__ __forceinline__ void ng_sub_terms(E &a, E &b, bool hb, const E *__restrict__ base, size_t ld, int off,
+                                             const E *coef, int l0, int l1) {
+    int l = l0;
+    for (; l + NG_UNROLL <= l1; l += NG_UNROLL) {
+        E xa[NG_UNROLL], xb[NG_UNROLL];
+#pragma unroll
+        for (int k = 0; k < NG_UNROLL; ++k) {
+            xa[k] = base[(size_t)(l + k) * ld];
+            xb[k] = hb ? base[(size_t)(l + k) * ld + off] : xa[k];
+        }
+#pragma unroll
+        for (int k = 0; k < NG_UNROLL; ++k) {
+            const E c = coef[l + k - l0];
+            a = Op::submul(a, c, xa[k]);
+            b = Op::submul(b, c, xb[k]);
+        }
+    }
+    for (; l < l1; ++l) {
+        const E c = coef[l - l0];
+        a = Op::submul(a, c, base[(size_t)l * ld]);
+        if (hb) b = Op::submul(b, c, base[(size_t)l * ld + off]);
+    }
+}
+// The last chunk's step for residual-column entry t: scaled by the pivot,
+// stored, its square summed, the row-pivot candidate updated.
+template <class Op, class E>
+__device__ __forceinline__ void ng_col_final(E c, int t, E piv, int ri, const uint32_t *rm, E *Ur,
+                                             typename Op::Acc &us, double &u0, int &j0) {
+    const E u = Op::div(c, piv);
+    Ur[t] = u;
+    us += Op::sq(u);
+    if (t != ri && !ng_bit(rm, t)) {
+        const double a = Op::mag(c);
+        if (ng_better(a, t, u0, j0)) { u0 = a; j0 = t; }
+    }
+}
+
+// One lane's share of <a, b> over a CTA's chunks of NG_THREADS entries
+// (first entry t0, chunks cstride apart), summed in entry order; the loads of
+// a full chunk are issued before its products.
+template <class Op, class E>
+__device__ __forceinline__ void ng_dot_part(const E *__restrict__ a, const E *__restrict__ b, int n, int t0,
+                                            int cstride, typename Op::Acc &d) {
+    constexpr int K = NG_THREADS / 32;
+    for (; t0 < n; t0 += cstride) {
+        if (t0 + 32 * (K - 1) < n) {
+            E xa[K], xb[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                xa[k] = a[t0 + 32 * k];
+                xb[k] = b[t0 + 32 * k];
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k) d += Op::dot(xa[k], xb[k]);
+        } else {
+            for (int t = t0; t < n; t += 32) d += Op::dot(a[t], b[t]);
+        }
+    }
+}
+
 template <class E>
-__global__ void __launch_bounds__(NG_THREADS)
+__global__ void __launch_bounds__(NG_THREADS, 2)
     nca_group_kernel(const NcaProb *__restrict__ probs, const int64_t *__restrict__ moff, int nprob, int G,
                      const int32_t *__restrict__ idx, KParams kp, double tol, E *__restrict__ scr,
                      uint32_t *__restrict__ masks, int32_t *__restrict__ rank_out, int32_t *__restrict__ prow,
@@ -266,15 +331,31 @@ __global__ void __launch_bounds__(NG_THREADS)
                 __syncthreads();
                 for (int l = l0 + tid; l < l1; l += NG_THREADS) ng_coef[l - l0] = U[(size_t)l * n1 + ri];
                 __syncthreads();
-                for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += cstride) {
-                    E v = l0 == 0 ? Op::from(kentry(kp, I[ri], J[s2])) : Vr[s2];
-                    for (int l = l0; l < l1; ++l) v = Op::submul(v, ng_coef[l - l0], V[(size_t)l * n2 + s2]);
-                    Vr[s2] = v;
+                // two columns per thread and NG_UNROLL kept terms loaded ahead of
+                // their subtractions: the loads of a term do not wait on the
+                // previous subtraction (same operations, same order per entry)
+                for (int s2 = gi * NG_THREADS + tid; s2 < n2; s2 += 2 * cstride) {
+                    const int s2b = s2 + cstride;
+                    const bool hb = s2b < n2;
+                    E va = l0 == 0 ? Op::from(kentry(kp, I[ri], J[s2])) : Vr[s2];
+                    E vb = Op::from(0.0);
+                    if (hb) vb = l0 == 0 ? Op::from(kentry(kp, I[ri], J[s2b])) : Vr[s2b];
+                    const E *Vc = V + s2;
+                    ng_sub_terms<Op, E>(va, vb, hb, Vc, (size_t)n2, cstride, ng_coef, l0, l1);
+                    Vr[s2] = va;
+                    if (hb) Vr[s2b] = vb;
                     if (last) {
-                        vs += Op::sq(v);
+                        vs += Op::sq(va);
                         if (!ng_bit(cm, s2)) {
-                            const double a = Op::mag(v);
+                            const double a = Op::mag(va);
                             if (ng_better(a, s2, v0, i0)) { v0 = a; i0 = s2; }
+                        }
+                        if (hb) {
+                            vs += Op::sq(vb);
+                            if (!ng_bit(cm, s2b)) {
+                                const double a = Op::mag(vb);
+                                if (ng_better(a, s2b, v0, i0)) { v0 = a; i0 = s2b; }
+                            }
                         }
                     }
                 }
@@ -302,20 +383,21 @@ __global__ void __launch_bounds__(NG_THREADS)
                 __syncthreads();
                 for (int l = l0 + tid; l < l1; l += NG_THREADS) ng_coef[l - l0] = V[(size_t)l * n2 + ci];
                 __syncthreads();
-                for (int t = gi * NG_THREADS + tid; t < n1; t += cstride) {
-                    E c = l0 == 0 ? Op::from(kentry(kp, I[t], J[ci])) : Ur[t];
-                    for (int l = l0; l < l1; ++l) c = Op::submul(c, ng_coef[l - l0], U[(size_t)l * n1 + t]);
+                for (int t = gi * NG_THREADS + tid; t < n1; t += 2 * cstride) {
+                    const int tb = t + cstride;
+                    const bool hb = tb < n1;
+                    E ca = l0 == 0 ? Op::from(kentry(kp, I[t], J[ci])) : Ur[t];
+                    E cb = Op::from(0.0);
+                    if (hb) cb = l0 == 0 ? Op::from(kentry(kp, I[tb], J[ci])) : Ur[tb];
+                    const E *Uc = U + t;
+                    ng_sub_terms<Op, E>(ca, cb, hb, Uc, (size_t)n1, cstride, ng_coef, l0, l1);
                     if (!last) {
-                        Ur[t] = c;
+                        Ur[t] = ca;
+                        if (hb) Ur[tb] = cb;
                         continue;
                     }
-                    const E u = Op::div(c, piv);
-                    Ur[t] = u;
-                    us += Op::sq(u);
-                    if (t != ri && !ng_bit(rm, t)) {
-                        const double a = Op::mag(c);
-                        if (ng_better(a, t, u0, j0)) { u0 = a; j0 = t; }
-                    }
+                    ng_col_final<Op, E>(ca, t, piv, ri, rm, Ur, us, u0, j0);
+                    if (hb) ng_col_final<Op, E>(cb, tb, piv, ri, rm, Ur, us, u0, j0);
                 }
             }
             ng_cta_part(u0, j0, (double)us, pcol_part + blockIdx.x, shv, shi, shs);
@@ -338,10 +420,8 @@ __global__ void __launch_bounds__(NG_THREADS)
             for (int l = warp; l < rank; l += NG_THREADS / 32) {
                 const E *Ul = U + (size_t)l * n1, *Vl = V + (size_t)l * n2;
                 Acc du = 0, dv = 0;
-                for (int t0 = gi * NG_THREADS; t0 < n1; t0 += cstride)
-                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n1; t += 32) du += Op::dot(Ul[t], Ur[t]);
-                for (int t0 = gi * NG_THREADS; t0 < n2; t0 += cstride)
-                    for (int t = t0 + lane; t < t0 + NG_THREADS && t < n2; t += 32) dv += Op::dot(Vl[t], Vr[t]);
+                ng_dot_part<Op, E>(Ul, Ur, n1, gi * NG_THREADS + lane, cstride, du);
+                ng_dot_part<Op, E>(Vl, Vr, n2, gi * NG_THREADS + lane, cstride, dv);
                 for (int o = 16; o > 0; o >>= 1) {
                     du += __shfl_xor_sync(0xffffffffu, du, o);
                     dv += __shfl_xor_sync(0xffffffffu, dv, o);
