@@ -142,6 +142,7 @@ struct h2w_handle {
     DBuf<unsigned long long> d_fly_ctr;
     DBuf<float> d_pts4;
     DBuf<float> d_ptsdf, d_logtab;  // (hi, lo) points and the log table of the double-FP32 form
+    DBuf<float> d_nca_logtab;       // the log table of the double-FP32 pivot search
     int fly_split = 0;
     int64_t fly_entries = 0;  // kernel entries one product evaluates
     std::vector<std::pair<int64_t, int64_t>> fly_rows;  // workspace rows the kernel writes
@@ -417,6 +418,11 @@ void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, cons
             // kernels built on log: residuals in double-FP32 arithmetic on the FP32 pipes
             const bool df = h->nca_df && ((h->cfg.dim < 3 && h->cfg.choice == 0) || (h->cfg.dim == 3 && h->cfg.choice == 1));
             const int grid = nca_group_grid(dcap, df);
+            if (df && !h->d_nca_logtab.p) {  // the pair logarithm's table
+                std::vector<float> lt(128 * 8);
+                fly_df_logtab(lt.data());
+                h->d_nca_logtab.upload(lt, st);
+            }
             if (grid <= 0) throw ApiError(H2W_ERR_CUDA, "NCA group kernel: no co-resident grid");
             const int nb = (int)probs.size();
             // groups sized to the widest block (about four residual entries per
@@ -451,7 +457,8 @@ void run_nca_big(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, cons
             CK(cudaMemsetAsync(derr.p, 0, 4, st));
             CK(cudaMemsetAsync(dbar.p, 0, (size_t)2 * G * sizeof(unsigned), st));
             CK(launch_nca_group(dp.p, dm.p, nb, G, grid, di.p, kp, tol, dscr.p, dmask.p, drank.p, dpr.p, dpc.p, dst.p,
-                                dbar.p, derr.p, dpartr.p, dpartc.p, ddots.p, dcap, df, st));
+                                dbar.p, derr.p, dpartr.p, dpartc.p, ddots.p, dcap, df, df ? h->d_nca_logtab.p : nullptr,
+                                st));
             std::vector<int32_t> rk((size_t)nb), hpr((size_t)piv), hpc((size_t)piv);
             int32_t status = 0, errf = 0;
             CK(cudaMemcpyAsync(rk.data(), drank.p, rk.size() * 4, cudaMemcpyDeviceToHost, st));

@@ -48,7 +48,7 @@ cudaError_t launch_nca_group(const NcaProb *probs, const int64_t *moff, int npro
                              const int32_t *idx, const KParams &kp, double tol, double *scr, uint32_t *masks,
                              int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status, unsigned *bars,
                              int32_t *err, void *prow_part, void *pcol_part, double *dots, int dcap, bool df,
-                             cudaStream_t st);
+                             const void *logtab, cudaStream_t st);
 cudaError_t launch_factor(const FactorJob *jobs, int njobs, const int32_t *idx, const KParams &kp, double *F,
                           cudaStream_t st);
 cudaError_t launch_xfer(const XferJob *jobs, int njobs, int max_n, const int32_t *idx, const KParams &kp,

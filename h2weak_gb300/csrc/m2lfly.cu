@@ -21,6 +21,7 @@
 // them in FP32 from FP32 coordinates.
 #include <cmath>
 
+#include "dfmath.cuh"
 #include "entry.cuh"
 
 namespace h2w {
@@ -238,76 +239,13 @@ __global__ void __launch_bounds__(FLY_THREADS)
 // ---- double-FP32 form (FP64-accurate far M2L on the FP32 pipes) ---------
 //
 // GB300 runs FP64 at 1/64 of its FP32 rate, and the FP64 entries spend it on
-// the logarithm. Here every value is an unevaluated pair of floats (hi + lo,
-// about 2^-48 relative) and every operation an error-free transformation:
-// TwoSum (Knuth), TwoProduct with the FMA (Ogita, Rump and Oishi 2005), the
-// pair arithmetic of Dekker (1971). The points are split once into (hi, lo)
-// pairs; R^2 is formed from pair differences; log(R^2) follows Tang's
-// table-driven method (ACM TOMS 16(4), 1990): R^2 = 2^e m, m in [1, 2),
-// c_k the centre of the 1/128-wide bin of m (exact in FP32), log m =
-// log c_k + log(1 + u) with u = (m - c_k) / c_k, |u| <= 2^-8, log c_k and
-// 1 / c_k from a table of pairs computed on the host in FP64, and
-// log(1 + u) = u - u^2/2 + u^3 (1/3 - u/4 + u^2/5) (the u^6 term is below
-// 2^-50); e log 2 with log 2 split so that e * hi is exact. Each row's sum
-// is a pair; the kernel's constant multiplies it once. For the kernels built
-// on log(R^2) (3D RBF, 2D integral equation) with every far pair farther
-// apart than a; the others keep the FP64 form.
-struct Df { float h, l; };
-__device__ __forceinline__ Df df_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
-    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
-}
-__device__ __forceinline__ Df df_fast(float a, float b) {  // |a| >= |b|
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ Df df_add(Df a, Df b) {
-    const Df s = df_two_sum(a.h, b.h);
-    return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
-}
-__device__ __forceinline__ Df df_sub(Df a, Df b) { return df_add(a, Df{-b.h, -b.l}); }
-// (a.h + a.l)^2, not renormalised: hi and a correction below 2^-22 |hi|
-__device__ __forceinline__ Df df_sqr(Df a) {
-    const float p = __fmul_rn(a.h, a.h);
-    return {p, __fmaf_rn(__fadd_rn(a.h, a.h), a.l, __fmaf_rn(a.h, a.h, -p))};
-}
-__device__ __forceinline__ Df df_mul(Df a, Df b) {
-    const float p = __fmul_rn(a.h, b.h);
-    float e = __fmaf_rn(a.h, b.h, -p);
-    e = __fmaf_rn(a.h, b.l, e);
-    e = __fmaf_rn(a.l, b.h, e);
-    return df_fast(p, e);
-}
-
-struct DfLogTab { float c, lh, ll, ih, il, pad0, pad1, pad2; };  // bin centre, log c (pair), 1/c (pair)
-
-// log(R^2) as a pair, R^2 = r.h + r.l > 0 and normal
-__device__ __forceinline__ Df df_log(Df r, const DfLogTab *tab) {
-    const int bits = __float_as_int(r.h);
-    const int e = (bits >> 23) - 127;
-    const int k = (bits >> 16) & 0x7f;
-    const float m = __int_as_float((bits & 0x7fffff) | 0x3f800000);
-    const DfLogTab t = tab[k];
-    const float d = __fsub_rn(m, t.c);                                   // exact (Sterbenz)
-    const float lm = __fmul_rn(r.l, __int_as_float((127 - e) << 23));   // r.l / 2^e, exact
-    const Df dd = df_two_sum(d, lm);
-    // u = dd / c as a pair
-    const float uh = __fmul_rn(dd.h, t.ih);
-    float ue = __fmaf_rn(dd.h, t.ih, -uh);
-    ue = __fmaf_rn(dd.h, t.il, ue);
-    ue = __fmaf_rn(dd.l, t.ih, ue);
-    const Df u = df_fast(uh, ue);
-    // log(1 + u) = u - u^2/2 + u^3 (1/3 - u/4 + u^2/5)
-    const Df u2 = df_sqr(u);
-    const float poly = __fmaf_rn(u.h, __fmaf_rn(u.h, 0.2f, -0.25f), 0.33333334f);
-    const float tail = __fmul_rn(__fmul_rn(u2.h, u.h), poly);
-    Df l1 = df_add(u, Df{-0.5f * u2.h, __fmaf_rn(-0.5f, u2.l, tail)});
-    // + e log 2 (hi exact for |e| < 128) + log c
-    const float ln2h = 0.693145751953125f, ln2l = 1.42860676533018704e-6f;
-    const Df el = df_fast(__fmul_rn((float)e, ln2h), __fmul_rn((float)e, ln2l));
-    const Df lc = Df{t.lh, t.ll};
-    return df_add(df_add(el, lc), l1);
-}
+// the logarithm. Here every value is an unevaluated pair of floats and every
+// operation an error-free transformation (dfmath.cuh); the points are split
+// once into (hi, lo) pairs, R^2 is formed from pair differences and log(R^2)
+// by the table-driven pair logarithm. Each row's sum is a pair; the kernel's
+// constant multiplies it once. For the kernels built on log(R^2) (3D RBF, 2D
+// integral equation) with every far pair farther apart than a; the others
+// keep the FP64 form.
 
 // the FP64-accurate far M2L: rows' sums as pairs times `scale`, into an FP64 workspace
 template <int DIM>

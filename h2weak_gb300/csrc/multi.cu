@@ -17,6 +17,7 @@
 #include <cfloat>
 #include <type_traits>
 
+#include "dfmath.cuh"
 #include "kernels.cuh"
 #include "sync.cuh"
 
@@ -85,26 +86,6 @@ __device__ __forceinline__ void mr_get4(float *o, const float *p) {
 // two cross terms, and a sum as an unevaluated pair (sh, sl) advanced by
 // Knuth's TwoSum, so every rounding of the FP32 sum is kept in sl. All
 // operations are explicitly rounded (no contraction may merge them).
-__device__ __forceinline__ float2 df_split(double a) {
-    const float h = __double2float_rn(a);
-    return make_float2(h, __double2float_rn(__dsub_rn(a, (double)h)));
-}
-// The same pair without FP64 instructions (GB300 runs those at 1/64 rate):
-// hi = the double's top 24 significand bits as a float (truncated), lo = the
-// remaining 29 bits, converted to float (rounded to 24 bits) and scaled by the
-// exact power of two 2^(E-52); hi + lo carries 47 bits. Used when both parts
-// are normal floats (exponent E in [-74, 127]); otherwise (zero, tiny or huge
-// values) the FP64 split.
-__device__ __forceinline__ float2 df_split_fast(double a) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(a);
-    const int e = (int)((u >> 52) & 0x7ff);
-    if (e < 1023 - 74 || e > 1023 + 127) return df_split(a);
-    const unsigned sign = (unsigned)(u >> 63) << 31;
-    const float hi = __uint_as_float(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((u >> 29) & 0x7fffffu));
-    const float scale = __uint_as_float((unsigned)(e - 1023 - 52 + 127) << 23);
-    const float lo = __fmul_rn(__uint2float_rn((unsigned)(u & 0x1fffffffu)), scale);
-    return make_float2(hi, sign ? -lo : lo);
-}
 __device__ __forceinline__ void df_fma(float &sh, float &sl, const float2 a, const float2 x) {
     const float p = __fmul_rn(a.x, x.x);
     float e = __fmaf_rn(a.x, x.x, -p);
