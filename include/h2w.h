@@ -261,12 +261,16 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 accuracy, for the kernels built on log(R^2); the stored
  *                 passes in FP64), and h2w_gmres_ir forms its accurate
  *                 residuals that way when H2W_OPT_IR_RESIDUAL is DF64.
- *  H2W_OPT_NCA_DF  1 (default): the pivot search of large blocks (groups of
- *                 CTAs) for the kernels built on log (1D and 2D integral
- *                 equation, 3D RBF), whose entries already differ from the
- *                 reference's in the last bit, forms its residuals in
- *                 double-FP32 arithmetic (about 2^-48 relative) on the FP32
- *                 pipes instead of FP64; 0: FP64. The other kernels always
+ *  H2W_OPT_NCA_DF  1 (default): the pivot search on groups of CTAs for the
+ *                 kernels built on log (1D and 2D integral equation, 3D
+ *                 RBF), whose entries already differ from the reference's
+ *                 in the last bit, runs in double-FP32 arithmetic (about
+ *                 2^-48 relative) on the FP32 pipes instead of FP64: the
+ *                 residuals, the entries (FP64 coordinate differences, then
+ *                 R^2 and the logarithm as pairs), and the stopping test's
+ *                 dots, which are summed inside the next pivot's residual
+ *                 passes; every block of 2048 or more rows + columns is
+ *                 searched on groups then. 0: FP64. The other kernels always
  *                 search in FP64 (their pivots are bitwise the reference's). */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
        H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8,
