@@ -1,17 +1,27 @@
 """Benchmark: GMRES time-to-1e-10 and matvec HBM GB/s of the GB300 H2*
-operator, mixed precision and batched right-hand sides against the plain
-FP64 GPU form, with the CPU oracle timed beside it.
+operator, mixed precision against the plain FP64 GPU form.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME] [--rhs R]
 
-A step solves A X = B for R = 64 right-hand sides together (one multi-vector
-product per Arnoldi step) to relative residual 1e-10 per column from X0 = 1,
-with the compressed operator resident in HBM: FP32-operator inner GMRES and
-iterative refinement. value = solved right-hand sides per second over all
-ranks. Beside it: the same columns by batched FP64 GMRES, and one right-hand
-side b = A_dense x_true (manufactured solution) by the single-vector mixed and
-plain FP64 solvers. Multi-GPU runs are independent replicas (one problem per
-GPU, no collective on the data path).
+Default workload (3d_rbf_1048576): 3D H2* RBF on 2^20 uniform random points,
+nmax 128, NCA tol 1e-10, the far-field M2L evaluated during each product. A
+step is one solve of A x = b (b = A x_true, x0 = 1) to relative residual
+1e-10 with the compressed operator resident in HBM: FP32-operator inner GMRES
+and iterative refinement with FP64-accurate residuals. value = solves per
+second over all ranks. Beside it: the plain FP64 GMRES solve of the same
+system, assembly time, storage, the operator's error on exact dense rows.
+The CPU reference arm cannot assemble this operator in bounded time and says
+so.
+
+Other workloads: 2d_ie_65536 (2D H2* integral equation, 256^2 grid): a step
+solves A X = B for R = 64 right-hand sides together (one multi-vector product
+per Arnoldi step), beside it batched FP64 GMRES and one right-hand side by
+the single-vector mixed and plain FP64 solvers, and the CPU oracle timed on
+the same workload (--impl reference). 1d_rbf_32768 likewise; 3d_rbf_131072 is
+the default family at 2^17 points (for profiler captures).
+
+Multi-GPU runs are independent replicas (one problem per GPU, no collective
+on the data path).
 """
 import argparse
 import json
@@ -42,6 +52,11 @@ WORKLOADS = {
                            desc="3D H2* RBF (choice 1), N=1048576 uniform random points in [-1,1)^3 "
                                 "(splitmix64 stream), nmax=128 (5 levels), NCA tol 1e-10, GMRES to 1e-10, "
                                 "one right-hand side per solve; far-field M2L evaluated during each product"),
+    # the same family at 2^17 points (4 levels): a case small enough for ncu captures of the far-field kernel
+    "3d_rbf_131072": dict(dim=3, form=0, choice=1, tol=10, npts=131072, nmax=128, gtol=10, single=True,
+                          desc="3D H2* RBF (choice 1), N=131072 uniform random points in [-1,1)^3 "
+                               "(splitmix64 stream), nmax=128 (4 levels), NCA tol 1e-10, GMRES to 1e-10, "
+                               "one right-hand side per solve; far-field M2L evaluated during each product"),
     "1d_rbf_32768": dict(dim=1, form=0, choice=1, tol=10, grid=32768, leaf=64, gtol=10,
                          desc="1D H2* RBF (choice 1), N=32768 grid on [-1,1], nmax=64, NCA tol 1e-10, GMRES to 1e-10"),
 }
@@ -222,13 +237,31 @@ def cpu_oracle_solves(wl, R, steps, warmup, budget_s=150.0):
 def run_single_random(args, wl, rank, world, local):
     """The 2^20-point 3D workload: one right-hand side per solve, b = A x_true with
     the FP64 compressed operator, x0 = 1. value = mixed-precision solves per
-    second (FP32 inner GMRES, FP64 refinement); beside it the plain FP64 GMRES,
-    the operator's error on exact dense rows, assembly time and storage."""
+    second over all ranks (FP32 inner GMRES, FP64-accurate refinement); beside
+    it the plain FP64 GMRES, the operator's error on exact dense rows, assembly
+    time and storage. Multi-GPU runs are independent replicas (one problem per
+    GPU, no collective on the data path)."""
     import math
     import torch
+    import torch.distributed as dist
     import h2weak_gb300 as hw
     from h2weak_gb300 import synth
     torch.cuda.set_device(local)
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", rank=rank, world_size=world, device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     hw.build()
     N, dim = wl["npts"], wl["dim"]
     nlev = int(math.ceil(math.log(N / float(wl["nmax"])) / math.log(2.0 ** dim)))
@@ -257,6 +290,8 @@ def run_single_random(args, wl, rank, world, local):
 
     def ev_time(fn, k):
         torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = hw.launch_count()
         t0w = time.time()
@@ -266,9 +301,11 @@ def run_single_random(args, wl, rank, world, local):
             out = fn()
         e1.record()
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1), out, hw.launch_count() - l0, (t0w, time.time())
+        barrier()
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1)), out, hw.launch_count() - l0, (t0w, time.time())
 
-    # products on this stream: FP32 and FP64, each with its far M2L kernel
+    # products on this stream: FP32, double-FP32 and FP64, each with its far M2L kernel
     mv = {}
     y = torch.empty_like(xt)
     for prec, nm, reps in ((hw.PREC_FP32, "fp32", 5), (hw.PREC_DF64, "df64", 3), (hw.PREC_FP64, "fp64", 1)):
@@ -289,6 +326,15 @@ def run_single_random(args, wl, rank, world, local):
     clocks.stop()
     outer, inner, res_m = out_m
     err_m = float(torch.linalg.norm(x - xt) / torch.linalg.norm(xt))
+    # the far-field M2L kernel alone (CUDA events on this stream around each of its
+    # launches), inside FP32 and double-FP32 products
+    op.profile(True)
+    for _ in range(5):
+        op.matvec_device(xt.data_ptr(), y.data_ptr(), precision=hw.PREC_FP32, stream=st)
+    op.matvec_device(xt.data_ptr(), y.data_ptr(), precision=hw.PREC_DF64, stream=st)
+    fly32 = op.profile_fly(hw.PREC_FP32)
+    flydf = op.profile_fly(hw.PREC_DF64)
+    op.profile(False)
     # end to end: host b in, host x out through the C ABI
     b_h = b.cpu().pin_memory()
     x_h = torch.ones_like(b_h).pin_memory()
@@ -310,36 +356,67 @@ def run_single_random(args, wl, rank, world, local):
     dense_err = op.total_error(xt.cpu().numpy(), 1024)
     peak, peak_kind = load_peaks()
     stored = op.operator_bytes(hw.PREC_FP32)
+    E = op.storage_entries()
+    # Roofline of the dominant kernel, the FP32 far-field M2L of the inner products:
+    # algorithmic bytes = its kernel entries as the stored FP32 operator would hold
+    # them (4 B each; the reference stores these blocks, w_op * E with E its storage
+    # count), over its mean CUDA-event launch time. It reads almost none of them from
+    # DRAM (it forms them from the points), so the figure is the rate at which the
+    # kernel delivers operator entries, in bytes of HBM that reading them would take.
+    fl_n, fl_ms, fl_e = fly32
+    fl_t = fl_ms / max(fl_n, 1)
+    fl_gbs = 4.0 * fl_e / (fl_t * 1e-3) / 1e9 if fl_n else None
+    prod_bytes = 4.0 * E + 2 * 8.0 * N
     line = {
         "metric": METRIC, "value": K * world / (ms_m / 1e3), "unit": "solves/s", "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_m / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*", "rhs_per_step": 1,
+                   "rhs": "x_true N(0,1) from a seeded splitmix64 stream, b = A x_true with the FP64 compressed "
+                          "operator, x0 = 1",
                    "tolerance": "relative residual 1e-%d" % gtol, "parallelism": "replicas (one problem per GPU)",
                    "l2": "no flush: the stored operator exceeds the 129 MB L2 (inputs larger than L2)"},
         "solver": "mixed: FP32-operator inner GMRES + iterative refinement with FP64-accurate residuals (stored "
                   "passes FP64, far-field M2L in double-FP32 arithmetic), CUDA-graph Arnoldi loop; far-field M2L "
                   "evaluated from the points in every product; the plain form is FP64 throughout",
-        "e2e": {"value": 1.0 / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N,
+        "e2e": {"value": world / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N,
                 "d2h_bytes_per_step": 8 * N},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None, "traffic": None,
-                     "note": "the product is bound by the far M2L kernel's entry evaluation (FP32 pipes; FP64 "
-                             "pipe in the FP64 residuals), not HBM: stored operator %.1f GB FP32" % (stored / 1e9)},
+        "roofline": {"bound": "hbm", "kernel": "m2l_fly32_sep_kernel (FP32 far-field M2L, entries from the points)",
+                     "achieved": fl_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": fl_gbs / peak if fl_gbs else None, "traffic": None,
+                     "launch_ms": fl_t, "entries_per_launch": fl_e,
+                     "bytes_per_launch": 4.0 * fl_e,
+                     "note": "achieved = 4 B x the kernel entries one launch evaluates (the far-field M2L blocks "
+                             "the reference stores, at the FP32 operator's width) / mean CUDA-event launch time, "
+                             "against the measured HBM copy bandwidth (%s); the kernel forms these entries from "
+                             "the points and reads almost nothing from DRAM (ncu DRAM bytes per entry in "
+                             "profiles/m2l_fly32_sep_3d_rbf_131072.md), so traffic is null and the figure is the "
+                             "rate at which it delivers operator entries" % peak_kind,
+                     "product": {"what": "whole FP32 product (stored passes + far M2L kernel)",
+                                 "algorithmic_bytes": prod_bytes, "ms": mv["fp32"],
+                                 "achieved_gbs": prod_bytes / (mv["fp32"] * 1e-3) / 1e9,
+                                 "frac": prod_bytes / (mv["fp32"] * 1e-3) / 1e9 / peak,
+                                 "stored_fp32_bytes": stored}},
+        "compute": {"fly32_entries_per_s": fl_e / (fl_t * 1e-3) if fl_n else None,
+                    "flydf_ms": flydf[1] / max(flydf[0], 1), "flydf_entries_per_s":
+                        flydf[2] / (flydf[1] / max(flydf[0], 1) * 1e-3) if flydf[0] else None},
         "cpu_baseline": {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": "none: the CPU oracle's assembly of this operator takes hours on the host "
-                                   "cores (42 s at 2^15 points, growing faster than N^1.5)"},
+                                   "cores (42 s at 2^15 points on 8 cores, growing faster than N^1.5)"},
         "clocks": clocks.summary(*win),
         "mixed": {"ms_per_solve": ms_m / K, "outer": outer, "inner_total": inner, "resid": res_m,
                   "rel_err_vs_xtrue": err_m},
         "single_fp64": {"ms_per_solve": ms_64, "iters": it64, "resid": res64, "rel_err_vs_xtrue": err_64},
         "speedup_vs_plain_fp64": {"single_mixed_over_single_fp64": ms_64 / (ms_m / K)},
         "matvec_ms": mv, "operator_error_1024_dense_rows": dense_err,
-        "assembly_s": t_asm, "storage_entries": op.storage_entries(),
+        "assembly_s": t_asm, "storage_entries": E,
         "stored_bytes": {"fp64": op.operator_bytes(hw.PREC_FP64), "fp32": stored},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
 
 
 def run_reference(args, wl):
@@ -370,7 +447,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="2d_ie_65536", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="3d_rbf_1048576", choices=sorted(WORKLOADS))
     ap.add_argument("--rhs", type=int, default=64, help="right-hand sides solved together per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -101,6 +101,7 @@ def lib():
         "h2w_get_config": [P, ctypes.POINTER(_Config)],
         "h2w_profile": [P, I],
         "h2w_profile_multi": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(D)],
+        "h2w_profile_fly": [P, I, ctypes.POINTER(I64), ctypes.POINTER(D), ctypes.POINTER(I64)],
         "h2w_plan_stats": [P, P, I],
         "h2w_set_option": [P, I, I64],
         "h2w_learn_record": [P, I],
@@ -310,6 +311,13 @@ class H2Operator:
         la, ms, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
         self._ck(lib().h2w_profile_multi(self.h, precision, ctypes.byref(la), ctypes.byref(ms), ctypes.byref(by)))
         return la.value, ms.value, by.value
+
+    def profile_fly(self, precision=PREC_FP32):
+        """(launches, total ms, kernel entries per launch) of the far-field M2L
+        kernel of products with the far field on the fly."""
+        la, ms, en = ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
+        self._ck(lib().h2w_profile_fly(self.h, precision, ctypes.byref(la), ctypes.byref(ms), ctypes.byref(en)))
+        return la.value, ms.value, en.value
 
     def plan_stats(self):
         """Multi-vector plan: targets, panels, operator entries per column, entries

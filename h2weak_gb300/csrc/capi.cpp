@@ -2262,7 +2262,9 @@ cudaEvent_t prof_event(h2w_handle *h) {
     return e;
 }
 
-// phase == number of phases: the whole matvec (cooperative launch)
+// phase == number of phases: the whole matvec (cooperative launch);
+// FLY_PHASE: the far-field M2L kernel of a product with the far field on the fly
+constexpr int FLY_PHASE = 1 << 20;
 template <class F>
 void prof_launch(h2w_handle *h, int prec, int phase, cudaStream_t st, F &&launch) {
     const bool whole = phase >= (int)h->phases.size();
@@ -2307,7 +2309,7 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
             }
         };
         stored(0, h->fly_split);
-        prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
+        prof_launch(h, df ? H2W_PREC_DF64 : H2W_PREC_FP64, FLY_PHASE, st, [&] {
             if (df)
                 return launch_fly_df64(h->d_fly_items.p, (int64_t)h->d_fly_items.n, h->d_fly_ctr.p, h->d_fly_rowpid.p,
                                        h->d_fly_cpid.p, h->d_fly_cws.p, h->d_ptsdf.p, h->d_logtab.p, h->d_ws.p,
@@ -2389,7 +2391,7 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
             }
         };
         stored(0, h->fly_split);
-        prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
+        prof_launch(h, H2W_PREC_FP32, FLY_PHASE, st, [&] {
             return launch_fly_f32(h->d_fly_items.p, (int64_t)h->d_fly_items.n, h->d_fly_ctr.p, h->d_fly_rowpid.p,
                                   h->d_fly_cpid.p, h->d_fly_cws.p, h->d_pts4.p, h->d_ws32.p, h->kparams(), h->k32, st);
         });
@@ -4603,7 +4605,7 @@ int h2w_profile_multi(h2w_handle *h, int precision, int64_t *launches, double *m
         *ms = 0.0;
         double by = 0.0;
         for (auto &r : h->prof_recs) {
-            if (r.prec != precision + 2) continue;
+            if (r.prec != precision + 2 || r.phase == FLY_PHASE) continue;
             float t = 0.f;
             CK(cudaEventElapsedTime(&t, r.a, r.b));
             *launches += 1;
@@ -4612,6 +4614,25 @@ int h2w_profile_multi(h2w_handle *h, int precision, int64_t *launches, double *m
             by += (double)h->op_bytes_read * w + (double)h->tree.N * r.rp * (w + 8.0);
         }
         *bytes = *launches ? by / (double)*launches : 0.0;
+        return H2W_OK;
+    });
+}
+
+int h2w_profile_fly(h2w_handle *h, int precision, int64_t *launches, double *ms, int64_t *entries) {
+    return guarded(h, [&] {
+        require_op(h);
+        if (!launches || !ms || !entries) throw ApiError(H2W_ERR_ARG, "null output");
+        CK(cudaDeviceSynchronize());
+        *launches = 0;
+        *ms = 0.0;
+        *entries = h->fly_active ? h->fly_entries : 0;
+        for (auto &r : h->prof_recs) {
+            if (r.phase != FLY_PHASE || r.prec != precision) continue;
+            float t = 0.f;
+            CK(cudaEventElapsedTime(&t, r.a, r.b));
+            *launches += 1;
+            *ms += (double)t;
+        }
         return H2W_OK;
     });
 }

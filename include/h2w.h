@@ -371,6 +371,14 @@ int h2w_profile_phases(h2w_handle *h, int precision, int max_phases, int64_t *la
  * operator once, the input block in the kernel's precision, the FP64 result
  * block). */
 int h2w_profile_multi(h2w_handle *h, int precision, int64_t *launches, double *ms, double *bytes);
+/* Launch statistics of the far-field M2L kernel of single-vector products
+ * with H2W_OPT_FAR_ON_THE_FLY (precision H2W_PREC_FP32, H2W_PREC_FP64 or
+ * H2W_PREC_DF64) while profiling is enabled: launches, total device ms, and
+ * the kernel entries one launch evaluates (the far M2L blocks the reference
+ * stores, evaluateFarField / assemble_M2L_far in 3D/codes/HODLR3Dtree.hpp,
+ * formed from the points instead of read). entries is 0 when the operator
+ * stores its far field. (No counterpart in the reference.) */
+int h2w_profile_fly(h2w_handle *h, int precision, int64_t *launches, double *ms, int64_t *entries);
 /* Shape of the multi-vector product's plan (host-side figures, no device
  * work): stats[0] targets, [1] operator panels, [2] operator entries read per
  * column, [3] entries the kernel multiplies per column (rows rounded to the
