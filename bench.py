@@ -357,16 +357,16 @@ def run_single_random(args, wl, rank, world, local):
     peak, peak_kind = load_peaks()
     stored = op.operator_bytes(hw.PREC_FP32)
     E = op.storage_entries()
-    # Roofline of the dominant kernel, the FP32 far-field M2L of the inner products:
-    # algorithmic bytes = its kernel entries as the stored FP32 operator would hold
-    # them (4 B each; the reference stores these blocks, w_op * E with E its storage
-    # count), over its mean CUDA-event launch time. It reads almost none of them from
-    # DRAM (it forms them from the points), so the figure is the rate at which the
-    # kernel delivers operator entries, in bytes of HBM that reading them would take.
+    # Roofline. The unit is one FP32 product (the inner GMRES's matvec, 50 of them in a
+    # solve): algorithmic bytes = 4 B x E (E the reference's storage count, every block
+    # it stores, at the FP32 operator's width) + the FP64 input and output vectors, over
+    # the product's CUDA-event time. The product streams its stored 30.8 GB and forms
+    # the far-field M2L entries (84 % of E) from the points in m2l_fly32_sep_kernel,
+    # which is bound by instruction issue, not DRAM (its own figures beside it).
     fl_n, fl_ms, fl_e = fly32
     fl_t = fl_ms / max(fl_n, 1)
-    fl_gbs = 4.0 * fl_e / (fl_t * 1e-3) / 1e9 if fl_n else None
     prod_bytes = 4.0 * E + 2 * 8.0 * N
+    prod_gbs = prod_bytes / (mv["fp32"] * 1e-3) / 1e9
     line = {
         "metric": METRIC, "value": K * world / (ms_m / 1e3), "unit": "solves/s", "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_m / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -382,24 +382,19 @@ def run_single_random(args, wl, rank, world, local):
         "e2e": {"value": world / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N,
                 "d2h_bytes_per_step": 8 * N},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "m2l_fly32_sep_kernel (FP32 far-field M2L, entries from the points)",
-                     "achieved": fl_gbs, "peak": peak, "unit": "GB/s",
-                     "frac": fl_gbs / peak if fl_gbs else None, "traffic": None,
-                     "launch_ms": fl_t, "entries_per_launch": fl_e,
-                     "bytes_per_launch": 4.0 * fl_e,
-                     "note": "achieved = 4 B x the kernel entries one launch evaluates (the far-field M2L blocks "
-                             "the reference stores, at the FP32 operator's width) / mean CUDA-event launch time, "
-                             "against the measured HBM copy bandwidth (%s); the kernel forms these entries from "
-                             "the points and reads almost nothing from DRAM (ncu DRAM bytes per entry in "
-                             "profiles/m2l_fly32_sep_3d_rbf_131072.md), so traffic is null and the figure is the "
-                             "rate at which it delivers operator entries" % peak_kind,
-                     "product": {"what": "whole FP32 product (stored passes + far M2L kernel)",
-                                 "algorithmic_bytes": prod_bytes, "ms": mv["fp32"],
-                                 "achieved_gbs": prod_bytes / (mv["fp32"] * 1e-3) / 1e9,
-                                 "frac": prod_bytes / (mv["fp32"] * 1e-3) / 1e9 / peak,
-                                 "stored_fp32_bytes": stored}},
-        "compute": {"fly32_entries_per_s": fl_e / (fl_t * 1e-3) if fl_n else None,
-                    "flydf_ms": flydf[1] / max(flydf[0], 1), "flydf_entries_per_s":
+        "roofline": {"bound": "hbm", "unit_of_work": "one FP32 product (stored passes + far-field M2L kernel)",
+                     "achieved": prod_gbs, "peak": peak, "unit": "GB/s", "frac": prod_gbs / peak, "traffic": None,
+                     "algorithmic_bytes": prod_bytes, "ms": mv["fp32"], "stored_fp32_bytes": stored,
+                     "note": "achieved = (4 B x the reference's storage count E + 16 B x N) / the product's "
+                             "CUDA-event time, against the measured HBM copy bandwidth (%s). The product reads "
+                             "its stored %.1f GB and evaluates the far-field M2L entries (%.3g of E's %.3g) from "
+                             "the points; traffic is null (three launches; DRAM bytes per far-field entry "
+                             "0.066 in profiles/m2l_fly32_sep_3d_rbf_131072.md)" % (peak_kind, stored / 1e9, fl_e, E),
+                     "far_field_kernel": {"name": "m2l_fly32_sep_kernel", "bound": "instruction issue",
+                                          "launch_ms": fl_t, "entries_per_launch": fl_e,
+                                          "entries_per_s": fl_e / (fl_t * 1e-3) if fl_n else None,
+                                          "share_of_product": fl_t / mv["fp32"] if fl_n else None}},
+        "compute": {"flydf_ms": flydf[1] / max(flydf[0], 1), "flydf_entries_per_s":
                         flydf[2] / (flydf[1] / max(flydf[0], 1) * 1e-3) if flydf[0] else None},
         "cpu_baseline": {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": "none: the CPU oracle's assembly of this operator takes hours on the host "

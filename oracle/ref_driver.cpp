@@ -17,6 +17,9 @@
 //   findMemory_n/_sn      1D/codes/HODLR1Dtree.hpp:535-588, 2D/codes/HODLR2Dtree.hpp:1207-1305,
 //                         3D/codes/HODLR3Dtree.hpp:2505-2628
 //
+// Complex Helmholtz build (-DUSE_Helm, 3D, choice 2): every vector in and out
+// is N interleaved (re, im) pairs of doubles.
+//
 // Usage: refXd_F <n_param> <nLevels> <leaf_param> <L> <tol_pow> <choice>
 //                <in.bin> <out.bin> <gmres_maxiter> <gmres_tolpow>
 // n_param is N (1D), sqrt(N) (2D) or cbrt(N) (3D); leaf_param is nmax (1D)
@@ -90,6 +93,26 @@ static const int NCHILD = 8;
 static const int NNB = 26;
 #define NBOXES(K, j) ((K)->nBoxesPerLevel[j])
 #endif
+
+// Scalars on the wire: one double (real kernels) or an interleaved (re, im)
+// pair (the complex Helmholtz build, -DUSE_Helm: 3D/codes/headers.hpp:35-40).
+#ifdef USE_Helm
+static const int CW = 2;
+static dtype scal_in(const double *p) { return dtype(p[0], p[1]); }
+static void scal_out(std::vector<double> &o, const dtype &v) {
+    o.push_back(v.real());
+    o.push_back(v.imag());
+}
+#else
+static const int CW = 1;
+static dtype scal_in(const double *p) { return p[0]; }
+static void scal_out(std::vector<double> &o, const dtype &v) { o.push_back(v); }
+#endif
+static void put_vec(const char *n, const Vec &v) {
+    std::vector<double> o;
+    for (long i = 0; i < v.size(); ++i) scal_out(o, v(i));
+    put_f64(n, o);
+}
 
 static void pt_to_doubles(const PtT &p, double *o) {
 #if H2W_DIM == 1
@@ -189,10 +212,10 @@ int main(int argc, char **argv) {
     const int nL = K->nLevels;
 
     int64_t nvec = read_i64(fi);
-    std::vector<double> vecs = read_f64(fi, nvec * N);
+    std::vector<double> vecs = read_f64(fi, nvec * N * CW);
     int64_t do_gmres = read_i64(fi);
     std::vector<double> xtrue;
-    if (do_gmres) xtrue = read_f64(fi, N);
+    if (do_gmres) xtrue = read_f64(fi, (int64_t)N * CW);
     int64_t do_dense = read_i64(fi);
     fclose(fi);
 
@@ -282,23 +305,23 @@ int main(int argc, char **argv) {
     std::vector<double> ys;
     for (int64_t v = 0; v < nvec; ++v) {
         Vec x(N), y;
-        for (int i = 0; i < N; ++i) x(i) = vecs[(size_t)(v * N + i)];
+        for (int i = 0; i < N; ++i) x(i) = scal_in(&vecs[(size_t)((v * N + i) * CW)]);
         p->mat_vec_prod(x, y);
-        for (int i = 0; i < N; ++i) ys.push_back(y(i));
+        for (int i = 0; i < N; ++i) scal_out(ys, y(i));
     }
     auto t3 = std::chrono::steady_clock::now();
     put_f64("matvec", ys);
 
     if (do_dense && nvec > 0) {
         Vec x(N);
-        for (int i = 0; i < N; ++i) x(i) = vecs[(size_t)i];
+        for (int i = 0; i < N; ++i) x(i) = scal_in(&vecs[(size_t)i * CW]);
         Vec yd = K->getTruePoten(x);
-        put_f64p("dense_matvec", yd.data(), N);
+        put_vec("dense_matvec", yd);
     }
     double t_gmres = 0.0;
     if (do_gmres) {
         Vec b(N);
-        for (int i = 0; i < N; ++i) b(i) = xtrue[(size_t)i];
+        for (int i = 0; i < N; ++i) b(i) = scal_in(&xtrue[(size_t)i * CW]);
         Vec rhs = K->getTruePoten(b);
         Vec x = Vec::Ones(N);
         auto g0 = std::chrono::steady_clock::now();
@@ -306,8 +329,8 @@ int main(int argc, char **argv) {
         its->GMRES<initialisation>(p, x, rhs);
         auto g1 = std::chrono::steady_clock::now();
         t_gmres = std::chrono::duration<double>(g1 - g0).count();
-        put_f64p("gmres_rhs", rhs.data(), N);
-        put_f64p("gmres_x", x.data(), N);
+        put_vec("gmres_rhs", rhs);
+        put_vec("gmres_x", x);
         put_f64("gmres_stats", {(double)its->max_iter, its->resid, (x - b).norm() / b.norm()});
     }
     put_f64("timing", {std::chrono::duration<double>(t1 - t0).count(),

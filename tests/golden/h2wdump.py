@@ -33,6 +33,13 @@ def csr(d, name):
     return [val[ptr[i]:ptr[i + 1]] for i in range(len(ptr) - 1)]
 
 
+def _f64(v):
+    """Real vectors as doubles; complex ones as interleaved (re, im) doubles."""
+    if np.iscomplexobj(v):
+        return np.ascontiguousarray(v, dtype=np.complex128).view(np.float64)
+    return np.ascontiguousarray(v, dtype=np.float64)
+
+
 def write_input(path, points=None, vecs=(), xtrue=None, dense=False):
     with open(path, "wb") as f:
         if points is None:
@@ -41,7 +48,7 @@ def write_input(path, points=None, vecs=(), xtrue=None, dense=False):
             p = np.ascontiguousarray(points, dtype=np.float64)
             f.write(struct.pack("<q", p.shape[0]))
             f.write(p.tobytes())
-        vecs = [np.ascontiguousarray(v, dtype=np.float64) for v in vecs]
+        vecs = [_f64(v) for v in vecs]
         f.write(struct.pack("<q", len(vecs)))
         for v in vecs:
             f.write(v.tobytes())
@@ -49,5 +56,5 @@ def write_input(path, points=None, vecs=(), xtrue=None, dense=False):
             f.write(struct.pack("<q", 0))
         else:
             f.write(struct.pack("<q", 1))
-            f.write(np.ascontiguousarray(xtrue, dtype=np.float64).tobytes())
+            f.write(_f64(xtrue).tobytes())
         f.write(struct.pack("<q", 1 if dense else 0))
