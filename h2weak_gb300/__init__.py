@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libh2w.so")
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_RANK, ERR_NOT_CONVERGED, ERR_STATE = -1, -2, -3, -4, -5, -6
 FORM_NESTED, FORM_SEMINESTED, FORM_NONNESTED = 0, 1, 2
-KERNEL_IE, KERNEL_RBF = 0, 1
+KERNEL_IE, KERNEL_RBF, KERNEL_HELMHOLTZ = 0, 1, 2
 ASSEMBLE_NCA, ASSEMBLE_IMPORT, ASSEMBLE_LEARNED = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
 HOST, DEVICE = 0, 1
@@ -169,6 +169,8 @@ class H2Operator:
             raise H2WError(rc, "h2w_create failed (no CUDA device or bad configuration)")
         self.h = h
         self.dim, self.form, self.choice, self.tol_pow, self.nlevels = dim, form, choice, tol_pow, nlevels
+        # the Helmholtz kernel is complex: vectors are complex128 (interleaved (re, im) doubles in the C ABI)
+        self.complex = choice == KERNEL_HELMHOLTZ
 
     @classmethod
     def open(cls, path, device=0):
@@ -184,6 +186,7 @@ class H2Operator:
         self._ck(lib().h2w_get_config(self.h, ctypes.byref(cfg)))
         self.dim, self.form, self.choice, self.tol_pow, self.nlevels = (cfg.dim, cfg.form, cfg.choice, cfg.tol_pow,
                                                                         cfg.nlevels)
+        self.complex = cfg.choice == KERNEL_HELMHOLTZ
         return self
 
     def save(self, path):
@@ -341,6 +344,12 @@ class H2Operator:
 
     # products
     def matvec(self, x, precision=PREC_FP64):
+        if self.complex:
+            x = np.ascontiguousarray(x, dtype=np.complex128)
+            y = np.empty_like(x)
+            self._ck(lib().h2w_matvec(self.h, ctypes.c_void_p(x.ctypes.data), ctypes.c_void_p(y.ctypes.data), 1,
+                                      precision, HOST, None))
+            return y
         x = np.ascontiguousarray(x, dtype=np.float64)
         nrhs = 1 if x.ndim == 1 else x.shape[1]
         xc = np.asfortranarray(x.reshape(self.N, nrhs)) if x.ndim > 1 else x
@@ -354,9 +363,10 @@ class H2Operator:
                                   ctypes.c_void_p(stream) if stream else None))
 
     def dense_matvec(self, x, row0=0, nrows=None):
-        x = np.ascontiguousarray(x, dtype=np.float64)
+        dt = np.complex128 if self.complex else np.float64
+        x = np.ascontiguousarray(x, dtype=dt)
         n = self.N - row0 if nrows is None else nrows
-        y = np.empty(n)
+        y = np.empty(n, dtype=dt)
         self._ck(lib().h2w_dense_matvec(self.h, _ptr(x), _ptr(y), row0, n, HOST))
         return y
 
@@ -390,8 +400,9 @@ class H2Operator:
         return it.value, res.value
 
     def gmres(self, b, x0=None, max_iter=500, tol_pow=10):
-        b = np.ascontiguousarray(b, dtype=np.float64)
-        x = np.ones(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        dt = np.complex128 if self.complex else np.float64
+        b = np.ascontiguousarray(b, dtype=dt)
+        x = np.ones(self.N, dtype=dt) if x0 is None else np.array(x0, dtype=dt)
         it, res = ctypes.c_int(), ctypes.c_double()
         rc = lib().h2w_gmres(self.h, _ptr(b), _ptr(x), max_iter, tol_pow, HOST, ctypes.byref(it), ctypes.byref(res))
         self._ck(rc, allow=(ERR_NOT_CONVERGED,))

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libh2w.so")
-SOURCES = ["kernels.cu", "multi.cu", "mrtc.cu", "mrws.cu", "gmbatch.cu", "batch.cu", "learn.cu", "ncabig.cu", "m2lfly.cu", "noalloc.cu", "capi.cpp", "tree.cpp"]
+SOURCES = ["kernels.cu", "multi.cu", "mrtc.cu", "mrws.cu", "gmbatch.cu", "batch.cu", "learn.cu", "ncabig.cu", "m2lfly.cu", "noalloc.cu", "helm.cu", "capi.cpp", "tree.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

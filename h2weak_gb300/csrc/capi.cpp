@@ -6,6 +6,7 @@
 #include <atomic>
 #include <climits>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -109,6 +110,13 @@ struct h2w_handle {
     std::vector<std::vector<int32_t>> imp_val;
     // kernel parameters
     double diag = 0, c2d = 0, four_pi = 0, loga = 0, den_small = 0, kii = 0;
+    // complex kernel (choice H2W_KERNEL_HELMHOLTZ): complex entries, the operator
+    // stored realified (every complex block as [[Re, -Im], [Im, Re]] with rows and
+    // columns interleaved), vectors as interleaved (re, im) doubles
+    bool cplx = false;
+    double diag_im = 0;
+    DBuf<double2> c_V, c_w, c_r, c_ax, c_part, c_h, c_y;  // complex GMRES state
+    int64_t nv() const { return cplx ? 2 * tree.N : tree.N; }  // doubles per vector
     // device state
     DBuf<double> d_pts;
     DBuf<int32_t> d_perm;
@@ -229,6 +237,7 @@ struct h2w_handle {
         k.four_pi = four_pi;
         k.loga = loga;
         k.den_small = den_small;
+        k.diag_im = diag_im;
         return k;
     }
 };
@@ -322,6 +331,10 @@ void setup_kernel(h2w_handle *h) {
         }
         h->kii = res;
         h->diag = (1.0 + res) / hd;
+    } else if (h->cfg.choice == H2W_KERNEL_HELMHOLTZ) {
+        // Helmholtz3D diagonal, 3D/codes/kernel.hpp:140-141
+        h->diag = 500 * std::sqrt(double(dn));
+        h->diag_im = 0.0;
     } else {
         h->diag = dim == 2 ? 1.0 : std::sqrt((double)dn);
     }
@@ -850,9 +863,116 @@ void run_nca_learned(h2w_handle *h, const std::vector<std::vector<int32_t>> &R,
     }
 }
 
+// Complex kernel: one CTA per block (nca_c_kernel). Each block starts with
+// scratch for 128 pivots (at most min(rows, columns)); blocks that fill it run
+// again with twice as many, up to what one CTA's shared memory holds (the
+// reference's own bound, min(rows, columns), otherwise; an explicit rank_cap
+// stops earlier with H2W_ERR_RANK).
+void run_nca_complex(h2w_handle *h, const std::vector<std::vector<int32_t>> &R,
+                     const std::vector<std::vector<int32_t>> &C, std::vector<std::vector<int32_t>> &prow,
+                     std::vector<std::vector<int32_t>> &pcol) {
+    const size_t np = R.size();
+    prow.assign(np, {});
+    pcol.assign(np, {});
+    const double tol = std::pow(10, -1.0 * h->cfg.tol_pow);
+    const int cap = h->cfg.rank_cap > 0 ? h->cfg.rank_cap : INT32_MAX;
+    int smem_max = 0;
+    CK(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->cfg.device));
+    KParams kp = h->kparams();
+    std::vector<std::pair<size_t, int>> pend;
+    for (size_t p = 0; p < np; ++p) {
+        const int mn = (int)std::min(R[p].size(), C[p].size());
+        pend.push_back({p, std::min(std::min(mn, cap), 128)});
+    }
+    const size_t budget = (size_t)2 << 30;  // scratch bytes per batch
+    while (!pend.empty()) {
+        std::vector<std::pair<size_t, int>> again;
+        size_t q0 = 0;
+        while (q0 < pend.size()) {
+            std::vector<NcaProb> probs;
+            std::vector<int32_t> idx;
+            size_t scr = 0;
+            int64_t piv = 0;
+            int mx1 = 1, mx2 = 1, mxr = 1;
+            size_t q = q0;
+            for (; q < pend.size(); ++q) {
+                const size_t p = pend[q].first;
+                const int n1 = (int)R[p].size(), n2 = (int)C[p].size(), rc = pend[q].second;
+                const size_t need = (size_t)rc * (size_t)(n1 + n2);
+                if (!probs.empty() && (scr + need) * 16 > budget) break;
+                if (nca_c_smem(std::max(mx1, n1), std::max(mx2, n2), std::max(mxr, rc)) > (size_t)smem_max) {
+                    if (probs.empty())
+                        throw ApiError(H2W_ERR_RANK, "a complex NCA block needs more pivots than one CTA holds (" +
+                                                         std::to_string(rc) + ")");
+                    break;
+                }
+                NcaProb pb{};
+                pb.ri = (int64_t)idx.size();
+                append(idx, R[p].data(), n1);
+                pb.ci = (int64_t)idx.size();
+                append(idx, C[p].data(), n2);
+                pb.u = (int64_t)scr;
+                pb.v = (int64_t)(scr + (size_t)rc * n1);
+                scr += need;
+                pb.piv = piv;
+                piv += rc;
+                pb.n1 = n1;
+                pb.n2 = n2;
+                pb.rcap = rc;
+                probs.push_back(pb);
+                mx1 = std::max(mx1, n1);
+                mx2 = std::max(mx2, n2);
+                mxr = std::max(mxr, rc);
+            }
+            DBuf<NcaProb> dp;
+            DBuf<int32_t> di, drank, dpr, dpc, dst;
+            DBuf<double2> dscr;
+            dp.upload(probs, h->stream);
+            di.upload(idx, h->stream);
+            dscr.alloc(std::max<size_t>(scr, 1));
+            drank.alloc(probs.size());
+            dpr.alloc((size_t)std::max<int64_t>(piv, 1));
+            dpc.alloc((size_t)std::max<int64_t>(piv, 1));
+            dst.alloc(1);
+            CK(cudaMemsetAsync(dst.p, 0, 4, h->stream));
+            CK(launch_nca_c(dp.p, (int)probs.size(), di.p, kp, tol, dscr.p, drank.p, dpr.p, dpc.p, dst.p, mx1, mx2,
+                            mxr, h->stream));
+            std::vector<int32_t> rk(probs.size()), hpr((size_t)piv), hpc((size_t)piv);
+            int32_t status = 0;
+            CK(cudaMemcpyAsync(rk.data(), drank.p, rk.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+            if (piv) {
+                CK(cudaMemcpyAsync(hpr.data(), dpr.p, hpr.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+                CK(cudaMemcpyAsync(hpc.data(), dpc.p, hpc.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+            }
+            CK(cudaMemcpyAsync(&status, dst.p, 4, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (status & 2) throw ApiError(H2W_ERR_ARG, "non-finite kernel entries (coincident points?) in an NCA block");
+            for (size_t k = 0; k < probs.size(); ++k) {
+                const auto &pq = pend[q0 + k];
+                const size_t p = pq.first;
+                if (rk[k] < 0) {
+                    const int mn = (int)std::min(R[p].size(), C[p].size());
+                    const int lim = std::min(mn, cap);
+                    if (pq.second >= lim)
+                        throw ApiError(H2W_ERR_RANK, "an NCA block needed more than rank_cap = " +
+                                                         std::to_string(h->cfg.rank_cap) + " pivots");
+                    again.push_back({p, std::min(lim, 2 * pq.second)});
+                    continue;
+                }
+                const NcaProb &pb = probs[k];
+                prow[p].assign(hpr.begin() + pb.piv, hpr.begin() + pb.piv + rk[k]);
+                pcol[p].assign(hpc.begin() + pb.piv, hpc.begin() + pb.piv + rk[k]);
+            }
+            q0 = q;
+        }
+        pend.swap(again);
+    }
+}
+
 void run_nca(h2w_handle *h, const std::vector<std::vector<int32_t>> &R, const std::vector<std::vector<int32_t>> &C,
              std::vector<std::vector<int32_t>> &prow, std::vector<std::vector<int32_t>> &pcol) {
-    if (h->learned) run_nca_learned(h, R, C, prow, pcol);
+    if (h->cplx) run_nca_complex(h, R, C, prow, pcol);
+    else if (h->learned) run_nca_learned(h, R, C, prow, pcol);
     else run_nca_plain(h, R, C, prow, pcol);
 }
 
@@ -1092,11 +1212,48 @@ struct PlanBuilder {
     bool fused = true;        // no leaf (scatter) target was column-split
 
     // column-major block: element (i, c) at a + c*lda + i, lda = pad4(rows)
+    std::vector<int64_t> blocks;  // (a, lda, cols) of every block, in allocation order
     int64_t alloc(int64_t rows, int64_t cols, int32_t &lda) {
         lda = (int32_t)pad4(rows);
         int64_t a = opn;
         opn += pad4((int64_t)lda * cols);
+        blocks.push_back(a);
+        blocks.push_back(lda);
+        blocks.push_back(cols);
         return a;
+    }
+    // The logical targets of a complex operator rewritten for its realified
+    // form: every row, column, workspace and vector position doubled (interleaved
+    // (re, im)), every block address mapped to its real block (4a, lda 2 lda).
+    void realify() {
+        auto addr = [&](int64_t a) {
+            // the block holding complex address a: element (i, c) at base + c lda + i
+            size_t lo = 0, hi = blocks.size() / 3;
+            while (hi - lo > 1) {
+                size_t mid = (lo + hi) / 2;
+                if (blocks[3 * mid] <= a) lo = mid;
+                else hi = mid;
+            }
+            const int64_t base = blocks[3 * lo], ld = blocks[3 * lo + 1];
+            const int64_t o = a - base, c = o / ld, i = o - c * ld;
+            return 4 * base + 2 * c * (2 * ld) + 2 * i;
+        };
+        for (LTarget &l : logical) {
+            l.dst *= 2;
+            l.nrows *= 2;
+            for (PanelSpec &p : l.panels) {
+                p.a = addr(p.a);
+                p.lda *= 2;
+                p.w *= 2;
+                for (Seg &g : p.segs) {
+                    g.src *= 2;
+                    g.len *= 2;
+                    g.xoff *= 2;
+                }
+            }
+        }
+        opn *= 4;
+        read_elems *= 4;
     }
     int64_t put_idx(const int32_t *v, int64_t n) {
         int64_t o = (int64_t)idx.size();
@@ -1240,7 +1397,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h, const std::vector
     for (const Target &t : pb.T) {
         if (t.nrows < 1 || t.dst < 0 || t.dst + t.nrows > wsn) bad("target rows");
         if (t.p0 < 0 || t.p1 < t.p0 || t.p1 > (int32_t)pb.P.size() || t.p1 - t.p0 > BRG_MAX_PANELS) bad("target panels");
-        if ((t.flags & T_SCATTER) && (t.dst < h->yperm_off || t.dst + t.nrows > h->yperm_off + N)) bad("scatter rows");
+        if ((t.flags & T_SCATTER) && (t.dst < h->yperm_off || t.dst + t.nrows > h->yperm_off + h->nv())) bad("scatter rows");
         int64_t xw = 0;
         for (int32_t q = t.p0; q < t.p1; ++q) {
             const Panel &p = pb.P[(size_t)q];
@@ -1253,7 +1410,7 @@ void validate_plan(const PlanBuilder &pb, const h2w_handle *h, const std::vector
                 const Seg &sg = pb.S[(size_t)e];
                 if (sg.len < 0 || sg.xoff < 0 || sg.xoff + sg.len > p.w) bad("segment span");
                 if (sg.flags & S_GATHER) {
-                    if (sg.src < 0 || sg.src + sg.len > N) bad("gather segment");
+                    if (sg.src < 0 || sg.src + sg.len > h->nv()) bad("gather segment");
                 } else if (sg.src < 0 || sg.src + sg.len > wsn) bad("workspace segment");
             }
             xw += pad4(p.w);
@@ -1330,7 +1487,7 @@ void assign_phases(h2w_handle *h, PlanBuilder &pb, int NPH, std::vector<Phase> &
     const Phase &lp = phases.back();
     for (int64_t r = lp.t0; r < lp.t1; ++r)
         if (pb.T[(size_t)r].flags & T_SCATTER) covered += pb.T[(size_t)r].nrows;
-    fused = pb.fused && covered == h->tree.N;
+    fused = pb.fused && covered == h->nv();
     if (!fused)
         for (int64_t r = lp.t0; r < lp.t1; ++r)
             if (pb.T[(size_t)r].flags & T_SCATTER) pb.T[(size_t)r].flags = T_ACCUM;
@@ -1786,7 +1943,7 @@ void build_plan(h2w_handle *h) {
     // ---- coupling phase: M2L (far, vertex), near field, pair phase A
     std::vector<std::vector<int64_t>> pfac((size_t)L + 1);
     // far M2L on the fly: its work items instead of stored blocks
-    const bool fly = h->far_fly && has_far && L >= 2;
+    const bool fly = h->far_fly && has_far && L >= 2 && !h->cplx;
     h->fly_active = fly;
     h->fly_rows.clear();
     h->fly_entries = 0;
@@ -2129,32 +2286,69 @@ void build_plan(h2w_handle *h) {
         h->d_ptsdf.reset();
         h->d_logtab.reset();
     }
-    h->op_n = pb.opn;
-    h->op_bytes_read = pb.read_elems;
-    h->d_op.alloc((size_t)pb.opn);
-    CK(cudaMemsetAsync(h->d_op.p, 0, (size_t)pb.opn * 8, st));
-    DBuf<int32_t> didx;
-    DBuf<FillJob> dfill;
-    DBuf<FactorJob> dfac;
-    DBuf<XferJob> dxf;
-    DBuf<double> dF;
-    didx.upload(pb.idx, st);
-    dfill.upload(pb.fills, st);
-    dfac.upload(pb.factors, st);
-    dxf.upload(pb.xfers, st);
-    dF.alloc((size_t)std::max<int64_t>(pb.fn, 1));
-    KParams kp = h->kparams();
-    CK(launch_factor(dfac.p, (int)pb.factors.size(), didx.p, kp, dF.p, st));
-    CK(launch_xfer(dxf.p, (int)pb.xfers.size(), pb.max_xfer_n, didx.p, kp, dF.p, h->d_op.p, st));
-    CK(launch_fill(dfill.p, (int)pb.fills.size(), didx.p, kp, h->d_op.p, st));
-    // the assembly's index and job lists are not needed again
-    pb.idx = std::vector<int32_t>();
-    pb.fills = std::vector<FillJob>();
-    pb.factors = std::vector<FactorJob>();
-    pb.xfers = std::vector<XferJob>();
-    h->plan = pbp;
-    realize_single(h, h->row_split);
-    realize_multi(h, h->mr_xw);
+    if (h->cplx) {
+        // complex operator image from the same jobs (complex units), then its
+        // realified form; the real FP64 product kernels apply it
+        DBuf<int32_t> didx;
+        DBuf<FillJob> dfill;
+        DBuf<FactorJob> dfac;
+        DBuf<XferJob> dxf;
+        DBuf<double2> dF, opc;
+        DBuf<int64_t> dblk;
+        didx.upload(pb.idx, st);
+        dfill.upload(pb.fills, st);
+        dfac.upload(pb.factors, st);
+        dxf.upload(pb.xfers, st);
+        dF.alloc((size_t)std::max<int64_t>(pb.fn, 1));
+        opc.alloc((size_t)std::max<int64_t>(pb.opn, 1));
+        CK(cudaMemsetAsync(opc.p, 0, (size_t)std::max<int64_t>(pb.opn, 1) * 16, st));
+        CK(launch_assemble_c(dfac.p, (int)pb.factors.size(), dxf.p, (int)pb.xfers.size(), pb.max_xfer_n, dfill.p,
+                             (int)pb.fills.size(), didx.p, h->kparams(), dF.p, opc.p, st));
+        pb.realify();
+        h->ws_n *= 2;
+        h->yperm_off *= 2;
+        h->op_n = pb.opn;
+        h->op_bytes_read = pb.read_elems;
+        h->d_op.alloc((size_t)pb.opn);
+        CK(cudaMemsetAsync(h->d_op.p, 0, (size_t)pb.opn * 8, st));
+        dblk.upload(pb.blocks, st);
+        CK(launch_realify(dblk.p, (int64_t)pb.blocks.size() / 3, opc.p, h->d_op.p, st));
+        CK(cudaStreamSynchronize(st));
+        pb.idx = std::vector<int32_t>();
+        pb.fills = std::vector<FillJob>();
+        pb.factors = std::vector<FactorJob>();
+        pb.xfers = std::vector<XferJob>();
+        pb.blocks = std::vector<int64_t>();
+        h->plan = pbp;
+        realize_single(h, h->row_split);
+    } else {
+        h->op_n = pb.opn;
+        h->op_bytes_read = pb.read_elems;
+        h->d_op.alloc((size_t)pb.opn);
+        CK(cudaMemsetAsync(h->d_op.p, 0, (size_t)pb.opn * 8, st));
+        DBuf<int32_t> didx;
+        DBuf<FillJob> dfill;
+        DBuf<FactorJob> dfac;
+        DBuf<XferJob> dxf;
+        DBuf<double> dF;
+        didx.upload(pb.idx, st);
+        dfill.upload(pb.fills, st);
+        dfac.upload(pb.factors, st);
+        dxf.upload(pb.xfers, st);
+        dF.alloc((size_t)std::max<int64_t>(pb.fn, 1));
+        KParams kp = h->kparams();
+        CK(launch_factor(dfac.p, (int)pb.factors.size(), didx.p, kp, dF.p, st));
+        CK(launch_xfer(dxf.p, (int)pb.xfers.size(), pb.max_xfer_n, didx.p, kp, dF.p, h->d_op.p, st));
+        CK(launch_fill(dfill.p, (int)pb.fills.size(), didx.p, kp, h->d_op.p, st));
+        // the assembly's index and job lists are not needed again
+        pb.idx = std::vector<int32_t>();
+        pb.fills = std::vector<FillJob>();
+        pb.factors = std::vector<FactorJob>();
+        pb.xfers = std::vector<XferJob>();
+        h->plan = pbp;
+        realize_single(h, h->row_split);
+        realize_multi(h, h->mr_xw);
+    }
     h->d_ws.alloc((size_t)h->ws_n);
     h->d_ctr.alloc(h->phases.size() + 1);
     h->d_err.alloc(1);
@@ -2340,9 +2534,9 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     }
     if (!h->fused_scatter) {
         if (permuted)
-            CK(cudaMemcpyAsync(dy, h->d_ws.p + h->yperm_off, (size_t)h->tree.N * 8, cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(dy, h->d_ws.p + h->yperm_off, (size_t)h->nv() * 8, cudaMemcpyDeviceToDevice, st));
         else
-            CK(launch_scatter_f64(h->d_ws.p + h->yperm_off, dy, h->d_perm.p, h->tree.N, st));
+            CK(launch_scatter_f64(h->d_ws.p + h->yperm_off, dy, h->d_perm.p, h->nv(), st));
     }
 }
 
@@ -3311,6 +3505,140 @@ void require_tree(h2w_handle *h) {
 void require_op(h2w_handle *h) {
     if (!h->has_op) throw ApiError(H2W_ERR_STATE, "operator not assembled (call h2w_assemble)");
 }
+// Entry points of the real kernels only (mixed precision, batched, learned,
+// far field on the fly, allocation-free product).
+void require_real(const h2w_handle *h, const char *what) {
+    if (h->cplx) throw ApiError(H2W_ERR_ARG, std::string(what) + " is not available for the complex Helmholtz kernel");
+}
+
+// The reference GMRES (3D/codes/gmres.hpp:92-200, USE_Helm) on the complex
+// operator: restart = max_iter, x0 from x, H(k,i) = w.dot(v_k) with Eigen's
+// conjugate-first dot (sum conj(w) v_k), modified Gram-Schmidt in the
+// reference's order, the reference's complex Givens formulas
+// (GeneratePlaneRotation, gmres.hpp:52-68; ApplyPlaneRotation, :70-75) and
+// back substitution on the host in std::complex arithmetic, stop when
+// |s(i+1)| / ||b|| < tol. Krylov vectors, products and Gram-Schmidt on the
+// GPU; the Hessenberg column comes to the host once per step. b, x: leaf
+// order, interleaved (re, im), device.
+int cgmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double tol, int *iters, double *resid) {
+    typedef std::complex<double> cd;
+    cudaStream_t st = h->stream;
+    const int64_t n = h->tree.N;
+    const int m = max_iter;
+    if (h->c_V.n < (size_t)n * (size_t)(m + 1)) h->c_V.alloc((size_t)n * (size_t)(m + 1));
+    if (h->c_w.n < (size_t)n) h->c_w.alloc((size_t)n);
+    if (h->c_r.n < (size_t)n) h->c_r.alloc((size_t)n);
+    if (h->c_ax.n < (size_t)n) h->c_ax.alloc((size_t)n);
+    if (h->c_part.n < (size_t)cgm_blocks()) h->c_part.alloc((size_t)cgm_blocks());
+    if (h->c_h.n < (size_t)(m + 2)) h->c_h.alloc((size_t)(m + 2));
+    if (h->c_y.n < (size_t)(m + 1)) h->c_y.alloc((size_t)(m + 1));
+    const double2 *b = reinterpret_cast<const double2 *>(db);
+    double2 *x = reinterpret_cast<double2 *>(dx);
+    auto A = [&](const double2 *in, double2 *out) {
+        run_matvec_f64(h, reinterpret_cast<const double *>(in), reinterpret_cast<double *>(out), st, true);
+    };
+    auto dot = [&](const double2 *a, const double2 *bb, double2 *out) { CK(cgm_dot(a, bb, n, h->c_part.p, out, st)); };
+    auto fetch = [&](const double2 *src, int cnt, std::vector<cd> &o) {
+        std::vector<double2> t((size_t)cnt);
+        CK(cudaMemcpyAsync(t.data(), src, (size_t)cnt * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        o.resize((size_t)cnt);
+        for (int i = 0; i < cnt; ++i) o[(size_t)i] = cd(t[(size_t)i].x, t[(size_t)i].y);
+    };
+    auto norm = [&](const double2 *a) {
+        dot(a, a, h->c_h.p + m + 1);
+        std::vector<cd> o;
+        fetch(h->c_h.p + m + 1, 1, o);
+        return std::sqrt(o[0].real());
+    };
+    auto gen_rot = [](cd &dxv, cd &dyv, cd &cs, cd &sn) {
+        if (dxv == cd(0)) {
+            cs = cd(0);
+            sn = cd(1);
+        } else {
+            double scale = std::abs(dxv) + std::abs(dyv);
+            double nrm = scale * std::sqrt(std::abs(dxv / scale) * std::abs(dxv / scale) +
+                                           std::abs(dyv / scale) * std::abs(dyv / scale));
+            cd alpha = dxv / std::abs(dxv);
+            cs = std::abs(dxv) / nrm;
+            sn = alpha * std::conj(dyv) / nrm;
+        }
+    };
+    auto app_rot = [](cd &dxv, cd &dyv, cd &cs, cd &sn) {
+        cd temp = cs * dxv + sn * dyv;
+        dyv = -sn * dxv + cs * dyv;
+        dxv = temp;
+    };
+    std::vector<cd> H((size_t)(m + 1) * m, cd(0)), s((size_t)m + 1), cs((size_t)m + 1), sn((size_t)m + 1);
+    auto Hc = [&](int r, int c) -> cd & { return H[(size_t)c * (m + 1) + r]; };
+    auto update = [&](int k) {  // Update(x, k, H, s, v): back substitution, then x += sum_j v_j y_j
+        std::vector<cd> y(s);
+        for (int i = k; i >= 0; i--) {
+            y[(size_t)i] /= Hc(i, i);
+            for (int j = i - 1; j >= 0; j--) y[(size_t)j] -= Hc(j, i) * y[(size_t)i];
+        }
+        std::vector<double2> yd((size_t)k + 1);
+        for (int j = 0; j <= k; ++j) yd[(size_t)j] = make_double2(y[(size_t)j].real(), y[(size_t)j].imag());
+        CK(cudaMemcpyAsync(h->c_y.p, yd.data(), yd.size() * 16, cudaMemcpyHostToDevice, st));
+        CK(cgm_update_launch(x, h->c_V.p, h->c_y.p, k + 1, n, st));
+        CK(cudaStreamSynchronize(st));
+    };
+    double normb = norm(b);
+    A(x, h->c_ax.p);
+    CK(cgm_resid_launch(h->c_r.p, b, h->c_ax.p, n, st));
+    double beta = norm(h->c_r.p);
+    if (normb == 0.0) normb = 1;
+    double res = beta / normb;
+    *resid = res;
+    *iters = 0;
+    if (res <= tol) return H2W_OK;
+    int j = 1;
+    while (j <= max_iter) {
+        CK(cgm_scale_launch(h->c_V.p, h->c_r.p, 1.0 / beta, n, st));
+        std::fill(s.begin(), s.end(), cd(0));
+        s[0] = beta;
+        int i;
+        for (i = 0; i < m && j <= max_iter; i++, j++) {
+            double2 *vi = h->c_V.p + (size_t)i * n;
+            A(vi, h->c_w.p);
+            for (int k = 0; k <= i; k++) {
+                double2 *hk = h->c_h.p + k;
+                dot(h->c_w.p, h->c_V.p + (size_t)k * n, hk);
+                CK(cgm_axpy_launch(h->c_w.p, h->c_V.p + (size_t)k * n, hk, n, st));
+            }
+            const double hn = norm(h->c_w.p);
+            std::vector<cd> col;
+            fetch(h->c_h.p, i + 1, col);
+            for (int k = 0; k <= i; ++k) Hc(k, i) = col[(size_t)k];
+            Hc(i + 1, i) = hn;
+            CK(cgm_scale_launch(h->c_V.p + (size_t)(i + 1) * n, h->c_w.p, 1.0 / hn, n, st));
+            for (int k = 0; k < i; k++) app_rot(Hc(k, i), Hc(k + 1, i), cs[(size_t)k], sn[(size_t)k]);
+            gen_rot(Hc(i, i), Hc(i + 1, i), cs[(size_t)i], sn[(size_t)i]);
+            app_rot(Hc(i, i), Hc(i + 1, i), cs[(size_t)i], sn[(size_t)i]);
+            app_rot(s[(size_t)i], s[(size_t)i + 1], cs[(size_t)i], sn[(size_t)i]);
+            res = std::abs(s[(size_t)i + 1]) / normb;
+            if (res < tol) {
+                update(i);
+                *resid = res;
+                *iters = j;
+                return H2W_OK;
+            }
+        }
+        update(m - 1);
+        A(x, h->c_ax.p);
+        CK(cgm_resid_launch(h->c_r.p, b, h->c_ax.p, n, st));
+        beta = norm(h->c_r.p);
+        res = beta / normb;
+        if (res < tol) {
+            *resid = res;
+            *iters = j;
+            return H2W_OK;
+        }
+    }
+    *resid = res;
+    *iters = max_iter;
+    return H2W_OK;
+}
 
 }  // namespace
 
@@ -3347,6 +3675,7 @@ int matvec_external_ws(h2w_handle *h, const double *x, double *y, int precision,
                        int64_t ws_cap, unsigned *bar, int32_t *err) {
     return guarded(h, [&] {
         require_op(h);
+        require_real(h, "the allocation-free product");
         if (!x || !y || !ws || !bar || !err || (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32))
             throw ApiError(H2W_ERR_ARG, "bad matvec arguments");
         const bool f32 = precision == H2W_PREC_FP32;
@@ -3405,8 +3734,10 @@ extern "C" {
 int h2w_create(const h2w_config *cfg, h2w_handle **out) {
     if (!cfg || !out) return H2W_ERR_ARG;
     *out = nullptr;
-    if (cfg->dim < 1 || cfg->dim > 3 || (cfg->form != 0 && cfg->form != 1 && cfg->form != 2) || (cfg->form == 2 && cfg->dim == 1) || (cfg->choice != 0 && cfg->choice != 1) ||
-        cfg->nlevels < 1 || cfg->tol_pow < 0 || cfg->rank_cap < 0)
+    if (cfg->dim < 1 || cfg->dim > 3 || (cfg->form != 0 && cfg->form != 1 && cfg->form != 2) || (cfg->form == 2 && cfg->dim == 1) ||
+        (cfg->choice != 0 && cfg->choice != 1 && cfg->choice != H2W_KERNEL_HELMHOLTZ) ||
+        (cfg->choice == H2W_KERNEL_HELMHOLTZ && (cfg->dim != 3 || cfg->form == 2)) || cfg->nlevels < 1 ||
+        cfg->tol_pow < 0 || cfg->rank_cap < 0)
         return H2W_ERR_ARG;
     h2w_handle *h = nullptr;
     if (cfg->device >= 0) {
@@ -3415,6 +3746,7 @@ int h2w_create(const h2w_config *cfg, h2w_handle **out) {
         if (cfg->device >= ndev) return H2W_ERR_ARG;
         h = new h2w_handle;
         h->cfg = *cfg;
+        h->cplx = cfg->choice == H2W_KERNEL_HELMHOLTZ;
         if (cudaSetDevice(cfg->device) != cudaSuccess ||
             cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
             delete h;
@@ -3424,6 +3756,7 @@ int h2w_create(const h2w_config *cfg, h2w_handle **out) {
         // host-only handle: points, tree and lists, no device work
         h = new h2w_handle;
         h->cfg = *cfg;
+        h->cplx = cfg->choice == H2W_KERNEL_HELMHOLTZ;
     }
     *out = h;
     return H2W_OK;
@@ -3543,7 +3876,16 @@ int h2w_build_tree(h2w_handle *h) {
         h->has_op = false;
         if (h->cfg.device >= 0) {
             h->d_pts.upload(h->pts, h->stream);
-            h->d_perm.upload(h->tree.perm, h->stream);
+            if (h->cplx) {  // realified permutation: (re, im) of leaf position p -> of point perm[p]
+                std::vector<int32_t> p2((size_t)(2 * h->tree.N));
+                for (int64_t i = 0; i < h->tree.N; ++i) {
+                    p2[(size_t)(2 * i)] = 2 * h->tree.perm[(size_t)i];
+                    p2[(size_t)(2 * i + 1)] = 2 * h->tree.perm[(size_t)i] + 1;
+                }
+                h->d_perm.upload(p2, h->stream);
+            } else {
+                h->d_perm.upload(h->tree.perm, h->stream);
+            }
             CK(cudaStreamSynchronize(h->stream));
         }
         setup_kernel(h);
@@ -3665,6 +4007,7 @@ int h2w_assemble(h2w_handle *h, int mode) {
         const bool nn = h->cfg.form == H2W_FORM_NONNESTED;
         h->phases.clear();
         h->has_op = false;
+        if (mode == H2W_ASSEMBLE_LEARNED) require_real(h, "learned assembly");
         if (mode == H2W_ASSEMBLE_LEARNED && !h->d_mlp.p)
             throw ApiError(H2W_ERR_STATE, "learned assembly needs a model (h2w_learn_set_model)");
         h->learned = mode == H2W_ASSEMBLE_LEARNED;
@@ -3756,6 +4099,27 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
         const int64_t N = h->tree.N;
         if (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32 && precision != H2W_PREC_DF64)
             throw ApiError(H2W_ERR_ARG, "unknown precision");
+        if (h->cplx) {  // complex operator: one FP64 product of interleaved (re, im) vectors
+            if (precision != H2W_PREC_FP64 || nrhs != 1)
+                throw ApiError(H2W_ERR_ARG, "the complex Helmholtz kernel has the FP64 single-vector product only");
+            const int64_t nv = h->nv();
+            const double *dx = x;
+            double *dy = y;
+            if (where == H2W_HOST) {
+                h->d_x.n < (size_t)nv ? h->d_x.alloc((size_t)nv) : (void)0;
+                h->d_y.n < (size_t)nv ? h->d_y.alloc((size_t)nv) : (void)0;
+                CK(cudaMemcpyAsync(h->d_x.p, x, (size_t)nv * 8, cudaMemcpyHostToDevice, st));
+                dx = h->d_x.p;
+                dy = h->d_y.p;
+            }
+            run_matvec_f64(h, dx, dy, st);
+            if (where == H2W_HOST) {
+                CK(cudaMemcpyAsync(y, h->d_y.p, (size_t)nv * 8, cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                check_device_error(h);
+            }
+            return H2W_OK;
+        }
         const bool df_single = nrhs == 1 && precision == H2W_PREC_DF64 && h->fly_active;
         if (nrhs > 1 || (precision == H2W_PREC_DF64 && !df_single)) {
             // blocks of up to 64 columns through the multi-vector kernel
@@ -3817,7 +4181,7 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
     return guarded(h, [&] {
         require_op(h);
         if (!b || !x || max_iter < 1 || !iters || !resid) throw ApiError(H2W_ERR_ARG, "bad gmres arguments");
-        const int64_t N = h->tree.N;
+        const int64_t N = h->nv();  // doubles per vector (interleaved (re, im) for the complex kernel)
         double tol = std::pow(10, -1.0 * tol_pow);
         const double *db = b;
         double *dx = x;
@@ -3834,7 +4198,8 @@ int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_p
         if (xp.n < (size_t)N) xp.alloc((size_t)N);
         CK(launch_gather_f64(db, bp.p, h->d_perm.p, N, h->stream));
         CK(launch_gather_f64(dx, xp.p, h->d_perm.p, N, h->stream));
-        int rc = gmres_run(h, bp.p, xp.p, max_iter, tol, H2W_PREC_FP64, iters, resid);
+        int rc = h->cplx ? cgmres_run(h, bp.p, xp.p, max_iter, tol, iters, resid)
+                         : gmres_run(h, bp.p, xp.p, max_iter, tol, H2W_PREC_FP64, iters, resid);
         CK(launch_scatter_f64(xp.p, dx, h->d_perm.p, N, h->stream));
         CK(cudaStreamSynchronize(h->stream));
         check_device_error(h);
@@ -3850,6 +4215,7 @@ int h2w_gmres_ir(h2w_handle *h, const double *b, double *x, int max_outer, int i
                  int *outer_iters, int *inner_total, double *resid) {
     return guarded(h, [&] {
         require_op(h);
+        require_real(h, "h2w_gmres_ir");
         if (!b || !x || max_outer < 1 || inner_iter < 1 || !outer_iters || !inner_total || !resid)
             throw ApiError(H2W_ERR_ARG, "bad gmres_ir arguments");
         const int64_t N = h->tree.N;
@@ -3936,6 +4302,7 @@ int h2w_gmres_batch(h2w_handle *h, const double *b, double *x, int nrhs, int max
                     int *iters, double *resid) {
     return guarded(h, [&] {
         require_op(h);
+        require_real(h, "h2w_gmres_batch");
         if (!b || !x || nrhs < 1 || max_iter < 1 || max_iter > 400 || !iters || !resid ||
             (where != H2W_HOST && where != H2W_DEVICE))
             throw ApiError(H2W_ERR_ARG, "bad gmres_batch arguments");
@@ -3953,6 +4320,7 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
                        int tol_pow, int where, int *outer_iters, int *inner_total, double *resid) {
     return guarded(h, [&] {
         require_op(h);
+        require_real(h, "h2w_gmres_ir_batch");
         if (!b || !x || nrhs < 1 || max_outer < 1 || inner_iter < 1 || inner_iter > 400 || !outer_iters ||
             !inner_total || !resid || (where != H2W_HOST && where != H2W_DEVICE))
             throw ApiError(H2W_ERR_ARG, "bad gmres_ir_batch arguments");
@@ -4160,6 +4528,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
 int h2w_autotune(h2w_handle *h, int nrhs, int precision, int reps, int64_t *chosen, double *best_ms) {
     return guarded(h, [&] {
         require_op(h);
+        require_real(h, "h2w_autotune");
         const bool mix = precision == H2W_TUNE_IR_MIX;
         if (nrhs < 1 || reps < 1 ||
             (precision != H2W_PREC_FP64 && precision != H2W_PREC_FP32 && precision != H2W_PREC_DF64 && !mix) ||
@@ -4252,7 +4621,7 @@ int h2w_batch_create(h2w_handle *const *handles, int n, h2w_batch **out) {
     auto *b = new h2w_batch();
     b->hs.assign(handles, handles + n);
     for (h2w_handle *h : b->hs)
-        if (!h || !h->has_op || !h->plan || h->cfg.device != b->hs[0]->cfg.device || h->fly_active) {
+        if (!h || !h->has_op || !h->plan || h->cfg.device != b->hs[0]->cfg.device || h->fly_active || h->cplx) {
             delete b;
             return H2W_ERR_STATE;
         }
@@ -4654,18 +5023,23 @@ int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, in
         const int64_t N = h->tree.N;
         if (!x || !y || row0 < 0 || nrows < 0 || row0 + nrows > N) throw ApiError(H2W_ERR_ARG, "bad dense arguments");
         cudaStream_t st = h->stream;
+        const int cw = h->cplx ? 2 : 1;  // doubles per entry
         const double *dx = x;
         double *dy = y;
         DBuf<double> bx, by;
         if (where == H2W_HOST) {
-            bx.alloc((size_t)N);
-            by.alloc((size_t)std::max<int64_t>(nrows, 1));
-            CK(cudaMemcpyAsync(bx.p, x, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+            bx.alloc((size_t)N * cw);
+            by.alloc((size_t)std::max<int64_t>(nrows, 1) * cw);
+            CK(cudaMemcpyAsync(bx.p, x, (size_t)N * 8 * cw, cudaMemcpyHostToDevice, st));
             dx = bx.p;
             dy = by.p;
         }
-        CK(launch_dense_matvec(h->kparams(), N, dx, dy, row0, nrows, st));
-        if (where == H2W_HOST) CK(cudaMemcpyAsync(y, by.p, (size_t)nrows * 8, cudaMemcpyDeviceToHost, st));
+        if (h->cplx)
+            CK(launch_dense_c(h->kparams(), N, reinterpret_cast<const double2 *>(dx), reinterpret_cast<double2 *>(dy),
+                              row0, nrows, st));
+        else
+            CK(launch_dense_matvec(h->kparams(), N, dx, dy, row0, nrows, st));
+        if (where == H2W_HOST) CK(cudaMemcpyAsync(y, by.p, (size_t)nrows * 8 * cw, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         return H2W_OK;
     });
@@ -4845,6 +5219,7 @@ int h2w_open_operator(const char *path, int device, h2w_handle **out) {
 int h2w_total_error(h2w_handle *h, const double *x, int64_t nrows, int where, double *err) {
     return guarded(h, [&] {
         require_op(h);
+        require_real(h, "h2w_total_error");
         if (!x || !err || (where != H2W_HOST && where != H2W_DEVICE)) throw ApiError(H2W_ERR_ARG, "bad error arguments");
         const int64_t N = h->tree.N;
         cudaStream_t st = h->stream;

@@ -549,10 +549,8 @@ __global__ void cgm_axpy(double2 *__restrict__ w, const double2 *__restrict__ v,
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         w[i] = c_sub(w[i], c_mul(c, v[i]));
 }
-// dst = src * (1 / *den): den holds a real norm in .x
-__global__ void cgm_scale(double2 *__restrict__ dst, const double2 *__restrict__ src, const double2 *__restrict__ den,
-                          int64_t n) {
-    const double s = __ddiv_rn(1.0, den->x);
+// dst = src * s (s real)
+__global__ void cgm_scale(double2 *__restrict__ dst, const double2 *__restrict__ src, double s, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = make_double2(__dmul_rn(src[i].x, s), __dmul_rn(src[i].y, s));
 }
@@ -583,8 +581,8 @@ cudaError_t cgm_axpy_launch(double2 *w, const double2 *v, const double2 *h, int6
     count_launch();
     return cudaGetLastError();
 }
-cudaError_t cgm_scale_launch(double2 *dst, const double2 *src, const double2 *den, int64_t n, cudaStream_t st) {
-    cgm_scale<<<CGM_BLOCKS, CGM_THREADS, 0, st>>>(dst, src, den, n);
+cudaError_t cgm_scale_launch(double2 *dst, const double2 *src, double s, int64_t n, cudaStream_t st) {
+    cgm_scale<<<CGM_BLOCKS, CGM_THREADS, 0, st>>>(dst, src, s, n);
     count_launch();
     return cudaGetLastError();
 }

@@ -21,6 +21,7 @@ struct KParams {
     double four_pi;      // 3D IE: 4 pi
     double loga;         // 3D RBF: log(a)
     double den_small;    // 3D RBF: a log(a) - 1
+    double diag_im;      // complex kernels: imaginary part of the diagonal value
 };
 
 struct NcaProb {
@@ -120,6 +121,31 @@ cudaError_t launch_fly_df64(const FlyItem *items, int64_t nitems, unsigned long 
                             double *ws, const KParams &kp, const FlyK32 &k32, cudaStream_t st);
 void fly_df_logtab(float *out);
 cudaError_t launch_ptsdf(const double *pts, int dim, int64_t n, float *out, cudaStream_t st);
+
+// Complex Helmholtz kernels (helm.cu). Positions of the assembly jobs are in
+// complex units of a complex operator image opc; launch_realify expands each
+// complex block (a, lda, cols triples in blk, complex units) into the real
+// block [[Re, -Im], [Im, Re]] with interleaved rows and columns at 4a,
+// leading dimension 2 lda, of the real operator.
+size_t nca_c_smem(int max_n1, int max_n2, int max_rcap);
+cudaError_t launch_nca_c(const NcaProb *probs, int nprob, const int32_t *idx, const KParams &kp, double tol,
+                         double2 *scratch, int32_t *rank, int32_t *prow, int32_t *pcol, int32_t *status, int max_n1,
+                         int max_n2, int max_rcap, cudaStream_t st);
+cudaError_t launch_assemble_c(const FactorJob *fac, int nfac, const XferJob *xf, int nxf, int max_n,
+                              const FillJob *fill, int nfill, const int32_t *idx, const KParams &kp, double2 *F,
+                              double2 *opc, cudaStream_t st);
+cudaError_t launch_realify(const int64_t *blk, int64_t nblk, const double2 *opc, double *op, cudaStream_t st);
+cudaError_t launch_dense_c(const KParams &kp, int64_t N, const double2 *x, double2 *y, int64_t row0, int64_t nrows,
+                           cudaStream_t st);
+// The reference GMRES's complex vector operations (n complex entries):
+// out = sum conj(a_i) b_i (part: cgm_blocks() scratch entries), w -= (*h) v,
+// dst = s src (s real), x += sum_j V[:, j] y_j, r = b - ax.
+int cgm_blocks();
+cudaError_t cgm_dot(const double2 *a, const double2 *b, int64_t n, double2 *part, double2 *out, cudaStream_t st);
+cudaError_t cgm_axpy_launch(double2 *w, const double2 *v, const double2 *h, int64_t n, cudaStream_t st);
+cudaError_t cgm_scale_launch(double2 *dst, const double2 *src, double s, int64_t n, cudaStream_t st);
+cudaError_t cgm_update_launch(double2 *x, const double2 *V, const double2 *y, int k, int64_t n, cudaStream_t st);
+cudaError_t cgm_resid_launch(double2 *r, const double2 *b, const double2 *ax, int64_t n, cudaStream_t st);
 
 // Dense FP64 oracle rows y[r] = sum_j K(r, j) x[j], r in [row0, row0+nrows).
 cudaError_t launch_dense_matvec(const KParams &kp, int64_t N, const double *x, double *y, int64_t row0,

@@ -35,8 +35,12 @@ CASES = {
     "g2d_nn_rbf": (2, "nn", 48, 3, 6, 10, 1, None, 10),
     "g3d_nn_ie": (3, "nn", 16, 2, 4, 8, 0, None, 10),
     "g2d_nn_rand": (2, "nn", 0, 3, 0, 8, 0, ("uniform", 2, 3000), 10),
+    # complex Helmholtz kernel (USE_Helm, choice 2): complex vectors
+    "g3d_n_helm": (3, "n_helm", 16, 2, 4, 10, 2, None, 10),
+    "g3d_sn_helm": (3, "sn_helm", 16, 2, 4, 8, 2, None, 10),
+    "g3d_n_helm_rand": (3, "n_helm", 0, 2, 0, 8, 2, ("uniform", 3, 4000), 10),
 }
-FORMS = {"n": 0, "sn": 1, "nn": 2}
+FORMS = {"n": 0, "sn": 1, "nn": 2, "n_helm": 0, "sn_helm": 1}
 LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge", "sn_row", "sn_col"]
 
 
@@ -47,18 +51,25 @@ def run_case(name, spec):
         N = len(pts)
     else:
         N = npar ** dim
-    vecs = [synth.normal(synth.config_seed(90, v), N) for v in range(2)]
-    xtrue = synth.normal(synth.config_seed(91, 0), N)
+    cplx = form.endswith("_helm")
+    if cplx:  # real and imaginary parts from separate streams
+        vecs = [synth.normal(synth.config_seed(90, v), N) + 1j * synth.normal(synth.config_seed(92, v), N)
+                for v in range(2)]
+        xtrue = synth.normal(synth.config_seed(91, 0), N) + 1j * synth.normal(synth.config_seed(93, 0), N)
+    else:
+        vecs = [synth.normal(synth.config_seed(90, v), N) for v in range(2)]
+        xtrue = synth.normal(synth.config_seed(91, 0), N)
     inp, out = "/tmp/golden_in_%s.bin" % name, "/tmp/golden_out_%s.bin" % name
     write_input(inp, pts, vecs, xtrue, dense=True)
     exe = os.path.join(ROOT, "oracle", "_ref", "ref%dd_%s" % (dim, form))
     r = subprocess.run([exe, str(npar), str(nlev), str(leaf), "1", str(tol), str(ch), inp, out, "500", str(gtol)],
                        capture_output=True, text=True, check=True)
     d = read_dump(out)
+    vec = (lambda a: a.view(np.complex128)) if cplx else (lambda a: a)
     rec = {"spec": np.array([dim, FORMS[form], npar, nlev, leaf, tol, ch, gtol, N], dtype=np.int64),
            "points": d["points"].reshape(N, dim), "vecs": np.stack(vecs), "xtrue": xtrue,
-           "memory": d["memory"], "matvec": d["matvec"].reshape(2, N), "dense_matvec": d["dense_matvec"],
-           "gmres_rhs": d["gmres_rhs"], "gmres_x": d["gmres_x"], "gmres_stats": d["gmres_stats"]}
+           "memory": d["memory"], "matvec": vec(d["matvec"]).reshape(2, N), "dense_matvec": vec(d["dense_matvec"]),
+           "gmres_rhs": vec(d["gmres_rhs"]), "gmres_x": vec(d["gmres_x"]), "gmres_stats": d["gmres_stats"]}
     for nm in LISTS:
         rec[nm + "_ptr"] = d[nm + ".ptr"]
         rec[nm + "_val"] = d[nm + ".val"]

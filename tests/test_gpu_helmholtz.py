@@ -1,0 +1,82 @@
+"""The complex Helmholtz kernel (the reference's USE_Helm build, choice 2:
+exp(iR)/(4 pi) off the diagonal, 500 sqrt(N) on it, 3D/codes/kernel.hpp:132-144).
+
+Parity against the reference's own outputs runs through the golden fixtures
+g3d_*_helm* (tests/test_gpu_golden.py: pivots, storage, the product on the
+reference's pivots to <= 1e-13, GMRES iterations +-1; tests/test_gpu_configs.py:
+the dense product). This file adds what the fixtures do not cover: a larger
+problem against the exact dense product, complex linearity of the product,
+and the refusal of the entry points that are real-only."""
+import numpy as np
+import pytest
+
+from h2weak_gb300 import synth
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def cvec(seed, n):
+    return synth.normal(synth.config_seed(95, seed), n) + 1j * synth.normal(synth.config_seed(96, seed), n)
+
+
+def helm_op(hw, n, nlev, tol, form=0, seed=7):
+    op = hw.H2Operator(3, form, hw.KERNEL_HELMHOLTZ, tol, nlev, device=0)
+    op.set_points(synth.uniform_points(synth.config_seed(97, seed), n, 3))
+    op.build_tree()
+    op.assemble(hw.ASSEMBLE_NCA)
+    return op
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1])
+def test_helmholtz_product_against_dense_rows(gpu, form):
+    """3D Helmholtz on 20 000 random points, 3 levels, tol 1e-8: the compressed
+    product agrees with the exact dense product (sampled rows) to the NCA
+    tolerance, and is linear over the complex numbers."""
+    hw = gpu
+    n = 20000
+    op = helm_op(hw, n, 3, 8, form)
+    x = cvec(0, n)
+    y = op.matvec(x)
+    rows = np.arange(0, n, 37)
+    yd = np.concatenate([op.dense_matvec(x, row0=int(r), nrows=1) for r in rows[:64]])
+    err = relerr(y[rows[:64]], yd)
+    assert err < 1e-7, err
+    a = 0.3 - 1.7j
+    x2 = cvec(1, n)
+    y2 = op.matvec(x2)
+    assert relerr(op.matvec(a * x + x2), a * y + y2) < 1e-13
+    # the entries are symmetric (K(i,j) = K(j,i), not Hermitian): x^T A z = z^T A x
+    assert abs(x2 @ y - x @ y2) <= 1e-9 * abs(x @ y2)
+
+
+@pytest.mark.gpu
+def test_helmholtz_gmres_solves(gpu):
+    """GMRES on the complex operator reaches its stopping test; the residual
+    it reports is the reference's |s(i+1)| / ||b||."""
+    hw = gpu
+    n = 8000
+    op = helm_op(hw, n, 2, 10)
+    xt = cvec(2, n)
+    b = op.matvec(xt)
+    x, it, res = op.gmres(b, max_iter=200, tol_pow=10)
+    assert res < 1e-10 and 1 <= it <= 200
+    assert np.all(np.isfinite(x))
+
+
+@pytest.mark.gpu
+def test_helmholtz_refuses_real_only_entry_points(gpu):
+    hw = gpu
+    op = helm_op(hw, 4096, 2, 6)
+    x = cvec(3, op.N)
+    with pytest.raises(hw.H2WError) as e:
+        op.matvec(x, precision=hw.PREC_FP32)
+    assert e.value.code == hw.ERR_ARG
+    with pytest.raises(hw.H2WError) as e:
+        op.gmres_ir(x.real)
+    assert e.value.code == hw.ERR_ARG
+    with pytest.raises(hw.H2WError) as e:
+        op.autotune(nrhs=64)
+    assert e.value.code == hw.ERR_ARG
