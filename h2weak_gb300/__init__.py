@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libh2w.so")
 OK = 0
 ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_RANK, ERR_NOT_CONVERGED, ERR_STATE = -1, -2, -3, -4, -5, -6
 FORM_NESTED, FORM_SEMINESTED, FORM_NONNESTED = 0, 1, 2
-KERNEL_IE, KERNEL_RBF, KERNEL_HELMHOLTZ = 0, 1, 2
+KERNEL_IE, KERNEL_RBF, KERNEL_HELMHOLTZ, KERNEL_HANKEL = 0, 1, 2, 10
 ASSEMBLE_NCA, ASSEMBLE_IMPORT, ASSEMBLE_LEARNED = 0, 1, 2
 PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
 HOST, DEVICE = 0, 1
@@ -169,8 +169,8 @@ class H2Operator:
             raise H2WError(rc, "h2w_create failed (no CUDA device or bad configuration)")
         self.h = h
         self.dim, self.form, self.choice, self.tol_pow, self.nlevels = dim, form, choice, tol_pow, nlevels
-        # the Helmholtz kernel is complex: vectors are complex128 (interleaved (re, im) doubles in the C ABI)
-        self.complex = choice == KERNEL_HELMHOLTZ
+        # the Helmholtz kernels are complex: vectors are complex128 (interleaved (re, im) doubles in the C ABI)
+        self.complex = choice in (KERNEL_HELMHOLTZ, KERNEL_HANKEL)
 
     @classmethod
     def open(cls, path, device=0):
@@ -186,7 +186,7 @@ class H2Operator:
         self._ck(lib().h2w_get_config(self.h, ctypes.byref(cfg)))
         self.dim, self.form, self.choice, self.tol_pow, self.nlevels = (cfg.dim, cfg.form, cfg.choice, cfg.tol_pow,
                                                                         cfg.nlevels)
-        self.complex = cfg.choice == KERNEL_HELMHOLTZ
+        self.complex = cfg.choice in (KERNEL_HELMHOLTZ, KERNEL_HANKEL)
         return self
 
     def save(self, path):

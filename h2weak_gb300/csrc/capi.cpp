@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include "bessel.cuh"
 #include "h2w_internal.h"
 #include "kernels.cuh"
 
@@ -331,10 +332,37 @@ void setup_kernel(h2w_handle *h) {
         }
         h->kii = res;
         h->diag = (1.0 + res) / hd;
-    } else if (h->cfg.choice == H2W_KERNEL_HELMHOLTZ) {
+    } else if (h->cfg.choice == H2W_KERNEL_HELMHOLTZ && dim == 3) {
         // Helmholtz3D diagonal, 3D/codes/kernel.hpp:140-141
         h->diag = 500 * std::sqrt(double(dn));
         h->diag_im = 0.0;
+    } else if (h->cfg.choice == H2W_KERNEL_HANKEL) {
+        // IE_2D_Helm diagonal (1 + 15 ln N + Kii) / h^2 (2D/codes/kernel.hpp:128-132); Kii the
+        // 16 x 16 Gauss-Legendre integral of i H0^(1)(R) / 4 over [0, h/2]^2, times 4
+        // (the userkernel constructor, 2D/codes/kernel.hpp:101-114; double_integral,
+        // 2D/codes/integral2d.hpp:59-90)
+        const double hh = 1.0 / std::sqrt(double(kn));
+        std::vector<double> x, w;
+        gl16(x, w);
+        const double lo = 0.0, hi = hh * 0.5, cx = 0.5 * (hi - lo), Lx = 0.5 * (hi + lo);
+        std::complex<double> res = 0.0;
+        for (int i = 0; i < 16; ++i) {
+            const double tx = cx * x[i] + Lx;
+            for (int j = 0; j < 16; ++j) {
+                const double ty = cx * x[j] + Lx;
+                double j0, y0;
+                bessel::j0y0(std::sqrt(tx * tx + ty * ty), j0, y0);
+                const std::complex<double> f(-y0 / 4.0, j0 / 4.0);
+                res += w[i] * w[j] * f;
+            }
+        }
+        res *= (cx * cx);
+        res *= 4;
+        const double h2 = std::pow(hh, 2.0);
+        const std::complex<double> d = (1.0 + 15 * std::log(double(dn)) + res) / h2;
+        h->kii = res.real();
+        h->diag = d.real();
+        h->diag_im = d.imag();
     } else {
         h->diag = dim == 2 ? 1.0 : std::sqrt((double)dn);
     }
@@ -3735,8 +3763,9 @@ int h2w_create(const h2w_config *cfg, h2w_handle **out) {
     if (!cfg || !out) return H2W_ERR_ARG;
     *out = nullptr;
     if (cfg->dim < 1 || cfg->dim > 3 || (cfg->form != 0 && cfg->form != 1 && cfg->form != 2) || (cfg->form == 2 && cfg->dim == 1) ||
-        (cfg->choice != 0 && cfg->choice != 1 && cfg->choice != H2W_KERNEL_HELMHOLTZ) ||
-        (cfg->choice == H2W_KERNEL_HELMHOLTZ && (cfg->dim != 3 || cfg->form == 2)) || cfg->nlevels < 1 ||
+        (cfg->choice != 0 && cfg->choice != 1 && cfg->choice != H2W_KERNEL_HELMHOLTZ && cfg->choice != H2W_KERNEL_HANKEL) ||
+        (cfg->choice == H2W_KERNEL_HELMHOLTZ && (cfg->dim != 3 || cfg->form == 2)) ||
+        (cfg->choice == H2W_KERNEL_HANKEL && (cfg->dim != 2 || cfg->form == 2)) || cfg->nlevels < 1 ||
         cfg->tol_pow < 0 || cfg->rank_cap < 0)
         return H2W_ERR_ARG;
     h2w_handle *h = nullptr;
@@ -3746,7 +3775,7 @@ int h2w_create(const h2w_config *cfg, h2w_handle **out) {
         if (cfg->device >= ndev) return H2W_ERR_ARG;
         h = new h2w_handle;
         h->cfg = *cfg;
-        h->cplx = cfg->choice == H2W_KERNEL_HELMHOLTZ;
+        h->cplx = cfg->choice == H2W_KERNEL_HELMHOLTZ || cfg->choice == H2W_KERNEL_HANKEL;
         if (cudaSetDevice(cfg->device) != cudaSuccess ||
             cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
             delete h;
@@ -3756,7 +3785,7 @@ int h2w_create(const h2w_config *cfg, h2w_handle **out) {
         // host-only handle: points, tree and lists, no device work
         h = new h2w_handle;
         h->cfg = *cfg;
-        h->cplx = cfg->choice == H2W_KERNEL_HELMHOLTZ;
+        h->cplx = cfg->choice == H2W_KERNEL_HELMHOLTZ || cfg->choice == H2W_KERNEL_HANKEL;
     }
     *out = h;
     return H2W_OK;

@@ -1,8 +1,11 @@
 // Complex Helmholtz kernels of the GB300 H2* library (sm_103a): the
-// reference's USE_Helm build (3D/codes/kernel.hpp:132-144,195-208, complex
-// scalars throughout, 3D/codes/headers.hpp:35-40).
+// reference's USE_Helm build in 3D (3D/codes/kernel.hpp:132-144,195-208) and
+// USE_Hankel build in 2D (2D/codes/kernel.hpp:126-144,321-333,
+// 2D/codes/integral2d.hpp:16-57), complex scalars throughout
+// (3D/codes/headers.hpp:35-40, 2D/codes/headers.hpp:34-40).
 //
-//  * kentry_c          entries exp(iR)/(4 pi) off the diagonal, 500 sqrt(N) on it
+//  * kentry_c          3D: exp(iR)/(4 pi) off the diagonal, 500 sqrt(N) on it;
+//                      2D: i H0^(1)(R) / 4 with J0, Y0 of bessel.cuh
 //  * nca_c_kernel      the NCA/ACA pivot search in complex arithmetic, one CTA
 //                      per block (3D/codes/aca.hpp:180-275)
 //  * factor_c / xfer_c / fill_c   operator formation into a complex image
@@ -22,6 +25,7 @@
 #include <cfloat>
 #include <climits>
 
+#include "bessel.cuh"
 #include "kernels.cuh"
 
 namespace h2w {
@@ -61,8 +65,19 @@ __device__ __forceinline__ double2 c_cmul(double2 a, double2 b) {
 // --------------------------------------------------------------- entries ---
 // Helmholtz3D (3D/codes/kernel.hpp:133-144): R2 = (dx^2 + dy^2) + dz^2,
 // exp(i R) = (cos R, sin R), each part divided by 4 pi; diagonal 500 sqrt(N).
+// Helmholtz2D (2D/codes/kernel.hpp:126-144): R2 = dx^2 + dy^2,
+// i (J0(R) + i Y0(R)) / 4 = (-Y0(R) / 4, J0(R) / 4); diagonal
+// (1 + 15 ln N + Kii) / h^2 with the complex self term Kii.
 __device__ __forceinline__ double2 kentry_c(const KParams &k, int i, int j) {
     if (i == j) return make_double2(k.diag, k.diag_im);
+    if (k.dim == 2) {
+        const double *a = k.pts + (size_t)i * 2, *b = k.pts + (size_t)j * 2;
+        const double dx = __dsub_rn(a[0], b[0]), dy = __dsub_rn(a[1], b[1]);
+        const double R = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+        double j0, y0;
+        bessel::j0y0(R, j0, y0);
+        return make_double2(__ddiv_rn(-y0, 4.0), __ddiv_rn(j0, 4.0));
+    }
     const double *a = k.pts + (size_t)i * 3, *b = k.pts + (size_t)j * 3;
     const double dx = __dsub_rn(a[0], b[0]), dy = __dsub_rn(a[1], b[1]), dz = __dsub_rn(a[2], b[2]);
     const double R2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));

@@ -34,16 +34,20 @@ enum {
  * every interaction-list pair compressed on its own, 2D and 3D only,
  * 2D/codes/matvec.hpp:136-172, 3D/codes/matvec.hpp:138-180) */
 enum { H2W_FORM_NESTED = 0, H2W_FORM_SEMINESTED = 1, H2W_FORM_NONNESTED = 2 };
-/* reference "choice". H2W_KERNEL_HELMHOLTZ (3D, nested or semi-nested forms):
- * the complex kernel of the reference's USE_Helm build, exp(iR)/(4 pi) off the
- * diagonal and 500 sqrt(N) on it (3D/codes/kernel.hpp:132-144,195-208, complex
- * scalars throughout, 3D/codes/headers.hpp:35-40). A handle with this kernel
- * takes and returns complex vectors as N interleaved (re, im) pairs of doubles
- * (the layout of std::complex<double>) in h2w_matvec (FP64, one right-hand
- * side), h2w_gmres and h2w_dense_matvec; the mixed-precision, batched,
- * learned, far-field-on-the-fly and allocation-free entry points refuse it
- * with H2W_ERR_ARG. */
-enum { H2W_KERNEL_IE = 0, H2W_KERNEL_RBF = 1, H2W_KERNEL_HELMHOLTZ = 2 };
+/* reference "choice". The complex kernels (nested or semi-nested forms):
+ *  H2W_KERNEL_HELMHOLTZ (3D): the reference's USE_Helm build, exp(iR)/(4 pi)
+ *    off the diagonal and 500 sqrt(N) on it (3D/codes/kernel.hpp:132-144,195-208);
+ *  H2W_KERNEL_HANKEL (2D): the reference's USE_Hankel build, i H0^(1)(R) / 4
+ *    = (-Y0(R) + i J0(R)) / 4 off the diagonal and (1 + 15 ln N + Kii) / h^2 on
+ *    it (2D/codes/kernel.hpp:126-144,321-333, 2D/codes/integral2d.hpp:16-90),
+ *    with the library's own J0 and Y0 where the reference calls Boost;
+ * complex scalars throughout (3D/codes/headers.hpp:35-40, 2D/codes/headers.hpp:34-40).
+ * A handle with a complex kernel takes and returns complex vectors as N
+ * interleaved (re, im) pairs of doubles (the layout of std::complex<double>)
+ * in h2w_matvec (FP64, one right-hand side), h2w_gmres and h2w_dense_matvec;
+ * the mixed-precision, batched, learned, far-field-on-the-fly and
+ * allocation-free entry points refuse it with H2W_ERR_ARG. */
+enum { H2W_KERNEL_IE = 0, H2W_KERNEL_RBF = 1, H2W_KERNEL_HELMHOLTZ = 2, H2W_KERNEL_HANKEL = 10 };
 enum { H2W_ASSEMBLE_NCA = 0, H2W_ASSEMBLE_IMPORT = 1, H2W_ASSEMBLE_LEARNED = 2 };
 /* FP64: FP64 operator and arithmetic. FP32: FP32 operator copy and arithmetic.
  * DF64 (multi-vector products only: h2w_matvec with nrhs > 1 and the batched
@@ -68,7 +72,7 @@ enum {
 typedef struct h2w_config {
     int dim;          /* 1, 2 or 3 */
     int form;         /* H2W_FORM_* */
-    int choice;       /* H2W_KERNEL_*: kernel.hpp getMatrixEntry choice 0 / 1 / 2 */
+    int choice;       /* H2W_KERNEL_*: kernel.hpp getMatrixEntry choice 0 / 1 / 2 / 10 */
     int tol_pow;      /* NCA/ACA tolerance 10^-tol_pow (aca.hpp LowRank) */
     int nlevels;      /* tree depth (main.cpp computes it from N and nmax) */
     int rank_cap;     /* max NCA rank per block; 0 = min(rows, cols) */

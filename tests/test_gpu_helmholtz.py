@@ -80,3 +80,54 @@ def test_helmholtz_refuses_real_only_entry_points(gpu):
     with pytest.raises(hw.H2WError) as e:
         op.autotune(nrhs=64)
     assert e.value.code == hw.ERR_ARG
+
+
+# ------------------------------------------------------------- 2D Hankel ---
+def hankel_op(hw, n, nlev, tol, form=0, seed=11):
+    op = hw.H2Operator(2, form, hw.KERNEL_HANKEL, tol, nlev, device=0)
+    op.set_points(synth.uniform_points(synth.config_seed(97, seed), n, 2))
+    op.build_tree()
+    op.assemble(hw.ASSEMBLE_NCA)
+    return op
+
+
+@pytest.mark.gpu
+def test_hankel_entries_match_independent_values(gpu):
+    """Column 0 of the 2D Hankel kernel matrix from the GPU's entries (dense
+    product with e_0) against (-Y0 + i J0) / 4 from scipy, and the diagonal
+    (1 + 15 ln N + Kii) / h^2 with Kii integrated from scipy's Bessel values
+    (tests/golden/make_bessel.py)."""
+    import os
+    hw = gpu
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bessel_j0y0.npz"))
+    pts = g["hankel_points"]
+    n = len(pts)
+    op = hw.H2Operator(2, 0, hw.KERNEL_HANKEL, 8, 2, device=0)
+    op.set_points(pts)
+    op.build_tree()
+    e0 = np.zeros(n, dtype=np.complex128)
+    e0[0] = 1.0
+    col = op.dense_matvec(e0)
+    ref = g["hankel_col0"]
+    assert np.max(np.abs(col - ref) / np.abs(ref)) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1])
+def test_hankel_product_and_gmres(gpu, form):
+    """2D Hankel on 16 384 random points, 3 levels, tol 1e-8: the compressed
+    product against exact dense rows, complex linearity, and GMRES to 1e-10."""
+    hw = gpu
+    n = 16384
+    op = hankel_op(hw, n, 3, 8, form)
+    x = cvec(4, n)
+    y = op.matvec(x)
+    rows = np.arange(0, n, 257)[:64]
+    yd = np.concatenate([op.dense_matvec(x, row0=int(r), nrows=1) for r in rows])
+    assert relerr(y[rows], yd) < 1e-7
+    x2 = cvec(5, n)
+    a = -0.8 + 0.6j
+    assert relerr(op.matvec(a * x + x2), a * y + op.matvec(x2)) < 1e-13
+    xs, it, res = op.gmres(y, max_iter=300, tol_pow=10)
+    assert res < 1e-10 and it >= 1
+    assert relerr(op.matvec(xs), y) < 1e-8
