@@ -35,6 +35,7 @@ OPT_PRODUCER_WARP = 9
 OPT_SPIN_LIMIT = 10
 OPT_FAR_ON_THE_FLY = 11
 OPT_NCA_DF = 12
+OPT_COMPLEX_ARNOLDI = 13
 TUNE_IR_MIX = 16
 LISTS = {"charge": 0, "nbr": 1, "il": 2, "isvertex": 3, "far_check": 4, "far_charge": 5,
          "ver_check": 6, "ver_charge": 7, "sn_row": 8, "sn_col": 9}

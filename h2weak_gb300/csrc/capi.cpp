@@ -115,6 +115,7 @@ struct h2w_handle {
     // stored realified (every complex block as [[Re, -Im], [Im, Re]] with rows and
     // columns interleaved), vectors as interleaved (re, im) doubles
     bool cplx = false;
+    bool cgm_hermitian = false;  // H2W_OPT_COMPLEX_ARNOLDI
     double diag_im = 0;
     DBuf<double2> c_V, c_w, c_r, c_ax, c_part, c_h, c_y;  // complex GMRES state
     int64_t nv() const { return cplx ? 2 * tree.N : tree.N; }  // doubles per vector
@@ -3539,15 +3540,17 @@ void require_real(const h2w_handle *h, const char *what) {
     if (h->cplx) throw ApiError(H2W_ERR_ARG, std::string(what) + " is not available for the complex Helmholtz kernel");
 }
 
-// The reference GMRES (3D/codes/gmres.hpp:92-200, USE_Helm) on the complex
-// operator: restart = max_iter, x0 from x, H(k,i) = w.dot(v_k) with Eigen's
-// conjugate-first dot (sum conj(w) v_k), modified Gram-Schmidt in the
-// reference's order, the reference's complex Givens formulas
+// The reference GMRES (3D/codes/gmres.hpp:92-200, USE_Helm / USE_Hankel) on
+// the complex operator: restart = max_iter, x0 from x, H(k,i) = w.dot(v_k)
+// with Eigen's conjugate-first dot (sum conj(w) v_k), modified Gram-Schmidt
+// in the reference's order, the reference's complex Givens formulas
 // (GeneratePlaneRotation, gmres.hpp:52-68; ApplyPlaneRotation, :70-75) and
 // back substitution on the host in std::complex arithmetic, stop when
-// |s(i+1)| / ||b|| < tol. Krylov vectors, products and Gram-Schmidt on the
-// GPU; the Hessenberg column comes to the host once per step. b, x: leaf
-// order, interleaved (re, im), device.
+// |s(i+1)| / ||b|| < tol. With H2W_OPT_COMPLEX_ARNOLDI the projections are
+// Hermitian (sum conj(v_k) w) and the rotations unitary (dy' = -conj(sn) dx
+// + cs dy). Krylov vectors, products and Gram-Schmidt on the GPU; the
+// Hessenberg column comes to the host once per step. b, x: leaf order,
+// interleaved (re, im), device.
 int cgmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double tol, int *iters, double *resid) {
     typedef std::complex<double> cd;
     cudaStream_t st = h->stream;
@@ -3592,9 +3595,10 @@ int cgmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double
             sn = alpha * std::conj(dyv) / nrm;
         }
     };
-    auto app_rot = [](cd &dxv, cd &dyv, cd &cs, cd &sn) {
+    const bool herm = h->cgm_hermitian;
+    auto app_rot = [herm](cd &dxv, cd &dyv, cd &cs, cd &sn) {
         cd temp = cs * dxv + sn * dyv;
-        dyv = -sn * dxv + cs * dyv;
+        dyv = (herm ? -std::conj(sn) : -sn) * dxv + cs * dyv;
         dxv = temp;
     };
     std::vector<cd> H((size_t)(m + 1) * m, cd(0)), s((size_t)m + 1), cs((size_t)m + 1), sn((size_t)m + 1);
@@ -3631,7 +3635,8 @@ int cgmres_run(h2w_handle *h, const double *db, double *dx, int max_iter, double
             A(vi, h->c_w.p);
             for (int k = 0; k <= i; k++) {
                 double2 *hk = h->c_h.p + k;
-                dot(h->c_w.p, h->c_V.p + (size_t)k * n, hk);
+                if (herm) dot(h->c_V.p + (size_t)k * n, h->c_w.p, hk);
+                else dot(h->c_w.p, h->c_V.p + (size_t)k * n, hk);
                 CK(cgm_axpy_launch(h->c_w.p, h->c_V.p + (size_t)k * n, hk, n, st));
             }
             const double hn = norm(h->c_w.p);
@@ -4517,6 +4522,8 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
             h->spin_limit = value;
         } else if (option == H2W_OPT_NCA_DF) {
             h->nca_df = value != 0;
+        } else if (option == H2W_OPT_COMPLEX_ARNOLDI) {
+            h->cgm_hermitian = value != 0;
         } else if (option == H2W_OPT_FAR_ON_THE_FLY) {
             h->far_fly = value != 0;  // takes effect at the next h2w_assemble
         } else if (option == H2W_OPT_COOP) {
@@ -4549,6 +4556,7 @@ int h2w_get_option(h2w_handle *h, int option, int64_t *value) {
         else if (option == H2W_OPT_SPIN_LIMIT) *value = h->spin_limit;
         else if (option == H2W_OPT_FAR_ON_THE_FLY) *value = h->far_fly ? 1 : 0;
         else if (option == H2W_OPT_NCA_DF) *value = h->nca_df ? 1 : 0;
+        else if (option == H2W_OPT_COMPLEX_ARNOLDI) *value = h->cgm_hermitian ? 1 : 0;
         else throw ApiError(H2W_ERR_ARG, "unknown option");
         return H2W_OK;
     });

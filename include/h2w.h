@@ -284,10 +284,22 @@ int h2w_gmres_ir_batch(h2w_handle *h, const double *b, double *x, int nrhs, int 
  *                 dots, which are summed inside the next pivot's residual
  *                 passes; every block of 2048 or more rows + columns is
  *                 searched on groups then. 0: FP64. The other kernels always
- *                 search in FP64 (their pivots are bitwise the reference's). */
+ *                 search in FP64 (their pivots are bitwise the reference's).
+ *  H2W_OPT_COMPLEX_ARNOLDI  complex kernels only. 0 (default): h2w_gmres is
+ *                 the reference's GMRES as written (3D/codes/gmres.hpp:52-68,
+ *                 :92-200): its Gram-Schmidt coefficients are Eigen's
+ *                 w.dot(v_k) = sum conj(w) v_k, the conjugates of the
+ *                 projections, and its rotations apply -sn dx where a unitary
+ *                 rotation has -conj(sn) dx, so for complex operators the
+ *                 Krylov vectors are not orthogonal and |s(i+1)| / ||b|| is
+ *                 not the true residual (iteration counts and results match
+ *                 the reference's). 1: Hermitian projections sum conj(v_k) w
+ *                 and unitary rotations: GMRES proper, whose stopping test
+ *                 bounds the true residual. */
 enum { H2W_OPT_GRAPH = 0, H2W_OPT_COOP = 1, H2W_OPT_IR_RESIDUAL = 2, H2W_OPT_MULTI_XW = 3, H2W_OPT_ROW_SPLIT = 4,
        H2W_OPT_IR_UPDATE = 5, H2W_OPT_TENSOR = 6, H2W_OPT_F32_BASIS = 7, H2W_OPT_DATAFLOW = 8,
-       H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10, H2W_OPT_FAR_ON_THE_FLY = 11, H2W_OPT_NCA_DF = 12 };
+       H2W_OPT_PRODUCER_WARP = 9, H2W_OPT_SPIN_LIMIT = 10, H2W_OPT_FAR_ON_THE_FLY = 11, H2W_OPT_NCA_DF = 12,
+       H2W_OPT_COMPLEX_ARNOLDI = 13 };
 int h2w_set_option(h2w_handle *h, int option, int64_t value);
 int h2w_get_option(h2w_handle *h, int option, int64_t *value);
 

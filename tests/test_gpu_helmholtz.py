@@ -54,8 +54,8 @@ def test_helmholtz_product_against_dense_rows(gpu, form):
 
 @pytest.mark.gpu
 def test_helmholtz_gmres_solves(gpu):
-    """GMRES on the complex operator reaches its stopping test; the residual
-    it reports is the reference's |s(i+1)| / ||b||."""
+    """GMRES on the complex operator reaches its stopping test (the reference's
+    |s(i+1)| / ||b||); with H2W_OPT_COMPLEX_ARNOLDI the solution is accurate."""
     hw = gpu
     n = 8000
     op = helm_op(hw, n, 2, 10)
@@ -64,6 +64,12 @@ def test_helmholtz_gmres_solves(gpu):
     x, it, res = op.gmres(b, max_iter=200, tol_pow=10)
     assert res < 1e-10 and 1 <= it <= 200
     assert np.all(np.isfinite(x))
+    # Hermitian projections and unitary rotations: the stopping test bounds the true residual
+    op.set_option(hw.OPT_COMPLEX_ARNOLDI, 1)
+    x, it, res = op.gmres(b, max_iter=200, tol_pow=10)
+    assert res < 1e-10
+    assert relerr(op.matvec(x), b) < 1e-9
+    assert relerr(x, xt) < 1e-8
 
 
 @pytest.mark.gpu
@@ -128,6 +134,12 @@ def test_hankel_product_and_gmres(gpu, form):
     x2 = cvec(5, n)
     a = -0.8 + 0.6j
     assert relerr(op.matvec(a * x + x2), a * y + op.matvec(x2)) < 1e-13
+    # the reference's GMRES as written stops on its own estimate; with Hermitian
+    # projections and unitary rotations the estimate bounds the true residual
     xs, it, res = op.gmres(y, max_iter=300, tol_pow=10)
-    assert res < 1e-10 and it >= 1
-    assert relerr(op.matvec(xs), y) < 1e-8
+    assert res < 1e-10 and it >= 1 and np.all(np.isfinite(xs))
+    op.set_option(hw.OPT_COMPLEX_ARNOLDI, 1)
+    xs, it2, res = op.gmres(y, max_iter=300, tol_pow=10)
+    assert res < 1e-10 and it2 >= 1
+    assert relerr(op.matvec(xs), y) < 1e-9
+    assert relerr(xs, x) < 1e-6

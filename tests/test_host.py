@@ -125,3 +125,18 @@ def test_nonnested_form_is_2d_3d_only():
     op = hw.H2Operator(3, hw.FORM_NONNESTED, 0, 8, 2, device=-1)
     op.gen_grid(8)
     op.build_tree()
+
+
+def test_complex_kernel_configurations():
+    """The complex kernels exist where the reference builds them: Helmholtz
+    (choice 2) in 3D, Hankel (choice 10) in 2D, nested and semi-nested forms;
+    other combinations are refused at creation."""
+    for dim, form, choice in ((3, 0, 2), (3, 1, 2), (2, 0, 10), (2, 1, 10)):
+        op = hw.H2Operator(dim, form, choice, 8, 2, device=-1)
+        assert op.complex
+        assert op.get_option(hw.OPT_COMPLEX_ARNOLDI) == 0
+        op.set_option(hw.OPT_COMPLEX_ARNOLDI, 1)
+        assert op.get_option(hw.OPT_COMPLEX_ARNOLDI) == 1
+    for dim, form, choice in ((2, 0, 2), (1, 0, 2), (3, 0, 10), (3, 2, 2), (2, 2, 10), (2, 0, 3)):
+        with pytest.raises(hw.H2WError):
+            hw.H2Operator(dim, form, choice, 8, 2, device=-1)
