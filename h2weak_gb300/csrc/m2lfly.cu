@@ -167,12 +167,20 @@ __global__ void __launch_bounds__(FLY_THREADS)
 // entry is then one function of R^2 times a constant: log2(R^2) (3D RBF,
 // 2D IE) or 1/sqrt(R^2) (3D IE, 2D RBF); the constant multiplies the row's
 // sum once. Eight threads share a row pair (rows r and r + 16 of the item),
-// each over every eighth staged column: one shared-memory load feeds two
-// entries, and the two rows' sums are independent chains.
+// each over every eighth staged column, and the pair is computed with
+// Blackwell's paired FP32 instructions (__fadd2_rn / __fmul2_rn / __ffma2_rn:
+// one instruction for both rows): a column is staged negated and duplicated,
+// ((-x, -x), (-y, -y), (-z, -z), (v, v)), so the differences, R^2 and the
+// accumulation of the two rows are 3 + 3 + 1 paired instructions; the
+// function itself is one MUFU instruction per entry without the subnormal
+// fix-up (R^2 of a far pair is never subnormal). The same operations in the
+// same order as one row at a time, so the sums are unchanged bit for bit.
 template <int DIM, int CH>
 __device__ __forceinline__ float fly_g32(float R2) {
-    if ((DIM == 3 && CH == 1) || (DIM == 2 && CH == 0)) return __log2f(R2);
-    return rsqrtf(R2);
+    float y;
+    if ((DIM == 3 && CH == 1) || (DIM == 2 && CH == 0)) asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(R2));
+    else asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(R2));
+    return y;
 }
 
 template <int DIM, int CH>
@@ -182,7 +190,8 @@ __global__ void __launch_bounds__(FLY_THREADS)
                          const int32_t *__restrict__ cws, const float *__restrict__ pts4, float *ws, float scale) {
     constexpr int TPR = 8, HALF = FLY_ROWS / 2;
     static_assert(HALF * TPR == FLY_THREADS, "two rows per thread");
-    __shared__ __align__(16) float4 sc[FLY_TILE];
+    // column c: sc[2c] = (-x, -x, -y, -y), sc[2c + 1] = (-z, -z, v, v)
+    __shared__ __align__(16) float4 sc[2 * FLY_TILE];
     __shared__ long long s_it;
     for (;;) {
         __syncthreads();
@@ -193,37 +202,41 @@ __global__ void __launch_bounds__(FLY_THREADS)
         const FlyItem m = items[it];
         const int row = threadIdx.x / TPR, sub = threadIdx.x - row * TPR;
         const bool h0 = row < m.nrows, h1 = row + HALF < m.nrows;
-        float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+        float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (h0) a0 = reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + row]];
-        if (h1) a1 = reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + row + HALF]];
-        float acc0 = 0.f, acc1 = 0.f;
+        // a row past the item's last repeats the first row's point: its sum is dropped
+        const float4 a1 = h1 ? reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + row + HALF]] : a0;
+        const float2 ax = make_float2(a0.x, a1.x), ay = make_float2(a0.y, a1.y), az = make_float2(a0.z, a1.z);
+        float2 acc = make_float2(0.f, 0.f);
         for (int c0 = 0; c0 < m.ncols; c0 += FLY_TILE) {
             const int nc = m.ncols - c0 < FLY_TILE ? m.ncols - c0 : FLY_TILE;
             __syncthreads();
             for (int c = threadIdx.x; c < nc; c += FLY_THREADS) {
                 const int64_t e = m.cbeg + c0 + c;
-                float4 q = reinterpret_cast<const float4 *>(pts4)[cpid[e]];
-                q.w = ws[cws[e]];
-                sc[c] = q;
+                const float4 q = reinterpret_cast<const float4 *>(pts4)[cpid[e]];
+                const float v = ws[cws[e]];
+                sc[2 * c] = make_float4(-q.x, -q.x, -q.y, -q.y);
+                sc[2 * c + 1] = make_float4(-q.z, -q.z, v, v);
             }
             __syncthreads();
             if (h0) {
 #pragma unroll 4
                 for (int c = sub; c < nc; c += TPR) {
-                    const float4 q = sc[c];
-                    const float x0 = a0.x - q.x, y0 = a0.y - q.y, x1 = a1.x - q.x, y1 = a1.y - q.y;
-                    float r0 = fmaf(y0, y0, x0 * x0), r1 = fmaf(y1, y1, x1 * x1);
+                    const float4 p = sc[2 * c], p2 = sc[2 * c + 1];
+                    const float2 dx = __fadd2_rn(ax, make_float2(p.x, p.y));
+                    const float2 dy = __fadd2_rn(ay, make_float2(p.z, p.w));
+                    float2 r = __fmul2_rn(dx, dx);
+                    r = __ffma2_rn(dy, dy, r);
                     if (DIM == 3) {
-                        const float z0 = a0.z - q.z, z1 = a1.z - q.z;
-                        r0 = fmaf(z0, z0, r0);
-                        r1 = fmaf(z1, z1, r1);
+                        const float2 dz = __fadd2_rn(az, make_float2(p2.x, p2.y));
+                        r = __ffma2_rn(dz, dz, r);
                     }
-                    acc0 = fmaf(fly_g32<DIM, CH>(r0), q.w, acc0);
-                    // a row past the item's last reads distance 0 to nothing useful: its sum is dropped
-                    acc1 = fmaf(fly_g32<DIM, CH>(h1 ? r1 : 1.f), q.w, acc1);
+                    const float2 g = make_float2(fly_g32<DIM, CH>(r.x), fly_g32<DIM, CH>(r.y));
+                    acc = __ffma2_rn(g, make_float2(p2.z, p2.w), acc);
                 }
             }
         }
+        float acc0 = acc.x, acc1 = acc.y;
 #pragma unroll
         for (int o = 1; o < TPR; o <<= 1) {
             acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
