@@ -166,15 +166,15 @@ __global__ void __launch_bounds__(FLY_THREADS)
 // boxes are not adjacent, so its points are at least a box width apart). The
 // entry is then one function of R^2 times a constant: log2(R^2) (3D RBF,
 // 2D IE) or 1/sqrt(R^2) (3D IE, 2D RBF); the constant multiplies the row's
-// sum once. Eight threads share a row pair (rows r and r + 16 of the item),
-// each over every eighth staged column, and the pair is computed with
-// Blackwell's paired FP32 instructions (__fadd2_rn / __fmul2_rn / __ffma2_rn:
-// one instruction for both rows): a column is staged negated and duplicated,
-// ((-x, -x), (-y, -y), (-z, -z), (v, v)), so the differences, R^2 and the
-// accumulation of the two rows are 3 + 3 + 1 paired instructions; the
-// function itself is one MUFU instruction per entry without the subnormal
-// fix-up (R^2 of a far pair is never subnormal). The same operations in the
-// same order as one row at a time, so the sums are unchanged bit for bit.
+// sum once. Sixteen threads share four rows of the item (rows g, g + 8,
+// g + 16, g + 24), each over every sixteenth staged column: one shared-memory
+// load feeds four entries, whose sums are independent chains, and the
+// function is one MUFU instruction without the subnormal fix-up (R^2 of a
+// far pair is never subnormal). Measured on the 2^17-point 3D RBF operator:
+// 1.57 -> 1.20 ms per launch against two rows per thread with the library
+// log2 (profiles/m2l_fly32_sep_3d_rbf_131072.md). (Paired FP32 instructions,
+// __ffma2_rn and kin, on the two rows of a thread measured 3.46 ms: issue
+// fell to 28 %.)
 template <int DIM, int CH>
 __device__ __forceinline__ float fly_g32(float R2) {
     float y;
@@ -188,10 +188,9 @@ __global__ void __launch_bounds__(FLY_THREADS)
     m2l_fly32_sep_kernel(const FlyItem *__restrict__ items, int64_t nitems, unsigned long long *ctr,
                          const int32_t *__restrict__ rowpid, const int32_t *__restrict__ cpid,
                          const int32_t *__restrict__ cws, const float *__restrict__ pts4, float *ws, float scale) {
-    constexpr int TPR = 8, HALF = FLY_ROWS / 2;
-    static_assert(HALF * TPR == FLY_THREADS, "two rows per thread");
-    // column c: sc[2c] = (-x, -x, -y, -y), sc[2c + 1] = (-z, -z, v, v)
-    __shared__ __align__(16) float4 sc[2 * FLY_TILE];
+    constexpr int RPT = 4, TPR = 16, GROUPS = FLY_ROWS / RPT;  // rows per thread, threads per row group
+    static_assert(GROUPS * TPR == FLY_THREADS, "four rows per thread");
+    __shared__ __align__(16) float4 sc[FLY_TILE];
     __shared__ long long s_it;
     for (;;) {
         __syncthreads();
@@ -200,51 +199,56 @@ __global__ void __launch_bounds__(FLY_THREADS)
         const long long it = s_it;
         if (it >= nitems) return;
         const FlyItem m = items[it];
-        const int row = threadIdx.x / TPR, sub = threadIdx.x - row * TPR;
-        const bool h0 = row < m.nrows, h1 = row + HALF < m.nrows;
-        float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (h0) a0 = reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + row]];
-        // a row past the item's last repeats the first row's point: its sum is dropped
-        const float4 a1 = h1 ? reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + row + HALF]] : a0;
-        const float2 ax = make_float2(a0.x, a1.x), ay = make_float2(a0.y, a1.y), az = make_float2(a0.z, a1.z);
-        float2 acc = make_float2(0.f, 0.f);
+        const int grp = threadIdx.x / TPR, sub = threadIdx.x - grp * TPR;
+        const bool any = grp < m.nrows;
+        float ax[RPT], ay[RPT], az[RPT], acc[RPT];
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            const int r = grp + k * GROUPS;
+            // rows past the item's last repeat its first row's point: their sums are dropped
+            const int rr = r < m.nrows ? r : grp;
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (any) a = reinterpret_cast<const float4 *>(pts4)[rowpid[m.rows + rr]];
+            ax[k] = a.x;
+            ay[k] = a.y;
+            az[k] = a.z;
+            acc[k] = 0.f;
+        }
         for (int c0 = 0; c0 < m.ncols; c0 += FLY_TILE) {
             const int nc = m.ncols - c0 < FLY_TILE ? m.ncols - c0 : FLY_TILE;
             __syncthreads();
             for (int c = threadIdx.x; c < nc; c += FLY_THREADS) {
                 const int64_t e = m.cbeg + c0 + c;
-                const float4 q = reinterpret_cast<const float4 *>(pts4)[cpid[e]];
-                const float v = ws[cws[e]];
-                sc[2 * c] = make_float4(-q.x, -q.x, -q.y, -q.y);
-                sc[2 * c + 1] = make_float4(-q.z, -q.z, v, v);
+                float4 q = reinterpret_cast<const float4 *>(pts4)[cpid[e]];
+                q.w = ws[cws[e]];
+                sc[c] = q;
             }
             __syncthreads();
-            if (h0) {
-#pragma unroll 4
+            if (any) {
+#pragma unroll 2
                 for (int c = sub; c < nc; c += TPR) {
-                    const float4 p = sc[2 * c], p2 = sc[2 * c + 1];
-                    const float2 dx = __fadd2_rn(ax, make_float2(p.x, p.y));
-                    const float2 dy = __fadd2_rn(ay, make_float2(p.z, p.w));
-                    float2 r = __fmul2_rn(dx, dx);
-                    r = __ffma2_rn(dy, dy, r);
-                    if (DIM == 3) {
-                        const float2 dz = __fadd2_rn(az, make_float2(p2.x, p2.y));
-                        r = __ffma2_rn(dz, dz, r);
+                    const float4 q = sc[c];
+#pragma unroll
+                    for (int k = 0; k < RPT; ++k) {
+                        const float dx = ax[k] - q.x, dy = ay[k] - q.y;
+                        float r2 = fmaf(dy, dy, dx * dx);
+                        if (DIM == 3) {
+                            const float dz = az[k] - q.z;
+                            r2 = fmaf(dz, dz, r2);
+                        }
+                        acc[k] = fmaf(fly_g32<DIM, CH>(r2), q.w, acc[k]);
                     }
-                    const float2 g = make_float2(fly_g32<DIM, CH>(r.x), fly_g32<DIM, CH>(r.y));
-                    acc = __ffma2_rn(g, make_float2(p2.z, p2.w), acc);
                 }
             }
         }
-        float acc0 = acc.x, acc1 = acc.y;
 #pragma unroll
-        for (int o = 1; o < TPR; o <<= 1) {
-            acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
-            acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
-        }
+        for (int k = 0; k < RPT; ++k)
+#pragma unroll
+            for (int o = 1; o < TPR; o <<= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
         if (sub == 0) {
-            if (h0) ws[m.dst + row] = acc0 * scale;
-            if (h1) ws[m.dst + row + HALF] = acc1 * scale;
+#pragma unroll
+            for (int k = 0; k < RPT; ++k)
+                if (grp + k * GROUPS < m.nrows) ws[m.dst + grp + k * GROUPS] = acc[k] * scale;
         }
     }
 }
