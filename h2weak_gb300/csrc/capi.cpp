@@ -2513,24 +2513,10 @@ void run_matvec_f64(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws.p, 0, (size_t)h->ws_n * 8, st));
     if (h->fly_active) {
-        // stored passes up to the upward ones, the far M2L kernel, the rest. The
-        // dataflow form runs the two stored ranges as two launches over one set of
-        // producer counts (every producer precedes its consumers in the stored order,
-        // so the second launch finds the first range's releases already made); the
-        // far M2L kernel between them is ordered by the stream.
-        const bool flow = h->coop && h->dataflow;
-        if (flow) CK(cudaMemcpyAsync(h->d_sdep.p, h->d_sdep0.p, h->d_sdep0.n * 4, cudaMemcpyDeviceToDevice, st));
+        // stored passes up to the upward ones, the far M2L kernel, the rest
         auto stored = [&](int a, int b) {
             if (b <= a) return;
-            if (flow) {
-                const int64_t t0 = h->phases[(size_t)a].t0, t1 = h->phases[(size_t)b - 1].t1;
-                CK(cudaMemsetAsync(h->d_sctr.p, 0, 4, st));
-                prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
-                    return launch_brg_flow_f64(h->d_roff.p, h->d_blob.p, t0, t1, h->d_sctr.p, h->d_sdep.p,
-                                               h->d_scoff.p, h->d_scidx.p, h->d_op.p, h->d_ws.p, dx, dy, perm,
-                                               h->d_err.p, st);
-                });
-            } else if (h->coop) {
+            if (h->coop) {
                 prof_launch(h, H2W_PREC_FP64, nph, st, [&] {
                     return launch_coop_f64(h->d_roff.p, h->d_blob.p, h->d_pstart.p + a, b - a, h->d_op.p, h->d_ws.p,
                                            dx, dy, perm, h->d_bar.p, h->d_err.p, st, h->spin_limit);
@@ -2610,19 +2596,9 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
     if (h->fly_active) {
-        const bool flow = h->coop && h->dataflow;  // as in run_matvec_f64
-        if (flow) CK(cudaMemcpyAsync(h->d_sdep.p, h->d_sdep0.p, h->d_sdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         auto stored = [&](int a, int b) {
             if (b <= a) return;
-            if (flow) {
-                const int64_t t0 = h->phases[(size_t)a].t0, t1 = h->phases[(size_t)b - 1].t1;
-                CK(cudaMemsetAsync(h->d_sctr.p, 0, 4, st));
-                prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
-                    return launch_brg_flow_f32(h->d_roff.p, h->d_blob.p, t0, t1, h->d_sctr.p, h->d_sdep.p,
-                                               h->d_scoff.p, h->d_scidx.p, h->d_op32.p, h->d_ws32.p, dx, dy, perm,
-                                               h->d_err.p, st);
-                });
-            } else if (h->coop) {
+            if (h->coop) {
                 prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
                     return launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p + a, b - a, h->d_op32.p,
                                            h->d_ws32.p, dx, dy, perm, h->d_bar.p, h->d_err.p, st, h->spin_limit);
