@@ -132,6 +132,13 @@ struct h2w_handle {
     DBuf<float> d_op32m;
     DBuf<int64_t> d_blob_mw, d_mslices;
     int64_t op32m_n = 0;
+    // the same for the single-vector stream's FP32 products: each (target, panel)
+    // slice of the FP32 operator contiguous at its padded height, so that a row
+    // chunk of a block streams whole sectors (made on the first FP32 product)
+    DBuf<float> d_op32s;
+    DBuf<int64_t> d_blob_s, d_sslices;
+    int64_t op32s_n = 0;
+    bool op32s_ready = false;
     bool op32m_ready = false;
     DBuf<int32_t> d_mctr;                           // its per-phase target counters
     std::vector<Phase> mphases;
@@ -1720,6 +1727,30 @@ void realize_single(h2w_handle *h, int64_t row_split) {
     pack_records(pb, h->phases, roff, blob, pstart);
     first_writers_overwrite(roff, blob, h->ws_n, h->fly_active ? &h->fly_rows : nullptr);
     check_phase_writers(roff, blob, h->phases);
+    {
+        // FP32 records on the slice-contiguous copy: panel q of target t reads its
+        // rows from slice (a', pad4(nrows)) instead of (a, lda); slices 16-byte aligned
+        std::vector<int64_t> bs(blob), sl;
+        int64_t off = 0;
+        for (size_t t = 0; t + 1 < roff.size(); ++t) {
+            const int64_t o = roff[t];
+            const int64_t nrows = bs[(size_t)o + 1] & 0xffffffff, np = bs[(size_t)o + 2] & 0xffffffff;
+            const int64_t ld = pad4(nrows);
+            for (int64_t q = 0; q < np; ++q) {
+                const size_t wa = (size_t)(o + 3 + 3 * q), wl = wa + 1;
+                const int64_t a = bs[wa], lda = bs[wl] & 0xffffffff, w = bs[wl] >> 32;
+                sl.insert(sl.end(), {a, lda, nrows, w, off, ld});
+                bs[wa] = off;
+                bs[wl] = (int64_t)(uint32_t)ld | (w << 32);
+                off += pad4(ld * w);
+            }
+        }
+        h->d_blob_s.upload(bs, h->stream);
+        h->d_sslices.upload(sl, h->stream);
+        h->op32s_n = off;
+        h->op32s_ready = false;
+        h->d_op32s.reset();
+    }
     // the far M2L kernel runs between the upward passes (logical phases <= L)
     // and the downward ones (>= L + 1)
     h->fly_split = (int)h->phases.size();
@@ -2588,10 +2619,21 @@ void ensure_f32m(h2w_handle *h) {
     h->op32m_ready = true;
 }
 
+// the slice-contiguous FP32 operator of the single-vector stream
+void ensure_f32s(h2w_handle *h) {
+    ensure_f32(h);
+    if (h->op32s_ready) return;
+    h->d_op32s.reset();
+    h->d_op32s.alloc((size_t)std::max<int64_t>(h->op32s_n, 4));
+    CK(launch_slice_copy_f32(h->d_op32.p, h->d_sslices.p, (int64_t)h->d_sslices.n / 6, h->d_op32s.p, h->stream));
+    CK(cudaStreamSynchronize(h->stream));  // products may run on a caller's stream
+    h->op32s_ready = true;
+}
+
 // FP32 operator and workspace; x and y stay FP64 in original order (the
 // conversions happen in the kernel's gather and scatter).
 void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st, bool permuted = false) {
-    ensure_f32(h);
+    ensure_f32s(h);
     const int32_t *perm = permuted ? nullptr : h->d_perm.p;
     const int nph = (int)h->phases.size();
     CK(cudaMemsetAsync(h->d_ws32.p, 0, (size_t)h->ws_n * 4, st));
@@ -2600,14 +2642,14 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
             if (b <= a) return;
             if (h->coop) {
                 prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
-                    return launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p + a, b - a, h->d_op32.p,
+                    return launch_coop_f32(h->d_roff.p, h->d_blob_s.p, h->d_pstart.p + a, b - a, h->d_op32s.p,
                                            h->d_ws32.p, dx, dy, perm, h->d_bar.p, h->d_err.p, st, h->spin_limit);
                 });
             } else {
                 for (int q = a; q < b; ++q) {
                     const Phase &ph = h->phases[(size_t)q];
                     prof_launch(h, H2W_PREC_FP32, q, st, [&] {
-                        return launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, h->d_ws32.p, dx, dy,
+                        return launch_brg_f32(h->d_roff.p, h->d_blob_s.p, ph.t0, ph.t1, h->d_op32s.p, h->d_ws32.p, dx, dy,
                                               perm, st);
                     });
                 }
@@ -2623,20 +2665,20 @@ void run_matvec_f32(h2w_handle *h, const double *dx, double *dy, cudaStream_t st
         CK(cudaMemcpyAsync(h->d_sdep.p, h->d_sdep0.p, h->d_sdep0.n * 4, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemsetAsync(h->d_sctr.p, 0, 4, st));
         prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
-            return launch_brg_flow_f32(h->d_roff.p, h->d_blob.p, 0, (int64_t)h->d_roff.n - 1, h->d_sctr.p, h->d_sdep.p,
-                                       h->d_scoff.p, h->d_scidx.p, h->d_op32.p, h->d_ws32.p, dx, dy, perm, h->d_err.p,
+            return launch_brg_flow_f32(h->d_roff.p, h->d_blob_s.p, 0, (int64_t)h->d_roff.n - 1, h->d_sctr.p, h->d_sdep.p,
+                                       h->d_scoff.p, h->d_scidx.p, h->d_op32s.p, h->d_ws32.p, dx, dy, perm, h->d_err.p,
                                        st);
         });
     } else if (h->coop) {
         prof_launch(h, H2W_PREC_FP32, nph, st, [&] {
-            return launch_coop_f32(h->d_roff.p, h->d_blob.p, h->d_pstart.p, nph, h->d_op32.p, h->d_ws32.p, dx, dy,
+            return launch_coop_f32(h->d_roff.p, h->d_blob_s.p, h->d_pstart.p, nph, h->d_op32s.p, h->d_ws32.p, dx, dy,
                                    perm, h->d_bar.p, h->d_err.p, st, h->spin_limit);
         });
     } else {
         for (size_t q = 0; q < h->phases.size(); ++q) {
             const Phase &ph = h->phases[q];
             prof_launch(h, H2W_PREC_FP32, (int)q, st, [&] {
-                return launch_brg_f32(h->d_roff.p, h->d_blob.p, ph.t0, ph.t1, h->d_op32.p, h->d_ws32.p, dx, dy, perm,
+                return launch_brg_f32(h->d_roff.p, h->d_blob_s.p, ph.t0, ph.t1, h->d_op32s.p, h->d_ws32.p, dx, dy, perm,
                                       st);
             });
         }
