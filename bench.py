@@ -388,12 +388,21 @@ def run_single_random(args, wl, rank, world, local):
                      "note": "achieved = (4 B x the reference's storage count E + 16 B x N) / the product's "
                              "CUDA-event time, against the measured HBM copy bandwidth (%s). The product reads "
                              "its stored %.1f GB and evaluates the far-field M2L entries (%.3g of E's %.3g) from "
-                             "the points; traffic is null (three launches; DRAM bytes per far-field entry "
-                             "0.066 in profiles/m2l_fly32_sep_3d_rbf_131072.md)" % (peak_kind, stored / 1e9, fl_e, E),
+                             "the points instead of reading them, so achieved can exceed the copy bandwidth; "
+                             "stored_passes gives the HBM rate of the part that streams its operator. traffic "
+                             "is null (three launches; DRAM bytes per far-field entry 0.062 in "
+                             "profiles/m2l_fly32_sep_3d_rbf_131072.md)" % (peak_kind, stored / 1e9, fl_e, E),
                      "far_field_kernel": {"name": "m2l_fly32_sep_kernel", "bound": "instruction issue",
                                           "launch_ms": fl_t, "entries_per_launch": fl_e,
                                           "entries_per_s": fl_e / (fl_t * 1e-3) if fl_n else None,
-                                          "share_of_product": fl_t / mv["fp32"] if fl_n else None}},
+                                          "share_of_product": fl_t / mv["fp32"] if fl_n else None},
+                     # the part of the product that streams its operator from HBM: the stored
+                     # passes (the product's time less the far-field kernel's), their FP32 bytes
+                     "stored_passes": {"bytes": stored, "ms": mv["fp32"] - fl_t,
+                                       "achieved_gbs": stored / ((mv["fp32"] - fl_t) * 1e-3) / 1e9
+                                       if fl_n and mv["fp32"] > fl_t else None,
+                                       "frac": stored / ((mv["fp32"] - fl_t) * 1e-3) / 1e9 / peak
+                                       if fl_n and mv["fp32"] > fl_t else None}},
         "compute": {"flydf_ms": flydf[1] / max(flydf[0], 1), "flydf_entries_per_s":
                         flydf[2] / (flydf[1] / max(flydf[0], 1) * 1e-3) if flydf[0] else None},
         "cpu_baseline": {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
