@@ -128,6 +128,25 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(v, world, device=None):
+    """The slowest rank's figure: replicas end with their last rank, so a
+    multi-GPU run's time is the maximum over ranks (torch.distributed, any
+    backend; the value is the same on every rank)."""
+    if world <= 1:
+        return float(v)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, world, ms):
+    """Whole-job throughput of independent replicas: every rank's units over
+    the slowest rank's time (ms, the maximum over ranks)."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 def nlevels_for(dim, n_param, leaf_param):
     """Tree depth as the reference's drivers compute it (1D/codes/main.cpp:13,
     2D/codes/main.cpp:13, 3D/codes/main.cpp:11)."""
@@ -255,13 +274,6 @@ def run_single_random(args, wl, rank, world, local):
         if world > 1:
             dist.barrier()
 
-    def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
     hw.build()
     N, dim = wl["npts"], wl["dim"]
     nlev = int(math.ceil(math.log(N / float(wl["nmax"])) / math.log(2.0 ** dim)))
@@ -303,7 +315,7 @@ def run_single_random(args, wl, rank, world, local):
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
-        return max_over_ranks(e0.elapsed_time(e1)), out, hw.launch_count() - l0, (t0w, time.time())
+        return max_over_ranks(e0.elapsed_time(e1), world, dev), out, hw.launch_count() - l0, (t0w, time.time())
 
     # products on this stream: FP32, double-FP32 and FP64, each with its far M2L kernel
     mv = {}
@@ -368,7 +380,7 @@ def run_single_random(args, wl, rank, world, local):
     prod_bytes = 4.0 * E + 2 * 8.0 * N
     prod_gbs = prod_bytes / (mv["fp32"] * 1e-3) / 1e9
     line = {
-        "metric": METRIC, "value": K * world / (ms_m / 1e3), "unit": "solves/s", "n_gpus": world, "steps": K,
+        "metric": METRIC, "value": replica_throughput(K, world, ms_m), "unit": "solves/s", "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_m / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": wl["desc"], "N": N, "nlevels": nlev, "form": "H2*", "rhs_per_step": 1,
@@ -379,7 +391,7 @@ def run_single_random(args, wl, rank, world, local):
         "solver": "mixed: FP32-operator inner GMRES + iterative refinement with FP64-accurate residuals (stored "
                   "passes FP64, far-field M2L in double-FP32 arithmetic), CUDA-graph Arnoldi loop; far-field M2L "
                   "evaluated from the points in every product; the plain form is FP64 throughout",
-        "e2e": {"value": world / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N,
+        "e2e": {"value": replica_throughput(1, world, ms_e2e), "unit": "solves/s", "h2d_bytes_per_step": 16 * N,
                 "d2h_bytes_per_step": 8 * N},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "unit_of_work": "one FP32 product (stored passes + far-field M2L kernel)",
@@ -556,11 +568,7 @@ def main():
         torch.cuda.synchronize()
         t1w = time.time()
         barrier()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            tt = torch.tensor([ms], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            ms = float(tt.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
         return ms, out, hw.launch_count() - l0, (t0w, t1w)
 
     def col_err(X):
@@ -707,7 +715,7 @@ def main():
                       "blocks": blocks, "accepted": acc}
     asm["learned_speedup"] = asm["plain"]["s"] / t_l
 
-    value = K * R * world / (ms_b / 1e3)
+    value = replica_throughput(K * R, world, ms_b)
     ms_solve_b = ms_b / K / R
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -722,7 +730,7 @@ def main():
                       "fp32_producer_warp": op.get_option(hw.OPT_PRODUCER_WARP),
                       "single_row_split": tuned_rs, "single_fp32_ms": tuned_rs_ms},
         "operator_mb": {"fp64": op.operator_bytes(hw.PREC_FP64) / 1e6, "fp32": op.operator_bytes(hw.PREC_FP32) / 1e6},
-        "e2e": {"value": K * R * world / (ms_e2e / 1e3), "unit": "solves/s", "h2d_bytes_per_step": 16 * N * R,
+        "e2e": {"value": replica_throughput(K * R, world, ms_e2e), "unit": "solves/s", "h2d_bytes_per_step": 16 * N * R,
                 "d2h_bytes_per_step": 8 * N * R},
         "gpu_launches": int(launches),
         "roofline": roof,
