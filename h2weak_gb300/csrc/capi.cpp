@@ -4567,6 +4567,7 @@ int h2w_set_option(h2w_handle *h, int option, int64_t value) {
         } else if (option == H2W_OPT_COMPLEX_ARNOLDI) {
             h->cgm_hermitian = value != 0;
         } else if (option == H2W_OPT_FAR_ON_THE_FLY) {
+            if (value != 0) require_real(h, "the far field on the fly");
             h->far_fly = value != 0;  // takes effect at the next h2w_assemble
         } else if (option == H2W_OPT_COOP) {
             h->coop = value != 0;

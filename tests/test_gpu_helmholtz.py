@@ -143,3 +143,18 @@ def test_hankel_product_and_gmres(gpu, form):
     assert res < 1e-10 and it2 >= 1
     assert relerr(op.matvec(xs), y) < 1e-9
     assert relerr(xs, x) < 1e-6
+
+
+@pytest.mark.gpu
+def test_helmholtz_operator_file_round_trip(gpu, tmp_path):
+    """An operator file of a complex operator (points and pivots) reopens to
+    the same operator: the products agree bit for bit."""
+    hw = gpu
+    op = helm_op(hw, 6000, 2, 8)
+    x = cvec(6, op.N)
+    y = op.matvec(x)
+    path = str(tmp_path / "helm.h2wop")
+    op.save(path)
+    op2 = hw.H2Operator.open(path)
+    assert op2.complex and op2.storage_entries() == op.storage_entries()
+    assert np.array_equal(op2.matvec(x), y)

@@ -140,3 +140,7 @@ def test_complex_kernel_configurations():
     for dim, form, choice in ((2, 0, 2), (1, 0, 2), (3, 0, 10), (3, 2, 2), (2, 2, 10), (2, 0, 3)):
         with pytest.raises(hw.H2WError):
             hw.H2Operator(dim, form, choice, 8, 2, device=-1)
+    op = hw.H2Operator(3, 0, 2, 8, 2, device=-1)
+    with pytest.raises(hw.H2WError) as e:
+        op.set_option(hw.OPT_FAR_ON_THE_FLY, 1)  # real kernels only
+    assert e.value.code == hw.ERR_ARG
