@@ -1,6 +1,8 @@
-// CPU restatement of H2weak's nested H2* and semi-nested (H2+H)* HODLRdD
-// operators (tree build, NCA/ACA compression, matvec passes, GMRES) in
-// 1D/2D/3D, real FP64 kernels choice 0 and 1.
+// CPU restatement of H2weak's nested H2*, semi-nested (H2+H)* and non-nested
+// H* HODLRdD operators (tree build, NCA/ACA compression, matvec passes,
+// GMRES) in 1D/2D/3D: real FP64 kernels choice 0 and 1, and the complex
+// Helmholtz kernel choice 2 of the reference's USE_Helm build (3D), the
+// operator templated on its scalar.
 //
 // TEST INFRASTRUCTURE ONLY (the oracle): tests, smoke() and bench.py's CPU
 // baseline call it as the checker; the GPU library never links it.
@@ -17,10 +19,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <type_traits>
 #include <vector>
 #include <omp.h>
 
@@ -28,80 +32,85 @@ namespace {
 
 const double PI = 4.0 * std::atan(1.0);  // */codes/headers.hpp:18
 
-struct Mat {  // column-major dense block
+// Scalars: double (the reference's real build) or std::complex<double> (its
+// complex Helmholtz build, 3D/codes/headers.hpp:35-40); abs, conj and |.|^2
+// as the C++ runtime and Eigen evaluate them (gmres_ref.hpp).
+using h2w_ref::abs_;
+using h2w_ref::abs2_;
+using h2w_ref::conj_;
+using cplx = std::complex<double>;
+
+template <class S> struct MatT {  // column-major dense block
     int r = 0, c = 0;
-    std::vector<double> a;
-    Mat() {}
-    Mat(int rr, int cc) : r(rr), c(cc), a((size_t)rr * cc, 0.0) {}
-    double &operator()(int i, int j) { return a[(size_t)i + (size_t)j * r]; }
-    double operator()(int i, int j) const { return a[(size_t)i + (size_t)j * r]; }
+    std::vector<S> a;
+    MatT() {}
+    MatT(int rr, int cc) : r(rr), c(cc), a((size_t)rr * cc, S(0.0)) {}
+    S &operator()(int i, int j) { return a[(size_t)i + (size_t)j * r]; }
+    S operator()(int i, int j) const { return a[(size_t)i + (size_t)j * r]; }
     long size() const { return (long)r * c; }
 };
-using Vec = std::vector<double>;
+template <class S> using VecT = std::vector<S>;
 
 // y = A x (rows summed in ascending column order)
-Vec gemv(const Mat &A, const Vec &x) {
-    Vec y((size_t)A.r, 0.0);
+template <class S> VecT<S> gemv(const MatT<S> &A, const VecT<S> &x) {
+    VecT<S> y((size_t)A.r, S(0.0));
     for (int i = 0; i < A.r; ++i) {
-        double s = 0.0;
-        for (int j = 0; j < A.c; ++j) { double p = A(i, j) * x[(size_t)j]; s = s + p; }
+        S s = S(0.0);
+        for (int j = 0; j < A.c; ++j) { S p = A(i, j) * x[(size_t)j]; s = s + p; }
         y[(size_t)i] = s;
     }
     return y;
 }
-// y = A^T x
-Vec gemvT(const Mat &A, const Vec &x) {
-    Vec y((size_t)A.c, 0.0);
+// y = A^T x (a transpose: no conjugation)
+template <class S> VecT<S> gemvT(const MatT<S> &A, const VecT<S> &x) {
+    VecT<S> y((size_t)A.c, S(0.0));
     for (int j = 0; j < A.c; ++j) {
-        double s = 0.0;
-        for (int i = 0; i < A.r; ++i) { double p = A(i, j) * x[(size_t)i]; s = s + p; }
+        S s = S(0.0);
+        for (int i = 0; i < A.r; ++i) { S p = A(i, j) * x[(size_t)i]; s = s + p; }
         y[(size_t)j] = s;
     }
     return y;
 }
-void addto(Vec &y, const Vec &x) { for (size_t i = 0; i < y.size(); ++i) y[i] += x[i]; }
-double dot(const Vec &a, const Vec &b) {
-    double s = 0.0;
-    for (size_t i = 0; i < a.size(); ++i) { double p = a[i] * b[i]; s = s + p; }
-    return s;
-}
-double nrm(const Vec &a) { return std::sqrt(dot(a, a)); }
+template <class S> void addto(VecT<S> &y, const VecT<S> &x) { for (size_t i = 0; i < y.size(); ++i) y[i] += x[i]; }
+// Eigen's a.dot(b) (conjugate-first) and norm()
+template <class S> S dot(const VecT<S> &a, const VecT<S> &b) { return h2w_ref::dot(a, b); }
+template <class S> double nrm(const VecT<S> &a) { return h2w_ref::nrm(a); }
 
 // Triangular solves with the semantics of Eigen's triangularView::solve.
 // Lower, on the left, column by column: T X = B.
-void trsv_lower(const Mat &T, bool transposed, double *x, int n) {
+template <class S> void trsv_lower(const MatT<S> &T, bool transposed, S *x, int n) {
     // T lower (or T^T lower when transposed=true, i.e. T upper read as T(q,i))
     for (int i = 0; i < n; ++i) {
-        double s = x[i];
+        S s = x[i];
         for (int q = 0; q < i; ++q) {
-            double t = transposed ? T(q, i) : T(i, q);
-            double p = t * x[q];
+            S t = transposed ? T(q, i) : T(i, q);
+            S p = t * x[q];
             s = s - p;
         }
         x[i] = s / (transposed ? T(i, i) : T(i, i));
     }
 }
-void trsv_upper(const Mat &T, bool transposed, double *x, int n) {
+template <class S> void trsv_upper(const MatT<S> &T, bool transposed, S *x, int n) {
     for (int i = n - 1; i >= 0; --i) {
-        double s = x[i];
+        S s = x[i];
         for (int q = i + 1; q < n; ++q) {
-            double t = transposed ? T(q, i) : T(i, q);
-            double p = t * x[q];
+            S t = transposed ? T(q, i) : T(i, q);
+            S p = t * x[q];
             s = s - p;
         }
         x[i] = s / T(i, i);
     }
 }
 // X T = B with T upper: row by row forward substitution.
-Mat solve_right_upper(const Mat &T, const Mat &B) {
-    Mat X = B;
+template <class S> MatT<S> solve_right_upper(const MatT<S> &T, const MatT<S> &B) {
+    MatT<S> X = B;
     int n = T.r;
-    std::vector<double> x((size_t)n);
+    std::vector<S> x((size_t)n);
     for (int rr = 0; rr < B.r; ++rr) {
         for (int j = 0; j < n; ++j) x[(size_t)j] = B(rr, j);
         for (int j = 0; j < n; ++j) {
-            double s = x[(size_t)j];
-            for (int q = 0; q < j; ++q) { double p = x[(size_t)q] * T(q, j); s = s - p; }
+            S s = x[(size_t)j];
+            for (int q = 0; q < j; ++q) { S p = x[(size_t)q] * T(q, j); s = s - p; }
             x[(size_t)j] = s / T(j, j);
         }
         for (int j = 0; j < n; ++j) X(rr, j) = x[(size_t)j];
@@ -109,15 +118,15 @@ Mat solve_right_upper(const Mat &T, const Mat &B) {
     return X;
 }
 // X T = B with T lower: row by row backward substitution.
-Mat solve_right_lower(const Mat &T, const Mat &B) {
-    Mat X = B;
+template <class S> MatT<S> solve_right_lower(const MatT<S> &T, const MatT<S> &B) {
+    MatT<S> X = B;
     int n = T.r;
-    std::vector<double> x((size_t)n);
+    std::vector<S> x((size_t)n);
     for (int rr = 0; rr < B.r; ++rr) {
         for (int j = 0; j < n; ++j) x[(size_t)j] = B(rr, j);
         for (int j = n - 1; j >= 0; --j) {
-            double s = x[(size_t)j];
-            for (int q = j + 1; q < n; ++q) { double p = x[(size_t)q] * T(q, j); s = s - p; }
+            S s = x[(size_t)j];
+            for (int q = j + 1; q < n; ++q) { S p = x[(size_t)q] * T(q, j); s = s - p; }
             x[(size_t)j] = s / T(j, j);
         }
         for (int j = 0; j < n; ++j) X(rr, j) = x[(size_t)j];
@@ -164,7 +173,9 @@ void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
     for (auto &p : pr) { x.push_back((double)p.first); w.push_back((double)p.second); }
 }
 
-struct Box {
+template <class S> struct BoxT {
+    using Mat = MatT<S>;
+    using Vec = VecT<S>;
     std::vector<int> pts;            // chargeLocations
     int nb[26];                      // neighborNumbers
     std::vector<int> il;             // interactionList
@@ -186,19 +197,37 @@ struct Box {
     Vec q, out, in, inv, pot, potv;
 };
 
-struct Oracle {
+template <class S> struct OracleT {
+    using Mat = MatT<S>;
+    using Vec = VecT<S>;
+    using Box = BoxT<S>;
     int dim, form, nL, tol_pow, choice;
     int64_t N;
     std::vector<double> P;  // n*dim
     int64_t kernel_n, diag_n;
-    double Kii = 0.0, hd = 1.0, diag_val = 1.0;
+    double Kii = 0.0, hd = 1.0;
+    S diag_val = S(1.0);
     int nch, nnb;
     std::vector<std::vector<Box>> T;
 
     // ---- kernel entries: 1D/codes/kernel.hpp:108-185, 2D/codes/kernel.hpp:118-124,197-228,298-318,
     //      3D/codes/kernel.hpp:123-129,146-170,172-193
-    double entry(int i, int j) const {
-        if (i == j) return diag_val;
+    S entry(int i, int j) const {
+        if constexpr (std::is_same<S, double>::value) return entry_real(i, j);
+        else return entry_helm(i, j);
+    }
+    // Helmholtz3D (3D/codes/kernel.hpp:133-144, choice 2), the reference's expression:
+    // exp(I R) / (4 PI) off the diagonal, 500 sqrt(N) on it
+    cplx entry_helm(int i, int j) const {
+        const double *a = &P[(size_t)i * dim], *b = &P[(size_t)j * dim];
+        double R2 = (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]);
+        double R = std::sqrt(R2);
+        if (i == j) return 500 * std::sqrt(double(diag_n));
+        const cplx I(0.0, 1.0);
+        return (std::exp(I * R)) / (4.0 * PI);
+    }
+    double entry_real(int i, int j) const {
+        if (i == j) return h2w_ref::real_(diag_val);
         const double *a = &P[(size_t)i * dim], *b = &P[(size_t)j * dim];
         if (dim == 1) {
             double R = std::fabs(a[0] - b[0]);
@@ -481,8 +510,8 @@ struct Oracle {
         double mx = 0.0;
         for (size_t i = 0; i < v.size(); ++i) {
             if (!allowed[i]) continue;
-            if (index < 0) { index = (int)i; mx = std::fabs(v[i]); continue; }
-            if (std::fabs(v[i]) > std::fabs(mx)) { index = (int)i; mx = std::fabs(v[i]); }
+            if (index < 0) { index = (int)i; mx = abs_(v[i]); continue; }
+            if (abs_(v[i]) > std::fabs(mx)) { index = (int)i; mx = abs_(v[i]); }
         }
         return index;
     }
@@ -506,7 +535,7 @@ struct Oracle {
             row_index = l_local;
             get_row(row_index, row);
             col_index = max_abs(row, rcol);
-            if (col_index >= 0 && std::fabs(row[(size_t)col_index]) > tiny) break;
+            if (col_index >= 0 && abs_(row[(size_t)col_index]) > tiny) break;
         }
         if (l_local == N1) return res;
         Vec v = row;
@@ -514,7 +543,7 @@ struct Oracle {
         res.cols.push_back(col_index);
         get_col(col_index, col);
         Vec u((size_t)N1);
-        double piv = row[(size_t)col_index];
+        S piv = row[(size_t)col_index];
         for (int s = 0; s < N1; ++s) u[(size_t)s] = col[(size_t)s] / piv;
         Uv.push_back(u);
         Vv.push_back(v);
@@ -529,9 +558,9 @@ struct Oracle {
             get_row(row_index, row);
             Vec row_temp = row;
             for (int l = 0; l < res.rank; ++l) {
-                double ul = Uv[(size_t)l][(size_t)row_index];
+                S ul = Uv[(size_t)l][(size_t)row_index];
                 const Vec &Vl = Vv[(size_t)l];
-                for (int s = 0; s < N2; ++s) { double p = ul * Vl[(size_t)s]; row[(size_t)s] -= p; }
+                for (int s = 0; s < N2; ++s) { S p = ul * Vl[(size_t)s]; row[(size_t)s] -= p; }
             }
             col_index = max_abs(row, rcol);
             res.cols.push_back(col_index);
@@ -539,9 +568,9 @@ struct Oracle {
             get_col(col_index, col);
             Vec col_temp = col;
             for (int l = 0; l < res.rank; ++l) {
-                double vl = Vv[(size_t)l][(size_t)col_index];
+                S vl = Vv[(size_t)l][(size_t)col_index];
                 const Vec &Ul = Uv[(size_t)l];
-                for (int s = 0; s < N1; ++s) { double p = vl * Ul[(size_t)s]; col[(size_t)s] -= p; }
+                for (int s = 0; s < N1; ++s) { S p = vl * Ul[(size_t)s]; col[(size_t)s] -= p; }
             }
             piv = row[(size_t)col_index];
             for (int s = 0; s < N1; ++s) u[(size_t)s] = col[(size_t)s] / piv;
@@ -559,9 +588,9 @@ struct Oracle {
             double uv = nrm(u) * nrm(v);
             normS = normS * normS + uv * uv;
             for (int l = 0; l < res.rank; ++l) {
-                double du = dot(Uv[(size_t)l], u), dv = dot(Vv[(size_t)l], v);
-                double t = du * dv;
-                normS += 2 * std::fabs(t);
+                S du = dot(Uv[(size_t)l], u), dv = dot(Vv[(size_t)l], v);
+                S t = du * dv;
+                normS += 2 * abs_(t);
             }
             normS = std::sqrt(normS);
             row_index = max_abs(col, rrow);
@@ -597,7 +626,7 @@ struct Oracle {
     Mat lr_t_solve(const Mat &L, const Mat &R, Mat B) const {
         int n = L.r;
         for (int c = 0; c < B.c; ++c) {
-            double *x = &B.a[(size_t)c * (size_t)B.r];
+            S *x = &B.a[(size_t)c * (size_t)B.r];
             trsv_lower(R, true, x, n);  // R^T is lower
             trsv_upper(L, true, x, n);  // L^T is upper
         }
@@ -813,20 +842,20 @@ struct Oracle {
     }
 
     // ---- matvec ---------------------------------------------------------
-    void assign_charges(const double *x) {  // assignCharges (1D :215-229, 3D :1854-1868)
+    void assign_charges(const S *x) {  // assignCharges (1D :215-229, 3D :1854-1868)
         for (int j = 1; j <= nL; ++j)
             for (auto &b : T[(size_t)j]) {
                 b.q.resize(b.pts.size());
                 for (size_t i = 0; i < b.pts.size(); ++i) b.q[i] = x[b.pts[i]];
             }
     }
-    void reorder(const Vec &yp, double *y) {  // reorder (1D :519-533, 3D :2489-2503)
+    void reorder(const Vec &yp, S *y) {  // reorder (1D :519-533, 3D :2489-2503)
         size_t cnt = 0;
         for (auto &b : T[(size_t)nL])
             for (int idx : b.pts) y[idx] = yp[cnt++];
     }
 
-    void matvec_1d(const double *x, double *y) {
+    void matvec_1d(const S *x, S *y) {
         assign_charges(x);
         Vec yp((size_t)N, 0.0);
         if (form == 0) {
@@ -872,7 +901,7 @@ struct Oracle {
             // collect_all_potentials (1D :487-501)
             size_t cnt = 0;
             for (auto &b : lf)
-                for (double v : b.pot) { yp[cnt] = 0.0 + v; ++cnt; }
+                for (S v : b.pot) { yp[cnt] = 0.0 + v; ++cnt; }
         } else {
             // fast_multiplication_nn (1D :445-464)
             for (int j = 1; j <= nL; ++j) {
@@ -892,7 +921,7 @@ struct Oracle {
             for (int j = 1; j <= nL; ++j) {
                 size_t cnt = 0;
                 for (auto &b : T[(size_t)j])
-                    for (double v : b.pot) { yp[cnt] += v; ++cnt; }
+                    for (S v : b.pot) { yp[cnt] += v; ++cnt; }
             }
         }
         reorder(yp, y);
@@ -901,7 +930,7 @@ struct Oracle {
     // H* (USE_HODLRdD): evaluateFarField_nn (2D :1053-1071, 3D :2353-2373) sets every
     // box's potential from its pairs, evaluate_NearField adds the leaf blocks,
     // collect_all_potentials_nn (2D :1175-1189, 3D :2473-2487) sums the levels.
-    void matvec_nn(const double *x, double *y) {
+    void matvec_nn(const S *x, S *y) {
         assign_charges(x);
         for (int j = 1; j <= nL; ++j) {
             auto &lv = T[(size_t)j];
@@ -931,12 +960,12 @@ struct Oracle {
         for (int j = 1; j <= nL; ++j) {
             size_t cnt = 0;
             for (auto &b : T[(size_t)j])
-                for (double v : b.pot) { yp[cnt] += v; ++cnt; }
+                for (S v : b.pot) { yp[cnt] += v; ++cnt; }
         }
         reorder(yp, y);
     }
 
-    void matvec_nd(const double *x, double *y) {
+    void matvec_nd(const S *x, S *y) {
         if (form == 2) {
             matvec_nn(x, y);
             return;
@@ -1042,7 +1071,7 @@ struct Oracle {
             size_t cnt = 0;
             for (auto &b : lf)
                 for (size_t i = 0; i < b.pot.size(); ++i) {
-                    double pv = b.pot[i] + b.potv[i];
+                    S pv = b.pot[i] + b.potv[i];
                     yp[cnt] = 0.0 + pv;
                     ++cnt;
                 }
@@ -1067,11 +1096,11 @@ struct Oracle {
             // collect_all_potentials_semi_1 / _semi_2 (2D :1144-1173, 3D :2442-2471)
             size_t cnt = 0;
             for (auto &b : lf)
-                for (double v : b.pot) { yp[cnt] = 0.0 + v; ++cnt; }
+                for (S v : b.pot) { yp[cnt] = 0.0 + v; ++cnt; }
             for (int j = 1; j <= nL; ++j) {
                 cnt = 0;
                 for (auto &b : T[(size_t)j])
-                    for (double v : b.potv) { yp[cnt] += v; ++cnt; }
+                    for (S v : b.potv) { yp[cnt] += v; ++cnt; }
             }
         }
         reorder(yp, y);
@@ -1123,32 +1152,39 @@ struct Oracle {
         return mem;
     }
 
-    void matvec(const double *x, double *y) {
+    void matvec(const S *x, S *y) {
         if (dim == 1) matvec_1d(x, y);
         else matvec_nd(x, y);
     }
 
     // ---- GMRES: */codes/gmres.hpp:30-200 (oracle/gmres_ref.hpp) ------------
-    int gmres(const double *bb, double *x, int max_iter, int tol_pow, int *iters, double *resid) {
-        return h2w_ref::gmres([this](const double *in, double *out) { matvec(in, out); }, (size_t)N, bb, x, max_iter,
+    int gmres(const S *bb, S *x, int max_iter, int tol_pow, int *iters, double *resid) {
+        return h2w_ref::gmres([this](const S *in, S *out) { matvec(in, out); }, (size_t)N, bb, x, max_iter,
                               tol_pow, iters, resid);
     }
 };
 
 }  // namespace
 
+// One oracle handle: the real operator, or the complex Helmholtz one (choice 2,
+// 3D); complex vectors cross the C API as interleaved (re, im) doubles.
 struct h2wo {
-    Oracle o;
+    OracleT<double> *r = nullptr;
+    OracleT<cplx> *c = nullptr;
+    ~h2wo() {
+        delete r;
+        delete c;
+    }
 };
 
-extern "C" {
+// run f on the handle's operator with its scalar pointer type
+template <class F> auto on(h2wo *h, F &&f) {
+    if (h->c) return f(*h->c, (cplx *)nullptr);
+    return f(*h->r, (double *)nullptr);
+}
 
-h2wo *h2wo_create(int dim, int form, int64_t n, const double *pts, int nlevels, int tol_pow, int choice,
-                  int64_t kernel_n, int64_t diag_n) {
-    if (dim < 1 || dim > 3 || n < 1 || nlevels < 1 || (form != 0 && form != 1 && form != 2) || (form == 2 && dim == 1) || (choice != 0 && choice != 1))
-        return nullptr;
-    h2wo *h = new h2wo;
-    Oracle &o = h->o;
+template <class S> void init_oracle(OracleT<S> &o, int dim, int form, int64_t n, const double *pts, int nlevels,
+                                    int tol_pow, int choice, int64_t kernel_n, int64_t diag_n) {
     o.dim = dim;
     o.form = form;
     o.N = n;
@@ -1160,48 +1196,10 @@ h2wo *h2wo_create(int dim, int form, int64_t n, const double *pts, int nlevels, 
     o.diag_n = diag_n;
     o.setup_kernel();
     o.build_tree();
-    return h;
 }
 
-void h2wo_destroy(h2wo *o) { delete o; }
-
-int h2wo_assemble(h2wo *h) {
-    if (h->o.dim == 1) h->o.assemble_1d();
-    else h->o.assemble_nd();
-    return 0;
-}
-
-int h2wo_matvec(h2wo *h, const double *x, double *y) {
-    h->o.matvec(x, y);
-    return 0;
-}
-
-int h2wo_dense_matvec(h2wo *h, const double *x, double *y) {
-    // getTruePoten (1D :590-604, 2D :1333-1346, 3D :2630-2643)
-    const Oracle &o = h->o;
-#pragma omp parallel for schedule(dynamic, 64)
-    for (long i = 0; i < (long)o.N; ++i) {
-        double s = 0.0;
-        for (long j = 0; j < (long)o.N; ++j) { double p = o.entry((int)i, (int)j) * x[j]; s = s + p; }
-        y[i] = s;
-    }
-    return 0;
-}
-
-int h2wo_gmres(h2wo *h, const double *b, double *x, int max_iter, int tol_pow, int *iters, double *resid) {
-    return h->o.gmres(b, x, max_iter, tol_pow, iters, resid);
-}
-
-double h2wo_memory(h2wo *h) { return h->o.memory(); }
-double h2wo_kii(h2wo *h) { return h->o.Kii; }
-
-int h2wo_entries(h2wo *h, const int32_t *rows, int64_t nr, const int32_t *cols, int64_t nc, double *out) {
-    for (int64_t i = 0; i < nr; ++i)
-        for (int64_t j = 0; j < nc; ++j) out[i * nc + j] = h->o.entry(rows[i], cols[j]);
-    return 0;
-}
-
-static void list_of(const Oracle &o, int which, std::vector<int64_t> &ptr, std::vector<int32_t> &val) {
+template <class S>
+static void list_of(const OracleT<S> &o, int which, std::vector<int64_t> &ptr, std::vector<int32_t> &val) {
     ptr.assign(1, 0);
     val.clear();
     auto add = [&](const std::vector<int> &v) {
@@ -1248,10 +1246,90 @@ static void list_of(const Oracle &o, int which, std::vector<int64_t> &ptr, std::
         }
 }
 
+
+extern "C" {
+
+h2wo *h2wo_create(int dim, int form, int64_t n, const double *pts, int nlevels, int tol_pow, int choice,
+                  int64_t kernel_n, int64_t diag_n) {
+    if (dim < 1 || dim > 3 || n < 1 || nlevels < 1 || (form != 0 && form != 1 && form != 2) || (form == 2 && dim == 1) ||
+        (choice != 0 && choice != 1 && choice != 2) || (choice == 2 && (dim != 3 || form == 2)))
+        return nullptr;
+    h2wo *h = new h2wo;
+    if (choice == 2) {
+        h->c = new OracleT<cplx>;
+        init_oracle(*h->c, dim, form, n, pts, nlevels, tol_pow, choice, kernel_n, diag_n);
+    } else {
+        h->r = new OracleT<double>;
+        init_oracle(*h->r, dim, form, n, pts, nlevels, tol_pow, choice, kernel_n, diag_n);
+    }
+    return h;
+}
+
+void h2wo_destroy(h2wo *o) { delete o; }
+
+int h2wo_assemble(h2wo *h) {
+    return on(h, [](auto &o, auto *) {
+        if (o.dim == 1) o.assemble_1d();
+        else o.assemble_nd();
+        return 0;
+    });
+}
+
+int h2wo_matvec(h2wo *h, const double *x, double *y) {
+    return on(h, [&](auto &o, auto *t) {
+        using S = std::remove_pointer_t<decltype(t)>;
+        o.matvec(reinterpret_cast<const S *>(x), reinterpret_cast<S *>(y));
+        return 0;
+    });
+}
+
+int h2wo_dense_matvec(h2wo *h, const double *x, double *y) {
+    // getTruePoten (1D :590-604, 2D :1333-1346, 3D :2630-2643)
+    return on(h, [&](auto &o, auto *t) {
+        using S = std::remove_pointer_t<decltype(t)>;
+        const S *xs = reinterpret_cast<const S *>(x);
+        S *ys = reinterpret_cast<S *>(y);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long i = 0; i < (long)o.N; ++i) {
+            S s = S(0.0);
+            for (long j = 0; j < (long)o.N; ++j) { S p = o.entry((int)i, (int)j) * xs[j]; s = s + p; }
+            ys[i] = s;
+        }
+        return 0;
+    });
+}
+
+int h2wo_gmres(h2wo *h, const double *b, double *x, int max_iter, int tol_pow, int *iters, double *resid) {
+    return on(h, [&](auto &o, auto *t) {
+        using S = std::remove_pointer_t<decltype(t)>;
+        return o.gmres(reinterpret_cast<const S *>(b), reinterpret_cast<S *>(x), max_iter, tol_pow, iters, resid);
+    });
+}
+
+double h2wo_memory(h2wo *h) {
+    return on(h, [](auto &o, auto *) { return o.memory(); });
+}
+double h2wo_kii(h2wo *h) {
+    return on(h, [](auto &o, auto *) { return o.Kii; });
+}
+
+/* entries K(rows[i], cols[j]); complex kernels write (re, im) pairs */
+int h2wo_entries(h2wo *h, const int32_t *rows, int64_t nr, const int32_t *cols, int64_t nc, double *out) {
+    return on(h, [&](auto &o, auto *t) {
+        using S = std::remove_pointer_t<decltype(t)>;
+        S *os = reinterpret_cast<S *>(out);
+        for (int64_t i = 0; i < nr; ++i)
+            for (int64_t j = 0; j < nc; ++j) os[i * nc + j] = o.entry(rows[i], cols[j]);
+        return 0;
+    });
+}
+
+int h2wo_is_complex(h2wo *h) { return h->c ? 1 : 0; }
+
 int64_t h2wo_list(h2wo *h, int which, int64_t *ptr, int32_t *val) {
     std::vector<int64_t> p;
     std::vector<int32_t> v;
-    list_of(h->o, which, p, v);
+    on(h, [&](auto &o, auto *) { list_of(o, which, p, v); return 0; });
     if (ptr) std::memcpy(ptr, p.data(), p.size() * sizeof(int64_t));
     if (val && !v.empty()) std::memcpy(val, v.data(), v.size() * sizeof(int32_t));
     return (int64_t)v.size();
@@ -1260,7 +1338,7 @@ int64_t h2wo_list(h2wo *h, int which, int64_t *ptr, int32_t *val) {
 int64_t h2wo_list_nptr(h2wo *h, int which) {
     std::vector<int64_t> p;
     std::vector<int32_t> v;
-    list_of(h->o, which, p, v);
+    on(h, [&](auto &o, auto *) { list_of(o, which, p, v); return 0; });
     return (int64_t)p.size();
 }
 

@@ -18,7 +18,11 @@ extern "C" {
 
 typedef struct h2wo h2wo;
 
-/* dim 1..3; form 0 = nested H2*, 1 = semi-nested (H2+H)*; pts n*dim
+/* dim 1..3; form 0 = nested H2*, 1 = semi-nested (H2+H)*, 2 = H*;
+ * choice 0 / 1 (real kernels) or 2 (the complex Helmholtz kernel of the
+ * reference's USE_Helm build, 3D, forms 0 and 1), whose vectors (x, y, b in
+ * matvec, dense_matvec, gmres; out in entries) are interleaved (re, im)
+ * doubles; pts n*dim
  * row-major; kernel_n = particles.size() when the reference kernel object
  * is built (sets h), diag_n = particles.size() when entries are evaluated
  * (1D drivers push the grid twice, so diag_n = 2N there). */
@@ -39,6 +43,8 @@ int h2wo_entries(h2wo *o, const int32_t *rows, int64_t nr, const int32_t *cols, 
  * Returns the number of values; ptr/val may be NULL to query sizes
  * (h2wo_list_nptr gives the ptr length). */
 int64_t h2wo_list(h2wo *o, int which, int64_t *ptr, int32_t *val);
+/* 1 for the complex kernel */
+int h2wo_is_complex(h2wo *o);
 int64_t h2wo_list_nptr(h2wo *o, int which);
 
 #ifdef __cplusplus

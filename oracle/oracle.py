@@ -44,6 +44,8 @@ def lib():
         L.h2wo_list.argtypes = [P, I, P, P]
         L.h2wo_list_nptr.restype = I64
         L.h2wo_list_nptr.argtypes = [P, I]
+        L.h2wo_is_complex.argtypes = [P]
+        L.h2wo_is_complex.restype = I
         _lib = L
     return _lib
 
@@ -66,6 +68,8 @@ class Oracle:
         self.h = L.h2wo_create(dim, form, self.N, _p(self.points), nlevels, tol_pow, choice, kn, dn)
         if not self.h:
             raise ValueError("bad oracle arguments")
+        # the complex Helmholtz kernel (choice 2): complex128 vectors
+        self.dtype = np.complex128 if L.h2wo_is_complex(self.h) else np.float64
         if assemble:
             L.h2wo_assemble(self.h)
 
@@ -75,20 +79,20 @@ class Oracle:
             self.h = None
 
     def matvec(self, x):
-        x = np.ascontiguousarray(x, dtype=np.float64)
-        y = np.empty(self.N)
+        x = np.ascontiguousarray(x, dtype=self.dtype)
+        y = np.empty(self.N, dtype=self.dtype)
         lib().h2wo_matvec(self.h, _p(x), _p(y))
         return y
 
     def dense_matvec(self, x):
-        x = np.ascontiguousarray(x, dtype=np.float64)
-        y = np.empty(self.N)
+        x = np.ascontiguousarray(x, dtype=self.dtype)
+        y = np.empty(self.N, dtype=self.dtype)
         lib().h2wo_dense_matvec(self.h, _p(x), _p(y))
         return y
 
     def gmres(self, b, x0=None, max_iter=500, tol_pow=10):
-        b = np.ascontiguousarray(b, dtype=np.float64)
-        x = np.ones(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=self.dtype)
+        x = np.ones(self.N, dtype=self.dtype) if x0 is None else np.array(x0, dtype=self.dtype)
         it = ctypes.c_int(0)
         res = ctypes.c_double(0)
         lib().h2wo_gmres(self.h, _p(b), _p(x), max_iter, tol_pow, ctypes.byref(it), ctypes.byref(res))
@@ -103,7 +107,7 @@ class Oracle:
     def entries(self, rows, cols):
         r = np.ascontiguousarray(rows, dtype=np.int32)
         c = np.ascontiguousarray(cols, dtype=np.int32)
-        out = np.empty((len(r), len(c)))
+        out = np.empty((len(r), len(c)), dtype=self.dtype)
         lib().h2wo_entries(self.h, _p(r), len(r), _p(c), len(c), _p(out))
         return out
 

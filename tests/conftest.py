@@ -21,10 +21,6 @@ def golden_names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("g"))
 
 
-def real_golden_names():
-    """The fixtures of the real kernels (the CPU restatement in oracle/ covers
-    those; the complex Helmholtz fixtures are pinned by the reference build alone)."""
-    return [n for n in golden_names() if "_helm" not in n]
 
 
 def load_golden(name):

@@ -158,3 +158,29 @@ def test_helmholtz_operator_file_round_trip(gpu, tmp_path):
     op2 = hw.H2Operator.open(path)
     assert op2.complex and op2.storage_entries() == op.storage_entries()
     assert np.array_equal(op2.matvec(x), y)
+
+
+@pytest.mark.gpu
+def test_helmholtz_against_the_oracle(gpu):
+    """Seeded random points outside the fixtures: the GPU product on the CPU
+    oracle's pivots (the restatement, bit-exact with the reference's complex
+    build) matches the oracle's product to 1e-13, and GMRES takes the
+    oracle's iteration count +-1."""
+    from oracle import Oracle
+    hw = gpu
+    n = 6000
+    pts = synth.uniform_points(synth.config_seed(97, 21), n, 3)
+    o = Oracle(3, 0, pts, 2, 8, hw.KERNEL_HELMHOLTZ)
+    op = hw.H2Operator(3, 0, hw.KERNEL_HELMHOLTZ, 8, 2, device=0)
+    op.set_points(pts)
+    op.build_tree()
+    for nm in ("far_check", "far_charge", "ver_check", "ver_charge"):
+        op.import_list(nm, *o.csr(nm))
+    op.assemble(hw.ASSEMBLE_IMPORT)
+    assert op.storage_entries() == o.memory()
+    x = cvec(7, n)
+    assert relerr(op.matvec(x), o.matvec(x)) <= 1e-13
+    b = o.dense_matvec(cvec(8, n))
+    xs, it, res = op.gmres(b, max_iter=200, tol_pow=10)
+    xo, ito, reso = o.gmres(b, max_iter=200, tol_pow=10)
+    assert abs(it - ito) <= 1 and res < 1e-10

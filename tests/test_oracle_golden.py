@@ -4,7 +4,7 @@ storage count and matvec must agree bit for bit."""
 import numpy as np
 import pytest
 
-from conftest import real_golden_names, load_golden
+from conftest import golden_names, load_golden
 
 LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge"]
 
@@ -16,7 +16,7 @@ def oracle_for(g):
     return Oracle(dim, g["form"], g["points"], g["nlevels"], g["tol_pow"], g["choice"], kn, dn)
 
 
-@pytest.mark.parametrize("name", real_golden_names())
+@pytest.mark.parametrize("name", golden_names())
 def test_oracle_matches_reference(name):
     g = load_golden(name)
     o = oracle_for(g)
@@ -36,7 +36,7 @@ def test_oracle_matches_reference(name):
         assert np.array_equal(o.matvec(g["vecs"][k]), g["matvec"][k])
 
 
-@pytest.mark.parametrize("name", ["g1d_n_rbf", "g2d_n_ie", "g3d_sn_ie"])
+@pytest.mark.parametrize("name", ["g1d_n_rbf", "g2d_n_ie", "g3d_sn_ie", "g3d_n_helm"])
 def test_oracle_dense_and_gmres(name):
     g = load_golden(name)
     o = oracle_for(g)
