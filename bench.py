@@ -41,13 +41,13 @@ sys.path.insert(0, ROOT)
 METRIC = "GMRES time-to-1e-10 & matvec HBM GB/s: mixed+batched+learned vs plain FP64 GPU"
 
 WORKLOADS = {
-    # the workload the metric is quoted on: 2D H2* integral equation, 256^2 grid, nmax 64, NCA tol 1e-10
+    # 2D H2* integral equation, 256^2 grid, nmax 64, NCA tol 1e-10 (64 right-hand sides per step; the CPU
+    # oracle runs beside it)
     "2d_ie_65536": dict(dim=2, form=0, choice=0, tol=10, grid=256, leaf=8, gtol=10,
                         desc="2D H2* IE (choice 0), N=65536 (256^2 grid on [-1,1]^2), nmax=64, NCA tol 1e-10, "
                              "GMRES to 1e-10"),
-    # the CPU-sized case: 1D H2* (HSS) RBF, N=32768, nmax 64
-    # the benchmark spec's target: 3D H2* RBF, 2^20 uniform random points, nmax 128, tol 1e-10; its stored
-    # operator (about 4e10 entries) exceeds HBM, so the far-field M2L is evaluated during each product
+    # the default workload: 3D H2* RBF, 2^20 uniform random points, nmax 128, tol 1e-10; its stored
+    # operator (about 4.8e10 entries) exceeds HBM, so the far-field M2L is evaluated during each product
     "3d_rbf_1048576": dict(dim=3, form=0, choice=1, tol=10, npts=1048576, nmax=128, gtol=10, single=True,
                            desc="3D H2* RBF (choice 1), N=1048576 uniform random points in [-1,1)^3 "
                                 "(splitmix64 stream), nmax=128 (5 levels), NCA tol 1e-10, GMRES to 1e-10, "
@@ -57,6 +57,7 @@ WORKLOADS = {
                           desc="3D H2* RBF (choice 1), N=131072 uniform random points in [-1,1)^3 "
                                "(splitmix64 stream), nmax=128 (4 levels), NCA tol 1e-10, GMRES to 1e-10, "
                                "one right-hand side per solve; far-field M2L evaluated during each product"),
+    # the CPU-sized case: 1D H2* (HSS) RBF, N=32768, nmax 64
     "1d_rbf_32768": dict(dim=1, form=0, choice=1, tol=10, grid=32768, leaf=64, gtol=10,
                          desc="1D H2* RBF (choice 1), N=32768 grid on [-1,1], nmax=64, NCA tol 1e-10, GMRES to 1e-10"),
 }
