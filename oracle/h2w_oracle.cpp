@@ -134,6 +134,31 @@ template <class S> MatT<S> solve_right_lower(const MatT<S> &T, const MatT<S> &B)
     return X;
 }
 
+// J0 and Y0 for the 2D Hankel kernel (the reference calls Boost,
+// 2D/codes/integral2d.hpp:16-50): the power series (Abramowitz & Stegun
+// 9.1.10, 9.1.13) summed in long double, valid here for 0 < x <= 8 (pair
+// distances of points in a square of semi-length up to 2.8); larger
+// arguments are refused (NaN), since the oracle is only run on such sets.
+inline void j0y0_series(double xd, double &j0, double &y0) {
+    if (!(xd > 0.0) || xd > 8.0) {
+        j0 = y0 = std::nan("");
+        return;
+    }
+    const long double x = xd, t = 0.25L * x * x;
+    long double term = 1.0L, sj = 1.0L, sy = 0.0L, hk = 0.0L;
+    for (int k = 1; k < 200; ++k) {
+        term = term * (-t) / ((long double)k * (long double)k);
+        hk += 1.0L / (long double)k;
+        sj += term;
+        sy -= hk * term;
+        if (fabsl(term) * (hk + 1.0L) < 1e-30L) break;
+    }
+    const long double gamma = 0.577215664901532860606512090082402431L;
+    const long double two_over_pi = 0.636619772367581343075535053490057448L;
+    j0 = (double)sj;
+    y0 = (double)(two_over_pi * ((logl(0.5L * x) + gamma) * sj + sy));
+}
+
 // Gauss-Legendre nodes and weights on [-1,1] by Newton iteration on the
 // Legendre recurrence in long double, ordered as the reference's table
 // (*/codes/Gauss_Legendre_Nodes_and_Weights.hpp:17): by increasing |x|,
@@ -206,6 +231,7 @@ template <class S> struct OracleT {
     std::vector<double> P;  // n*dim
     int64_t kernel_n, diag_n;
     double Kii = 0.0, hd = 1.0;
+    cplx Kii_c = 0.0;  // the 2D Hankel kernel's complex self term
     S diag_val = S(1.0);
     int nch, nnb;
     std::vector<std::vector<Box>> T;
@@ -214,7 +240,20 @@ template <class S> struct OracleT {
     //      3D/codes/kernel.hpp:123-129,146-170,172-193
     S entry(int i, int j) const {
         if constexpr (std::is_same<S, double>::value) return entry_real(i, j);
-        else return entry_helm(i, j);
+        else return dim == 2 ? entry_hankel(i, j) : entry_helm(i, j);
+    }
+    // IE_2D_Helm / Helmholtz2D (2D/codes/kernel.hpp:126-144, choice 10), the
+    // reference's expression I * (J0(R) + I * Y0(R)) / 4.0 with R2 = X + Y;
+    // diagonal (1 + 15 ln N + Kii) / h^2
+    cplx entry_hankel(int i, int j) const {
+        if (i == j) return diag_val;
+        const double *a = &P[(size_t)i * dim], *b = &P[(size_t)j * dim];
+        double R2 = (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]);
+        double R = std::sqrt(R2);
+        double j0, y0;
+        j0y0_series(R, j0, y0);
+        const cplx I(0.0, 1.0);
+        return I * (j0 + I * y0) / 4.0;
     }
     // Helmholtz3D (3D/codes/kernel.hpp:133-144, choice 2), the reference's expression:
     // exp(I R) / (4 PI) off the diagonal, 500 sqrt(N) on it
@@ -329,6 +368,32 @@ template <class S> struct OracleT {
                 hd = std::pow(h, 3.0);
             }
             diag_val = (1.0 + Kii) / hd;
+        } else if (choice == 10) {
+            // userkernel constructor (2D/codes/kernel.hpp:101-114): the complex self
+            // term by double_integral (2D/codes/integral2d.hpp:59-90) over [0, h/2]^2
+            double h = 1.0 / std::sqrt(double(kernel_n));
+            std::vector<double> x, w;
+            gauss_legendre(16, x, w);
+            double lo = 0.0, hi = h * 0.5;
+            double cx = 0.5 * (hi - lo), Lx = 0.5 * (hi + lo);
+            cplx res = 0.0;
+            const cplx I(0.0, 1.0);
+            for (int i = 0; i < 16; ++i) {
+                double tx = cx * x[(size_t)i] + Lx;
+                for (int j = 0; j < 16; ++j) {
+                    double ty = cx * x[(size_t)j] + Lx;
+                    double j0, y0;
+                    j0y0_series(std::sqrt(tx * tx + ty * ty), j0, y0);
+                    res += w[(size_t)i] * w[(size_t)j] * (I * (j0 + I * y0) / 4.0);
+                }
+            }
+            res *= (cx * cx);
+            res *= 4;
+            Kii_c = res;
+            Kii = res.real();
+            hd = std::pow(h, 2.0);
+            if constexpr (!std::is_same<S, double>::value)
+                diag_val = (1.0 + 15 * std::log(double(diag_n)) + res) / hd;
         } else {
             if (dim == 1) diag_val = std::sqrt((double)diag_n);
             else if (dim == 2) diag_val = 1.0;
@@ -1252,10 +1317,11 @@ extern "C" {
 h2wo *h2wo_create(int dim, int form, int64_t n, const double *pts, int nlevels, int tol_pow, int choice,
                   int64_t kernel_n, int64_t diag_n) {
     if (dim < 1 || dim > 3 || n < 1 || nlevels < 1 || (form != 0 && form != 1 && form != 2) || (form == 2 && dim == 1) ||
-        (choice != 0 && choice != 1 && choice != 2) || (choice == 2 && (dim != 3 || form == 2)))
+        (choice != 0 && choice != 1 && choice != 2 && choice != 10) || (choice == 2 && (dim != 3 || form == 2)) ||
+        (choice == 10 && (dim != 2 || form == 2)))
         return nullptr;
     h2wo *h = new h2wo;
-    if (choice == 2) {
+    if (choice == 2 || choice == 10) {
         h->c = new OracleT<cplx>;
         init_oracle(*h->c, dim, form, n, pts, nlevels, tol_pow, choice, kernel_n, diag_n);
     } else {
