@@ -87,6 +87,9 @@ def test_train_and_learned_assembly(gpu):
         blocks, acc = op.learn_stats()
         e = _dense_rows_err(op, x)
         assert e <= 10 * e_plain + 1e-12, (name, e, e_plain)
+        # accepted proposals keep the NCA's tolerance at about the plain ranks
+        assert op.storage_entries() <= 1.05 * plain.storage_entries(), (name, op.storage_entries(),
+                                                                        plain.storage_entries())
         stats[name] = (blocks, acc, t, e)
     print("plain %.3fs err %.2e; " % (t_plain, e_plain) + "; ".join(
         "%s: %d/%d accepted, %.3fs, err %.2e" % (k, v[1], v[0], v[2], v[3]) for k, v in stats.items()))
