@@ -125,7 +125,9 @@ int h2w_operator_bytes(h2w_handle *h, int precision, int64_t *bytes);
 /* y = A x for nrhs right-hand sides (column-major N x nrhs, leading dim N),
  * x and y in original point order. Replaces initialisation::mat_vec_prod
  * (1D/codes/matvec.hpp:121-138,163-178; 2D :163-182,212-233; 3D :63-83,115-136).
- * where = H2W_HOST or H2W_DEVICE; stream = cudaStream_t or NULL (default). */
+ * where = H2W_HOST or H2W_DEVICE; stream = cudaStream_t or NULL (default).
+ * Complex kernels (H2W_KERNEL_HELMHOLTZ / _HANKEL): nrhs = 1, H2W_PREC_FP64,
+ * x and y N interleaved (re, im) pairs. */
 int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precision, int where, void *stream);
 
 /* y = A x like h2w_matvec (one right-hand side, x and y DEVICE pointers in
@@ -154,7 +156,9 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
 int h2w_matvec_static(h2w_handle *h, const double *x, double *y, int precision, void *stream);
 
 /* GMRES, unrestarted, FP64, device-resident. Replaces iterative_solver::GMRES
- * ({1D,2D,3D}/codes/gmres.hpp:92-200): x0 = x on entry, stops when |s(i+1)|/||b|| < 10^-tol_pow. */
+ * ({1D,2D,3D}/codes/gmres.hpp:92-200): x0 = x on entry, stops when |s(i+1)|/||b|| < 10^-tol_pow.
+ * Complex kernels: b and x N interleaved (re, im) pairs; the reference's
+ * complex GMRES (H2W_OPT_COMPLEX_ARNOLDI selects GMRES proper). */
 int h2w_gmres(h2w_handle *h, const double *b, double *x, int max_iter, int tol_pow, int where, int *iters,
               double *resid);
 /* Mixed precision: FP32 inner GMRES (FP32 operator, from d = 0; relative
@@ -416,7 +420,8 @@ int h2w_plan_stats(h2w_handle *h, int64_t *stats, int n);
 int64_t h2w_launch_count(void);
 
 /* Dense FP64 product with the exact kernel matrix (getTruePoten,
- * 1D/codes/HODLR1Dtree.hpp:590-604), on the GPU, rows [row0, row0 + nrows). */
+ * 1D/codes/HODLR1Dtree.hpp:590-604), on the GPU, rows [row0, row0 + nrows).
+ * Complex kernels: x (N) and y (nrows) interleaved (re, im) pairs. */
 int h2w_dense_matvec(h2w_handle *h, const double *x, double *y, int64_t row0, int64_t nrows, int where);
 /* Operator files (no counterpart in the reference, which re-assembles on
  * every run, 3D/codes/main.cpp:21-25). h2w_save_operator writes the
