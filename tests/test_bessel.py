@@ -37,3 +37,22 @@ def test_j0_y0_match_independent_values(j0y0):
     ey = np.abs(y - g["y0"]) / np.maximum(np.abs(g["y0"]), env)
     assert ej.max() < 1e-14, ej.max()
     assert ey.max() < 1e-14, ey.max()
+
+
+def test_library_and_oracle_bessel_agree(j0y0):
+    """The oracle's own J0 / Y0 (a long-double power series, for its 2D Hankel
+    entries) and the library's agree, pair distances in (0, 2.83]: the 2D
+    Hankel entries of the oracle's column 0 against (-Y0 + i J0) / 4 from the
+    library's functions."""
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "..", "oracle"))
+    sys.path.insert(0, os.path.join(HERE, ".."))
+    from oracle import Oracle
+    from h2weak_gb300 import synth
+    pts = synth.uniform_points(synth.config_seed(98, 3), 2000, 2)
+    o = Oracle(2, 0, pts, 2, 8, 10, assemble=False)
+    col = o.entries(np.arange(1, len(pts)), [0])[:, 0]
+    R = np.sqrt(((pts[1:] - pts[0]) ** 2).sum(axis=1))
+    j, y = j0y0(R)
+    lib = (-y + 1j * j) / 4.0
+    assert np.max(np.abs(col - lib) / np.abs(lib)) < 1e-14
