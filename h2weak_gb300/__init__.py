@@ -568,7 +568,9 @@ class initialisation:
     3D/codes/matvec.hpp:6-180): constructor arguments as the reference's,
     tree_initialisation() assembles, mat_vec_prod(charge, output) fills
     output in original point order. dim and form replace the compile-time
-    -DUSE_* choice; points (optional) replaces the uniform grid."""
+    -DUSE_* choice; points (optional) replaces the uniform grid. Kernel_Choice
+    2 (3D) / 10 (2D) are the complex Helmholtz kernels of the reference's
+    USE_Helm / USE_Hankel builds: charge and output are then complex128."""
 
     def __init__(self, n_param, nLevels, nParticlesInLeaf, L, TOL_POW, Kernel_Choice, dim=1, form=FORM_NESTED,
                  points=None, device=0, rank_cap=0):
@@ -606,7 +608,7 @@ class initialisation:
 
     def mat_vec_prod(self, charge, output=None):
         y = self.op.matvec(charge)
-        self.K.collective_charge = np.array(charge, dtype=np.float64)
+        self.K.collective_charge = np.array(charge, dtype=np.complex128 if self.op.complex else np.float64)
         if output is not None:
             output.resize(y.shape, refcheck=False)
             output[...] = y
