@@ -45,8 +45,9 @@ enum { H2W_FORM_NESTED = 0, H2W_FORM_SEMINESTED = 1, H2W_FORM_NONNESTED = 2 };
  * A handle with a complex kernel takes and returns complex vectors as N
  * interleaved (re, im) pairs of doubles (the layout of std::complex<double>)
  * in h2w_matvec (FP64, one right-hand side), h2w_gmres and h2w_dense_matvec;
- * the mixed-precision, batched, learned, far-field-on-the-fly and
- * allocation-free entry points refuse it with H2W_ERR_ARG. */
+ * the mixed-precision, many-right-hand-side, learned, far-field-on-the-fly
+ * and allocation-free entry points refuse it with H2W_ERR_ARG, and
+ * h2w_batch_create with H2W_ERR_STATE. */
 enum { H2W_KERNEL_IE = 0, H2W_KERNEL_RBF = 1, H2W_KERNEL_HELMHOLTZ = 2, H2W_KERNEL_HANKEL = 10 };
 enum { H2W_ASSEMBLE_NCA = 0, H2W_ASSEMBLE_IMPORT = 1, H2W_ASSEMBLE_LEARNED = 2 };
 /* FP64: FP64 operator and arithmetic. FP32: FP32 operator copy and arithmetic.
