@@ -35,7 +35,9 @@ def test_replicas_take_the_slowest_rank():
     mp = pytest.importorskip("torch.multiprocessing")
     world = 2
     ms_by_rank = [1500.0, 2100.0]
-    with mp.Manager() as m:
+    # the manager's server process is spawned, not forked: this process may already run
+    # the CPU oracle's OpenMP threads
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), ms_by_rank, out), nprocs=world, join=True)
         res = dict(out)
