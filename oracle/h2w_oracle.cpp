@@ -51,22 +51,53 @@ template <class S> struct MatT {  // column-major dense block
 };
 template <class S> using VecT = std::vector<S>;
 
-// y = A x (rows summed in ascending column order)
+// y = A x, every row summed from 0 in ascending column order. The block is
+// swept column by column: each y[i] still takes exactly the row's sequence of
+// rounded products and sums, while the column-major block streams
+// contiguously and the rows vectorise.
 template <class S> VecT<S> gemv(const MatT<S> &A, const VecT<S> &x) {
     VecT<S> y((size_t)A.r, S(0.0));
-    for (int i = 0; i < A.r; ++i) {
-        S s = S(0.0);
-        for (int j = 0; j < A.c; ++j) { S p = A(i, j) * x[(size_t)j]; s = s + p; }
-        y[(size_t)i] = s;
+    S *yp = y.data();
+    const int r = A.r;
+    for (int j = 0; j < A.c; ++j) {
+        const S xj = x[(size_t)j];
+        const S *col = A.a.data() + (size_t)j * (size_t)r;
+        for (int i = 0; i < r; ++i) {
+            S p = col[i] * xj;
+            yp[i] = yp[i] + p;
+        }
     }
     return y;
 }
-// y = A^T x (a transpose: no conjugation)
+// y = A^T x (a transpose: no conjugation), every column summed from 0 in
+// ascending row order; four columns at a time, each with its own running sum,
+// so that four independent chains of adds overlap.
 template <class S> VecT<S> gemvT(const MatT<S> &A, const VecT<S> &x) {
     VecT<S> y((size_t)A.c, S(0.0));
-    for (int j = 0; j < A.c; ++j) {
+    const int r = A.r;
+    const S *xp = x.data();
+    int j = 0;
+    for (; j + 4 <= A.c; j += 4) {
+        const S *c0 = A.a.data() + (size_t)j * (size_t)r;
+        const S *c1 = c0 + r, *c2 = c1 + r, *c3 = c2 + r;
+        S s0 = S(0.0), s1 = S(0.0), s2 = S(0.0), s3 = S(0.0);
+        for (int i = 0; i < r; ++i) {
+            const S xi = xp[i];
+            S p0 = c0[i] * xi, p1 = c1[i] * xi, p2 = c2[i] * xi, p3 = c3[i] * xi;
+            s0 = s0 + p0;
+            s1 = s1 + p1;
+            s2 = s2 + p2;
+            s3 = s3 + p3;
+        }
+        y[(size_t)j] = s0;
+        y[(size_t)j + 1] = s1;
+        y[(size_t)j + 2] = s2;
+        y[(size_t)j + 3] = s3;
+    }
+    for (; j < A.c; ++j) {
+        const S *cj = A.a.data() + (size_t)j * (size_t)r;
         S s = S(0.0);
-        for (int i = 0; i < A.r; ++i) { S p = A(i, j) * x[(size_t)i]; s = s + p; }
+        for (int i = 0; i < r; ++i) { S p = cj[i] * xp[i]; s = s + p; }
         y[(size_t)j] = s;
     }
     return y;
