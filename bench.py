@@ -287,9 +287,10 @@ def cpu_oracle_sample_random(wl, steps, warmup, n_sample=32768):
     Assembly is untimed; each step is one FP64 GMRES solve of the sample,
     scaled to one solve of the full workload by the stored entries a solve
     streams, E x (iterations + 1): the full operator's E and FP64 iteration
-    count are the workload's full_e / full_it. The solve is its products (the
-    operator streamed once each); orthogonalisation is below 0.1 % of it at
-    either size."""
+    count are the workload's full_e / full_it. The products (the operator
+    streamed once each) are about 96 % of the sample's solve; the rest, the
+    Arnoldi work, grows as N x iterations^2 (77x to the full size, not 138x),
+    so the scaled time is at most about 2 % high."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
     synth = load_synth()
