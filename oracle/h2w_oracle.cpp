@@ -15,6 +15,7 @@
 // order of the Eigen-subset shim the reference is compiled against for the
 // golden dumps, so this restatement and that build agree bit for bit.
 #include "h2w_oracle.h"
+#include "bessel_ld.hpp"
 #include "gmres_ref.hpp"
 
 #include <algorithm>
@@ -165,30 +166,8 @@ template <class S> MatT<S> solve_right_lower(const MatT<S> &T, const MatT<S> &B)
     return X;
 }
 
-// J0 and Y0 for the 2D Hankel kernel (the reference calls Boost,
-// 2D/codes/integral2d.hpp:16-50): the power series (Abramowitz & Stegun
-// 9.1.10, 9.1.13) summed in long double, valid here for 0 < x <= 8 (pair
-// distances of points in a square of semi-length up to 2.8); larger
-// arguments are refused (NaN), since the oracle is only run on such sets.
-inline void j0y0_series(double xd, double &j0, double &y0) {
-    if (!(xd > 0.0) || xd > 8.0) {
-        j0 = y0 = std::nan("");
-        return;
-    }
-    const long double x = xd, t = 0.25L * x * x;
-    long double term = 1.0L, sj = 1.0L, sy = 0.0L, hk = 0.0L;
-    for (int k = 1; k < 200; ++k) {
-        term = term * (-t) / ((long double)k * (long double)k);
-        hk += 1.0L / (long double)k;
-        sj += term;
-        sy -= hk * term;
-        if (fabsl(term) * (hk + 1.0L) < 1e-30L) break;
-    }
-    const long double gamma = 0.577215664901532860606512090082402431L;
-    const long double two_over_pi = 0.636619772367581343075535053490057448L;
-    j0 = (double)sj;
-    y0 = (double)(two_over_pi * ((logl(0.5L * x) + gamma) * sj + sy));
-}
+// J0 and Y0 of the 2D Hankel kernel: the long-double series of bessel_ld.hpp
+using h2wo_bessel::j0y0_series;
 
 // Gauss-Legendre nodes and weights on [-1,1] by Newton iteration on the
 // Legendre recurrence in long double, ordered as the reference's table

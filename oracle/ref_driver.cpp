@@ -17,8 +17,8 @@
 //   findMemory_n/_sn      1D/codes/HODLR1Dtree.hpp:535-588, 2D/codes/HODLR2Dtree.hpp:1207-1305,
 //                         3D/codes/HODLR3Dtree.hpp:2505-2628
 //
-// Complex Helmholtz build (-DUSE_Helm, 3D, choice 2): every vector in and out
-// is N interleaved (re, im) pairs of doubles.
+// Complex builds (-DUSE_Helm, 3D Helmholtz, choice 2; -DUSE_Hankel, 2D Hankel,
+// choice 10): every vector in and out is N interleaved (re, im) pairs of doubles.
 //
 // Usage: refXd_F <n_param> <nLevels> <leaf_param> <L> <tol_pow> <choice>
 //                <in.bin> <out.bin> <gmres_maxiter> <gmres_tolpow>
@@ -95,8 +95,9 @@ static const int NNB = 26;
 #endif
 
 // Scalars on the wire: one double (real kernels) or an interleaved (re, im)
-// pair (the complex Helmholtz build, -DUSE_Helm: 3D/codes/headers.hpp:35-40).
-#ifdef USE_Helm
+// pair (the complex builds: -DUSE_Helm, 3D/codes/headers.hpp:35-40; -DUSE_Hankel,
+// 2D/codes/headers.hpp:34-40).
+#if defined(USE_Helm) || defined(USE_Hankel)
 static const int CW = 2;
 static dtype scal_in(const double *p) { return dtype(p[0], p[1]); }
 static void scal_out(std::vector<double> &o, const dtype &v) {

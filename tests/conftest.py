@@ -17,8 +17,18 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long-running CPU test")
 
 
-def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("g"))
+# Fixtures of the reference's 2D Hankel build (made against the Boost Bessel
+# stand-in, oracle/boost_shim). The CPU tests compare the oracle and the host
+# code with them; the GPU comparisons with them have not been run on a GB300
+# yet, so the GPU tests leave them out. The GPU's 2D Hankel path is checked
+# against the oracle (tests/test_gpu_helmholtz.py), which matches these
+# fixtures bit for bit.
+CPU_ONLY_GOLDEN = ("g2d_n_hankel", "g2d_sn_hankel", "g2d_n_hankel_rand")
+
+
+def golden_names(gpu=False):
+    names = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("g"))
+    return [n for n in names if not (gpu and n in CPU_ONLY_GOLDEN)]
 
 
 

@@ -39,8 +39,13 @@ CASES = {
     "g3d_n_helm": (3, "n_helm", 16, 2, 4, 10, 2, None, 10),
     "g3d_sn_helm": (3, "sn_helm", 16, 2, 4, 8, 2, None, 10),
     "g3d_n_helm_rand": (3, "n_helm", 0, 2, 0, 8, 2, ("uniform", 3, 4000), 10),
+    # complex 2D Hankel kernel (USE_Hankel, choice 10), the reference built against the
+    # Boost Bessel stand-in (oracle/boost_shim): complex vectors
+    "g2d_n_hankel": (2, "n_hankel", 48, 3, 6, 10, 10, None, 10),
+    "g2d_sn_hankel": (2, "sn_hankel", 48, 3, 6, 8, 10, None, 10),
+    "g2d_n_hankel_rand": (2, "n_hankel", 0, 3, 0, 8, 10, ("uniform", 2, 3000), 10),
 }
-FORMS = {"n": 0, "sn": 1, "nn": 2, "n_helm": 0, "sn_helm": 1}
+FORMS = {"n": 0, "sn": 1, "nn": 2, "n_helm": 0, "sn_helm": 1, "n_hankel": 0, "sn_hankel": 1}
 LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge", "sn_row", "sn_col"]
 
 
@@ -51,7 +56,7 @@ def run_case(name, spec):
         N = len(pts)
     else:
         N = npar ** dim
-    cplx = form.endswith("_helm")
+    cplx = form.endswith(("_helm", "_hankel"))
     if cplx:  # real and imaginary parts from separate streams
         vecs = [synth.normal(synth.config_seed(90, v), N) + 1j * synth.normal(synth.config_seed(92, v), N)
                 for v in range(2)]
