@@ -44,6 +44,12 @@ CASES = {
     "g2d_n_hankel": (2, "n_hankel", 48, 3, 6, 10, 10, None, 10),
     "g2d_sn_hankel": (2, "sn_hankel", 48, 3, 6, 8, 10, None, 10),
     "g2d_n_hankel_rand": (2, "n_hankel", 0, 3, 0, 8, 10, ("uniform", 2, 3000), 10),
+    # ties of the partition rule: random points with about 30 % of their coordinates moved
+    # down onto the grid of quarters, so that many lie exactly on the split planes of
+    # levels 1-3 (and on the domain's lower faces); duplicates removed
+    "g2d_n_snap": (2, "n", 0, 3, 0, 8, 1, ("snapped", 2, 3000), 10),
+    "g2d_sn_snap": (2, "sn", 0, 3, 0, 8, 1, ("snapped", 2, 3000), 10),
+    "g3d_n_snap": (3, "n", 0, 3, 0, 8, 1, ("snapped", 3, 4000), 10),
 }
 FORMS = {"n": 0, "sn": 1, "nn": 2, "n_helm": 0, "sn_helm": 1, "n_hankel": 0, "sn_hankel": 1}
 LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge", "sn_row", "sn_col"]
@@ -52,7 +58,13 @@ LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_chec
 def run_case(name, spec):
     dim, form, npar, nlev, leaf, tol, ch, pts, gtol = spec
     if pts is not None:
-        pts = synth.uniform_points(synth.config_seed(40 + dim, 0), pts[2], dim)
+        kind, n = pts[0], pts[2]
+        pts = synth.uniform_points(synth.config_seed(40 + dim, 0), n, dim)
+        if kind == "snapped":
+            snap = synth.uniform01(synth.config_seed(44, dim), n * dim).reshape(n, dim) < 0.3
+            pts = np.where(snap, np.floor(pts * 4.0) / 4.0, pts)
+            _, first = np.unique(pts, axis=0, return_index=True)
+            pts = np.ascontiguousarray(pts[np.sort(first)])
         N = len(pts)
     else:
         N = npar ** dim

@@ -36,7 +36,7 @@ def test_oracle_matches_reference(name):
         assert np.array_equal(o.matvec(g["vecs"][k]), g["matvec"][k])
 
 
-@pytest.mark.parametrize("name", ["g1d_n_rbf", "g2d_n_ie", "g3d_sn_ie", "g3d_n_helm", "g2d_n_hankel", "g2d_sn_hankel"])
+@pytest.mark.parametrize("name", ["g1d_n_rbf", "g2d_n_ie", "g3d_sn_ie", "g3d_n_helm", "g2d_n_hankel", "g2d_sn_hankel", "g2d_n_snap", "g3d_n_snap"])
 def test_oracle_dense_and_gmres(name):
     g = load_golden(name)
     o = oracle_for(g)
