@@ -17,14 +17,9 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long-running CPU test")
 
 
-# Fixtures whose GPU comparisons have not been run on a GB300 yet, so the GPU
-# tests leave them out; the CPU tests compare the oracle and the host code
-# with them. g2d_*_hankel*: the reference's 2D Hankel build (made against the
-# Boost Bessel stand-in, oracle/boost_shim); the GPU's 2D Hankel path is
-# checked against the oracle (tests/test_gpu_helmholtz.py), which matches
-# these fixtures bit for bit. g*_snap: points on the split planes.
-CPU_ONLY_GOLDEN = ("g2d_n_hankel", "g2d_sn_hankel", "g2d_n_hankel_rand", "g2d_n_snap", "g2d_sn_snap",
-                   "g3d_n_snap")
+# Fixtures that the GPU tests leave out (none at present: every fixture's GPU
+# comparisons have been run on a GB300).
+CPU_ONLY_GOLDEN = ()
 
 
 def golden_names(gpu=False):
