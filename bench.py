@@ -446,9 +446,12 @@ def run_single_random(args, wl, rank, world, local):
     cpu = {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
            "sample": "timed on one-GPU runs only (--no-cpu-baseline skips it)"}
     if world == 1 and not args.no_cpu_baseline:
-        r = cpu_oracle_sample_random(wl, 2, 0)
-        cpu = {"value": 1.0 / r["t_full"], "unit": "solves/s", "cores": r["cores"], "kind": "port",
-               "sample": r["sample"]}
+        try:
+            r = cpu_oracle_sample_random(wl, 2, 0)
+            cpu = {"value": 1.0 / r["t_full"], "unit": "solves/s", "cores": r["cores"], "kind": "port",
+                   "sample": r["sample"]}
+        except Exception as e:  # the GPU figures above still print
+            cpu["sample"] = "CPU oracle failed: %s" % str(e)[:200]
     peak, peak_kind = load_peaks()
     stored = op.operator_bytes(hw.PREC_FP32)
     E = op.storage_entries()
@@ -779,11 +782,15 @@ def main():
     # ---- CPU baseline (one-GPU runs): the oracle on this host's cores, a bounded sample of the same workload
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        r = cpu_oracle_solves(wl, R, 1, 0, budget_s=20.0)
-        cpu = {"value": 1.0 / r["t_solve"], "unit": "solves/s", "cores": r["cores"], "kind": "port",
-               "sample": "%d of the %d right-hand sides, each a full FP64 GMRES solve to 1e-%d (CPU oracle, "
-                         "assembly %.2fs untimed, %d iterations, matvec %.1f ms)"
-                         % (r["cols_per_step"], R, gtol, r["t_asm"], r["iters"], r["t_mv"] * 1e3)}
+        try:
+            r = cpu_oracle_solves(wl, R, 1, 0, budget_s=20.0)
+            cpu = {"value": 1.0 / r["t_solve"], "unit": "solves/s", "cores": r["cores"], "kind": "port",
+                   "sample": "%d of the %d right-hand sides, each a full FP64 GMRES solve to 1e-%d (CPU oracle, "
+                             "assembly %.2fs untimed, %d iterations, matvec %.1f ms)"
+                             % (r["cols_per_step"], R, gtol, r["t_asm"], r["iters"], r["t_mv"] * 1e3)}
+        except Exception as e:  # the GPU figures still print
+            cpu = {"value": None, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": "CPU oracle failed: %s" % str(e)[:200]}
 
     # ---- assembly: plain NCA (timed again, warm) against learned proposals (the
     # shipped model; blocks the NCA stopping test rejects fall back to the plain
