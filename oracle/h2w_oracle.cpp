@@ -52,6 +52,11 @@ template <class S> struct MatT {  // column-major dense block
 };
 template <class S> using VecT = std::vector<S>;
 
+// Order of the sums in gemv / gemvT: ascending (the shim's, so results are
+// the reference build's bit for bit) or, set through h2wo_set_sum_order for a
+// test of how much a product depends on its summation order, descending.
+int g_sum_reverse = 0;
+
 // y = A x, every row summed from 0 in ascending column order. The block is
 // swept column by column: each y[i] still takes exactly the row's sequence of
 // rounded products and sums, while the column-major block streams
@@ -60,7 +65,8 @@ template <class S> VecT<S> gemv(const MatT<S> &A, const VecT<S> &x) {
     VecT<S> y((size_t)A.r, S(0.0));
     S *yp = y.data();
     const int r = A.r;
-    for (int j = 0; j < A.c; ++j) {
+    for (int jj = 0; jj < A.c; ++jj) {
+        const int j = g_sum_reverse ? A.c - 1 - jj : jj;
         const S xj = x[(size_t)j];
         const S *col = A.a.data() + (size_t)j * (size_t)r;
         for (int i = 0; i < r; ++i) {
@@ -73,16 +79,15 @@ template <class S> VecT<S> gemv(const MatT<S> &A, const VecT<S> &x) {
 // y = A^T x (a transpose: no conjugation), every column summed from 0 in
 // ascending row order; four columns at a time, each with its own running sum,
 // so that four independent chains of adds overlap.
-template <class S> VecT<S> gemvT(const MatT<S> &A, const VecT<S> &x) {
-    VecT<S> y((size_t)A.c, S(0.0));
+template <bool Rev, class S> void gemvT_cols(const MatT<S> &A, const S *xp, S *y) {
     const int r = A.r;
-    const S *xp = x.data();
     int j = 0;
     for (; j + 4 <= A.c; j += 4) {
         const S *c0 = A.a.data() + (size_t)j * (size_t)r;
         const S *c1 = c0 + r, *c2 = c1 + r, *c3 = c2 + r;
         S s0 = S(0.0), s1 = S(0.0), s2 = S(0.0), s3 = S(0.0);
-        for (int i = 0; i < r; ++i) {
+        for (int ii = 0; ii < r; ++ii) {
+            const int i = Rev ? r - 1 - ii : ii;
             const S xi = xp[i];
             S p0 = c0[i] * xi, p1 = c1[i] * xi, p2 = c2[i] * xi, p3 = c3[i] * xi;
             s0 = s0 + p0;
@@ -90,17 +95,26 @@ template <class S> VecT<S> gemvT(const MatT<S> &A, const VecT<S> &x) {
             s2 = s2 + p2;
             s3 = s3 + p3;
         }
-        y[(size_t)j] = s0;
-        y[(size_t)j + 1] = s1;
-        y[(size_t)j + 2] = s2;
-        y[(size_t)j + 3] = s3;
+        y[j] = s0;
+        y[j + 1] = s1;
+        y[j + 2] = s2;
+        y[j + 3] = s3;
     }
     for (; j < A.c; ++j) {
         const S *cj = A.a.data() + (size_t)j * (size_t)r;
         S s = S(0.0);
-        for (int i = 0; i < r; ++i) { S p = cj[i] * xp[i]; s = s + p; }
-        y[(size_t)j] = s;
+        for (int ii = 0; ii < r; ++ii) {
+            const int i = Rev ? r - 1 - ii : ii;
+            S p = cj[i] * xp[i];
+            s = s + p;
+        }
+        y[j] = s;
     }
+}
+template <class S> VecT<S> gemvT(const MatT<S> &A, const VecT<S> &x) {
+    VecT<S> y((size_t)A.c, S(0.0));
+    if (g_sum_reverse) gemvT_cols<true>(A, x.data(), y.data());
+    else gemvT_cols<false>(A, x.data(), y.data());
     return y;
 }
 template <class S> void addto(VecT<S> &y, const VecT<S> &x) { for (size_t i = 0; i < y.size(); ++i) y[i] += x[i]; }
@@ -1401,6 +1415,8 @@ int h2wo_entries(h2wo *h, const int32_t *rows, int64_t nr, const int32_t *cols, 
 }
 
 int h2wo_is_complex(h2wo *h) { return h->c ? 1 : 0; }
+
+void h2wo_set_sum_order(int reverse) { g_sum_reverse = reverse ? 1 : 0; }
 
 int64_t h2wo_list(h2wo *h, int which, int64_t *ptr, int32_t *val) {
     std::vector<int64_t> p;

@@ -19,8 +19,9 @@ extern "C" {
 typedef struct h2wo h2wo;
 
 /* dim 1..3; form 0 = nested H2*, 1 = semi-nested (H2+H)*, 2 = H*;
- * choice 0 / 1 (real kernels) or 2 (the complex Helmholtz kernel of the
- * reference's USE_Helm build, 3D, forms 0 and 1), whose vectors (x, y, b in
+ * choice 0 / 1 (real kernels), 2 (the complex Helmholtz kernel of the
+ * reference's USE_Helm build, 3D) or 10 (the complex Hankel kernel of its
+ * USE_Hankel build, 2D), complex in forms 0 and 1, whose vectors (x, y, b in
  * matvec, dense_matvec, gmres; out in entries) are interleaved (re, im)
  * doubles; pts n*dim
  * row-major; kernel_n = particles.size() when the reference kernel object
@@ -45,6 +46,10 @@ int h2wo_entries(h2wo *o, const int32_t *rows, int64_t nr, const int32_t *cols, 
 int64_t h2wo_list(h2wo *o, int which, int64_t *ptr, int32_t *val);
 /* 1 for the complex kernel */
 int h2wo_is_complex(h2wo *o);
+/* Summation order of every block product (process-wide): 0 = ascending, the
+ * reference build's order (the default); 1 = descending, for tests of how much
+ * a product depends on its summation order. */
+void h2wo_set_sum_order(int reverse);
 int64_t h2wo_list_nptr(h2wo *o, int which);
 
 #ifdef __cplusplus

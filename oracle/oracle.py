@@ -46,12 +46,20 @@ def lib():
         L.h2wo_list_nptr.argtypes = [P, I]
         L.h2wo_is_complex.argtypes = [P]
         L.h2wo_is_complex.restype = I
+        L.h2wo_set_sum_order.argtypes = [I]
+        L.h2wo_set_sum_order.restype = None
         _lib = L
     return _lib
 
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_sum_order(reverse):
+    """Sum every block product of every oracle in descending order (True) or in
+    the reference build's ascending order (False, the default)."""
+    lib().h2wo_set_sum_order(1 if reverse else 0)
 
 
 class Oracle:

@@ -16,7 +16,8 @@ MATVEC_RTOL = 1e-13
 # the split planes): the product on this operator cancels strongly, so its
 # rounding depends on the summation order. Summing every block product of the
 # CPU oracle in reverse order (the same operator, bit for bit) moves its result
-# 1.24e-13 from the reference's, against 3e-16 on every other fixture; the GPU
+# 1.24e-13 from the reference's, against 3e-16 on every other fixture
+# (test_oracle_golden.py::test_product_dependence_on_summation_order); the GPU
 # sums in its own order and measured 1.66e-13 on a GB300, with pivots and
 # storage bit-exact.
 MATVEC_RTOL_CASE = {"g2d_n_snap": 2.5e-13}

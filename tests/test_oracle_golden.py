@@ -46,3 +46,25 @@ def test_oracle_dense_and_gmres(name):
     assert it == int(g["gmres_stats"][0])
     assert res == pytest.approx(g["gmres_stats"][1], rel=1e-6)
     np.testing.assert_allclose(x, g["gmres_x"], rtol=0, atol=1e-12 * np.abs(g["gmres_x"]).max())
+
+
+def test_product_dependence_on_summation_order():
+    """The split-plane fixture's product cancels strongly: with every block
+    product summed in descending order (the same operator, bit for bit) the
+    oracle lands more than 1e-14 from the reference there, against less than
+    1e-15 on the random-point fixture of the same kernel and form. This is the
+    floor the GPU, which sums in its own order, meets on that fixture."""
+    import oracle as om
+    res = {}
+    for name in ("g2d_n_snap", "g2d_n_rand"):
+        g = load_golden(name)
+        o = oracle_for(g)
+        try:
+            om.set_sum_order(True)
+            y = o.matvec(g["vecs"][0])
+        finally:
+            om.set_sum_order(False)
+        res[name] = np.linalg.norm(y - g["matvec"][0]) / np.linalg.norm(g["matvec"][0])
+        assert np.array_equal(o.matvec(g["vecs"][0]), g["matvec"][0])
+    assert res["g2d_n_snap"] > 1e-14, res
+    assert res["g2d_n_rand"] < 1e-15, res
