@@ -3579,7 +3579,7 @@ void require_op(h2w_handle *h) {
 // Entry points of the real kernels only (mixed precision, batched, learned,
 // far field on the fly, allocation-free product).
 void require_real(const h2w_handle *h, const char *what) {
-    if (h->cplx) throw ApiError(H2W_ERR_ARG, std::string(what) + " is not available for the complex Helmholtz kernel");
+    if (h->cplx) throw ApiError(H2W_ERR_ARG, std::string(what) + " is not available for the complex kernels (Helmholtz, Hankel)");
 }
 
 // The reference GMRES (3D/codes/gmres.hpp:92-200, USE_Helm / USE_Hankel) on
@@ -4177,7 +4177,7 @@ int h2w_matvec(h2w_handle *h, const double *x, double *y, int nrhs, int precisio
             throw ApiError(H2W_ERR_ARG, "unknown precision");
         if (h->cplx) {  // complex operator: one FP64 product of interleaved (re, im) vectors
             if (precision != H2W_PREC_FP64 || nrhs != 1)
-                throw ApiError(H2W_ERR_ARG, "the complex Helmholtz kernel has the FP64 single-vector product only");
+                throw ApiError(H2W_ERR_ARG, "the complex kernels (Helmholtz, Hankel) have the FP64 single-vector product only");
             const int64_t nv = h->nv();
             const double *dx = x;
             double *dy = y;
