@@ -41,8 +41,9 @@ enum { H2W_FORM_NESTED = 0, H2W_FORM_SEMINESTED = 1, H2W_FORM_NONNESTED = 2 };
  *    = (-Y0(R) + i J0(R)) / 4 off the diagonal and (1 + 15 ln N + Kii) / h^2 on
  *    it (2D/codes/kernel.hpp:126-144,321-333, 2D/codes/integral2d.hpp:16-90),
  *    with the library's own J0 and Y0 where the reference calls Boost;
- * complex scalars throughout (3D/codes/headers.hpp:35-40, 2D/codes/headers.hpp:34-40).
- * A handle with a complex kernel takes and returns complex vectors as N
+ * complex scalars throughout (3D/codes/headers.hpp:35-40, 2D/codes/headers.hpp:34-40),
+ * in the nested and semi-nested forms (H2W_FORM_NONNESTED with a complex kernel is
+ * refused at h2w_create with H2W_ERR_ARG). A handle with a complex kernel takes and returns complex vectors as N
  * interleaved (re, im) pairs of doubles (the layout of std::complex<double>)
  * in h2w_matvec (FP64, one right-hand side), h2w_gmres and h2w_dense_matvec;
  * the mixed-precision, many-right-hand-side, learned, far-field-on-the-fly
