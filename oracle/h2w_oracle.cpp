@@ -1341,8 +1341,8 @@ extern "C" {
 h2wo *h2wo_create(int dim, int form, int64_t n, const double *pts, int nlevels, int tol_pow, int choice,
                   int64_t kernel_n, int64_t diag_n) {
     if (dim < 1 || dim > 3 || n < 1 || nlevels < 1 || (form != 0 && form != 1 && form != 2) || (form == 2 && dim == 1) ||
-        (choice != 0 && choice != 1 && choice != 2 && choice != 10) || (choice == 2 && (dim != 3 || form == 2)) ||
-        (choice == 10 && (dim != 2 || form == 2)))
+        (choice != 0 && choice != 1 && choice != 2 && choice != 10) || (choice == 2 && dim != 3) ||
+        (choice == 10 && dim != 2))
         return nullptr;
     h2wo *h = new h2wo;
     if (choice == 2 || choice == 10) {

@@ -21,7 +21,7 @@ typedef struct h2wo h2wo;
 /* dim 1..3; form 0 = nested H2*, 1 = semi-nested (H2+H)*, 2 = H*;
  * choice 0 / 1 (real kernels), 2 (the complex Helmholtz kernel of the
  * reference's USE_Helm build, 3D) or 10 (the complex Hankel kernel of its
- * USE_Hankel build, 2D), complex in forms 0 and 1, whose vectors (x, y, b in
+ * USE_Hankel build, 2D), in every form, whose vectors (x, y, b in
  * matvec, dense_matvec, gmres; out in entries) are interleaved (re, im)
  * doubles; pts n*dim
  * row-major; kernel_n = particles.size() when the reference kernel object

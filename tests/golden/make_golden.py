@@ -44,6 +44,9 @@ CASES = {
     "g2d_n_hankel": (2, "n_hankel", 48, 3, 6, 10, 10, None, 10),
     "g2d_sn_hankel": (2, "sn_hankel", 48, 3, 6, 8, 10, None, 10),
     "g2d_n_hankel_rand": (2, "n_hankel", 0, 3, 0, 8, 10, ("uniform", 2, 3000), 10),
+    # the complex kernels in the non-nested H* form (USE_HODLRdD with USE_Helm / USE_Hankel)
+    "g3d_nn_helm": (3, "nn_helm", 16, 2, 4, 8, 2, None, 10),
+    "g2d_nn_hankel": (2, "nn_hankel", 48, 3, 6, 8, 10, None, 10),
     # ties of the partition rule: random points with about 30 % of their coordinates moved
     # down onto the grid of quarters, so that many lie exactly on the split planes of
     # levels 1-3 (and on the domain's lower faces); duplicates removed
@@ -51,7 +54,8 @@ CASES = {
     "g2d_sn_snap": (2, "sn", 0, 3, 0, 8, 1, ("snapped", 2, 3000), 10),
     "g3d_n_snap": (3, "n", 0, 3, 0, 8, 1, ("snapped", 3, 4000), 10),
 }
-FORMS = {"n": 0, "sn": 1, "nn": 2, "n_helm": 0, "sn_helm": 1, "n_hankel": 0, "sn_hankel": 1}
+FORMS = {"n": 0, "sn": 1, "nn": 2, "n_helm": 0, "sn_helm": 1, "nn_helm": 2, "n_hankel": 0, "sn_hankel": 1,
+         "nn_hankel": 2}
 LISTS = ["charge", "nbr", "il", "isvertex", "far_check", "far_charge", "ver_check", "ver_charge", "sn_row", "sn_col"]
 
 

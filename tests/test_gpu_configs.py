@@ -184,7 +184,7 @@ def test_cfg2_gmres_vs_oracle(cfg2):
 
 # ------------------------------------------------------ dense product -------
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", golden_names(gpu=True))
+@pytest.mark.parametrize("name", golden_names())
 def test_dense_matvec_vs_reference_golden(gpu, name):
     hw = gpu
     g = load_golden(name)

@@ -37,7 +37,7 @@ def relerr(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", golden_names(gpu=True))
+@pytest.mark.parametrize("name", golden_names())
 def test_gpu_nca_assembly_vs_reference(gpu, name):
     hw = gpu
     g = load_golden(name)
@@ -72,7 +72,7 @@ def test_gpu_nca_assembly_vs_reference(gpu, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", [n for n in golden_names(gpu=True) if not n.startswith("g1d_sn")])
+@pytest.mark.parametrize("name", [n for n in golden_names() if not n.startswith("g1d_sn")])
 def test_gpu_matvec_on_reference_operator(gpu, name):
     """Import the reference's pivots: the GPU matvec then applies the same
     compressed operator, to <= 1e-13 relative."""
@@ -89,7 +89,7 @@ def test_gpu_matvec_on_reference_operator(gpu, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", golden_names(gpu=True))
+@pytest.mark.parametrize("name", golden_names())
 def test_gpu_gmres_vs_reference(gpu, name):
     hw = gpu
     g = load_golden(name)

@@ -16,7 +16,7 @@ def oracle_for(g):
     return Oracle(dim, g["form"], g["points"], g["nlevels"], g["tol_pow"], g["choice"], kn, dn)
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names(oracle=True))
 def test_oracle_matches_reference(name):
     g = load_golden(name)
     o = oracle_for(g)
@@ -36,7 +36,7 @@ def test_oracle_matches_reference(name):
         assert np.array_equal(o.matvec(g["vecs"][k]), g["matvec"][k])
 
 
-@pytest.mark.parametrize("name", ["g1d_n_rbf", "g2d_n_ie", "g3d_sn_ie", "g3d_n_helm", "g2d_n_hankel", "g2d_sn_hankel", "g2d_n_snap", "g3d_n_snap"])
+@pytest.mark.parametrize("name", ["g1d_n_rbf", "g2d_n_ie", "g3d_sn_ie", "g3d_n_helm", "g2d_n_hankel", "g2d_sn_hankel", "g2d_n_snap", "g3d_n_snap", "g3d_nn_helm", "g2d_nn_hankel"])
 def test_oracle_dense_and_gmres(name):
     g = load_golden(name)
     o = oracle_for(g)
