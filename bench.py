@@ -252,7 +252,7 @@ def cpu_oracle_solves(wl, R, steps, warmup, budget_s=150.0):
     t = time.time() - t0
     errs.append(float(np.linalg.norm(x - cols[q]) / np.linalg.norm(cols[q])))
     t0 = time.time()
-    nmv = 5
+    nmv = 10
     for _ in range(nmv):
         o.matvec(cols[0])
     t_mv = (time.time() - t0) / nmv
@@ -310,9 +310,9 @@ def cpu_oracle_sample_random(wl, steps, warmup, n_sample=32768):
         x, it, res = o.gmres(b, max_iter=500, tol_pow=wl["gtol"])
         ts.append(time.time() - t0)
     t0 = time.time()
-    for _ in range(3):
+    for _ in range(10):
         o.matvec(xt)
-    t_mv = (time.time() - t0) / 3
+    t_mv = (time.time() - t0) / 10
     E = o.memory()
     scale = wl["full_e"] * (wl["full_it"] + 1.0) / (E * (it + 1.0))
     t_solve = sum(ts) / len(ts)
